@@ -1,0 +1,406 @@
+"""Benchmark of the GB300 RPMD engine: bead-steps/s, mixed form vs plain FP64.
+
+One "step" is one RPMD velocity-Verlet step (Caracal's `verlet`,
+src/verlet.f90:65) of every bead of every trajectory of the workload.
+
+  value      bead-steps/s of the mixed form, state resident in HBM, the K timed
+             steps in one persistent launch (CUDA events on the engine stream)
+  plain_fp64 the same for the plain FP64 form
+  e2e        bead-steps/s through the C-ABI with host buffers: each step copies
+             q, p, dV/dq in from pinned memory, steps once, copies them out
+  roofline   the step kernel against the measured FP64 (or FP32) pipe peak
+  cpu_baseline  the oracle (the C++ restatement of Caracal's step) on the host
+             cores, OpenMP over trajectories, bounded sample
+
+`--impl reference` times the CPU restatement (Caracal's Fortran cannot be
+built on this image) on all host cores with the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic operations of one BKMP2 evaluation (one bead, reactant-like
+# geometry, no compact-geometry terms), counted by instantiating the oracle's
+# restatement of src/egrad_h3.f on an op-counting scalar; a CPU test checks
+# this table against the oracle.
+ALGO_PES_OPS = {
+    "h3": {"add": 491, "mul": 738, "div": 82, "sqrt": 5, "exp": 11, "pow": 6},
+}
+CALIB_OPS = {"fma": 0, "div": 1, "sqrt": 2, "exp": 3, "log": 4, "pow": 5, "sin": 6, "cos": 7,
+             "acos": 8, "erf": 9}
+
+
+def algo_flops_per_bead_step(pes, natoms, nbeads, thermostat, w):
+    """Algorithmic FP work of one bead-step in FMA-pipe flops (an add or a mul
+    is 1, an FMA 2, a division or transcendental 2 x its measured cost in FMAs).
+
+    PES: the reference formulas (table above).  Propagator: Caracal's four
+    length-P real DFTs per (atom, dim) as FFTs (2.5 P log2 P flops each) plus
+    the per-mode 2x2 update (6 flops).  Kicks: 2 x 2 flops per coordinate.
+    transrot: 30 flops per coordinate.  PILE: two half steps, each two FFT
+    pairs over p and the Gaussian draws (log, sqrt, sin, cos per pair).
+    """
+    ops = ALGO_PES_OPS[pes]
+    pes_f = ops["add"] + ops["mul"]
+    for k in ("div", "sqrt", "exp", "pow", "log", "sin", "cos", "acos", "erf"):
+        pes_f += ops.get(k, 0) * w[k]
+    nc = 3 * natoms
+    lg = math.log2(nbeads) if nbeads > 1 else 0.0
+    prop = nc * (4 * 2.5 * lg + 6)
+    kicks = nc * 4
+    trot = nc * 30
+    pile = 0.0
+    if thermostat == "pile":
+        pile = 2 * (nc * (2 * 2 * 2.5 * lg + 4) + (nc / 2) * (w["log"] + w["sqrt"] + w["sin"] + w["cos"]))
+    return pes_f + prop + kicks + trot + pile
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def calibrate(L):
+    """FP64 and FP32 FMA peaks and per-op costs (in FMAs) on this device."""
+    out = {}
+    for fp64, tag in ((1, "fp64"), (0, "fp32")):
+        rates = {}
+        for name, op in CALIB_OPS.items():
+            r = np.zeros(1)
+            iters = 20000 if name == "fma" else 400
+            L.check(L.lib().cr_calibrate_op(fp64, op, iters, L.dptr(r)), "calibrate")
+            rates[name] = float(r[0])
+        fma = rates["fma"]
+        out[tag] = {"fma_per_s": fma, "peak_tflops": 2 * fma / 1e12,
+                    "w": {k: 2.0 * fma / v for k, v in rates.items() if k != "fma"}}
+    return out
+
+
+def workload(name):
+    from caracal_gb300 import workloads as W
+    if name == "h3":
+        return W.h3_config(ntraj=64, nbeads=16, thermostat="pile")
+    if name == "h3_large":
+        return W.h3_config(ntraj=4096, nbeads=16, thermostat="pile")
+    raise SystemExit(f"unknown workload {name}")
+
+
+def make_engine(wl, precision, traj0=0):
+    from caracal_gb300 import RPMDEngine
+    eng = RPMDEngine(wl.pes, wl.mass, wl.nbeads, wl.ntraj, wl.dt_au, beta=wl.beta,
+                     thermostat=wl.thermostat, andersen_step=wl.andersen_step,
+                     pile_tau0_au=wl.pile_tau0_au, transrot=wl.transrot, precision=precision,
+                     seed=wl.seed, traj0=traj0)
+    eng.init_positions(wl.q0, wl.sigma_bohr)
+    eng.init_momenta()
+    eng.compute_forces()
+    return eng
+
+
+def cpu_baseline(wl, target_s=12.0, nthreads=0):
+    """The oracle on the host cores (OpenMP over trajectories), bounded sample."""
+    from oracle import oracle as orc
+    cfg = orc.Config(wl.pes, wl.mass, wl.nbeads, wl.dt_au, wl.beta, thermostat=wl.thermostat,
+                     andersen_step=wl.andersen_step, pile_tau0=wl.pile_tau0_au,
+                     transrot=wl.transrot, seed=wl.seed)
+    T = wl.ntraj
+    q = orc.init_positions(cfg, T, wl.q0, wl.sigma_bohr)
+    p = orc.init_momenta(cfg, T)
+    f, _ = orc.init_forces(cfg, q)
+    cores = nthreads or os.cpu_count()
+    n = 5
+    t0 = time.perf_counter()
+    q, p, f, _, _ = orc.run(cfg, q, p, f, n, nthreads=cores)
+    dt = time.perf_counter() - t0
+    steps = max(5, int(n * target_s / max(dt, 1e-6)))
+    steps = min(steps, wl.nsteps)
+    t0 = time.perf_counter()
+    orc.run(cfg, q, p, f, steps, istep0=n, nthreads=cores)
+    el = time.perf_counter() - t0
+    return {"value": T * wl.nbeads * steps / el, "unit": "bead-steps/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{T} trajectories x {wl.nbeads} beads x {steps} steps of the workload "
+                      f"(C++ restatement of Caracal's step, -O2, OpenMP over trajectories)"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def run_reference(args):
+    rank, ws, dist = dist_setup()
+    wl = workload(args.workload)
+    if rank != 0:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    # W warm-up samples, then K timed samples; each sample = a bounded number of
+    # steps of the whole workload on all host threads
+    from oracle import oracle as orc
+    cfg = orc.Config(wl.pes, wl.mass, wl.nbeads, wl.dt_au, wl.beta, thermostat=wl.thermostat,
+                     andersen_step=wl.andersen_step, pile_tau0=wl.pile_tau0_au,
+                     transrot=wl.transrot, seed=wl.seed)
+    T = wl.ntraj
+    q = orc.init_positions(cfg, T, wl.q0, wl.sigma_bohr)
+    p = orc.init_momenta(cfg, T)
+    f, _ = orc.init_forces(cfg, q)
+    cores = os.cpu_count()
+    per = max(1, min(args.ref_steps_per_sample, wl.nsteps))
+    istep = 0
+    for _ in range(args.warmup):
+        q, p, f, _, _ = orc.run(cfg, q, p, f, per, istep0=istep, nthreads=cores)
+        istep += per
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        q, p, f, _, _ = orc.run(cfg, q, p, f, per, istep0=istep, nthreads=cores)
+        istep += per
+    el = time.perf_counter() - t0
+    v = T * wl.nbeads * per * args.steps / el
+    line = {"impl": "reference", "metric": "bead-steps/s", "value": v, "unit": "bead-steps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl.name, "ntraj": T, "nbeads": wl.nbeads, "pes": wl.pes,
+                       "thermostat": wl.thermostat, "ref_steps_per_sample": per},
+            "cpu_baseline": {"value": v, "unit": "bead-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{per} steps of {T}x{wl.nbeads} beads per timed sample; "
+                                       "Caracal's Fortran is not buildable here, so its C++ "
+                                       "restatement (oracle/) is timed"},
+            "e2e": {"value": v, "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_ours(args):
+    import torch
+    from caracal_gb300 import _lib as L
+
+    rank, ws, dist = dist_setup()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = workload(args.workload)
+    K, W = args.steps, args.warmup
+    cal = calibrate(L)
+    eng_mx = make_engine(wl, "mixed", traj0=rank * wl.ntraj)
+    eng_64 = make_engine(wl, "fp64", traj0=rank * wl.ntraj)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed_run(eng):
+        eng.run(W)                       # warm-up launch (W steps)
+        flush.zero_()                    # L2 (129 MB) flushed before the timed launch
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        eng.run(K)                       # K steps, one persistent launch
+        torch.cuda.synchronize()
+        ms = eng.last_kernel_ms()
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    ms_64 = timed_run(eng_64)
+    with ClockSampler(dev) as clk:
+        ms_mx = timed_run(eng_mx)
+        # keep the sampler alive over at least a few samples
+        if ms_mx < 500:
+            extra = max(1, int(500 / max(ms_mx, 1e-3)))
+            for _ in range(min(extra, 50)):
+                eng_mx.run(K)
+    clocks = clk.summary()
+    bead_steps = wl.ntraj * wl.nbeads * K
+    value = ws * bead_steps / (ms_mx * 1e-3)
+    plain = ws * bead_steps / (ms_64 * 1e-3)
+
+    # force error of the mixed form against FP64 at the same positions
+    q, p, f, e, st = eng_64.get_state()
+    eng_mx.set_state(q, p)          # recomputes forces in the mixed form
+    _, _, f_mx, e_mx, _ = eng_mx.get_state()
+    ferr = float(np.max(np.abs(f_mx - f)) / np.max(np.abs(f)))
+    eerr = float(np.max(np.abs(e_mx - e)) / np.max(np.abs(e)))
+
+    # end to end through the C-ABI with pinned host buffers, every step
+    import ctypes as C
+    shape = (wl.ntraj, wl.nbeads, len(wl.mass), 3)
+    nbytes = int(np.prod(shape)) * 8
+    bufs = []
+    for _ in range(3):
+        ptr = C.c_void_p()
+        L.check(L.lib().cr_host_alloc(C.byref(ptr), nbytes), "host_alloc")
+        bufs.append((ptr, np.ctypeslib.as_array((C.c_double * (nbytes // 8)).from_address(ptr.value))
+                     .reshape(shape)))
+    (pq, hq), (pp, hp), (pf, hf) = bufs
+    q, p, f, e, st = eng_mx.get_state()
+    hq[...] = q
+    hp[...] = p
+    hf[...] = f
+    he = np.zeros(wl.ntraj)
+    K_e2e = min(K, args.e2e_steps)
+    for _ in range(min(W, 3)):
+        eng_mx.step_host(hq, hp, hf, he)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(K_e2e):
+        eng_mx.step_host(hq, hp, hf, he)
+    el = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([el], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el = float(t.item())
+    e2e = ws * wl.ntraj * wl.nbeads * K_e2e / el
+    for ptr, _ in bufs:
+        L.lib().cr_host_free(ptr)
+
+    # roofline of the step kernel (mixed form: FP64 propagator/thermostat + FP32 PES)
+    w64 = cal["fp64"]["w"]
+    flops64 = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat, w64)
+    ach64 = flops64 * bead_steps / (ms_64 * 1e-3) / 1e12
+    peak64 = cal["fp64"]["peak_tflops"]
+    info = eng_mx.launch_info()
+    line = {
+        "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": ws, "steps": K,
+        "warmup": W, "ms_per_step": ms_mx / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32 (mixed form)", "data": "synthetic",
+        "config": {"workload": wl.name, "pes": wl.pes, "ntraj": wl.ntraj, "nbeads": wl.nbeads,
+                   "natoms": len(wl.mass), "thermostat": wl.thermostat, "kelvin": wl.kelvin,
+                   "dt_fs": wl.dt_fs, "parallelism": f"replicas x{ws}",
+                   "l2": "flushed (256 MB write) before the timed launch; K steps in one launch"},
+        "plain_fp64": {"value": plain, "unit": "bead-steps/s", "ms_per_step": ms_64 / K},
+        "mixed_over_plain": value / plain,
+        "force_error_vs_fp64": ferr, "energy_error_vs_fp64": eerr,
+        "e2e": {"value": e2e, "unit": "bead-steps/s", "steps": K_e2e,
+                "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": 3 * nbytes + 8 * wl.ntraj},
+        "gpu_launches": 1,
+        "launch": info,
+        "roofline": {"kernel": "rpmd_run_kernel<PesH3, fp64> (plain form)", "bound": "fp64",
+                     "achieved": ach64, "peak": peak64, "unit": "TFLOP/s", "frac": ach64 / peak64,
+                     "traffic": None, "peak_source": "measured in this run (FP64 FMA microbenchmark)",
+                     "algo_flops_per_bead_step": flops64},
+        "calibration": {"fp64_peak_tflops": cal["fp64"]["peak_tflops"],
+                        "fp32_peak_tflops": cal["fp32"]["peak_tflops"],
+                        "fp64_op_cost_flops": w64, "fp32_op_cost_flops": cal["fp32"]["w"]},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl, target_s=args.cpu_seconds)
+    mp = measured_peaks()
+    if mp:
+        line["measured_peaks_file"] = {k: mp.get(k) for k in ("hbm_gbs", "bf16_tflops", "gpu_name")}
+    if rank == 0:
+        print(json.dumps(line))
+    eng_mx.close()
+    eng_64.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="h3")
+    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-steps-per-sample", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,11 @@
+"""GB300-native RPMD engine for Caracal's dynamic / calc_rate hot path.
+
+The compute path is the CUDA library built from ``csrc/`` (sm_103a); this
+package only loads it (``_lib``) and mirrors its C-ABI in Python
+(``engine``).  There is no CPU fallback.
+"""
+from . import units  # noqa: F401
+from ._lib import CaracalError, lib  # noqa: F401
+from .engine import RPMDEngine, egrad_h3  # noqa: F401
+
+__all__ = ["RPMDEngine", "egrad_h3", "CaracalError", "lib", "units"]

@@ -1,0 +1,119 @@
+"""ctypes binding of ``libcaracal_gb300.so`` (the C-ABI in include/caracal_gb300.h).
+
+The library is the only compute path: if it cannot be built or loaded, every
+call raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_lib = None
+
+c_double_p = C.POINTER(C.c_double)
+c_int_p = C.POINTER(C.c_int)
+
+CR_OK = 0
+CR_ERR_ARG = 1
+CR_ERR_CUDA = 2
+CR_ERR_NO_DEVICE = 3
+CR_ERR_UNSUPPORTED = 4
+CR_ERR_TRAJECTORY = 5
+CR_ERR_IO = 6
+
+CR_TRAJ_NONFINITE = 1
+CR_TRAJ_SINGULAR_INERTIA = 2
+
+CR_PES_H3 = 1
+CR_PES_CH4H = 2
+CR_PES_CH4OH = 3
+CR_PES_QMDFF = 4
+
+CR_THERMO_NONE = 0
+CR_THERMO_ANDERSEN = 1
+CR_THERMO_NHC = 2
+CR_THERMO_PILE = 3
+
+CR_PREC_FP64 = 0
+CR_PREC_MIXED = 1
+
+
+class CrConfig(C.Structure):
+    _fields_ = [("pes", C.c_int), ("natoms", C.c_int), ("nbeads", C.c_int), ("ntraj", C.c_int),
+                ("thermostat", C.c_int), ("andersen_step", C.c_int), ("transrot", C.c_int),
+                ("precision", C.c_int), ("seed", C.c_uint), ("traj0", C.c_uint),
+                ("dt", C.c_double), ("beta", C.c_double), ("pile_tau0", C.c_double),
+                ("mass", c_double_p)]
+
+
+class CaracalError(RuntimeError):
+    def __init__(self, code, where):
+        self.code = code
+        detail = ""
+        if _lib is not None:
+            buf = C.create_string_buffer(512)
+            _lib.cr_last_error_detail(buf, 512)
+            detail = buf.value.decode(errors="replace")
+            msg = _lib.cr_error_string(code).decode()
+        else:
+            msg = f"status {code}"
+        super().__init__(f"{where}: {msg} ({detail})")
+
+
+def _sig(lib):
+    d, i, v = c_double_p, c_int_p, C.c_void_p
+    eng = C.c_void_p
+    sigs = {
+        "cr_error_string": ([C.c_int], C.c_char_p),
+        "cr_last_error_detail": ([C.c_char_p, C.c_int], C.c_int),
+        "cr_device_count": ([i], C.c_int),
+        "cr_egrad_h3": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
+        "cr_egrad_h3_device": ([v, C.c_int, v, v, C.c_int, v], C.c_int),
+        "cr_engine_create": ([C.POINTER(CrConfig), C.POINTER(C.c_void_p)], C.c_int),
+        "cr_engine_destroy": ([eng], C.c_int),
+        "cr_engine_init_positions": ([eng, d, C.c_double], C.c_int),
+        "cr_engine_init_momenta": ([eng, C.c_int], C.c_int),
+        "cr_engine_compute_forces": ([eng], C.c_int),
+        "cr_engine_set_state": ([eng, d, d, d], C.c_int),
+        "cr_engine_get_state": ([eng, d, d, d, d, i], C.c_int),
+        "cr_engine_run": ([eng, C.c_int], C.c_int),
+        "cr_engine_step_host": ([eng, d, d, d, d], C.c_int),
+        "cr_engine_last_kernel_ms": ([eng, C.POINTER(C.c_float)], C.c_int),
+        "cr_engine_launch_info": ([eng, i, i, i, i], C.c_int),
+        "cr_engine_device_state": ([eng, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_void_p)], C.c_int),
+        "cr_host_alloc": ([C.POINTER(C.c_void_p), C.c_ulonglong], C.c_int),
+        "cr_host_free": ([v], C.c_int),
+        "cr_calibrate_op": ([C.c_int, C.c_int, C.c_int, d], C.c_int),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+
+
+def lib(build: bool = True):
+    """Load (building first if stale) the CUDA engine library."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build else _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"caracal_gb300 native library missing: {path}")
+        _lib = C.CDLL(path)
+        _sig(_lib)
+    return _lib
+
+
+def check(code, where):
+    if code != CR_OK:
+        raise CaracalError(code, where)
+
+
+def dptr(a):
+    return a.ctypes.data_as(c_double_p)
+
+
+def iptr(a):
+    return a.ctypes.data_as(c_int_p)

@@ -1,0 +1,621 @@
+// Host side of the GB300 RPMD engine and its C-ABI (include/caracal_gb300.h).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/caracal_gb300.h"
+#include "cr_common.cuh"
+#include "pes_h3.cuh"
+#include "rpmd_kernel.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CR_CUDA(call)                                                                 \
+  do {                                                                                \
+    cudaError_t _e = (call);                                                          \
+    if (_e != cudaSuccess)                                                            \
+      return fail(CR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));   \
+  } while (0)
+
+constexpr double kPi = 3.1415926535897932384626433832795029;
+
+int next_pow2(int x) {
+  int g = 1;
+  while (g < x) g <<= 1;
+  return g;
+}
+
+int pes_natoms(int pes) {
+  switch (pes) {
+    case CR_PES_H3: return 3;
+    default: return -1;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Device kernels outside the step loop
+// ---------------------------------------------------------------------------
+namespace cr {
+
+// q[t][k] = q0 + sigma * N(0,1) per coordinate (tag TAG_BEAD_JITTER, step 0)
+template <int NC>
+__global__ void init_positions_kernel(int T, int P, uint32_t seed, uint32_t traj0, const double* q0,
+                                      double sigma, double* q) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= T * P) return;
+  int t = idx / P, k = idx % P;
+  double z[NC];
+  normals_bead<NC>(seed, traj0 + t, (uint32_t)k, 0u, TAG_BEAD_JITTER, z);
+#pragma unroll
+  for (int c = 0; c < NC; ++c) q[(size_t)idx * NC + c] = q0[c] + sigma * z[c];
+}
+
+// mdinit Andersen draw: p = sqrt(m P / beta) N(0,1) (tag TAG_INIT_MOMENTA)
+template <int NC>
+__global__ void init_momenta_kernel(int T, int P, uint32_t seed, uint32_t traj0, StepParams prm,
+                                    int zero, double* p) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= T * P) return;
+  int t = idx / P, k = idx % P;
+  if (zero) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) p[(size_t)idx * NC + c] = 0.0;
+    return;
+  }
+  double z[NC];
+  normals_bead<NC>(seed, traj0 + t, (uint32_t)k, 0u, TAG_INIT_MOMENTA, z);
+#pragma unroll
+  for (int c = 0; c < NC; ++c) p[(size_t)idx * NC + c] = z[c] * prm.sigma[c / 3];
+}
+
+// One thread per bead: V and dV/dq.
+template <class PES, bool MIXED>
+__global__ void egrad_kernel(int nbeads_total, const double* q, double* V, double* g) {
+  constexpr int NC = 3 * PES::N;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbeads_total) return;
+  double qq[NC], gg[NC], v;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) qq[c] = q[(size_t)b * NC + c];
+  if (MIXED) PES::template egrad<float>(qq, v, gg);
+  else PES::template egrad<double>(qq, v, gg);
+  V[b] = v;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) g[(size_t)b * NC + c] = gg[c];
+}
+
+// epot[t] = sum over beads of V[t][k]
+__global__ void sum_beads_kernel(int T, int P, const double* V, double* epot) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  double s = 0.0;
+  for (int k = 0; k < P; ++k) s += V[(size_t)t * P + k];
+  epot[t] = s;
+}
+
+}  // namespace cr
+
+// ---------------------------------------------------------------------------
+// Engine
+// ---------------------------------------------------------------------------
+struct cr_engine {
+  cr_config cfg{};
+  std::vector<double> mass;
+  int N = 0, NC = 0, P = 0, T = 0, G = 1, H = 1;
+  int block = 32, grid = 1;
+  size_t smem = 0;
+  int istep = 0;
+  int launches = 0;
+  float last_ms = 0.f;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double *d_q = nullptr, *d_p = nullptr, *d_f = nullptr, *d_epot = nullptr, *d_V = nullptr;
+  double *d_prop = nullptr, *d_pile = nullptr, *d_q0 = nullptr;
+  int* d_status = nullptr;
+  cr::StepParams prm{};
+};
+
+namespace {
+
+// Propagator blocks K1, K2, K3 (unit mass) of the Caracal cosine transform,
+// restricted to the (P/2+1)^2 block that acts on symmetrised inputs.
+void build_propagator(int P, double beta, double dt, std::vector<double>& out) {
+  const int H = P / 2 + 1;
+  std::vector<double> C((size_t)P * P);
+  const double factor = std::sqrt(1.0 / P);
+  for (int j = 0; j < P; ++j)
+    for (int k = 0; k < P; ++k) {
+      long long m = ((long long)j * k) % P;
+      C[(size_t)j * P + k] = factor * std::cos(2.0 * kPi * (double)m / P);
+    }
+  // per-mode coefficients (src/verlet.f90:405-429) at unit mass
+  std::vector<double> pc(P, 1.0), pq(P, 0.0), pd(P, dt);
+  if (P > 1) {
+    const double beta_n = beta / P, twown = 2.0 / beta_n, pi_n = kPi / P;
+    for (int k = 1; k <= P / 2; ++k) {
+      double wk = twown * std::sin(k * pi_n);
+      double wt = wk * dt;
+      pc[k] = std::cos(wt);
+      pq[k] = -wk * std::sin(wt);
+      pd[k] = std::sin(wt) / wk;
+    }
+    for (int k = 1; k <= (P - 1) / 2; ++k) {
+      pc[P - k] = pc[k];
+      pq[P - k] = pq[k];
+      pd[P - k] = pd[k];
+    }
+  }
+  out.assign((size_t)3 * H * H, 0.0);
+  const std::vector<double>* diag[3] = {&pc, &pq, &pd};
+  for (int which = 0; which < 3; ++which)
+    for (int r = 0; r < H; ++r)
+      for (int l = 0; l < H; ++l) {
+        double s = 0.0;
+        for (int k = 0; k < P; ++k) s += C[(size_t)r * P + k] * (*diag[which])[k] * C[(size_t)k * P + l];
+        out[(size_t)which * H * H + (size_t)r * H + l] = s;
+      }
+}
+
+// PILE-L circulant vectors a (friction) and b (noise) of O^T diag(c) O with O
+// the orthonormal real normal-mode matrix; gamma_0 = 1/tau0, gamma_k = 2 w_k.
+void build_pile(int P, double beta, double dt, double tau0, std::vector<double>& out) {
+  std::vector<double> O((size_t)P * P);
+  for (int k = 0; k < P; ++k)
+    for (int j = 0; j < P; ++j) {
+      long long m = ((long long)j * k) % P;
+      double ang = 2.0 * kPi * (double)m / P, v;
+      if (k == 0) v = std::sqrt(1.0 / P);
+      else if (2 * k < P) v = std::sqrt(2.0 / P) * std::cos(ang);
+      else if (2 * k == P) v = ((j % 2) == 0 ? 1.0 : -1.0) * std::sqrt(1.0 / P);
+      else v = std::sqrt(2.0 / P) * std::sin(ang);
+      O[(size_t)k * P + j] = v;
+    }
+  std::vector<double> c1(P), c2(P);
+  const double twown = 2.0 * P / beta;
+  for (int k = 0; k < P; ++k) {
+    int kk = (2 * k <= P) ? k : P - k;
+    double gamma = (k == 0) ? 1.0 / tau0 : 2.0 * twown * std::sin(kk * kPi / P);
+    c1[k] = std::exp(-0.5 * dt * gamma);
+    c2[k] = std::sqrt(1.0 - c1[k] * c1[k]);
+  }
+  out.assign((size_t)2 * P, 0.0);
+  for (int m = 0; m < P; ++m) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < P; ++k) {
+      a += O[(size_t)k * P + m] * c1[k] * O[(size_t)k * P + 0];
+      b += O[(size_t)k * P + m] * c2[k] * O[(size_t)k * P + 0];
+    }
+    out[m] = a;
+    out[P + m] = b;
+  }
+}
+
+template <class PES>
+int launch_run(cr_engine* e, int nsteps) {
+  auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
+                                                  : cr::rpmd_run_kernel<PES, false>;
+  CR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
+  kern<<<e->grid, e->block, e->smem, e->stream>>>(e->prm, e->istep, nsteps);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+template <class PES>
+int launch_forces(cr_engine* e) {
+  const int nb = e->T * e->P;
+  const int bs = 128;
+  if (e->cfg.precision == CR_PREC_MIXED)
+    cr::egrad_kernel<PES, true><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, e->d_V, e->d_f);
+  else
+    cr::egrad_kernel<PES, false><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, e->d_V, e->d_f);
+  CR_CUDA(cudaGetLastError());
+  cr::sum_beads_kernel<<<(e->T + 127) / 128, 128, 0, e->stream>>>(e->T, e->P, e->d_V, e->d_epot);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+int dispatch_run(cr_engine* e, int nsteps) {
+  switch (e->cfg.pes) {
+    case CR_PES_H3: return launch_run<cr::PesH3>(e, nsteps);
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+}
+
+int dispatch_forces(cr_engine* e) {
+  switch (e->cfg.pes) {
+    case CR_PES_H3: return launch_forces<cr::PesH3>(e);
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+}
+
+// Launch shape: a tiny batch is latency-bound, so it is spread one warp per
+// SM; a large batch uses 128-thread blocks, shrunk until the shared memory fits.
+void choose_launch(cr_engine* e) {
+  const int G = e->G;
+  int sms = 152;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long threads = (long long)e->T * G;
+  int block = (threads <= (long long)sms * 128) ? 32 : 128;
+  if (block < G) block = G;
+  if (block > 256) block = 256;
+  while (block > G && cr::step_smem_doubles(e->P, G, e->NC, block / G) * 8 > 200 * 1024) block /= 2;
+  e->block = block;
+  const int groups = block / G;
+  e->grid = (e->T + groups - 1) / groups;
+  e->smem = cr::step_smem_doubles(e->P, G, e->NC, groups) * sizeof(double);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C-ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* cr_error_string(int code) {
+  switch (code) {
+    case CR_OK: return "ok";
+    case CR_ERR_ARG: return "invalid argument";
+    case CR_ERR_CUDA: return "CUDA runtime error";
+    case CR_ERR_NO_DEVICE: return "no CUDA device";
+    case CR_ERR_UNSUPPORTED: return "unsupported configuration";
+    case CR_ERR_TRAJECTORY: return "trajectory became non-finite";
+    case CR_ERR_IO: return "I/O error";
+    default: return "unknown status";
+  }
+}
+
+int cr_last_error_detail(char* buf, int len) {
+  if (!buf || len <= 0) return CR_ERR_ARG;
+  std::snprintf(buf, (size_t)len, "%s", g_last_error.c_str());
+  return CR_OK;
+}
+
+int cr_device_count(int* n) {
+  if (!n) return fail(CR_ERR_ARG, "n is NULL");
+  int c = 0;
+  cudaError_t err = cudaGetDeviceCount(&c);
+  if (err != cudaSuccess) {
+    *n = 0;
+    return fail(CR_ERR_NO_DEVICE, cudaGetErrorString(err));
+  }
+  *n = c;
+  return CR_OK;
+}
+
+int cr_egrad_h3_device(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
+                       void* stream) {
+  if (npts < 0 || (npts > 0 && (!d_q || !d_V || !d_dVdq))) return fail(CR_ERR_ARG, "bad egrad arguments");
+  if (npts == 0) return CR_OK;
+  const int bs = 128;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (precision == CR_PREC_MIXED)
+    cr::egrad_kernel<cr::PesH3, true><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
+  else if (precision == CR_PREC_FP64)
+    cr::egrad_kernel<cr::PesH3, false><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
+  else
+    return fail(CR_ERR_ARG, "unknown precision");
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
+  if (info) *info = 0;
+  if (natoms != 3) return fail(CR_ERR_ARG, "egrad_h3 needs natoms = 3");
+  if (nbeads < 0 || (nbeads > 0 && (!q || !V || !dVdq))) return fail(CR_ERR_ARG, "bad egrad_h3 arguments");
+  if (nbeads == 0) return CR_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(CR_ERR_NO_DEVICE, "no CUDA device");
+  const size_t nq = (size_t)9 * nbeads;
+  double *d_q = nullptr, *d_V = nullptr, *d_g = nullptr;
+  CR_CUDA(cudaMalloc(&d_q, nq * sizeof(double)));
+  cudaError_t e1 = cudaMalloc(&d_V, (size_t)nbeads * sizeof(double));
+  cudaError_t e2 = cudaMalloc(&d_g, nq * sizeof(double));
+  int rc = CR_OK;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    rc = fail(CR_ERR_CUDA, "cudaMalloc failed in cr_egrad_h3");
+  } else if (cudaMemcpy(d_q, q, nq * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = fail(CR_ERR_CUDA, "copy of q failed");
+  } else if ((rc = cr_egrad_h3_device(d_q, nbeads, d_V, d_g, CR_PREC_FP64, nullptr)) == CR_OK) {
+    if (cudaMemcpy(V, d_V, (size_t)nbeads * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(dVdq, d_g, nq * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = fail(CR_ERR_CUDA, "copy of results failed");
+  }
+  cudaFree(d_q);
+  cudaFree(d_V);
+  cudaFree(d_g);
+  return rc;
+}
+
+int cr_engine_create(const cr_config* cfg, cr_engine** out) {
+  if (!cfg || !out) return fail(CR_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  const int N = pes_natoms(cfg->pes);
+  if (N < 0) return fail(CR_ERR_UNSUPPORTED, "PES not available in this engine");
+  if (cfg->natoms != N) return fail(CR_ERR_ARG, "natoms does not match the PES");
+  if (cfg->nbeads < 1 || cfg->nbeads > cr::kMaxBeads) return fail(CR_ERR_ARG, "nbeads must be 1..128");
+  if (cfg->ntraj < 1) return fail(CR_ERR_ARG, "ntraj must be >= 1");
+  if (!(cfg->dt > 0.0)) return fail(CR_ERR_ARG, "dt must be > 0");
+  if (cfg->thermostat == CR_THERMO_NHC) return fail(CR_ERR_UNSUPPORTED, "Nose-Hoover chain not built yet");
+  if (cfg->thermostat != CR_THERMO_NONE && cfg->thermostat != CR_THERMO_ANDERSEN &&
+      cfg->thermostat != CR_THERMO_PILE)
+    return fail(CR_ERR_ARG, "unknown thermostat");
+  if (cfg->precision != CR_PREC_FP64 && cfg->precision != CR_PREC_MIXED)
+    return fail(CR_ERR_ARG, "unknown precision");
+  // P > 1 needs a finite beta for the free ring-polymer frequencies.  Caracal's
+  // dynamic.x in NVE sets kelvin = 0 (src/dynamic.f90:338), making beta = +Inf
+  // and the P > 1 propagator 0/0; the engine refuses that instead.
+  if (cfg->nbeads > 1 && !(cfg->beta > 0.0 && std::isfinite(cfg->beta)))
+    return fail(CR_ERR_ARG, "nbeads > 1 needs a finite temperature (beta)");
+  if (cfg->thermostat != CR_THERMO_NONE && !(cfg->beta > 0.0 && std::isfinite(cfg->beta)))
+    return fail(CR_ERR_ARG, "a thermostat needs a finite temperature (beta)");
+  if (cfg->thermostat == CR_THERMO_ANDERSEN && cfg->andersen_step < 1)
+    return fail(CR_ERR_ARG, "andersen_step must be >= 1");
+  if (cfg->thermostat == CR_THERMO_PILE && !(cfg->pile_tau0 > 0.0))
+    return fail(CR_ERR_ARG, "PILE needs tau0 > 0");
+  if (!cfg->mass) return fail(CR_ERR_ARG, "mass is NULL");
+  for (int i = 0; i < N; ++i)
+    if (!(cfg->mass[i] > 0.0)) return fail(CR_ERR_ARG, "masses must be > 0");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(CR_ERR_NO_DEVICE, "no CUDA device");
+
+  cr_engine* e = new cr_engine();
+  e->cfg = *cfg;
+  e->mass.assign(cfg->mass, cfg->mass + N);
+  e->cfg.mass = e->mass.data();
+  e->N = N;
+  e->NC = 3 * N;
+  e->P = cfg->nbeads;
+  e->T = cfg->ntraj;
+  e->G = next_pow2(e->P);
+  e->H = e->P / 2 + 1;
+  choose_launch(e);
+
+  auto cleanup_fail = [&](int code) {
+    cr_engine_destroy(e);
+    return code;
+  };
+  const size_t nall = (size_t)e->T * e->P * e->NC;
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess)
+    return cleanup_fail(fail(CR_ERR_CUDA, "stream/event creation failed"));
+  if (cudaMalloc(&e->d_q, nall * 8) != cudaSuccess || cudaMalloc(&e->d_p, nall * 8) != cudaSuccess ||
+      cudaMalloc(&e->d_f, nall * 8) != cudaSuccess ||
+      cudaMalloc(&e->d_epot, (size_t)e->T * 8) != cudaSuccess ||
+      cudaMalloc(&e->d_V, (size_t)e->T * e->P * 8) != cudaSuccess ||
+      cudaMalloc(&e->d_status, (size_t)e->T * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&e->d_q0, (size_t)e->NC * 8) != cudaSuccess)
+    return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the state failed"));
+  cudaMemsetAsync(e->d_q, 0, nall * 8, e->stream);
+  cudaMemsetAsync(e->d_p, 0, nall * 8, e->stream);
+  cudaMemsetAsync(e->d_f, 0, nall * 8, e->stream);
+  cudaMemsetAsync(e->d_status, 0, (size_t)e->T * sizeof(int), e->stream);
+
+  std::vector<double> prop, pile;
+  build_propagator(e->P, cfg->beta, cfg->dt, prop);
+  if (cfg->thermostat == CR_THERMO_PILE) build_pile(e->P, cfg->beta, cfg->dt, cfg->pile_tau0, pile);
+  else pile.assign((size_t)2 * e->P, 0.0);
+  if (cudaMalloc(&e->d_prop, prop.size() * 8) != cudaSuccess ||
+      cudaMalloc(&e->d_pile, pile.size() * 8) != cudaSuccess)
+    return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the tables failed"));
+  if (cudaMemcpyAsync(e->d_prop, prop.data(), prop.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(e->d_pile, pile.data(), pile.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return cleanup_fail(fail(CR_ERR_CUDA, "upload of the tables failed"));
+
+  cr::StepParams& s = e->prm;
+  s.T = e->T;
+  s.P = e->P;
+  s.G = e->G;
+  s.H = e->H;
+  s.thermostat = cfg->thermostat;
+  s.andersen_step = cfg->andersen_step > 0 ? cfg->andersen_step : 1;
+  s.transrot = cfg->transrot ? 1 : 0;
+  s.seed = cfg->seed;
+  s.traj0 = cfg->traj0;
+  s.dt = cfg->dt;
+  s.half_dt = 0.5 * cfg->dt;
+  s.beta = cfg->beta;
+  double tm = 0.0;  // src/transrot.f90:72-79
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < e->P; ++k) tm = tm + e->mass[i];
+  s.totmass = tm * e->P;
+  for (int i = 0; i < cr::kMaxAtoms; ++i) {
+    double m = i < N ? e->mass[i] : 1.0;
+    s.mass[i] = m;
+    s.inv_mass[i] = 1.0 / m;
+    s.sigma[i] = (cfg->beta > 0.0 && std::isfinite(cfg->beta)) ? std::sqrt(m / (cfg->beta / e->P)) : 0.0;
+  }
+  s.prop = e->d_prop;
+  s.pile = e->d_pile;
+  s.q = e->d_q;
+  s.p = e->d_p;
+  s.f = e->d_f;
+  s.epot = e->d_epot;
+  s.status = e->d_status;
+  *out = e;
+  return CR_OK;
+}
+
+int cr_engine_destroy(cr_engine* e) {
+  if (!e) return CR_OK;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  cudaFree(e->d_q);
+  cudaFree(e->d_p);
+  cudaFree(e->d_f);
+  cudaFree(e->d_epot);
+  cudaFree(e->d_V);
+  cudaFree(e->d_status);
+  cudaFree(e->d_q0);
+  cudaFree(e->d_prop);
+  cudaFree(e->d_pile);
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return CR_OK;
+}
+
+int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
+  if (!e || !q0) return fail(CR_ERR_ARG, "NULL argument");
+  if (!(sigma >= 0.0)) return fail(CR_ERR_ARG, "sigma must be >= 0");
+  CR_CUDA(cudaMemcpyAsync(e->d_q0, q0, (size_t)e->NC * 8, cudaMemcpyHostToDevice, e->stream));
+  const int nb = e->T * e->P;
+  switch (e->cfg.pes) {
+    case CR_PES_H3:
+      cr::init_positions_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
+      break;
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+  CR_CUDA(cudaGetLastError());
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_init_momenta(cr_engine* e, int zero) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (!zero && !(e->cfg.beta > 0.0 && std::isfinite(e->cfg.beta)))
+    return fail(CR_ERR_ARG, "Andersen momenta need a finite temperature");
+  const int nb = e->T * e->P;
+  switch (e->cfg.pes) {
+    case CR_PES_H3:
+      cr::init_momenta_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+      break;
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+  CR_CUDA(cudaGetLastError());
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_compute_forces(cr_engine* e) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  int rc = dispatch_forces(e);
+  if (rc) return rc;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_set_state(cr_engine* e, const double* q, const double* p, const double* f) {
+  if (!e || !q || !p) return fail(CR_ERR_ARG, "NULL argument");
+  const size_t bytes = (size_t)e->T * e->P * e->NC * 8;
+  CR_CUDA(cudaMemcpyAsync(e->d_q, q, bytes, cudaMemcpyHostToDevice, e->stream));
+  CR_CUDA(cudaMemcpyAsync(e->d_p, p, bytes, cudaMemcpyHostToDevice, e->stream));
+  if (f) {
+    CR_CUDA(cudaMemcpyAsync(e->d_f, f, bytes, cudaMemcpyHostToDevice, e->stream));
+  } else {
+    int rc = dispatch_forces(e);
+    if (rc) return rc;
+  }
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_get_state(cr_engine* e, double* q, double* p, double* f, double* epot, int* status) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  const size_t bytes = (size_t)e->T * e->P * e->NC * 8;
+  if (q) CR_CUDA(cudaMemcpyAsync(q, e->d_q, bytes, cudaMemcpyDeviceToHost, e->stream));
+  if (p) CR_CUDA(cudaMemcpyAsync(p, e->d_p, bytes, cudaMemcpyDeviceToHost, e->stream));
+  if (f) CR_CUDA(cudaMemcpyAsync(f, e->d_f, bytes, cudaMemcpyDeviceToHost, e->stream));
+  if (epot) CR_CUDA(cudaMemcpyAsync(epot, e->d_epot, (size_t)e->T * 8, cudaMemcpyDeviceToHost, e->stream));
+  if (status)
+    CR_CUDA(cudaMemcpyAsync(status, e->d_status, (size_t)e->T * sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+static int engine_run_async(cr_engine* e, int nsteps) {
+  CR_CUDA(cudaEventRecord(e->ev0, e->stream));
+  int rc = dispatch_run(e, nsteps);
+  if (rc) return rc;
+  CR_CUDA(cudaEventRecord(e->ev1, e->stream));
+  e->istep += nsteps;
+  e->launches = 1;
+  return CR_OK;
+}
+
+static int engine_finish(cr_engine* e) {
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  CR_CUDA(cudaEventElapsedTime(&e->last_ms, e->ev0, e->ev1));
+  std::vector<int> st((size_t)e->T);
+  CR_CUDA(cudaMemcpy(st.data(), e->d_status, st.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int v : st)
+    if (v) return fail(CR_ERR_TRAJECTORY, "a trajectory reported a non-finite coordinate or singular inertia");
+  return CR_OK;
+}
+
+int cr_engine_run(cr_engine* e, int nsteps) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (nsteps < 0) return fail(CR_ERR_ARG, "nsteps must be >= 0");
+  if (nsteps == 0) return CR_OK;
+  int rc = engine_run_async(e, nsteps);
+  if (rc) return rc;
+  return engine_finish(e);
+}
+
+int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* epot) {
+  if (!e || !q || !p || !f) return fail(CR_ERR_ARG, "NULL argument");
+  const size_t bytes = (size_t)e->T * e->P * e->NC * 8;
+  CR_CUDA(cudaMemcpyAsync(e->d_q, q, bytes, cudaMemcpyHostToDevice, e->stream));
+  CR_CUDA(cudaMemcpyAsync(e->d_p, p, bytes, cudaMemcpyHostToDevice, e->stream));
+  CR_CUDA(cudaMemcpyAsync(e->d_f, f, bytes, cudaMemcpyHostToDevice, e->stream));
+  int rc = engine_run_async(e, 1);
+  if (rc) return rc;
+  CR_CUDA(cudaMemcpyAsync(q, e->d_q, bytes, cudaMemcpyDeviceToHost, e->stream));
+  CR_CUDA(cudaMemcpyAsync(p, e->d_p, bytes, cudaMemcpyDeviceToHost, e->stream));
+  CR_CUDA(cudaMemcpyAsync(f, e->d_f, bytes, cudaMemcpyDeviceToHost, e->stream));
+  if (epot) CR_CUDA(cudaMemcpyAsync(epot, e->d_epot, (size_t)e->T * 8, cudaMemcpyDeviceToHost, e->stream));
+  return engine_finish(e);
+}
+
+int cr_engine_last_kernel_ms(const cr_engine* e, float* ms) {
+  if (!e || !ms) return fail(CR_ERR_ARG, "NULL argument");
+  *ms = e->last_ms;
+  return CR_OK;
+}
+
+int cr_engine_launch_info(const cr_engine* e, int* grid, int* block, int* smem_bytes, int* launches) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (grid) *grid = e->grid;
+  if (block) *block = e->block;
+  if (smem_bytes) *smem_bytes = (int)e->smem;
+  if (launches) *launches = e->launches;
+  return CR_OK;
+}
+
+int cr_engine_device_state(cr_engine* e, double** q, double** p, double** f) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (q) *q = e->d_q;
+  if (p) *p = e->d_p;
+  if (f) *f = e->d_f;
+  return CR_OK;
+}
+
+int cr_host_alloc(void** ptr, unsigned long long bytes) {
+  if (!ptr) return fail(CR_ERR_ARG, "NULL argument");
+  CR_CUDA(cudaMallocHost(ptr, (size_t)bytes));
+  return CR_OK;
+}
+
+int cr_host_free(void* ptr) {
+  if (ptr) CR_CUDA(cudaFreeHost(ptr));
+  return CR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,419 @@
+// Persistent RPMD step kernel: many trajectories, all steps of a run in one
+// launch, every bead's q, p, f held in registers across steps.
+//
+// Drop-in for the per-step work of Caracal's `verlet` (src/verlet.f90:65-1308)
+// on the gas-phase path: 1/2 kick, free ring-polymer propagation in Caracal's
+// cosine "normal modes", forces, 1/2 kick, Andersen or PILE thermostat,
+// NaN check, `transrot`.
+//
+// Thread layout: a trajectory owns a group of G = next_pow2(P) consecutive
+// threads, bead j on lane j of the group (lanes j >= P idle).  Groups of
+// G <= 32 live inside one warp; G = 64 or 128 span 2 or 4 warps.
+//
+// Bead coupling.  Caracal applies C = sqrt(1/P) cos(2 pi j k/P) (src/rfft.f90,
+// src/irfft.f90), a per-mode 2x2 rotation (src/verlet.f90:405-454), and C
+// again.  The composite is linear: p' = K1 p + m K2 q, q' = K3 p / m + K1 q
+// with K = C diag(poly) C.  Since poly(k) = poly(P-k), K[j][l] = K[-j][l] =
+// K[j][-l], so only the (P/2+1)^2 block acting on the symmetrised inputs
+// s_l = x_l + x_{-l} is stored (shared memory), and each output needs
+// P/2+1 FMAs instead of P.
+//
+// PILE (new; Caracal has Andersen and Nose-Hoover only) uses the orthonormal
+// real normal modes; O^T diag(c) O is circulant, so each half step is two
+// length-P circular convolutions: p' = a * p + sqrt(mP/beta) b * eta.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "cr_common.cuh"
+
+namespace cr {
+
+constexpr int kMaxBeads = 128;
+constexpr int kMaxAtoms = 7;
+
+struct StepParams {
+  int T;           // trajectories in the launch
+  int P;           // beads
+  int G;           // threads per trajectory (power of two >= P)
+  int H;           // P/2 + 1
+  int thermostat;  // CR_THERMO_*
+  int andersen_step;
+  int transrot;
+  uint32_t seed;
+  uint32_t traj0;  // global index of trajectory 0 (noise key)
+  double dt;
+  double half_dt;
+  double beta;
+  double totmass;  // Caracal's transrot total mass (P^2 sum m)
+  double mass[kMaxAtoms];
+  double inv_mass[kMaxAtoms];
+  double sigma[kMaxAtoms];    // sqrt(m P / beta): Andersen / PILE noise scale
+  const double* prop;  // [3][H][H]: K1, K2 (unit mass), K3 (unit mass)
+  const double* pile;  // [2][P]: circulant a (c1) and b (c2)
+  double* q;           // [T][P][N][3]
+  double* p;
+  double* f;
+  double* epot;        // [T]
+  int* status;         // [T]
+};
+
+// Sum over the G lanes of a group (deterministic tree).  red: per-group
+// shared scratch of (G/32) * NV doubles, used only when G > 32.
+template <int NV>
+__device__ inline void group_sum(double (&v)[NV], int G, double* red, int lane_in_group) {
+  const int w = G < 32 ? G : 32;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    if (o < w) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    }
+  }
+  if (G > 32) {
+    const int nw = G / 32, wid = lane_in_group / 32;
+    __syncthreads();
+    if ((lane_in_group & 31) == 0) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) red[wid * NV + i] = v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double s = red[i];
+      for (int k = 1; k < nw; ++k) s += red[k * NV + i];
+      v[i] = s;
+    }
+  }
+}
+
+__device__ inline void group_sync(int G) {
+  if (G > 32) __syncthreads();
+  else __syncwarp();
+}
+
+// Gauss-Jordan inverse with full pivoting of a 3x3 matrix (the algorithm of
+// Caracal's invert, src/invert.f90:38-124).  Returns false if singular.
+__device__ inline bool invert3(double (&a)[3][3]) {
+  int ipiv[3] = {0, 0, 0}, indxr[3], indxc[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double big = 0.0;
+    int irow = 0, icol = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (ipiv[j] != 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (ipiv[k] == 0 && fabs(a[j][k]) >= big) {
+            big = fabs(a[j][k]);
+            irow = j;
+            icol = k;
+          }
+        }
+      }
+    }
+    ipiv[icol] += 1;
+    if (irow != icol) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double t = a[irow][j];
+        a[irow][j] = a[icol][j];
+        a[icol][j] = t;
+      }
+    }
+    indxr[i] = irow;
+    indxc[i] = icol;
+    if (a[icol][icol] == 0.0) return false;
+    double ipivot = 1.0 / a[icol][icol];
+    a[icol][icol] = 1.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) a[icol][j] *= ipivot;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (j != icol) {
+        double t = a[j][icol];
+        a[j][icol] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a[j][k] -= a[icol][k] * t;
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 2; i >= 0; --i) {
+    if (indxr[i] != indxc[i]) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double t = a[k][indxr[i]];
+        a[k][indxr[i]] = a[k][indxc[i]];
+        a[k][indxc[i]] = t;
+      }
+    }
+  }
+  return true;
+}
+
+// Dynamic shared memory layout (doubles):
+//   [0, 3H^2)                      propagator blocks K1, K2, K3
+//   [3H^2, 3H^2 + 2P)              PILE circulant vectors a, b
+//   then per group: xs[2][NC][G], sym[2][NC][H], red[(G/32) * 16]
+__host__ __device__ inline size_t step_smem_doubles(int P, int G, int NC, int groups) {
+  const int H = P / 2 + 1;
+  size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 16;
+  return (size_t)3 * H * H + 2 * (size_t)P + per_group * groups;
+}
+
+template <class PES, bool MIXED>
+__global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep0, int nsteps) {
+  constexpr int N = PES::N;
+  constexpr int NC = 3 * N;
+  extern __shared__ double smem[];
+  const int P = prm.P, G = prm.G, H = prm.H;
+  const int groups = blockDim.x / G;
+  const int grp = threadIdx.x / G;
+  const int j = threadIdx.x % G;  // bead
+  const int t = blockIdx.x * groups + grp;
+  const bool active = (t < prm.T) && (j < P);
+
+  double* s_prop = smem;
+  double* s_pile = s_prop + 3 * H * H;
+  const size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 16;
+  double* s_grp = s_pile + 2 * P + per_group * grp;
+  double* xs = s_grp;                      // [2][NC][G]
+  double* sym = xs + 2 * NC * G;           // [2][NC][H]
+  double* red = sym + 2 * NC * H;          // [(G/32)][16]
+
+  for (int x = threadIdx.x; x < 3 * H * H; x += blockDim.x) s_prop[x] = prm.prop[x];
+  if (prm.thermostat == CR_THERMO_PILE)
+    for (int x = threadIdx.x; x < 2 * P; x += blockDim.x) s_pile[x] = prm.pile[x];
+
+  double q[NC], p[NC], f[NC];
+  const size_t base = ((size_t)t * P + j) * NC;
+  if (active) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      q[c] = prm.q[base + c];
+      p[c] = prm.p[base + c];
+      f[c] = prm.f[base + c];
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) { q[c] = 0.0; p[c] = 0.0; f[c] = 0.0; }
+  }
+  const uint32_t traj_key = prm.traj0 + (uint32_t)t;
+  int status = 0;
+  double vbead = 0.0;
+  __syncthreads();
+
+  // PILE half step on p (in place); eta from the per-bead Gaussian stream.
+  auto pile_half = [&](uint32_t step, uint32_t tag) {
+    double eta[NC];
+    normals_bead<NC>(prm.seed, traj_key, (uint32_t)j, step, tag, eta);
+    if (!active) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) eta[c] = 0.0;
+    }
+    group_sync(G);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      xs[c * G + j] = p[c];
+      xs[(NC + c) * G + j] = eta[c];
+    }
+    group_sync(G);
+    const double* a = s_pile;
+    const double* b = s_pile + P;
+    if (j < P) {
+      double acc_p[NC], acc_e[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) { acc_p[c] = 0.0; acc_e[c] = 0.0; }
+      int m = j;  // (j - l) mod P
+      for (int l = 0; l < P; ++l) {
+        const double al = a[m], bl = b[m];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          acc_p[c] = fma(al, xs[c * G + l], acc_p[c]);
+          acc_e[c] = fma(bl, xs[(NC + c) * G + l], acc_e[c]);
+        }
+        m = (m == 0) ? P - 1 : m - 1;
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) p[c] = acc_p[c] + prm.sigma[c / 3] * acc_e[c];
+    }
+  };
+
+  for (int n = 1; n <= nsteps; ++n) {
+    const int istep = istep0 + n;
+    if (prm.thermostat == CR_THERMO_PILE) pile_half((uint32_t)istep, TAG_PILE_A);
+
+    // 1/2 kick (src/verlet.f90:216-218)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) p[c] = p[c] - prm.half_dt * f[c];
+
+    // free ring polymer in Caracal's cosine modes (src/verlet.f90:377-463)
+    group_sync(G);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      xs[c * G + j] = p[c];
+      xs[(NC + c) * G + j] = q[c];
+    }
+    group_sync(G);
+    if (j < H) {
+      const int jm = (j == 0) ? 0 : P - j;
+      const bool self = (jm == j);
+#pragma unroll
+      for (int c = 0; c < 2 * NC; ++c) {
+        double v = xs[c * G + j];
+        if (!self) v += xs[c * G + jm];
+        sym[c * H + j] = v;
+      }
+    }
+    group_sync(G);
+    if (j < P) {
+      const int r = (j <= P - j) ? j : P - j;  // unique output row
+      const double* K1 = s_prop + r * H;
+      const double* K2 = s_prop + H * H + r * H;
+      const double* K3 = s_prop + 2 * H * H + r * H;
+      double a1[NC], a2[NC], a3[NC], a4[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) { a1[c] = 0.0; a2[c] = 0.0; a3[c] = 0.0; a4[c] = 0.0; }
+      for (int l = 0; l < H; ++l) {
+        const double k1 = K1[l], k2 = K2[l], k3 = K3[l];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const double sp = sym[c * H + l], sq = sym[(NC + c) * H + l];
+          a1[c] = fma(k1, sp, a1[c]);  // K1 p
+          a2[c] = fma(k2, sq, a2[c]);  // K2 q
+          a3[c] = fma(k3, sp, a3[c]);  // K3 p
+          a4[c] = fma(k1, sq, a4[c]);  // K1 q
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const double m = prm.mass[c / 3], im = prm.inv_mass[c / 3];
+        p[c] = fma(m, a2[c], a1[c]);
+        q[c] = fma(im, a3[c], a4[c]);
+      }
+    }
+
+    // per-bead forces (src/verlet.f90:772-777)
+    double g[NC];
+    if (MIXED) PES::template egrad<float>(q, vbead, g);
+    else PES::template egrad<double>(q, vbead, g);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) f[c] = active ? g[c] : 0.0;
+    if (!active) vbead = 0.0;
+
+    // 1/2 kick (src/verlet.f90:1060-1062)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) p[c] = p[c] - prm.half_dt * f[c];
+
+    // Andersen (src/verlet.f90:1159-1165): full resample every andersen_step
+    if (prm.thermostat == CR_THERMO_ANDERSEN && (istep % prm.andersen_step) == 0) {
+      double z[NC];
+      normals_bead<NC>(prm.seed, traj_key, (uint32_t)j, (uint32_t)istep, TAG_ANDERSEN, z);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) p[c] = active ? z[c] * prm.sigma[c / 3] : 0.0;
+    }
+    if (prm.thermostat == CR_THERMO_PILE) pile_half((uint32_t)istep, TAG_PILE_B);
+
+    // NaN / Inf check (src/verlet.f90:1256-1275)
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      if (!isfinite(q[c])) status |= CR_TRAJ_NONFINITE;
+
+    // transrot (src/transrot.f90:36-237): removed COM velocity and rotation
+    // centre both carry Caracal's extra 1/P (total mass P^2 sum m).
+    if (prm.transrot) {
+      double vel[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) vel[c] = p[c] * prm.inv_mass[c / 3];
+      double s1[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const double w = prm.mass[i];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          s1[d] = fma(vel[3 * i + d], w, s1[d]);
+          s1[3 + d] = fma(q[3 * i + d], w, s1[3 + d]);
+        }
+      }
+      if (!active) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s1[k] = 0.0;
+      }
+      group_sum<6>(s1, G, red, j);
+      const double itm = 1.0 / prm.totmass;
+      const double vt[3] = {s1[0] * itm, s1[1] * itm, s1[2] * itm};
+      const double xt[3] = {s1[3] * itm, s1[4] * itm, s1[5] * itm};
+      double s2[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const double w = prm.mass[i];
+        const double* qq = &q[3 * i];
+        const double* vv = &vel[3 * i];
+        s2[0] = fma(qq[1] * vv[2] - qq[2] * vv[1], w, s2[0]);
+        s2[1] = fma(qq[2] * vv[0] - qq[0] * vv[2], w, s2[1]);
+        s2[2] = fma(qq[0] * vv[1] - qq[1] * vv[0], w, s2[2]);
+        const double xd = qq[0] - xt[0], yd = qq[1] - xt[1], zd = qq[2] - xt[2];
+        s2[3] = fma(xd * xd, w, s2[3]);
+        s2[4] = fma(xd * yd, w, s2[4]);
+        s2[5] = fma(xd * zd, w, s2[5]);
+        s2[6] = fma(yd * yd, w, s2[6]);
+        s2[7] = fma(yd * zd, w, s2[7]);
+        s2[8] = fma(zd * zd, w, s2[8]);
+      }
+      if (!active) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) s2[k] = 0.0;
+      }
+      group_sum<9>(s2, G, red, j);
+      const double tm = prm.totmass;
+      double mang[3] = {s2[0] - (xt[1] * vt[2] - xt[2] * vt[1]) * tm,
+                        s2[1] - (xt[2] * vt[0] - xt[0] * vt[2]) * tm,
+                        s2[2] - (xt[0] * vt[1] - xt[1] * vt[0]) * tm};
+      double ten[3][3] = {{s2[6] + s2[8], -s2[4], -s2[5]},
+                          {-s2[4], s2[3] + s2[8], -s2[7]},
+                          {-s2[5], -s2[7], s2[3] + s2[6]}};
+      if (N <= 2) {
+        ten[0][0] += 0.000001;
+        ten[1][1] += 0.000001;
+        ten[2][2] += 0.000001;
+      }
+      if (!invert3(ten)) {
+        status |= CR_TRAJ_SINGULAR_INERTIA;
+      } else {
+        double va[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) va[a] = ten[a][0] * mang[0] + ten[a][1] * mang[1] + ten[a][2] * mang[2];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          double* vv = &vel[3 * i];
+          vv[0] -= vt[0];
+          vv[1] -= vt[1];
+          vv[2] -= vt[2];
+          const double xd = q[3 * i] - xt[0], yd = q[3 * i + 1] - xt[1], zd = q[3 * i + 2] - xt[2];
+          vv[0] = vv[0] - va[1] * zd + va[2] * yd;
+          vv[1] = vv[1] - va[2] * xd + va[0] * zd;
+          vv[2] = vv[2] - va[0] * yd + va[1] * xd;
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) p[c] = active ? vel[c] * prm.mass[c / 3] : 0.0;
+      }
+    }
+  }
+
+  // potential energy of the last step, summed over beads
+  double e[1] = {vbead};
+  group_sum<1>(e, G, red, j);
+  if (active) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      prm.q[base + c] = q[c];
+      prm.p[base + c] = p[c];
+      prm.f[base + c] = f[c];
+    }
+    if (j == 0) prm.epot[t] = e[0];
+    if (status) atomicOr(&prm.status[t], status);
+  }
+}
+
+}  // namespace cr

@@ -1,0 +1,140 @@
+"""Python host mirror of the engine's C-ABI, named after Caracal's routines.
+
+``egrad_h3`` mirrors ``subroutine egrad_h3(q,Natoms,Nbeads,V,dVdq,info)``
+(src/egrad_h3.f:29); ``RPMDEngine`` batches the ``dynamic`` stepping loop
+(src/dynamic.f90:1569-1579 -> ``verlet``, src/verlet.f90:65) over many
+independent trajectories, with ``mdinit`` (src/mdinit.f90:40-173) as
+``init_positions`` / ``init_momenta`` / ``compute_forces``.
+
+Arrays are numpy float64 of shape (ntraj, nbeads, natoms, 3) in C order,
+which is Caracal's q(3, natoms, nbeads) column-major layout per trajectory.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .units import beta_from_kelvin, dt_fs_to_au
+
+PES = {"h3": L.CR_PES_H3, "ana_h3": L.CR_PES_H3}
+PES_NATOMS = {L.CR_PES_H3: 3}
+THERMOSTAT = {"none": L.CR_THERMO_NONE, "nve": L.CR_THERMO_NONE, "andersen": L.CR_THERMO_ANDERSEN,
+              "nose-hoover": L.CR_THERMO_NHC, "pile": L.CR_THERMO_PILE}
+PRECISION = {"fp64": L.CR_PREC_FP64, "plain": L.CR_PREC_FP64, "mixed": L.CR_PREC_MIXED}
+
+
+def egrad_h3(q):
+    """BKMP2 energies and gradients of q (nbeads, 3, 3) bohr -> (V (nbeads,), dVdq)."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    if q.ndim == 2:
+        q = q[None]
+    nb = q.shape[0]
+    if q.shape[1:] != (3, 3):
+        raise ValueError("egrad_h3 expects q of shape (nbeads, 3, 3)")
+    V = np.zeros(nb)
+    g = np.zeros_like(q)
+    info = C.c_int(0)
+    L.check(L.lib().cr_egrad_h3(L.dptr(q), 3, nb, L.dptr(V), L.dptr(g), C.byref(info)), "egrad_h3")
+    return V, g
+
+
+class RPMDEngine:
+    """A batch of independent RPMD trajectories resident on one GPU."""
+
+    def __init__(self, pes, mass, nbeads, ntraj, dt_au, beta=None, thermostat="none",
+                 andersen_step=70, pile_tau0_au=0.0, transrot=True, precision="fp64", seed=0,
+                 traj0=0):
+        self.pes = PES[pes] if isinstance(pes, str) else int(pes)
+        self.mass = np.ascontiguousarray(mass, dtype=np.float64)
+        self.natoms = len(self.mass)
+        self.nbeads = int(nbeads)
+        self.ntraj = int(ntraj)
+        self.beta = float("inf") if beta is None else float(beta)
+        self.cfg = L.CrConfig(self.pes, self.natoms, self.nbeads, self.ntraj,
+                              THERMOSTAT[thermostat] if isinstance(thermostat, str) else int(thermostat),
+                              int(andersen_step), int(bool(transrot)),
+                              PRECISION[precision] if isinstance(precision, str) else int(precision),
+                              int(seed) & 0xFFFFFFFF, int(traj0) & 0xFFFFFFFF, float(dt_au),
+                              self.beta, float(pile_tau0_au), L.dptr(self.mass))
+        h = C.c_void_p()
+        L.check(L.lib().cr_engine_create(C.byref(self.cfg), C.byref(h)), "cr_engine_create")
+        self._h = h
+
+    @classmethod
+    def from_caracal_units(cls, pes, mass, nbeads, ntraj, dt_fs, kelvin=None, **kw):
+        beta = None if not kelvin else beta_from_kelvin(kelvin)
+        return cls(pes, mass, nbeads, ntraj, dt_fs_to_au(dt_fs), beta=beta, **kw)
+
+    @property
+    def shape(self):
+        return (self.ntraj, self.nbeads, self.natoms, 3)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().cr_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init_positions(self, q0, sigma=0.0):
+        q0 = np.ascontiguousarray(q0, dtype=np.float64).reshape(self.natoms, 3)
+        L.check(L.lib().cr_engine_init_positions(self._h, L.dptr(q0), float(sigma)), "init_positions")
+
+    def init_momenta(self, zero=False):
+        L.check(L.lib().cr_engine_init_momenta(self._h, int(bool(zero))), "init_momenta")
+
+    def compute_forces(self):
+        L.check(L.lib().cr_engine_compute_forces(self._h), "compute_forces")
+
+    def set_state(self, q, p, f=None):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.shape)
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(self.shape)
+        fp = None
+        if f is not None:
+            f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.shape)
+            fp = L.dptr(f)
+        L.check(L.lib().cr_engine_set_state(self._h, L.dptr(q), L.dptr(p), fp), "set_state")
+
+    def get_state(self):
+        q = np.zeros(self.shape)
+        p = np.zeros(self.shape)
+        f = np.zeros(self.shape)
+        e = np.zeros(self.ntraj)
+        st = np.zeros(self.ntraj, dtype=np.int32)
+        L.check(L.lib().cr_engine_get_state(self._h, L.dptr(q), L.dptr(p), L.dptr(f), L.dptr(e),
+                                            L.iptr(st)), "get_state")
+        return q, p, f, e, st
+
+    def run(self, nsteps, check=True):
+        rc = L.lib().cr_engine_run(self._h, int(nsteps))
+        if check:
+            L.check(rc, "run")
+        return rc
+
+    def step_host(self, q, p, f, epot=None):
+        """One verlet step through host arrays (modified in place)."""
+        ep = L.dptr(epot) if epot is not None else None
+        L.check(L.lib().cr_engine_step_host(self._h, L.dptr(q), L.dptr(p), L.dptr(f), ep), "step_host")
+
+    def last_kernel_ms(self):
+        ms = C.c_float()
+        L.check(L.lib().cr_engine_last_kernel_ms(self._h, C.byref(ms)), "last_kernel_ms")
+        return ms.value
+
+    def launch_info(self):
+        g, b, s, n = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        L.check(L.lib().cr_engine_launch_info(self._h, C.byref(g), C.byref(b), C.byref(s), C.byref(n)),
+                "launch_info")
+        return {"grid": g.value, "block": b.value, "smem_bytes": s.value, "launches": n.value}

@@ -1,0 +1,72 @@
+"""Synthetic workloads with the shapes of the engine's benchmark configurations.
+
+Caracal ships no benchmark inputs, so each configuration is a seeded
+synthetic input of the stated shape (geometry, bead count, trajectories,
+temperature, time step).  Interpretations of under-specified geometry are
+parameters here.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .units import angstrom_to_bohr, beta_from_kelvin, dt_fs_to_au, mass_au
+
+SEED = 20261203
+
+
+@dataclass
+class Workload:
+    name: str
+    pes: str
+    symbols: list
+    q0: np.ndarray          # (natoms, 3) bohr
+    nbeads: int
+    ntraj: int
+    kelvin: float
+    dt_fs: float
+    nsteps: int
+    thermostat: str
+    sigma_bohr: float = 0.0
+    andersen_step: int = 70
+    pile_tau0_fs: float = 100.0
+    transrot: bool = True
+    seed: int = SEED
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def mass(self):
+        return np.array([mass_au(s) for s in self.symbols])
+
+    @property
+    def dt_au(self):
+        return dt_fs_to_au(self.dt_fs)
+
+    @property
+    def beta(self):
+        return beta_from_kelvin(self.kelvin) if self.kelvin else float("inf")
+
+    @property
+    def pile_tau0_au(self):
+        return dt_fs_to_au(self.pile_tau0_fs)
+
+    @property
+    def bead_steps(self):
+        return self.nbeads * self.ntraj * self.nsteps
+
+
+def h3_collinear(r_hh_ang=0.74, r_inc_ang=2.5):
+    """Collinear H-H...H along z: H2 bond r_hh, incoming H r_inc from the nearer H."""
+    z = np.array([0.0, r_hh_ang, r_hh_ang + r_inc_ang])
+    q = np.zeros((3, 3))
+    q[:, 2] = z
+    return angstrom_to_bohr(q)
+
+
+def h3_config(ntraj=64, nbeads=16, nsteps=1000, thermostat="pile", kelvin=300.0, dt_fs=0.1):
+    """H + H2 on BKMP2: 3 atoms, 16 beads, 64 trajectories, 300 K, 0.1 fs, bead
+    jitter sigma = 0.01 Angstrom, PILE tau0 = 100 fs (Andersen: ANDERSEN_STEP 70)."""
+    return Workload(name=f"h3_bkmp2_P{nbeads}_T{ntraj}", pes="h3", symbols=["H", "H", "H"],
+                    q0=h3_collinear(), nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs,
+                    nsteps=nsteps, thermostat=thermostat, sigma_bohr=float(angstrom_to_bohr(0.01)))

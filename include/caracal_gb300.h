@@ -1,0 +1,151 @@
+/*
+ * caracal_gb300.h -- C-ABI of the GB300-native RPMD engine.
+ *
+ * A drop-in for the hot path of Caracal's `dynamic` / `calc_rate` programs:
+ * the per-bead PES gradient calls and the ring-polymer `verlet` step.  Every
+ * entry point takes plain pointers and sizes and returns an int status
+ * (CR_OK = 0, > 0 error; nothing in this library calls exit()).  Host arrays
+ * use Caracal's Fortran column-major layout q(3, natoms, nbeads) per
+ * trajectory, with trajectories outermost: element (d, i, k, t) sits at
+ * d + 3*(i + natoms*(k + nbeads*t)).  Units are atomic units (bohr, Hartree,
+ * electron masses), as inside Caracal.
+ *
+ * Each engine owns one CUDA stream and its device memory on the device that
+ * is current when it is created; calls on one engine are not thread-safe,
+ * different engines are independent.
+ */
+#ifndef CARACAL_GB300_H
+#define CARACAL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define CR_OK 0
+#define CR_ERR_ARG 1          /* invalid argument or configuration */
+#define CR_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define CR_ERR_NO_DEVICE 3    /* no CUDA device visible */
+#define CR_ERR_UNSUPPORTED 4  /* valid in Caracal, not provided by this engine */
+#define CR_ERR_TRAJECTORY 5   /* a trajectory went non-finite (Caracal: fatal) */
+#define CR_ERR_IO 6           /* file could not be read or parsed */
+
+/* per-trajectory status bits (cr_engine_get_state) */
+#define CR_TRAJ_NONFINITE 1        /* a coordinate became NaN/Inf (src/verlet.f90:1256-1275) */
+#define CR_TRAJ_SINGULAR_INERTIA 2 /* transrot could not invert the inertia tensor */
+
+/* ---- potentials (Caracal keyword PES) ----------------------------------- */
+#define CR_PES_H3 1      /* ANA_H3: BKMP2, src/egrad_h3.f */
+#define CR_PES_CH4H 2    /* ANA_CH4H: src/egrad_ch4h.f (not built yet) */
+#define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f (not built yet) */
+#define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90, ff_hb.f90 (not built yet) */
+
+/* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
+#define CR_THERMO_NONE 0      /* NVE */
+#define CR_THERMO_ANDERSEN 1  /* src/andersen.f90 */
+#define CR_THERMO_NHC 2       /* src/nhc.f90 (not built yet) */
+#define CR_THERMO_PILE 3      /* PILE-L, new (Ceriotti et al. 2010) */
+
+/* ---- precision forms ------------------------------------------------------ */
+#define CR_PREC_FP64 0   /* plain form: everything in FP64 */
+#define CR_PREC_MIXED 1  /* PES arithmetic in FP32; q, p, propagator, thermostat in FP64 */
+
+typedef struct cr_config {
+  int pes;            /* CR_PES_* */
+  int natoms;         /* must match the PES (H3: 3) */
+  int nbeads;         /* 1..128 (RPMD_BEADS) */
+  int ntraj;          /* independent trajectories in this engine */
+  int thermostat;     /* CR_THERMO_* */
+  int andersen_step;  /* ANDERSEN_STEP (Caracal default 70) */
+  int transrot;       /* 1: remove COM translation/rotation each step (dynamic.x); 0: off (recrossing children) */
+  int precision;      /* CR_PREC_* */
+  unsigned int seed;  /* Gaussian stream key */
+  unsigned int traj0; /* global index of this engine's first trajectory (stream key) */
+  double dt;          /* time step, a.u. (Caracal: DELTAT[fs] / 2.41888428E-2 as REAL(4)) */
+  double beta;        /* 1/(k_B T), a.u., k_B = 0.316679e-5 Eh/K */
+  double pile_tau0;   /* PILE centroid time constant, a.u. */
+  const double* mass; /* natoms masses, a.u. (amu / 5.485799095e-4) */
+} cr_config;
+
+typedef struct cr_engine cr_engine;
+
+/* Human-readable text for a status code, and the detail of the last error
+ * raised on this thread (copied into buf, NUL-terminated). */
+const char* cr_error_string(int code);
+int cr_last_error_detail(char* buf, int len);
+
+int cr_device_count(int* n);
+
+/* ---- PES gradient entry points --------------------------------------------
+ * Replaces `subroutine egrad_h3(q,Natoms,Nbeads,V,dVdq,info)`
+ * (src/egrad_h3.f:29-35; called from src/gradient.f90:172-200): q(3,natoms,nbeads)
+ * in bohr -> V(nbeads) in Hartree, dVdq(3,natoms,nbeads) in Hartree/bohr, info = 0.
+ * Host pointers; all beads are evaluated in one device launch (FP64). */
+int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+
+/* Same surface on device-resident arrays with an explicit precision form
+ * (CR_PREC_*); stream may be 0.  npts = number of (natoms=3) geometries. */
+int cr_egrad_h3_device(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
+                       void* stream);
+
+/* ---- RPMD engine -----------------------------------------------------------
+ * Replaces the stepping loop of `dynamic` (src/dynamic.f90:1569-1579) around
+ * `verlet` (src/verlet.f90:65) and the initialisation of `mdinit`
+ * (src/mdinit.f90:40-173), batched over ntraj independent trajectories. */
+int cr_engine_create(const cr_config* cfg, cr_engine** out);
+int cr_engine_destroy(cr_engine* e);
+
+/* Initial positions: every bead of every trajectory = q0(3,natoms) plus
+ * sigma * N(0,1) per coordinate (sigma in bohr; 0 gives Caracal's identical
+ * beads, src/dynamic.f90:1307-1314). */
+int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma);
+/* mdinit momenta: Andersen draw (NVT, src/mdinit.f90:118-121) or zeros
+ * (NVE, src/mdinit.f90:125). */
+int cr_engine_init_momenta(cr_engine* e, int zero);
+/* mdinit forces (src/mdinit.f90:80-83) of the current positions. */
+int cr_engine_compute_forces(cr_engine* e);
+
+/* Host <-> engine state, arrays (3, natoms, nbeads, ntraj).  f (dV/dq of the
+ * current positions) may be NULL in set_state; it is then recomputed. */
+int cr_engine_set_state(cr_engine* e, const double* q, const double* p, const double* f);
+int cr_engine_get_state(cr_engine* e, double* q, double* p, double* f, double* epot, int* status);
+
+/* Advances every trajectory by nsteps steps in one persistent launch; the
+ * step counter continues from previous runs.  Returns CR_ERR_TRAJECTORY if a
+ * trajectory reported a status bit (state is still returned). */
+int cr_engine_run(cr_engine* e, int nsteps);
+
+/* One `verlet` step through host buffers, as a Fortran caller holding
+ * q_i, p_i, derivs would use it: copy in, one step, copy out (epot may be NULL). */
+int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* epot);
+
+/* Device time of the last cr_engine_run / step kernel (CUDA events on the
+ * engine's stream), launches issued by it, and the launch shape chosen. */
+int cr_engine_last_kernel_ms(const cr_engine* e, float* ms);
+int cr_engine_launch_info(const cr_engine* e, int* grid, int* block, int* smem_bytes, int* launches);
+/* Device pointers of the state arrays (owned by the engine). */
+int cr_engine_device_state(cr_engine* e, double** q, double** p, double** f);
+/* Page-locked host buffers for fast host<->device copies. */
+int cr_host_alloc(void** ptr, unsigned long long bytes);
+int cr_host_free(void* ptr);
+
+/* ---- pipe calibration (no reference counterpart) ---------------------------
+ * Device throughput (operations per second over the whole GPU) of one
+ * operation class in FP64 (fp64 = 1) or FP32: used to weight counted
+ * transcendentals and divisions in FMA-equivalents for the roofline. */
+#define CR_CALIB_FMA 0
+#define CR_CALIB_DIV 1
+#define CR_CALIB_SQRT 2
+#define CR_CALIB_EXP 3
+#define CR_CALIB_LOG 4
+#define CR_CALIB_POW 5
+#define CR_CALIB_SIN 6
+#define CR_CALIB_COS 7
+#define CR_CALIB_ACOS 8
+#define CR_CALIB_ERF 9
+int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CARACAL_GB300_H */

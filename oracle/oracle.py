@@ -1,0 +1,174 @@
+"""ORACLE (test infrastructure only): ctypes view of the CPU restatement.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
+import this module, and only as the checker.  The product path (the CUDA
+library under ``caracal_gb300``) never loads it.
+
+Arrays follow Caracal's Fortran layout ``q(3, natoms, nbeads)`` per
+trajectory; numpy arrays of shape ``(ntraj, nbeads, natoms, 3)`` in C order
+have exactly that memory layout.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+PES_IDS = {"h3": 1}
+THERMOSTATS = {"none": 0, "andersen": 1, "pile": 3}
+OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",
+                  "acos", "erf", "cmp")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc/g++ only)."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    else:
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+class Cfg(C.Structure):
+    _fields_ = [("pes", C.c_int), ("natoms", C.c_int), ("nbeads", C.c_int),
+                ("thermostat", C.c_int), ("andersen_step", C.c_int), ("transrot", C.c_int),
+                ("seed", C.c_uint32), ("dt", C.c_double), ("beta", C.c_double),
+                ("pile_tau0", C.c_double), ("mass", C.POINTER(C.c_double))]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB_PATH)
+        d = C.POINTER(C.c_double)
+        _lib.orc_egrad_h3.argtypes = [d, C.c_int, C.c_int, d, d, C.POINTER(C.c_int)]
+        _lib.orc_h3_pote.argtypes = [d, d, d]
+        _lib.orc_cos_transform.argtypes = [d, C.c_int]
+        _lib.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32,
+                                           C.POINTER(C.c_uint32)]
+        _lib.orc_normal_pair.argtypes = [C.c_uint32] * 6 + [d]
+        _lib.orc_transrot.argtypes = [C.POINTER(Cfg), d, d]
+        _lib.orc_init_positions.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, d, C.c_double, d]
+        _lib.orc_init_momenta.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, d]
+        _lib.orc_init_forces.argtypes = [C.POINTER(Cfg), C.c_int, d, d, d]
+        _lib.orc_run.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_int, C.c_int, d, d, d, d,
+                                 C.POINTER(C.c_int), C.c_int]
+        _lib.orc_pes_opcount.argtypes = [C.c_int, d, C.POINTER(C.c_uint64)]
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Config:
+    """Step configuration for the oracle (all quantities in atomic units)."""
+
+    def __init__(self, pes, mass, nbeads, dt, beta, thermostat="none", andersen_step=70,
+                 pile_tau0=0.0, transrot=True, seed=0):
+        self.mass = np.ascontiguousarray(mass, dtype=np.float64)
+        self.natoms = len(self.mass)
+        self.nbeads = int(nbeads)
+        self.c = Cfg(PES_IDS[pes] if isinstance(pes, str) else int(pes), self.natoms,
+                     self.nbeads, THERMOSTATS[thermostat], int(andersen_step), int(bool(transrot)),
+                     int(seed) & 0xFFFFFFFF, float(dt), float(beta), float(pile_tau0),
+                     _dp(self.mass))
+
+    def shape(self, ntraj):
+        return (ntraj, self.nbeads, self.natoms, 3)
+
+
+def philox(ctr, k0, k1):
+    c = (C.c_uint32 * 4)(*ctr)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox4x32_10(c, k0, k1, o)
+    return list(o)
+
+
+def normal_pair(seed, traj, pair, bead, step, tag):
+    out = np.zeros(2)
+    lib().orc_normal_pair(seed, traj, pair, bead, step, tag, _dp(out))
+    return out
+
+
+def egrad_h3(q):
+    """q: (nbeads, natoms=3, 3) -> V (nbeads,), dVdq (nbeads, 3, 3)."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    nb = q.shape[0]
+    V = np.zeros(nb)
+    g = np.zeros_like(q)
+    info = C.c_int(0)
+    lib().orc_egrad_h3(_dp(q), 3, nb, _dp(V), _dp(g), C.byref(info))
+    return V, g
+
+
+def h3_pote(R):
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    V = np.zeros(1)
+    dV = np.zeros(3)
+    lib().orc_h3_pote(_dp(R), _dp(V), _dp(dV))
+    return V[0], dV
+
+
+def cos_transform(x):
+    x = np.array(x, dtype=np.float64)
+    lib().orc_cos_transform(_dp(x), len(x))
+    return x
+
+
+def transrot(cfg: Config, q, p):
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    p = np.array(p, dtype=np.float64)
+    rc = lib().orc_transrot(C.byref(cfg.c), _dp(q), _dp(p))
+    return rc, p
+
+
+def init_positions(cfg: Config, ntraj, q0, sigma, traj0=0):
+    q0 = np.ascontiguousarray(q0, dtype=np.float64)
+    q = np.zeros(cfg.shape(ntraj))
+    lib().orc_init_positions(C.byref(cfg.c), ntraj, traj0, _dp(q0), float(sigma), _dp(q))
+    return q
+
+
+def init_momenta(cfg: Config, ntraj, traj0=0):
+    p = np.zeros(cfg.shape(ntraj))
+    lib().orc_init_momenta(C.byref(cfg.c), ntraj, traj0, _dp(p))
+    return p
+
+
+def init_forces(cfg: Config, q):
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    f = np.zeros_like(q)
+    e = np.zeros(q.shape[0])
+    lib().orc_init_forces(C.byref(cfg.c), q.shape[0], _dp(q), _dp(f), _dp(e))
+    return f, e
+
+
+def run(cfg: Config, q, p, f, nsteps, istep0=0, traj0=0, nthreads=0):
+    """Advance copies of (q, p, f) by nsteps; returns (q, p, f, epot, status)."""
+    q = np.array(q, dtype=np.float64)
+    p = np.array(p, dtype=np.float64)
+    f = np.array(f, dtype=np.float64)
+    T = q.shape[0]
+    e = np.zeros(T)
+    st = np.zeros(T, dtype=np.int32)
+    lib().orc_run(C.byref(cfg.c), T, traj0, istep0, nsteps, _dp(q), _dp(p), _dp(f), _dp(e),
+                  st.ctypes.data_as(C.POINTER(C.c_int)), nthreads)
+    return q, p, f, e, st
+
+
+def pes_opcount(pes, q):
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    out = (C.c_uint64 * 12)()
+    lib().orc_pes_opcount(PES_IDS[pes] if isinstance(pes, str) else pes, _dp(q), out)
+    return dict(zip(OPCOUNT_FIELDS, list(out)))

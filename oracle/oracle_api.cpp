@@ -1,0 +1,140 @@
+// ORACLE (test infrastructure only) -- C entry points of the CPU restatement.
+#include "oracle_api.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "opcount.hpp"
+#include "pes_h3.hpp"
+#include "philox.hpp"
+#include "rpmd.hpp"
+
+namespace {
+
+orc::StepConfig to_step(const orc_cfg* c) {
+  orc::StepConfig s;
+  s.natoms = c->natoms;
+  s.nbeads = c->nbeads;
+  s.dt = c->dt;
+  s.beta = c->beta;
+  s.thermostat = c->thermostat;
+  s.andersen_step = c->andersen_step > 0 ? c->andersen_step : 1;
+  s.pile_tau0 = c->pile_tau0;
+  s.transrot = c->transrot;
+  s.seed = c->seed;
+  s.mass = c->mass;
+  return s;
+}
+
+// Per-bead PES call, q(3,N) -> V, g(3,N).
+struct BeadPES {
+  int pes;
+  int natoms;
+  void operator()(const double* q, double* V, double* g) const {
+    switch (pes) {
+      case 1: orc::h3::egrad_bead<double>(q, V, g); break;
+      default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+void orc_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
+  orc::Philox4 r = orc::philox4x32_10(ctr, k0, k1);
+  for (int i = 0; i < 4; ++i) out[i] = r.v[i];
+}
+
+void orc_normal_pair(uint32_t seed, uint32_t traj, uint32_t pair, uint32_t bead, uint32_t step,
+                     uint32_t tag, double out[2]) {
+  orc::normal_pair(seed, traj, pair, bead, step, tag, &out[0], &out[1]);
+}
+
+void orc_h3_pote(const double R[3], double* V, double dV[3]) { orc::h3::pote<double>(R, V, dV); }
+
+void orc_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
+  if (info) *info = 0;
+  for (int k = 0; k < nbeads; ++k)
+    orc::h3::egrad_bead<double>(&q[(size_t)k * 3 * natoms], &V[k], &dVdq[(size_t)k * 3 * natoms]);
+}
+
+void orc_cos_transform(double* x, int P) { orc::caracal_cos_transform(x, P); }
+
+int orc_transrot(const orc_cfg* cf, const double* q, double* p) {
+  orc::StepConfig s = to_step(cf);
+  return orc::transrot(s, q, p);
+}
+
+void orc_init_positions(const orc_cfg* cf, int ntraj, uint32_t traj0, const double* q0,
+                        double sigma, double* q) {
+  const int N = cf->natoms, P = cf->nbeads;
+  std::vector<double> z(3 * N);
+  for (int t = 0; t < ntraj; ++t)
+    for (int k = 0; k < P; ++k) {
+      orc::normals_bead(cf->seed, traj0 + t, (uint32_t)k, 0, orc::TAG_BEAD_JITTER, 3 * N, z.data());
+      double* qq = &q[((size_t)t * P + k) * 3 * N];
+      for (int x = 0; x < 3 * N; ++x) qq[x] = q0[x] + sigma * z[x];
+    }
+}
+
+void orc_init_momenta(const orc_cfg* cf, int ntraj, uint32_t traj0, double* p) {
+  orc::StepConfig s = to_step(cf);
+  const size_t per = (size_t)3 * cf->natoms * cf->nbeads;
+  for (int t = 0; t < ntraj; ++t) orc::andersen(s, traj0 + t, 0, orc::TAG_INIT_MOMENTA, &p[t * per]);
+}
+
+int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, double* epot) {
+  BeadPES pes{cf->pes, cf->natoms};
+  const int n3 = 3 * cf->natoms, P = cf->nbeads;
+  for (int t = 0; t < ntraj; ++t) {
+    double e = 0.0;
+    for (int k = 0; k < P; ++k) {
+      double v;
+      size_t off = ((size_t)t * P + k) * n3;
+      pes(&q[off], &v, &f[off]);
+      e = e + v;
+    }
+    if (epot) epot[t] = e;
+  }
+  return 0;
+}
+
+int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q,
+            double* p, double* f, double* epot, int* status, int nthreads) {
+  orc::StepConfig s = to_step(cf);
+  BeadPES pes{cf->pes, cf->natoms};
+  const size_t per = (size_t)3 * cf->natoms * cf->nbeads;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int t = 0; t < ntraj; ++t) {
+    int st = 0;
+    double e = 0.0;
+    for (int n = 1; n <= nsteps; ++n)
+      st |= orc::verlet_step(s, traj0 + t, istep0 + n, &q[t * per], &p[t * per], &f[t * per], &e, pes);
+    if (epot) epot[t] = e;
+    if (status) status[t] |= st;
+  }
+  return 0;
+}
+
+void orc_pes_opcount(int pes, const double* q, uint64_t out[12]) {
+  orc::tally().reset();
+  if (pes == 1) {
+    orc::OC qq[9], V, g[9];
+    for (int x = 0; x < 9; ++x) qq[x] = orc::OC(q[x]);
+    orc::h3::egrad_bead<orc::OC>(qq, &V, g);
+  }
+  const orc::OpTally& t = orc::tally();
+  uint64_t v[12] = {t.add, t.mul, t.div, t.sqrt, t.exp, t.log, t.pow, t.sin, t.cos, t.acos, t.erf, t.cmp};
+  for (int i = 0; i < 12; ++i) out[i] = v[i];
+}
+
+}  // extern "C"

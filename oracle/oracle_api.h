@@ -1,0 +1,54 @@
+/* ORACLE (test infrastructure only) -- C entry points of the CPU restatement.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * this library, and only as the checker.  Arrays are Fortran column-major
+ * q(3, natoms, nbeads) per trajectory, trajectories outermost. */
+#ifndef CARACAL_ORACLE_API_H
+#define CARACAL_ORACLE_API_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_cfg {
+  int pes;            /* 1 = H3 (BKMP2) */
+  int natoms;
+  int nbeads;
+  int thermostat;     /* 0 none, 1 Andersen, 3 PILE */
+  int andersen_step;
+  int transrot;       /* 1: remove COM translation/rotation every step */
+  uint32_t seed;
+  double dt;          /* a.u. */
+  double beta;        /* a.u. */
+  double pile_tau0;   /* a.u. */
+  const double* mass; /* natoms, a.u. */
+} orc_cfg;
+
+void orc_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]);
+void orc_normal_pair(uint32_t seed, uint32_t traj, uint32_t pair, uint32_t bead, uint32_t step,
+                     uint32_t tag, double out[2]);
+void orc_h3_pote(const double R[3], double* V, double dV[3]);
+/* egrad_h3(q, Natoms, Nbeads, V, dVdq, info) of src/egrad_h3.f:29 */
+void orc_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+void orc_cos_transform(double* x, int P);
+int orc_transrot(const orc_cfg* cf, const double* q, double* p);
+/* bead jitter: q[t] = q0 + sigma * N(0,1) (tag 4, step 0) */
+void orc_init_positions(const orc_cfg* cf, int ntraj, uint32_t traj0, const double* q0,
+                        double sigma, double* q);
+/* mdinit: Andersen draw at step 0 (tag 0) */
+void orc_init_momenta(const orc_cfg* cf, int ntraj, uint32_t traj0, double* p);
+/* mdinit: forces of the initial positions; epot[t] = sum over beads */
+int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, double* epot);
+/* nsteps verlet steps (istep0+1 .. istep0+nsteps) of ntraj trajectories;
+ * status[t] ORs the per-step status bits; nthreads <= 0 uses all cores. */
+int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q,
+            double* p, double* f, double* epot, int* status, int nthreads);
+/* algorithmic operation tallies (add, mul, div, sqrt, exp, log, pow, sin, cos,
+ * acos, erf, cmp) of one PES evaluation of one bead at geometry q. */
+void orc_pes_opcount(int pes, const double* q, uint64_t out[12]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
