@@ -37,38 +37,44 @@ template <> __device__ inline float fsqrt<float>(float x) { return sqrtf(x); }
 template <class F> __device__ inline F frcp(F x) { return F(1) / x; }
 
 // Schwenke H2 singlet E(R) and dE/dR (VH2OPT95).
+// The polynomial alpha(R) of the Schwenke curve sums terms up to ~1e6 at
+// R ~ 12 bohr that cancel to ~-25, so even the rounding of R to float moves
+// exp(alpha) by orders of magnitude: alpha and dalpha/dR are always evaluated
+// in FP64 from the FP64 distance Rd; the rest follows the compute type F.
 template <class F>
-__device__ inline void singlet(F R, F ir, F& E, F& dE) {
-  const F a0 = K4(0.03537359271649620), a1 = K4(2.013977588700072),
-          a2 = K4(-2.827452449964767), a3 = K4(2.713257715593500),
-          a4 = K4(-2.792039234205731), a5 = K4(2.166542078766724),
-          a6 = K4(-1.272679684173909), a7 = K4(0.5630423099212294),
-          a8 = K4(-0.1879397372273814), a9 = K4(0.04719891893374140),
-          a10 = K4(-0.008851622656489644), a11 = K4(0.001224998776243630),
-          a12 = K8(-1.227820520228028e-04), a13 = K8(8.638783190083473e-06),
-          a14 = K8(-4.036967926499151e-07), a15 = K8(1.123286608335365e-08),
-          a16 = K8(-1.406619156782167e-10);
+__device__ inline void singlet(double Rd, F R, F ir, F& E, F& dE) {
   const F R0 = K8(3.5284882), DD = K8(0.160979391);
   const F C6 = K8(6.499027), C8 = K8(124.3991), C10 = K8(3285.828);
-  // polynomial part a1 + a2 R + ... + a16 R^15 and its derivative, Horner form
-  F pa = a16, pd = F(15) * a16;
-  pa = pa * R + a15; pd = pd * R + F(14) * a15;
-  pa = pa * R + a14; pd = pd * R + F(13) * a14;
-  pa = pa * R + a13; pd = pd * R + F(12) * a13;
-  pa = pa * R + a12; pd = pd * R + F(11) * a12;
-  pa = pa * R + a11; pd = pd * R + F(10) * a11;
-  pa = pa * R + a10; pd = pd * R + F(9) * a10;
-  pa = pa * R + a9;  pd = pd * R + F(8) * a9;
-  pa = pa * R + a8;  pd = pd * R + F(7) * a8;
-  pa = pa * R + a7;  pd = pd * R + F(6) * a7;
-  pa = pa * R + a6;  pd = pd * R + F(5) * a6;
-  pa = pa * R + a5;  pd = pd * R + F(4) * a5;
-  pa = pa * R + a4;  pd = pd * R + F(3) * a4;
-  pa = pa * R + a3;  pd = pd * R + F(2) * a3;
-  pa = pa * R + a2;  pd = pd * R + a2;
-  pa = pa * R + a1;
-  F alpha = a0 * ir + pa;
-  F dalpha = pd - a0 * ir * ir;
+  // polynomial part a1 + a2 R + ... + a16 R^15 and its derivative, Horner
+  // form, FP64 (the a_i are the same widened REAL(4)/REAL(8) values)
+  const double b0 = (double)(0.03537359271649620f), b1 = (double)(2.013977588700072f),
+               b2 = (double)(-2.827452449964767f), b3 = (double)(2.713257715593500f),
+               b4 = (double)(-2.792039234205731f), b5 = (double)(2.166542078766724f),
+               b6 = (double)(-1.272679684173909f), b7 = (double)(0.5630423099212294f),
+               b8 = (double)(-0.1879397372273814f), b9 = (double)(0.04719891893374140f),
+               b10 = (double)(-0.008851622656489644f), b11 = (double)(0.001224998776243630f),
+               b12 = -1.227820520228028e-04, b13 = 8.638783190083473e-06,
+               b14 = -4.036967926499151e-07, b15 = 1.123286608335365e-08,
+               b16 = -1.406619156782167e-10;
+  double pa = b16, pd = 15.0 * b16;
+  pa = pa * Rd + b15; pd = pd * Rd + 14.0 * b15;
+  pa = pa * Rd + b14; pd = pd * Rd + 13.0 * b14;
+  pa = pa * Rd + b13; pd = pd * Rd + 12.0 * b13;
+  pa = pa * Rd + b12; pd = pd * Rd + 11.0 * b12;
+  pa = pa * Rd + b11; pd = pd * Rd + 10.0 * b11;
+  pa = pa * Rd + b10; pd = pd * Rd + 9.0 * b10;
+  pa = pa * Rd + b9;  pd = pd * Rd + 8.0 * b9;
+  pa = pa * Rd + b8;  pd = pd * Rd + 7.0 * b8;
+  pa = pa * Rd + b7;  pd = pd * Rd + 6.0 * b7;
+  pa = pa * Rd + b6;  pd = pd * Rd + 5.0 * b6;
+  pa = pa * Rd + b5;  pd = pd * Rd + 4.0 * b5;
+  pa = pa * Rd + b4;  pd = pd * Rd + 3.0 * b4;
+  pa = pa * Rd + b3;  pd = pd * Rd + 2.0 * b3;
+  pa = pa * Rd + b2;  pd = pd * Rd + b2;
+  pa = pa * Rd + b1;
+  const double ird = 1.0 / Rd;
+  F alpha = (F)(b0 * ird + pa);
+  F dalpha = (F)(pd - b0 * ird * ird);
   F ea = fexp<F>(alpha);
   F em1 = ea - F(1);
   F r2 = R * R, r4 = r2 * r2, r6 = r4 * r2;
@@ -112,14 +118,14 @@ __device__ inline void triplet(F R, F ir, F e1, F de1, F& E3, F& dE3) {
 
 // Full BKMP2 V(R1,R2,R3) and dV/dRi (POTE).
 template <class F>
-__device__ inline void pote(const F (&R)[3], F& V, F (&dV)[3]) {
+__device__ inline void pote(const F (&R)[3], const double (&Rd)[3], F& V, F (&dV)[3]) {
   F ir[3] = {frcp<F>(R[0]), frcp<F>(R[1]), frcp<F>(R[2])};
   // ---- London term (H3LOND95)
   F Q[3], J[3], dQ[3], dJ[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     F e1, de1, e3, de3;
-    singlet<F>(R[i], ir[i], e1, de1);
+    singlet<F>(Rd[i], R[i], ir[i], e1, de1);
     triplet<F>(R[i], ir[i], e1, de1, e3, de3);
     Q[i] = F(0.5) * (e1 + e3);
     J[i] = F(0.5) * (e1 - e3);
@@ -411,13 +417,17 @@ struct PesH3 {
       d[2][c] = (F)(q[6 + c] - q[3 + c]);
     }
     F R[3], iR[3];
+    double Rd[3];
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      R[b] = h3::fsqrt<F>(d[b][0] * d[b][0] + d[b][1] * d[b][1] + d[b][2] * d[b][2]);
+      const int i0 = (b == 0) ? 3 : (b == 1) ? 0 : 6, i1 = (b == 0) ? 0 : (b == 1) ? 6 : 3;
+      const double x = q[i0] - q[i1], y = q[i0 + 1] - q[i1 + 1], z = q[i0 + 2] - q[i1 + 2];
+      Rd[b] = sqrt(x * x + y * y + z * z);
+      R[b] = (F)Rd[b];
       iR[b] = F(1) / R[b];
     }
     F v, dv[3];
-    h3::pote<F>(R, v, dv);
+    h3::pote<F>(R, Rd, v, dv);
     V = (double)v;
     F u[3] = {dv[0] * iR[0], dv[1] * iR[1], dv[2] * iR[2]};
 #pragma unroll

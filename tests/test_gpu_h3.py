@@ -119,7 +119,7 @@ def test_step_host_equals_device_run(require_gpu):
 def test_nve_classical_energy_drift_no_larger_than_oracle(require_gpu):
     # P = 1, NVE, transrot on (src/verlet.f90:1300-1306); compare drift of E = K + V
     eng, cfg = make_pair(1, 4, thermostat="none", kelvin=None)
-    q, p, f, e = start(eng, cfg, sigma=0.05)
+    q, p, f, e = start(eng, cfg, sigma=0.05, zero_p=True)
     rng = np.random.default_rng(2)
     p = rng.normal(0, 3.0, p.shape)
     eng.set_state(q, p, f)
@@ -153,8 +153,6 @@ def test_nonfinite_trajectory_is_flagged_not_fatal(require_gpu):
 def test_mixed_form_force_error(require_gpu):
     rng = np.random.default_rng(4)
     q = h3_collinear()[None] + rng.normal(0, 0.2, (8192, 3, 3))
-    import ctypes
-    lib = L.lib()
     # the mixed form through the engine: one force evaluation at the same positions
     eng64, cfg = make_pair(16, 512, thermostat="none", kelvin=300.0, precision="fp64")
     eng32, _ = make_pair(16, 512, thermostat="none", kelvin=300.0, precision="mixed")
@@ -167,4 +165,17 @@ def test_mixed_form_force_error(require_gpu):
     err_f = rel_err(f32, f64)
     err_e = rel_err(e32, e64)
     print(f"mixed-form force error {err_f:.3e}, energy error {err_e:.3e}")
-    assert err_f < 1e-3 and err_e < 1e-5
+    # stated bound of the mixed form on this distribution (measured ~2e-7)
+    assert err_f < 1e-6 and err_e < 1e-6
+
+
+@pytest.mark.parametrize("thermostat", ["andersen", "pile"])
+def test_mixed_single_step_close_to_oracle(require_gpu, thermostat):
+    eng, cfg = make_pair(16, 8, thermostat=thermostat, precision="mixed", andersen_step=1)
+    q, p, f, e = start(eng, cfg)
+    eng.run(1)
+    qg, pg, fg, eg, st = eng.get_state()
+    qo, po, fo, eo, so = orc.run(cfg, q, p, f, 1)
+    assert rel_err(qg, qo) <= 1e-9
+    assert rel_err(fg, fo) <= 1e-6
+    assert rel_err(pg, po) <= 1e-6
