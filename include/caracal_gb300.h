@@ -83,6 +83,18 @@ int cr_device_count(int* n);
  * Host pointers; all beads are evaluated in one device launch (FP64). */
 int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
 
+/* No counterpart in Caracal.  The same BKMP2 gradient as cr_egrad_h3 (FP64,
+ * same arguments) for callers that cannot allocate device memory: an MD loop
+ * calling the PES every step cannot pay the device-wide synchronisation of
+ * cudaMalloc/cudaFree per call, and a host whose device memory belongs to its
+ * own pre-sized pool may not allocate outside it.  Stages through one fixed
+ * file-scope device array (2.49 MB per device, held until exit) and allocates
+ * nothing.  At most 16384 beads per call (more: CR_ERR_ARG).  All calls share
+ * that array, so calls that overlap on the GPU race; serialise them.  The
+ * first call on a device resolves the array's address (set-up), so make it
+ * before any stream capture. */
+int cr_egrad_h3_noalloc(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+
 /* Same surface on device-resident arrays with an explicit precision form
  * (CR_PREC_*); stream may be 0.  npts = number of (natoms=3) geometries. */
 int cr_egrad_h3_device(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
