@@ -71,6 +71,9 @@ def _sig(lib):
         "cr_device_count": ([i], C.c_int),
         "cr_egrad_h3": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
         "cr_egrad_h3_device": ([v, C.c_int, v, v, C.c_int, v], C.c_int),
+        "cr_egrad_ch4h": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
+        "cr_initialize_ch4h": ([], C.c_int),
+        "cr_egrad_device": ([C.c_int, v, C.c_int, v, v, C.c_int, v], C.c_int),
         "cr_engine_create": ([C.POINTER(CrConfig), C.POINTER(C.c_void_p)], C.c_int),
         "cr_engine_destroy": ([eng], C.c_int),
         "cr_engine_init_positions": ([eng, d, C.c_double], C.c_int),

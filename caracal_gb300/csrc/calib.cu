@@ -26,6 +26,8 @@ __device__ inline double op_apply<double>(int op, double x) {
     case CR_CALIB_COS: return cos(x);
     case CR_CALIB_ACOS: return acos(0.5 * x) * 0.3;
     case CR_CALIB_ERF: return erf(x) + 0.1;
+    case CR_CALIB_TANH: return tanh(x) + 0.2;
+    case CR_CALIB_COSH: return cosh(x) - 0.9;
     default: return x;
   }
 }
@@ -43,6 +45,8 @@ __device__ inline float op_apply<float>(int op, float x) {
     case CR_CALIB_COS: return cosf(x);
     case CR_CALIB_ACOS: return acosf(0.5f * x) * 0.3f;
     case CR_CALIB_ERF: return erff(x) + 0.1f;
+    case CR_CALIB_TANH: return tanhf(x) + 0.2f;
+    case CR_CALIB_COSH: return coshf(x) - 0.9f;
     default: return x;
   }
 }
@@ -85,6 +89,8 @@ int run_one(int op, int iters, float* ms) {
       case CR_CALIB_COS: calib_kernel<F, CR_CALIB_COS><<<grid, block>>>(out, iters); break;
       case CR_CALIB_ACOS: calib_kernel<F, CR_CALIB_ACOS><<<grid, block>>>(out, iters); break;
       case CR_CALIB_ERF: calib_kernel<F, CR_CALIB_ERF><<<grid, block>>>(out, iters); break;
+      case CR_CALIB_TANH: calib_kernel<F, CR_CALIB_TANH><<<grid, block>>>(out, iters); break;
+      case CR_CALIB_COSH: calib_kernel<F, CR_CALIB_COSH><<<grid, block>>>(out, iters); break;
       default: break;
     }
   };
@@ -103,7 +109,7 @@ int run_one(int op, int iters, float* ms) {
 }  // namespace
 
 extern "C" int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s) {
-  if (!ops_per_s || op < CR_CALIB_FMA || op > CR_CALIB_ERF || iters < 1) return CR_ERR_ARG;
+  if (!ops_per_s || op < CR_CALIB_FMA || op > CR_CALIB_COSH || iters < 1) return CR_ERR_ARG;
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CR_ERR_NO_DEVICE;
   float ms = 0.f;

@@ -9,6 +9,7 @@
 
 #include "../../include/caracal_gb300.h"
 #include "cr_common.cuh"
+#include "pes_ch4h.cuh"
 #include "pes_h3.cuh"
 #include "rpmd_kernel.cuh"
 
@@ -39,6 +40,7 @@ int next_pow2(int x) {
 int pes_natoms(int pes) {
   switch (pes) {
     case CR_PES_H3: return 3;
+    case CR_PES_CH4H: return 6;
     default: return -1;
   }
 }
@@ -230,6 +232,7 @@ int launch_forces(cr_engine* e) {
 int dispatch_run(cr_engine* e, int nsteps) {
   switch (e->cfg.pes) {
     case CR_PES_H3: return launch_run<cr::PesH3>(e, nsteps);
+    case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, nsteps);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -237,6 +240,7 @@ int dispatch_run(cr_engine* e, int nsteps) {
 int dispatch_forces(cr_engine* e) {
   switch (e->cfg.pes) {
     case CR_PES_H3: return launch_forces<cr::PesH3>(e);
+    case CR_PES_CH4H: return launch_forces<cr::PesCH4H>(e);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -264,6 +268,53 @@ void choose_launch(cr_engine* e) {
 // ---------------------------------------------------------------------------
 // C-ABI
 // ---------------------------------------------------------------------------
+template <class PES>
+static int egrad_device_impl(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
+                             cudaStream_t s) {
+  const int bs = 128;
+  if (precision == CR_PREC_MIXED)
+    cr::egrad_kernel<PES, true><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
+  else if (precision == CR_PREC_FP64)
+    cr::egrad_kernel<PES, false><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
+  else
+    return fail(CR_ERR_ARG, "unknown precision");
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+extern "C" int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq,
+                               int precision, void* stream);
+
+// Host-pointer egrad for any PES: stage through device buffers, one launch.
+static int egrad_host(int pes, int natoms_expected, const double* q, int natoms, int nbeads, double* V,
+                      double* dVdq, int* info) {
+  if (info) *info = 0;
+  if (natoms != natoms_expected) return fail(CR_ERR_ARG, "natoms does not match the PES");
+  if (nbeads < 0 || (nbeads > 0 && (!q || !V || !dVdq))) return fail(CR_ERR_ARG, "bad egrad arguments");
+  if (nbeads == 0) return CR_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(CR_ERR_NO_DEVICE, "no CUDA device");
+  const size_t nq = (size_t)3 * natoms * nbeads;
+  double *d_q = nullptr, *d_V = nullptr, *d_g = nullptr;
+  CR_CUDA(cudaMalloc(&d_q, nq * sizeof(double)));
+  cudaError_t e1 = cudaMalloc(&d_V, (size_t)nbeads * sizeof(double));
+  cudaError_t e2 = cudaMalloc(&d_g, nq * sizeof(double));
+  int rc = CR_OK;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    rc = fail(CR_ERR_CUDA, "cudaMalloc failed in egrad");
+  } else if (cudaMemcpy(d_q, q, nq * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = fail(CR_ERR_CUDA, "copy of q failed");
+  } else if ((rc = cr_egrad_device(pes, d_q, nbeads, d_V, d_g, CR_PREC_FP64, nullptr)) == CR_OK) {
+    if (cudaMemcpy(V, d_V, (size_t)nbeads * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(dVdq, d_g, nq * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = fail(CR_ERR_CUDA, "copy of results failed");
+  }
+  cudaFree(d_q);
+  cudaFree(d_V);
+  cudaFree(d_g);
+  return rc;
+}
+
 extern "C" {
 
 const char* cr_error_string(int code) {
@@ -297,21 +348,28 @@ int cr_device_count(int* n) {
   return CR_OK;
 }
 
-int cr_egrad_h3_device(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
-                       void* stream) {
+int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
+                    void* stream) {
   if (npts < 0 || (npts > 0 && (!d_q || !d_V || !d_dVdq))) return fail(CR_ERR_ARG, "bad egrad arguments");
   if (npts == 0) return CR_OK;
-  const int bs = 128;
   cudaStream_t s = (cudaStream_t)stream;
-  if (precision == CR_PREC_MIXED)
-    cr::egrad_kernel<cr::PesH3, true><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
-  else if (precision == CR_PREC_FP64)
-    cr::egrad_kernel<cr::PesH3, false><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
-  else
-    return fail(CR_ERR_ARG, "unknown precision");
-  CR_CUDA(cudaGetLastError());
-  return CR_OK;
+  switch (pes) {
+    case CR_PES_H3: return egrad_device_impl<cr::PesH3>(d_q, npts, d_V, d_dVdq, precision, s);
+    case CR_PES_CH4H: return egrad_device_impl<cr::PesCH4H>(d_q, npts, d_V, d_dVdq, precision, s);
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
 }
+
+int cr_egrad_h3_device(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
+                       void* stream) {
+  return cr_egrad_device(CR_PES_H3, d_q, npts, d_V, d_dVdq, precision, stream);
+}
+
+int cr_egrad_ch4h(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
+  return egrad_host(CR_PES_CH4H, 6, q, natoms, nbeads, V, dVdq, info);
+}
+
+int cr_initialize_ch4h(void) { return CR_OK; }
 
 int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
   if (info) *info = 0;
@@ -480,6 +538,10 @@ int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
       cr::init_positions_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
       break;
+    case CR_PES_CH4H:
+      cr::init_positions_kernel<18><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
+      break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
   CR_CUDA(cudaGetLastError());
@@ -495,6 +557,10 @@ int cr_engine_init_momenta(cr_engine* e, int zero) {
   switch (e->cfg.pes) {
     case CR_PES_H3:
       cr::init_momenta_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+      break;
+    case CR_PES_CH4H:
+      cr::init_momenta_kernel<18><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
       break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");

@@ -18,8 +18,8 @@ import numpy as np
 from . import _lib as L
 from .units import beta_from_kelvin, dt_fs_to_au
 
-PES = {"h3": L.CR_PES_H3, "ana_h3": L.CR_PES_H3}
-PES_NATOMS = {L.CR_PES_H3: 3}
+PES = {"h3": L.CR_PES_H3, "ana_h3": L.CR_PES_H3, "ch4h": L.CR_PES_CH4H, "ana_ch4h": L.CR_PES_CH4H}
+PES_NATOMS = {L.CR_PES_H3: 3, L.CR_PES_CH4H: 6}
 THERMOSTAT = {"none": L.CR_THERMO_NONE, "nve": L.CR_THERMO_NONE, "andersen": L.CR_THERMO_ANDERSEN,
               "nose-hoover": L.CR_THERMO_NHC, "pile": L.CR_THERMO_PILE}
 PRECISION = {"fp64": L.CR_PREC_FP64, "plain": L.CR_PREC_FP64, "mixed": L.CR_PREC_MIXED}
@@ -37,6 +37,21 @@ def egrad_h3(q):
     g = np.zeros_like(q)
     info = C.c_int(0)
     L.check(L.lib().cr_egrad_h3(L.dptr(q), 3, nb, L.dptr(V), L.dptr(g), C.byref(info)), "egrad_h3")
+    return V, g
+
+
+def egrad_ch4h(q):
+    """CH4+H energies and gradients of q (nbeads, 6, 3) bohr, Caracal's atom order."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    if q.ndim == 2:
+        q = q[None]
+    nb = q.shape[0]
+    if q.shape[1:] != (6, 3):
+        raise ValueError("egrad_ch4h expects q of shape (nbeads, 6, 3)")
+    V = np.zeros(nb)
+    g = np.zeros_like(q)
+    info = C.c_int(0)
+    L.check(L.lib().cr_egrad_ch4h(L.dptr(q), 6, nb, L.dptr(V), L.dptr(g), C.byref(info)), "egrad_ch4h")
     return V, g
 
 

@@ -70,3 +70,25 @@ def h3_config(ntraj=64, nbeads=16, nsteps=1000, thermostat="pile", kelvin=300.0,
     return Workload(name=f"h3_bkmp2_P{nbeads}_T{ntraj}", pes="h3", symbols=["H", "H", "H"],
                     q0=h3_collinear(), nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs,
                     nsteps=nsteps, thermostat=thermostat, sigma_bohr=float(angstrom_to_bohr(0.01)))
+
+
+def ch4h_dividing_surface(r_ch_ang=1.09, r_hh_ang=1.5):
+    """CH4 (tetrahedral, r(CH) = r_ch) + H collinear with one C-H bond, r_hh
+    beyond that bond's H (the H...H distance), in Caracal's atom order for
+    ANA_CH4H: H (the attacked methane H), C, H, H, H, H_b (abstracting H)."""
+    s3 = 1.0 / np.sqrt(3.0)
+    v = np.array([[s3, s3, s3], [s3, -s3, -s3], [-s3, s3, -s3], [-s3, -s3, s3]])
+    q = np.zeros((6, 3))
+    q[0] = v[0] * r_ch_ang
+    q[2], q[3], q[4] = v[1] * r_ch_ang, v[2] * r_ch_ang, v[3] * r_ch_ang
+    q[5] = v[0] * (r_ch_ang + r_hh_ang)
+    return angstrom_to_bohr(q)
+
+
+def ch4h_config(ntraj=4096, nbeads=32, nsteps=2000, kelvin=500.0, dt_fs=0.1):
+    """CH4 + H recrossing children: 6 atoms, 32 beads, 4096 NVE children from
+    one dividing-surface geometry, momenta Maxwell at 500 K, 0.1 fs."""
+    return Workload(name=f"ch4h_recross_P{nbeads}_T{ntraj}", pes="ch4h",
+                    symbols=["H", "C", "H", "H", "H", "H"], q0=ch4h_dividing_surface(),
+                    nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs, nsteps=nsteps,
+                    thermostat="none", sigma_bohr=0.0, transrot=False)

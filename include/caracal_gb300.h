@@ -36,7 +36,7 @@ extern "C" {
 
 /* ---- potentials (Caracal keyword PES) ----------------------------------- */
 #define CR_PES_H3 1      /* ANA_H3: BKMP2, src/egrad_h3.f */
-#define CR_PES_CH4H 2    /* ANA_CH4H: src/egrad_ch4h.f (not built yet) */
+#define CR_PES_CH4H 2    /* ANA_CH4H: src/egrad_ch4h.f + src/util_ch4h.f */
 #define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f (not built yet) */
 #define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90, ff_hb.f90 (not built yet) */
 
@@ -52,7 +52,7 @@ extern "C" {
 
 typedef struct cr_config {
   int pes;            /* CR_PES_* */
-  int natoms;         /* must match the PES (H3: 3) */
+  int natoms;         /* must match the PES (H3: 3, CH4H: 6) */
   int nbeads;         /* 1..128 (RPMD_BEADS) */
   int ntraj;          /* independent trajectories in this engine */
   int thermostat;     /* CR_THERMO_* */
@@ -99,6 +99,19 @@ int cr_egrad_h3_noalloc(const double* q, int natoms, int nbeads, double* V, doub
  * (CR_PREC_*); stream may be 0.  npts = number of (natoms=3) geometries. */
 int cr_egrad_h3_device(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
                        void* stream);
+
+/* Replaces `subroutine egrad_ch4h(q,Natoms,Nbeads,V,dVdq,info)` (src/egrad_ch4h.f:74-79;
+ * called from src/gradient.f90:178): natoms = 6 in Caracal's order H, C, H, H, H, H_b
+ * (methane H = atoms 3,4,5,1; the abstracting H is atom 6), bohr -> Hartree. */
+int cr_egrad_ch4h(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+/* Replaces `subroutine initialize_ch4h()` (src/egrad_ch4h.f:33, called from
+ * src/read_pes.f90:551).  The surface's constants are compiled in, so this
+ * only exists for call-site compatibility and always returns CR_OK. */
+int cr_initialize_ch4h(void);
+
+/* Any built PES (CR_PES_*) on device-resident arrays q(3,natoms,npts). */
+int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
+                    void* stream);
 
 /* ---- RPMD engine -----------------------------------------------------------
  * Replaces the stepping loop of `dynamic` (src/dynamic.f90:1569-1579) around
@@ -155,6 +168,8 @@ int cr_host_free(void* ptr);
 #define CR_CALIB_COS 7
 #define CR_CALIB_ACOS 8
 #define CR_CALIB_ERF 9
+#define CR_CALIB_TANH 10
+#define CR_CALIB_COSH 11
 int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s);
 
 #ifdef __cplusplus

@@ -12,7 +12,7 @@ namespace orc {
 
 struct OpTally {
   uint64_t add = 0, mul = 0, div = 0, sqrt = 0, exp = 0, log = 0, pow = 0;
-  uint64_t sin = 0, cos = 0, acos = 0, erf = 0, cmp = 0;
+  uint64_t sin = 0, cos = 0, acos = 0, erf = 0, cmp = 0, tanh = 0, cosh = 0;
   void reset() { *this = OpTally(); }
 };
 
@@ -51,6 +51,8 @@ inline OC sin(OC a) { tally().sin++; return OC(std::sin(a.v)); }
 inline OC cos(OC a) { tally().cos++; return OC(std::cos(a.v)); }
 inline OC acos(OC a) { tally().acos++; return OC(std::acos(a.v)); }
 inline OC erf(OC a) { tally().erf++; return OC(std::erf(a.v)); }
+inline OC tanh(OC a) { tally().tanh++; return OC(std::tanh(a.v)); }
+inline OC cosh(OC a) { tally().cosh++; return OC(std::cosh(a.v)); }
 inline OC fabs(OC a) { return OC(std::fabs(a.v)); }
 inline double val(OC a) { return a.v; }
 inline double val(double a) { return a; }

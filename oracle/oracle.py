@@ -19,10 +19,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-PES_IDS = {"h3": 1}
+PES_IDS = {"h3": 1, "ch4h": 2}
 THERMOSTATS = {"none": 0, "andersen": 1, "pile": 3}
 OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",
-                  "acos", "erf", "cmp")
+                  "acos", "erf", "cmp", "tanh", "cosh")
 
 
 def build(force: bool = False) -> str:
@@ -53,6 +53,7 @@ def lib():
         _lib.orc_egrad_h3.argtypes = [d, C.c_int, C.c_int, d, d, C.POINTER(C.c_int)]
         _lib.orc_h3_pote.argtypes = [d, d, d]
         _lib.orc_cos_transform.argtypes = [d, C.c_int]
+        _lib.orc_egrad.argtypes = [C.c_int, d, C.c_int, C.c_int, d, d]
         _lib.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32,
                                            C.POINTER(C.c_uint32)]
         _lib.orc_normal_pair.argtypes = [C.c_uint32] * 6 + [d]
@@ -109,6 +110,18 @@ def egrad_h3(q):
     g = np.zeros_like(q)
     info = C.c_int(0)
     lib().orc_egrad_h3(_dp(q), 3, nb, _dp(V), _dp(g), C.byref(info))
+    return V, g
+
+
+def egrad(pes, q):
+    """Any PES: q (nbeads, natoms, 3) bohr -> V (nbeads,), dVdq."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    if q.ndim == 2:
+        q = q[None]
+    V = np.zeros(q.shape[0])
+    g = np.zeros_like(q)
+    lib().orc_egrad(PES_IDS[pes] if isinstance(pes, str) else int(pes), _dp(q), q.shape[1],
+                    q.shape[0], _dp(V), _dp(g))
     return V, g
 
 
@@ -169,6 +182,6 @@ def run(cfg: Config, q, p, f, nsteps, istep0=0, traj0=0, nthreads=0):
 
 def pes_opcount(pes, q):
     q = np.ascontiguousarray(q, dtype=np.float64)
-    out = (C.c_uint64 * 12)()
+    out = (C.c_uint64 * 14)()
     lib().orc_pes_opcount(PES_IDS[pes] if isinstance(pes, str) else pes, _dp(q), out)
     return dict(zip(OPCOUNT_FIELDS, list(out)))

@@ -9,6 +9,7 @@
 #endif
 
 #include "opcount.hpp"
+#include "pes_ch4h.hpp"
 #include "pes_h3.hpp"
 #include "philox.hpp"
 #include "rpmd.hpp"
@@ -37,6 +38,7 @@ struct BeadPES {
   void operator()(const double* q, double* V, double* g) const {
     switch (pes) {
       case 1: orc::h3::egrad_bead<double>(q, V, g); break;
+      case 2: orc::ch4h::egrad_bead<double>(q, V, g); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
   }
@@ -62,6 +64,12 @@ void orc_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dV
   if (info) *info = 0;
   for (int k = 0; k < nbeads; ++k)
     orc::h3::egrad_bead<double>(&q[(size_t)k * 3 * natoms], &V[k], &dVdq[(size_t)k * 3 * natoms]);
+}
+
+void orc_egrad(int pes, const double* q, int natoms, int nbeads, double* V, double* dVdq) {
+  BeadPES f{pes, natoms};
+  for (int k = 0; k < nbeads; ++k)
+    f(&q[(size_t)k * 3 * natoms], &V[k], &dVdq[(size_t)k * 3 * natoms]);
 }
 
 void orc_cos_transform(double* x, int P) { orc::caracal_cos_transform(x, P); }
@@ -125,16 +133,21 @@ int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps
   return 0;
 }
 
-void orc_pes_opcount(int pes, const double* q, uint64_t out[12]) {
+void orc_pes_opcount(int pes, const double* q, uint64_t out[14]) {
   orc::tally().reset();
   if (pes == 1) {
     orc::OC qq[9], V, g[9];
     for (int x = 0; x < 9; ++x) qq[x] = orc::OC(q[x]);
     orc::h3::egrad_bead<orc::OC>(qq, &V, g);
+  } else if (pes == 2) {
+    orc::OC qq[18], V, g[18];
+    for (int x = 0; x < 18; ++x) qq[x] = orc::OC(q[x]);
+    orc::ch4h::egrad_bead<orc::OC>(qq, &V, g);
   }
   const orc::OpTally& t = orc::tally();
-  uint64_t v[12] = {t.add, t.mul, t.div, t.sqrt, t.exp, t.log, t.pow, t.sin, t.cos, t.acos, t.erf, t.cmp};
-  for (int i = 0; i < 12; ++i) out[i] = v[i];
+  uint64_t v[14] = {t.add, t.mul, t.div,  t.sqrt, t.exp, t.log,  t.pow,
+                    t.sin, t.cos, t.acos, t.erf,  t.cmp, t.tanh, t.cosh};
+  for (int i = 0; i < 14; ++i) out[i] = v[i];
 }
 
 }  // extern "C"

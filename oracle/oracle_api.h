@@ -12,7 +12,7 @@ extern "C" {
 #endif
 
 typedef struct orc_cfg {
-  int pes;            /* 1 = H3 (BKMP2) */
+  int pes;            /* 1 = H3 (BKMP2), 2 = CH4H */
   int natoms;
   int nbeads;
   int thermostat;     /* 0 none, 1 Andersen, 3 PILE */
@@ -31,6 +31,8 @@ void orc_normal_pair(uint32_t seed, uint32_t traj, uint32_t pair, uint32_t bead,
 void orc_h3_pote(const double R[3], double* V, double dV[3]);
 /* egrad_h3(q, Natoms, Nbeads, V, dVdq, info) of src/egrad_h3.f:29 */
 void orc_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+/* any PES (1 = H3, 2 = CH4H): q(3,natoms,nbeads) -> V(nbeads), dVdq */
+void orc_egrad(int pes, const double* q, int natoms, int nbeads, double* V, double* dVdq);
 void orc_cos_transform(double* x, int P);
 int orc_transrot(const orc_cfg* cf, const double* q, double* p);
 /* bead jitter: q[t] = q0 + sigma * N(0,1) (tag 4, step 0) */
@@ -45,8 +47,8 @@ int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, do
 int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q,
             double* p, double* f, double* epot, int* status, int nthreads);
 /* algorithmic operation tallies (add, mul, div, sqrt, exp, log, pow, sin, cos,
- * acos, erf, cmp) of one PES evaluation of one bead at geometry q. */
-void orc_pes_opcount(int pes, const double* q, uint64_t out[12]);
+ * acos, erf, cmp, tanh, cosh) of one PES evaluation of one bead at geometry q. */
+void orc_pes_opcount(int pes, const double* q, uint64_t out[14]);
 
 #ifdef __cplusplus
 }

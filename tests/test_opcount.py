@@ -1,0 +1,34 @@
+"""CPU: the algorithmic operation table bench.py divides by equals the oracle's
+op-counting instantiation of the reference formulas."""
+import importlib.util
+import os
+
+import numpy as np
+
+from caracal_gb300.workloads import ch4h_dividing_surface, h3_collinear
+from conftest import ROOT
+from oracle import oracle as orc
+
+
+def _bench():
+    spec = importlib.util.spec_from_file_location("bench", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_algo_table_matches_oracle_counts():
+    table = _bench().ALGO_PES_OPS
+    for pes, q in (("h3", h3_collinear()), ("ch4h", ch4h_dividing_surface())):
+        counted = {k: v for k, v in orc.pes_opcount(pes, q).items() if v and k != "cmp"}
+        assert counted == table[pes], (pes, counted)
+
+
+def test_algo_flops_positive_and_monotone_in_beads():
+    b = _bench()
+    w = {k: 20.0 for k in ("div", "sqrt", "exp", "pow", "log", "sin", "cos", "acos", "erf", "tanh",
+                           "cosh")}
+    f8 = b.algo_flops_per_bead_step("h3", 3, 8, "pile", w)
+    f64 = b.algo_flops_per_bead_step("h3", 3, 64, "pile", w)
+    assert 0 < f8 < f64
+    assert np.isfinite(b.algo_flops_per_bead_step("ch4h", 6, 32, "none", w))
