@@ -44,29 +44,66 @@ CALIB_OPS = {"fma": 0, "div": 1, "sqrt": 2, "exp": 3, "log": 4, "pow": 5, "sin":
              "acos": 8, "erf": 9, "tanh": 10, "cosh": 11}
 
 
-def algo_flops_per_bead_step(pes, natoms, nbeads, thermostat, w):
-    """Algorithmic FP work of one bead-step in FMA-pipe flops (an add or a mul
-    is 1, an FMA 2, a division or transcendental 2 x its measured cost in FMAs).
+TRANSCENDENTALS = ("exp", "log", "pow", "sin", "cos", "acos", "erf", "tanh", "cosh")
 
-    PES: the reference formulas (table above).  Propagator: Caracal's four
-    length-P real DFTs per (atom, dim) as FFTs (2.5 P log2 P flops each) plus
-    the per-mode 2x2 update (6 flops).  Kicks: 2 x 2 flops per coordinate.
-    transrot: 30 flops per coordinate.  PILE: two half steps, each two FFT
-    pairs over p and the Gaussian draws (log, sqrt, sin, cos per pair).
+
+def algo_flops_per_bead_step(pes, natoms, nbeads, thermostat, w, transrot=True, recross=False):
+    """Algorithmic FP work of one bead-step, (FP64 part, PES part) in flops.
+
+    Counting: add, mul, div and sqrt are 1 flop each (as counted in the
+    reference formulas by the oracle's op-counting instantiation);
+    transcendentals are weighted by their measured cost on the pipe that runs
+    them (w[k] = 2 x FMA rate / op rate, i.e. the FMA-pipe flops the op
+    occupies).  PES: the table above.  Per-bead FP64 work outside the PES:
+    Caracal's propagator as four length-P real FFTs per coordinate
+    (2.5 P log2 P flops each) plus the 2x2 mode update (6 flops), two half
+    kicks (4 flops per coordinate), transrot (30 flops per coordinate), PILE
+    (per half step two FFT pairs and the Gaussian draws), and for recrossing
+    children the centroid and xi (3 flops per coordinate).
     """
     ops = ALGO_PES_OPS[pes]
-    pes_f = ops["add"] + ops["mul"]
-    for k in ("div", "sqrt", "exp", "pow", "log", "sin", "cos", "acos", "erf", "tanh", "cosh"):
-        pes_f += ops.get(k, 0) * w[k]
+    pes_f = sum(ops.get(k, 0) for k in ("add", "mul", "div", "sqrt"))
+    pes_f += sum(ops.get(k, 0) * w[k] for k in TRANSCENDENTALS)
     nc = 3 * natoms
     lg = math.log2(nbeads) if nbeads > 1 else 0.0
-    prop = nc * (4 * 2.5 * lg + 6)
-    kicks = nc * 4
-    trot = nc * 30
-    pile = 0.0
+    f64 = nc * (4 * 2.5 * lg + 6) + nc * 4
+    if transrot:
+        f64 += nc * 30
     if thermostat == "pile":
-        pile = 2 * (nc * (2 * 2 * 2.5 * lg + 4) + (nc / 2) * (w["log"] + w["sqrt"] + w["sin"] + w["cos"]))
-    return pes_f + prop + kicks + trot + pile
+        f64 += 2 * (nc * (2 * 2 * 2.5 * lg + 4) + (nc / 2) * (w["log"] + 1 + w["sin"] + w["cos"]))
+    if recross:
+        f64 += nc * 3
+    return f64, pes_f
+
+
+def roofline(wl, mixed, ms, K, cal):
+    """Roofline of one step-kernel launch against the measured pipe peaks.
+
+    Plain form: everything on the FP64 pipe.  Mixed form: the PES on the FP32
+    pipe, the rest on FP64; the two are combined into FP64-equivalent flops
+    (FP32 flops x peak64/peak32), so frac is the fraction of the pipe-time
+    lower bound that the launch reaches.
+    """
+    w64, w32 = cal["fp64"]["w"], cal["fp32"]["w"]
+    n = len(wl.mass)
+    rec = wl.extra.get("recross") is not None
+    f64, pes64 = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w64, wl.transrot, rec)
+    _, pes32 = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w32, wl.transrot, rec)
+    p64, p32 = cal["fp64"]["peak_tflops"], cal["fp32"]["peak_tflops"]
+    units = wl.ntraj * wl.nbeads * K
+    if mixed:
+        eq = f64 + pes32 * p64 / p32
+        kern, bound = f"rpmd_run_kernel<{wl.pes}, mixed>", "fp64+fp32 (FP64-equivalent)"
+    else:
+        eq = f64 + pes64
+        kern, bound = f"rpmd_run_kernel<{wl.pes}, fp64>", "fp64"
+    ach = eq * units / (ms * 1e-3) / 1e12
+    return {"kernel": kern, "bound": bound, "achieved": ach, "peak": p64, "unit": "TFLOP/s",
+            "frac": ach / p64, "traffic": None,
+            "peak_source": "measured in this run (FP64/FP32 FMA microbenchmarks, cr_calibrate_op); "
+                           "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
+            "algo_flops_per_bead_step": {"fp64": f64, "pes_fp64": pes64, "pes_fp32": pes32,
+                                         "fp64_equivalent": eq}}
 
 
 class ClockSampler:
@@ -156,48 +193,81 @@ def workload(name):
         return W.h3_config(ntraj=64, nbeads=16, thermostat="pile")
     if name == "h3_large":
         return W.h3_config(ntraj=4096, nbeads=16, thermostat="pile")
-    if name == "ch4h":
-        return W.ch4h_config()
-    if name == "ch4h_small":
-        return W.ch4h_config(ntraj=256)
+    if name in ("ch4h", "ch4h_small"):
+        wl = W.ch4h_config(ntraj=4096 if name == "ch4h" else 256)
+        wl.extra["recross"] = W.ch4h_recross_definition(wl.q0)
+        return wl
     raise SystemExit(f"unknown workload {name}")
 
 
-def make_engine(wl, precision, traj0=0):
+def make_engine(wl, precision, traj0=0, max_steps=0):
+    """Engine for the workload: MD trajectories (positions + Andersen momenta +
+    forces) or, for a recrossing workload, children from one parent geometry."""
     from caracal_gb300 import RPMDEngine
     eng = RPMDEngine(wl.pes, wl.mass, wl.nbeads, wl.ntraj, wl.dt_au, beta=wl.beta,
                      thermostat=wl.thermostat, andersen_step=wl.andersen_step,
                      pile_tau0_au=wl.pile_tau0_au, transrot=wl.transrot, precision=precision,
                      seed=wl.seed, traj0=traj0)
-    eng.init_positions(wl.q0, wl.sigma_bohr)
-    eng.init_momenta()
-    eng.compute_forces()
+    rd = wl.extra.get("recross")
+    if rd is not None:
+        eng.set_recross(max_steps=max(1, max_steps), **rd)
+        eng.init_children(np.repeat(wl.q0[None], wl.nbeads, axis=0))
+    else:
+        eng.init_positions(wl.q0, wl.sigma_bohr)
+        eng.init_momenta()
+        eng.compute_forces()
     return eng
 
 
+class OracleRunner:
+    """The oracle (C++ restatement of Caracal's step) advancing the workload on
+    the host cores, OpenMP over trajectories.  MD workloads keep their state
+    between calls; recrossing workloads restart the children each call."""
+
+    def __init__(self, wl):
+        from oracle import oracle as orc
+        self.orc, self.wl = orc, wl
+        self.cfg = orc.Config(wl.pes, wl.mass, wl.nbeads, wl.dt_au, wl.beta,
+                              thermostat=wl.thermostat, andersen_step=wl.andersen_step,
+                              pile_tau0=wl.pile_tau0_au, transrot=wl.transrot, seed=wl.seed)
+        rd = wl.extra.get("recross")
+        if rd is not None:
+            self.xd = orc.make_xidef([a - 1 for a in rd["reac1"]], [a - 1 for a in rd["reac2"]],
+                                     (rd["bond_form"][0] - 1, rd["bond_form"][1] - 1),
+                                     (rd["bond_break"][0] - 1, rd["bond_break"][1] - 1),
+                                     rd["form_ref"], rd["break_ref"], rd["r_inf"], rd["xi_ideal"])
+            self.qpar = np.repeat(wl.q0[None], wl.nbeads, axis=0)
+        else:
+            self.xd = None
+            self.q = orc.init_positions(self.cfg, wl.ntraj, wl.q0, wl.sigma_bohr)
+            self.p = orc.init_momenta(self.cfg, wl.ntraj)
+            self.f, _ = orc.init_forces(self.cfg, self.q)
+        self.istep = 0
+
+    def advance(self, nsteps, cores):
+        if self.xd is not None:
+            self.orc.recross_children(self.cfg, self.xd, self.wl.ntraj, self.qpar, nsteps, nthreads=cores)
+        else:
+            self.q, self.p, self.f, _, _ = self.orc.run(self.cfg, self.q, self.p, self.f, nsteps,
+                                                         istep0=self.istep, nthreads=cores)
+        self.istep += nsteps
+
+
 def cpu_baseline(wl, target_s=12.0, nthreads=0):
-    """The oracle on the host cores (OpenMP over trajectories), bounded sample."""
-    from oracle import oracle as orc
-    cfg = orc.Config(wl.pes, wl.mass, wl.nbeads, wl.dt_au, wl.beta, thermostat=wl.thermostat,
-                     andersen_step=wl.andersen_step, pile_tau0=wl.pile_tau0_au,
-                     transrot=wl.transrot, seed=wl.seed)
-    T = wl.ntraj
-    q = orc.init_positions(cfg, T, wl.q0, wl.sigma_bohr)
-    p = orc.init_momenta(cfg, T)
-    f, _ = orc.init_forces(cfg, q)
+    """The oracle on the host cores, a bounded sample of the workload."""
+    run = OracleRunner(wl)
     cores = nthreads or os.cpu_count()
     n = 5
     t0 = time.perf_counter()
-    q, p, f, _, _ = orc.run(cfg, q, p, f, n, nthreads=cores)
+    run.advance(n, cores)
     dt = time.perf_counter() - t0
-    steps = max(5, int(n * target_s / max(dt, 1e-6)))
-    steps = min(steps, wl.nsteps)
+    steps = max(5, min(int(n * target_s / max(dt, 1e-6)), wl.nsteps))
     t0 = time.perf_counter()
-    orc.run(cfg, q, p, f, steps, istep0=n, nthreads=cores)
+    run.advance(steps, cores)
     el = time.perf_counter() - t0
-    return {"value": T * wl.nbeads * steps / el, "unit": "bead-steps/s", "cores": cores,
+    return {"value": wl.ntraj * wl.nbeads * steps / el, "unit": "bead-steps/s", "cores": cores,
             "kind": "port",
-            "sample": f"{T} trajectories x {wl.nbeads} beads x {steps} steps of the workload "
+            "sample": f"{wl.ntraj} trajectories x {wl.nbeads} beads x {steps} steps of the workload "
                       f"(C++ restatement of Caracal's step, -O2, OpenMP over trajectories)"}
 
 
@@ -224,24 +294,15 @@ def run_reference(args):
         return
     # W warm-up samples, then K timed samples; each sample = a bounded number of
     # steps of the whole workload on all host threads
-    from oracle import oracle as orc
-    cfg = orc.Config(wl.pes, wl.mass, wl.nbeads, wl.dt_au, wl.beta, thermostat=wl.thermostat,
-                     andersen_step=wl.andersen_step, pile_tau0=wl.pile_tau0_au,
-                     transrot=wl.transrot, seed=wl.seed)
+    run = OracleRunner(wl)
     T = wl.ntraj
-    q = orc.init_positions(cfg, T, wl.q0, wl.sigma_bohr)
-    p = orc.init_momenta(cfg, T)
-    f, _ = orc.init_forces(cfg, q)
     cores = os.cpu_count()
     per = max(1, min(args.ref_steps_per_sample, wl.nsteps))
-    istep = 0
     for _ in range(args.warmup):
-        q, p, f, _, _ = orc.run(cfg, q, p, f, per, istep0=istep, nthreads=cores)
-        istep += per
+        run.advance(per, cores)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        q, p, f, _, _ = orc.run(cfg, q, p, f, per, istep0=istep, nthreads=cores)
-        istep += per
+        run.advance(per, cores)
     el = time.perf_counter() - t0
     v = T * wl.nbeads * per * args.steps / el
     line = {"impl": "reference", "metric": "bead-steps/s", "value": v, "unit": "bead-steps/s",
@@ -271,10 +332,11 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     wl = workload(args.workload)
     K, W = args.steps, args.warmup
+    cap = W + K * 52 + args.e2e_steps + 16  # every step the engines take in this process
     if args.profile:
         # only the engine launches (for ncu): W warm-up steps and K timed steps per form
         for prec in ("fp64", "mixed"):
-            eng = make_engine(wl, prec, traj0=rank * wl.ntraj)
+            eng = make_engine(wl, prec, traj0=rank * wl.ntraj, max_steps=cap)
             eng.run(W)
             eng.run(K)
             print(json.dumps({"profile": wl.name, "precision": prec, "steps": K,
@@ -282,8 +344,8 @@ def run_ours(args):
             eng.close()
         return
     cal = calibrate(L)
-    eng_mx = make_engine(wl, "mixed", traj0=rank * wl.ntraj)
-    eng_64 = make_engine(wl, "fp64", traj0=rank * wl.ntraj)
+    eng_mx = make_engine(wl, "mixed", traj0=rank * wl.ntraj, max_steps=cap)
+    eng_64 = make_engine(wl, "fp64", traj0=rank * wl.ntraj, max_steps=cap)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def timed_run(eng):
@@ -354,11 +416,13 @@ def run_ours(args):
     for ptr, _ in bufs:
         L.lib().cr_host_free(ptr)
 
-    # roofline of the step kernel (mixed form: FP64 propagator/thermostat + FP32 PES)
-    w64 = cal["fp64"]["w"]
-    flops64 = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat, w64)
-    ach64 = flops64 * bead_steps / (ms_64 * 1e-3) / 1e12
-    peak64 = cal["fp64"]["peak_tflops"]
+    # rooflines of the step kernel (headline: the mixed form, whose launch `value` times)
+    roof = roofline(wl, True, ms_mx, K, cal)
+    roof_plain = roofline(wl, False, ms_64, K, cal)
+    kappa = None
+    if wl.extra.get("recross") is not None:
+        num, den, _ = eng_64.kappa(cap)
+        kappa = {"steps": len(num), "kappa_last": float(num[-1] / den) if den else None}
     info = eng_mx.launch_info()
     line = {
         "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": ws, "steps": K,
@@ -375,13 +439,12 @@ def run_ours(args):
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": 3 * nbytes + 8 * wl.ntraj},
         "gpu_launches": 1,
         "launch": info,
-        "roofline": {"kernel": "rpmd_run_kernel<PesH3, fp64> (plain form)", "bound": "fp64",
-                     "achieved": ach64, "peak": peak64, "unit": "TFLOP/s", "frac": ach64 / peak64,
-                     "traffic": None, "peak_source": "measured in this run (FP64 FMA microbenchmark)",
-                     "algo_flops_per_bead_step": flops64},
+        "roofline": roof,
+        "roofline_plain_fp64": roof_plain,
+        "recross": kappa,
         "calibration": {"fp64_peak_tflops": cal["fp64"]["peak_tflops"],
                         "fp32_peak_tflops": cal["fp32"]["peak_tflops"],
-                        "fp64_op_cost_flops": w64, "fp32_op_cost_flops": cal["fp32"]["w"]},
+                        "fp64_op_cost_flops": cal["fp64"]["w"], "fp32_op_cost_flops": cal["fp32"]["w"]},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -404,7 +467,9 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="h3")
+    ap.add_argument("--workload", default="ch4h",
+                    help="ch4h (CH4+H recrossing children, 4096 x 32 beads: the default), "
+                         "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16)")
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-steps-per-sample", type=int, default=20)

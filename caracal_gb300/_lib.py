@@ -48,6 +48,13 @@ class CrConfig(C.Structure):
                 ("mass", c_double_p)]
 
 
+class CrRecross(C.Structure):
+    _fields_ = [("nreac1", C.c_int), ("reac1", C.c_int * 8), ("nreac2", C.c_int),
+                ("reac2", C.c_int * 8), ("bond_form", C.c_int * 2), ("bond_break", C.c_int * 2),
+                ("form_ref", C.c_double), ("break_ref", C.c_double), ("r_inf", C.c_double),
+                ("xi_ideal", C.c_double)]
+
+
 class CaracalError(RuntimeError):
     def __init__(self, code, where):
         self.code = code
@@ -90,6 +97,9 @@ def _sig(lib):
         "cr_host_alloc": ([C.POINTER(C.c_void_p), C.c_ulonglong], C.c_int),
         "cr_host_free": ([v], C.c_int),
         "cr_calibrate_op": ([C.c_int, C.c_int, C.c_int, d], C.c_int),
+        "cr_engine_set_recross": ([eng, C.POINTER(CrRecross), C.c_int], C.c_int),
+        "cr_engine_init_children": ([eng, d], C.c_int),
+        "cr_engine_kappa": ([eng, d, d, d, i], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -99,6 +99,71 @@ __global__ void egrad_kernel(int nbeads_total, const double* q, double* V, doubl
   for (int c = 0; c < NC; ++c) g[(size_t)b * NC + c] = gg[c];
 }
 
+// Recrossing children (src/recross.f90:540-561): q = parent ring polymer,
+// p = Andersen draw keyed by the pair (trajectories 2i and 2i+1 share it),
+// the odd member gets -p.
+template <int NC>
+__global__ void init_children_kernel(int T, int P, uint32_t seed, uint32_t traj0, StepParams prm,
+                                     const double* qpar, double* q, double* p) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= T * P) return;
+  int t = idx / P, k = idx % P;
+  double z[NC];
+  normals_bead<NC>(seed, traj0 + (uint32_t)(t & ~1), (uint32_t)k, 0u, TAG_CHILD_MOMENTA, z);
+  const double sgn = (t & 1) ? -1.0 : 1.0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    q[(size_t)idx * NC + c] = qpar[(size_t)k * NC + c];
+    p[(size_t)idx * NC + c] = sgn * (z[c] * prm.sigma[c / 3]);
+  }
+}
+
+// Flux weight of each child (src/recross.f90:562-590): vs = dxi . sum_k p_k / m / P,
+// fs = sqrt(sum dxi^2 / m / (2 pi beta)), w = vs / fs, wpos = vs > 0.
+template <int N>
+__global__ void child_flux_kernel(int T, int P, StepParams prm, const double* q, const double* p,
+                                  double* w, int* wpos) {
+  constexpr int NC = 3 * N;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  double c[NC], dxi[NC];
+  for (int x = 0; x < NC; ++x) {
+    double acc = 0.0;
+    for (int k = 0; k < P; ++k) acc += q[((size_t)t * P + k) * NC + x];
+    c[x] = acc / P;
+  }
+  xi_bimolec<N>(prm.xi, c, prm.mass, dxi);
+  double vs = 0.0;
+  for (int l = 0; l < 3; ++l)
+    for (int m = 0; m < N; ++m)
+      for (int o = 0; o < P; ++o) vs += dxi[3 * m + l] * p[((size_t)t * P + o) * NC + 3 * m + l] / prm.mass[m];
+  vs = vs / P;
+  double fs = 0.0;
+  for (int l = 0; l < 3; ++l)
+    for (int m = 0; m < N; ++m) fs += dxi[3 * m + l] * dxi[3 * m + l] / prm.mass[m];
+  fs = sqrt(fs / (2.0 * 3.1415926535897932384 * prm.beta));
+  w[t] = vs / fs;
+  wpos[t] = vs > 0.0 ? 1 : 0;
+}
+
+// kappa(t) numerator and denominator, summed over trajectories in index order
+// (deterministic): num[s] = sum_t w[t] [xi_t > 0 after step s+1].
+__global__ void kappa_kernel(int T, int nsteps, int stride, const unsigned char* side, const double* w,
+                             const int* wpos, double* num, double* denom) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsteps) {
+    double acc = 0.0;
+    for (int t = 0; t < T; ++t)
+      if (side[(size_t)t * stride + s]) acc += w[t];
+    num[s] = acc;
+  } else if (s == nsteps) {
+    double acc = 0.0;
+    for (int t = 0; t < T; ++t)
+      if (wpos[t]) acc += w[t];
+    *denom = acc;
+  }
+}
+
 // epot[t] = sum over beads of V[t][k]
 __global__ void sum_beads_kernel(int T, int P, const double* V, double* epot) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -127,6 +192,11 @@ struct cr_engine {
   double *d_q = nullptr, *d_p = nullptr, *d_f = nullptr, *d_epot = nullptr, *d_V = nullptr;
   double *d_prop = nullptr, *d_pile = nullptr, *d_q0 = nullptr;
   int* d_status = nullptr;
+  // recrossing children
+  int xi_on = 0, side_cap = 0, side_step0 = 0;
+  unsigned char* d_side = nullptr;
+  double *d_w = nullptr, *d_kappa = nullptr, *d_qpar = nullptr;
+  int* d_wpos = nullptr;
   cr::StepParams prm{};
 };
 
@@ -521,6 +591,11 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_q0);
   cudaFree(e->d_prop);
   cudaFree(e->d_pile);
+  cudaFree(e->d_side);
+  cudaFree(e->d_w);
+  cudaFree(e->d_kappa);
+  cudaFree(e->d_qpar);
+  cudaFree(e->d_wpos);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -629,6 +704,8 @@ static int engine_finish(cr_engine* e) {
 int cr_engine_run(cr_engine* e, int nsteps) {
   if (!e) return fail(CR_ERR_ARG, "NULL engine");
   if (nsteps < 0) return fail(CR_ERR_ARG, "nsteps must be >= 0");
+  if (e->xi_on && e->istep + nsteps - e->side_step0 > e->side_cap)
+    return fail(CR_ERR_ARG, "run exceeds the recrossing step capacity set by cr_engine_set_recross");
   if (nsteps == 0) return CR_OK;
   int rc = engine_run_async(e, nsteps);
   if (rc) return rc;
@@ -637,6 +714,8 @@ int cr_engine_run(cr_engine* e, int nsteps) {
 
 int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* epot) {
   if (!e || !q || !p || !f) return fail(CR_ERR_ARG, "NULL argument");
+  if (e->xi_on && e->istep + 1 - e->side_step0 > e->side_cap)
+    return fail(CR_ERR_ARG, "step exceeds the recrossing step capacity set by cr_engine_set_recross");
   const size_t bytes = (size_t)e->T * e->P * e->NC * 8;
   CR_CUDA(cudaMemcpyAsync(e->d_q, q, bytes, cudaMemcpyHostToDevice, e->stream));
   CR_CUDA(cudaMemcpyAsync(e->d_p, p, bytes, cudaMemcpyHostToDevice, e->stream));
@@ -681,6 +760,125 @@ int cr_host_alloc(void** ptr, unsigned long long bytes) {
 
 int cr_host_free(void* ptr) {
   if (ptr) CR_CUDA(cudaFreeHost(ptr));
+  return CR_OK;
+}
+
+int cr_engine_set_recross(cr_engine* e, const cr_recross* rc, int max_steps) {
+  if (!e || !rc) return fail(CR_ERR_ARG, "NULL argument");
+  if (max_steps < 1) return fail(CR_ERR_ARG, "max_steps must be >= 1");
+  auto bad_atom = [&](int a) { return a < 1 || a > e->N; };
+  if (rc->nreac1 < 1 || rc->nreac1 > 8 || rc->nreac2 < 1 || rc->nreac2 > 8)
+    return fail(CR_ERR_ARG, "reactants need 1..8 atoms each");
+  cr::XiDev x{};
+  x.nreac1 = rc->nreac1;
+  x.nreac2 = rc->nreac2;
+  x.mreac1 = 0.0;
+  x.mreac2 = 0.0;
+  for (int k = 0; k < rc->nreac1; ++k) {
+    if (bad_atom(rc->reac1[k])) return fail(CR_ERR_ARG, "reactant atom out of range");
+    x.reac1[k] = rc->reac1[k] - 1;
+    x.mreac1 = x.mreac1 + e->mass[(size_t)x.reac1[k]];
+  }
+  for (int k = 0; k < rc->nreac2; ++k) {
+    if (bad_atom(rc->reac2[k])) return fail(CR_ERR_ARG, "reactant atom out of range");
+    x.reac2[k] = rc->reac2[k] - 1;
+    x.mreac2 = x.mreac2 + e->mass[(size_t)x.reac2[k]];
+  }
+  if (bad_atom(rc->bond_form[0]) || bad_atom(rc->bond_form[1]) || bad_atom(rc->bond_break[0]) ||
+      bad_atom(rc->bond_break[1]))
+    return fail(CR_ERR_ARG, "bond atom out of range");
+  x.form0 = rc->bond_form[0] - 1;
+  x.form1 = rc->bond_form[1] - 1;
+  x.brk0 = rc->bond_break[0] - 1;
+  x.brk1 = rc->bond_break[1] - 1;
+  x.form_ref = rc->form_ref;
+  x.break_ref = rc->break_ref;
+  x.r_inf = rc->r_inf;
+  x.xi_ideal = rc->xi_ideal;
+  cudaFree(e->d_side);
+  cudaFree(e->d_w);
+  cudaFree(e->d_kappa);
+  cudaFree(e->d_wpos);
+  e->d_side = nullptr;
+  e->d_w = e->d_kappa = nullptr;
+  e->d_wpos = nullptr;
+  CR_CUDA(cudaMalloc(&e->d_side, (size_t)e->T * max_steps));
+  CR_CUDA(cudaMalloc(&e->d_w, (size_t)e->T * sizeof(double)));
+  CR_CUDA(cudaMalloc(&e->d_wpos, (size_t)e->T * sizeof(int)));
+  CR_CUDA(cudaMalloc(&e->d_kappa, (size_t)(max_steps + 1) * sizeof(double)));
+  CR_CUDA(cudaMemsetAsync(e->d_side, 0, (size_t)e->T * max_steps, e->stream));
+  CR_CUDA(cudaMemsetAsync(e->d_w, 0, (size_t)e->T * sizeof(double), e->stream));
+  CR_CUDA(cudaMemsetAsync(e->d_wpos, 0, (size_t)e->T * sizeof(int), e->stream));
+  e->side_cap = max_steps;
+  e->side_step0 = e->istep;
+  e->xi_on = 1;
+  e->prm.xi = x;
+  e->prm.xi_on = 1;
+  e->prm.side = e->d_side;
+  e->prm.side_stride = max_steps;
+  e->prm.side_step0 = e->istep;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_init_children(cr_engine* e, const double* q_parent) {
+  if (!e || !q_parent) return fail(CR_ERR_ARG, "NULL argument");
+  if (!e->xi_on) return fail(CR_ERR_ARG, "call cr_engine_set_recross first");
+  if (!(e->cfg.beta > 0.0 && std::isfinite(e->cfg.beta))) return fail(CR_ERR_ARG, "children need a finite beta");
+  const size_t bytes = (size_t)e->NC * e->P * sizeof(double);
+  if (!e->d_qpar) CR_CUDA(cudaMalloc(&e->d_qpar, bytes));
+  CR_CUDA(cudaMemcpyAsync(e->d_qpar, q_parent, bytes, cudaMemcpyHostToDevice, e->stream));
+  const int nb = e->T * e->P;
+  switch (e->cfg.pes) {
+    case CR_PES_H3:
+      cr::init_children_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
+      break;
+    case CR_PES_CH4H:
+      cr::init_children_kernel<18><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
+      break;
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+  CR_CUDA(cudaGetLastError());
+  int rc = dispatch_forces(e);
+  if (rc) return rc;
+  const int tb = 128, gb = (e->T + tb - 1) / tb;
+  switch (e->cfg.pes) {
+    case CR_PES_H3:
+      cr::child_flux_kernel<3><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
+      break;
+    case CR_PES_CH4H:
+      cr::child_flux_kernel<6><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
+      break;
+    default: break;
+  }
+  CR_CUDA(cudaGetLastError());
+  CR_CUDA(cudaMemsetAsync(e->d_side, 0, (size_t)e->T * e->side_cap, e->stream));
+  CR_CUDA(cudaMemsetAsync(e->d_status, 0, (size_t)e->T * sizeof(int), e->stream));
+  e->side_step0 = e->istep;
+  e->prm.side_step0 = e->istep;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_kappa(cr_engine* e, double* num, double* denom, double* weights, int* nsteps) {
+  if (!e || !num || !denom || !nsteps) return fail(CR_ERR_ARG, "NULL argument");
+  if (!e->xi_on) return fail(CR_ERR_ARG, "no recrossing run in this engine");
+  const int ns = e->istep - e->side_step0;
+  *nsteps = ns;
+  if (ns <= 0) {
+    *denom = 0.0;
+    return CR_OK;
+  }
+  cr::kappa_kernel<<<(ns + 1 + 127) / 128, 128, 0, e->stream>>>(e->T, ns, e->side_cap, e->d_side, e->d_w,
+                                                                  e->d_wpos, e->d_kappa, e->d_kappa + ns);
+  CR_CUDA(cudaGetLastError());
+  CR_CUDA(cudaMemcpyAsync(num, e->d_kappa, (size_t)ns * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  CR_CUDA(cudaMemcpyAsync(denom, e->d_kappa + ns, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  if (weights)
+    CR_CUDA(cudaMemcpyAsync(weights, e->d_w, (size_t)e->T * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  CR_CUDA(cudaStreamSynchronize(e->stream));
   return CR_OK;
 }
 

@@ -31,6 +31,52 @@ namespace cr {
 constexpr int kMaxBeads = 128;
 constexpr int kMaxAtoms = 7;
 
+// BIMOLEC reaction coordinate of Caracal's recrossing (calc_xi mode 2,
+// src/calc_xi.f90:63-279): xi = xi_ideal*s1 + (1-xi_ideal)*s0 with
+// s1 = (r_break - break_ref) - (r_form - form_ref), s0 = R_inf - |COM2 - COM1|.
+struct XiDev {
+  int nreac1, reac1[8], nreac2, reac2[8];  // 0-based atoms
+  int form0, form1, brk0, brk1;
+  double form_ref, break_ref, r_inf, xi_ideal;
+  double mreac1, mreac2;
+};
+
+template <int N>
+__host__ __device__ inline double xi_bimolec(const XiDev& x, const double* c, const double* mass,
+                                             double* dxi) {
+  double Rf[3], Rb[3];
+  for (int d = 0; d < 3; ++d) {
+    Rf[d] = c[3 * x.form0 + d] - c[3 * x.form1 + d];
+    Rb[d] = c[3 * x.brk0 + d] - c[3 * x.brk1 + d];
+  }
+  const double rf = sqrt(Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2]);
+  const double rb = sqrt(Rb[0] * Rb[0] + Rb[1] * Rb[1] + Rb[2] * Rb[2]);
+  const double s1 = (rb - x.break_ref) - (rf - x.form_ref);
+  double c1[3] = {0, 0, 0}, c2[3] = {0, 0, 0};
+  for (int k = 0; k < x.nreac1; ++k)
+    for (int d = 0; d < 3; ++d) c1[d] += mass[x.reac1[k]] * c[3 * x.reac1[k] + d] / x.mreac1;
+  for (int k = 0; k < x.nreac2; ++k)
+    for (int d = 0; d < 3; ++d) c2[d] += mass[x.reac2[k]] * c[3 * x.reac2[k] + d] / x.mreac2;
+  const double Red[3] = {c2[0] - c1[0], c2[1] - c1[1], c2[2] - c1[2]};
+  const double reds = sqrt(Red[0] * Red[0] + Red[1] * Red[1] + Red[2] * Red[2]);
+  const double s0 = x.r_inf - reds;
+  if (dxi) {
+    const double a = x.xi_ideal, b = 1.0 - x.xi_ideal;
+    for (int i = 0; i < 3 * N; ++i) dxi[i] = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      dxi[3 * x.form0 + d] -= a * Rf[d] / rf;
+      dxi[3 * x.form1 + d] += a * Rf[d] / rf;
+      dxi[3 * x.brk0 + d] += a * Rb[d] / rb;
+      dxi[3 * x.brk1 + d] -= a * Rb[d] / rb;
+    }
+    for (int k = 0; k < x.nreac1; ++k)
+      for (int d = 0; d < 3; ++d) dxi[3 * x.reac1[k] + d] += b * Red[d] / reds * mass[x.reac1[k]] / x.mreac1;
+    for (int k = 0; k < x.nreac2; ++k)
+      for (int d = 0; d < 3; ++d) dxi[3 * x.reac2[k] + d] -= b * Red[d] / reds * mass[x.reac2[k]] / x.mreac2;
+  }
+  return x.xi_ideal * s1 + (1.0 - x.xi_ideal) * s0;
+}
+
 struct StepParams {
   int T;           // trajectories in the launch
   int P;           // beads
@@ -55,6 +101,13 @@ struct StepParams {
   double* f;
   double* epot;        // [T]
   int* status;         // [T]
+  // recrossing children: after each step, side[t*side_stride + istep-side_step0-1]
+  // records xi(centroid) > 0 (src/recross.f90:596-602)
+  int xi_on;
+  int side_step0;
+  int side_stride;
+  unsigned char* side;
+  XiDev xi;
 };
 
 // Sum over the G lanes of a group (deterministic tree).  red: per-group
@@ -155,10 +208,10 @@ __device__ inline bool invert3(double (&a)[3][3]) {
 // Dynamic shared memory layout (doubles):
 //   [0, 3H^2)                      propagator blocks K1, K2, K3
 //   [3H^2, 3H^2 + 2P)              PILE circulant vectors a, b
-//   then per group: xs[2][NC][G], sym[2][NC][H], red[(G/32) * 16]
+//   then per group: xs[2][NC][G], sym[2][NC][H], red[(G/32) * 32]
 __host__ __device__ inline size_t step_smem_doubles(int P, int G, int NC, int groups) {
   const int H = P / 2 + 1;
-  size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 16;
+  size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 32;
   return (size_t)3 * H * H + 2 * (size_t)P + per_group * groups;
 }
 
@@ -176,11 +229,11 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 
   double* s_prop = smem;
   double* s_pile = s_prop + 3 * H * H;
-  const size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 16;
+  const size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 32;
   double* s_grp = s_pile + 2 * P + per_group * grp;
   double* xs = s_grp;                      // [2][NC][G]
   double* sym = xs + 2 * NC * G;           // [2][NC][H]
-  double* red = sym + 2 * NC * H;          // [(G/32)][16]
+  double* red = sym + 2 * NC * H;          // [(G/32)][32]
 
   for (int x = threadIdx.x; x < 3 * H * H; x += blockDim.x) s_prop[x] = prm.prop[x];
   if (prm.thermostat == CR_THERMO_PILE)
@@ -301,6 +354,21 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 #pragma unroll
     for (int c = 0; c < NC; ++c) f[c] = active ? g[c] : 0.0;
     if (!active) vbead = 0.0;
+
+    // reaction coordinate of the centroid (umbrella mode 1 of a child step,
+    // src/verlet.f90:1049-1050 -> src/umbrella.f90:115-117)
+    if (prm.xi_on) {
+      double cq[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) cq[c] = active ? q[c] : 0.0;
+      group_sum<NC>(cq, G, red, j);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) cq[c] = cq[c] / P;
+      if (active && j == 0) {
+        const double xi = xi_bimolec<N>(prm.xi, cq, prm.mass, nullptr);
+        prm.side[(size_t)t * prm.side_stride + (istep - prm.side_step0 - 1)] = xi > 0.0 ? 1 : 0;
+      }
+    }
 
     // 1/2 kick (src/verlet.f90:1060-1062)
 #pragma unroll

@@ -143,6 +143,33 @@ class RPMDEngine:
         ep = L.dptr(epot) if epot is not None else None
         L.check(L.lib().cr_engine_step_host(self._h, L.dptr(q), L.dptr(p), L.dptr(f), ep), "step_host")
 
+    def set_recross(self, reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf,
+                    xi_ideal=1.0, max_steps=1):
+        """BIMOLEC recrossing bookkeeping; atom indices 1-based as in Caracal's MECHA block."""
+        rc = L.CrRecross()
+        rc.nreac1, rc.nreac2 = len(reac1), len(reac2)
+        for i, a in enumerate(reac1):
+            rc.reac1[i] = a
+        for i, a in enumerate(reac2):
+            rc.reac2[i] = a
+        rc.bond_form[0], rc.bond_form[1] = bond_form
+        rc.bond_break[0], rc.bond_break[1] = bond_break
+        rc.form_ref, rc.break_ref, rc.r_inf, rc.xi_ideal = form_ref, break_ref, r_inf, xi_ideal
+        L.check(L.lib().cr_engine_set_recross(self._h, C.byref(rc), int(max_steps)), "set_recross")
+
+    def init_children(self, q_parent):
+        qp = np.ascontiguousarray(q_parent, dtype=np.float64).reshape(self.nbeads, self.natoms, 3)
+        L.check(L.lib().cr_engine_init_children(self._h, L.dptr(qp)), "init_children")
+
+    def kappa(self, max_steps):
+        num = np.zeros(max_steps)
+        den = np.zeros(1)
+        w = np.zeros(self.ntraj)
+        ns = C.c_int(0)
+        L.check(L.lib().cr_engine_kappa(self._h, L.dptr(num), L.dptr(den), L.dptr(w), C.byref(ns)),
+                "kappa")
+        return num[:ns.value], float(den[0]), w
+
     def last_kernel_ms(self):
         ms = C.c_float()
         L.check(L.lib().cr_engine_last_kernel_ms(self._h, C.byref(ms)), "last_kernel_ms")

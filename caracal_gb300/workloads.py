@@ -92,3 +92,14 @@ def ch4h_config(ntraj=4096, nbeads=32, nsteps=2000, kelvin=500.0, dt_fs=0.1):
                     symbols=["H", "C", "H", "H", "H", "H"], q0=ch4h_dividing_surface(),
                     nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs, nsteps=nsteps,
                     thermostat="none", sigma_bohr=0.0, transrot=False)
+
+
+def ch4h_recross_definition(q0):
+    """BIMOLEC mechanism of CH4 + H -> CH3 + H2 for Caracal's MECHA block
+    (1-based atoms): reactant1 = CH4 (1-5), reactant2 = H_b (6), bond_form 1-6,
+    bond_break 2-1; reference bond lengths from the dividing-surface geometry,
+    DIST_INF 16 bohr, xi at the dividing surface 1.0."""
+    q0 = np.asarray(q0)
+    return dict(reac1=[1, 2, 3, 4, 5], reac2=[6], bond_form=(1, 6), bond_break=(2, 1),
+                form_ref=float(np.linalg.norm(q0[0] - q0[5])),
+                break_ref=float(np.linalg.norm(q0[1] - q0[0])), r_inf=16.0, xi_ideal=1.0)

@@ -144,6 +144,34 @@ int cr_engine_run(cr_engine* e, int nsteps);
  * q_i, p_i, derivs would use it: copy in, one step, copy out (epot may be NULL). */
 int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* epot);
 
+/* ---- recrossing children (calc_rate part 4) --------------------------------
+ * Replaces the child loop of `recross` (src/recross.f90:540-614): children in
+ * pairs with momenta +p and -p (Andersen draw at the engine's temperature),
+ * started from one parent ring polymer, run NVE without thermostat or
+ * transrot (verlet with constrain = 2); after every step the BIMOLEC reaction
+ * coordinate of the centroid (calc_xi mode 2, src/calc_xi.f90) decides the
+ * side.  kappa(t) = num[t] / denom (src/recross.f90:637). */
+typedef struct cr_recross {
+  int nreac1, reac1[8];        /* MECHA reactant1 atoms, 1-based */
+  int nreac2, reac2[8];        /* MECHA reactant2 atoms, 1-based */
+  int bond_form[2];            /* MECHA bond_form atoms, 1-based */
+  int bond_break[2];           /* MECHA bond_break atoms, 1-based */
+  double form_ref, break_ref;  /* bond lengths at the TS, bohr (src/bonds_ref.f90) */
+  double r_inf;                /* DIST_INF, bohr */
+  double xi_ideal;             /* xi of the dividing surface (PMF maximum) */
+} cr_recross;
+/* Enables the flux bookkeeping for runs of at most max_steps steps in total
+ * after the next cr_engine_init_children.  The engine must be created with
+ * thermostat CR_THERMO_NONE and transrot 0 to reproduce child steps. */
+int cr_engine_set_recross(cr_engine* e, const cr_recross* rc, int max_steps);
+/* q_parent(3,natoms,nbeads): every child starts there; pairs (2i, 2i+1) get
+ * +p/-p from the Gaussian stream keyed by traj0 + 2i; forces and the flux
+ * weights vs/fs are computed. */
+int cr_engine_init_children(cr_engine* e, const double* q_parent);
+/* num[nsteps] and denom summed over the engine's children (deterministic
+ * order); weights (may be NULL) gets vs/fs per child. */
+int cr_engine_kappa(cr_engine* e, double* num, double* denom, double* weights, int* nsteps);
+
 /* Device time of the last cr_engine_run / step kernel (CUDA events on the
  * engine's stream), launches issued by it, and the launch shape chosen. */
 int cr_engine_last_kernel_ms(const cr_engine* e, float* ms);

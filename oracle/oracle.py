@@ -41,6 +41,27 @@ class Cfg(C.Structure):
                 ("pile_tau0", C.c_double), ("mass", C.POINTER(C.c_double))]
 
 
+class XiDef(C.Structure):
+    _fields_ = [("nreac1", C.c_int), ("reac1", C.c_int * 8), ("nreac2", C.c_int),
+                ("reac2", C.c_int * 8), ("form", C.c_int * 2), ("brk", C.c_int * 2),
+                ("form_ref", C.c_double), ("break_ref", C.c_double), ("r_inf", C.c_double),
+                ("xi_ideal", C.c_double)]
+
+
+def make_xidef(reac1, reac2, form, brk, form_ref, break_ref, r_inf, xi_ideal):
+    """BIMOLEC definition from 0-based atom lists."""
+    x = XiDef()
+    x.nreac1, x.nreac2 = len(reac1), len(reac2)
+    for i, a in enumerate(reac1):
+        x.reac1[i] = a
+    for i, a in enumerate(reac2):
+        x.reac2[i] = a
+    x.form[0], x.form[1] = form
+    x.brk[0], x.brk[1] = brk
+    x.form_ref, x.break_ref, x.r_inf, x.xi_ideal = form_ref, break_ref, r_inf, xi_ideal
+    return x
+
+
 _lib = None
 
 
@@ -63,6 +84,10 @@ def lib():
         _lib.orc_init_forces.argtypes = [C.POINTER(Cfg), C.c_int, d, d, d]
         _lib.orc_run.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_int, C.c_int, d, d, d, d,
                                  C.POINTER(C.c_int), C.c_int]
+        _lib.orc_calc_xi.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d]
+        _lib.orc_calc_xi.restype = C.c_double
+        _lib.orc_recross_children.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, d,
+                                              C.c_int, d, d, d, d, d, C.c_int]
         _lib.orc_pes_opcount.argtypes = [C.c_int, d, C.POINTER(C.c_uint64)]
     return _lib
 
@@ -185,3 +210,25 @@ def pes_opcount(pes, q):
     out = (C.c_uint64 * 14)()
     lib().orc_pes_opcount(PES_IDS[pes] if isinstance(pes, str) else pes, _dp(q), out)
     return dict(zip(OPCOUNT_FIELDS, list(out)))
+
+
+def calc_xi(xd, coords, mass):
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    m = np.ascontiguousarray(mass, dtype=np.float64)
+    dxi = np.zeros_like(c)
+    xi = lib().orc_calc_xi(C.byref(xd), c.shape[0], _dp(c), _dp(m), _dp(dxi))
+    return xi, dxi
+
+
+def recross_children(cfg: Config, xd, ntraj, q_parent, nsteps, traj0=0, nthreads=0, states=False):
+    """Returns (num (nsteps,), denom, w (ntraj,)[, q, p])."""
+    qp = np.ascontiguousarray(q_parent, dtype=np.float64)
+    num = np.zeros(nsteps)
+    den = np.zeros(1)
+    w = np.zeros(ntraj)
+    q = np.zeros(cfg.shape(ntraj)) if states else None
+    p = np.zeros(cfg.shape(ntraj)) if states else None
+    lib().orc_recross_children(C.byref(cfg.c), C.byref(xd), ntraj, traj0, _dp(qp), nsteps, _dp(num),
+                               _dp(den), _dp(w), _dp(q) if states else None,
+                               _dp(p) if states else None, nthreads)
+    return (num, den[0], w, q, p) if states else (num, den[0], w)

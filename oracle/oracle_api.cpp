@@ -12,6 +12,7 @@
 #include "pes_ch4h.hpp"
 #include "pes_h3.hpp"
 #include "philox.hpp"
+#include "recross.hpp"
 #include "rpmd.hpp"
 
 namespace {
@@ -130,6 +131,69 @@ int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps
     if (epot) epot[t] = e;
     if (status) status[t] |= st;
   }
+  return 0;
+}
+
+static orc::XiDef to_xi(const orc_xidef* x) {
+  orc::XiDef d;
+  d.nreac1 = x->nreac1;
+  d.nreac2 = x->nreac2;
+  for (int i = 0; i < 8; ++i) {
+    d.reac1[i] = x->reac1[i];
+    d.reac2[i] = x->reac2[i];
+  }
+  d.form[0] = x->form[0];
+  d.form[1] = x->form[1];
+  d.brk[0] = x->brk[0];
+  d.brk[1] = x->brk[1];
+  d.form_ref = x->form_ref;
+  d.break_ref = x->break_ref;
+  d.r_inf = x->r_inf;
+  d.xi_ideal = x->xi_ideal;
+  return d;
+}
+
+double orc_calc_xi(const orc_xidef* xd, int natoms, const double* coords, const double* mass,
+                   double* dxi) {
+  return orc::calc_xi_mode2(to_xi(xd), natoms, coords, mass, dxi);
+}
+
+int orc_recross_children(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t traj0,
+                         const double* q_parent, int nsteps, double* num, double* denom,
+                         double* w_out, double* q_out, double* p_out, int nthreads) {
+  orc::StepConfig s = to_step(cf);
+  orc::XiDef x = to_xi(xd);
+  BeadPES pes{cf->pes, cf->natoms};
+  const size_t per = (size_t)3 * cf->natoms * cf->nbeads;
+  std::vector<double> w(ntraj);
+  std::vector<unsigned char> side((size_t)ntraj * nsteps), pos(ntraj);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int t = 0; t < ntraj; ++t) {
+    std::vector<double> q(per), p(per), f(per);
+    bool vp = false;
+    w[t] = orc::recross_child(s, x, traj0 + (uint32_t)(t & ~1), (t & 1) != 0, q_parent, nsteps, q.data(),
+                              p.data(), f.data(), &side[(size_t)t * nsteps], &vp, pes);
+    pos[t] = vp ? 1 : 0;
+    if (q_out)
+      for (size_t i = 0; i < per; ++i) q_out[t * per + i] = q[i];
+    if (p_out)
+      for (size_t i = 0; i < per; ++i) p_out[t * per + i] = p[i];
+  }
+  double den = 0.0;
+  for (int t = 0; t < ntraj; ++t)
+    if (pos[t]) den = den + w[t];
+  if (denom) *denom = den;
+  for (int st = 0; st < nsteps; ++st) {
+    double acc = 0.0;
+    for (int t = 0; t < ntraj; ++t)
+      if (side[(size_t)t * nsteps + st]) acc = acc + w[t];
+    num[st] = acc;
+  }
+  if (w_out)
+    for (int t = 0; t < ntraj; ++t) w_out[t] = w[t];
   return 0;
 }
 

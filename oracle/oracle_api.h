@@ -46,6 +46,25 @@ int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, do
  * status[t] ORs the per-step status bits; nthreads <= 0 uses all cores. */
 int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q,
             double* p, double* f, double* epot, int* status, int nthreads);
+/* BIMOLEC reaction coordinate of Caracal's recrossing (calc_xi mode 2). */
+typedef struct orc_xidef {
+  int nreac1, reac1[8];   /* 0-based atom indices of reactant 1 */
+  int nreac2, reac2[8];   /* 0-based atom indices of reactant 2 */
+  int form[2], brk[2];    /* 0-based atoms of the forming and the breaking bond */
+  double form_ref, break_ref, r_inf, xi_ideal;
+} orc_xidef;
+
+double orc_calc_xi(const orc_xidef* xd, int natoms, const double* coords, const double* mass,
+                   double* dxi);
+/* ntraj recrossing children (pairs 2i, 2i+1 share momenta with opposite
+ * signs, keyed by traj0 + 2i) from the parent ring polymer q_parent(3,N,P):
+ * num[s] = sum over children of w * [xi > 0 after step s+1], denom = sum of
+ * w over children with vs > 0, w = vs/fs; q_out/p_out get the final states
+ * (may be NULL). */
+int orc_recross_children(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t traj0,
+                         const double* q_parent, int nsteps, double* num, double* denom,
+                         double* w_out, double* q_out, double* p_out, int nthreads);
+
 /* algorithmic operation tallies (add, mul, div, sqrt, exp, log, pow, sin, cos,
  * acos, erf, cmp, tanh, cosh) of one PES evaluation of one bead at geometry q. */
 void orc_pes_opcount(int pes, const double* q, uint64_t out[14]);

@@ -28,7 +28,7 @@ def test_algo_flops_positive_and_monotone_in_beads():
     b = _bench()
     w = {k: 20.0 for k in ("div", "sqrt", "exp", "pow", "log", "sin", "cos", "acos", "erf", "tanh",
                            "cosh")}
-    f8 = b.algo_flops_per_bead_step("h3", 3, 8, "pile", w)
-    f64 = b.algo_flops_per_bead_step("h3", 3, 64, "pile", w)
+    f8 = sum(b.algo_flops_per_bead_step("h3", 3, 8, "pile", w))
+    f64 = sum(b.algo_flops_per_bead_step("h3", 3, 64, "pile", w))
     assert 0 < f8 < f64
-    assert np.isfinite(b.algo_flops_per_bead_step("ch4h", 6, 32, "none", w))
+    assert np.isfinite(sum(b.algo_flops_per_bead_step("ch4h", 6, 32, "none", w, False, True)))
