@@ -1,0 +1,312 @@
+"""QMDFF force-field data on the host: `.qmdff` files and the synthetic alkane.
+
+* ``read_qmdff`` / ``write_qmdff`` follow Caracal's file format: the reader of
+  src/rdsolvff.f90:34-202 (header ``n q d``, method line, ``at x y z q mol``
+  per atom, ``nbond nangl ntors nhb nnci``, the term lines, H-bond triples six
+  per line, NCI triples eight per line; torsion phases are stored over pi) and
+  the writer of src/main_gen.f90:825-847.
+* ``ElementTables`` are the per-element-pair non-bonded tables Caracal's
+  ``prepare`` hands to ``ff_nonb`` (src/setnonb.f90): sr42 = 3 s8 r2r4_i r2r4_j,
+  r094 = a1 sqrt(3 r2r4_i r2r4_j) + a2, zab = vz_i vz_j, r0ab = 16.5/R0AB^1.5,
+  with Caracal's REAL(4) literals (a1 = 0.45, s8 = 2.7, the valel factors).
+  The engine takes these tables (and the C6 pair matrix) from its caller, as
+  ff_nonb does.  For the synthetic alkane the C6 pair values and the D3 pair
+  radii R0AB are D3-like constants chosen here (Caracal's D3 reference data is
+  not reproduced), so that workload is "QMDFF-shaped", not a Caracal fit.
+* ``alkane`` builds the synthetic C_nH_2n+2 QMDFF of the benchmark: zig-zag
+  chain, r(CC) = 1.53 A, r(CH) = 1.09 A, tetrahedral angles, bond / angle /
+  torsion force constants drawn in +-20 % of 0.3 Eh/bohr^2, 0.1 Eh/rad^2,
+  0.002 Eh from the seed, charges +-0.1 e with exact neutrality, NCI = all
+  pairs three or more bonds apart (categories 3, 4, >=5 -> 5).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .units import BOHR_ANGSTROM
+
+F32 = lambda x: float(np.float32(x))  # noqa: E731  (REAL(4) literal widened to REAL(8))
+
+# published D3 values Caracal keeps in src/setnonb.f90 (r2r4) for H and C
+R2R4 = {1: F32(2.00734898), 6: F32(3.10492822)}
+# covalent radii (Mantina et al.), Angstrom, src/prepare.f90
+RAD_ANG = {1: 0.32, 6: 0.75}
+# synthetic D3-like inputs (not Caracal's D3 tables)
+C6_PAIR = {(1, 1): 3.0898, (1, 6): 7.5916, (6, 6): 18.1368}
+R0AB_PAIR_ANG = {(1, 1): 2.1823, (1, 6): 2.5984, (6, 6): 2.9146}
+
+
+def valence_charge(z):
+    """valel (src/valel.f90) for H and C: Z times the REAL(4) fit factor."""
+    if z <= 2:
+        return float(z) * F32(2.35)
+    if z <= 10:
+        return float(z - 2) * F32(0.95)
+    raise ValueError("only H and C are tabulated")
+
+
+@dataclass
+class ElementTables:
+    r0ab: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))   # alpha of the repulsion
+    zab: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))
+    r094: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))
+    sr42: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))
+
+    @classmethod
+    def d3_like(cls, elements=(1, 6)):
+        t = cls()
+        a1, s8, a2 = F32(0.45), F32(2.7), 4.0
+        for zi in elements:
+            for zj in elements:
+                t.sr42[zi, zj] = 3.0 * s8 * R2R4[zi] * R2R4[zj]
+                t.r094[zi, zj] = a1 * np.sqrt(3.0 * R2R4[zi] * R2R4[zj]) + a2
+                t.zab[zi, zj] = valence_charge(zi) * valence_charge(zj)
+                key = (min(zi, zj), max(zi, zj))
+                r0 = R0AB_PAIR_ANG[key] / BOHR_ANGSTROM
+                t.r0ab[zi, zj] = F32(16.5) / r0 ** 1.5
+        return t
+
+
+@dataclass
+class QMDFF:
+    at: np.ndarray            # (n,) element numbers
+    xyz: np.ndarray           # (n, 3) reference geometry, bohr
+    q: np.ndarray             # (n,) charges
+    bond: np.ndarray          # (nbond, 2) 1-based
+    vbond: np.ndarray         # (nbond, 3): r0 (bohr), k, a
+    angl: np.ndarray          # (nangl, 3) 1-based, centre first
+    vangl: np.ndarray         # (nangl, 2): theta0 (rad), k
+    tors: np.ndarray          # (ntors, 6): i j k l nt type (1-based atoms)
+    vtors: np.ndarray         # (ntors, 14): phi0, V, (rn, phase*pi, Vn) x 4
+    nci: np.ndarray           # (nnci, 3): i j category (1-based atoms)
+    c6: np.ndarray            # (n, n) pair C6 (Caracal's c6xy)
+    e_zero: float = 0.0
+    method: str = "synthetic"
+
+    @property
+    def n(self):
+        return len(self.at)
+
+    def rad_bohr(self):
+        return np.array([RAD_ANG[int(z)] / BOHR_ANGSTROM for z in self.at])
+
+
+def _fmt(x):
+    return f"{x:18.12f}"
+
+
+def write_qmdff(ff: QMDFF, path):
+    """Caracal's .qmdff text format (src/main_gen.f90:825-847)."""
+    with open(path, "w") as fh:
+        fh.write(f"{ff.n:4d}{1.0:10.4f}{0.0:10.4f}\n{ff.method}\n")
+        for i in range(ff.n):
+            fh.write(f"{int(ff.at[i]):5d}" + "".join(_fmt(v) for v in ff.xyz[i]) + _fmt(ff.q[i]) + f"{0:5d}\n")
+        fh.write("".join(f"{v:8d}" for v in (len(ff.bond), len(ff.angl), len(ff.tors), 0, len(ff.nci), 0)) + "\n")
+        for b, v in zip(ff.bond, ff.vbond):
+            fh.write(f"{b[0]:5d}{b[1]:5d}" + "".join(_fmt(x) for x in v) + "\n")
+        for a, v in zip(ff.angl, ff.vangl):
+            fh.write(f"{a[0]:5d}{a[1]:5d}{a[2]:5d}" + "".join(_fmt(x) for x in v) + "\n")
+        for t, v in zip(ff.tors, ff.vtors):
+            s = "".join(f"{x:4d}" for x in t[:4]) + "".join(f"{x:2d}" for x in t[4:6])
+            s += f"{v[0]:16.12f}{v[1]:16.12f}"
+            for j in range(int(t[4])):
+                s += f"{v[2 + 3 * j]:4.1f}{v[3 + 3 * j] / np.pi:4.1f}{v[4 + 3 * j]:16.8E}"
+            fh.write(s + "\n")
+        trip = [f"{a:4d}{b:4d}{c:4d}  " for a, b, c in ff.nci]
+        for k in range(0, len(trip), 8):
+            fh.write("".join(trip[k:k + 8]) + "\n")
+
+
+def _records(path):
+    with open(path) as fh:
+        return fh.read().splitlines()
+
+
+def read_qmdff(path, c6=None):
+    """Read a .qmdff file with the record semantics of Caracal's list-directed
+    reads (each read starts on a new line and may continue over lines)."""
+    lines = _records(path)
+    pos = [0]
+
+    def read(nvals, conv=float):
+        vals = []
+        while len(vals) < nvals:
+            toks = lines[pos[0]].replace("D", "E").replace("d", "e").split()
+            pos[0] += 1
+            vals.extend(toks)
+        return [conv(v) for v in vals[:nvals]]
+
+    head = lines[0].split()
+    n = int(float(head[0]))
+    pos[0] = 2
+    at, xyz, q = np.zeros(n, int), np.zeros((n, 3)), np.zeros(n)
+    for i in range(n):
+        v = read(6)
+        at[i], xyz[i], q[i] = int(v[0]), v[1:4], v[4]
+    nbond, nangl, ntors, nhb, nnci = [int(x) for x in read(5)]
+    if nhb:
+        raise NotImplementedError("H/halogen-bond terms (ff_hb) are not supported yet")
+    bond, vbond = np.zeros((nbond, 2), int), np.zeros((nbond, 3))
+    for m in range(nbond):
+        v = read(5)
+        bond[m], vbond[m] = [int(v[0]), int(v[1])], v[2:5]
+    angl, vangl = np.zeros((nangl, 3), int), np.zeros((nangl, 2))
+    for m in range(nangl):
+        v = read(5)
+        angl[m], vangl[m] = [int(x) for x in v[:3]], v[3:5]
+    tors, vtors = np.zeros((ntors, 6), int), np.zeros((ntors, 14))
+    for m in range(ntors):
+        line = lines[pos[0]].replace("D", "E").replace("d", "e")
+        pos[0] += 1
+        toks = line.split()
+        tors[m] = [int(x) for x in toks[:6]]
+        nt = tors[m, 4]
+        vals = [float(x) for x in toks[6:6 + 2 + 3 * nt]]
+        vtors[m, :2] = vals[:2]
+        for j in range(nt):
+            vtors[m, 2 + 3 * j] = vals[2 + 3 * j]
+            vtors[m, 3 + 3 * j] = vals[3 + 3 * j] * np.pi
+            vtors[m, 4 + 3 * j] = vals[4 + 3 * j]
+    nci = np.array(read(3 * nnci, int), dtype=int).reshape(nnci, 3) if nnci else np.zeros((0, 3), int)
+    if c6 is None:
+        c6 = pair_c6(at)
+    return QMDFF(at=at, xyz=xyz, q=q, bond=bond, vbond=vbond, angl=angl, vangl=vangl, tors=tors,
+                 vtors=vtors, nci=nci, c6=c6)
+
+
+def pair_c6(at):
+    n = len(at)
+    c6 = np.zeros((n, n))
+    for i in range(n):
+        for j in range(n):
+            c6[i, j] = C6_PAIR[(min(at[i], at[j]), max(at[i], at[j]))]
+    return c6
+
+
+def alkane_geometry(nc=20, r_cc=1.53, r_ch=1.09):
+    """Zig-zag C_nH_2n+2, Angstrom; returns (at, xyz, carbon neighbour list)."""
+    th = np.arccos(-1.0 / 3.0)
+    ux, uz = np.sin(th / 2.0), np.cos(th / 2.0)
+    cpos = np.array([[k * r_cc * ux, 0.0, (k % 2) * r_cc * uz] for k in range(nc)])
+    at, xyz = [6] * nc, [c for c in cpos]
+    hs = []
+    for k in range(nc):
+        nbr = []
+        if k > 0:
+            nbr.append(cpos[k - 1] - cpos[k])
+        if k < nc - 1:
+            nbr.append(cpos[k + 1] - cpos[k])
+        if len(nbr) == 1:   # terminal: continue the zig-zag for the in-plane H
+            nbr.append(np.array([-nbr[0][0], 0.0, nbr[0][2]]))
+            inplane = nbr[1] / np.linalg.norm(nbr[1])
+            hs.append((k, inplane))
+        b = -(nbr[0] / np.linalg.norm(nbr[0]) + nbr[1] / np.linalg.norm(nbr[1]))
+        b /= np.linalg.norm(b)
+        y = np.array([0.0, 1.0, 0.0])
+        for s in (1.0, -1.0):
+            d = np.cos(th / 2.0) * b + s * np.sin(th / 2.0) * y
+            hs.append((k, d / np.linalg.norm(d)))
+    for k, d in hs:
+        at.append(1)
+        xyz.append(cpos[k] + r_ch * d)
+    return np.array(at), np.array(xyz)
+
+
+def _topology(at, xyz_ang):
+    n = len(at)
+    bonds = []
+    for i in range(n):
+        for j in range(i + 1, n):
+            d = np.linalg.norm(xyz_ang[i] - xyz_ang[j])
+            cut = 1.7 if at[i] == 6 and at[j] == 6 else 1.2
+            if d < cut:
+                bonds.append((i, j))
+    adj = [[] for _ in range(n)]
+    for i, j in bonds:
+        adj[i].append(j)
+        adj[j].append(i)
+    # topological distance by BFS
+    dist = np.full((n, n), 99, dtype=int)
+    for s in range(n):
+        dist[s, s] = 0
+        front = [s]
+        while front:
+            nxt = []
+            for u in front:
+                for v in adj[u]:
+                    if dist[s, v] > dist[s, u] + 1:
+                        dist[s, v] = dist[s, u] + 1
+                        nxt.append(v)
+            front = nxt
+    return bonds, adj, dist
+
+
+def alkane(nc=20, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002):
+    """Synthetic C_nH_2n+2 QMDFF (bohr, Hartree)."""
+    rng = np.random.default_rng(seed)
+    at, xa = alkane_geometry(nc)
+    xyz = xa / BOHR_ANGSTROM
+    n = len(at)
+    bonds, adj, dist = _topology(at, xa)
+    bond = np.array([[i + 1, j + 1] for i, j in bonds])
+    vbond = np.zeros((len(bonds), 3))
+    a_exp = 6.0
+    for m, (i, j) in enumerate(bonds):
+        r0 = np.linalg.norm(xyz[i] - xyz[j])
+        K = k_bond * rng.uniform(0.8, 1.2)          # curvature Eh/bohr^2
+        vbond[m] = [r0, 2.0 * K * r0 * r0 / (a_exp * a_exp), a_exp]
+    angl, vangl = [], []
+    for j in range(n):
+        nb = adj[j]
+        for x in range(len(nb)):
+            for y in range(x + 1, len(nb)):
+                i, k = nb[x], nb[y]
+                v1, v2 = xyz[i] - xyz[j], xyz[k] - xyz[j]
+                th0 = np.arccos(np.dot(v1, v2) / np.linalg.norm(v1) / np.linalg.norm(v2))
+                K = k_angle * rng.uniform(0.8, 1.2)   # Eh/rad^2
+                angl.append([j + 1, i + 1, k + 1])
+                vangl.append([th0, K / (2.0 * np.sin(th0) ** 2)])
+    tors, vtors = [], []
+    for b, c in bonds:
+        for a in adj[b]:
+            if a == c:
+                continue
+            for d in adj[c]:
+                if d == b or d == a:
+                    continue
+                v = np.zeros(14)
+                v[0] = np.pi          # phi0 (staggered reference)
+                v[1] = v_tors * rng.uniform(0.8, 1.2)
+                v[2], v[3], v[4] = 3.0, np.pi, 1.0   # rn = 3, phase pi: minima at staggered
+                tors.append([a + 1, b + 1, c + 1, d + 1, 1, 0])
+                vtors.append(v)
+    nci = []
+    for i in range(n):
+        for j in range(i + 1, n):
+            if dist[i, j] >= 3:
+                nci.append([i + 1, j + 1, min(int(dist[i, j]), 5)])
+    q = np.where(at == 6, -0.1, 0.1).astype(float)
+    # exact neutrality: spread the remainder over the hydrogens
+    q[at == 1] -= q.sum() / np.count_nonzero(at == 1)
+    return QMDFF(at=at, xyz=xyz, q=q, bond=bond, vbond=vbond, angl=np.array(angl),
+                 vangl=np.array(vangl), tors=np.array(tors), vtors=np.array(vtors),
+                 nci=np.array(nci), c6=pair_c6(at))
+
+
+def pair_parameters(ff: QMDFF, tab: ElementTables):
+    """Per-NCI-pair R0, C6, sr42, zab, alpha as ff_nonb reads them."""
+    i1, i2 = ff.nci[:, 0] - 1, ff.nci[:, 1] - 1
+    z1, z2 = ff.at[i1], ff.at[i2]
+    return (tab.r094[z1, z2].copy(), ff.c6[i2, i1].copy(), tab.sr42[z1, z2].copy(),
+            tab.zab[z1, z2].copy(), tab.r0ab[z1, z2].copy())
+
+
+def eps_factors():
+    """eps1, eps2 of src/setnonb.f90:164-190 (index = NCI category)."""
+    eps1 = np.zeros(7)
+    eps2 = np.zeros(7)
+    eps1[3], eps1[4], eps1[5] = F32(0.85), 1.0, 1.0
+    eps2[3], eps2[4], eps2[5], eps2[6] = 0.5, 0.5, 1.0, 1.0
+    return eps1, eps2

@@ -19,7 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-PES_IDS = {"h3": 1, "ch4h": 2}
+PES_IDS = {"h3": 1, "ch4h": 2, "qmdff": 4}
 THERMOSTATS = {"none": 0, "andersen": 1, "pile": 3}
 OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",
                   "acos", "erf", "cmp", "tanh", "cosh")
@@ -39,6 +39,50 @@ class Cfg(C.Structure):
                 ("thermostat", C.c_int), ("andersen_step", C.c_int), ("transrot", C.c_int),
                 ("seed", C.c_uint32), ("dt", C.c_double), ("beta", C.c_double),
                 ("pile_tau0", C.c_double), ("mass", C.POINTER(C.c_double))]
+
+
+class QmdffDef(C.Structure):
+    _fields_ = [("natoms", C.c_int), ("at", C.POINTER(C.c_int)), ("q", C.POINTER(C.c_double)),
+                ("rad", C.POINTER(C.c_double)), ("nbond", C.c_int), ("nangl", C.c_int),
+                ("ntors", C.c_int), ("nnci", C.c_int), ("bond", C.POINTER(C.c_int)),
+                ("vbond", C.POINTER(C.c_double)), ("angl", C.POINTER(C.c_int)),
+                ("vangl", C.POINTER(C.c_double)), ("tors", C.POINTER(C.c_int)),
+                ("vtors", C.POINTER(C.c_double)), ("nci", C.POINTER(C.c_int)),
+                ("pR0", C.POINTER(C.c_double)), ("pC6", C.POINTER(C.c_double)),
+                ("pSr42", C.POINTER(C.c_double)), ("pZab", C.POINTER(C.c_double)),
+                ("pAlpha", C.POINTER(C.c_double)), ("eps1", C.c_double * 7), ("eps2", C.c_double * 7),
+                ("coul_cut", C.c_double), ("zahn", C.c_int), ("zahn_a", C.c_double),
+                ("zahn_par", C.c_double), ("e_zero", C.c_double)]
+
+
+_keep = []
+
+
+def set_qmdff(ff, tables, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
+    """Load a caracal_gb300.qmdff.QMDFF (1-based atoms) as the oracle's PES 4."""
+    from caracal_gb300 import qmdff as Q
+    ip = lambda a: np.ascontiguousarray(a, dtype=np.int32)  # noqa: E731
+    fp = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    arrs = dict(at=ip(ff.at), q=fp(ff.q), rad=fp(ff.rad_bohr()), bond=ip(ff.bond - 1),
+                vbond=fp(ff.vbond), angl=ip(ff.angl - 1), vangl=fp(ff.vangl),
+                tors=ip(np.column_stack([ff.tors[:, :4] - 1, ff.tors[:, 4:]])), vtors=fp(ff.vtors),
+                nci=ip(np.column_stack([ff.nci[:, :2] - 1, ff.nci[:, 2]])))
+    pr = [fp(a) for a in Q.pair_parameters(ff, tables)]
+    _keep[:] = [arrs, pr]
+    e1, e2 = Q.eps_factors()
+    d = QmdffDef()
+    d.natoms = ff.n
+    d.nbond, d.nangl, d.ntors, d.nnci = len(ff.bond), len(ff.angl), len(ff.tors), len(ff.nci)
+    for k in ("q", "rad", "vbond", "vangl", "vtors"):
+        setattr(d, k, arrs[k].ctypes.data_as(C.POINTER(C.c_double)))
+    for k in ("at", "bond", "angl", "tors", "nci"):
+        setattr(d, k, arrs[k].ctypes.data_as(C.POINTER(C.c_int)))
+    for k, a in zip(("pR0", "pC6", "pSr42", "pZab", "pAlpha"), pr):
+        setattr(d, k, a.ctypes.data_as(C.POINTER(C.c_double)))
+    for i in range(7):
+        d.eps1[i], d.eps2[i] = e1[i], e2[i]
+    d.coul_cut, d.zahn, d.zahn_a, d.zahn_par, d.e_zero = coul_cut, int(zahn), zahn_a, zahn_par, ff.e_zero
+    lib().orc_qmdff_set(C.byref(d))
 
 
 class XiDef(C.Structure):
@@ -84,6 +128,7 @@ def lib():
         _lib.orc_init_forces.argtypes = [C.POINTER(Cfg), C.c_int, d, d, d]
         _lib.orc_run.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_int, C.c_int, d, d, d, d,
                                  C.POINTER(C.c_int), C.c_int]
+        _lib.orc_qmdff_set.argtypes = [C.POINTER(QmdffDef)]
         _lib.orc_calc_xi.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d]
         _lib.orc_calc_xi.restype = C.c_double
         _lib.orc_recross_children.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, d,

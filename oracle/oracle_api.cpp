@@ -11,6 +11,7 @@
 #include "opcount.hpp"
 #include "pes_ch4h.hpp"
 #include "pes_h3.hpp"
+#include "pes_qmdff.hpp"
 #include "philox.hpp"
 #include "recross.hpp"
 #include "rpmd.hpp"
@@ -32,6 +33,8 @@ orc::StepConfig to_step(const orc_cfg* c) {
   return s;
 }
 
+orc::qmdff::FF g_qmdff;
+
 // Per-bead PES call, q(3,N) -> V, g(3,N).
 struct BeadPES {
   int pes;
@@ -40,6 +43,7 @@ struct BeadPES {
     switch (pes) {
       case 1: orc::h3::egrad_bead<double>(q, V, g); break;
       case 2: orc::ch4h::egrad_bead<double>(q, V, g); break;
+      case 4: orc::qmdff::egrad(g_qmdff, q, V, g); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
   }
@@ -48,6 +52,40 @@ struct BeadPES {
 }  // namespace
 
 extern "C" {
+
+void orc_qmdff_set(const orc_qmdff_def* d) {
+  orc::qmdff::FF& f = g_qmdff;
+  f = orc::qmdff::FF();
+  f.n = d->natoms;
+  f.at.assign(d->at, d->at + f.n);
+  f.q.assign(d->q, d->q + f.n);
+  f.rad.assign(d->rad, d->rad + f.n);
+  f.nbond = d->nbond;
+  f.nangl = d->nangl;
+  f.ntors = d->ntors;
+  f.nnci = d->nnci;
+  f.bond.assign(d->bond, d->bond + 2 * f.nbond);
+  f.vbond.assign(d->vbond, d->vbond + 3 * f.nbond);
+  f.angl.assign(d->angl, d->angl + 3 * f.nangl);
+  f.vangl.assign(d->vangl, d->vangl + 2 * f.nangl);
+  f.tors.assign(d->tors, d->tors + 6 * f.ntors);
+  f.vtors.assign(d->vtors, d->vtors + 14 * f.ntors);
+  f.nci.assign(d->nci, d->nci + 3 * f.nnci);
+  f.pR0.assign(d->pR0, d->pR0 + f.nnci);
+  f.pC6.assign(d->pC6, d->pC6 + f.nnci);
+  f.pSr42.assign(d->pSr42, d->pSr42 + f.nnci);
+  f.pZab.assign(d->pZab, d->pZab + f.nnci);
+  f.pAlpha.assign(d->pAlpha, d->pAlpha + f.nnci);
+  for (int i = 0; i < 7; ++i) {
+    f.eps1[i] = d->eps1[i];
+    f.eps2[i] = d->eps2[i];
+  }
+  f.coul_cut = d->coul_cut;
+  f.zahn = d->zahn != 0;
+  f.zahn_a = d->zahn_a;
+  f.zahn_par = d->zahn_par;
+  f.e_zero = d->e_zero;
+}
 
 void orc_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
   orc::Philox4 r = orc::philox4x32_10(ctr, k0, k1);

@@ -12,7 +12,7 @@ extern "C" {
 #endif
 
 typedef struct orc_cfg {
-  int pes;            /* 1 = H3 (BKMP2), 2 = CH4H */
+  int pes;            /* 1 = H3 (BKMP2), 2 = CH4H, 4 = QMDFF (orc_qmdff_set) */
   int natoms;
   int nbeads;
   int thermostat;     /* 0 none, 1 Andersen, 3 PILE */
@@ -46,6 +46,30 @@ int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, do
  * status[t] ORs the per-step status bits; nthreads <= 0 uses all cores. */
 int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q,
             double* p, double* f, double* epot, int* status, int nthreads);
+/* QMDFF definition (0-based atoms); per-NCI-pair R0, C6, sr42, zab, alpha. */
+typedef struct orc_qmdff_def {
+  int natoms;
+  const int* at;
+  const double* q;
+  const double* rad;  /* covalent radius per atom, bohr */
+  int nbond, nangl, ntors, nnci;
+  const int* bond;    /* 2 per bond */
+  const double* vbond;
+  const int* angl;    /* 3 per angle, centre first */
+  const double* vangl;
+  const int* tors;    /* 6 per torsion */
+  const double* vtors;/* 14 per torsion */
+  const int* nci;     /* 3 per pair */
+  const double *pR0, *pC6, *pSr42, *pZab, *pAlpha;
+  double eps1[7], eps2[7];
+  double coul_cut;
+  int zahn;
+  double zahn_a, zahn_par, e_zero;
+} orc_qmdff_def;
+
+/* Sets the force field used by PES id 4 (QMDFF) in all oracle entry points. */
+void orc_qmdff_set(const orc_qmdff_def* d);
+
 /* BIMOLEC reaction coordinate of Caracal's recrossing (calc_xi mode 2). */
 typedef struct orc_xidef {
   int nreac1, reac1[8];   /* 0-based atom indices of reactant 1 */
