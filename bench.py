@@ -39,6 +39,10 @@ ALGO_PES_OPS = {
     "h3": {"add": 491, "mul": 738, "div": 82, "sqrt": 5, "exp": 11, "pow": 6},
     "ch4h": {"add": 3839, "mul": 7125, "div": 1812, "sqrt": 135, "exp": 54, "acos": 18, "tanh": 21,
              "cosh": 21},
+    # synthetic C20H42 QMDFF (ff_eg + ff_nonb), thermal geometry (reference
+    # geometry + N(0, 0.05 bohr) per coordinate, seed 0); asin counted with acos
+    "qmdff": {"add": 92211, "mul": 117770, "div": 20592, "sqrt": 4525, "exp": 1415, "pow": 122,
+              "sin": 633, "cos": 753, "acos": 291, "erf": 171},
 }
 CALIB_OPS = {"fma": 0, "div": 1, "sqrt": 2, "exp": 3, "log": 4, "pow": 5, "sin": 6, "cos": 7,
              "acos": 8, "erf": 9, "tanh": 10, "cosh": 11}
@@ -69,6 +73,9 @@ def algo_flops_per_bead_step(pes, natoms, nbeads, thermostat, w, transrot=True, 
     f64 = nc * (4 * 2.5 * lg + 6) + nc * 4
     if transrot:
         f64 += nc * 30
+    if thermostat == "andersen":
+        # a full resample every ANDERSEN_STEP steps (70): the Gaussian draws
+        f64 += (nc / 2) * (w["log"] + 1 + w["sin"] + w["cos"]) / 70.0
     if thermostat == "pile":
         f64 += 2 * (nc * (2 * 2 * 2.5 * lg + 4) + (nc / 2) * (w["log"] + 1 + w["sin"] + w["cos"]))
     if recross:
@@ -91,12 +98,13 @@ def roofline(wl, mixed, ms, K, cal):
     _, pes32 = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w32, wl.transrot, rec)
     p64, p32 = cal["fp64"]["peak_tflops"], cal["fp32"]["peak_tflops"]
     units = wl.ntraj * wl.nbeads * K
+    step = "qmdff step graph" if wl.pes == "qmdff" else "rpmd_run_kernel"
     if mixed:
         eq = f64 + pes32 * p64 / p32
-        kern, bound = f"rpmd_run_kernel<{wl.pes}, mixed>", "fp64+fp32 (FP64-equivalent)"
+        kern, bound = f"{step}<{wl.pes}, mixed>", "fp64+fp32 (FP64-equivalent)"
     else:
         eq = f64 + pes64
-        kern, bound = f"rpmd_run_kernel<{wl.pes}, fp64>", "fp64"
+        kern, bound = f"{step}<{wl.pes}, fp64>", "fp64"
     ach = eq * units / (ms * 1e-3) / 1e12
     return {"kernel": kern, "bound": bound, "achieved": ach, "peak": p64, "unit": "TFLOP/s",
             "frac": ach / p64, "traffic": None,
@@ -197,14 +205,28 @@ def workload(name):
         wl = W.ch4h_config(ntraj=4096 if name == "ch4h" else 256)
         wl.extra["recross"] = W.ch4h_recross_definition(wl.q0)
         return wl
+    if name == "qmdff":
+        return W.qmdff_config(ntraj=1024, nbeads=64)
+    if name == "qmdff_small":
+        return W.qmdff_config(ntraj=64, nbeads=16)
     raise SystemExit(f"unknown workload {name}")
+
+
+def make_pes(wl):
+    """The engine's PES argument: a surface name, or the device QMDFF."""
+    if wl.pes == "qmdff":
+        from caracal_gb300.engine import QMDFFForceField
+        if "gpu_ff" not in wl.extra:
+            wl.extra["gpu_ff"] = QMDFFForceField(wl.extra["ff"])
+        return wl.extra["gpu_ff"]
+    return wl.pes
 
 
 def make_engine(wl, precision, traj0=0, max_steps=0):
     """Engine for the workload: MD trajectories (positions + Andersen momenta +
     forces) or, for a recrossing workload, children from one parent geometry."""
     from caracal_gb300 import RPMDEngine
-    eng = RPMDEngine(wl.pes, wl.mass, wl.nbeads, wl.ntraj, wl.dt_au, beta=wl.beta,
+    eng = RPMDEngine(make_pes(wl), wl.mass, wl.nbeads, wl.ntraj, wl.dt_au, beta=wl.beta,
                      thermostat=wl.thermostat, andersen_step=wl.andersen_step,
                      pile_tau0_au=wl.pile_tau0_au, transrot=wl.transrot, precision=precision,
                      seed=wl.seed, traj0=traj0)
@@ -227,6 +249,9 @@ class OracleRunner:
     def __init__(self, wl):
         from oracle import oracle as orc
         self.orc, self.wl = orc, wl
+        if wl.pes == "qmdff":
+            from caracal_gb300 import qmdff as Q
+            orc.set_qmdff(wl.extra["ff"], Q.ElementTables.d3_like())
         self.cfg = orc.Config(wl.pes, wl.mass, wl.nbeads, wl.dt_au, wl.beta,
                               thermostat=wl.thermostat, andersen_step=wl.andersen_step,
                               pile_tau0=wl.pile_tau0_au, transrot=wl.transrot, seed=wl.seed)
@@ -354,7 +379,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-        eng.run(K)                       # K steps, one persistent launch
+        eng.run(K)                       # K steps: one persistent launch (analytic PES) or K graph replays (QMDFF)
         torch.cuda.synchronize()
         ms = eng.last_kernel_ms()
         if dist:
@@ -431,13 +456,15 @@ def run_ours(args):
         "config": {"workload": wl.name, "pes": wl.pes, "ntraj": wl.ntraj, "nbeads": wl.nbeads,
                    "natoms": len(wl.mass), "thermostat": wl.thermostat, "kelvin": wl.kelvin,
                    "dt_fs": wl.dt_fs, "parallelism": f"replicas x{ws}",
-                   "l2": "flushed (256 MB write) before the timed launch; K steps in one launch"},
+                   "l2": "flushed (256 MB write) before the timed launch"
+                         + ("; K steps in one launch" if wl.pes != "qmdff" else
+                            "; state (3 x 97.5 MB) larger than L2 is streamed every step")},
         "plain_fp64": {"value": plain, "unit": "bead-steps/s", "ms_per_step": ms_64 / K},
         "mixed_over_plain": value / plain,
         "force_error_vs_fp64": ferr, "energy_error_vs_fp64": eerr,
         "e2e": {"value": e2e, "unit": "bead-steps/s", "steps": K_e2e,
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": 3 * nbytes + 8 * wl.ntraj},
-        "gpu_launches": 1,
+        "gpu_launches": info["launches"],
         "launch": info,
         "roofline": roof,
         "roofline_plain_fp64": roof_plain,
@@ -469,7 +496,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ch4h",
                     help="ch4h (CH4+H recrossing children, 4096 x 32 beads: the default), "
-                         "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16)")
+                         "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16), "
+                         "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (64 x 16)")
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-steps-per-sample", type=int, default=20)

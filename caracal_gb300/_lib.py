@@ -55,6 +55,17 @@ class CrRecross(C.Structure):
                 ("xi_ideal", C.c_double)]
 
 
+class CrQmdffDef(C.Structure):
+    _fields_ = [("natoms", C.c_int), ("at", c_int_p), ("q", c_double_p), ("rad", c_double_p),
+                ("nbond", C.c_int), ("nangl", C.c_int), ("ntors", C.c_int), ("nnci", C.c_int),
+                ("bond", c_int_p), ("vbond", c_double_p), ("angl", c_int_p), ("vangl", c_double_p),
+                ("tors", c_int_p), ("vtors", c_double_p), ("nci", c_int_p),
+                ("r0ab", c_double_p), ("zab", c_double_p), ("r0094", c_double_p), ("sr42", c_double_p),
+                ("c66ab", c_double_p), ("eps1", C.c_double * 6), ("eps2", C.c_double * 6),
+                ("coul_cut", C.c_double), ("zahn", C.c_int), ("zahn_a", C.c_double),
+                ("zahn_par", C.c_double), ("e_zero", C.c_double)]
+
+
 class CaracalError(RuntimeError):
     def __init__(self, code, where):
         self.code = code
@@ -100,6 +111,12 @@ def _sig(lib):
         "cr_engine_set_recross": ([eng, C.POINTER(CrRecross), C.c_int], C.c_int),
         "cr_engine_init_children": ([eng, d], C.c_int),
         "cr_engine_kappa": ([eng, d, d, d, i], C.c_int),
+        "cr_qmdff_create": ([C.POINTER(CrQmdffDef), C.POINTER(C.c_void_p)], C.c_int),
+        "cr_qmdff_destroy": ([v], C.c_int),
+        "cr_qmdff_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
+        "cr_qmdff_egrad_device": ([v, v, C.c_int, v, v, C.c_int, v], C.c_int),
+        "cr_qmdff_schedule_info": ([v, i, i], C.c_int),
+        "cr_engine_create_qmdff": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

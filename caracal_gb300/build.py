@@ -1,7 +1,8 @@
 """Compile the CUDA engine (sm_103a) into an in-tree shared library.
 
-One nvcc invocation, one -gencode: the library is rebuilt only when a source
-under ``csrc/`` or ``include/`` is newer than it.
+One nvcc process per translation unit (run in parallel), one -gencode; the
+library is rebuilt only when a source under ``csrc/`` or ``include/`` is
+newer than it.
 """
 from __future__ import annotations
 
@@ -9,6 +10,7 @@ import glob
 import os
 import shutil
 import subprocess
+from concurrent.futures import ThreadPoolExecutor
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
@@ -37,21 +39,34 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
-    tmp = LIB + ".tmp"
-    cmd = [nvcc_path(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-           "-o", tmp] + sources()
+def _compile(src: str, verbose: bool) -> tuple[str, str]:
+    obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
+    cmd = [nvcc_path(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + res.stdout + res.stderr)
+        raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n" + res.stdout + res.stderr)
+    return obj, res.stdout + res.stderr
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile every csrc/*.cu in parallel (one process each), then link."""
+    if not force and not _stale():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    srcs = sources()
+    with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as pool:
+        results = list(pool.map(lambda s: _compile(s, verbose), srcs))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc_path(), ARCH, "-shared", "-o", tmp] + [o for o, _ in results]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("nvcc link failed:\n" + res.stdout + res.stderr)
     os.replace(tmp, LIB)
     if verbose:
-        print(res.stdout + res.stderr)
+        for _, log in results:
+            print(log)
     return LIB
 
 

@@ -12,6 +12,9 @@
 #include "pes_ch4h.cuh"
 #include "pes_h3.cuh"
 #include "rpmd_kernel.cuh"
+#include "host_util.h"
+#include "qmdff_host.h"
+#include "split.cuh"
 
 namespace {
 
@@ -46,6 +49,8 @@ int pes_natoms(int pes) {
 }
 
 }  // namespace
+
+int cr_set_error(int code, const std::string& msg) { return fail(code, msg); }
 
 // ---------------------------------------------------------------------------
 // Device kernels outside the step loop
@@ -198,22 +203,31 @@ struct cr_engine {
   double *d_w = nullptr, *d_kappa = nullptr, *d_qpar = nullptr;
   int* d_wpos = nullptr;
   cr::StepParams prm{};
+  // large-molecule path (QMDFF): state in HBM, a captured graph per step
+  cr_qmdff* ff = nullptr;
+  bool split = false;
+  cr::SplitParams sp{};
+  double *d_mass = nullptr, *d_inv_mass = nullptr, *d_sigma = nullptr, *d_ke = nullptr, *d_ko = nullptr;
+  int* d_istep = nullptr;
+  int h_istep = 0;
+  size_t smem_drift = 0, smem_kick = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
 };
 
 namespace {
 
-// Propagator blocks K1, K2, K3 (unit mass) of the Caracal cosine transform,
-// restricted to the (P/2+1)^2 block that acts on symmetrised inputs.
-void build_propagator(int P, double beta, double dt, std::vector<double>& out) {
-  const int H = P / 2 + 1;
-  std::vector<double> C((size_t)P * P);
+// Caracal's cosine transform C = sqrt(1/P) cos(2 pi j k / P) and the per-mode
+// coefficients of the free ring polymer at unit mass (src/verlet.f90:405-429):
+// pc = cos(w dt), pq = -w sin(w dt), pd = sin(w dt) / w (mode 0: 1, 0, dt).
+void mode_tables(int P, double beta, double dt, std::vector<double>& C, std::vector<double> (&diag)[3]) {
+  C.assign((size_t)P * P, 0.0);
   const double factor = std::sqrt(1.0 / P);
   for (int j = 0; j < P; ++j)
     for (int k = 0; k < P; ++k) {
       long long m = ((long long)j * k) % P;
       C[(size_t)j * P + k] = factor * std::cos(2.0 * kPi * (double)m / P);
     }
-  // per-mode coefficients (src/verlet.f90:405-429) at unit mass
   std::vector<double> pc(P, 1.0), pq(P, 0.0), pd(P, dt);
   if (P > 1) {
     const double beta_n = beta / P, twown = 2.0 / beta_n, pi_n = kPi / P;
@@ -230,15 +244,60 @@ void build_propagator(int P, double beta, double dt, std::vector<double>& out) {
       pd[P - k] = pd[k];
     }
   }
+  diag[0] = pc;
+  diag[1] = pq;
+  diag[2] = pd;
+}
+
+// sum over modes k (of parity `par`: 0 even, 1 odd, -1 all) of C[r][k] D[k] C[k][l]
+double kentry(const std::vector<double>& C, const std::vector<double>& D, int P, int r, int l, int par) {
+  double s = 0.0;
+  for (int k = 0; k < P; ++k)
+    if (par < 0 || (k & 1) == par) s += C[(size_t)r * P + k] * D[k] * C[(size_t)k * P + l];
+  return s;
+}
+
+// Propagator blocks K1, K2, K3 (unit mass) of the Caracal cosine transform,
+// restricted to the (P/2+1)^2 block that acts on symmetrised inputs.
+void build_propagator(int P, double beta, double dt, std::vector<double>& out) {
+  const int H = P / 2 + 1;
+  std::vector<double> C, diag[3];
+  mode_tables(P, beta, dt, C, diag);
   out.assign((size_t)3 * H * H, 0.0);
-  const std::vector<double>* diag[3] = {&pc, &pq, &pd};
   for (int which = 0; which < 3; ++which)
     for (int r = 0; r < H; ++r)
-      for (int l = 0; l < H; ++l) {
-        double s = 0.0;
-        for (int k = 0; k < P; ++k) s += C[(size_t)r * P + k] * (*diag[which])[k] * C[(size_t)k * P + l];
-        out[(size_t)which * H * H + (size_t)r * H + l] = s;
-      }
+      for (int l = 0; l < H; ++l)
+        out[(size_t)which * H * H + (size_t)r * H + l] = kentry(C, diag[which], P, r, l, -1);
+}
+
+// Parity-split blocks of the large-molecule path: for even P, Ke[w][r][l]
+// (even modes, l < nu) and Ko[w][r][l] (odd modes, l < nv), r < nr; for odd P
+// the unique rows of K (nr = nu = P/2+1, nv = 0).
+void build_split_propagator(int P, double beta, double dt, cr::SplitParams& s, std::vector<double>& ke,
+                            std::vector<double>& ko) {
+  std::vector<double> C, diag[3];
+  mode_tables(P, beta, dt, C, diag);
+  s.M = P / 2;
+  s.split = (P % 2 == 0) ? 1 : 0;
+  if (s.split) {
+    s.nr = s.M / 2 + 1;
+    s.nu = s.M / 2 + 1;
+    s.nv = s.M - s.M / 2;
+  } else {
+    s.nr = P / 2 + 1;
+    s.nu = s.nr;
+    s.nv = 0;
+  }
+  s.su = s.nu | 1;
+  s.sv = s.nv > 0 ? (s.nv | 1) : 0;
+  ke.assign((size_t)3 * s.nr * s.nu, 0.0);
+  ko.assign((size_t)3 * s.nr * (s.nv > 0 ? s.nv : 1), 0.0);
+  for (int w = 0; w < 3; ++w)
+    for (int r = 0; r < s.nr; ++r) {
+      for (int l = 0; l < s.nu; ++l)
+        ke[((size_t)w * s.nr + r) * s.nu + l] = kentry(C, diag[w], P, r, l, s.split ? 0 : -1);
+      for (int l = 0; l < s.nv; ++l) ko[((size_t)w * s.nr + r) * s.nv + l] = kentry(C, diag[w], P, r, l, 1);
+    }
 }
 
 // PILE-L circulant vectors a (friction) and b (noise) of O^T diag(c) O with O
@@ -299,7 +358,53 @@ int launch_forces(cr_engine* e) {
   return CR_OK;
 }
 
+// One step of the large-molecule path as kernel launches on e->stream
+// (recorded once into a CUDA graph).
+int split_step_launches(cr_engine* e) {
+  const int cw = cr::split_chunk(e->P);
+  const dim3 grid((e->NC + cw - 1) / cw, e->T);
+  cr::split_drift_kernel<<<grid, cr::kSplitBlock, e->smem_drift, e->stream>>>(e->sp);
+  CR_CUDA(cudaGetLastError());
+  int rc = qmdff_launch(e->ff, e->d_q, e->T * e->P, e->d_V, e->d_f, e->cfg.precision, e->stream);
+  if (rc) return rc;
+  cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp);
+  CR_CUDA(cudaGetLastError());
+  cr::split_finish_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+  CR_CUDA(cudaGetLastError());
+  cr::split_advance_kernel<<<1, 1, 0, e->stream>>>(e->d_istep);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+int split_run(cr_engine* e, int nsteps) {
+  if (!e->graph_exec) {
+    CR_CUDA(cudaFuncSetAttribute(cr::split_drift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)e->smem_drift));
+    CR_CUDA(cudaFuncSetAttribute(cr::split_kick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)e->smem_kick));
+    // the force kernel sets its own shared-memory limit outside the capture
+    int rc = qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
+    if (rc) return rc;
+    CR_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    rc = split_step_launches(e);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(CR_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ce));
+    e->graph = g;
+    CR_CUDA(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
+  }
+  e->h_istep = e->istep;
+  CR_CUDA(cudaMemcpyAsync(e->d_istep, &e->h_istep, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  for (int n = 0; n < nsteps; ++n) CR_CUDA(cudaGraphLaunch(e->graph_exec, e->stream));
+  return CR_OK;
+}
+
 int dispatch_run(cr_engine* e, int nsteps) {
+  if (e->split) return split_run(e, nsteps);
   switch (e->cfg.pes) {
     case CR_PES_H3: return launch_run<cr::PesH3>(e, nsteps);
     case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, nsteps);
@@ -308,6 +413,13 @@ int dispatch_run(cr_engine* e, int nsteps) {
 }
 
 int dispatch_forces(cr_engine* e) {
+  if (e->split) {
+    int rc = qmdff_launch(e->ff, e->d_q, e->T * e->P, e->d_V, e->d_f, e->cfg.precision, e->stream);
+    if (rc) return rc;
+    cr::split_sum_beads_kernel<<<(e->T + 127) / 128, 128, 0, e->stream>>>(e->T, e->P, e->d_V, e->d_epot);
+    CR_CUDA(cudaGetLastError());
+    return CR_OK;
+  }
   switch (e->cfg.pes) {
     case CR_PES_H3: return launch_forces<cr::PesH3>(e);
     case CR_PES_CH4H: return launch_forces<cr::PesCH4H>(e);
@@ -469,14 +581,27 @@ int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq
   return rc;
 }
 
-int cr_engine_create(const cr_config* cfg, cr_engine** out) {
+}  // extern "C"
+
+// Validation and set-up shared by both engine paths; ff != NULL selects the
+// large-molecule (QMDFF) path.
+static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
   if (!cfg || !out) return fail(CR_ERR_ARG, "NULL argument");
   *out = nullptr;
-  const int N = pes_natoms(cfg->pes);
-  if (N < 0) return fail(CR_ERR_UNSUPPORTED, "PES not available in this engine");
+  int N = -1;
+  if (ff) {
+    if (cfg->pes != CR_PES_QMDFF) return fail(CR_ERR_ARG, "cr_engine_create_qmdff needs pes = CR_PES_QMDFF");
+    N = ff->n;
+  } else {
+    if (cfg->pes == CR_PES_QMDFF) return fail(CR_ERR_ARG, "QMDFF engines are created with cr_engine_create_qmdff");
+    N = pes_natoms(cfg->pes);
+    if (N < 0) return fail(CR_ERR_UNSUPPORTED, "PES not available in this engine");
+  }
   if (cfg->natoms != N) return fail(CR_ERR_ARG, "natoms does not match the PES");
   if (cfg->nbeads < 1 || cfg->nbeads > cr::kMaxBeads) return fail(CR_ERR_ARG, "nbeads must be 1..128");
   if (cfg->ntraj < 1) return fail(CR_ERR_ARG, "ntraj must be >= 1");
+  if (ff && (long long)cfg->ntraj * cfg->nbeads > (1LL << 26))
+    return fail(CR_ERR_ARG, "ntraj * nbeads must be <= 2^26 on the QMDFF path");
   if (!(cfg->dt > 0.0)) return fail(CR_ERR_ARG, "dt must be > 0");
   if (cfg->thermostat == CR_THERMO_NHC) return fail(CR_ERR_UNSUPPORTED, "Nose-Hoover chain not built yet");
   if (cfg->thermostat != CR_THERMO_NONE && cfg->thermostat != CR_THERMO_ANDERSEN &&
@@ -505,13 +630,15 @@ int cr_engine_create(const cr_config* cfg, cr_engine** out) {
   e->cfg = *cfg;
   e->mass.assign(cfg->mass, cfg->mass + N);
   e->cfg.mass = e->mass.data();
+  e->ff = ff;
+  e->split = ff != nullptr;
   e->N = N;
   e->NC = 3 * N;
   e->P = cfg->nbeads;
   e->T = cfg->ntraj;
   e->G = next_pow2(e->P);
   e->H = e->P / 2 + 1;
-  choose_launch(e);
+  if (!e->split) choose_launch(e);
 
   auto cleanup_fail = [&](int code) {
     cr_engine_destroy(e);
@@ -531,6 +658,7 @@ int cr_engine_create(const cr_config* cfg, cr_engine** out) {
   cudaMemsetAsync(e->d_q, 0, nall * 8, e->stream);
   cudaMemsetAsync(e->d_p, 0, nall * 8, e->stream);
   cudaMemsetAsync(e->d_f, 0, nall * 8, e->stream);
+  cudaMemsetAsync(e->d_V, 0, (size_t)e->T * e->P * 8, e->stream);
   cudaMemsetAsync(e->d_status, 0, (size_t)e->T * sizeof(int), e->stream);
 
   std::vector<double> prop, pile;
@@ -545,6 +673,68 @@ int cr_engine_create(const cr_config* cfg, cr_engine** out) {
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return cleanup_fail(fail(CR_ERR_CUDA, "upload of the tables failed"));
 
+  double tm = 0.0;  // src/transrot.f90:72-79
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < e->P; ++k) tm = tm + e->mass[i];
+  const double totmass = tm * e->P;
+  std::vector<double> sig((size_t)N), inv((size_t)N);
+  for (int i = 0; i < N; ++i) {
+    inv[(size_t)i] = 1.0 / e->mass[i];
+    sig[(size_t)i] = (cfg->beta > 0.0 && std::isfinite(cfg->beta)) ? std::sqrt(e->mass[i] / (cfg->beta / e->P)) : 0.0;
+  }
+
+  if (e->split) {
+    cr::SplitParams& s = e->sp;
+    std::vector<double> ke, ko;
+    build_split_propagator(e->P, cfg->beta, cfg->dt, s, ke, ko);
+    if (cudaMalloc(&e->d_mass, (size_t)N * 8) != cudaSuccess || cudaMalloc(&e->d_inv_mass, (size_t)N * 8) != cudaSuccess ||
+        cudaMalloc(&e->d_sigma, (size_t)N * 8) != cudaSuccess || cudaMalloc(&e->d_ke, ke.size() * 8) != cudaSuccess ||
+        cudaMalloc(&e->d_ko, ko.size() * 8) != cudaSuccess || cudaMalloc(&e->d_istep, sizeof(int)) != cudaSuccess)
+      return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the split tables failed"));
+    if (cudaMemcpy(e->d_mass, e->mass.data(), (size_t)N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_inv_mass, inv.data(), (size_t)N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_sigma, sig.data(), (size_t)N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_ke, ke.data(), ke.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_ko, ko.data(), ko.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(e->d_istep, 0, sizeof(int)) != cudaSuccess)
+      return cleanup_fail(fail(CR_ERR_CUDA, "upload of the split tables failed"));
+    s.T = e->T;
+    s.P = e->P;
+    s.N = N;
+    s.NC = e->NC;
+    s.thermostat = cfg->thermostat;
+    s.andersen_step = cfg->andersen_step > 0 ? cfg->andersen_step : 1;
+    s.transrot = cfg->transrot ? 1 : 0;
+    s.seed = cfg->seed;
+    s.traj0 = cfg->traj0;
+    s.half_dt = 0.5 * cfg->dt;
+    s.totmass = totmass;
+    s.mass = e->d_mass;
+    s.inv_mass = e->d_inv_mass;
+    s.sigma = e->d_sigma;
+    s.ke = e->d_ke;
+    s.ko = e->d_ko;
+    s.pile = e->d_pile;
+    s.q = e->d_q;
+    s.p = e->d_p;
+    s.f = e->d_f;
+    s.V = e->d_V;
+    s.epot = e->d_epot;
+    s.status = e->d_status;
+    s.istep = e->d_istep;
+    const bool pl = cfg->thermostat == CR_THERMO_PILE;
+    const int cw = cr::split_chunk(e->P), sp1 = e->P + 1;
+    e->smem_drift = cr::split_smem_doubles(s, pl) * sizeof(double);
+    e->smem_kick = pl ? ((size_t)3 * cw * sp1 + 2 * (size_t)e->P) * sizeof(double) : 0;
+    if (e->smem_drift > 200 * 1024) return cleanup_fail(fail(CR_ERR_UNSUPPORTED, "bead count too large for the split path"));
+    e->block = cr::kSplitBlock;
+    e->grid = ((e->NC + cw - 1) / cw) * e->T;
+    e->smem = e->smem_drift;
+    *out = e;
+    return CR_OK;
+  }
+  if (N > cr::kMaxAtoms) return cleanup_fail(fail(CR_ERR_UNSUPPORTED, "too many atoms for the persistent kernel"));
+
   cr::StepParams& s = e->prm;
   s.T = e->T;
   s.P = e->P;
@@ -558,15 +748,12 @@ int cr_engine_create(const cr_config* cfg, cr_engine** out) {
   s.dt = cfg->dt;
   s.half_dt = 0.5 * cfg->dt;
   s.beta = cfg->beta;
-  double tm = 0.0;  // src/transrot.f90:72-79
-  for (int i = 0; i < N; ++i)
-    for (int k = 0; k < e->P; ++k) tm = tm + e->mass[i];
-  s.totmass = tm * e->P;
+  s.totmass = totmass;
   for (int i = 0; i < cr::kMaxAtoms; ++i) {
     double m = i < N ? e->mass[i] : 1.0;
     s.mass[i] = m;
     s.inv_mass[i] = 1.0 / m;
-    s.sigma[i] = (cfg->beta > 0.0 && std::isfinite(cfg->beta)) ? std::sqrt(m / (cfg->beta / e->P)) : 0.0;
+    s.sigma[i] = i < N ? sig[(size_t)i] : 0.0;
   }
   s.prop = e->d_prop;
   s.pile = e->d_pile;
@@ -577,6 +764,15 @@ int cr_engine_create(const cr_config* cfg, cr_engine** out) {
   s.status = e->d_status;
   *out = e;
   return CR_OK;
+}
+
+extern "C" {
+
+int cr_engine_create(const cr_config* cfg, cr_engine** out) { return engine_create(cfg, nullptr, out); }
+
+int cr_engine_create_qmdff(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
+  if (!ff) return fail(CR_ERR_ARG, "NULL force field");
+  return engine_create(cfg, ff, out);
 }
 
 int cr_engine_destroy(cr_engine* e) {
@@ -596,6 +792,14 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_kappa);
   cudaFree(e->d_qpar);
   cudaFree(e->d_wpos);
+  cudaFree(e->d_mass);
+  cudaFree(e->d_inv_mass);
+  cudaFree(e->d_sigma);
+  cudaFree(e->d_ke);
+  cudaFree(e->d_ko);
+  cudaFree(e->d_istep);
+  if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
+  if (e->graph) cudaGraphDestroy(e->graph);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -608,6 +812,14 @@ int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
   if (!(sigma >= 0.0)) return fail(CR_ERR_ARG, "sigma must be >= 0");
   CR_CUDA(cudaMemcpyAsync(e->d_q0, q0, (size_t)e->NC * 8, cudaMemcpyHostToDevice, e->stream));
   const int nb = e->T * e->P;
+  if (e->split) {
+    const long long n = (long long)nb * ((e->NC + 1) / 2);
+    cr::split_init_positions_kernel<<<(unsigned)((n + 127) / 128), 128, 0, e->stream>>>(
+        e->T, e->P, e->NC, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
+    CR_CUDA(cudaGetLastError());
+    CR_CUDA(cudaStreamSynchronize(e->stream));
+    return CR_OK;
+  }
   switch (e->cfg.pes) {
     case CR_PES_H3:
       cr::init_positions_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
@@ -629,6 +841,14 @@ int cr_engine_init_momenta(cr_engine* e, int zero) {
   if (!zero && !(e->cfg.beta > 0.0 && std::isfinite(e->cfg.beta)))
     return fail(CR_ERR_ARG, "Andersen momenta need a finite temperature");
   const int nb = e->T * e->P;
+  if (e->split) {
+    const long long n = (long long)nb * ((e->NC + 1) / 2);
+    cr::split_init_momenta_kernel<<<(unsigned)((n + 127) / 128), 128, 0, e->stream>>>(
+        e->T, e->P, e->NC, e->cfg.seed, e->cfg.traj0, e->d_sigma, zero, e->d_p);
+    CR_CUDA(cudaGetLastError());
+    CR_CUDA(cudaStreamSynchronize(e->stream));
+    return CR_OK;
+  }
   switch (e->cfg.pes) {
     case CR_PES_H3:
       cr::init_momenta_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
@@ -687,7 +907,7 @@ static int engine_run_async(cr_engine* e, int nsteps) {
   if (rc) return rc;
   CR_CUDA(cudaEventRecord(e->ev1, e->stream));
   e->istep += nsteps;
-  e->launches = 1;
+  e->launches = e->split ? 5 * nsteps : 1;
   return CR_OK;
 }
 
@@ -766,6 +986,7 @@ int cr_host_free(void* ptr) {
 int cr_engine_set_recross(cr_engine* e, const cr_recross* rc, int max_steps) {
   if (!e || !rc) return fail(CR_ERR_ARG, "NULL argument");
   if (max_steps < 1) return fail(CR_ERR_ARG, "max_steps must be >= 1");
+  if (e->split) return fail(CR_ERR_UNSUPPORTED, "recrossing children are built for the analytic surfaces only");
   auto bad_atom = [&](int a) { return a < 1 || a > e->N; };
   if (rc->nreac1 < 1 || rc->nreac1 > 8 || rc->nreac2 < 1 || rc->nreac2 > 8)
     return fail(CR_ERR_ARG, "reactants need 1..8 atoms each");
@@ -824,6 +1045,7 @@ int cr_engine_set_recross(cr_engine* e, const cr_recross* rc, int max_steps) {
 int cr_engine_init_children(cr_engine* e, const double* q_parent) {
   if (!e || !q_parent) return fail(CR_ERR_ARG, "NULL argument");
   if (!e->xi_on) return fail(CR_ERR_ARG, "call cr_engine_set_recross first");
+  if (e->split) return fail(CR_ERR_UNSUPPORTED, "recrossing children are built for the analytic surfaces only");
   if (!(e->cfg.beta > 0.0 && std::isfinite(e->cfg.beta))) return fail(CR_ERR_ARG, "children need a finite beta");
   const size_t bytes = (size_t)e->NC * e->P * sizeof(double);
   if (!e->d_qpar) CR_CUDA(cudaMalloc(&e->d_qpar, bytes));

@@ -1,0 +1,323 @@
+// QMDFF force field: host set-up (parameter tables, the warp term schedule)
+// and the per-bead energy/gradient kernel behind cr_qmdff_* (C-ABI).
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "host_util.h"
+#include "qmdff_host.h"
+
+namespace {
+
+using cr::qmdff::kVAngl;
+using cr::qmdff::kVPair;
+
+// Term schedule of one kind: batches of 32 lanes; within a batch, terms of
+// one colour touch disjoint atoms.  Greedy: each colour takes, in order, the
+// remaining terms that do not touch an atom already used by that colour,
+// until the batch holds 32 terms.
+void schedule_kind(int nterm, int arity, const std::vector<int>& atoms, const std::vector<int>& order,
+                   int natoms, std::vector<int>& slot, std::vector<unsigned char>& color,
+                   std::vector<unsigned char>& ncol, int& nbatch, int& colours) {
+  std::vector<int> remaining = order;
+  std::vector<int> stamp((size_t)natoms, -1);
+  int stamp_id = 0;
+  nbatch = 0;
+  while (!remaining.empty()) {
+    std::vector<int> bt, bc;
+    int col = 0;
+    while ((int)bt.size() < 32 && !remaining.empty()) {
+      ++stamp_id;
+      std::vector<int> rest;
+      rest.reserve(remaining.size());
+      for (int t : remaining) {
+        bool ok = (int)bt.size() < 32;
+        for (int a = 0; ok && a < arity; ++a)
+          if (stamp[(size_t)atoms[(size_t)t * arity + a]] == stamp_id) ok = false;
+        if (!ok) {
+          rest.push_back(t);
+          continue;
+        }
+        for (int a = 0; a < arity; ++a) stamp[(size_t)atoms[(size_t)t * arity + a]] = stamp_id;
+        bt.push_back(t);
+        bc.push_back(col);
+      }
+      remaining.swap(rest);
+      ++col;
+    }
+    for (int l = 0; l < 32; ++l) {
+      slot.push_back(l < (int)bt.size() ? bt[(size_t)l] : -1);
+      color.push_back((unsigned char)(l < (int)bc.size() ? bc[(size_t)l] : 0));
+    }
+    ncol.push_back((unsigned char)col);
+    colours += col;
+    ++nbatch;
+  }
+  (void)nterm;
+}
+
+template <class T>
+int upload(cr_qmdff* ff, const std::vector<T>& h, const T** d) {
+  *d = nullptr;
+  if (h.empty()) return CR_OK;
+  void* p = nullptr;
+  CR_TRY_CUDA(cudaMalloc(&p, h.size() * sizeof(T)));
+  ff->allocs.push_back(p);
+  CR_TRY_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *d = (const T*)p;
+  return CR_OK;
+}
+
+template <class T>
+std::vector<float> to_float(const std::vector<T>& v) {
+  std::vector<float> o(v.size());
+  for (size_t i = 0; i < v.size(); ++i) o[i] = (float)v[i];
+  return o;
+}
+
+}  // namespace
+
+namespace cr {
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kQmdffWarps * 32) qmdff_egrad_kernel(qmdff::Dev D, int nbeads, const double* q,
+                                                                      double* e, double* g) {
+  extern __shared__ double qsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n3 = 3 * D.n;
+  double* xs = qsm + (size_t)warp * 2 * n3;
+  double* gs = xs + n3;
+  for (int b = blockIdx.x * kQmdffWarps + warp; b < nbeads; b += gridDim.x * kQmdffWarps) {
+    const double* qb = q + (size_t)b * n3;
+    for (int a = lane; a < n3; a += 32) xs[a] = qb[a];
+    __syncwarp();
+    const double v = qmdff::warp_egrad<MIXED>(D, xs, gs, g + (size_t)b * n3, 1.0, lane);
+    if (lane == 0) e[b] = v;
+    __syncwarp();
+  }
+}
+
+}  // namespace cr
+
+int qmdff_launch(const cr_qmdff* ff, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
+                 cudaStream_t s) {
+  if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
+  const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(ff->n);
+  // the attribute is set even for nbeads = 0, so a caller can prepare the
+  // kernel before a stream capture
+  if (smem > 48 * 1024) {
+    if (precision == CR_PREC_MIXED)
+      CR_TRY_CUDA(cudaFuncSetAttribute(cr::qmdff_egrad_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    else
+      CR_TRY_CUDA(cudaFuncSetAttribute(cr::qmdff_egrad_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+  }
+  if (nbeads <= 0) return CR_OK;
+  int grid = (nbeads + kQmdffWarps - 1) / kQmdffWarps;
+  if (grid > 1 << 20) grid = 1 << 20;
+  if (precision == CR_PREC_MIXED)
+    cr::qmdff_egrad_kernel<true><<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, nbeads, d_q, d_e, d_g);
+  else
+    cr::qmdff_egrad_kernel<false><<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, nbeads, d_q, d_e, d_g);
+  CR_TRY_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+extern "C" {
+
+int cr_qmdff_destroy(cr_qmdff* ff) {
+  if (!ff) return CR_OK;
+  for (void* p : ff->allocs) cudaFree(p);
+  delete ff;
+  return CR_OK;
+}
+
+int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
+  if (!d || !out) return cr_set_error(CR_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  const int n = d->natoms;
+  if (n < 1 || n > cr::qmdff::kMaxAtoms) return cr_set_error(CR_ERR_ARG, "natoms must be 1..1024");
+  if (d->nbond < 0 || d->nangl < 0 || d->ntors < 0 || d->nnci < 0)
+    return cr_set_error(CR_ERR_ARG, "negative term count");
+  if (!d->at || !d->q || !d->rad || (d->nbond && (!d->bond || !d->vbond)) || (d->nangl && (!d->angl || !d->vangl)) ||
+      (d->ntors && (!d->tors || !d->vtors)) ||
+      (d->nnci && (!d->nci || !d->r0ab || !d->zab || !d->r0094 || !d->sr42 || !d->c66ab)))
+    return cr_set_error(CR_ERR_ARG, "missing force-field array");
+  for (int i = 0; i < n; ++i)
+    if (d->at[i] < 1 || d->at[i] > 94) return cr_set_error(CR_ERR_ARG, "element number out of 1..94");
+  auto atom_ok = [&](int a) { return a >= 1 && a <= n; };
+  for (int m = 0; m < 2 * d->nbond; ++m)
+    if (!atom_ok(d->bond[m])) return cr_set_error(CR_ERR_ARG, "bond atom out of range");
+  for (int m = 0; m < 3 * d->nangl; ++m)
+    if (!atom_ok(d->angl[m])) return cr_set_error(CR_ERR_ARG, "angle atom out of range");
+  for (int m = 0; m < d->ntors; ++m) {
+    for (int a = 0; a < 4; ++a)
+      if (!atom_ok(d->tors[6 * m + a])) return cr_set_error(CR_ERR_ARG, "torsion atom out of range");
+    const int nt = d->tors[6 * m + 4];
+    if (d->tors[6 * m + 5] != 2 && (nt < 0 || nt > 4)) return cr_set_error(CR_ERR_ARG, "torsion term count not 0..4");
+  }
+  for (int m = 0; m < d->nnci; ++m) {
+    if (!atom_ok(d->nci[3 * m]) || !atom_ok(d->nci[3 * m + 1])) return cr_set_error(CR_ERR_ARG, "NCI atom out of range");
+    if (d->nci[3 * m + 2] < 1 || d->nci[3 * m + 2] > 6) return cr_set_error(CR_ERR_ARG, "NCI category not 1..6");
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return cr_set_error(CR_ERR_NO_DEVICE, "no CUDA device");
+
+  const double pi = 3.1415926535897932384626433832795029;
+  std::vector<double> rad((size_t)n), vbond(d->vbond, d->vbond + 3 * d->nbond), vtors(d->vtors, d->vtors + 14 * d->ntors);
+  for (int i = 0; i < n; ++i) rad[(size_t)i] = d->rad[d->at[i] - 1];
+  std::vector<double> vangl((size_t)kVAngl * d->nangl);
+  for (int m = 0; m < d->nangl; ++m) {
+    const double th0 = d->vangl[2 * m];
+    vangl[(size_t)kVAngl * m] = th0;
+    vangl[(size_t)kVAngl * m + 1] = d->vangl[2 * m + 1];
+    vangl[(size_t)kVAngl * m + 2] = std::cos(th0);
+    vangl[(size_t)kVAngl * m + 3] = (pi - th0 < 1e-6) ? 1.0 : 0.0;
+  }
+  std::vector<int> bond((size_t)2 * d->nbond), angl((size_t)3 * d->nangl), tors((size_t)6 * d->ntors),
+      pair((size_t)2 * d->nnci);
+  for (int m = 0; m < 2 * d->nbond; ++m) bond[(size_t)m] = d->bond[m] - 1;
+  for (int m = 0; m < 3 * d->nangl; ++m) angl[(size_t)m] = d->angl[m] - 1;
+  for (int m = 0; m < d->ntors; ++m) {
+    for (int a = 0; a < 4; ++a) tors[(size_t)6 * m + a] = d->tors[6 * m + a] - 1;
+    tors[(size_t)6 * m + 4] = d->tors[6 * m + 4];
+    tors[(size_t)6 * m + 5] = d->tors[6 * m + 5];
+  }
+  std::vector<double> vpair((size_t)kVPair * d->nnci, 0.0);
+  for (int m = 0; m < d->nnci; ++m) {
+    const int i1 = d->nci[3 * m] - 1, i2 = d->nci[3 * m + 1] - 1, nk = d->nci[3 * m + 2];
+    pair[(size_t)2 * m] = i1;
+    pair[(size_t)2 * m + 1] = i2;
+    const int z1 = d->at[i1] - 1, z2 = d->at[i2] - 1;
+    const size_t e12 = (size_t)z1 + 94 * (size_t)z2;  // (iz1, iz2) column-major
+    double* v = &vpair[(size_t)kVPair * m];
+    v[0] = d->r0094[e12];
+    v[1] = d->c66ab[(size_t)i2 + (size_t)n * i1];     // c66ab(i2, i1)
+    v[2] = d->sr42[e12];
+    v[3] = d->zab[e12];
+    v[4] = d->r0ab[e12];
+    v[5] = d->eps2[nk - 1];
+    v[6] = d->zahn ? d->q[i1] * d->q[i2] : d->q[i1] * d->q[i2] * d->eps1[nk - 1];
+  }
+
+  cr_qmdff* ff = new cr_qmdff();
+  ff->n = n;
+  ff->nterm[0] = d->nbond;
+  ff->nterm[1] = d->nangl;
+  ff->nterm[2] = d->ntors;
+  ff->nterm[3] = d->nnci;
+
+  // schedule: torsions grouped by (type, nt) so a batch runs one code path
+  std::vector<int> slot;
+  std::vector<unsigned char> color, ncol;
+  cr::qmdff::Dev& D = ff->dev;
+  D.n = n;
+  int boff = 0;
+  for (int kind = 0; kind < 4; ++kind) {
+    std::vector<int> order((size_t)ff->nterm[kind]);
+    for (int m = 0; m < ff->nterm[kind]; ++m) order[(size_t)m] = m;
+    std::vector<int> atoms;
+    int arity = 2;
+    if (kind == 0) atoms = bond;
+    if (kind == 1) {
+      arity = 3;
+      atoms = angl;
+    }
+    if (kind == 2) {
+      arity = 4;
+      atoms.resize((size_t)4 * d->ntors);
+      for (int m = 0; m < d->ntors; ++m)
+        for (int a = 0; a < 4; ++a) atoms[(size_t)4 * m + a] = tors[(size_t)6 * m + a];
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const int kx = tors[(size_t)6 * x + 5] * 8 + tors[(size_t)6 * x + 4];
+        const int ky = tors[(size_t)6 * y + 5] * 8 + tors[(size_t)6 * y + 4];
+        return kx < ky;
+      });
+    }
+    if (kind == 3) atoms = pair;
+    int nb = 0;
+    schedule_kind(ff->nterm[kind], arity, atoms, order, n, slot, color, ncol, nb, ff->ncolors);
+    D.nb[kind] = nb;
+    D.boff[kind] = boff;
+    boff += nb;
+  }
+
+  int rc = CR_OK;
+  auto up = [&](auto& h, auto** dp) {
+    if (rc == CR_OK) rc = upload(ff, h, dp);
+  };
+  up(slot, &D.slot);
+  up(color, &D.color);
+  up(ncol, &D.ncol);
+  up(bond, &D.bond);
+  up(angl, &D.angl);
+  up(tors, &D.tors);
+  up(pair, &D.pair);
+  up(rad, &D.d.rad);
+  up(vbond, &D.d.vbond);
+  up(vangl, &D.d.vangl);
+  up(vtors, &D.d.vtors);
+  up(vpair, &D.d.vpair);
+  std::vector<float> frad = to_float(rad), fvbond = to_float(vbond), fvangl = to_float(vangl),
+                     fvtors = to_float(vtors), fvpair = to_float(vpair);
+  up(frad, &D.f.rad);
+  up(fvbond, &D.f.vbond);
+  up(fvangl, &D.f.vangl);
+  up(fvtors, &D.f.vtors);
+  up(fvpair, &D.f.vpair);
+  if (rc != CR_OK) {
+    cr_qmdff_destroy(ff);
+    return rc;
+  }
+  D.coul_cut = d->coul_cut;
+  D.zahn = d->zahn ? 1 : 0;
+  D.zahn_a = d->zahn_a;
+  D.zahn_par = d->zahn_par;
+  D.e_zero = d->e_zero;
+  *out = ff;
+  return CR_OK;
+}
+
+int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (batches)
+    for (int k = 0; k < 4; ++k) batches[k] = ff->dev.nb[k];
+  if (colors) *colors = ff->ncolors;
+  return CR_OK;
+}
+
+int cr_qmdff_egrad_device(cr_qmdff* ff, const double* d_xyz, int nbeads, double* d_e, double* d_g, int precision,
+                          void* stream) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (nbeads < 0 || (nbeads > 0 && (!d_xyz || !d_e || !d_g))) return cr_set_error(CR_ERR_ARG, "bad egrad arguments");
+  return qmdff_launch(ff, d_xyz, nbeads, d_e, d_g, precision, (cudaStream_t)stream);
+}
+
+int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (nbeads < 0 || (nbeads > 0 && (!xyz || !e || !g))) return cr_set_error(CR_ERR_ARG, "bad egrad arguments");
+  if (nbeads == 0) return CR_OK;
+  const size_t nq = (size_t)3 * ff->n * nbeads;
+  double *d_q = nullptr, *d_e = nullptr, *d_g = nullptr;
+  CR_TRY_CUDA(cudaMalloc(&d_q, nq * sizeof(double)));
+  cudaError_t e1 = cudaMalloc(&d_e, (size_t)nbeads * sizeof(double));
+  cudaError_t e2 = cudaMalloc(&d_g, nq * sizeof(double));
+  int rc = CR_OK;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    rc = cr_set_error(CR_ERR_CUDA, "cudaMalloc failed in cr_qmdff_egrad");
+  } else if (cudaMemcpy(d_q, xyz, nq * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = cr_set_error(CR_ERR_CUDA, "copy of xyz failed");
+  } else if ((rc = qmdff_launch(ff, d_q, nbeads, d_e, d_g, precision, nullptr)) == CR_OK) {
+    if (cudaMemcpy(e, d_e, (size_t)nbeads * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(g, d_g, nq * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = cr_set_error(CR_ERR_CUDA, "copy of results failed");
+  }
+  cudaFree(d_q);
+  cudaFree(d_e);
+  cudaFree(d_g);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,570 @@
+// QMDFF force field on the GB300: one warp per bead.
+//
+// Drop-in for Caracal's per-bead QMDFF gradient (src/gradient.f90:342-358:
+// ff_eg src/ff_eg.f90:41-629, ff_nonb src/ff_nonb.f90:34-889, E_zero shift),
+// non-periodic, one molecule.  A bead's coordinates and gradient live in the
+// warp's shared memory.  The host packs the terms of each kind into batches
+// of 32 (one term per lane) and colours each batch so that no atom appears
+// twice within a colour; a lane computes its term, then the warp scatters the
+// term gradients colour by colour.  No atomics, fixed accumulation order:
+// results are deterministic run to run.
+//
+// Precision: the plain form computes every term in FP64 with Caracal's
+// formulas.  The mixed form computes each term in FP32 from FP64 displacement
+// vectors, with cancellation-free rewrites where the FP64 formula subtracts
+// nearly equal numbers (bond stretch from an FP64 r^2 - r0^2, dihedral angle
+// from atan2 instead of acos), and accumulates the gradient with compensated
+// (Neumaier) FP32 sums and the energy in FP64.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "../../include/caracal_gb300.h"
+
+namespace cr {
+namespace qmdff {
+
+constexpr int kMaxAtoms = 1024;
+constexpr int kVAngl = 4;   // theta0, k, cos(theta0), linear flag
+constexpr int kVPair = 8;   // R0, C6, sr42, zab, alpha, eps2, qq (eps1 q_i q_j or q_i q_j), 0
+
+// Per-term parameter tables in the arithmetic type of the form.
+template <class F>
+struct Tables {
+  const F* rad;    // covalent radius per atom (bohr)
+  const F* vbond;  // 3 per bond: r0, k, a
+  const F* vangl;  // kVAngl per angle
+  const F* vtors;  // 14 per torsion: phi0, V, (rn, phase, Vn) x 4
+  const F* vpair;  // kVPair per NCI pair
+};
+
+struct Dev {
+  int n;
+  int nb[4];       // batches per kind: bonds, angles, torsions, NCI pairs
+  int boff[4];     // first batch of each kind
+  const int* slot;             // [batches][32]: term index or -1
+  const unsigned char* color;  // [batches][32]
+  const unsigned char* ncol;   // [batches]
+  const int* bond;   // 2 per bond (0-based)
+  const int* angl;   // 3 per angle (centre, i, k)
+  const int* tors;   // 6 per torsion: i, j, k, l, nt, type
+  const int* pair;   // 2 per NCI pair
+  Tables<double> d;
+  Tables<float> f;
+  double coul_cut, zahn_a, zahn_par, e_zero;
+  int zahn;
+};
+
+template <class F> __device__ inline F q_sqrt(F x);
+template <> __device__ inline double q_sqrt<double>(double x) { return sqrt(x); }
+template <> __device__ inline float q_sqrt<float>(float x) { return sqrtf(x); }
+template <class F> __device__ inline F q_exp(F x);
+template <> __device__ inline double q_exp<double>(double x) { return exp(x); }
+template <> __device__ inline float q_exp<float>(float x) { return expf(x); }
+template <class F> __device__ inline F q_acos(F x);
+template <> __device__ inline double q_acos<double>(double x) { return acos(x); }
+template <> __device__ inline float q_acos<float>(float x) { return acosf(x); }
+template <class F> __device__ inline F q_asin(F x);
+template <> __device__ inline double q_asin<double>(double x) { return asin(x); }
+template <> __device__ inline float q_asin<float>(float x) { return asinf(x); }
+template <class F> __device__ inline F q_erf(F x);
+template <> __device__ inline double q_erf<double>(double x) { return erf(x); }
+template <> __device__ inline float q_erf<float>(float x) { return erff(x); }
+template <class F> __device__ inline F q_erfc(F x);
+template <> __device__ inline double q_erfc<double>(double x) { return erfc(x); }
+template <> __device__ inline float q_erfc<float>(float x) { return erfcf(x); }
+template <class F> __device__ inline F q_sin(F x);
+template <> __device__ inline double q_sin<double>(double x) { return sin(x); }
+template <> __device__ inline float q_sin<float>(float x) { return sinf(x); }
+template <class F> __device__ inline F q_cos(F x);
+template <> __device__ inline double q_cos<double>(double x) { return cos(x); }
+template <> __device__ inline float q_cos<float>(float x) { return cosf(x); }
+
+template <class F>
+__device__ inline void cross(const F* a, const F* b, F* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+template <class F>
+__device__ inline F dot3(const F* a, const F* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Gradient contribution of one term: up to four atoms.
+template <class F>
+struct Contrib {
+  int na;
+  int a[4];
+  F g[4][3];
+};
+
+// Gradient accumulator of one bead in shared memory: FP64 in the plain form,
+// compensated FP32 (sum and compensation arrays) in the mixed form.
+template <class F>
+struct Grad;
+template <>
+struct Grad<double> {
+  double* g;
+  __device__ inline void add(int i, double v) { g[i] += v; }
+  __device__ inline double get(int i) const { return g[i]; }
+};
+template <>
+struct Grad<float> {
+  float* s;
+  float* k;
+  __device__ inline void add(int i, float v) {
+    float a = s[i], t = a + v;
+    k[i] += (fabsf(a) >= fabsf(v)) ? ((a - t) + v) : ((v - t) + a);
+    s[i] = t;
+  }
+  __device__ inline double get(int i) const { return (double)s[i] + (double)k[i]; }
+};
+
+template <class F>
+__device__ inline void scatter(const Contrib<F>& c, Grad<F>& G) {
+  for (int m = 0; m < c.na; ++m)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
+}
+
+// abdamp (src/abdamp.f90:36-51); the cutoff prefactor is the REAL(4) product 3.0*3.5710642
+template <class F>
+__device__ inline void abdamp(F radi, F radj, F r2, F& damp, F& ddamp) {
+  const F pre = (F)(double)(3.0f * 3.5710642f);
+  const F s = radi + radj;
+  const F rcut = pre * (s * s);
+  const F rr = (r2 / rcut) * (r2 / rcut);
+  damp = F(1) / (F(1) + rr);
+  ddamp = F(-4) * rr / (r2 * ((F(1) + rr) * (F(1) + rr)));
+}
+
+template <class F>
+__device__ inline void disp(const double* x, int a, int b, F* v) {
+  v[0] = (F)(x[3 * a] - x[3 * b]);
+  v[1] = (F)(x[3 * a + 1] - x[3 * b + 1]);
+  v[2] = (F)(x[3 * a + 2] - x[3 * b + 2]);
+}
+
+// Bond stretch, generalised Lennard-Jones (src/ff_eg.f90:87-163):
+// e = k (1 + (r0/r)^a - 2 (r0/r)^(a/2)).
+__device__ inline double bond_f64(const Dev& D, const double* x, int m, Contrib<double>& c) {
+  const int i = D.bond[2 * m], j = D.bond[2 * m + 1];
+  double rb[3];
+  disp<double>(x, i, j, rb);
+  const double r2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+  const double r = sqrt(r2);
+  const double* v = &D.d.vbond[3 * m];
+  const double rij = v[0], kij = v[1], aai = v[2];
+  const double pa = pow(rij / r, aai), pa2 = pow(rij / r, aai / 2);
+  const double fac = aai * kij * (-pa + pa2) / r2;
+  c.na = 2;
+  c.a[0] = i;
+  c.a[1] = j;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    c.g[0][d] = fac * rb[d];
+    c.g[1][d] = -fac * rb[d];
+  }
+  return kij * (1. + pa - 2. * pa2);
+}
+
+// Mixed form: with u = (r0/r)^(a/2) = exp(-(a/2) log1p(x)), x = (r - r0)/r0
+// taken from the FP64 r^2 - r0^2, e = k (1 - u)^2 and the gradient factor
+// a k u (1 - u) / r^2 are free of the cancellation in 1 + u^2 - 2u.
+__device__ inline double bond_mixed(const Dev& D, const double* x, int m, Contrib<float>& c) {
+  const int i = D.bond[2 * m], j = D.bond[2 * m + 1];
+  double rd[3];
+  disp<double>(x, i, j, rd);
+  const double r2d = rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2];
+  const double r0d = D.d.vbond[3 * m];
+  const float r2 = (float)r2d;
+  const float r = sqrtf(r2);
+  const float r0 = (float)r0d;
+  const float dr = (float)(r2d - r0d * r0d) / (r + r0);  // r - r0
+  const float kij = D.f.vbond[3 * m + 1], aai = D.f.vbond[3 * m + 2];
+  const float lg = -0.5f * aai * log1pf(dr / r0);
+  const float omu = -expm1f(lg);  // 1 - u
+  const float u = 1.0f - omu;
+  const float fac = aai * kij * u * omu / r2;  // a k (u - u^2) / r^2
+  c.na = 2;
+  c.a[0] = i;
+  c.a[1] = j;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float rb = (float)rd[d];
+    c.g[0][d] = fac * rb;
+    c.g[1][d] = -fac * rb;
+  }
+  return (double)(kij * omu * omu);
+}
+
+// Angle bend with abdamp damping (src/ff_eg.f90:167-299).
+template <class F>
+__device__ inline F angle_term(const Dev& D, const Tables<F>& T, const double* x, int m, Contrib<F>& c) {
+  const int j = D.angl[3 * m], i = D.angl[3 * m + 1], k = D.angl[3 * m + 2];
+  const F* v = &T.vangl[kVAngl * m];
+  const F c0 = v[0], kijk = v[1], cc0 = v[2];
+  F vab[3], vcb[3], vp[3];
+  disp<F>(x, i, j, vab);
+  disp<F>(x, k, j, vcb);
+  const F rab2 = dot3(vab, vab), rcb2 = dot3(vcb, vcb);
+  cross(vcb, vab, vp);
+  const F vpl = dot3(vp, vp);
+  const F rp = (vpl > F(0) ? q_sqrt<F>(vpl) : F(0)) + F(1e-14);
+  const F al = q_sqrt<F>(rab2), bl = q_sqrt<F>(rcb2);
+  F cosa = (al > F(0) && bl > F(0)) ? dot3(vab, vcb) / (al * bl) : F(0);
+  cosa = fmin(F(1), fmax(F(-1), cosa));
+  const F theta = q_acos<F>(cosa);
+  F dampij, damp2ij, dampjk, damp2jk;
+  abdamp<F>(T.rad[i], T.rad[j], rab2, dampij, damp2ij);
+  abdamp<F>(T.rad[k], T.rad[j], rcb2, dampjk, damp2jk);
+  const F damp = dampij * dampjk;
+  F ea, deddt;
+  if (v[3] != F(0)) {  // linear reference angle: harmonic in theta
+    const F dt = theta - c0;
+    ea = kijk * (dt * dt);
+    deddt = F(2) * kijk * dt;
+  } else {
+    const F dd = cosa - cc0;
+    ea = kijk * (dd * dd);
+    deddt = F(2) * kijk * q_sin<F>(theta) * (cc0 - cosa);
+  }
+  F deda[3], dedc[3];
+  cross(vab, vp, deda);
+  cross(vcb, vp, dedc);
+  const F rmul1 = -deddt / (rab2 * rp), rmul2 = deddt / (rcb2 * rp);
+  c.na = 3;
+  c.a[0] = i;
+  c.a[1] = j;
+  c.a[2] = k;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const F da = deda[d] * rmul1, dc = dedc[d] * rmul2;
+    const F t1 = ea * damp2ij * dampjk * vab[d];
+    const F t2 = ea * damp2jk * dampij * vcb[d];
+    c.g[0][d] = da * damp + t1;
+    c.g[1][d] = -(da + dc) * damp - t1 - t2;
+    c.g[2][d] = dc * damp + t2;
+  }
+  return ea * damp;
+}
+
+// Torsion angle phi in [0, pi] of i-j-k-l (valijkl, src/valijkl.f90) with
+// its cosine and sine.  FP64: Caracal's acos of the normalised plane normals.
+// FP32: atan2(|rb| |na . rc|, na . nb), accurate near 0 and pi.
+template <class F>
+__device__ inline F dihedral(const F* ra, const F* rb, const F* rc, F* na, F* nb, F& nan_, F& nbn,
+                             F& cosphi, F& sinphi) {
+  cross(ra, rb, na);
+  cross(rb, rc, nb);
+  nan_ = q_sqrt<F>(dot3(na, na));
+  nbn = q_sqrt<F>(dot3(nb, nb));
+  F phi;
+  if constexpr (std::is_same<F, double>::value) {
+    double a[3] = {na[0], na[1], na[2]}, b[3] = {nb[0], nb[1], nb[2]};
+    if (fabs(nan_) > 1e-14) {
+      const double o = 1.0 / nan_;
+      a[0] *= o;
+      a[1] *= o;
+      a[2] *= o;
+    }
+    if (fabs(nbn) > 1e-14) {
+      const double o = 1.0 / nbn;
+      b[0] *= o;
+      b[1] *= o;
+      b[2] *= o;
+    }
+    double s = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    if (fabs(fabs(s) - 1.0) < 1e-14) s = s >= 0 ? 1.0 : -1.0;
+    phi = acos(s);
+    cosphi = cos(phi);
+    sinphi = sin(phi);
+  } else {
+    const float cn = dot3(na, nb);
+    const float sn = sqrtf(dot3(rb, rb)) * fabsf(dot3(na, rc));
+    phi = atan2f(sn, cn);
+    const float den = nan_ * nbn;
+    cosphi = den > 0.f ? cn / den : 1.f;
+    sinphi = den > 0.f ? sn / den : 0.f;
+  }
+  return phi;
+}
+
+// Torsions (erf-blended cosine series, src/ff_eg.f90:303-440) and
+// inversions (tors type 2, src/ff_eg.f90:441-618).
+template <class F>
+__device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const double* x, int m, Contrib<F>& c) {
+  const F pi = (F)3.1415926535897932384626433832795029;
+  const F pi2 = (F)6.28318530717958623199592693708837;
+  const F spi = (F)1.77245385090551599275151910313925;
+  const int i = D.tors[6 * m], j = D.tors[6 * m + 1], k = D.tors[6 * m + 2], l = D.tors[6 * m + 3];
+  const int nt = D.tors[6 * m + 4], type = D.tors[6 * m + 5];
+  const F* vt = &T.vtors[14 * m];
+  const F phi0 = vt[0];
+  F vab[3], vcb[3], vdc[3], dda[3], ddb[3], ddc[3], ddd[3];
+  F et, dij, dampij, dampjk, dampX, d2ij, d2jk, d2X;
+  c.na = 4;
+  c.a[0] = i;
+  c.a[1] = j;
+  c.a[2] = k;
+  c.a[3] = l;
+  if (type != 2) {
+    disp<F>(x, i, j, vab);
+    disp<F>(x, j, k, vcb);
+    disp<F>(x, k, l, vdc);
+    abdamp<F>(T.rad[i], T.rad[j], dot3(vab, vab), dampij, d2ij);
+    abdamp<F>(T.rad[k], T.rad[j], dot3(vcb, vcb), dampjk, d2jk);
+    abdamp<F>(T.rad[k], T.rad[l], dot3(vdc, vdc), dampX, d2X);
+    // dphidr (src/dphidr.f90): ra = r_j - r_i, rb = r_k - r_j, rc = r_l - r_k
+    const F ra[3] = {-vab[0], -vab[1], -vab[2]}, rb[3] = {-vcb[0], -vcb[1], -vcb[2]};
+    const F rc[3] = {-vdc[0], -vdc[1], -vdc[2]};
+    F na[3], nb[3], nan_, nbn, cosphi, sinphi;
+    const F phi = dihedral<F>(ra, rb, rc, na, nb, nan_, nbn, cosphi, sinphi);
+    const F nenner = nan_ * nbn * sinphi;
+    if (fabs((double)nenner) < 1e-14) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = F(0);
+    } else {
+      const F on = F(1) / nenner, rba_ = nbn / nan_, rab_ = nan_ / nbn;
+      const F rapb[3] = {ra[0] + rb[0], ra[1] + rb[1], ra[2] + rb[2]};
+      const F rbpc[3] = {rb[0] + rc[0], rb[1] + rc[1], rb[2] + rc[2]};
+      F t_rab[3], t_rba[3], t_rac[3], t_rbb[3], t_rbc[3], t_raa[3], rapba[3], rapbb[3], rbpca[3], rbpcb[3];
+      cross(na, rb, t_rab);
+      cross(nb, ra, t_rba);
+      cross(na, rc, t_rac);
+      cross(nb, rb, t_rbb);
+      cross(nb, rc, t_rbc);
+      cross(na, ra, t_raa);
+      cross(rapb, na, rapba);
+      cross(rapb, nb, rapbb);
+      cross(rbpc, na, rbpca);
+      cross(rbpc, nb, rbpcb);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        dda[d] = on * (cosphi * rba_ * t_rab[d] - t_rbb[d]);
+        ddb[d] = on * (cosphi * (rba_ * rapba[d] + rab_ * t_rbc[d]) - (t_rac[d] + rapbb[d]));
+        ddc[d] = on * (cosphi * (rba_ * t_raa[d] + rab_ * rbpcb[d]) - (t_rba[d] + rbpca[d]));
+        ddd[d] = on * (cosphi * rab_ * t_rbb[d] - t_rab[d]);
+      }
+    }
+    et = F(0);
+    dij = F(0);
+    const F phipi = phi - pi;
+    const F ef = q_erf<F>(phipi);
+    const F expo = q_exp<F>(-(phipi * phipi)) / spi;
+    for (int it = 0; it < nt; ++it) {
+      const F rn = vt[2 + 3 * it], ph = vt[3 + 3 * it], vn = vt[4 + 3 * it];
+      const F c1 = rn * (phi - phi0) + ph;
+      const F c2 = rn * (phi + phi0 - pi2) + ph;
+      const F x1cos = q_cos<F>(c1), x2cos = q_cos<F>(c2), x1sin = q_sin<F>(c1), x2sin = q_sin<F>(c2);
+      const F e1 = vn * (F(1) + x1cos), e2 = vn * (F(1) + x2cos);
+      et = et + F(0.5) * (F(1) - ef) * e1 + (F(0.5) + F(0.5) * ef) * e2;
+      dij = dij - expo * e1 - F(0.5) * (F(1) - ef) * vn * x1sin * rn + expo * e2 -
+            (F(0.5) + F(0.5) * ef) * vn * x2sin * rn;
+    }
+    et = et * vt[1];
+    const F damp = dampjk * dampij * dampX;
+    dij = dij * vt[1] * damp;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const F t1 = et * d2ij * dampjk * dampX * vab[d];
+      const F t2 = et * d2jk * dampij * dampX * vcb[d];
+      const F t3 = et * d2X * dampij * dampjk * vdc[d];
+      c.g[0][d] = dij * dda[d] + t1;
+      c.g[1][d] = dij * ddb[d] - t1 + t2;
+      c.g[2][d] = dij * ddc[d] + t3 - t2;
+      c.g[3][d] = dij * ddd[d] - t3;
+    }
+    return et * damp;
+  }
+  // inversion: omega (src/omega.f90) and domegadr (src/domegadr.f90)
+  disp<F>(x, j, i, vab);
+  disp<F>(x, j, k, vcb);
+  disp<F>(x, j, l, vdc);
+  abdamp<F>(T.rad[i], T.rad[j], dot3(vab, vab), dampij, d2ij);
+  abdamp<F>(T.rad[k], T.rad[j], dot3(vcb, vcb), dampjk, d2jk);
+  abdamp<F>(T.rad[j], T.rad[l], dot3(vdc, vdc), dampX, d2X);
+  const F re[3] = {-vab[0], -vab[1], -vab[2]};  // r_i - r_j
+  const F rd[3] = {-vcb[0], -vcb[1], -vcb[2]};  // r_k - r_j
+  F rv[3];
+  disp<F>(x, l, i, rv);                          // r_l - r_i
+  F rn[3];
+  cross(re, rd, rn);
+  const F rnn = q_sqrt<F>(dot3(rn, rn)), rvn = q_sqrt<F>(dot3(rv, rv));
+  F om;
+  if constexpr (std::is_same<F, double>::value) {
+    double a[3] = {rn[0], rn[1], rn[2]}, b[3] = {rv[0], rv[1], rv[2]};
+    if (fabs(rnn) > 1e-14) {
+      const double o = 1.0 / rnn;
+      a[0] *= o;
+      a[1] *= o;
+      a[2] *= o;
+    }
+    if (fabs(rvn) > 1e-14) {
+      const double o = 1.0 / rvn;
+      b[0] *= o;
+      b[1] *= o;
+      b[2] *= o;
+    }
+    om = asin(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+  } else {
+    om = q_asin<F>(fmin(F(1), fmax(F(-1), dot3(rn, rv) / (rnn * rvn))));
+  }
+  const F sinom = q_sin<F>(om), cosom = q_cos<F>(om);
+  const F rdme[3] = {rd[0] - re[0], rd[1] - re[1], rd[2] - re[2]};
+  F rve[3], rne[3], rdv[3], rdn[3], rvdme[3], rndme[3];
+  cross(rv, re, rve);
+  cross(rn, re, rne);
+  cross(rd, rv, rdv);
+  cross(rd, rn, rdn);
+  cross(rv, rdme, rvdme);
+  cross(rn, rdme, rndme);
+  const F nenner = rnn * rvn * cosom;
+  if (fabs((double)nenner) > 1e-14) {
+    const F on = F(1) / nenner;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      dda[d] = on * (rdv[d] - rn[d] - sinom * (rvn / rnn * rdn[d] - rnn / rvn * rv[d]));
+      ddb[d] = on * (rvdme[d] - sinom * rvn / rnn * rndme[d]);
+      ddc[d] = on * (rve[d] - sinom * rvn / rnn * rne[d]);
+      ddd[d] = on * (rn[d] - sinom * rnn / rvn * rv[d]);
+    }
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = F(0);
+  }
+  const F damp = dampjk * dampij * dampX;
+  if (vt[2] > F(1e-6)) {
+    const F c1 = (om - phi0) + pi;
+    et = (F(1) + q_cos<F>(c1)) * vt[1];
+    dij = -q_sin<F>(c1) * vt[1] * damp;
+  } else {
+    const F dd = q_cos<F>(om) - q_cos<F>(phi0);
+    et = vt[1] * (dd * dd);
+    dij = F(2) * vt[1] * q_sin<F>(om) * (q_cos<F>(phi0) - q_cos<F>(om)) * damp;
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const F t1 = et * d2ij * dampjk * dampX * vab[d];
+    const F t2 = et * d2jk * dampij * dampX * vcb[d];
+    const F t3 = et * d2X * dampij * dampjk * vdc[d];
+    c.g[0][d] = dij * dda[d] - t1;
+    c.g[1][d] = dij * ddb[d] + t1 + t2 + t3;
+    c.g[2][d] = dij * ddc[d] - t2;
+    c.g[3][d] = dij * ddd[d] - t3;
+  }
+  return et * damp;
+}
+
+// One NCI pair (src/ff_nonb.f90): BJ-damped C6/C8 dispersion and, for
+// r < 25 bohr, exponential repulsion, both times eps2 (:79-193); Coulomb
+// within coul_cut (:337-416), eps1 q_i q_j / r or the Zahn form.
+template <class F>
+__device__ inline F pair_term(const Dev& D, const Tables<F>& T, const double* x, int kp, Contrib<F>& c) {
+  const int i1 = D.pair[2 * kp], i2 = D.pair[2 * kp + 1];
+  const F* v = &T.vpair[kVPair * kp];
+  F vab[3];
+  disp<F>(x, i1, i2, vab);
+  const F r2 = dot3(vab, vab);
+  const F r = q_sqrt<F>(r2);
+  const F oner = F(1) / r;
+  const F R0 = v[0], c6 = v[1], eps2 = v[5];
+  const F r4 = r2 * r2, r6 = r4 * r2;
+  const F R02 = R0 * R0, r06 = R02 * R02 * R02;
+  const F t6 = r6 + r06;
+  const F t8 = r6 * r2 + r06 * R0 * R0;
+  const F c6t6 = c6 / t6, c6t8 = c6 / t8;
+  const F t27 = v[2] * c6t8;
+  F e = -(c6t6 + t27) * eps2;
+  F drij = eps2 * (c6t6 * F(6) * r4 / t6 + F(8) * t27 * r6 / t8);
+  if (r < F(25)) {
+    const F alpha = v[4];
+    const F t = v[3] * q_exp<F>(-alpha * r);
+    e = e + t * oner * eps2;
+    drij = drij - eps2 * t * (alpha * r + F(1)) * oner / r2;
+  }
+  if (!(r > (F)D.coul_cut)) {
+    F e0;
+    if (D.zahn) e0 = v[6] * ((q_erfc<F>((F)D.zahn_a * r) * oner) - (F)D.zahn_par * (r - (F)D.coul_cut));
+    else e0 = v[6] * oner;
+    e = e + e0;
+    drij = drij - e0 / r2;
+  }
+  c.na = 2;
+  c.a[0] = i1;
+  c.a[1] = i2;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    c.g[0][d] = vab[d] * drij;
+    c.g[1][d] = -vab[d] * drij;
+  }
+  return e;
+}
+
+// Energy of one term of kind `kind` (0 bond, 1 angle, 2 torsion, 3 pair).
+template <bool MIXED>
+__device__ inline double term(const Dev& D, int kind, const double* x, int m,
+                              Contrib<typename std::conditional<MIXED, float, double>::type>& c) {
+  if constexpr (MIXED) {
+    switch (kind) {
+      case 0: return bond_mixed(D, x, m, c);
+      case 1: return (double)angle_term<float>(D, D.f, x, m, c);
+      case 2: return (double)torsion_term<float>(D, D.f, x, m, c);
+      default: return (double)pair_term<float>(D, D.f, x, m, c);
+    }
+  } else {
+    switch (kind) {
+      case 0: return bond_f64(D, x, m, c);
+      case 1: return angle_term<double>(D, D.d, x, m, c);
+      case 2: return torsion_term<double>(D, D.d, x, m, c);
+      default: return pair_term<double>(D, D.d, x, m, c);
+    }
+  }
+}
+
+// Shared memory per warp (bytes): coordinates (3n doubles) + gradient
+// (3n doubles, or 2 x 3n floats in the mixed form).
+__host__ __device__ inline size_t warp_smem_bytes(int n) { return (size_t)3 * n * 8 * 2; }
+
+// Energy (with E_zero) and gradient (times gscale) of one bead by one warp.
+// xs: the bead's coordinates in shared memory; gs: 3n doubles of shared
+// scratch; gout: the gradient destination.  Returns the energy on every lane.
+template <bool MIXED>
+__device__ inline double warp_egrad(const Dev& D, const double* xs, void* gs, double* gout, double gscale,
+                                    int lane) {
+  using F = typename std::conditional<MIXED, float, double>::type;
+  const int n3 = 3 * D.n;
+  Grad<F> G;
+  if constexpr (MIXED) {
+    G.s = (float*)gs;
+    G.k = (float*)gs + n3;
+    for (int a = lane; a < 2 * n3; a += 32) ((float*)gs)[a] = 0.f;
+  } else {
+    G.g = (double*)gs;
+    for (int a = lane; a < n3; a += 32) G.g[a] = 0.0;
+  }
+  __syncwarp();
+  double e = 0.0;
+  for (int kind = 0; kind < 4; ++kind) {
+    const int b0 = D.boff[kind], nb = D.nb[kind];
+    for (int b = b0; b < b0 + nb; ++b) {
+      const int m = D.slot[32 * b + lane];
+      const int col = D.color[32 * b + lane];
+      const int ncol = D.ncol[b];
+      Contrib<F> c;
+      c.na = 0;
+      if (m >= 0) e += term<MIXED>(D, kind, xs, m, c);
+      for (int k = 0; k < ncol; ++k) {
+        if (m >= 0 && col == k) scatter(c, G);
+        __syncwarp();
+      }
+    }
+  }
+  for (int a = lane; a < n3; a += 32) gout[a] = gscale * G.get(a);
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  return e + D.e_zero;
+}
+
+}  // namespace qmdff
+}  // namespace cr

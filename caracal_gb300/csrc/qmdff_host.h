@@ -1,0 +1,23 @@
+// Device-resident QMDFF force field (the object behind cr_qmdff) and its
+// launch entry for the engine.
+#pragma once
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "qmdff.cuh"
+
+struct cr_qmdff {
+  int n = 0;
+  int nterm[4] = {0, 0, 0, 0};  // bonds, angles, torsions, NCI pairs
+  int ncolors = 0;              // colours summed over batches
+  cr::qmdff::Dev dev{};
+  std::vector<void*> allocs;    // device buffers owned by the force field
+};
+
+// Warps per block of the QMDFF force kernel and its dynamic shared memory.
+constexpr int kQmdffWarps = 4;
+
+// e[b] (with E_zero) and g = dV/dq for nbeads beads of d_q(3, n, nbeads).
+int qmdff_launch(const cr_qmdff* ff, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
+                 cudaStream_t s);

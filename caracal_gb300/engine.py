@@ -55,13 +55,95 @@ def egrad_ch4h(q):
     return V, g
 
 
+class QMDFFForceField:
+    """A QMDFF resident on the device (cr_qmdff): Caracal's ff_eg + ff_nonb +
+    E_zero (src/gradient.f90:342-358) for one molecule, no H-bond terms.
+
+    ``ff`` is a :class:`caracal_gb300.qmdff.QMDFF` (1-based topology, as read
+    from a .qmdff file); ``tables`` the element-pair tables ff_nonb takes
+    (:class:`caracal_gb300.qmdff.ElementTables`).  NVT runs use eps1-scaled
+    Coulomb within 50 bohr; Caracal's NVE runs use ``zahn=True`` with
+    ``coul_cut=10``, ``zahn_a = zahn_par = 0``.
+    """
+
+    def __init__(self, ff, tables=None, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
+        from . import qmdff as Q
+        tables = tables if tables is not None else Q.ElementTables.d3_like()
+        ip = lambda a: np.ascontiguousarray(a, dtype=np.int32)  # noqa: E731
+        fp = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+        self.n = int(ff.n)
+        tors = np.asarray(ff.tors).reshape(-1, 6)
+        self._arrs = dict(
+            at=ip(ff.at), q=fp(ff.q), rad=fp(Q.element_radii()),
+            bond=ip(np.asarray(ff.bond).reshape(-1, 2)), vbond=fp(np.asarray(ff.vbond).reshape(-1, 3)),
+            angl=ip(np.asarray(ff.angl).reshape(-1, 3)), vangl=fp(np.asarray(ff.vangl).reshape(-1, 2)),
+            tors=ip(tors), vtors=fp(np.asarray(ff.vtors).reshape(-1, 14)),
+            nci=ip(np.asarray(ff.nci).reshape(-1, 3)),
+            r0ab=fp(tables.r0ab[1:, 1:].T), zab=fp(tables.zab[1:, 1:].T),
+            r0094=fp(tables.r094[1:, 1:].T), sr42=fp(tables.sr42[1:, 1:].T), c66ab=fp(np.asarray(ff.c6).T))
+        a = self._arrs
+        d = L.CrQmdffDef()
+        d.natoms = self.n
+        d.nbond, d.nangl, d.ntors, d.nnci = len(a["bond"]), len(a["angl"]), len(a["tors"]), len(a["nci"])
+        for k in ("at", "bond", "angl", "tors", "nci"):
+            setattr(d, k, L.iptr(a[k]))
+        for k in ("q", "rad", "vbond", "vangl", "vtors", "r0ab", "zab", "r0094", "sr42", "c66ab"):
+            setattr(d, k, L.dptr(a[k]))
+        e1, e2 = Q.eps_factors()
+        for k in range(6):
+            d.eps1[k], d.eps2[k] = e1[k + 1], e2[k + 1]
+        d.coul_cut, d.zahn, d.zahn_a, d.zahn_par = float(coul_cut), int(bool(zahn)), float(zahn_a), float(zahn_par)
+        d.e_zero = float(ff.e_zero)
+        h = C.c_void_p()
+        L.check(L.lib().cr_qmdff_create(C.byref(d), C.byref(h)), "cr_qmdff_create")
+        self._h = h
+
+    def egrad(self, xyz, precision="fp64"):
+        """Energies (with E_zero) and gradients of xyz (nbeads, n, 3) bohr."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        if x.ndim == 2:
+            x = x[None]
+        if x.shape[1:] != (self.n, 3):
+            raise ValueError(f"expected xyz of shape (nbeads, {self.n}, 3)")
+        e = np.zeros(x.shape[0])
+        g = np.zeros_like(x)
+        prec = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        L.check(L.lib().cr_qmdff_egrad(self._h, L.dptr(x), x.shape[0], L.dptr(e), L.dptr(g), prec),
+                "cr_qmdff_egrad")
+        return e, g
+
+    def schedule_info(self):
+        b = np.zeros(4, dtype=np.int32)
+        c = C.c_int()
+        L.check(L.lib().cr_qmdff_schedule_info(self._h, L.iptr(b), C.byref(c)), "schedule_info")
+        return {"batches": b.tolist(), "colors": c.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().cr_qmdff_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class RPMDEngine:
-    """A batch of independent RPMD trajectories resident on one GPU."""
+    """A batch of independent RPMD trajectories resident on one GPU.
+
+    ``pes`` is an analytic surface name ("h3", "ch4h") or a
+    :class:`QMDFFForceField`, which must stay alive while the engine runs."""
 
     def __init__(self, pes, mass, nbeads, ntraj, dt_au, beta=None, thermostat="none",
                  andersen_step=70, pile_tau0_au=0.0, transrot=True, precision="fp64", seed=0,
                  traj0=0):
-        self.pes = PES[pes] if isinstance(pes, str) else int(pes)
+        self.ff = pes if isinstance(pes, QMDFFForceField) else None
+        if self.ff is not None:
+            self.pes = L.CR_PES_QMDFF
+        else:
+            self.pes = PES[pes] if isinstance(pes, str) else int(pes)
         self.mass = np.ascontiguousarray(mass, dtype=np.float64)
         self.natoms = len(self.mass)
         self.nbeads = int(nbeads)
@@ -74,7 +156,11 @@ class RPMDEngine:
                               int(seed) & 0xFFFFFFFF, int(traj0) & 0xFFFFFFFF, float(dt_au),
                               self.beta, float(pile_tau0_au), L.dptr(self.mass))
         h = C.c_void_p()
-        L.check(L.lib().cr_engine_create(C.byref(self.cfg), C.byref(h)), "cr_engine_create")
+        if self.ff is not None:
+            L.check(L.lib().cr_engine_create_qmdff(C.byref(self.cfg), self.ff._h, C.byref(h)),
+                    "cr_engine_create_qmdff")
+        else:
+            L.check(L.lib().cr_engine_create(C.byref(self.cfg), C.byref(h)), "cr_engine_create")
         self._h = h
 
     @classmethod

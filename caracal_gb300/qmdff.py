@@ -38,6 +38,14 @@ C6_PAIR = {(1, 1): 3.0898, (1, 6): 7.5916, (6, 6): 18.1368}
 R0AB_PAIR_ANG = {(1, 1): 2.1823, (1, 6): 2.5984, (6, 6): 2.9146}
 
 
+def element_radii():
+    """rad(94) of module qmdff: covalent radius per element in bohr (H and C set)."""
+    r = np.zeros(94)
+    for z, v in RAD_ANG.items():
+        r[z - 1] = v / BOHR_ANGSTROM
+    return r
+
+
 def valence_charge(z):
     """valel (src/valel.f90) for H and C: Z times the REAL(4) fit factor."""
     if z <= 2:

@@ -103,3 +103,19 @@ def ch4h_recross_definition(q0):
     return dict(reac1=[1, 2, 3, 4, 5], reac2=[6], bond_form=(1, 6), bond_break=(2, 1),
                 form_ref=float(np.linalg.norm(q0[0] - q0[5])),
                 break_ref=float(np.linalg.norm(q0[1] - q0[0])), r_inf=16.0, xi_ideal=1.0)
+
+
+def qmdff_config(ntraj=1024, nbeads=64, nsteps=500, kelvin=300.0, dt_fs=0.5, nc=20,
+                 thermostat="andersen", andersen_step=70):
+    """Synthetic QMDFF of C20H42 (62 atoms: the saturated 20-carbon chain), zig-zag
+    r(CC) = 1.53 A, r(CH) = 1.09 A, tetrahedral angles: 64 beads, 1024 trajectories,
+    NVT 300 K (Andersen, ANDERSEN_STEP 70), 0.5 fs, beads start on the reference
+    geometry with 0.01 A jitter.  The force field itself is built by
+    ``caracal_gb300.qmdff.alkane`` (extra["ff"])."""
+    from . import qmdff as Q
+    ff = Q.alkane(nc=nc)
+    sym = ["C" if z == 6 else "H" for z in ff.at]
+    return Workload(name=f"qmdff_c{nc}h{2 * nc + 2}_P{nbeads}_T{ntraj}", pes="qmdff", symbols=sym,
+                    q0=ff.xyz.copy(), nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs,
+                    nsteps=nsteps, thermostat=thermostat, andersen_step=andersen_step,
+                    sigma_bohr=float(angstrom_to_bohr(0.01)), transrot=True, extra={"ff": ff})

@@ -38,7 +38,7 @@ extern "C" {
 #define CR_PES_H3 1      /* ANA_H3: BKMP2, src/egrad_h3.f */
 #define CR_PES_CH4H 2    /* ANA_CH4H: src/egrad_ch4h.f + src/util_ch4h.f */
 #define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f (not built yet) */
-#define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90, ff_hb.f90 (not built yet) */
+#define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90 (ff_hb not built yet) */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
 #define CR_THERMO_NONE 0      /* NVE */
@@ -52,7 +52,7 @@ extern "C" {
 
 typedef struct cr_config {
   int pes;            /* CR_PES_* */
-  int natoms;         /* must match the PES (H3: 3, CH4H: 6) */
+  int natoms;         /* must match the PES (H3: 3, CH4H: 6, QMDFF: the force field's n) */
   int nbeads;         /* 1..128 (RPMD_BEADS) */
   int ntraj;          /* independent trajectories in this engine */
   int thermostat;     /* CR_THERMO_* */
@@ -113,11 +113,59 @@ int cr_initialize_ch4h(void);
 int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
                     void* stream);
 
+/* ---- QMDFF force field ------------------------------------------------------
+ * Replaces the QMDFF branch of `gradient` (src/gradient.f90:342-358):
+ * `ff_eg(n,at,xyz,e,g)` (src/ff_eg.f90:41) + `ff_nonb(n,at,xyz,q,r0ab,zab,
+ * r0094,sr42,c66ab,enb,g)` (src/ff_nonb.f90:34) + E_zero, one molecule, not
+ * periodic, no H/halogen-bond terms (nhb = 0).  The arrays are those of module
+ * qmdff (src/qmdff.f90:52-57, 1-based atom indices, Fortran column-major) and
+ * the ff_nonb arguments; they are copied to the device at creation. */
+typedef struct cr_qmdff_def {
+  int natoms;
+  const int* at;          /* at(natoms): element numbers 1..94 */
+  const double* q;        /* q(natoms): charges */
+  const double* rad;      /* rad(94): covalent radius per element, bohr (module qmdff) */
+  int nbond, nangl, ntors, nnci;
+  const int* bond;        /* bond(2,nbond) */
+  const double* vbond;    /* vbond(3,nbond): r0, k, a */
+  const int* angl;        /* angl(3,nangl): centre, i, k */
+  const double* vangl;    /* vangl(2,nangl): theta0, k */
+  const int* tors;        /* tors(6,ntors): i, j, k, l, nt, type (2 = inversion) */
+  const double* vtors;    /* vtors(14,ntors): phi0, V, (rn, phase, Vn) x 4 */
+  const int* nci;         /* nci(3,nnci): i, j, category 1..6 */
+  const double* r0ab;     /* r0ab(94,94): repulsion exponent alpha */
+  const double* zab;      /* zab(94,94) */
+  const double* r0094;    /* r0094(94,94): BJ radius R0 */
+  const double* sr42;     /* sr42(94,94) */
+  const double* c66ab;    /* c66ab(natoms,natoms): pair C6 */
+  double eps1[6], eps2[6];/* setnonb category scalings (src/setnonb.f90:164-190) */
+  double coul_cut;        /* bohr: 50 (NVT) or 10 (NVE Zahn, src/dynamic.f90) */
+  int zahn;               /* 1: Zahn Coulomb q q (erfc(a r)/r - par (r - cut)), no eps1 */
+  double zahn_a, zahn_par;
+  double e_zero;          /* E_zero1 shift */
+} cr_qmdff_def;
+typedef struct cr_qmdff cr_qmdff;
+int cr_qmdff_create(const cr_qmdff_def* def, cr_qmdff** out);
+int cr_qmdff_destroy(cr_qmdff* ff);
+/* Host arrays xyz(3,natoms,nbeads) -> e(nbeads) (with E_zero), g(3,natoms,nbeads). */
+int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
+/* Same on device-resident arrays; stream may be 0. */
+int cr_qmdff_egrad_device(cr_qmdff* ff, const double* d_xyz, int nbeads, double* d_e, double* d_g,
+                          int precision, void* stream);
+/* Term batches of the warp schedule (bonds, angles, torsions, NCI pairs) and
+ * the colours they need (diagnostics). */
+int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors);
+
 /* ---- RPMD engine -----------------------------------------------------------
  * Replaces the stepping loop of `dynamic` (src/dynamic.f90:1569-1579) around
  * `verlet` (src/verlet.f90:65) and the initialisation of `mdinit`
  * (src/mdinit.f90:40-173), batched over ntraj independent trajectories. */
 int cr_engine_create(const cr_config* cfg, cr_engine** out);
+/* Engine on a QMDFF (cfg->pes = CR_PES_QMDFF, cfg->natoms = the force
+ * field's natoms, cfg->mass natoms masses).  The force field must outlive the
+ * engine.  Steps run as a CUDA graph of kernels (kick + free ring polymer,
+ * forces, kick + thermostat, transrot) instead of one persistent launch. */
+int cr_engine_create_qmdff(const cr_config* cfg, cr_qmdff* ff, cr_engine** out);
 int cr_engine_destroy(cr_engine* e);
 
 /* Initial positions: every bead of every trajectory = q0(3,natoms) plus

@@ -54,6 +54,10 @@ inline OC erf(OC a) { tally().erf++; return OC(std::erf(a.v)); }
 inline OC tanh(OC a) { tally().tanh++; return OC(std::tanh(a.v)); }
 inline OC cosh(OC a) { tally().cosh++; return OC(std::cosh(a.v)); }
 inline OC fabs(OC a) { return OC(std::fabs(a.v)); }
+inline OC asin(OC a) { tally().acos++; return OC(std::asin(a.v)); }    // counted with acos
+inline OC erfc(OC a) { tally().erf++; return OC(std::erfc(a.v)); }     // counted with erf
+inline OC fmin(OC a, OC b) { tally().cmp++; return OC(std::fmin(a.v, b.v)); }
+inline OC fmax(OC a, OC b) { tally().cmp++; return OC(std::fmax(a.v, b.v)); }
 inline double val(OC a) { return a.v; }
 inline double val(double a) { return a; }
 

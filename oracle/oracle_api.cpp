@@ -245,6 +245,12 @@ void orc_pes_opcount(int pes, const double* q, uint64_t out[14]) {
     orc::OC qq[18], V, g[18];
     for (int x = 0; x < 18; ++x) qq[x] = orc::OC(q[x]);
     orc::ch4h::egrad_bead<orc::OC>(qq, &V, g);
+  } else if (pes == 4) {
+    const int n3 = 3 * g_qmdff.n;
+    std::vector<orc::OC> qq((size_t)n3), g((size_t)n3);
+    orc::OC V;
+    for (int x = 0; x < n3; ++x) qq[(size_t)x] = orc::OC(q[x]);
+    orc::qmdff::egrad<orc::OC>(g_qmdff, qq.data(), &V, g.data());
   }
   const orc::OpTally& t = orc::tally();
   uint64_t v[14] = {t.add, t.mul, t.div,  t.sqrt, t.exp, t.log,  t.pow,

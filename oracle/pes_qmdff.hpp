@@ -24,6 +24,19 @@
 namespace orc {
 namespace qmdff {
 
+using std::acos;
+using std::asin;
+using std::cos;
+using std::erf;
+using std::erfc;
+using std::exp;
+using std::fabs;
+using std::fmax;
+using std::fmin;
+using std::pow;
+using std::sin;
+using std::sqrt;
+
 struct FF {
   int n = 0;
   std::vector<int> at;          // element numbers (n)
@@ -47,25 +60,29 @@ struct FF {
   double e_zero = 0.0;
 };
 
-inline double vlen(const double* a) {
-  double tot = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
-  return tot > 0.0 ? std::sqrt(tot) : 0.0;
+template <class T>
+inline T vlen(const T* a) {
+  T tot = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+  return tot > 0.0 ? sqrt(tot) : T(0.0);
 }
-inline void crprod(const double* a, const double* b, double* c) {
+template <class T>
+inline void crprod(const T* a, const T* b, T* c) {
   c[0] = a[1] * b[2] - a[2] * b[1];
   c[1] = a[2] * b[0] - a[0] * b[2];
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
-inline double impsc(const double* a, const double* b) {
-  double rimp = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-  double al = vlen(a), bl = vlen(b);
-  return (al > 0.0 && bl > 0.0) ? rimp / (al * bl) : 0.0;
+template <class T>
+inline T impsc(const T* a, const T* b) {
+  T rimp = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+  T al = vlen(a), bl = vlen(b);
+  return (al > 0.0 && bl > 0.0) ? rimp / (al * bl) : T(0.0);
 }
-inline double vecnorm(double* r, bool normalise) {
-  double sp = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-  double rn = std::sqrt(sp);
-  if (normalise && std::fabs(rn) > 1e-14) {
-    double o = 1.0 / rn;
+template <class T>
+inline T vecnorm(T* r, bool normalise) {
+  T sp = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  T rn = sqrt(sp);
+  if (normalise && fabs(rn) > 1e-14) {
+    T o = 1.0 / rn;
     r[0] *= o;
     r[1] *= o;
     r[2] *= o;
@@ -74,18 +91,20 @@ inline double vecnorm(double* r, bool normalise) {
 }
 
 // abdamp (src/abdamp.f90:36-51); the cutoff prefactor is a REAL(4) product
-inline void abdamp(double radi, double radj, double r2, double* damp, double* ddamp) {
+template <class T>
+inline void abdamp(double radi, double radj, T r2, T* damp, T* ddamp) {
   const double pre = (double)(3.0f * 3.5710642f);
-  double s = radi + radj;
-  double rcut = pre * (s * s);
-  double rr = (r2 / rcut) * (r2 / rcut);
+  const double s = radi + radj;
+  const double rcut = pre * (s * s);
+  T rr = (r2 / rcut) * (r2 / rcut);
   *damp = 1.0 / (1.0 + rr);
   *ddamp = -2.0 * 2 * rr / (r2 * ((1.0 + rr) * (1.0 + rr)));
 }
 
 // torsion angle (valijkl)
-inline double valijkl(const double* x, int i, int j, int k, int l) {
-  double ra[3], rb[3], rc[3], na[3], nb[3];
+template <class T>
+inline T valijkl(const T* x, int i, int j, int k, int l) {
+  T ra[3], rb[3], rc[3], na[3], nb[3];
   for (int c = 0; c < 3; ++c) {
     ra[c] = x[3 * j + c] - x[3 * i + c];
     rb[c] = x[3 * k + c] - x[3 * j + c];
@@ -95,16 +114,16 @@ inline double valijkl(const double* x, int i, int j, int k, int l) {
   crprod(rb, rc, nb);
   vecnorm(na, true);
   vecnorm(nb, true);
-  double s = na[0] * nb[0] + na[1] * nb[1] + na[2] * nb[2];
-  if (std::fabs(std::fabs(s) - 1.0) < 1e-14) s = s >= 0 ? 1.0 : -1.0;
-  return std::acos(s);
+  T s = na[0] * nb[0] + na[1] * nb[1] + na[2] * nb[2];
+  if (fabs(fabs(s) - 1.0) < 1e-14) s = s >= 0.0 ? T(1.0) : T(-1.0);
+  return acos(s);
 }
 
 // d phi / d r (dphidr)
-inline void dphidr(const double* x, int i, int j, int k, int l, double phi, double* di, double* dj,
-                   double* dk, double* dl) {
-  double cosphi = std::cos(phi), sinphi = std::sin(phi);
-  double ra[3], rb[3], rc[3], rapb[3], rbpc[3], na[3], nb[3];
+template <class T>
+inline void dphidr(const T* x, int i, int j, int k, int l, T phi, T* di, T* dj, T* dk, T* dl) {
+  T cosphi = cos(phi), sinphi = sin(phi);
+  T ra[3], rb[3], rc[3], rapb[3], rbpc[3], na[3], nb[3];
   for (int c = 0; c < 3; ++c) {
     ra[c] = x[3 * j + c] - x[3 * i + c];
     rb[c] = x[3 * k + c] - x[3 * j + c];
@@ -114,14 +133,14 @@ inline void dphidr(const double* x, int i, int j, int k, int l, double phi, doub
   }
   crprod(ra, rb, na);
   crprod(rb, rc, nb);
-  double nan_ = vecnorm(na, false), nbn = vecnorm(nb, false);
-  double nenner = nan_ * nbn * sinphi;
-  if (std::fabs(nenner) < 1e-14) {
+  T nan_ = vecnorm(na, false), nbn = vecnorm(nb, false);
+  T nenner = nan_ * nbn * sinphi;
+  if (fabs(nenner) < 1e-14) {
     for (int c = 0; c < 3; ++c) di[c] = dj[c] = dk[c] = dl[c] = 0.0;
     return;
   }
-  double on = 1.0 / nenner;
-  double rab[3], rba[3], rac[3], rbb[3], rbc[3], raa[3], rapba[3], rapbb[3], rbpca[3], rbpcb[3];
+  T on = 1.0 / nenner;
+  T rab[3], rba[3], rac[3], rbb[3], rbc[3], raa[3], rapba[3], rapbb[3], rbpca[3], rbpcb[3];
   crprod(na, rb, rab);
   crprod(nb, ra, rba);
   crprod(na, rc, rac);
@@ -141,8 +160,9 @@ inline void dphidr(const double* x, int i, int j, int k, int l, double phi, doub
 }
 
 // out-of-plane angle (omega) and its gradient (domegadr)
-inline double omega(const double* x, int i, int j, int k, int l) {
-  double re[3], rd[3], rv[3], rn[3];
+template <class T>
+inline T omega(const T* x, int i, int j, int k, int l) {
+  T re[3], rd[3], rv[3], rn[3];
   for (int c = 0; c < 3; ++c) {
     re[c] = x[3 * i + c] - x[3 * j + c];
     rd[c] = x[3 * k + c] - x[3 * j + c];
@@ -151,13 +171,13 @@ inline double omega(const double* x, int i, int j, int k, int l) {
   crprod(re, rd, rn);
   vecnorm(rn, true);
   vecnorm(rv, true);
-  return std::asin(rn[0] * rv[0] + rn[1] * rv[1] + rn[2] * rv[2]);
+  return asin(rn[0] * rv[0] + rn[1] * rv[1] + rn[2] * rv[2]);
 }
 
-inline void domegadr(const double* x, int i, int j, int k, int l, double om, double* di, double* dj,
-                     double* dk, double* dl) {
-  double sinom = std::sin(om);
-  double rv[3], rd[3], re[3], rdme[3], rn[3];
+template <class T>
+inline void domegadr(const T* x, int i, int j, int k, int l, T om, T* di, T* dj, T* dk, T* dl) {
+  T sinom = sin(om);
+  T rv[3], rd[3], re[3], rdme[3], rn[3];
   for (int c = 0; c < 3; ++c) {
     rv[c] = x[3 * l + c] - x[3 * i + c];
     rd[c] = x[3 * k + c] - x[3 * j + c];
@@ -165,17 +185,17 @@ inline void domegadr(const double* x, int i, int j, int k, int l, double om, dou
     rdme[c] = rd[c] - re[c];
   }
   crprod(re, rd, rn);
-  double rvn = vecnorm(rv, false), rnn = vecnorm(rn, false);
-  double rve[3], rne[3], rdv[3], rdn[3], rvdme[3], rndme[3];
+  T rvn = vecnorm(rv, false), rnn = vecnorm(rn, false);
+  T rve[3], rne[3], rdv[3], rdn[3], rvdme[3], rndme[3];
   crprod(rv, re, rve);
   crprod(rn, re, rne);
   crprod(rd, rv, rdv);
   crprod(rd, rn, rdn);
   crprod(rv, rdme, rvdme);
   crprod(rn, rdme, rndme);
-  double nenner = rnn * rvn * std::cos(om);
-  if (std::fabs(nenner) > 1e-14) {
-    double on = 1.0 / nenner;
+  T nenner = rnn * rvn * cos(om);
+  if (fabs(nenner) > 1e-14) {
+    T on = 1.0 / nenner;
     for (int c = 0; c < 3; ++c) {
       di[c] = on * (rdv[c] - rn[c] - sinom * (rvn / rnn * rdn[c] - rnn / rvn * rv[c]));
       dj[c] = on * (rvdme[c] - sinom * rvn / rnn * rndme[c]);
@@ -188,23 +208,24 @@ inline void domegadr(const double* x, int i, int j, int k, int l, double om, dou
 }
 
 // ff_eg: overwrites e and g(3,n)
-inline void ff_eg(const FF& ff, const double* x, double* e_out, double* g) {
+template <class T>
+inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
   const double pi = 3.1415926535897932384626433832795029;
   const double pi2 = 6.28318530717958623199592693708837;
   const double spi = 1.77245385090551599275151910313925;
-  double e = 0.0;
+  T e = 0.0;
   for (int a = 0; a < 3 * ff.n; ++a) g[a] = 0.0;
   for (int m = 0; m < ff.nbond; ++m) {
     int i = ff.bond[2 * m], j = ff.bond[2 * m + 1];
-    double rb[3];
+    T rb[3];
     for (int c = 0; c < 3; ++c) rb[c] = x[3 * i + c] - x[3 * j + c];
-    double r2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
-    double r = std::sqrt(r2);
-    double rij = ff.vbond[3 * m], kij = ff.vbond[3 * m + 1], aai = ff.vbond[3 * m + 2];
-    double aai2 = aai / 2;
-    double pa = std::pow(rij / r, aai), pa2 = std::pow(rij / r, aai2);
+    T r2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+    T r = sqrt(r2);
+    T rij = ff.vbond[3 * m], kij = ff.vbond[3 * m + 1], aai = ff.vbond[3 * m + 2];
+    T aai2 = aai / 2;
+    T pa = pow(rij / r, aai), pa2 = pow(rij / r, aai2);
     e = e + kij * (1. + pa - 2. * pa2);
-    double fac = aai * kij * (-pa + pa2) / r2;
+    T fac = aai * kij * (-pa + pa2) / r2;
     for (int c = 0; c < 3; ++c) {
       g[3 * i + c] += fac * rb[c];
       g[3 * j + c] -= fac * rb[c];
@@ -212,45 +233,45 @@ inline void ff_eg(const FF& ff, const double* x, double* e_out, double* g) {
   }
   for (int m = 0; m < ff.nangl; ++m) {
     int j = ff.angl[3 * m], i = ff.angl[3 * m + 1], k = ff.angl[3 * m + 2];
-    double c0 = ff.vangl[2 * m], kijk = ff.vangl[2 * m + 1];
-    double vab[3], vcb[3], vp[3];
+    T c0 = ff.vangl[2 * m], kijk = ff.vangl[2 * m + 1];
+    T vab[3], vcb[3], vp[3];
     for (int c = 0; c < 3; ++c) {
       vab[c] = x[3 * i + c] - x[3 * j + c];
       vcb[c] = x[3 * k + c] - x[3 * j + c];
     }
-    double rab2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
-    double rcb2 = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
+    T rab2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
+    T rcb2 = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
     crprod(vcb, vab, vp);
-    double rp = vlen(vp) + 1e-14;
-    double cosa = impsc(vab, vcb);
-    cosa = std::fmin(1.0, std::fmax(-1.0, cosa));
-    double theta = std::acos(cosa);
-    double dampij, damp2ij, dampjk, damp2jk;
+    T rp = vlen(vp) + 1e-14;
+    T cosa = impsc(vab, vcb);
+    cosa = fmin(1.0, fmax(-1.0, cosa));
+    T theta = acos(cosa);
+    T dampij, damp2ij, dampjk, damp2jk;
     abdamp(ff.rad[i], ff.rad[j], rab2, &dampij, &damp2ij);
     abdamp(ff.rad[k], ff.rad[j], rcb2, &dampjk, &damp2jk);
-    double damp = dampij * dampjk;
-    double ea, deddt;
+    T damp = dampij * dampjk;
+    T ea, deddt;
     if (pi - c0 < 1e-6) {
-      double dt = theta - c0;
+      T dt = theta - c0;
       ea = kijk * (dt * dt);
       deddt = 2.0 * kijk * dt;
     } else {
-      double d = cosa - std::cos(c0);
+      T d = cosa - cos(c0);
       ea = kijk * (d * d);
-      deddt = 2. * kijk * std::sin(theta) * (std::cos(c0) - cosa);
+      deddt = 2. * kijk * sin(theta) * (cos(c0) - cosa);
     }
     e = e + ea * damp;
-    double deda[3], dedc[3];
+    T deda[3], dedc[3];
     crprod(vab, vp, deda);
-    double rmul1 = -deddt / (rab2 * rp);
+    T rmul1 = -deddt / (rab2 * rp);
     crprod(vcb, vp, dedc);
-    double rmul2 = deddt / (rcb2 * rp);
+    T rmul2 = deddt / (rcb2 * rp);
     for (int c = 0; c < 3; ++c) {
       deda[c] *= rmul1;
       dedc[c] *= rmul2;
-      double dedb = deda[c] + dedc[c];
-      double t1 = ea * damp2ij * dampjk * vab[c];
-      double t2 = ea * damp2jk * dampij * vcb[c];
+      T dedb = deda[c] + dedc[c];
+      T t1 = ea * damp2ij * dampjk * vab[c];
+      T t2 = ea * damp2jk * dampij * vcb[c];
       g[3 * i + c] += deda[c] * damp + t1;
       g[3 * j + c] += -dedb * damp - t1 - t2;
       g[3 * k + c] += dedc[c] * damp + t2;
@@ -260,41 +281,41 @@ inline void ff_eg(const FF& ff, const double* x, double* e_out, double* g) {
     int i = ff.tors[6 * m], j = ff.tors[6 * m + 1], k = ff.tors[6 * m + 2], l = ff.tors[6 * m + 3];
     int nt = ff.tors[6 * m + 4], type = ff.tors[6 * m + 5];
     const double* vt = &ff.vtors[14 * m];
-    double phi0 = vt[0];
-    double vab[3], vcb[3], vdc[3], dda[3], ddb[3], ddc[3], ddd[3];
-    double et, dij, damp, d2a, d2b, d2c;
-    double dmp[3];
+    T phi0 = vt[0];
+    T vab[3], vcb[3], vdc[3], dda[3], ddb[3], ddc[3], ddd[3];
+    T et, dij, damp, d2a, d2b, d2c;
+    T dmp[3];
     if (type != 2) {
       for (int c = 0; c < 3; ++c) {
         vab[c] = x[3 * i + c] - x[3 * j + c];
         vcb[c] = x[3 * j + c] - x[3 * k + c];
         vdc[c] = x[3 * k + c] - x[3 * l + c];
       }
-      double rij = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
-      double rjk = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
-      double rkl = vdc[0] * vdc[0] + vdc[1] * vdc[1] + vdc[2] * vdc[2];
+      T rij = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
+      T rjk = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
+      T rkl = vdc[0] * vdc[0] + vdc[1] * vdc[1] + vdc[2] * vdc[2];
       abdamp(ff.rad[i], ff.rad[j], rij, &dmp[0], &d2a);
       abdamp(ff.rad[k], ff.rad[j], rjk, &dmp[1], &d2b);
       abdamp(ff.rad[k], ff.rad[l], rkl, &dmp[2], &d2c);
-      double dampij = dmp[0], dampjk = dmp[1], dampkl = dmp[2];
+      T dampij = dmp[0], dampjk = dmp[1], dampkl = dmp[2];
       damp = dampjk * dampij * dampkl;
-      double phi = valijkl(x, i, j, k, l);
+      T phi = valijkl(x, i, j, k, l);
       dphidr(x, i, j, k, l, phi, dda, ddb, ddc, ddd);
       et = 0.0;
       dij = 0.0;
       int mm = 2;
       for (int it = 0; it < nt; ++it) {
-        double rn = vt[mm];
-        double dphi1 = phi - phi0, dphi2 = phi + phi0 - pi2;
-        double c1 = rn * dphi1 + vt[mm + 1];
-        double c2 = rn * dphi2 + vt[mm + 1];
-        double x1cos = std::cos(c1), x2cos = std::cos(c2), x1sin = std::sin(c1), x2sin = std::sin(c2);
-        double phipi = phi - pi;
-        double ef = std::erf(phipi);
-        double e1 = vt[mm + 2] * (1. + x1cos);
-        double e2 = vt[mm + 2] * (1. + x2cos);
+        T rn = vt[mm];
+        T dphi1 = phi - phi0, dphi2 = phi + phi0 - pi2;
+        T c1 = rn * dphi1 + vt[mm + 1];
+        T c2 = rn * dphi2 + vt[mm + 1];
+        T x1cos = cos(c1), x2cos = cos(c2), x1sin = sin(c1), x2sin = sin(c2);
+        T phipi = phi - pi;
+        T ef = erf(phipi);
+        T e1 = vt[mm + 2] * (1. + x1cos);
+        T e2 = vt[mm + 2] * (1. + x2cos);
         et = et + 0.5 * (1. - ef) * e1 + (0.5 + 0.5 * ef) * e2;
-        double expo = std::exp(-(phipi * phipi)) / spi;
+        T expo = exp(-(phipi * phipi)) / spi;
         dij = dij - expo * e1 - 0.5 * (1. - ef) * vt[mm + 2] * x1sin * rn + expo * e2 -
               (0.5 + 0.5 * ef) * vt[mm + 2] * x2sin * rn;
         mm += 3;
@@ -302,9 +323,9 @@ inline void ff_eg(const FF& ff, const double* x, double* e_out, double* g) {
       et = et * vt[1];
       dij = dij * vt[1] * damp;
       for (int c = 0; c < 3; ++c) {
-        double t1 = et * d2a * dampjk * dampkl * vab[c];
-        double t2 = et * d2b * dampij * dampkl * vcb[c];
-        double t3 = et * d2c * dampij * dampjk * vdc[c];
+        T t1 = et * d2a * dampjk * dampkl * vab[c];
+        T t2 = et * d2b * dampij * dampkl * vcb[c];
+        T t3 = et * d2c * dampij * dampjk * vdc[c];
         g[3 * i + c] += dij * dda[c] + t1;
         g[3 * j + c] += dij * ddb[c] - t1 + t2;
         g[3 * k + c] += dij * ddc[c] + t3 - t2;
@@ -317,30 +338,30 @@ inline void ff_eg(const FF& ff, const double* x, double* e_out, double* g) {
         vcb[c] = x[3 * j + c] - x[3 * k + c];
         vdc[c] = x[3 * j + c] - x[3 * l + c];
       }
-      double rij = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
-      double rjk = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
-      double rjl = vdc[0] * vdc[0] + vdc[1] * vdc[1] + vdc[2] * vdc[2];
+      T rij = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
+      T rjk = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
+      T rjl = vdc[0] * vdc[0] + vdc[1] * vdc[1] + vdc[2] * vdc[2];
       abdamp(ff.rad[i], ff.rad[j], rij, &dmp[0], &d2a);
       abdamp(ff.rad[k], ff.rad[j], rjk, &dmp[1], &d2b);
       abdamp(ff.rad[j], ff.rad[l], rjl, &dmp[2], &d2c);
-      double dampij = dmp[0], dampjk = dmp[1], dampjl = dmp[2];
+      T dampij = dmp[0], dampjk = dmp[1], dampjl = dmp[2];
       damp = dampjk * dampij * dampjl;
-      double phi = omega(x, i, j, k, l);
+      T phi = omega(x, i, j, k, l);
       domegadr(x, i, j, k, l, phi, dda, ddb, ddc, ddd);
-      double rn = vt[2];
+      T rn = vt[2];
       if (rn > 1e-6) {
-        double c1 = (phi - phi0) + pi;
-        et = (1. + std::cos(c1)) * vt[1];
-        dij = -std::sin(c1) * vt[1] * damp;
+        T c1 = (phi - phi0) + pi;
+        et = (1. + cos(c1)) * vt[1];
+        dij = -sin(c1) * vt[1] * damp;
       } else {
-        double d = std::cos(phi) - std::cos(phi0);
+        T d = cos(phi) - cos(phi0);
         et = vt[1] * (d * d);
-        dij = 2. * vt[1] * std::sin(phi) * (std::cos(phi0) - std::cos(phi)) * damp;
+        dij = 2. * vt[1] * sin(phi) * (cos(phi0) - cos(phi)) * damp;
       }
       for (int c = 0; c < 3; ++c) {
-        double t1 = et * d2a * dampjk * dampjl * vab[c];
-        double t2 = et * d2b * dampij * dampjl * vcb[c];
-        double t3 = et * d2c * dampij * dampjk * vdc[c];
+        T t1 = et * d2a * dampjk * dampjl * vab[c];
+        T t2 = et * d2b * dampij * dampjl * vcb[c];
+        T t3 = et * d2c * dampij * dampjk * vdc[c];
         g[3 * i + c] += dij * dda[c] - t1;
         g[3 * j + c] += dij * ddb[c] + t1 + t2 + t3;
         g[3 * k + c] += dij * ddc[c] - t2;
@@ -353,32 +374,33 @@ inline void ff_eg(const FF& ff, const double* x, double* e_out, double* g) {
 }
 
 // ff_nonb (non-periodic, one molecule): accumulates into enb and g
-inline void ff_nonb(const FF& ff, const double* x, double* enb, double* g) {
-  double e = 0.0;
+template <class T>
+inline void ff_nonb(const FF& ff, const T* x, T* enb, T* g) {
+  T e = 0.0;
   for (int kp = 0; kp < ff.nnci; ++kp) {
     int i1 = ff.nci[3 * kp], i2 = ff.nci[3 * kp + 1], nk = ff.nci[3 * kp + 2];
-    double vab[3];
+    T vab[3];
     for (int c = 0; c < 3; ++c) vab[c] = x[3 * i1 + c] - x[3 * i2 + c];
-    double r2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
-    double r = std::sqrt(r2);
-    double oner = 1.0 / r;
-    double R0 = ff.pR0[kp], c6 = ff.pC6[kp];
-    double r4 = r2 * r2, r6 = r4 * r2;
-    double R02 = R0 * R0, r06 = R02 * R02 * R02;
-    double t6 = r6 + r06;
-    double t8 = r6 * r2 + r06 * R0 * R0;
-    double c6t6 = c6 / t6, c6t8 = c6 / t8;
-    double t27 = ff.pSr42[kp] * c6t8;
-    double e0 = c6t6 + t27;
+    T r2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
+    T r = sqrt(r2);
+    T oner = 1.0 / r;
+    T R0 = ff.pR0[kp], c6 = ff.pC6[kp];
+    T r4 = r2 * r2, r6 = r4 * r2;
+    T R02 = R0 * R0, r06 = R02 * R02 * R02;
+    T t6 = r6 + r06;
+    T t8 = r6 * r2 + r06 * R0 * R0;
+    T c6t6 = c6 / t6, c6t8 = c6 / t8;
+    T t27 = ff.pSr42[kp] * c6t8;
+    T e0 = c6t6 + t27;
     e = e - e0 * ff.eps2[nk];
-    double drij = ff.eps2[nk] * (c6t6 * 6.0 * r4 / t6 + 8.0 * t27 * r6 / t8);
-    double ga[3] = {vab[0] * drij, vab[1] * drij, vab[2] * drij};
+    T drij = ff.eps2[nk] * (c6t6 * 6.0 * r4 / t6 + 8.0 * t27 * r6 / t8);
+    T ga[3] = {vab[0] * drij, vab[1] * drij, vab[2] * drij};
     if (r < 25) {
-      double xz = ff.pZab[kp], alpha = ff.pAlpha[kp];
-      double t = xz * std::exp(-alpha * r);
-      double e1 = t * oner;
+      T xz = ff.pZab[kp], alpha = ff.pAlpha[kp];
+      T t = xz * exp(-alpha * r);
+      T e1 = t * oner;
       e = e + e1 * ff.eps2[nk];
-      double dr2 = ff.eps2[nk] * t * (alpha * r + 1.0) * oner / r2;
+      T dr2 = ff.eps2[nk] * t * (alpha * r + 1.0) * oner / r2;
       for (int c = 0; c < 3; ++c) ga[c] = ga[c] - vab[c] * dr2;
     }
     for (int c = 0; c < 3; ++c) {
@@ -388,21 +410,21 @@ inline void ff_nonb(const FF& ff, const double* x, double* enb, double* g) {
   }
   for (int kp = 0; kp < ff.nnci; ++kp) {
     int i1 = ff.nci[3 * kp], i2 = ff.nci[3 * kp + 1], nk = ff.nci[3 * kp + 2];
-    double vab[3];
+    T vab[3];
     for (int c = 0; c < 3; ++c) vab[c] = x[3 * i1 + c] - x[3 * i2 + c];
-    double r2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
-    double r = std::sqrt(r2);
+    T r2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
+    T r = sqrt(r2);
     if (r > ff.coul_cut) continue;
-    double oner = 1.0 / r;
-    double e0;
+    T oner = 1.0 / r;
+    T e0;
     if (ff.zahn)
-      e0 = ff.q[i1] * ff.q[i2] * ((std::erfc(ff.zahn_a * r) * oner) - ff.zahn_par * (r - ff.coul_cut));
+      e0 = ff.q[i1] * ff.q[i2] * ((erfc(ff.zahn_a * r) * oner) - ff.zahn_par * (r - ff.coul_cut));
     else
       e0 = ff.q[i1] * ff.q[i2] * oner * ff.eps1[nk] * 1.0;
     e = e + e0;
-    double drij = e0 / r2;
+    T drij = e0 / r2;
     for (int c = 0; c < 3; ++c) {
-      double ga = -vab[c] * drij;
+      T ga = -vab[c] * drij;
       g[3 * i1 + c] += ga;
       g[3 * i2 + c] -= ga;
     }
@@ -411,8 +433,9 @@ inline void ff_nonb(const FF& ff, const double* x, double* enb, double* g) {
 }
 
 // gradient dispatch for one QMDFF (src/gradient.f90:342-358)
-inline void egrad(const FF& ff, const double* x, double* V, double* g) {
-  double e;
+template <class T>
+inline void egrad(const FF& ff, const T* x, T* V, T* g) {
+  T e;
   ff_eg(ff, x, &e, g);
   ff_nonb(ff, x, &e, g);
   *V = e + ff.e_zero;

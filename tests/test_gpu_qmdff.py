@@ -1,0 +1,183 @@
+"""GPU: the QMDFF force kernel and the large-molecule engine path against the
+oracle, synthetic C20H42 (62 atoms).
+
+Tolerances (norm-wise relative, max|a-b|/max|b|):
+  plain FP64 form: energies and gradients <= 1e-12, single engine step
+                   <= 1e-12, 20-step trajectories <= 1e-9;
+  mixed form:      gradient error against FP64 bounded by 2e-6 (measured
+                   ~3e-7 on thermal geometries).
+"""
+import numpy as np
+import pytest
+
+from caracal_gb300 import RPMDEngine
+from caracal_gb300 import qmdff as Q
+from caracal_gb300.engine import QMDFFForceField
+from caracal_gb300.units import beta_from_kelvin, dt_fs_to_au
+from caracal_gb300.workloads import qmdff_config
+from conftest import rel_err
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def alkane():
+    return Q.alkane()
+
+
+@pytest.fixture(scope="module")
+def gpu_ff(alkane, require_gpu):
+    ff = QMDFFForceField(alkane)
+    yield ff
+    ff.close()
+
+
+@pytest.fixture(autouse=True)
+def oracle_ff(alkane):
+    orc.set_qmdff(alkane, Q.ElementTables.d3_like())
+
+
+def geoms(ff, nb, sigma, seed):
+    rng = np.random.default_rng(seed)
+    return ff.xyz[None] + rng.normal(0, sigma, (nb,) + ff.xyz.shape)
+
+
+def test_schedule_covers_every_term(gpu_ff):
+    info = gpu_ff.schedule_info()
+    b = info["batches"]
+    # bonds pack 31 per colour on 62 atoms, so every batch holds 32 terms
+    assert b[0] == 2 and b[3] == (1710 + 31) // 32
+    assert b[1] >= 4 and b[2] >= 6
+    assert info["colors"] >= sum(b)
+
+
+def test_egrad_fp64_matches_oracle(gpu_ff, alkane):
+    x = geoms(alkane, 256, 0.1, 1)
+    e, g = gpu_ff.egrad(x, "fp64")
+    eo, go = orc.egrad("qmdff", x)
+    assert rel_err(e, eo) <= 1e-12
+    assert rel_err(g, go) <= 1e-12
+
+
+def test_egrad_mixed_error(gpu_ff, alkane):
+    x = geoms(alkane, 256, 0.1, 2)
+    e, g = gpu_ff.egrad(x, "mixed")
+    e64, g64 = gpu_ff.egrad(x, "fp64")
+    err = np.sqrt(np.sum((g - g64) ** 2) / np.sum(g64 ** 2))
+    assert err <= 2e-6
+    assert rel_err(e, e64) <= 2e-6
+
+
+def test_egrad_zahn_matches_oracle(alkane, require_gpu):
+    ff = QMDFFForceField(alkane, coul_cut=10.0, zahn=True)
+    orc.set_qmdff(alkane, Q.ElementTables.d3_like(), coul_cut=10.0, zahn=True)
+    x = geoms(alkane, 64, 0.1, 3)
+    e, g = ff.egrad(x, "fp64")
+    eo, go = orc.egrad("qmdff", x)
+    ff.close()
+    assert rel_err(e, eo) <= 1e-12
+    assert rel_err(g, go) <= 1e-12
+
+
+def make_pair(gpu_ff, alkane, nbeads, ntraj, thermostat, andersen_step=5, precision="fp64",
+              transrot=True, kelvin=300.0, dt_fs=0.5, seed=77):
+    mass = qmdff_config().mass
+    beta = beta_from_kelvin(kelvin)
+    dt = dt_fs_to_au(dt_fs)
+    tau0 = dt_fs_to_au(100.0)
+    eng = RPMDEngine(gpu_ff, mass, nbeads, ntraj, dt, beta=beta, thermostat=thermostat,
+                     andersen_step=andersen_step, pile_tau0_au=tau0, transrot=transrot,
+                     precision=precision, seed=seed)
+    cfg = orc.Config("qmdff", mass, nbeads, dt, beta, thermostat=thermostat,
+                     andersen_step=andersen_step, pile_tau0=tau0, transrot=transrot, seed=seed)
+    return eng, cfg
+
+
+def start(eng, cfg, alkane, sigma=0.02):
+    eng.init_positions(alkane.xyz, sigma)
+    eng.init_momenta()
+    eng.compute_forces()
+    q = orc.init_positions(cfg, eng.ntraj, alkane.xyz, sigma)
+    p = orc.init_momenta(cfg, eng.ntraj)
+    f, e = orc.init_forces(cfg, q)
+    return q, p, f, e
+
+
+def test_init_matches_oracle(gpu_ff, alkane):
+    eng, cfg = make_pair(gpu_ff, alkane, 8, 2, "andersen")
+    q, p, f, e = start(eng, cfg, alkane)
+    qg, pg, fg, eg, st = eng.get_state()
+    eng.close()
+    assert rel_err(qg, q) <= 1e-15
+    assert rel_err(pg, p) <= 1e-14
+    assert rel_err(fg, f) <= 1e-12
+    assert rel_err(eg, e) <= 1e-12
+
+
+@pytest.mark.parametrize("thermostat", ["andersen", "pile", "none"])
+@pytest.mark.parametrize("nbeads", [1, 2, 3, 4, 6, 8, 16, 64])
+def test_single_step_matches_oracle(gpu_ff, alkane, thermostat, nbeads):
+    eng, cfg = make_pair(gpu_ff, alkane, nbeads, 2, thermostat, andersen_step=1)
+    q, p, f, e = start(eng, cfg, alkane)
+    eng.run(1)
+    qg, pg, fg, eg, st = eng.get_state()
+    eng.close()
+    qo, po, fo, eo, sto = orc.run(cfg, q, p, f, 1)
+    assert rel_err(qg, qo) <= 1e-12
+    assert rel_err(pg, po) <= 1e-12
+    assert rel_err(fg, fo) <= 1e-12
+    assert rel_err(eg, eo) <= 1e-12
+    assert not st.any() and not sto.any()
+
+
+@pytest.mark.parametrize("thermostat,nbeads", [("andersen", 8), ("pile", 6), ("none", 4)])
+def test_trajectory_matches_oracle(gpu_ff, alkane, thermostat, nbeads):
+    eng, cfg = make_pair(gpu_ff, alkane, nbeads, 2, thermostat, andersen_step=5)
+    q, p, f, e = start(eng, cfg, alkane)
+    eng.run(12)
+    eng.run(8)
+    qg, pg, fg, eg, st = eng.get_state()
+    eng.close()
+    qo, po, fo, eo, sto = orc.run(cfg, q, p, f, 20)
+    assert rel_err(qg, qo) <= 1e-9
+    assert rel_err(pg, po) <= 1e-9
+    assert rel_err(eg, eo) <= 1e-9
+
+
+def test_step_host_matches_run(gpu_ff, alkane):
+    eng, cfg = make_pair(gpu_ff, alkane, 8, 3, "andersen", andersen_step=2)
+    start(eng, cfg, alkane)
+    q, p, f, e, st = eng.get_state()
+    eng.step_host(q, p, f)
+    eng.step_host(q, p, f)
+    eng2, _ = make_pair(gpu_ff, alkane, 8, 3, "andersen", andersen_step=2)
+    start(eng2, cfg, alkane)
+    eng2.run(2)
+    q2, p2, f2, e2, st2 = eng2.get_state()
+    eng.close()
+    eng2.close()
+    assert rel_err(q, q2) <= 1e-15
+    assert rel_err(p, p2) <= 1e-15
+
+
+def test_mixed_engine_tracks_fp64(gpu_ff, alkane):
+    a, cfg = make_pair(gpu_ff, alkane, 16, 4, "none", precision="fp64")
+    b, _ = make_pair(gpu_ff, alkane, 16, 4, "none", precision="mixed")
+    for eng in (a, b):
+        start(eng, cfg, alkane)
+        eng.run(10)
+    qa, pa, fa, ea, _ = a.get_state()
+    qb, pb, fb, eb, _ = b.get_state()
+    a.close()
+    b.close()
+    assert rel_err(qb, qa) <= 1e-8
+    assert rel_err(fb, fa) <= 1e-5
+
+
+def test_recross_unsupported_on_qmdff(gpu_ff, alkane):
+    from caracal_gb300 import CaracalError
+    eng, _ = make_pair(gpu_ff, alkane, 4, 2, "none")
+    with pytest.raises(CaracalError):
+        eng.set_recross([1], [2], (1, 2), (1, 3), 2.0, 2.0, 10.0, max_steps=4)
+    eng.close()

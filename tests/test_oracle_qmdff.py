@@ -1,0 +1,91 @@
+"""CPU: the QMDFF oracle (ff_eg + ff_nonb restatement) and the host-side
+QMDFF data: topology of the synthetic C20H42, the .qmdff reader/writer, and
+the oracle's analytic gradient against central differences (Caracal's own
+NUM_GRAD check, src/gradient.f90)."""
+import numpy as np
+import pytest
+
+from caracal_gb300 import qmdff as Q
+from oracle import oracle as orc
+
+
+@pytest.fixture(scope="module")
+def alkane():
+    ff = Q.alkane()
+    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    return ff
+
+
+def test_alkane_topology(alkane):
+    ff = alkane
+    assert ff.n == 62 and int((ff.at == 6).sum()) == 20
+    assert len(ff.bond) == 61 and len(ff.angl) == 120 and len(ff.tors) == 171
+    # all pairs three or more bonds apart
+    assert len(ff.nci) == 1710
+    assert set(np.unique(ff.nci[:, 2])) <= {3, 4, 5}
+    assert abs(ff.q.sum()) < 1e-12
+
+
+def test_reference_geometry_is_valence_minimum(alkane):
+    ff = alkane
+    # bonds, angles and torsions sit at their reference values, so only the
+    # non-bonded pairs contribute: a copy without NCI pairs has E = 0, g = 0
+    ff0 = Q.QMDFF(at=ff.at, xyz=ff.xyz, q=ff.q, bond=ff.bond, vbond=ff.vbond, angl=ff.angl,
+                  vangl=ff.vangl, tors=ff.tors, vtors=ff.vtors, nci=ff.nci[:0], c6=ff.c6)
+    orc.set_qmdff(ff0, Q.ElementTables.d3_like())
+    V, g = orc.egrad("qmdff", ff.xyz)
+    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    assert abs(V[0]) < 1e-20
+    assert np.max(np.abs(g)) < 1e-12
+
+
+def test_gradient_matches_central_differences(alkane):
+    rng = np.random.default_rng(5)
+    x = alkane.xyz + rng.normal(0, 0.1, alkane.xyz.shape)
+    V, g = orc.egrad("qmdff", x)
+    h = 1e-5
+    fd = np.zeros_like(x)
+    for a in range(x.shape[0]):
+        for d in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[a, d] += h
+            xm[a, d] -= h
+            fd[a, d] = (orc.egrad("qmdff", xp)[0][0] - orc.egrad("qmdff", xm)[0][0]) / (2 * h)
+    assert np.max(np.abs(fd - g[0])) / np.max(np.abs(g[0])) < 1e-7
+
+
+def test_zahn_coulomb_gradient(alkane):
+    # NVE form: q q (erfc(a r)/r - par (r - cut)) within 10 bohr
+    ff = alkane
+    orc.set_qmdff(ff, Q.ElementTables.d3_like(), coul_cut=10.0, zahn=True)
+    try:
+        x = ff.xyz + np.random.default_rng(6).normal(0, 0.05, ff.xyz.shape)
+        V, g = orc.egrad("qmdff", x)
+        assert np.isfinite(V).all() and np.isfinite(g).all()
+    finally:
+        orc.set_qmdff(ff, Q.ElementTables.d3_like())
+
+
+def test_qmdff_file_round_trip(alkane, tmp_path):
+    ff = alkane
+    path = tmp_path / "c20h42.qmdff"
+    Q.write_qmdff(ff, path)
+    rd = Q.read_qmdff(path)
+    assert np.array_equal(rd.at, ff.at)
+    np.testing.assert_allclose(rd.xyz, ff.xyz, atol=1e-11)
+    np.testing.assert_allclose(rd.q, ff.q, atol=1e-11)
+    for k in ("bond", "angl", "tors", "nci"):
+        assert np.array_equal(getattr(rd, k), getattr(ff, k)), k
+    np.testing.assert_allclose(rd.vbond, ff.vbond, atol=1e-11)
+    np.testing.assert_allclose(rd.vangl, ff.vangl, atol=1e-11)
+    np.testing.assert_allclose(rd.vtors, ff.vtors, atol=1e-11)
+
+
+def test_element_tables_real4_literals():
+    t = Q.ElementTables.d3_like()
+    # setnonb's a1 = 0.45 and s8 = 2.7 are REAL(4) literals widened to REAL(8)
+    s8 = float(np.float32(2.7))
+    assert t.sr42[6, 6] == 3.0 * s8 * Q.R2R4[6] * Q.R2R4[6]
+    assert Q.eps_factors()[0][3] == float(np.float32(0.85))
+    r = Q.element_radii()
+    assert r.shape == (94,) and r[0] > 0 and r[5] > 0
