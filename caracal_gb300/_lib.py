@@ -45,7 +45,7 @@ class CrConfig(C.Structure):
                 ("thermostat", C.c_int), ("andersen_step", C.c_int), ("transrot", C.c_int),
                 ("precision", C.c_int), ("seed", C.c_uint), ("traj0", C.c_uint),
                 ("dt", C.c_double), ("beta", C.c_double), ("pile_tau0", C.c_double),
-                ("mass", c_double_p)]
+                ("mass", c_double_p), ("nose_q", C.c_double)]
 
 
 class CrRecross(C.Structure):

@@ -195,7 +195,7 @@ struct cr_engine {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double *d_q = nullptr, *d_p = nullptr, *d_f = nullptr, *d_epot = nullptr, *d_V = nullptr;
-  double *d_prop = nullptr, *d_pile = nullptr, *d_q0 = nullptr;
+  double *d_pile = nullptr, *d_q0 = nullptr;
   int* d_status = nullptr;
   // recrossing children
   int xi_on = 0, side_cap = 0, side_step0 = 0;
@@ -210,6 +210,7 @@ struct cr_engine {
   double *d_mass = nullptr, *d_inv_mass = nullptr, *d_sigma = nullptr, *d_ke = nullptr, *d_ko = nullptr;
   int* d_istep = nullptr;
   int h_istep = 0;
+  double* d_vnh = nullptr;  // [T][4] Nose-Hoover chain velocities
   size_t smem_drift = 0, smem_kick = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -257,46 +258,20 @@ double kentry(const std::vector<double>& C, const std::vector<double>& D, int P,
   return s;
 }
 
-// Propagator blocks K1, K2, K3 (unit mass) of the Caracal cosine transform,
-// restricted to the (P/2+1)^2 block that acts on symmetrised inputs.
-void build_propagator(int P, double beta, double dt, std::vector<double>& out) {
-  const int H = P / 2 + 1;
-  std::vector<double> C, diag[3];
-  mode_tables(P, beta, dt, C, diag);
-  out.assign((size_t)3 * H * H, 0.0);
-  for (int which = 0; which < 3; ++which)
-    for (int r = 0; r < H; ++r)
-      for (int l = 0; l < H; ++l)
-        out[(size_t)which * H * H + (size_t)r * H + l] = kentry(C, diag[which], P, r, l, -1);
-}
-
-// Parity-split blocks of the large-molecule path: for even P, Ke[w][r][l]
+// Parity-split propagator blocks (both step paths): for even P, Ke[w][r][l]
 // (even modes, l < nu) and Ko[w][r][l] (odd modes, l < nv), r < nr; for odd P
 // the unique rows of K (nr = nu = P/2+1, nv = 0).
-void build_split_propagator(int P, double beta, double dt, cr::SplitParams& s, std::vector<double>& ke,
+void build_split_propagator(int P, double beta, double dt, const cr::PropDims& d, std::vector<double>& ke,
                             std::vector<double>& ko) {
   std::vector<double> C, diag[3];
   mode_tables(P, beta, dt, C, diag);
-  s.M = P / 2;
-  s.split = (P % 2 == 0) ? 1 : 0;
-  if (s.split) {
-    s.nr = s.M / 2 + 1;
-    s.nu = s.M / 2 + 1;
-    s.nv = s.M - s.M / 2;
-  } else {
-    s.nr = P / 2 + 1;
-    s.nu = s.nr;
-    s.nv = 0;
-  }
-  s.su = s.nu | 1;
-  s.sv = s.nv > 0 ? (s.nv | 1) : 0;
-  ke.assign((size_t)3 * s.nr * s.nu, 0.0);
-  ko.assign((size_t)3 * s.nr * (s.nv > 0 ? s.nv : 1), 0.0);
+  ke.assign((size_t)3 * d.nr * d.nu, 0.0);
+  ko.assign((size_t)3 * d.nr * (d.nv > 0 ? d.nv : 1), 0.0);
   for (int w = 0; w < 3; ++w)
-    for (int r = 0; r < s.nr; ++r) {
-      for (int l = 0; l < s.nu; ++l)
-        ke[((size_t)w * s.nr + r) * s.nu + l] = kentry(C, diag[w], P, r, l, s.split ? 0 : -1);
-      for (int l = 0; l < s.nv; ++l) ko[((size_t)w * s.nr + r) * s.nv + l] = kentry(C, diag[w], P, r, l, 1);
+    for (int r = 0; r < d.nr; ++r) {
+      for (int l = 0; l < d.nu; ++l)
+        ke[((size_t)w * d.nr + r) * d.nu + l] = kentry(C, diag[w], P, r, l, d.split ? 0 : -1);
+      for (int l = 0; l < d.nv; ++l) ko[((size_t)w * d.nr + r) * d.nv + l] = kentry(C, diag[w], P, r, l, 1);
     }
 }
 
@@ -363,12 +338,21 @@ int launch_forces(cr_engine* e) {
 int split_step_launches(cr_engine* e) {
   const int cw = cr::split_chunk(e->P);
   const dim3 grid((e->NC + cw - 1) / cw, e->T);
+  const bool nhc = e->cfg.thermostat == CR_THERMO_NHC;
+  if (nhc) {
+    cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+    CR_CUDA(cudaGetLastError());
+  }
   cr::split_drift_kernel<<<grid, cr::kSplitBlock, e->smem_drift, e->stream>>>(e->sp);
   CR_CUDA(cudaGetLastError());
   int rc = qmdff_launch(e->ff, e->d_q, e->T * e->P, e->d_V, e->d_f, e->cfg.precision, e->stream);
   if (rc) return rc;
   cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp);
   CR_CUDA(cudaGetLastError());
+  if (nhc) {
+    cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+    CR_CUDA(cudaGetLastError());
+  }
   cr::split_finish_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
   CR_CUDA(cudaGetLastError());
   cr::split_advance_kernel<<<1, 1, 0, e->stream>>>(e->d_istep);
@@ -603,7 +587,8 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
   if (ff && (long long)cfg->ntraj * cfg->nbeads > (1LL << 26))
     return fail(CR_ERR_ARG, "ntraj * nbeads must be <= 2^26 on the QMDFF path");
   if (!(cfg->dt > 0.0)) return fail(CR_ERR_ARG, "dt must be > 0");
-  if (cfg->thermostat == CR_THERMO_NHC) return fail(CR_ERR_UNSUPPORTED, "Nose-Hoover chain not built yet");
+  if (cfg->thermostat == CR_THERMO_NHC && !(cfg->nose_q > 0.0 && std::isfinite(cfg->nose_q)))
+    return fail(CR_ERR_ARG, "the Nose-Hoover chain needs nose_q > 0");
   if (cfg->thermostat != CR_THERMO_NONE && cfg->thermostat != CR_THERMO_ANDERSEN &&
       cfg->thermostat != CR_THERMO_PILE)
     return fail(CR_ERR_ARG, "unknown thermostat");
@@ -661,17 +646,38 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
   cudaMemsetAsync(e->d_V, 0, (size_t)e->T * e->P * 8, e->stream);
   cudaMemsetAsync(e->d_status, 0, (size_t)e->T * sizeof(int), e->stream);
 
-  std::vector<double> prop, pile;
-  build_propagator(e->P, cfg->beta, cfg->dt, prop);
+  const cr::PropDims pd = cr::prop_dims(e->P);
+  std::vector<double> ke, ko, pile;
+  build_split_propagator(e->P, cfg->beta, cfg->dt, pd, ke, ko);
   if (cfg->thermostat == CR_THERMO_PILE) build_pile(e->P, cfg->beta, cfg->dt, cfg->pile_tau0, pile);
   else pile.assign((size_t)2 * e->P, 0.0);
-  if (cudaMalloc(&e->d_prop, prop.size() * 8) != cudaSuccess ||
+  if (cudaMalloc(&e->d_ke, ke.size() * 8) != cudaSuccess || cudaMalloc(&e->d_ko, ko.size() * 8) != cudaSuccess ||
       cudaMalloc(&e->d_pile, pile.size() * 8) != cudaSuccess)
     return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the tables failed"));
-  if (cudaMemcpyAsync(e->d_prop, prop.data(), prop.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
+  if (cudaMemcpyAsync(e->d_ke, ke.data(), ke.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(e->d_ko, ko.data(), ko.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
       cudaMemcpyAsync(e->d_pile, pile.data(), pile.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return cleanup_fail(fail(CR_ERR_CUDA, "upload of the tables failed"));
+
+  // Nose-Hoover chain constants (src/mdinit.f90:128-147, src/nhc.f90:47-54)
+  cr::NhcParams nhc{};
+  if (cfg->thermostat == CR_THERMO_NHC) {
+    const double kB = 0.316679e-5;  // src/dynamic.f90:79
+    const double kelvin = 1.0 / (cfg->beta * kB);
+    const double qterm = kB * kelvin * cfg->nose_q * cfg->nose_q;
+    nhc.nfree = 3 * N;
+    nhc.qnh[0] = (double)nhc.nfree * qterm;
+    nhc.qnh[1] = nhc.qnh[2] = nhc.qnh[3] = qterm;
+    nhc.ekt = (double)(1.380649E-23f / 4.3597447E-18f) * kelvin;
+    nhc.dtc = cfg->dt / 5.0;
+    nhc.w[0] = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0));
+    nhc.w[1] = 1.0 - 2.0 * nhc.w[0];
+    nhc.w[2] = nhc.w[0];
+  }
+  if (cudaMalloc(&e->d_vnh, (size_t)e->T * 4 * sizeof(double)) != cudaSuccess ||
+      cudaMemset(e->d_vnh, 0, (size_t)e->T * 4 * sizeof(double)) != cudaSuccess)
+    return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the chain state failed"));
 
   double tm = 0.0;  // src/transrot.f90:72-79
   for (int i = 0; i < N; ++i)
@@ -685,17 +691,19 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
 
   if (e->split) {
     cr::SplitParams& s = e->sp;
-    std::vector<double> ke, ko;
-    build_split_propagator(e->P, cfg->beta, cfg->dt, s, ke, ko);
+    s.M = pd.M;
+    s.split = pd.split;
+    s.nr = pd.nr;
+    s.nu = pd.nu;
+    s.nv = pd.nv;
+    s.su = pd.su;
+    s.sv = pd.sv;
     if (cudaMalloc(&e->d_mass, (size_t)N * 8) != cudaSuccess || cudaMalloc(&e->d_inv_mass, (size_t)N * 8) != cudaSuccess ||
-        cudaMalloc(&e->d_sigma, (size_t)N * 8) != cudaSuccess || cudaMalloc(&e->d_ke, ke.size() * 8) != cudaSuccess ||
-        cudaMalloc(&e->d_ko, ko.size() * 8) != cudaSuccess || cudaMalloc(&e->d_istep, sizeof(int)) != cudaSuccess)
+        cudaMalloc(&e->d_sigma, (size_t)N * 8) != cudaSuccess || cudaMalloc(&e->d_istep, sizeof(int)) != cudaSuccess)
       return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the split tables failed"));
     if (cudaMemcpy(e->d_mass, e->mass.data(), (size_t)N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_inv_mass, inv.data(), (size_t)N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_sigma, sig.data(), (size_t)N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(e->d_ke, ke.data(), ke.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(e->d_ko, ko.data(), ko.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(e->d_istep, 0, sizeof(int)) != cudaSuccess)
       return cleanup_fail(fail(CR_ERR_CUDA, "upload of the split tables failed"));
     s.T = e->T;
@@ -722,6 +730,8 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
     s.epot = e->d_epot;
     s.status = e->d_status;
     s.istep = e->d_istep;
+    s.nhc = nhc;
+    s.vnh = e->d_vnh;
     const bool pl = cfg->thermostat == CR_THERMO_PILE;
     const int cw = cr::split_chunk(e->P), sp1 = e->P + 1;
     e->smem_drift = cr::split_smem_doubles(s, pl) * sizeof(double);
@@ -755,7 +765,11 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
     s.inv_mass[i] = 1.0 / m;
     s.sigma[i] = i < N ? sig[(size_t)i] : 0.0;
   }
-  s.prop = e->d_prop;
+  s.nhc = nhc;
+  s.vnh = e->d_vnh;
+  s.pd = pd;
+  s.ke = e->d_ke;
+  s.ko = e->d_ko;
   s.pile = e->d_pile;
   s.q = e->d_q;
   s.p = e->d_p;
@@ -785,7 +799,6 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_V);
   cudaFree(e->d_status);
   cudaFree(e->d_q0);
-  cudaFree(e->d_prop);
   cudaFree(e->d_pile);
   cudaFree(e->d_side);
   cudaFree(e->d_w);
@@ -798,6 +811,7 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_ke);
   cudaFree(e->d_ko);
   cudaFree(e->d_istep);
+  cudaFree(e->d_vnh);
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   if (e->ev0) cudaEventDestroy(e->ev0);
@@ -840,6 +854,8 @@ int cr_engine_init_momenta(cr_engine* e, int zero) {
   if (!e) return fail(CR_ERR_ARG, "NULL engine");
   if (!zero && !(e->cfg.beta > 0.0 && std::isfinite(e->cfg.beta)))
     return fail(CR_ERR_ARG, "Andersen momenta need a finite temperature");
+  // mdinit also starts the Nose-Hoover chain at rest (src/mdinit.f90:140-145)
+  CR_CUDA(cudaMemsetAsync(e->d_vnh, 0, (size_t)e->T * 4 * sizeof(double), e->stream));
   const int nb = e->T * e->P;
   if (e->split) {
     const long long n = (long long)nb * ((e->NC + 1) / 2);
@@ -907,7 +923,7 @@ static int engine_run_async(cr_engine* e, int nsteps) {
   if (rc) return rc;
   CR_CUDA(cudaEventRecord(e->ev1, e->stream));
   e->istep += nsteps;
-  e->launches = e->split ? 5 * nsteps : 1;
+  e->launches = e->split ? (e->cfg.thermostat == CR_THERMO_NHC ? 7 : 5) * nsteps : 1;
   return CR_OK;
 }
 

@@ -16,10 +16,13 @@ using cr::qmdff::kVPair;
 // Term schedule of one kind: batches of 32 lanes; within a batch, terms of
 // one colour touch disjoint atoms.  Greedy: each colour takes, in order, the
 // remaining terms that do not touch an atom already used by that colour,
-// until the batch holds 32 terms.
-void schedule_kind(int nterm, int arity, const std::vector<int>& atoms, const std::vector<int>& order,
-                   int natoms, std::vector<int>& slot, std::vector<unsigned char>& color,
-                   std::vector<unsigned char>& ncol, int& nbatch, int& colours) {
+// until the batch holds 32 terms or has max_colours colours.  Every colour
+// costs one scatter round of the warp, so light terms (bonds, pairs) get
+// one colour per batch and heavier ones (angles, torsions) two.
+void schedule_kind(int nterm, int arity, int max_colours, const std::vector<int>& atoms,
+                   const std::vector<int>& order, int natoms, std::vector<int>& slot,
+                   std::vector<unsigned char>& color, std::vector<unsigned char>& ncol, int& nbatch,
+                   int& colours) {
   std::vector<int> remaining = order;
   std::vector<int> stamp((size_t)natoms, -1);
   int stamp_id = 0;
@@ -27,7 +30,7 @@ void schedule_kind(int nterm, int arity, const std::vector<int>& atoms, const st
   while (!remaining.empty()) {
     std::vector<int> bt, bc;
     int col = 0;
-    while ((int)bt.size() < 32 && !remaining.empty()) {
+    while ((int)bt.size() < 32 && !remaining.empty() && col < max_colours) {
       ++stamp_id;
       std::vector<int> rest;
       rest.reserve(remaining.size());
@@ -86,13 +89,12 @@ __global__ void __launch_bounds__(kQmdffWarps * 32) qmdff_egrad_kernel(qmdff::De
   extern __shared__ double qsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n3 = 3 * D.n;
-  double* xs = qsm + (size_t)warp * 2 * n3;
-  double* gs = xs + n3;
+  double* ws = qsm + (size_t)warp * (qmdff::warp_smem_bytes(D.n) / sizeof(double));
   for (int b = blockIdx.x * kQmdffWarps + warp; b < nbeads; b += gridDim.x * kQmdffWarps) {
     const double* qb = q + (size_t)b * n3;
-    for (int a = lane; a < n3; a += 32) xs[a] = qb[a];
+    for (int a = lane; a < n3; a += 32) ws[a] = qb[a];
     __syncwarp();
-    const double v = qmdff::warp_egrad<MIXED>(D, xs, gs, g + (size_t)b * n3, 1.0, lane);
+    const double v = qmdff::warp_egrad<MIXED>(D, ws, g + (size_t)b * n3, 1.0, lane);
     if (lane == 0) e[b] = v;
     __syncwarp();
   }
@@ -215,6 +217,7 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   cr::qmdff::Dev& D = ff->dev;
   D.n = n;
   int boff = 0;
+  bool distinct = true;
   for (int kind = 0; kind < 4; ++kind) {
     std::vector<int> order((size_t)ff->nterm[kind]);
     for (int m = 0; m < ff->nterm[kind]; ++m) order[(size_t)m] = m;
@@ -238,7 +241,12 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
     }
     if (kind == 3) atoms = pair;
     int nb = 0;
-    schedule_kind(ff->nterm[kind], arity, atoms, order, n, slot, color, ncol, nb, ff->ncolors);
+    const int max_colours = (kind == 0 || kind == 3) ? 1 : 2;
+    schedule_kind(ff->nterm[kind], arity, max_colours, atoms, order, n, slot, color, ncol, nb, ff->ncolors);
+    for (int m = 0; m < ff->nterm[kind]; ++m)
+      for (int x = 0; x < arity; ++x)
+        for (int y = x + 1; y < arity; ++y)
+          if (atoms[(size_t)m * arity + x] == atoms[(size_t)m * arity + y]) distinct = false;
     D.nb[kind] = nb;
     D.boff[kind] = boff;
     boff += nb;
@@ -276,6 +284,7 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   D.zahn_a = d->zahn_a;
   D.zahn_par = d->zahn_par;
   D.e_zero = d->e_zero;
+  D.distinct = distinct ? 1 : 0;
   *out = ff;
   return CR_OK;
 }

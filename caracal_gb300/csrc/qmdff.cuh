@@ -10,11 +10,14 @@
 // results are deterministic run to run.
 //
 // Precision: the plain form computes every term in FP64 with Caracal's
-// formulas.  The mixed form computes each term in FP32 from FP64 displacement
-// vectors, with cancellation-free rewrites where the FP64 formula subtracts
-// nearly equal numbers (bond stretch from an FP64 r^2 - r0^2, dihedral angle
-// from atan2 instead of acos), and accumulates the gradient with compensated
-// (Neumaier) FP32 sums and the energy in FP64.
+// formulas (divisions by a shared denominator taken as one reciprocal).  The
+// mixed form splits each FP64 coordinate once per bead into an FP32 pair
+// x = hi + lo; a displacement (hi_a - hi_b) + (lo_a - lo_b) is then within
+// about one FP32 ulp of the exact difference without any FP64 work per term.
+// Terms run in FP32 with cancellation-free rewrites where the FP64 formula
+// subtracts nearly equal numbers (bond stretch from an FP64 r^2 - r0^2,
+// dihedral angle from atan2 instead of acos); gradient and energy are
+// accumulated with compensated (Neumaier) FP32 sums.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -54,6 +57,7 @@ struct Dev {
   Tables<float> f;
   double coul_cut, zahn_a, zahn_par, e_zero;
   int zahn;
+  int distinct;  // 1: every term's atoms are pairwise distinct
 };
 
 template <class F> __device__ inline F q_sqrt(F x);
@@ -120,11 +124,53 @@ struct Grad<float> {
   __device__ inline double get(int i) const { return (double)s[i] + (double)k[i]; }
 };
 
-template <class F>
-__device__ inline void scatter(const Contrib<F>& c, Grad<F>& G) {
-  for (int m = 0; m < c.na; ++m)
+// Adds a term's gradient for its NA atoms (compile-time count).  With
+// distinct atoms (checked on the host, `Dev::distinct`) all loads are issued
+// before the stores, so the shared-memory round trips overlap.
+template <int NA>
+__device__ inline void scatter(const Contrib<double>& c, Grad<double>& G, bool distinct) {
+  if (distinct) {
+    double v[NA][3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
+    for (int m = 0; m < NA; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[m][d] = G.g[3 * c.a[m] + d];
+#pragma unroll
+    for (int m = 0; m < NA; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) G.g[3 * c.a[m] + d] = v[m][d] + c.g[m][d];
+  } else {
+#pragma unroll
+    for (int m = 0; m < NA; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
+  }
+}
+template <int NA>
+__device__ inline void scatter(const Contrib<float>& c, Grad<float>& G, bool distinct) {
+  if (distinct) {
+    float a[NA][3], k[NA][3];
+#pragma unroll
+    for (int m = 0; m < NA; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        a[m][d] = G.s[3 * c.a[m] + d];
+        k[m][d] = G.k[3 * c.a[m] + d];
+      }
+#pragma unroll
+    for (int m = 0; m < NA; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float v = c.g[m][d], t = a[m][d] + v;
+        G.k[3 * c.a[m] + d] = k[m][d] + ((fabsf(a[m][d]) >= fabsf(v)) ? ((a[m][d] - t) + v) : ((v - t) + a[m][d]));
+        G.s[3 * c.a[m] + d] = t;
+      }
+  } else {
+#pragma unroll
+    for (int m = 0; m < NA; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
+  }
 }
 
 // abdamp (src/abdamp.f90:36-51); the cutoff prefactor is the REAL(4) product 3.0*3.5710642
@@ -133,21 +179,36 @@ __device__ inline void abdamp(F radi, F radj, F r2, F& damp, F& ddamp) {
   const F pre = (F)(double)(3.0f * 3.5710642f);
   const F s = radi + radj;
   const F rcut = pre * (s * s);
-  const F rr = (r2 / rcut) * (r2 / rcut);
+  const F x = r2 / rcut;
+  const F rr = x * x;
   damp = F(1) / (F(1) + rr);
-  ddamp = F(-4) * rr / (r2 * ((F(1) + rr) * (F(1) + rr)));
+  ddamp = F(-4) * rr * (damp * damp) / r2;
 }
 
+// A bead's coordinates: FP64, and (mixed form) the FP32 split x = hi + lo.
+struct BeadPos {
+  const double* x;
+  const float* hi;
+  const float* lo;
+};
+
 template <class F>
-__device__ inline void disp(const double* x, int a, int b, F* v) {
-  v[0] = (F)(x[3 * a] - x[3 * b]);
-  v[1] = (F)(x[3 * a + 1] - x[3 * b + 1]);
-  v[2] = (F)(x[3 * a + 2] - x[3 * b + 2]);
+__device__ inline void disp(const BeadPos& X, int a, int b, F* v);
+template <>
+__device__ inline void disp<double>(const BeadPos& X, int a, int b, double* v) {
+  v[0] = X.x[3 * a] - X.x[3 * b];
+  v[1] = X.x[3 * a + 1] - X.x[3 * b + 1];
+  v[2] = X.x[3 * a + 2] - X.x[3 * b + 2];
+}
+template <>
+__device__ inline void disp<float>(const BeadPos& X, int a, int b, float* v) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) v[d] = (X.hi[3 * a + d] - X.hi[3 * b + d]) + (X.lo[3 * a + d] - X.lo[3 * b + d]);
 }
 
 // Bond stretch, generalised Lennard-Jones (src/ff_eg.f90:87-163):
 // e = k (1 + (r0/r)^a - 2 (r0/r)^(a/2)).
-__device__ inline double bond_f64(const Dev& D, const double* x, int m, Contrib<double>& c) {
+__device__ inline double bond_f64(const Dev& D, const BeadPos& x, int m, Contrib<double>& c) {
   const int i = D.bond[2 * m], j = D.bond[2 * m + 1];
   double rb[3];
   disp<double>(x, i, j, rb);
@@ -155,7 +216,7 @@ __device__ inline double bond_f64(const Dev& D, const double* x, int m, Contrib<
   const double r = sqrt(r2);
   const double* v = &D.d.vbond[3 * m];
   const double rij = v[0], kij = v[1], aai = v[2];
-  const double pa = pow(rij / r, aai), pa2 = pow(rij / r, aai / 2);
+  const double pa2 = pow(rij / r, aai / 2), pa = pa2 * pa2;
   const double fac = aai * kij * (-pa + pa2) / r2;
   c.na = 2;
   c.a[0] = i;
@@ -171,7 +232,7 @@ __device__ inline double bond_f64(const Dev& D, const double* x, int m, Contrib<
 // Mixed form: with u = (r0/r)^(a/2) = exp(-(a/2) log1p(x)), x = (r - r0)/r0
 // taken from the FP64 r^2 - r0^2, e = k (1 - u)^2 and the gradient factor
 // a k u (1 - u) / r^2 are free of the cancellation in 1 + u^2 - 2u.
-__device__ inline double bond_mixed(const Dev& D, const double* x, int m, Contrib<float>& c) {
+__device__ inline float bond_mixed(const Dev& D, const BeadPos& x, int m, Contrib<float>& c) {
   const int i = D.bond[2 * m], j = D.bond[2 * m + 1];
   double rd[3];
   disp<double>(x, i, j, rd);
@@ -195,12 +256,12 @@ __device__ inline double bond_mixed(const Dev& D, const double* x, int m, Contri
     c.g[0][d] = fac * rb;
     c.g[1][d] = -fac * rb;
   }
-  return (double)(kij * omu * omu);
+  return kij * omu * omu;
 }
 
 // Angle bend with abdamp damping (src/ff_eg.f90:167-299).
 template <class F>
-__device__ inline F angle_term(const Dev& D, const Tables<F>& T, const double* x, int m, Contrib<F>& c) {
+__device__ inline F angle_term(const Dev& D, const Tables<F>& T, const BeadPos& x, int m, Contrib<F>& c) {
   const int j = D.angl[3 * m], i = D.angl[3 * m + 1], k = D.angl[3 * m + 2];
   const F* v = &T.vangl[kVAngl * m];
   const F c0 = v[0], kijk = v[1], cc0 = v[2];
@@ -293,7 +354,7 @@ __device__ inline F dihedral(const F* ra, const F* rb, const F* rc, F* na, F* nb
 // Torsions (erf-blended cosine series, src/ff_eg.f90:303-440) and
 // inversions (tors type 2, src/ff_eg.f90:441-618).
 template <class F>
-__device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const double* x, int m, Contrib<F>& c) {
+__device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const BeadPos& x, int m, Contrib<F>& c) {
   const F pi = (F)3.1415926535897932384626433832795029;
   const F pi2 = (F)6.28318530717958623199592693708837;
   const F spi = (F)1.77245385090551599275151910313925;
@@ -456,39 +517,59 @@ __device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const double*
   return et * damp;
 }
 
+// kVPair parameters of one pair with 16-byte loads (rows are 32 / 64 bytes).
+__device__ inline void load_pair_params(const float* p, float* v) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ inline void load_pair_params(const double* p, double* v) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double2 t = __ldg(q + k);
+    v[2 * k] = t.x;
+    v[2 * k + 1] = t.y;
+  }
+}
+
 // One NCI pair (src/ff_nonb.f90): BJ-damped C6/C8 dispersion and, for
 // r < 25 bohr, exponential repulsion, both times eps2 (:79-193); Coulomb
 // within coul_cut (:337-416), eps1 q_i q_j / r or the Zahn form.
 template <class F>
-__device__ inline F pair_term(const Dev& D, const Tables<F>& T, const double* x, int kp, Contrib<F>& c) {
-  const int i1 = D.pair[2 * kp], i2 = D.pair[2 * kp + 1];
-  const F* v = &T.vpair[kVPair * kp];
+__device__ inline F pair_term(const Dev& D, const Tables<F>& T, const BeadPos& x, int kp, Contrib<F>& c) {
+  const int2 ij = __ldg(reinterpret_cast<const int2*>(D.pair) + kp);
+  const int i1 = ij.x, i2 = ij.y;
+  F v[kVPair];
+  load_pair_params(&T.vpair[kVPair * kp], v);
   F vab[3];
   disp<F>(x, i1, i2, vab);
   const F r2 = dot3(vab, vab);
   const F r = q_sqrt<F>(r2);
   const F oner = F(1) / r;
+  const F ir2 = oner * oner;
   const F R0 = v[0], c6 = v[1], eps2 = v[5];
   const F r4 = r2 * r2, r6 = r4 * r2;
   const F R02 = R0 * R0, r06 = R02 * R02 * R02;
   const F t6 = r6 + r06;
   const F t8 = r6 * r2 + r06 * R0 * R0;
-  const F c6t6 = c6 / t6, c6t8 = c6 / t8;
+  const F it6 = F(1) / t6, it8 = F(1) / t8;
+  const F c6t6 = c6 * it6, c6t8 = c6 * it8;
   const F t27 = v[2] * c6t8;
   F e = -(c6t6 + t27) * eps2;
-  F drij = eps2 * (c6t6 * F(6) * r4 / t6 + F(8) * t27 * r6 / t8);
+  F drij = eps2 * (c6t6 * F(6) * r4 * it6 + F(8) * t27 * r6 * it8);
   if (r < F(25)) {
     const F alpha = v[4];
     const F t = v[3] * q_exp<F>(-alpha * r);
     e = e + t * oner * eps2;
-    drij = drij - eps2 * t * (alpha * r + F(1)) * oner / r2;
+    drij = drij - eps2 * t * (alpha * r + F(1)) * oner * ir2;
   }
   if (!(r > (F)D.coul_cut)) {
     F e0;
     if (D.zahn) e0 = v[6] * ((q_erfc<F>((F)D.zahn_a * r) * oner) - (F)D.zahn_par * (r - (F)D.coul_cut));
     else e0 = v[6] * oner;
     e = e + e0;
-    drij = drij - e0 / r2;
+    drij = drij - e0 * ir2;
   }
   c.na = 2;
   c.a[0] = i1;
@@ -503,14 +584,14 @@ __device__ inline F pair_term(const Dev& D, const Tables<F>& T, const double* x,
 
 // Energy of one term of kind `kind` (0 bond, 1 angle, 2 torsion, 3 pair).
 template <bool MIXED>
-__device__ inline double term(const Dev& D, int kind, const double* x, int m,
-                              Contrib<typename std::conditional<MIXED, float, double>::type>& c) {
+__device__ inline typename std::conditional<MIXED, float, double>::type term(
+    const Dev& D, int kind, const BeadPos& x, int m, Contrib<typename std::conditional<MIXED, float, double>::type>& c) {
   if constexpr (MIXED) {
     switch (kind) {
       case 0: return bond_mixed(D, x, m, c);
-      case 1: return (double)angle_term<float>(D, D.f, x, m, c);
-      case 2: return (double)torsion_term<float>(D, D.f, x, m, c);
-      default: return (double)pair_term<float>(D, D.f, x, m, c);
+      case 1: return angle_term<float>(D, D.f, x, m, c);
+      case 2: return torsion_term<float>(D, D.f, x, m, c);
+      default: return pair_term<float>(D, D.f, x, m, c);
     }
   } else {
     switch (kind) {
@@ -522,20 +603,59 @@ __device__ inline double term(const Dev& D, int kind, const double* x, int m,
   }
 }
 
-// Shared memory per warp (bytes): coordinates (3n doubles) + gradient
-// (3n doubles, or 2 x 3n floats in the mixed form).
-__host__ __device__ inline size_t warp_smem_bytes(int n) { return (size_t)3 * n * 8 * 2; }
+// All batches of one term kind (NA atoms per term): each lane evaluates its
+// slot's term, then the warp scatters colour by colour.
+template <bool MIXED, int KIND, int NA>
+__device__ inline void kind_batches(const Dev& D, const BeadPos& X,
+                                    Grad<typename std::conditional<MIXED, float, double>::type>& G,
+                                    typename std::conditional<MIXED, float, double>::type& es,
+                                    typename std::conditional<MIXED, float, double>::type& ec, int lane) {
+  using F = typename std::conditional<MIXED, float, double>::type;
+  const int b0 = D.boff[KIND], nb = D.nb[KIND];
+  const bool distinct = D.distinct != 0;
+  for (int b = b0; b < b0 + nb; ++b) {
+    const int m = D.slot[32 * b + lane];
+    const int col = D.color[32 * b + lane];
+    const int ncol = D.ncol[b];
+    Contrib<F> c;
+    if (m >= 0) {
+      const F v = term<MIXED>(D, KIND, X, m, c);
+      const F t = es + v;
+      ec += (fabs(es) >= fabs(v)) ? ((es - t) + v) : ((v - t) + es);
+      es = t;
+    }
+    for (int k = 0; k < ncol; ++k) {
+      if (m >= 0 && col == k) scatter<NA>(c, G, distinct);
+      __syncwarp();
+    }
+  }
+}
+
+// Shared memory per warp (bytes): coordinates (3n doubles), the FP32 split
+// hi, lo (3n floats each) and the gradient (3n doubles, or sum and
+// compensation, 3n floats each).
+__host__ __device__ inline size_t warp_smem_bytes(int n) { return (size_t)3 * n * (8 + 4 + 4 + 8); }
 
 // Energy (with E_zero) and gradient (times gscale) of one bead by one warp.
-// xs: the bead's coordinates in shared memory; gs: 3n doubles of shared
-// scratch; gout: the gradient destination.  Returns the energy on every lane.
+// ws: the warp's shared memory with the bead's FP64 coordinates in its first
+// 3n doubles; gout: the gradient destination.  Returns the energy on every lane.
 template <bool MIXED>
-__device__ inline double warp_egrad(const Dev& D, const double* xs, void* gs, double* gout, double gscale,
-                                    int lane) {
+__device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, double gscale, int lane) {
   using F = typename std::conditional<MIXED, float, double>::type;
   const int n3 = 3 * D.n;
+  double* xs = ws;
+  float* hi = (float*)(ws + n3);
+  float* lo = hi + n3;
+  void* gs = lo + n3;
+  BeadPos X{xs, hi, lo};
   Grad<F> G;
   if constexpr (MIXED) {
+    for (int a = lane; a < n3; a += 32) {
+      const double v = xs[a];
+      const float h = __double2float_rn(v);
+      hi[a] = h;
+      lo[a] = __double2float_rn(v - (double)h);
+    }
     G.s = (float*)gs;
     G.k = (float*)gs + n3;
     for (int a = lane; a < 2 * n3; a += 32) ((float*)gs)[a] = 0.f;
@@ -544,23 +664,13 @@ __device__ inline double warp_egrad(const Dev& D, const double* xs, void* gs, do
     for (int a = lane; a < n3; a += 32) G.g[a] = 0.0;
   }
   __syncwarp();
-  double e = 0.0;
-  for (int kind = 0; kind < 4; ++kind) {
-    const int b0 = D.boff[kind], nb = D.nb[kind];
-    for (int b = b0; b < b0 + nb; ++b) {
-      const int m = D.slot[32 * b + lane];
-      const int col = D.color[32 * b + lane];
-      const int ncol = D.ncol[b];
-      Contrib<F> c;
-      c.na = 0;
-      if (m >= 0) e += term<MIXED>(D, kind, xs, m, c);
-      for (int k = 0; k < ncol; ++k) {
-        if (m >= 0 && col == k) scatter(c, G);
-        __syncwarp();
-      }
-    }
-  }
+  F es = F(0), ec = F(0);  // compensated lane sum of term energies
+  kind_batches<MIXED, 0, 2>(D, X, G, es, ec, lane);
+  kind_batches<MIXED, 1, 3>(D, X, G, es, ec, lane);
+  kind_batches<MIXED, 2, 4>(D, X, G, es, ec, lane);
+  kind_batches<MIXED, 3, 2>(D, X, G, es, ec, lane);
   for (int a = lane; a < n3; a += 32) gout[a] = gscale * G.get(a);
+  double e = (double)es + (double)ec;
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
   return e + D.e_zero;

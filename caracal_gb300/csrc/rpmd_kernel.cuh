@@ -14,9 +14,15 @@
 // src/irfft.f90), a per-mode 2x2 rotation (src/verlet.f90:405-454), and C
 // again.  The composite is linear: p' = K1 p + m K2 q, q' = K3 p / m + K1 q
 // with K = C diag(poly) C.  Since poly(k) = poly(P-k), K[j][l] = K[-j][l] =
-// K[j][-l], so only the (P/2+1)^2 block acting on the symmetrised inputs
-// s_l = x_l + x_{-l} is stored (shared memory), and each output needs
-// P/2+1 FMAs instead of P.
+// K[j][-l]: beads j and P-j get the same output and only the P/2+1
+// symmetrised inputs s_l = x_l + x_{-l} matter.  For even P (M = P/2),
+// C[M-r][k] = (-1)^k C[r][k], so with K = Ke + Ko split by mode parity,
+// K[r] = Ke[r] + Ko[r] and K[M-r] = Ke[r] - Ko[r]; Ke is even and Ko odd
+// under l -> M-l.  One pass over u_l = s_l + s_{M-l}, v_l = s_l - s_{M-l}
+// gives rows r and M-r together.  The group's lanes share the (coordinate,
+// row pair) tasks, so each unique output is computed once: per coordinate
+// 4 (M/2+1)(M+1) FP64 FMAs for the whole ring polymer, against 4 P (M+1)
+// when every bead computes its own row.
 //
 // PILE (new; Caracal has Andersen and Nose-Hoover only) uses the orthonormal
 // real normal modes; O^T diag(c) O is circulant, so each half step is two
@@ -77,6 +83,89 @@ __host__ __device__ inline double xi_bimolec(const XiDev& x, const double* c, co
   return x.xi_ideal * s1 + (1.0 - x.xi_ideal) * s0;
 }
 
+// Shape of the parity-split propagator blocks for P beads.
+struct PropDims {
+  int M;      // P / 2
+  int split;  // 1: even P, parity-split blocks; 0: odd P, unique rows only
+  int nr;     // task rows
+  int nu;     // length of u (even part)
+  int nv;     // length of v (odd part)
+  int su, sv; // padded (odd) shared-memory strides of u and v
+};
+
+__host__ __device__ inline PropDims prop_dims(int P) {
+  PropDims d;
+  d.M = P / 2;
+  d.split = (P % 2 == 0) ? 1 : 0;
+  if (d.split) {
+    d.nr = d.M / 2 + 1;
+    d.nu = d.M / 2 + 1;
+    d.nv = d.M - d.M / 2;
+  } else {
+    d.nr = P / 2 + 1;
+    d.nu = d.nr;
+    d.nv = 0;
+  }
+  d.su = d.nu | 1;
+  d.sv = d.nv > 0 ? (d.nv | 1) : 0;
+  return d;
+}
+
+__device__ inline double sym_at(const double* x, int l, int P) {
+  return (l == 0 || 2 * l == P) ? x[l] : x[l] + x[P - l];
+}
+
+// Nose-Hoover chain constants of one engine (src/nhc.f90:35-171 with the
+// masses of src/mdinit.f90:128-147), precomputed on the host.
+struct NhcParams {
+  double ekt;     // nhc's kT: the REAL(4) quotient 1.380649E-23/4.3597447E-18 times kelvin
+  double qnh[4];  // chain masses: 3N Q, Q, Q, Q with Q = k_B T nose_q^2
+  double dtc;     // dt / nc
+  double w[3];    // Suzuki-Yoshida weights
+  int nfree;      // 3N
+};
+
+// One nhc call on a trajectory whose kinetic sum (centroid-normalised, as
+// Caracal: sum p.p/(2m)/P/P) is eksum: advances the chain velocities vnh and
+// returns the factor every momentum is scaled by.  Same operation order as
+// the reference loop (nc = 5 passes of ns = 3 weights).
+__host__ __device__ inline double nhc_scale(const NhcParams& c, double eksum, double (&vnh)[4]) {
+  double gnh[4];
+  double scale = 1.0;
+  for (int ic = 0; ic < 5; ++ic)
+    for (int j = 0; j < 3; ++j) {
+      const double dts = c.w[j] * c.dtc;
+      const double dt2 = 0.5 * dts, dt4 = 0.25 * dts, dt8 = 0.125 * dts;
+      double ex;
+      gnh[3] = (c.qnh[2] * vnh[2] * vnh[2] - c.ekt) / c.qnh[3];
+      vnh[3] = vnh[3] + gnh[3] * dt4;
+      gnh[2] = (c.qnh[1] * vnh[1] * vnh[1] - c.ekt) / c.qnh[2];
+      ex = exp(-vnh[3] * dt8);
+      vnh[2] = ex * (vnh[2] * ex + gnh[2] * dt4);
+      gnh[1] = (c.qnh[0] * vnh[0] * vnh[0] - c.ekt) / c.qnh[1];
+      ex = exp(-vnh[2] * dt8);
+      vnh[1] = ex * (vnh[1] * ex + gnh[1] * dt4);
+      gnh[0] = (2.0 * eksum - (double)c.nfree * c.ekt) / c.qnh[0];
+      ex = exp(-vnh[1] * dt8);
+      vnh[0] = ex * (vnh[0] * ex + gnh[0] * dt4);
+      ex = exp(-vnh[0] * dt2);
+      scale = scale * ex;
+      eksum = eksum * ex * ex;
+      gnh[0] = (2.0 * eksum - (double)c.nfree * c.ekt) / c.qnh[0];
+      ex = exp(-vnh[1] * dt8);
+      vnh[0] = ex * (vnh[0] * ex + gnh[0] * dt4);
+      gnh[1] = (c.qnh[0] * vnh[0] * vnh[0] - c.ekt) / c.qnh[1];
+      ex = exp(-vnh[2] * dt8);
+      vnh[1] = ex * (vnh[1] * ex + gnh[1] * dt4);
+      gnh[2] = (c.qnh[1] * vnh[1] * vnh[1] - c.ekt) / c.qnh[2];
+      ex = exp(-vnh[3] * dt8);
+      vnh[2] = ex * (vnh[2] * ex + gnh[2] * dt4);
+      gnh[3] = (c.qnh[2] * vnh[2] * vnh[2] - c.ekt) / c.qnh[3];
+      vnh[3] = vnh[3] + gnh[3] * dt4;
+    }
+  return scale;
+}
+
 struct StepParams {
   int T;           // trajectories in the launch
   int P;           // beads
@@ -94,8 +183,12 @@ struct StepParams {
   double mass[kMaxAtoms];
   double inv_mass[kMaxAtoms];
   double sigma[kMaxAtoms];    // sqrt(m P / beta): Andersen / PILE noise scale
-  const double* prop;  // [3][H][H]: K1, K2 (unit mass), K3 (unit mass)
+  PropDims pd;
+  const double* ke;    // [3][nr][nu]: K1, K2, K3 (unit mass), even-mode part (odd P: unique rows)
+  const double* ko;    // [3][nr][nv]: odd-mode part
   const double* pile;  // [2][P]: circulant a (c1) and b (c2)
+  NhcParams nhc;
+  double* vnh;         // [T][4] Nose-Hoover chain velocities
   double* q;           // [T][P][N][3]
   double* p;
   double* f;
@@ -206,13 +299,17 @@ __device__ inline bool invert3(double (&a)[3][3]) {
 }
 
 // Dynamic shared memory layout (doubles):
-//   [0, 3H^2)                      propagator blocks K1, K2, K3
-//   [3H^2, 3H^2 + 2P)              PILE circulant vectors a, b
-//   then per group: xs[2][NC][G], sym[2][NC][H], red[(G/32) * 32]
+//   [0, 3 nr (nu + nv))            propagator blocks Ke, Ko of K1, K2, K3
+//   then 2P                        PILE circulant vectors a, b
+//   then per group: xs[2 NC][G] (reused as the outputs [2 NC][P/2+1]),
+//                   u[2 NC][su], v[2 NC][sv], red[(G/32) * 32]
+__host__ __device__ inline size_t step_group_doubles(int P, int G, int NC) {
+  const PropDims d = prop_dims(P);
+  return (size_t)2 * NC * G + (size_t)2 * NC * (d.su + d.sv) + (size_t)((G + 31) / 32) * 32;
+}
 __host__ __device__ inline size_t step_smem_doubles(int P, int G, int NC, int groups) {
-  const int H = P / 2 + 1;
-  size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 32;
-  return (size_t)3 * H * H + 2 * (size_t)P + per_group * groups;
+  const PropDims d = prop_dims(P);
+  return (size_t)3 * d.nr * (d.nu + d.nv) + 2 * (size_t)P + step_group_doubles(P, G, NC) * groups;
 }
 
 template <class PES, bool MIXED>
@@ -227,15 +324,19 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
   const int t = blockIdx.x * groups + grp;
   const bool active = (t < prm.T) && (j < P);
 
-  double* s_prop = smem;
-  double* s_pile = s_prop + 3 * H * H;
-  const size_t per_group = (size_t)2 * NC * G + (size_t)2 * NC * H + (size_t)((G + 31) / 32) * 32;
-  double* s_grp = s_pile + 2 * P + per_group * grp;
-  double* xs = s_grp;                      // [2][NC][G]
-  double* sym = xs + 2 * NC * G;           // [2][NC][H]
-  double* red = sym + 2 * NC * H;          // [(G/32)][32]
+  const PropDims pd = prm.pd;
+  const int nke = 3 * pd.nr * pd.nu, nko = 3 * pd.nr * pd.nv;
+  double* s_ke = smem;
+  double* s_ko = s_ke + nke;
+  double* s_pile = s_ko + nko;
+  double* s_grp = s_pile + 2 * P + step_group_doubles(P, G, NC) * grp;
+  double* xs = s_grp;                      // [2][NC][G]; after the fold: outputs [2][NC][H]
+  double* su = xs + 2 * NC * G;            // [2 NC][su]
+  double* sv = su + 2 * NC * pd.su;        // [2 NC][sv]
+  double* red = sv + 2 * NC * pd.sv;       // [(G/32)][32]
 
-  for (int x = threadIdx.x; x < 3 * H * H; x += blockDim.x) s_prop[x] = prm.prop[x];
+  for (int x = threadIdx.x; x < nke; x += blockDim.x) s_ke[x] = prm.ke[x];
+  for (int x = threadIdx.x; x < nko; x += blockDim.x) s_ko[x] = prm.ko[x];
   if (prm.thermostat == CR_THERMO_PILE)
     for (int x = threadIdx.x; x < 2 * P; x += blockDim.x) s_pile[x] = prm.pile[x];
 
@@ -255,7 +356,29 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
   const uint32_t traj_key = prm.traj0 + (uint32_t)t;
   int status = 0;
   double vbead = 0.0;
+  const bool nhc = prm.thermostat == CR_THERMO_NHC;
+  double vnh[4] = {0.0, 0.0, 0.0, 0.0};
+  if (nhc && t < prm.T) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) vnh[k] = prm.vnh[4 * (size_t)t + k];
+  }
   __syncthreads();
+
+  // nhc (src/nhc.f90): group sum of p.p/(2m)/P/P, the chain, one scale.
+  auto nhc_half = [&]() {
+    double ek[1] = {0.0};
+    if (active) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const double pp = p[3 * i] * p[3 * i] + p[3 * i + 1] * p[3 * i + 1] + p[3 * i + 2] * p[3 * i + 2];
+        ek[0] = ek[0] + pp / (2.0 * prm.mass[i]) / P / P;
+      }
+    }
+    group_sum<1>(ek, G, red, j);
+    const double sc = nhc_scale(prm.nhc, ek[0], vnh);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) p[c] = sc * p[c];
+  };
 
   // PILE half step on p (in place); eta from the per-bead Gaussian stream.
   auto pile_half = [&](uint32_t step, uint32_t tag) {
@@ -295,6 +418,7 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 
   for (int n = 1; n <= nsteps; ++n) {
     const int istep = istep0 + n;
+    if (nhc) nhc_half();  // src/verlet.f90:186-208
     if (prm.thermostat == CR_THERMO_PILE) pile_half((uint32_t)istep, TAG_PILE_A);
 
     // 1/2 kick (src/verlet.f90:216-218)
@@ -309,41 +433,66 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
       xs[(NC + c) * G + j] = q[c];
     }
     group_sync(G);
-    if (j < H) {
-      const int jm = (j == 0) ? 0 : P - j;
-      const bool self = (jm == j);
-#pragma unroll
-      for (int c = 0; c < 2 * NC; ++c) {
-        double v = xs[c * G + j];
-        if (!self) v += xs[c * G + jm];
-        sym[c * H + j] = v;
+    // fold each coordinate's P values into u (and v): tasks (cc, l)
+    for (int idx = j; idx < 2 * NC * pd.nu; idx += G) {
+      const int cc = idx / pd.nu, l = idx - cc * pd.nu;
+      const double* x = xs + cc * G;
+      const double a = sym_at(x, l, P);
+      if (pd.split && 2 * l != pd.M) {
+        const double b = sym_at(x, pd.M - l, P);
+        su[cc * pd.su + l] = a + b;
+        if (l < pd.nv) sv[cc * pd.sv + l] = a - b;
+      } else {
+        su[cc * pd.su + l] = a;
+      }
+    }
+    group_sync(G);
+    // row pairs (r, M - r) of every coordinate: tasks (c, r); outputs into xs
+    for (int idx = j; idx < NC * pd.nr; idx += G) {
+      const int c = idx / pd.nr, r = idx - c * pd.nr;
+      const double* k1e = s_ke + (0 * pd.nr + r) * pd.nu;
+      const double* k2e = s_ke + (1 * pd.nr + r) * pd.nu;
+      const double* k3e = s_ke + (2 * pd.nr + r) * pd.nu;
+      const double* up = su + c * pd.su;
+      const double* uq = su + (NC + c) * pd.su;
+      double e1q = 0.0, e1p = 0.0, e2q = 0.0, e3p = 0.0;
+      for (int l = 0; l < pd.nu; ++l) {
+        const double a1 = k1e[l], a2 = k2e[l], a3 = k3e[l], xq = uq[l], xp = up[l];
+        e1q = fma(a1, xq, e1q);
+        e1p = fma(a1, xp, e1p);
+        e2q = fma(a2, xq, e2q);
+        e3p = fma(a3, xp, e3p);
+      }
+      double o1q = 0.0, o1p = 0.0, o2q = 0.0, o3p = 0.0;
+      if (pd.nv > 0) {
+        const double* k1o = s_ko + (0 * pd.nr + r) * pd.nv;
+        const double* k2o = s_ko + (1 * pd.nr + r) * pd.nv;
+        const double* k3o = s_ko + (2 * pd.nr + r) * pd.nv;
+        const double* vp = sv + c * pd.sv;
+        const double* vq = sv + (NC + c) * pd.sv;
+        for (int l = 0; l < pd.nv; ++l) {
+          const double a1 = k1o[l], a2 = k2o[l], a3 = k3o[l], xq = vq[l], xp = vp[l];
+          o1q = fma(a1, xq, o1q);
+          o1p = fma(a1, xp, o1p);
+          o2q = fma(a2, xq, o2q);
+          o3p = fma(a3, xp, o3p);
+        }
+      }
+      const double m = prm.mass[c / 3], im = prm.inv_mass[c / 3];
+      xs[c * H + r] = fma(m, e2q + o2q, e1p + o1p);
+      xs[(NC + c) * H + r] = fma(im, e3p + o3p, e1q + o1q);
+      if (pd.split && 2 * r != pd.M) {
+        xs[c * H + pd.M - r] = fma(m, e2q - o2q, e1p - o1p);
+        xs[(NC + c) * H + pd.M - r] = fma(im, e3p - o3p, e1q - o1q);
       }
     }
     group_sync(G);
     if (j < P) {
-      const int r = (j <= P - j) ? j : P - j;  // unique output row
-      const double* K1 = s_prop + r * H;
-      const double* K2 = s_prop + H * H + r * H;
-      const double* K3 = s_prop + 2 * H * H + r * H;
-      double a1[NC], a2[NC], a3[NC], a4[NC];
-#pragma unroll
-      for (int c = 0; c < NC; ++c) { a1[c] = 0.0; a2[c] = 0.0; a3[c] = 0.0; a4[c] = 0.0; }
-      for (int l = 0; l < H; ++l) {
-        const double k1 = K1[l], k2 = K2[l], k3 = K3[l];
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-          const double sp = sym[c * H + l], sq = sym[(NC + c) * H + l];
-          a1[c] = fma(k1, sp, a1[c]);  // K1 p
-          a2[c] = fma(k2, sq, a2[c]);  // K2 q
-          a3[c] = fma(k3, sp, a3[c]);  // K3 p
-          a4[c] = fma(k1, sq, a4[c]);  // K1 q
-        }
-      }
+      const int row = (j <= P - j) ? j : P - j;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        const double m = prm.mass[c / 3], im = prm.inv_mass[c / 3];
-        p[c] = fma(m, a2[c], a1[c]);
-        q[c] = fma(im, a3[c], a4[c]);
+        p[c] = xs[c * H + row];
+        q[c] = xs[(NC + c) * H + row];
       }
     }
 
@@ -373,6 +522,8 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
     // 1/2 kick (src/verlet.f90:1060-1062)
 #pragma unroll
     for (int c = 0; c < NC; ++c) p[c] = p[c] - prm.half_dt * f[c];
+
+    if (nhc) nhc_half();  // src/verlet.f90:1085-1106
 
     // Andersen (src/verlet.f90:1159-1165): full resample every andersen_step
     if (prm.thermostat == CR_THERMO_ANDERSEN && (istep % prm.andersen_step) == 0) {
@@ -480,6 +631,10 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
       prm.f[base + c] = f[c];
     }
     if (j == 0) prm.epot[t] = e[0];
+    if (j == 0 && nhc) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) prm.vnh[4 * (size_t)t + k] = vnh[k];
+    }
     if (status) atomicOr(&prm.status[t], status);
   }
 }

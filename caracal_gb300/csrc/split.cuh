@@ -2,9 +2,11 @@
 // state in registers (QMDFF): the state stays in HBM, laid out
 // q[traj][bead][atom][3], and one step is a short chain of kernels captured
 // in a CUDA graph:
+//   split_nhc_kernel     Nose-Hoover chain (NHC only)
 //   split_drift_kernel   PILE half (if PILE), 1/2 kick, free ring polymer
 //   (force kernel)       dV/dq and V of every bead
 //   split_kick_kernel    1/2 kick, Andersen resample or PILE half
+//   split_nhc_kernel     Nose-Hoover chain (NHC only)
 //   split_finish_kernel  NaN check, transrot, epot per trajectory
 //   split_advance_kernel step counter + 1
 // The order is Caracal's verlet (src/verlet.f90:216-218, 377-463, 772-777,
@@ -52,6 +54,8 @@ struct SplitParams {
   double* epot;            // [T]
   int* status;             // [T]
   int* istep;              // device step counter (last completed step)
+  NhcParams nhc;
+  double* vnh;             // [T][4] Nose-Hoover chain velocities
 };
 
 constexpr int kSplitBlock = 128;
@@ -67,10 +71,6 @@ __host__ __device__ inline size_t split_smem_doubles(const SplitParams& s, bool 
   n += (size_t)2 * cw * (s.su + s.sv);                 // u, v (q and p)
   if (pile) n += (size_t)2 * cw * sp + 2 * (size_t)s.P;  // eta, tmp, circulants
   return n;
-}
-
-__device__ inline double sym_at(const double* x, int l, int P) {
-  return (l == 0 || 2 * l == P) ? x[l] : x[l] + x[P - l];
 }
 
 // Normals of coordinates [c0, c0+cw) of every bead into eta[c][j] (row stride sp).
@@ -400,6 +400,31 @@ __global__ void __launch_bounds__(kFinishBlock) split_finish_kernel(SplitParams 
     }
   }
   if (threadIdx.x == 0 && status) atomicOr(&s.status[t], status);
+}
+
+// nhc (src/nhc.f90:35-171) on one trajectory per block: the kinetic sum
+// p.p/(2m)/P/P over beads and atoms, the chain, one scale of every momentum.
+__global__ void __launch_bounds__(kFinishBlock) split_nhc_kernel(SplitParams s) {
+  __shared__ double red[kFinishBlock];
+  __shared__ double ssc;
+  const int t = blockIdx.x, P = s.P, N = s.N, NC = s.NC;
+  const size_t tb = (size_t)t * P * NC;
+  double ek[1] = {0.0};
+  for (int idx = threadIdx.x; idx < P * N; idx += blockDim.x) {
+    const double* pp = s.p + tb + 3 * (size_t)idx;
+    const double w = s.mass[idx % N];
+    ek[0] = ek[0] + (pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2]) / (2.0 * w) / P / P;
+  }
+  block_sum<1>(ek, red);
+  if (threadIdx.x == 0) {
+    double v[4];
+    for (int k = 0; k < 4; ++k) v[k] = s.vnh[4 * (size_t)t + k];
+    ssc = nhc_scale(s.nhc, ek[0], v);
+    for (int k = 0; k < 4; ++k) s.vnh[4 * (size_t)t + k] = v[k];
+  }
+  __syncthreads();
+  const double sc = ssc;
+  for (int x = threadIdx.x; x < P * NC; x += blockDim.x) s.p[tb + x] = sc * s.p[tb + x];
 }
 
 __global__ void split_advance_kernel(int* istep) { *istep += 1; }

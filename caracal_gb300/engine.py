@@ -21,7 +21,7 @@ from .units import beta_from_kelvin, dt_fs_to_au
 PES = {"h3": L.CR_PES_H3, "ana_h3": L.CR_PES_H3, "ch4h": L.CR_PES_CH4H, "ana_ch4h": L.CR_PES_CH4H}
 PES_NATOMS = {L.CR_PES_H3: 3, L.CR_PES_CH4H: 6}
 THERMOSTAT = {"none": L.CR_THERMO_NONE, "nve": L.CR_THERMO_NONE, "andersen": L.CR_THERMO_ANDERSEN,
-              "nose-hoover": L.CR_THERMO_NHC, "pile": L.CR_THERMO_PILE}
+              "nose-hoover": L.CR_THERMO_NHC, "nhc": L.CR_THERMO_NHC, "pile": L.CR_THERMO_PILE}
 PRECISION = {"fp64": L.CR_PREC_FP64, "plain": L.CR_PREC_FP64, "mixed": L.CR_PREC_MIXED}
 
 
@@ -138,7 +138,7 @@ class RPMDEngine:
 
     def __init__(self, pes, mass, nbeads, ntraj, dt_au, beta=None, thermostat="none",
                  andersen_step=70, pile_tau0_au=0.0, transrot=True, precision="fp64", seed=0,
-                 traj0=0):
+                 traj0=0, nose_q_au=0.0):
         self.ff = pes if isinstance(pes, QMDFFForceField) else None
         if self.ff is not None:
             self.pes = L.CR_PES_QMDFF
@@ -154,7 +154,7 @@ class RPMDEngine:
                               int(andersen_step), int(bool(transrot)),
                               PRECISION[precision] if isinstance(precision, str) else int(precision),
                               int(seed) & 0xFFFFFFFF, int(traj0) & 0xFFFFFFFF, float(dt_au),
-                              self.beta, float(pile_tau0_au), L.dptr(self.mass))
+                              self.beta, float(pile_tau0_au), L.dptr(self.mass), float(nose_q_au))
         h = C.c_void_p()
         if self.ff is not None:
             L.check(L.lib().cr_engine_create_qmdff(C.byref(self.cfg), self.ff._h, C.byref(h)),

@@ -39,3 +39,9 @@ def angstrom_to_bohr(x):
 def temperature_from_ekin(ekin: float, natoms: int, nbeads: int) -> float:
     """Caracal's printed temperature 2 Ekin / (3 k_B N P^2) (src/verlet.f90:1186-1188)."""
     return 2.0 * ekin / 3.0 / K_BOLTZMANN_AU / natoms / nbeads / nbeads
+
+
+def nose_q_to_au(nose_q_steps: float, dt_fs: float) -> float:
+    """NOSE_Q in time steps -> a.u. as Caracal computes it: nose_q*dt/2.41888428E-2
+    with dt still in fs (src/dynamic.f90:578)."""
+    return float(nose_q_steps) * float(dt_fs) / FS_PER_AU_REAL4

@@ -43,7 +43,7 @@ extern "C" {
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
 #define CR_THERMO_NONE 0      /* NVE */
 #define CR_THERMO_ANDERSEN 1  /* src/andersen.f90 */
-#define CR_THERMO_NHC 2       /* src/nhc.f90 (not built yet) */
+#define CR_THERMO_NHC 2       /* Nose-Hoover chain, src/nhc.f90 */
 #define CR_THERMO_PILE 3      /* PILE-L, new (Ceriotti et al. 2010) */
 
 /* ---- precision forms ------------------------------------------------------ */
@@ -65,6 +65,7 @@ typedef struct cr_config {
   double beta;        /* 1/(k_B T), a.u., k_B = 0.316679e-5 Eh/K */
   double pile_tau0;   /* PILE centroid time constant, a.u. */
   const double* mass; /* natoms masses, a.u. (amu / 5.485799095e-4) */
+  double nose_q;      /* NHC chain time, a.u.: NOSE_Q (in time steps) x dt (src/dynamic.f90:578) */
 } cr_config;
 
 typedef struct cr_engine cr_engine;

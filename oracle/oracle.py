@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 PES_IDS = {"h3": 1, "ch4h": 2, "qmdff": 4}
-THERMOSTATS = {"none": 0, "andersen": 1, "pile": 3}
+THERMOSTATS = {"none": 0, "andersen": 1, "nose-hoover": 2, "nhc": 2, "pile": 3}
 OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",
                   "acos", "erf", "cmp", "tanh", "cosh")
 
@@ -38,7 +38,7 @@ class Cfg(C.Structure):
     _fields_ = [("pes", C.c_int), ("natoms", C.c_int), ("nbeads", C.c_int),
                 ("thermostat", C.c_int), ("andersen_step", C.c_int), ("transrot", C.c_int),
                 ("seed", C.c_uint32), ("dt", C.c_double), ("beta", C.c_double),
-                ("pile_tau0", C.c_double), ("mass", C.POINTER(C.c_double))]
+                ("pile_tau0", C.c_double), ("mass", C.POINTER(C.c_double)), ("nose_q", C.c_double)]
 
 
 class QmdffDef(C.Structure):
@@ -127,8 +127,9 @@ def lib():
         _lib.orc_init_momenta.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, d]
         _lib.orc_init_forces.argtypes = [C.POINTER(Cfg), C.c_int, d, d, d]
         _lib.orc_run.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_int, C.c_int, d, d, d, d,
-                                 C.POINTER(C.c_int), C.c_int]
+                                 C.POINTER(C.c_int), C.c_int, d]
         _lib.orc_qmdff_set.argtypes = [C.POINTER(QmdffDef)]
+        _lib.orc_nhc_half.argtypes = [C.POINTER(Cfg), d, d]
         _lib.orc_calc_xi.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d]
         _lib.orc_calc_xi.restype = C.c_double
         _lib.orc_recross_children.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, d,
@@ -146,14 +147,15 @@ class Config:
     """Step configuration for the oracle (all quantities in atomic units)."""
 
     def __init__(self, pes, mass, nbeads, dt, beta, thermostat="none", andersen_step=70,
-                 pile_tau0=0.0, transrot=True, seed=0):
+                 pile_tau0=0.0, transrot=True, seed=0, nose_q=0.0):
         self.mass = np.ascontiguousarray(mass, dtype=np.float64)
         self.natoms = len(self.mass)
         self.nbeads = int(nbeads)
+        self.thermostat = THERMOSTATS[thermostat]
         self.c = Cfg(PES_IDS[pes] if isinstance(pes, str) else int(pes), self.natoms,
-                     self.nbeads, THERMOSTATS[thermostat], int(andersen_step), int(bool(transrot)),
+                     self.nbeads, self.thermostat, int(andersen_step), int(bool(transrot)),
                      int(seed) & 0xFFFFFFFF, float(dt), float(beta), float(pile_tau0),
-                     _dp(self.mass))
+                     _dp(self.mass), float(nose_q))
 
     def shape(self, ntraj):
         return (ntraj, self.nbeads, self.natoms, 3)
@@ -237,16 +239,24 @@ def init_forces(cfg: Config, q):
     return f, e
 
 
-def run(cfg: Config, q, p, f, nsteps, istep0=0, traj0=0, nthreads=0):
-    """Advance copies of (q, p, f) by nsteps; returns (q, p, f, epot, status)."""
+def run(cfg: Config, q, p, f, nsteps, istep0=0, traj0=0, nthreads=0, vnh=None):
+    """Advance copies of (q, p, f) by nsteps; returns (q, p, f, epot, status).
+    For the Nose-Hoover chain, vnh (ntraj, 4) is the chain state, updated in
+    place (zeros when None, as after mdinit)."""
     q = np.array(q, dtype=np.float64)
     p = np.array(p, dtype=np.float64)
     f = np.array(f, dtype=np.float64)
     T = q.shape[0]
     e = np.zeros(T)
     st = np.zeros(T, dtype=np.int32)
+    if cfg.thermostat == 2 and vnh is None:
+        vnh = np.zeros((T, 4))
+    vp = None
+    if vnh is not None:
+        assert vnh.dtype == np.float64 and vnh.flags.c_contiguous and vnh.shape == (T, 4)
+        vp = _dp(vnh)
     lib().orc_run(C.byref(cfg.c), T, traj0, istep0, nsteps, _dp(q), _dp(p), _dp(f), _dp(e),
-                  st.ctypes.data_as(C.POINTER(C.c_int)), nthreads)
+                  st.ctypes.data_as(C.POINTER(C.c_int)), nthreads, vp)
     return q, p, f, e, st
 
 
@@ -277,3 +287,11 @@ def recross_children(cfg: Config, xd, ntraj, q_parent, nsteps, traj0=0, nthreads
                                _dp(den), _dp(w), _dp(q) if states else None,
                                _dp(p) if states else None, nthreads)
     return (num, den[0], w, q, p) if states else (num, den[0], w)
+
+
+def nhc_half(cfg: Config, vnh, p):
+    """One Nose-Hoover chain call on one trajectory: returns (vnh, p) updated."""
+    v = np.array(vnh, dtype=np.float64)
+    pp = np.array(p, dtype=np.float64)
+    lib().orc_nhc_half(C.byref(cfg.c), _dp(v), _dp(pp))
+    return v, pp

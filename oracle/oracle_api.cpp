@@ -27,6 +27,7 @@ orc::StepConfig to_step(const orc_cfg* c) {
   s.thermostat = c->thermostat;
   s.andersen_step = c->andersen_step > 0 ? c->andersen_step : 1;
   s.pile_tau0 = c->pile_tau0;
+  s.nose_q = c->nose_q;
   s.transrot = c->transrot;
   s.seed = c->seed;
   s.mass = c->mass;
@@ -153,7 +154,8 @@ int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, do
 }
 
 int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q,
-            double* p, double* f, double* epot, int* status, int nthreads) {
+            double* p, double* f, double* epot, int* status, int nthreads, double* vnh) {
+  if (cf->thermostat == 2 && !vnh) return -1;
   orc::StepConfig s = to_step(cf);
   BeadPES pes{cf->pes, cf->natoms};
   const size_t per = (size_t)3 * cf->natoms * cf->nbeads;
@@ -165,11 +167,17 @@ int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps
     int st = 0;
     double e = 0.0;
     for (int n = 1; n <= nsteps; ++n)
-      st |= orc::verlet_step(s, traj0 + t, istep0 + n, &q[t * per], &p[t * per], &f[t * per], &e, pes);
+      st |= orc::verlet_step(s, traj0 + t, istep0 + n, &q[t * per], &p[t * per], &f[t * per], &e, pes,
+                             vnh ? &vnh[4 * (size_t)t] : nullptr);
     if (epot) epot[t] = e;
     if (status) status[t] |= st;
   }
   return 0;
+}
+
+void orc_nhc_half(const orc_cfg* cf, double* vnh, double* p) {
+  orc::StepConfig s = to_step(cf);
+  orc::nhc_half(s, vnh, p);
 }
 
 static orc::XiDef to_xi(const orc_xidef* x) {

@@ -15,7 +15,7 @@ typedef struct orc_cfg {
   int pes;            /* 1 = H3 (BKMP2), 2 = CH4H, 4 = QMDFF (orc_qmdff_set) */
   int natoms;
   int nbeads;
-  int thermostat;     /* 0 none, 1 Andersen, 3 PILE */
+  int thermostat;     /* 0 none, 1 Andersen, 2 Nose-Hoover chain, 3 PILE */
   int andersen_step;
   int transrot;       /* 1: remove COM translation/rotation every step */
   uint32_t seed;
@@ -23,6 +23,7 @@ typedef struct orc_cfg {
   double beta;        /* a.u. */
   double pile_tau0;   /* a.u. */
   const double* mass; /* natoms, a.u. */
+  double nose_q;      /* a.u.: NOSE_Q (time steps) x dt */
 } orc_cfg;
 
 void orc_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]);
@@ -43,9 +44,13 @@ void orc_init_momenta(const orc_cfg* cf, int ntraj, uint32_t traj0, double* p);
 /* mdinit: forces of the initial positions; epot[t] = sum over beads */
 int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, double* epot);
 /* nsteps verlet steps (istep0+1 .. istep0+nsteps) of ntraj trajectories;
- * status[t] ORs the per-step status bits; nthreads <= 0 uses all cores. */
+ * status[t] ORs the per-step status bits; nthreads <= 0 uses all cores.
+ * vnh[4 * ntraj]: Nose-Hoover chain velocities (in/out; NULL unless
+ * thermostat 2). */
 int orc_run(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q,
-            double* p, double* f, double* epot, int* status, int nthreads);
+            double* p, double* f, double* epot, int* status, int nthreads, double* vnh);
+/* One nhc call (src/nhc.f90) on one trajectory's p(3,natoms,nbeads); vnh[4] in/out. */
+void orc_nhc_half(const orc_cfg* cf, double* vnh, double* p);
 /* QMDFF definition (0-based atoms); per-NCI-pair R0, C6, sr42, zab, alpha. */
 typedef struct orc_qmdff_def {
   int natoms;

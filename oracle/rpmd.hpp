@@ -8,6 +8,7 @@
 //   per-bead forces                src/verlet.f90:772-777
 //   1/2 kick                       src/verlet.f90:1060-1062
 //   Andersen every andersen_step   src/verlet.f90:1159-1165, src/andersen.f90:37-71
+//   Nose-Hoover chain              src/verlet.f90:186-208 and 1085-1106, src/nhc.f90
 //   kinetic energy / temperature   src/verlet.f90:1174-1188
 //   NaN / Inf stop                 src/verlet.f90:1256-1275
 //   transrot (constrain <= 0)      src/verlet.f90:1300-1306, src/transrot.f90:36-237
@@ -39,9 +40,10 @@ struct StepConfig {
   int nbeads = 1;
   double dt = 0.0;        // a.u.
   double beta = 0.0;      // 1/(k_B T), a.u.; +inf allowed only for nbeads == 1
-  int thermostat = 0;     // 0 none, 1 Andersen, 3 PILE
+  int thermostat = 0;     // 0 none, 1 Andersen, 2 Nose-Hoover chain, 3 PILE
   int andersen_step = 70;
   double pile_tau0 = 0.0; // a.u. (centroid friction 1/tau0)
+  double nose_q = 0.0;    // a.u. (NOSE_Q time steps x dt, src/dynamic.f90:578)
   int transrot = 1;       // 1: remove COM translation/rotation (constrain <= 0)
   uint32_t seed = 0;
   const double* mass = nullptr;  // natoms, a.u.
@@ -348,6 +350,68 @@ inline double kinetic_energy(const StepConfig& cf, const double* p) {
   return e;
 }
 
+// Nose-Hoover chain (src/nhc.f90:35-171): 4 links, nc = 5 Suzuki-Yoshida
+// passes of ns = 3 weights, one global scale of every momentum.  The chain
+// masses come from mdinit (src/mdinit.f90:128-147): Q = k_B T nose_q^2 with
+// k_B = 0.316679D-5, Q_1 = 3N Q.  nhc's own kT is 1.380649E-23/4.3597447E-18
+// * kelvin, a REAL(4) quotient, kelvin = 1/(beta k_B).  vnh[4] is the chain
+// velocity state of one trajectory (zero at mdinit).
+inline void nhc_half(const StepConfig& cf, double* vnh, double* p) {
+  const int N = cf.natoms, P = cf.nbeads;
+  const double kelvin = 1.0 / (cf.beta * kBoltzmannAu);
+  const double ekt_md = kBoltzmannAu * kelvin;
+  const double qterm = ekt_md * cf.nose_q * cf.nose_q;
+  const int nfree = 3 * N;
+  double qnh[4] = {(double)nfree * qterm, qterm, qterm, qterm};
+  double gnh[4] = {0.0, 0.0, 0.0, 0.0};
+  const double ekt = (double)(1.380649E-23f / 4.3597447E-18f) * kelvin;
+  const int nc = 5, ns = 3;
+  const double dtc = cf.dt / (double)nc;
+  double w[3];
+  w[0] = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0));
+  w[1] = 1.0 - 2.0 * w[0];
+  w[2] = w[0];
+  double scale = 1.0;
+  double eksum = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < P; ++k) {
+      const double* pp = &p[(k * N + i) * 3];
+      eksum = eksum + (pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2]) / (2.0 * cf.mass[i]) / P / P;
+    }
+  for (int ic = 0; ic < nc; ++ic)
+    for (int j = 0; j < ns; ++j) {
+      const double dts = w[j] * dtc;
+      const double dt2 = 0.5 * dts, dt4 = 0.25 * dts, dt8 = 0.125 * dts;
+      double ex;
+      gnh[3] = (qnh[2] * vnh[2] * vnh[2] - ekt) / qnh[3];
+      vnh[3] = vnh[3] + gnh[3] * dt4;
+      gnh[2] = (qnh[1] * vnh[1] * vnh[1] - ekt) / qnh[2];
+      ex = std::exp(-vnh[3] * dt8);
+      vnh[2] = ex * (vnh[2] * ex + gnh[2] * dt4);
+      gnh[1] = (qnh[0] * vnh[0] * vnh[0] - ekt) / qnh[1];
+      ex = std::exp(-vnh[2] * dt8);
+      vnh[1] = ex * (vnh[1] * ex + gnh[1] * dt4);
+      gnh[0] = (2.0 * eksum - (double)nfree * ekt) / qnh[0];
+      ex = std::exp(-vnh[1] * dt8);
+      vnh[0] = ex * (vnh[0] * ex + gnh[0] * dt4);
+      ex = std::exp(-vnh[0] * dt2);
+      scale = scale * ex;
+      eksum = eksum * ex * ex;
+      gnh[0] = (2.0 * eksum - (double)nfree * ekt) / qnh[0];
+      ex = std::exp(-vnh[1] * dt8);
+      vnh[0] = ex * (vnh[0] * ex + gnh[0] * dt4);
+      gnh[1] = (qnh[0] * vnh[0] * vnh[0] - ekt) / qnh[1];
+      ex = std::exp(-vnh[2] * dt8);
+      vnh[1] = ex * (vnh[1] * ex + gnh[1] * dt4);
+      gnh[2] = (qnh[1] * vnh[1] * vnh[1] - ekt) / qnh[2];
+      ex = std::exp(-vnh[3] * dt8);
+      vnh[2] = ex * (vnh[2] * ex + gnh[2] * dt4);
+      gnh[3] = (qnh[2] * vnh[2] * vnh[2] - ekt) / qnh[3];
+      vnh[3] = vnh[3] + gnh[3] * dt4;
+    }
+  for (int x = 0; x < 3 * N * P; ++x) p[x] = scale * p[x];
+}
+
 // Trajectory status bits (shared meaning with the engine).
 enum TrajStatus : int { TRAJ_OK = 0, TRAJ_NONFINITE = 1, TRAJ_SINGULAR_INERTIA = 2 };
 
@@ -355,9 +419,10 @@ enum TrajStatus : int { TRAJ_OK = 0, TRAJ_NONFINITE = 1, TRAJ_SINGULAR_INERTIA =
 // bead; f holds dV/dq of the previous step on entry and of this step on exit.
 template <class EGrad>
 inline int verlet_step(const StepConfig& cf, uint32_t traj, int istep, double* q, double* p,
-                       double* f, double* epot, EGrad egrad) {
+                       double* f, double* epot, EGrad egrad, double* vnh = nullptr) {
   const int N = cf.natoms, P = cf.nbeads, n3 = 3 * N;
   const size_t nall = (size_t)n3 * P;
+  if (cf.thermostat == 2) nhc_half(cf, vnh, p);  // src/verlet.f90:186-208
   if (cf.thermostat == 3) pile_half(cf, traj, (uint32_t)istep, TAG_PILE_A, p);
   for (size_t x = 0; x < nall; ++x) p[x] = p[x] - 0.5 * cf.dt * f[x];
   free_rp_step(cf, q, p);
@@ -369,6 +434,7 @@ inline int verlet_step(const StepConfig& cf, uint32_t traj, int istep, double* q
   }
   *epot = e;
   for (size_t x = 0; x < nall; ++x) p[x] = p[x] - 0.5 * cf.dt * f[x];
+  if (cf.thermostat == 2) nhc_half(cf, vnh, p);  // src/verlet.f90:1085-1106
   if (cf.thermostat == 1 && istep % cf.andersen_step == 0)
     andersen(cf, traj, (uint32_t)istep, TAG_ANDERSEN, p);
   if (cf.thermostat == 3) pile_half(cf, traj, (uint32_t)istep, TAG_PILE_B, p);
