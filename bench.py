@@ -476,6 +476,10 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, target_s=args.cpu_seconds)
+    if wl.pes == "qmdff":
+        gff = wl.extra["gpu_ff"]
+        line["autotune"] = {"qmdff_egrad_kernel": {"fp64": gff.tuning("fp64"), "mixed": gff.tuning("mixed"),
+                                                   "variants": "min blocks/SM 2,3,4 (fp64); 4,5,6 (mixed)"}}
     mp = measured_peaks()
     if mp:
         line["measured_peaks_file"] = {k: mp.get(k) for k in ("hbm_gbs", "bf16_tflops", "gpu_name")}

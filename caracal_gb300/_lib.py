@@ -116,6 +116,7 @@ def _sig(lib):
         "cr_qmdff_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
         "cr_qmdff_egrad_device": ([v, v, C.c_int, v, v, C.c_int, v], C.c_int),
         "cr_qmdff_schedule_info": ([v, i, i], C.c_int),
+        "cr_qmdff_tuning": ([v, C.c_int, i, C.POINTER(C.c_float)], C.c_int),
         "cr_engine_create_qmdff": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
     }
     for name, (args, res) in sigs.items():

@@ -369,6 +369,16 @@ int split_run(cr_engine* e, int nsteps) {
     // the force kernel sets its own shared-memory limit outside the capture
     int rc = qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
     if (rc) return rc;
+    // let the autotuner pick the force-kernel variant on this batch before it
+    // is frozen into the graph; the gradient goes to scratch so f is untouched
+    const size_t nall = (size_t)e->T * e->P * e->NC;
+    double* scratch = nullptr;
+    if (cudaMalloc(&scratch, nall * sizeof(double)) == cudaSuccess) {
+      rc = qmdff_launch(e->ff, e->d_q, e->T * e->P, e->d_V, scratch, e->cfg.precision, e->stream);
+      cudaStreamSynchronize(e->stream);
+      cudaFree(scratch);
+      if (rc) return rc;
+    }
     CR_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     rc = split_step_launches(e);
     cudaGraph_t g = nullptr;
@@ -590,7 +600,7 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
   if (cfg->thermostat == CR_THERMO_NHC && !(cfg->nose_q > 0.0 && std::isfinite(cfg->nose_q)))
     return fail(CR_ERR_ARG, "the Nose-Hoover chain needs nose_q > 0");
   if (cfg->thermostat != CR_THERMO_NONE && cfg->thermostat != CR_THERMO_ANDERSEN &&
-      cfg->thermostat != CR_THERMO_PILE)
+      cfg->thermostat != CR_THERMO_NHC && cfg->thermostat != CR_THERMO_PILE)
     return fail(CR_ERR_ARG, "unknown thermostat");
   if (cfg->precision != CR_PREC_FP64 && cfg->precision != CR_PREC_MIXED)
     return fail(CR_ERR_ARG, "unknown precision");

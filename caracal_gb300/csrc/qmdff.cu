@@ -83,9 +83,12 @@ std::vector<float> to_float(const std::vector<T>& v) {
 
 namespace cr {
 
-template <bool MIXED>
-__global__ void __launch_bounds__(kQmdffWarps * 32) qmdff_egrad_kernel(qmdff::Dev D, int nbeads, const double* q,
-                                                                      double* e, double* g) {
+// MINB: blocks of kQmdffWarps warps kept resident per SM (the register cap
+// follows: 65536 / (MINB * 128) per thread).  The FP64 form trades spills for
+// occupancy differently from the mixed form; the autotuner below picks.
+template <bool MIXED, int MINB>
+__global__ void __launch_bounds__(kQmdffWarps * 32, MINB)
+    qmdff_egrad_kernel(qmdff::Dev D, int nbeads, const double* q, double* e, double* g) {
   extern __shared__ double qsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n3 = 3 * D.n;
@@ -102,29 +105,79 @@ __global__ void __launch_bounds__(kQmdffWarps * 32) qmdff_egrad_kernel(qmdff::De
 
 }  // namespace cr
 
-int qmdff_launch(const cr_qmdff* ff, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
-                 cudaStream_t s) {
-  if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
+namespace {
+
+using QmdffKernel = void (*)(cr::qmdff::Dev, int, const double*, double*, double*);
+constexpr int kVariants = 3;
+// [precision][variant]: blocks per SM 2 / 3 / 4 (FP64), 4 / 5 / 6 (mixed)
+const QmdffKernel kKernels[2][kVariants] = {
+    {cr::qmdff_egrad_kernel<false, 2>, cr::qmdff_egrad_kernel<false, 3>, cr::qmdff_egrad_kernel<false, 4>},
+    {cr::qmdff_egrad_kernel<true, 4>, cr::qmdff_egrad_kernel<true, 5>, cr::qmdff_egrad_kernel<true, 6>}};
+constexpr int kDefaultVariant = 1;
+constexpr int kTuneMinBeads = 2048;  // smaller batches keep the default
+
+int launch_variant(const cr_qmdff* ff, int prec, int v, const double* d_q, int nbeads, double* d_e, double* d_g,
+                   cudaStream_t s) {
   const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(ff->n);
-  // the attribute is set even for nbeads = 0, so a caller can prepare the
-  // kernel before a stream capture
-  if (smem > 48 * 1024) {
-    if (precision == CR_PREC_MIXED)
-      CR_TRY_CUDA(cudaFuncSetAttribute(cr::qmdff_egrad_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-    else
-      CR_TRY_CUDA(cudaFuncSetAttribute(cr::qmdff_egrad_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-  }
-  if (nbeads <= 0) return CR_OK;
   int grid = (nbeads + kQmdffWarps - 1) / kQmdffWarps;
   if (grid > 1 << 20) grid = 1 << 20;
-  if (precision == CR_PREC_MIXED)
-    cr::qmdff_egrad_kernel<true><<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, nbeads, d_q, d_e, d_g);
-  else
-    cr::qmdff_egrad_kernel<false><<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, nbeads, d_q, d_e, d_g);
+  kKernels[prec][v]<<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, nbeads, d_q, d_e, d_g);
   CR_TRY_CUDA(cudaGetLastError());
   return CR_OK;
+}
+
+}  // namespace
+
+// Autotuner: the first launch with at least kTuneMinBeads beads outside a
+// stream capture times every variant once on the caller's data (each writes
+// the same outputs) and keeps the fastest for this force field and form.
+int qmdff_launch(const cr_qmdff* ff_c, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
+                 cudaStream_t s) {
+  cr_qmdff* ff = const_cast<cr_qmdff*>(ff_c);
+  if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
+  const int prec = precision == CR_PREC_MIXED ? 1 : 0;
+  const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(ff->n);
+  // the attribute is set even for nbeads = 0, so a caller can prepare the
+  // kernels before a stream capture
+  if (smem > 48 * 1024)
+    for (int v = 0; v < kVariants; ++v)
+      CR_TRY_CUDA(cudaFuncSetAttribute(kKernels[prec][v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nbeads <= 0) return CR_OK;
+  int choice = ff->variant[prec];
+  if (choice < 0) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CR_TRY_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (nbeads >= kTuneMinBeads && cap == cudaStreamCaptureStatusNone) {
+      cudaEvent_t a, b;
+      CR_TRY_CUDA(cudaEventCreate(&a));
+      CR_TRY_CUDA(cudaEventCreate(&b));
+      float best = 0.f;
+      for (int v = 0; v < kVariants; ++v) {
+        cudaEventRecord(a, s);
+        int rc = launch_variant(ff, prec, v, d_q, nbeads, d_e, d_g, s);
+        if (rc) {
+          cudaEventDestroy(a);
+          cudaEventDestroy(b);
+          return rc;
+        }
+        cudaEventRecord(b, s);
+        CR_TRY_CUDA(cudaEventSynchronize(b));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        ff->tune_ms[prec][v] = ms;
+        if (v == 0 || ms < best) {
+          best = ms;
+          choice = v;
+        }
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      ff->variant[prec] = choice;
+      return CR_OK;  // the last variant's outputs equal the chosen one's
+    }
+    choice = kDefaultVariant;
+  }
+  return launch_variant(ff, prec, choice, d_q, nbeads, d_e, d_g, s);
 }
 
 extern "C" {
@@ -294,6 +347,16 @@ int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors) {
   if (batches)
     for (int k = 0; k < 4; ++k) batches[k] = ff->dev.nb[k];
   if (colors) *colors = ff->ncolors;
+  return CR_OK;
+}
+
+int cr_qmdff_tuning(const cr_qmdff* ff, int precision, int* variant, float* ms) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
+  const int prec = precision == CR_PREC_MIXED ? 1 : 0;
+  if (variant) *variant = ff->variant[prec];
+  if (ms)
+    for (int v = 0; v < kVariants; ++v) ms[v] = ff->tune_ms[prec][v];
   return CR_OK;
 }
 

@@ -124,27 +124,17 @@ struct Grad<float> {
   __device__ inline double get(int i) const { return (double)s[i] + (double)k[i]; }
 };
 
-// Adds a term's gradient for its NA atoms (compile-time count).  With
-// distinct atoms (checked on the host, `Dev::distinct`) all loads are issued
-// before the stores, so the shared-memory round trips overlap.
+// Adds a term's gradient for its NA atoms (compile-time count).  Mixed form
+// with distinct atoms (checked on the host, `Dev::distinct`): all loads are
+// issued before the stores, so the shared-memory round trips overlap.  The
+// FP64 form is bound by the FP64 pipe, not by these round trips, and keeps
+// the sequential adds (fewer live registers).
 template <int NA>
-__device__ inline void scatter(const Contrib<double>& c, Grad<double>& G, bool distinct) {
-  if (distinct) {
-    double v[NA][3];
+__device__ inline void scatter(const Contrib<double>& c, Grad<double>& G, bool) {
 #pragma unroll
-    for (int m = 0; m < NA; ++m)
+  for (int m = 0; m < NA; ++m)
 #pragma unroll
-      for (int d = 0; d < 3; ++d) v[m][d] = G.g[3 * c.a[m] + d];
-#pragma unroll
-    for (int m = 0; m < NA; ++m)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) G.g[3 * c.a[m] + d] = v[m][d] + c.g[m][d];
-  } else {
-#pragma unroll
-    for (int m = 0; m < NA; ++m)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
-  }
+    for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
 }
 template <int NA>
 __device__ inline void scatter(const Contrib<float>& c, Grad<float>& G, bool distinct) {

@@ -13,6 +13,8 @@ struct cr_qmdff {
   int ncolors = 0;              // colours summed over batches
   cr::qmdff::Dev dev{};
   std::vector<void*> allocs;    // device buffers owned by the force field
+  int variant[2] = {-1, -1};    // autotuned kernel variant per form (FP64, mixed); -1: not yet
+  float tune_ms[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 };
 
 // Warps per block of the QMDFF force kernel and its dynamic shared memory.

@@ -118,6 +118,14 @@ class QMDFFForceField:
         L.check(L.lib().cr_qmdff_schedule_info(self._h, L.iptr(b), C.byref(c)), "schedule_info")
         return {"batches": b.tolist(), "colors": c.value}
 
+    def tuning(self, precision="fp64"):
+        """The autotuner's choice and timings of the force-kernel variants."""
+        v = C.c_int()
+        ms = (C.c_float * 3)()
+        prec = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        L.check(L.lib().cr_qmdff_tuning(self._h, prec, C.byref(v), ms), "qmdff_tuning")
+        return {"variant": v.value, "ms": list(ms)}
+
     def close(self):
         if getattr(self, "_h", None):
             L.lib().cr_qmdff_destroy(self._h)

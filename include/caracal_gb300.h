@@ -156,6 +156,11 @@ int cr_qmdff_egrad_device(cr_qmdff* ff, const double* d_xyz, int nbeads, double*
 /* Term batches of the warp schedule (bonds, angles, torsions, NCI pairs) and
  * the colours they need (diagnostics). */
 int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors);
+/* No counterpart in Caracal.  The force kernel comes in three occupancy
+ * variants per form; the first launch of >= 2048 beads outside a stream
+ * capture times each once and keeps the fastest.  variant = -1 before that;
+ * ms[3] = the measured times. */
+int cr_qmdff_tuning(const cr_qmdff* ff, int precision, int* variant, float* ms);
 
 /* ---- RPMD engine -----------------------------------------------------------
  * Replaces the stepping loop of `dynamic` (src/dynamic.f90:1569-1579) around

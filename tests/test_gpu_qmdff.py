@@ -61,6 +61,20 @@ def test_egrad_fp64_matches_oracle(gpu_ff, alkane):
     assert rel_err(g, go) <= 1e-12
 
 
+def test_autotuner_picks_a_variant_and_keeps_parity(alkane, require_gpu):
+    ff = QMDFFForceField(alkane)
+    assert ff.tuning("fp64")["variant"] == -1
+    x = geoms(alkane, 2048, 0.1, 9)
+    e, g = ff.egrad(x, "fp64")          # first launch of >= 2048 beads: tunes
+    t = ff.tuning("fp64")
+    e2, g2 = ff.egrad(x, "fp64")        # the chosen variant
+    ff.close()
+    assert t["variant"] in (0, 1, 2) and min(t["ms"]) > 0.0
+    eo, go = orc.egrad("qmdff", x)
+    assert rel_err(e2, eo) <= 1e-12 and rel_err(g2, go) <= 1e-12
+    assert rel_err(e, eo) <= 1e-12 and rel_err(g, go) <= 1e-12
+
+
 def test_egrad_mixed_error(gpu_ff, alkane):
     x = geoms(alkane, 256, 0.1, 2)
     e, g = gpu_ff.egrad(x, "mixed")
