@@ -91,6 +91,8 @@ def _sig(lib):
         "cr_egrad_h3_device": ([v, C.c_int, v, v, C.c_int, v], C.c_int),
         "cr_egrad_ch4h": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
         "cr_initialize_ch4h": ([], C.c_int),
+        "cr_egrad_ch4oh": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
+        "cr_initialize_ch4oh": ([], C.c_int),
         "cr_egrad_device": ([C.c_int, v, C.c_int, v, v, C.c_int, v], C.c_int),
         "cr_engine_create": ([C.POINTER(CrConfig), C.POINTER(C.c_void_p)], C.c_int),
         "cr_engine_destroy": ([eng], C.c_int),

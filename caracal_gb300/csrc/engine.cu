@@ -10,6 +10,7 @@
 #include "../../include/caracal_gb300.h"
 #include "cr_common.cuh"
 #include "pes_ch4h.cuh"
+#include "pes_ch4oh.cuh"
 #include "pes_h3.cuh"
 #include "rpmd_kernel.cuh"
 #include "host_util.h"
@@ -44,6 +45,7 @@ int pes_natoms(int pes) {
   switch (pes) {
     case CR_PES_H3: return 3;
     case CR_PES_CH4H: return 6;
+    case CR_PES_CH4OH: return 7;
     default: return -1;
   }
 }
@@ -402,6 +404,7 @@ int dispatch_run(cr_engine* e, int nsteps) {
   switch (e->cfg.pes) {
     case CR_PES_H3: return launch_run<cr::PesH3>(e, nsteps);
     case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, nsteps);
+    case CR_PES_CH4OH: return launch_run<cr::PesCH4OH>(e, nsteps);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -417,6 +420,7 @@ int dispatch_forces(cr_engine* e) {
   switch (e->cfg.pes) {
     case CR_PES_H3: return launch_forces<cr::PesH3>(e);
     case CR_PES_CH4H: return launch_forces<cr::PesCH4H>(e);
+    case CR_PES_CH4OH: return launch_forces<cr::PesCH4OH>(e);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -532,6 +536,7 @@ int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d
   switch (pes) {
     case CR_PES_H3: return egrad_device_impl<cr::PesH3>(d_q, npts, d_V, d_dVdq, precision, s);
     case CR_PES_CH4H: return egrad_device_impl<cr::PesCH4H>(d_q, npts, d_V, d_dVdq, precision, s);
+    case CR_PES_CH4OH: return egrad_device_impl<cr::PesCH4OH>(d_q, npts, d_V, d_dVdq, precision, s);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -546,6 +551,12 @@ int cr_egrad_ch4h(const double* q, int natoms, int nbeads, double* V, double* dV
 }
 
 int cr_initialize_ch4h(void) { return CR_OK; }
+
+int cr_egrad_ch4oh(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
+  return egrad_host(CR_PES_CH4OH, 7, q, natoms, nbeads, V, dVdq, info);
+}
+
+int cr_initialize_ch4oh(void) { return CR_OK; }
 
 int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
   if (info) *info = 0;
@@ -853,6 +864,10 @@ int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
       cr::init_positions_kernel<18><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
       break;
+    case CR_PES_CH4OH:
+      cr::init_positions_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
+      break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
   CR_CUDA(cudaGetLastError());
@@ -882,6 +897,10 @@ int cr_engine_init_momenta(cr_engine* e, int zero) {
       break;
     case CR_PES_CH4H:
       cr::init_momenta_kernel<18><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+      break;
+    case CR_PES_CH4OH:
+      cr::init_momenta_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
       break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
@@ -1086,6 +1105,10 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
       cr::init_children_kernel<18><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
       break;
+    case CR_PES_CH4OH:
+      cr::init_children_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
+      break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
   CR_CUDA(cudaGetLastError());
@@ -1098,6 +1121,9 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
       break;
     case CR_PES_CH4H:
       cr::child_flux_kernel<6><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
+      break;
+    case CR_PES_CH4OH:
+      cr::child_flux_kernel<7><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
       break;
     default: break;
   }

@@ -119,3 +119,21 @@ def qmdff_config(ntraj=1024, nbeads=64, nsteps=500, kelvin=300.0, dt_fs=0.5, nc=
                     q0=ff.xyz.copy(), nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs,
                     nsteps=nsteps, thermostat=thermostat, andersen_step=andersen_step,
                     sigma_bohr=float(angstrom_to_bohr(0.01)), transrot=True, extra={"ff": ff})
+
+
+def ch4oh_geometry(r_ch_ang=1.09, r_ho_ang=1.3, r_oh_ang=0.97, angle_deg=100.0):
+    """CH4 (tetrahedral, r(CH) = r_ch) + OH with O collinear with one C-H bond,
+    r_ho beyond that bond's H, and the hydroxyl H at r_oh from O bent by angle_deg
+    from the C-H axis, in Caracal's atom order for ANA_CH4OH: H (the attacked
+    methane H), C, H, H, H, O, H(O)."""
+    s3 = 1.0 / np.sqrt(3.0)
+    v = np.array([[s3, s3, s3], [s3, -s3, -s3], [-s3, s3, -s3], [-s3, -s3, s3]])
+    q = np.zeros((7, 3))
+    q[0] = v[0] * r_ch_ang
+    q[2], q[3], q[4] = v[1] * r_ch_ang, v[2] * r_ch_ang, v[3] * r_ch_ang
+    q[5] = v[0] * (r_ch_ang + r_ho_ang)
+    perp = np.cross(v[0], [0.0, 0.0, 1.0])
+    perp /= np.linalg.norm(perp)
+    a = np.radians(angle_deg)
+    q[6] = q[5] + (-v[0] * np.cos(a) + perp * np.sin(a)) * r_oh_ang
+    return angstrom_to_bohr(q)

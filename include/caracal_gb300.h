@@ -37,7 +37,7 @@ extern "C" {
 /* ---- potentials (Caracal keyword PES) ----------------------------------- */
 #define CR_PES_H3 1      /* ANA_H3: BKMP2, src/egrad_h3.f */
 #define CR_PES_CH4H 2    /* ANA_CH4H: src/egrad_ch4h.f + src/util_ch4h.f */
-#define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f (not built yet) */
+#define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f + src/util_ch4oh.f */
 #define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90 (ff_hb not built yet) */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
@@ -52,7 +52,7 @@ extern "C" {
 
 typedef struct cr_config {
   int pes;            /* CR_PES_* */
-  int natoms;         /* must match the PES (H3: 3, CH4H: 6, QMDFF: the force field's n) */
+  int natoms;         /* must match the PES (H3: 3, CH4H: 6, CH4OH: 7, QMDFF: the force field's n) */
   int nbeads;         /* 1..128 (RPMD_BEADS) */
   int ntraj;          /* independent trajectories in this engine */
   int thermostat;     /* CR_THERMO_* */
@@ -109,6 +109,14 @@ int cr_egrad_ch4h(const double* q, int natoms, int nbeads, double* V, double* dV
  * src/read_pes.f90:551).  The surface's constants are compiled in, so this
  * only exists for call-site compatibility and always returns CR_OK. */
 int cr_initialize_ch4h(void);
+
+/* Replaces `subroutine egrad_ch4oh(q,Natoms,Nbeads,V,dVdq,info)` (src/egrad_ch4oh.f:69-124;
+ * called from src/gradient.f90:180): natoms = 7 in Caracal's order H, C, H, H, H, O, H(O)
+ * (methane H = atoms 3,4,5,1; O abstracts), bohr -> Hartree. */
+int cr_egrad_ch4oh(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+/* Replaces `subroutine initialize_ch4oh()` (src/egrad_ch4oh.f:33, called from
+ * src/read_pes.f90:591); constants are compiled in, always CR_OK. */
+int cr_initialize_ch4oh(void);
 
 /* Any built PES (CR_PES_*) on device-resident arrays q(3,natoms,npts). */
 int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,

@@ -19,7 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-PES_IDS = {"h3": 1, "ch4h": 2, "qmdff": 4}
+PES_IDS = {"h3": 1, "ch4h": 2, "ch4oh": 3, "qmdff": 4}
 THERMOSTATS = {"none": 0, "andersen": 1, "nose-hoover": 2, "nhc": 2, "pile": 3}
 OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",
                   "acos", "erf", "cmp", "tanh", "cosh")

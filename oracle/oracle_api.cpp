@@ -10,6 +10,7 @@
 
 #include "opcount.hpp"
 #include "pes_ch4h.hpp"
+#include "pes_ch4oh.hpp"
 #include "pes_h3.hpp"
 #include "pes_qmdff.hpp"
 #include "philox.hpp"
@@ -44,6 +45,7 @@ struct BeadPES {
     switch (pes) {
       case 1: orc::h3::egrad_bead<double>(q, V, g); break;
       case 2: orc::ch4h::egrad_bead<double>(q, V, g); break;
+      case 3: orc::ch4oh::egrad_bead<double>(q, V, g); break;
       case 4: orc::qmdff::egrad(g_qmdff, q, V, g); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
@@ -253,6 +255,10 @@ void orc_pes_opcount(int pes, const double* q, uint64_t out[14]) {
     orc::OC qq[18], V, g[18];
     for (int x = 0; x < 18; ++x) qq[x] = orc::OC(q[x]);
     orc::ch4h::egrad_bead<orc::OC>(qq, &V, g);
+  } else if (pes == 3) {
+    orc::OC qq[21], V, g[21];
+    for (int x = 0; x < 21; ++x) qq[x] = orc::OC(q[x]);
+    orc::ch4oh::egrad_bead<orc::OC>(qq, &V, g);
   } else if (pes == 4) {
     const int n3 = 3 * g_qmdff.n;
     std::vector<orc::OC> qq((size_t)n3), g((size_t)n3);

@@ -12,7 +12,7 @@ extern "C" {
 #endif
 
 typedef struct orc_cfg {
-  int pes;            /* 1 = H3 (BKMP2), 2 = CH4H, 4 = QMDFF (orc_qmdff_set) */
+  int pes;            /* 1 = H3 (BKMP2), 2 = CH4H, 3 = CH4OH, 4 = QMDFF (orc_qmdff_set) */
   int natoms;
   int nbeads;
   int thermostat;     /* 0 none, 1 Andersen, 2 Nose-Hoover chain, 3 PILE */
