@@ -30,6 +30,7 @@ CR_PES_H3 = 1
 CR_PES_CH4H = 2
 CR_PES_CH4OH = 3
 CR_PES_QMDFF = 4
+CR_PES_EVB = 5
 
 CR_THERMO_NONE = 0
 CR_THERMO_ANDERSEN = 1
@@ -64,6 +65,10 @@ class CrQmdffDef(C.Structure):
                 ("c66ab", c_double_p), ("eps1", C.c_double * 6), ("eps2", C.c_double * 6),
                 ("coul_cut", C.c_double), ("zahn", C.c_int), ("zahn_a", C.c_double),
                 ("zahn_par", C.c_double), ("e_zero", C.c_double)]
+
+
+class CrEvbDef(C.Structure):
+    _fields_ = [("basis", C.c_int)] + [(k, C.c_double) for k in "abcdefghmn"]
 
 
 class CaracalError(RuntimeError):
@@ -120,6 +125,10 @@ def _sig(lib):
         "cr_qmdff_schedule_info": ([v, i, i], C.c_int),
         "cr_qmdff_tuning": ([v, C.c_int, i, C.POINTER(C.c_float)], C.c_int),
         "cr_engine_create_qmdff": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
+        "cr_evb_create": ([v, v, C.POINTER(CrEvbDef), C.POINTER(C.c_void_p)], C.c_int),
+        "cr_evb_destroy": ([v], C.c_int),
+        "cr_evb_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
+        "cr_engine_create_evb": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

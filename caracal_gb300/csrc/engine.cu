@@ -207,6 +207,8 @@ struct cr_engine {
   cr::StepParams prm{};
   // large-molecule path (QMDFF): state in HBM, a captured graph per step
   cr_qmdff* ff = nullptr;
+  cr_evb* evb = nullptr;               // dE-EVB of two force fields (ff = the first)
+  double *d_V2 = nullptr, *d_f2 = nullptr;  // second force field's energies / gradients
   bool split = false;
   cr::SplitParams sp{};
   double *d_mass = nullptr, *d_inv_mass = nullptr, *d_sigma = nullptr, *d_ke = nullptr, *d_ko = nullptr;
@@ -335,6 +337,13 @@ int launch_forces(cr_engine* e) {
   return CR_OK;
 }
 
+// Forces of the large-molecule path: one QMDFF, or the dE-EVB of two.
+int split_forces(cr_engine* e, double* V, double* f) {
+  if (e->evb)
+    return evb_launch(e->evb, e->d_q, e->T * e->P, V, f, e->d_V2, e->d_f2, e->cfg.precision, e->stream);
+  return qmdff_launch(e->ff, e->d_q, e->T * e->P, V, f, e->cfg.precision, e->stream);
+}
+
 // One step of the large-molecule path as kernel launches on e->stream
 // (recorded once into a CUDA graph).
 int split_step_launches(cr_engine* e) {
@@ -347,7 +356,7 @@ int split_step_launches(cr_engine* e) {
   }
   cr::split_drift_kernel<<<grid, cr::kSplitBlock, e->smem_drift, e->stream>>>(e->sp);
   CR_CUDA(cudaGetLastError());
-  int rc = qmdff_launch(e->ff, e->d_q, e->T * e->P, e->d_V, e->d_f, e->cfg.precision, e->stream);
+  int rc = split_forces(e, e->d_V, e->d_f);
   if (rc) return rc;
   cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp);
   CR_CUDA(cudaGetLastError());
@@ -368,15 +377,16 @@ int split_run(cr_engine* e, int nsteps) {
                                  (int)e->smem_drift));
     CR_CUDA(cudaFuncSetAttribute(cr::split_kick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)e->smem_kick));
-    // the force kernel sets its own shared-memory limit outside the capture
-    int rc = qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
+    // the force kernels set their shared-memory limits outside the capture
+    int rc = e->evb ? evb_launch(e->evb, e->d_q, 0, e->d_V, e->d_f, e->d_V2, e->d_f2, e->cfg.precision, e->stream)
+                    : qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
     if (rc) return rc;
     // let the autotuner pick the force-kernel variant on this batch before it
     // is frozen into the graph; the gradient goes to scratch so f is untouched
     const size_t nall = (size_t)e->T * e->P * e->NC;
     double* scratch = nullptr;
     if (cudaMalloc(&scratch, nall * sizeof(double)) == cudaSuccess) {
-      rc = qmdff_launch(e->ff, e->d_q, e->T * e->P, e->d_V, scratch, e->cfg.precision, e->stream);
+      rc = split_forces(e, e->d_V, scratch);
       cudaStreamSynchronize(e->stream);
       cudaFree(scratch);
       if (rc) return rc;
@@ -411,7 +421,7 @@ int dispatch_run(cr_engine* e, int nsteps) {
 
 int dispatch_forces(cr_engine* e) {
   if (e->split) {
-    int rc = qmdff_launch(e->ff, e->d_q, e->T * e->P, e->d_V, e->d_f, e->cfg.precision, e->stream);
+    int rc = split_forces(e, e->d_V, e->d_f);
     if (rc) return rc;
     cr::split_sum_beads_kernel<<<(e->T + 127) / 128, 128, 0, e->stream>>>(e->T, e->P, e->d_V, e->d_epot);
     CR_CUDA(cudaGetLastError());
@@ -590,15 +600,20 @@ int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq
 
 // Validation and set-up shared by both engine paths; ff != NULL selects the
 // large-molecule (QMDFF) path.
-static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
+static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_engine** out) {
   if (!cfg || !out) return fail(CR_ERR_ARG, "NULL argument");
   *out = nullptr;
   int N = -1;
-  if (ff) {
+  if (evb) {
+    if (cfg->pes != CR_PES_EVB) return fail(CR_ERR_ARG, "cr_engine_create_evb needs pes = CR_PES_EVB");
+    ff = evb_first(evb);
+    N = ff->n;
+  } else if (ff) {
     if (cfg->pes != CR_PES_QMDFF) return fail(CR_ERR_ARG, "cr_engine_create_qmdff needs pes = CR_PES_QMDFF");
     N = ff->n;
   } else {
-    if (cfg->pes == CR_PES_QMDFF) return fail(CR_ERR_ARG, "QMDFF engines are created with cr_engine_create_qmdff");
+    if (cfg->pes == CR_PES_QMDFF || cfg->pes == CR_PES_EVB)
+      return fail(CR_ERR_ARG, "force-field engines are created with cr_engine_create_qmdff / _evb");
     N = pes_natoms(cfg->pes);
     if (N < 0) return fail(CR_ERR_UNSUPPORTED, "PES not available in this engine");
   }
@@ -637,6 +652,7 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
   e->mass.assign(cfg->mass, cfg->mass + N);
   e->cfg.mass = e->mass.data();
   e->ff = ff;
+  e->evb = evb;
   e->split = ff != nullptr;
   e->N = N;
   e->NC = 3 * N;
@@ -661,6 +677,9 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
       cudaMalloc(&e->d_status, (size_t)e->T * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&e->d_q0, (size_t)e->NC * 8) != cudaSuccess)
     return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the state failed"));
+  if (evb && (cudaMalloc(&e->d_V2, (size_t)e->T * e->P * 8) != cudaSuccess ||
+              cudaMalloc(&e->d_f2, nall * 8) != cudaSuccess))
+    return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the EVB buffers failed"));
   cudaMemsetAsync(e->d_q, 0, nall * 8, e->stream);
   cudaMemsetAsync(e->d_p, 0, nall * 8, e->stream);
   cudaMemsetAsync(e->d_f, 0, nall * 8, e->stream);
@@ -803,11 +822,16 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
 
 extern "C" {
 
-int cr_engine_create(const cr_config* cfg, cr_engine** out) { return engine_create(cfg, nullptr, out); }
+int cr_engine_create(const cr_config* cfg, cr_engine** out) { return engine_create(cfg, nullptr, nullptr, out); }
 
 int cr_engine_create_qmdff(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
   if (!ff) return fail(CR_ERR_ARG, "NULL force field");
-  return engine_create(cfg, ff, out);
+  return engine_create(cfg, ff, nullptr, out);
+}
+
+int cr_engine_create_evb(const cr_config* cfg, cr_evb* evb, cr_engine** out) {
+  if (!evb) return fail(CR_ERR_ARG, "NULL EVB");
+  return engine_create(cfg, nullptr, evb, out);
 }
 
 int cr_engine_destroy(cr_engine* e) {
@@ -833,6 +857,8 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_ko);
   cudaFree(e->d_istep);
   cudaFree(e->d_vnh);
+  cudaFree(e->d_V2);
+  cudaFree(e->d_f2);
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   if (e->ev0) cudaEventDestroy(e->ev0);

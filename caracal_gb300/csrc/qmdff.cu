@@ -17,8 +17,8 @@ using cr::qmdff::kVPair;
 // one colour touch disjoint atoms.  Greedy: each colour takes, in order, the
 // remaining terms that do not touch an atom already used by that colour,
 // until the batch holds 32 terms or has max_colours colours.  Every colour
-// costs one scatter round of the warp, so light terms (bonds, pairs) get
-// one colour per batch and heavier ones (angles, torsions) two.
+// costs one scatter round of the warp, so bonds get one colour per batch and
+// angles and torsions (heavier terms) two; pairs use schedule_pairs.
 void schedule_kind(int nterm, int arity, int max_colours, const std::vector<int>& atoms,
                    const std::vector<int>& order, int natoms, std::vector<int>& slot,
                    std::vector<unsigned char>& color, std::vector<unsigned char>& ncol, int& nbatch,
@@ -58,6 +58,38 @@ void schedule_kind(int nterm, int arity, int max_colours, const std::vector<int>
     ++nbatch;
   }
   (void)nterm;
+}
+
+// Pair terms: the circle method splits all atom pairs of n atoms (n even; a
+// dummy atom for odd n) into n-1 perfect matchings; the pairs of one
+// matching touch disjoint atoms, so each matching is one single-colour batch
+// (split in 32-lane pieces when n > 64).
+void schedule_pairs(int nterm, const std::vector<int>& atoms, int natoms, std::vector<int>& slot,
+                    std::vector<unsigned char>& color, std::vector<unsigned char>& ncol, int& nbatch,
+                    int& colours) {
+  const int m = natoms + (natoms & 1);  // players, even
+  std::vector<std::vector<int>> rounds((size_t)(m > 1 ? m - 1 : 1));
+  for (int t = 0; t < nterm; ++t) {
+    int i = atoms[(size_t)2 * t], j = atoms[(size_t)2 * t + 1];
+    if (i > j) std::swap(i, j);
+    // round r holds (r, m-1) and the pairs (r + k, r - k) mod (m-1), i.e. the
+    // pairs with i + j = 2r (mod m-1); m/2 is the inverse of 2 modulo m-1
+    const int r = (j == m - 1) ? i : (int)(((long long)(i + j) * (m / 2)) % (m - 1));
+    rounds[(size_t)r].push_back(t);
+  }
+  nbatch = 0;
+  for (const auto& rd : rounds) {
+    for (size_t k0 = 0; k0 < rd.size(); k0 += 32) {
+      for (int l = 0; l < 32; ++l) {
+        const size_t k = k0 + (size_t)l;
+        slot.push_back(k < rd.size() ? rd[k] : -1);
+        color.push_back(0);
+      }
+      ncol.push_back(1);
+      colours += 1;
+      ++nbatch;
+    }
+  }
 }
 
 template <class T>
@@ -294,8 +326,12 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
     }
     if (kind == 3) atoms = pair;
     int nb = 0;
-    const int max_colours = (kind == 0 || kind == 3) ? 1 : 2;
-    schedule_kind(ff->nterm[kind], arity, max_colours, atoms, order, n, slot, color, ncol, nb, ff->ncolors);
+    if (kind == 3) {
+      schedule_pairs(ff->nterm[kind], atoms, n, slot, color, ncol, nb, ff->ncolors);
+    } else {
+      const int max_colours = (kind == 0) ? 1 : 2;
+      schedule_kind(ff->nterm[kind], arity, max_colours, atoms, order, n, slot, color, ncol, nb, ff->ncolors);
+    }
     for (int m = 0; m < ff->nterm[kind]; ++m)
       for (int x = 0; x < arity; ++x)
         for (int y = x + 1; y < arity; ++y)

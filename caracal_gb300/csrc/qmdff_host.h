@@ -23,3 +23,10 @@ constexpr int kQmdffWarps = 4;
 // e[b] (with E_zero) and g = dV/dq for nbeads beads of d_q(3, n, nbeads).
 int qmdff_launch(const cr_qmdff* ff, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
                  cudaStream_t s);
+
+// dE-EVB of two force fields (csrc/evb.cu): e, g <- EVB energy and gradient;
+// e2, g2 are scratch of the same sizes for the second force field.
+struct cr_evb;
+int evb_launch(const cr_evb* evb, const double* d_q, int nbeads, double* d_e, double* d_g, double* d_e2,
+               double* d_g2, int precision, cudaStream_t s);
+cr_qmdff* evb_first(const cr_evb* evb);

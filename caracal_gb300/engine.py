@@ -155,6 +155,49 @@ class QMDFFForceField:
             pass
 
 
+EVB_BASES = {"const": 0, "1g": 1, "2g": 2, "3g": 3, "sp": 4, "sd": 5, "sd2": 6, "sp2d": 7}
+
+
+class EVBPair:
+    """dE-EVB of two device QMDFFs (cr_evb): Caracal's two-QMDFF gradient
+    branch (src/gradient.f90:361-386, 1228-1304).  Each force field carries
+    its E_zero; ``basis`` is Caracal's off_basis and ``par`` the offa..offh,
+    offm, offn values as a dict with keys a..h, m, n.  Both force fields must
+    stay alive while the pair is used."""
+
+    def __init__(self, ff1, ff2, basis="1g", **par):
+        self.ff1, self.ff2 = ff1, ff2
+        self.n = ff1.n
+        d = L.CrEvbDef()
+        d.basis = EVB_BASES[basis]
+        for k in "abcdefghmn":
+            setattr(d, k, float(par.get(k, 0.0)))
+        h = C.c_void_p()
+        L.check(L.lib().cr_evb_create(ff1._h, ff2._h, C.byref(d), C.byref(h)), "cr_evb_create")
+        self._h = h
+
+    def egrad(self, xyz, precision="fp64"):
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        if x.ndim == 2:
+            x = x[None]
+        e = np.zeros(x.shape[0])
+        g = np.zeros_like(x)
+        prec = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        L.check(L.lib().cr_evb_egrad(self._h, L.dptr(x), x.shape[0], L.dptr(e), L.dptr(g), prec), "cr_evb_egrad")
+        return e, g
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().cr_evb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class RPMDEngine:
     """A batch of independent RPMD trajectories resident on one GPU.
 
@@ -164,8 +207,10 @@ class RPMDEngine:
     def __init__(self, pes, mass, nbeads, ntraj, dt_au, beta=None, thermostat="none",
                  andersen_step=70, pile_tau0_au=0.0, transrot=True, precision="fp64", seed=0,
                  traj0=0, nose_q_au=0.0):
-        self.ff = pes if isinstance(pes, QMDFFForceField) else None
-        if self.ff is not None:
+        self.ff = pes if isinstance(pes, (QMDFFForceField, EVBPair)) else None
+        if isinstance(pes, EVBPair):
+            self.pes = L.CR_PES_EVB
+        elif self.ff is not None:
             self.pes = L.CR_PES_QMDFF
         else:
             self.pes = PES[pes] if isinstance(pes, str) else int(pes)
@@ -181,7 +226,10 @@ class RPMDEngine:
                               int(seed) & 0xFFFFFFFF, int(traj0) & 0xFFFFFFFF, float(dt_au),
                               self.beta, float(pile_tau0_au), L.dptr(self.mass), float(nose_q_au))
         h = C.c_void_p()
-        if self.ff is not None:
+        if isinstance(self.ff, EVBPair):
+            L.check(L.lib().cr_engine_create_evb(C.byref(self.cfg), self.ff._h, C.byref(h)),
+                    "cr_engine_create_evb")
+        elif self.ff is not None:
             L.check(L.lib().cr_engine_create_qmdff(C.byref(self.cfg), self.ff._h, C.byref(h)),
                     "cr_engine_create_qmdff")
         else:

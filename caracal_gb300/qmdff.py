@@ -251,20 +251,44 @@ def _topology(at, xyz_ang):
     return bonds, adj, dist
 
 
-def alkane(nc=20, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002):
-    """Synthetic C_nH_2n+2 QMDFF (bohr, Hartree)."""
+def _adjacency(n, bonds):
+    adj = [[] for _ in range(n)]
+    for i, j in bonds:
+        adj[i].append(j)
+        adj[j].append(i)
+    dist = np.full((n, n), 99, dtype=int)
+    for s in range(n):
+        dist[s, s] = 0
+        front = [s]
+        while front:
+            nxt = []
+            for u in front:
+                for v in adj[u]:
+                    if dist[s, v] > dist[s, u] + 1:
+                        dist[s, v] = dist[s, u] + 1
+                        nxt.append(v)
+            front = nxt
+    return adj, dist
+
+
+def from_topology(at, xyz, bonds, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002, r0=None,
+                  e_zero=0.0):
+    """QMDFF terms for a bond list (0-based pairs) on geometry xyz (bohr): bond
+    curvature k_bond, angle curvature k_angle, torsion barrier v_tors (each
+    drawn in +-20 % from the seed), reference values from the geometry (or
+    r0[(i, j)] for given bonds), charges +-0.1 e neutral, NCI = pairs three or
+    more bonds apart."""
     rng = np.random.default_rng(seed)
-    at, xa = alkane_geometry(nc)
-    xyz = xa / BOHR_ANGSTROM
+    at = np.asarray(at)
     n = len(at)
-    bonds, adj, dist = _topology(at, xa)
+    adj, dist = _adjacency(n, bonds)
     bond = np.array([[i + 1, j + 1] for i, j in bonds])
     vbond = np.zeros((len(bonds), 3))
     a_exp = 6.0
     for m, (i, j) in enumerate(bonds):
-        r0 = np.linalg.norm(xyz[i] - xyz[j])
+        rr = np.linalg.norm(xyz[i] - xyz[j]) if r0 is None or (i, j) not in r0 else r0[(i, j)]
         K = k_bond * rng.uniform(0.8, 1.2)          # curvature Eh/bohr^2
-        vbond[m] = [r0, 2.0 * K * r0 * r0 / (a_exp * a_exp), a_exp]
+        vbond[m] = [rr, 2.0 * K * rr * rr / (a_exp * a_exp), a_exp]
     angl, vangl = [], []
     for j in range(n):
         nb = adj[j]
@@ -272,7 +296,9 @@ def alkane(nc=20, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002):
             for y in range(x + 1, len(nb)):
                 i, k = nb[x], nb[y]
                 v1, v2 = xyz[i] - xyz[j], xyz[k] - xyz[j]
-                th0 = np.arccos(np.dot(v1, v2) / np.linalg.norm(v1) / np.linalg.norm(v2))
+                th0 = np.arccos(np.clip(np.dot(v1, v2) / np.linalg.norm(v1) / np.linalg.norm(v2), -1, 1))
+                if at[i] == 1 and at[k] == 1 or abs(th0 - np.arccos(-1 / 3)) > 0.6:
+                    th0 = np.arccos(-1.0 / 3.0)       # tetrahedral reference for distorted centres
                 K = k_angle * rng.uniform(0.8, 1.2)   # Eh/rad^2
                 angl.append([j + 1, i + 1, k + 1])
                 vangl.append([th0, K / (2.0 * np.sin(th0) ** 2)])
@@ -296,11 +322,31 @@ def alkane(nc=20, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002):
             if dist[i, j] >= 3:
                 nci.append([i + 1, j + 1, min(int(dist[i, j]), 5)])
     q = np.where(at == 6, -0.1, 0.1).astype(float)
-    # exact neutrality: spread the remainder over the hydrogens
-    q[at == 1] -= q.sum() / np.count_nonzero(at == 1)
-    return QMDFF(at=at, xyz=xyz, q=q, bond=bond, vbond=vbond, angl=np.array(angl),
-                 vangl=np.array(vangl), tors=np.array(tors), vtors=np.array(vtors),
-                 nci=np.array(nci), c6=pair_c6(at))
+    q[at == 1] -= q.sum() / np.count_nonzero(at == 1)   # exact neutrality
+    return QMDFF(at=at, xyz=xyz.copy(), q=q, bond=bond, vbond=vbond, angl=np.array(angl),
+                 vangl=np.array(vangl), tors=np.array(tors).reshape(-1, 6),
+                 vtors=np.array(vtors).reshape(-1, 14), nci=np.array(nci), c6=pair_c6(at), e_zero=e_zero)
+
+
+def alkane(nc=20, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002):
+    """Synthetic C_nH_2n+2 QMDFF (bohr, Hartree)."""
+    at, xa = alkane_geometry(nc)
+    bonds, _, _ = _topology(at, xa)
+    return from_topology(at, xa / BOHR_ANGSTROM, bonds, seed=seed, k_bond=k_bond, k_angle=k_angle,
+                         v_tors=v_tors)
+
+
+def alkane_evb_partner(ff: QMDFF, seed=20261207, e_zero=0.02):
+    """EVB partner of an alkane QMDFF: the first hydrogen of carbon 0 is bonded
+    to carbon 1 instead (a 1,2 H shift), with r(CH) = 1.09 A as the partner's
+    reference bond length; same atoms, own parameters and E_zero."""
+    n = ff.n
+    bonds = [(int(i) - 1, int(j) - 1) for i, j in ff.bond]
+    h = next(j for i, j in bonds if i == 0 and ff.at[j] == 1)
+    bonds = [(i, j) for i, j in bonds if not (i == 0 and j == h)] + [(1, h)]
+    r0 = {(1, h): 1.09 / BOHR_ANGSTROM}
+    assert len(bonds) == n - 1
+    return from_topology(ff.at, ff.xyz, bonds, seed=seed, r0=r0, e_zero=e_zero)
 
 
 def pair_parameters(ff: QMDFF, tab: ElementTables):

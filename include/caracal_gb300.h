@@ -39,6 +39,7 @@ extern "C" {
 #define CR_PES_CH4H 2    /* ANA_CH4H: src/egrad_ch4h.f + src/util_ch4h.f */
 #define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f + src/util_ch4oh.f */
 #define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90 (ff_hb not built yet) */
+#define CR_PES_EVB 5     /* dE-EVB of two QMDFFs: src/gradient.f90:361-386, 1228-1304 */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
 #define CR_THERMO_NONE 0      /* NVE */
@@ -170,6 +171,31 @@ int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors);
  * ms[3] = the measured times. */
 int cr_qmdff_tuning(const cr_qmdff* ff, int precision, int* variant, float* ms);
 
+/* ---- dE-EVB of two QMDFFs ---------------------------------------------------
+ * Replaces the two-QMDFF branch of `gradient` (src/gradient.f90:361-386 and
+ * 1228-1304, EVB_QMDFF with a dE coupling, keyword DE_EVB): each force
+ * field's energy includes its E_zero (cr_qmdff_def.e_zero = E_zero1 / E_zero2),
+ * dE = E1 - E2, V12 = the coupling of the basis, E = (E1 + E2 -
+ * sqrt(dE^2 + 4 V12^2)) / 2 and its analytic gradient as Caracal writes it. */
+#define CR_EVB_CONST 0  /* V = a */
+#define CR_EVB_1G 1     /* V = a exp(-b dE^2) */
+#define CR_EVB_2G 2     /* + c exp(-d (dE+m)^2) */
+#define CR_EVB_3G 3     /* + e exp(-f (dE+n)^2) */
+#define CR_EVB_SP 4     /* a exp(-b dE^2) + c dE exp(-d dE^2) */
+#define CR_EVB_SD 5     /* a exp(-b dE^2) + c dE^2 exp(-d dE^2) */
+#define CR_EVB_SD2 6    /* + e dE^2 exp(-f dE^2) */
+#define CR_EVB_SP2D 7   /* a exp(-b dE^2) + c dE exp(-d dE^2) + e dE exp(-f dE^2) + g dE^2 exp(-h dE^2) */
+typedef struct cr_evb_def {
+  int basis;                               /* CR_EVB_* (Caracal's off_basis) */
+  double a, b, c, d, e, f, g, h, m, n;     /* offa..offh, offm, offn */
+} cr_evb_def;
+typedef struct cr_evb cr_evb;
+/* Both force fields must describe the same atoms and outlive the EVB object. */
+int cr_evb_create(cr_qmdff* ff1, cr_qmdff* ff2, const cr_evb_def* def, cr_evb** out);
+int cr_evb_destroy(cr_evb* evb);
+/* Host arrays xyz(3,natoms,nbeads) -> e(nbeads), g(3,natoms,nbeads). */
+int cr_evb_egrad(cr_evb* evb, const double* xyz, int nbeads, double* e, double* g, int precision);
+
 /* ---- RPMD engine -----------------------------------------------------------
  * Replaces the stepping loop of `dynamic` (src/dynamic.f90:1569-1579) around
  * `verlet` (src/verlet.f90:65) and the initialisation of `mdinit`
@@ -180,6 +206,9 @@ int cr_engine_create(const cr_config* cfg, cr_engine** out);
  * engine.  Steps run as a CUDA graph of kernels (kick + free ring polymer,
  * forces, kick + thermostat, transrot) instead of one persistent launch. */
 int cr_engine_create_qmdff(const cr_config* cfg, cr_qmdff* ff, cr_engine** out);
+/* Engine on a dE-EVB of two QMDFFs (cfg->pes = CR_PES_EVB); the EVB object
+ * and its force fields must outlive the engine. */
+int cr_engine_create_evb(const cr_config* cfg, cr_evb* evb, cr_engine** out);
 int cr_engine_destroy(cr_engine* e);
 
 /* Initial positions: every bead of every trajectory = q0(3,natoms) plus

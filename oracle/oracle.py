@@ -19,7 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-PES_IDS = {"h3": 1, "ch4h": 2, "ch4oh": 3, "qmdff": 4}
+PES_IDS = {"h3": 1, "ch4h": 2, "ch4oh": 3, "qmdff": 4, "evb": 5}
+EVB_BASES = {"const": 0, "1g": 1, "2g": 2, "3g": 3, "sp": 4, "sd": 5, "sd2": 6, "sp2d": 7}
 THERMOSTATS = {"none": 0, "andersen": 1, "nose-hoover": 2, "nhc": 2, "pile": 3}
 OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",
                   "acos", "erf", "cmp", "tanh", "cosh")
@@ -58,6 +59,23 @@ class QmdffDef(C.Structure):
 _keep = []
 
 
+def set_evb(ff1, ff2, tables, basis="1g", par=None, **kw):
+    """PES 5: dE-EVB of ff1 and ff2 (each with its own E_zero); par = dict of
+    offa..offh, offm, offn (a..h, m, n)."""
+    set_qmdff(ff2, tables, **kw)
+    lib().orc_qmdff_set2(C.byref(_last_def[0]))
+    _keep2[:] = list(_keep)
+    set_qmdff(ff1, tables, **kw)
+    p = np.zeros(10)
+    for k, name in enumerate("abcdefghmn"):
+        p[k] = float((par or {}).get(name, 0.0))
+    lib().orc_evb_set(EVB_BASES[basis], _dp(p))
+
+
+_keep2 = []
+_last_def = [None]
+
+
 def set_qmdff(ff, tables, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
     """Load a caracal_gb300.qmdff.QMDFF (1-based atoms) as the oracle's PES 4."""
     from caracal_gb300 import qmdff as Q
@@ -82,6 +100,7 @@ def set_qmdff(ff, tables, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
     for i in range(7):
         d.eps1[i], d.eps2[i] = e1[i], e2[i]
     d.coul_cut, d.zahn, d.zahn_a, d.zahn_par, d.e_zero = coul_cut, int(zahn), zahn_a, zahn_par, ff.e_zero
+    _last_def[0] = d
     lib().orc_qmdff_set(C.byref(d))
 
 
@@ -129,6 +148,8 @@ def lib():
         _lib.orc_run.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_int, C.c_int, d, d, d, d,
                                  C.POINTER(C.c_int), C.c_int, d]
         _lib.orc_qmdff_set.argtypes = [C.POINTER(QmdffDef)]
+        _lib.orc_qmdff_set2.argtypes = [C.POINTER(QmdffDef)]
+        _lib.orc_evb_set.argtypes = [C.c_int, d]
         _lib.orc_nhc_half.argtypes = [C.POINTER(Cfg), d, d]
         _lib.orc_calc_xi.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d]
         _lib.orc_calc_xi.restype = C.c_double

@@ -12,6 +12,7 @@
 #include "pes_ch4h.hpp"
 #include "pes_ch4oh.hpp"
 #include "pes_h3.hpp"
+#include "pes_evb.hpp"
 #include "pes_qmdff.hpp"
 #include "philox.hpp"
 #include "recross.hpp"
@@ -35,7 +36,8 @@ orc::StepConfig to_step(const orc_cfg* c) {
   return s;
 }
 
-orc::qmdff::FF g_qmdff;
+orc::qmdff::FF g_qmdff, g_qmdff2;
+orc::evb::Coupling g_evb;
 
 // Per-bead PES call, q(3,N) -> V, g(3,N).
 struct BeadPES {
@@ -47,6 +49,7 @@ struct BeadPES {
       case 2: orc::ch4h::egrad_bead<double>(q, V, g); break;
       case 3: orc::ch4oh::egrad_bead<double>(q, V, g); break;
       case 4: orc::qmdff::egrad(g_qmdff, q, V, g); break;
+      case 5: orc::evb::egrad(g_qmdff, g_qmdff2, g_evb, q, V, g); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
   }
@@ -55,6 +58,19 @@ struct BeadPES {
 }  // namespace
 
 extern "C" {
+
+void orc_qmdff_set2(const orc_qmdff_def* d) {
+  orc::qmdff::FF keep = g_qmdff;
+  orc_qmdff_set(d);
+  g_qmdff2 = g_qmdff;
+  g_qmdff = keep;
+}
+
+void orc_evb_set(int basis, const double* par) {
+  g_evb.basis = basis;
+  double* dst[10] = {&g_evb.a, &g_evb.b, &g_evb.c, &g_evb.d, &g_evb.e, &g_evb.f, &g_evb.g, &g_evb.h, &g_evb.m, &g_evb.n};
+  for (int k = 0; k < 10; ++k) *dst[k] = par[k];
+}
 
 void orc_qmdff_set(const orc_qmdff_def* d) {
   orc::qmdff::FF& f = g_qmdff;

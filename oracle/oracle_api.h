@@ -12,7 +12,7 @@ extern "C" {
 #endif
 
 typedef struct orc_cfg {
-  int pes;            /* 1 = H3 (BKMP2), 2 = CH4H, 3 = CH4OH, 4 = QMDFF (orc_qmdff_set) */
+  int pes;            /* 1 H3 (BKMP2), 2 CH4H, 3 CH4OH, 4 QMDFF (orc_qmdff_set), 5 dE-EVB of two QMDFFs */
   int natoms;
   int nbeads;
   int thermostat;     /* 0 none, 1 Andersen, 2 Nose-Hoover chain, 3 PILE */
@@ -74,6 +74,10 @@ typedef struct orc_qmdff_def {
 
 /* Sets the force field used by PES id 4 (QMDFF) in all oracle entry points. */
 void orc_qmdff_set(const orc_qmdff_def* d);
+/* The second force field and the coupling of PES id 5 (dE-EVB of the two):
+ * basis 0..7 = const, 1g, 2g, 3g, sp, sd, sd2, sp2d; par = offa..offh, offm, offn. */
+void orc_qmdff_set2(const orc_qmdff_def* d);
+void orc_evb_set(int basis, const double par[10]);
 
 /* BIMOLEC reaction coordinate of Caracal's recrossing (calc_xi mode 2). */
 typedef struct orc_xidef {

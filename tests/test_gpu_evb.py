@@ -1,0 +1,70 @@
+"""GPU: dE-EVB of two QMDFFs (cr_evb, src/gradient.f90:361-386, 1228-1304)
+and the EVB engine against the oracle.  Plain FP64: energies and gradients
+<= 1e-12, one step <= 1e-12, 10 steps <= 1e-9 (norm-wise relative)."""
+import numpy as np
+import pytest
+
+from caracal_gb300 import RPMDEngine
+from caracal_gb300 import qmdff as Q
+from caracal_gb300.engine import EVBPair, QMDFFForceField
+from caracal_gb300.units import beta_from_kelvin, dt_fs_to_au
+from caracal_gb300.workloads import qmdff_config
+from conftest import rel_err
+from oracle import oracle as orc
+from test_oracle_evb import BASES
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def fields(require_gpu):
+    ff = Q.alkane()
+    ff2 = Q.alkane_evb_partner(ff)
+    g1, g2 = QMDFFForceField(ff), QMDFFForceField(ff2)
+    yield ff, ff2, g1, g2
+    g1.close()
+    g2.close()
+
+
+@pytest.mark.parametrize("basis", list(BASES))
+def test_evb_egrad_matches_oracle(fields, basis):
+    ff, ff2, g1, g2 = fields
+    orc.set_evb(ff, ff2, Q.ElementTables.d3_like(), basis, BASES[basis])
+    pair = EVBPair(g1, g2, basis, **BASES[basis])
+    x = ff.xyz[None] + np.random.default_rng(3).normal(0, 0.05, (96,) + ff.xyz.shape)
+    e, g = pair.egrad(x, "fp64")
+    eo, go = orc.egrad("evb", x)
+    em, gm = pair.egrad(x, "mixed")
+    pair.close()
+    assert rel_err(e, eo) <= 1e-12
+    assert rel_err(g, go) <= 1e-12
+    assert np.sqrt(np.sum((gm - g) ** 2) / np.sum(g ** 2)) <= 2e-6
+
+
+def test_evb_engine_matches_oracle(fields):
+    ff, ff2, g1, g2 = fields
+    par = BASES["1g"]
+    orc.set_evb(ff, ff2, Q.ElementTables.d3_like(), "1g", par)
+    pair = EVBPair(g1, g2, "1g", **par)
+    mass = qmdff_config().mass
+    beta, dt = beta_from_kelvin(300.0), dt_fs_to_au(0.5)
+    eng = RPMDEngine(pair, mass, 8, 2, dt, beta=beta, thermostat="andersen", andersen_step=4, seed=9)
+    cfg = orc.Config("evb", mass, 8, dt, beta, thermostat="andersen", andersen_step=4, seed=9)
+    eng.init_positions(ff.xyz, 0.02)
+    eng.init_momenta()
+    eng.compute_forces()
+    q = orc.init_positions(cfg, 2, ff.xyz, 0.02)
+    p = orc.init_momenta(cfg, 2)
+    f, e0 = orc.init_forces(cfg, q)
+    _, _, fg0, eg0, _ = eng.get_state()
+    assert rel_err(fg0, f) <= 1e-12 and rel_err(eg0, e0) <= 1e-12
+    eng.run(1)
+    q1, p1, f1, e1, _ = eng.get_state()
+    qo, po, fo, eo, _ = orc.run(cfg, q, p, f, 1)
+    assert rel_err(q1, qo) <= 1e-12 and rel_err(p1, po) <= 1e-12 and rel_err(e1, eo) <= 1e-12
+    eng.run(9)
+    q10, p10, _, e10, _ = eng.get_state()
+    eng.close()
+    pair.close()
+    qo, po, fo, eo, _ = orc.run(cfg, q, p, f, 10)
+    assert rel_err(q10, qo) <= 1e-9 and rel_err(p10, po) <= 1e-9 and rel_err(e10, eo) <= 1e-9
