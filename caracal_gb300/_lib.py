@@ -64,7 +64,8 @@ class CrQmdffDef(C.Structure):
                 ("r0ab", c_double_p), ("zab", c_double_p), ("r0094", c_double_p), ("sr42", c_double_p),
                 ("c66ab", c_double_p), ("eps1", C.c_double * 6), ("eps2", C.c_double * 6),
                 ("coul_cut", C.c_double), ("zahn", C.c_int), ("zahn_a", C.c_double),
-                ("zahn_par", C.c_double), ("e_zero", C.c_double)]
+                ("zahn_par", C.c_double), ("e_zero", C.c_double), ("nhb", C.c_int), ("hb", c_int_p),
+                ("vhb", c_double_p)]
 
 
 class CrEvbDef(C.Structure):

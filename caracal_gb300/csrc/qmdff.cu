@@ -249,6 +249,9 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
     if (!atom_ok(d->nci[3 * m]) || !atom_ok(d->nci[3 * m + 1])) return cr_set_error(CR_ERR_ARG, "NCI atom out of range");
     if (d->nci[3 * m + 2] < 1 || d->nci[3 * m + 2] > 6) return cr_set_error(CR_ERR_ARG, "NCI category not 1..6");
   }
+  if (d->nhb < 0 || (d->nhb > 0 && (!d->hb || !d->vhb))) return cr_set_error(CR_ERR_ARG, "missing H-bond arrays");
+  for (int m = 0; m < 3 * d->nhb; ++m)
+    if (!atom_ok(d->hb[m])) return cr_set_error(CR_ERR_ARG, "H-bond atom out of range");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return cr_set_error(CR_ERR_NO_DEVICE, "no CUDA device");
 
@@ -289,12 +292,21 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
     v[6] = d->zahn ? d->q[i1] * d->q[i2] : d->q[i1] * d->q[i2] * d->eps1[nk - 1];
   }
 
+  // H/halogen bonds: A, B, H (0-based) and the kind (src/ff_hb.f90:71-78)
+  std::vector<int> hb((size_t)4 * d->nhb);
+  std::vector<double> vhb(d->vhb, d->vhb + 2 * d->nhb);
+  for (int m = 0; m < d->nhb; ++m) {
+    for (int a = 0; a < 3; ++a) hb[(size_t)4 * m + a] = d->hb[3 * m + a] - 1;
+    hb[(size_t)4 * m + 3] = d->at[d->hb[3 * m + 2] - 1] == 1 ? 1 : 2;
+  }
+
   cr_qmdff* ff = new cr_qmdff();
   ff->n = n;
   ff->nterm[0] = d->nbond;
   ff->nterm[1] = d->nangl;
   ff->nterm[2] = d->ntors;
   ff->nterm[3] = d->nnci;
+  ff->nterm[4] = d->nhb;
 
   // schedule: torsions grouped by (type, nt) so a batch runs one code path
   std::vector<int> slot;
@@ -303,7 +315,7 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   D.n = n;
   int boff = 0;
   bool distinct = true;
-  for (int kind = 0; kind < 4; ++kind) {
+  for (int kind = 0; kind < cr::qmdff::kKinds; ++kind) {
     std::vector<int> order((size_t)ff->nterm[kind]);
     for (int m = 0; m < ff->nterm[kind]; ++m) order[(size_t)m] = m;
     std::vector<int> atoms;
@@ -325,6 +337,12 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
       });
     }
     if (kind == 3) atoms = pair;
+    if (kind == 4) {
+      arity = 3;
+      atoms.resize((size_t)3 * d->nhb);
+      for (int m = 0; m < d->nhb; ++m)
+        for (int a = 0; a < 3; ++a) atoms[(size_t)3 * m + a] = hb[(size_t)4 * m + a];
+    }
     int nb = 0;
     if (kind == 3) {
       schedule_pairs(ff->nterm[kind], atoms, n, slot, color, ncol, nb, ff->ncolors);
@@ -352,6 +370,8 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   up(angl, &D.angl);
   up(tors, &D.tors);
   up(pair, &D.pair);
+  up(hb, &D.hb);
+  up(vhb, &D.vhb);
   up(rad, &D.d.rad);
   up(vbond, &D.d.vbond);
   up(vangl, &D.d.vangl);
@@ -381,7 +401,7 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
 int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors) {
   if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
   if (batches)
-    for (int k = 0; k < 4; ++k) batches[k] = ff->dev.nb[k];
+    for (int k = 0; k < cr::qmdff::kKinds; ++k) batches[k] = ff->dev.nb[k];
   if (colors) *colors = ff->ncolors;
   return CR_OK;
 }

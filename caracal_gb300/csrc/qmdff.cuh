@@ -42,10 +42,12 @@ struct Tables {
   const F* vpair;  // kVPair per NCI pair
 };
 
+constexpr int kKinds = 5;  // bonds, angles, torsions, NCI pairs, H/halogen bonds
+
 struct Dev {
   int n;
-  int nb[4];       // batches per kind: bonds, angles, torsions, NCI pairs
-  int boff[4];     // first batch of each kind
+  int nb[kKinds];    // batches per kind
+  int boff[kKinds];  // first batch of each kind
   const int* slot;             // [batches][32]: term index or -1
   const unsigned char* color;  // [batches][32]
   const unsigned char* ncol;   // [batches]
@@ -53,6 +55,8 @@ struct Dev {
   const int* angl;   // 3 per angle (centre, i, k)
   const int* tors;   // 6 per torsion: i, j, k, l, nt, type
   const int* pair;   // 2 per NCI pair
+  const int* hb;     // 4 per H/halogen bond: A, B, H, type (1 hydrogen bond, 2 halogen bond)
+  const double* vhb; // 2 per H/halogen bond: ca, cb
   Tables<double> d;
   Tables<float> f;
   double coul_cut, zahn_a, zahn_par, e_zero;
@@ -572,7 +576,167 @@ __device__ inline F pair_term(const Dev& D, const Tables<F>& T, const BeadPos& x
   return e;
 }
 
-// Energy of one term of kind `kind` (0 bond, 1 angle, 2 torsion, 3 pair).
+// x^5, x^6, x^12 by products (the reference's real-exponent ** operators)
+template <class F>
+__device__ inline F pow6(F x) {
+  const F x2 = x * x;
+  return x2 * x2 * x2;
+}
+
+// eabhag (src/eabhag.f90:35-220): hydrogen bond A...H-B; nothing if the
+// energy is above -1e-8 (the reference returns before its gradient).
+template <class F>
+__device__ inline F hbond_term(const BeadPos& X, int A, int B, int H, F ca, F cb, Contrib<F>& c) {
+  const F longcut = F(8.0), alp7 = F(12.0), alp3 = F(6.0);
+  F drah[3], drbh[3], drab[3];
+  disp<F>(X, A, H, drah);
+  disp<F>(X, B, H, drbh);
+  disp<F>(X, A, B, drab);
+  c.a[0] = A;
+  c.a[1] = B;
+  c.a[2] = H;
+  const F rab2 = dot3(drab, drab), rab = q_sqrt<F>(rab2);
+  const F rah2 = dot3(drah, drah), rah = q_sqrt<F>(rah2);
+  const F rbh2 = dot3(drbh, drbh), rbh = q_sqrt<F>(rbh2);
+  const F q6 = pow6<F>(rab / longcut);
+  const F ratio = q6 * q6;
+  F rdampl = F(1) / (F(1) + ratio);
+  rdampl = rdampl / rab2 / rab;
+  const bool far_a = rah2 > rbh2;
+  F cosabh, aprod;
+  if (far_a) {
+    aprod = F(1) / rbh / rab;
+    cosabh = -dot3(drbh, drab) * aprod;
+  } else {
+    aprod = F(1) / rah / rab;
+    cosabh = dot3(drah, drab) * aprod;
+  }
+  F aterm = F(0.5) * (cosabh + F(1));
+  const F a2 = aterm * aterm;
+  F apref = a2 * a2 * aterm;  // aterm**(alp3-1)
+  aterm = aterm * apref;
+  apref = alp3 * F(0.5) * apref;
+  const F rah4 = rah2 * rah2, rbh4 = rbh2 * rbh2;
+  const F denom = F(1) / (rah4 + rbh4);
+  const F da = (ca * rah4 + cb * rbh4) * denom;
+  const F eabh = -da * rdampl * aterm;
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) c.g[m][d] = F(0);
+  if (eabh > F(-1.0e-8)) return F(0);
+  F ga[3], gb[3], gh[3];
+  F gi = F(4) * (ca - cb) * rah2 * rbh4 * denom * denom;
+  gi = -gi * rdampl * aterm;
+  F gj = F(4) * (cb - ca) * rbh2 * rah4 * denom * denom;
+  gj = -gj * rdampl * aterm;
+  F gl = rdampl * rdampl * rab * (F(3) + (F(3) + alp7) * ratio);
+  gl = gl * da * aterm;
+  const F gn = -da * rdampl * apref;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    ga[d] = gi * drah[d];
+    gb[d] = gj * drbh[d];
+    gh[d] = -ga[d] - gb[d];
+    const F dl = gl * drab[d];
+    ga[d] += dl;
+    gb[d] -= dl;
+    if (far_a) {
+      const F dg = gn * (-aprod * drbh[d] - cosabh * drab[d] / rab2);
+      const F dg2 = gn * (aprod * drab[d] + cosabh * drbh[d] / rbh2);
+      ga[d] += dg;
+      gh[d] += dg2;
+      gb[d] = gb[d] - dg - dg2;
+    } else {
+      const F dg = gn * (-aprod * drah[d] + cosabh * drab[d] / rab2);
+      const F dg2 = gn * (-aprod * drab[d] + cosabh * drah[d] / rah2);
+      gb[d] += dg;
+      gh[d] += dg2;
+      ga[d] = ga[d] - dg - dg2;
+    }
+    c.g[0][d] = ga[d];
+    c.g[1][d] = gb[d];
+    c.g[2][d] = gh[d];
+  }
+  return eabh;
+}
+
+// eabx (src/eabx.f90:34-111) on the three atoms' coordinates xa, xb, xh.
+__device__ inline double eabx(const double* xa, const double* xb, const double* xh, double ca) {
+  double rb[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) rb[d] = xa[d] - xb[d];
+  const double rab2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+  const double dampl = 1.0 / (1.0 + pow6<double>(rab2 / 120.0));
+#pragma unroll
+  for (int d = 0; d < 3; ++d) rb[d] = xa[d] - xh[d];
+  const double d2ik = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) rb[d] = xh[d] - xb[d];
+  const double d2jk = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+  double term;
+  if (d2ik > d2jk) term = 0.5 * (rab2 + d2jk - d2ik) / sqrt(rab2 * d2jk);
+  else term = 0.5 * (rab2 + d2ik - d2jk) / sqrt(rab2 * d2ik);
+  const double aterm = pow6<double>(0.5 * (term + 1.0));
+  return -ca * dampl * aterm / d2jk;
+}
+
+// eabxag (src/eabxag.f90:35-156): halogen bond A...X-B, energy and Caracal's
+// central-difference gradient (step 1e-6), FP64 in both forms.  As in the
+// reference, each atom's three components all receive the z quotient.
+template <class F>
+__device__ inline F xbond_term(const BeadPos& X, int A, int B, int H, double ca, Contrib<F>& c) {
+  double p[3][3];
+  const int at[3] = {A, B, H};
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) p[m][d] = X.x[3 * at[m] + d];
+  const double e = eabx(p[0], p[1], p[2], ca);
+  const double step = 1.0e-6, dum = 1.0 / (2.0 * step);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    double last = 0.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      p[m][j] = p[m][j] + step;
+      const double er = eabx(p[0], p[1], p[2], ca);
+      p[m][j] = p[m][j] - step * 2.0;
+      const double el = eabx(p[0], p[1], p[2], ca);
+      p[m][j] = p[m][j] + step;
+      last = (er - el) * dum;
+    }
+    c.a[m] = at[m];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) c.g[m][d] = (F)last;
+  }
+  return (F)e;
+}
+
+// One entry of ff_hb (src/ff_hb.f90:55-79): skipped beyond 15 bohr A-B.
+// Out of line (a handful of terms per molecule) to keep the register count
+// of the frequent terms.
+template <class F>
+__device__ __noinline__ F hb_term(const Dev& D, const Tables<F>&, const BeadPos& X, int k, Contrib<F>& c) {
+  const int4 t = __ldg(reinterpret_cast<const int4*>(D.hb) + k);
+  const double r2 = (X.x[3 * t.x] - X.x[3 * t.y]) * (X.x[3 * t.x] - X.x[3 * t.y]) +
+                    (X.x[3 * t.x + 1] - X.x[3 * t.y + 1]) * (X.x[3 * t.x + 1] - X.x[3 * t.y + 1]) +
+                    (X.x[3 * t.x + 2] - X.x[3 * t.y + 2]) * (X.x[3 * t.x + 2] - X.x[3 * t.y + 2]);
+  c.a[0] = t.x;
+  c.a[1] = t.y;
+  c.a[2] = t.z;
+  if (sqrt(r2) > 15.0) {
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) c.g[m][d] = F(0);
+    return F(0);
+  }
+  if (t.w == 1) return hbond_term<F>(X, t.x, t.y, t.z, (F)D.vhb[2 * k], (F)D.vhb[2 * k + 1], c);
+  return xbond_term<F>(X, t.x, t.y, t.z, D.vhb[2 * k], c);
+}
+
+// Energy of one term of kind `kind` (0 bond, 1 angle, 2 torsion, 3 pair, 4 H/halogen bond).
 template <bool MIXED>
 __device__ inline typename std::conditional<MIXED, float, double>::type term(
     const Dev& D, int kind, const BeadPos& x, int m, Contrib<typename std::conditional<MIXED, float, double>::type>& c) {
@@ -581,14 +745,16 @@ __device__ inline typename std::conditional<MIXED, float, double>::type term(
       case 0: return bond_mixed(D, x, m, c);
       case 1: return angle_term<float>(D, D.f, x, m, c);
       case 2: return torsion_term<float>(D, D.f, x, m, c);
-      default: return pair_term<float>(D, D.f, x, m, c);
+      case 3: return pair_term<float>(D, D.f, x, m, c);
+      default: return hb_term<float>(D, D.f, x, m, c);
     }
   } else {
     switch (kind) {
       case 0: return bond_f64(D, x, m, c);
       case 1: return angle_term<double>(D, D.d, x, m, c);
       case 2: return torsion_term<double>(D, D.d, x, m, c);
-      default: return pair_term<double>(D, D.d, x, m, c);
+      case 3: return pair_term<double>(D, D.d, x, m, c);
+      default: return hb_term<double>(D, D.d, x, m, c);
     }
   }
 }
@@ -659,6 +825,7 @@ __device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, doub
   kind_batches<MIXED, 1, 3>(D, X, G, es, ec, lane);
   kind_batches<MIXED, 2, 4>(D, X, G, es, ec, lane);
   kind_batches<MIXED, 3, 2>(D, X, G, es, ec, lane);
+  kind_batches<MIXED, 4, 3>(D, X, G, es, ec, lane);
   for (int a = lane; a < n3; a += 32) gout[a] = gscale * G.get(a);
   double e = (double)es + (double)ec;
 #pragma unroll

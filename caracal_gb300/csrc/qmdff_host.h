@@ -9,7 +9,7 @@
 
 struct cr_qmdff {
   int n = 0;
-  int nterm[4] = {0, 0, 0, 0};  // bonds, angles, torsions, NCI pairs
+  int nterm[cr::qmdff::kKinds] = {0, 0, 0, 0, 0};  // bonds, angles, torsions, NCI pairs, H/halogen bonds
   int ncolors = 0;              // colours summed over batches
   cr::qmdff::Dev dev{};
   std::vector<void*> allocs;    // device buffers owned by the force field

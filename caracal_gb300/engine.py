@@ -96,16 +96,18 @@ class QMDFFForceField:
             angl=ip(np.asarray(ff.angl).reshape(-1, 3)), vangl=fp(np.asarray(ff.vangl).reshape(-1, 2)),
             tors=ip(tors), vtors=fp(np.asarray(ff.vtors).reshape(-1, 14)),
             nci=ip(np.asarray(ff.nci).reshape(-1, 3)),
+            hb=ip(np.asarray(ff.hb).reshape(-1, 3)), vhb=fp(Q.hb_parameters(ff).reshape(-1, 2)),
             r0ab=fp(tables.r0ab[1:, 1:].T), zab=fp(tables.zab[1:, 1:].T),
             r0094=fp(tables.r094[1:, 1:].T), sr42=fp(tables.sr42[1:, 1:].T), c66ab=fp(np.asarray(ff.c6).T))
         a = self._arrs
         d = L.CrQmdffDef()
         d.natoms = self.n
         d.nbond, d.nangl, d.ntors, d.nnci = len(a["bond"]), len(a["angl"]), len(a["tors"]), len(a["nci"])
-        for k in ("at", "bond", "angl", "tors", "nci"):
+        for k in ("at", "bond", "angl", "tors", "nci", "hb"):
             setattr(d, k, L.iptr(a[k]))
-        for k in ("q", "rad", "vbond", "vangl", "vtors", "r0ab", "zab", "r0094", "sr42", "c66ab"):
+        for k in ("q", "rad", "vbond", "vangl", "vtors", "r0ab", "zab", "r0094", "sr42", "c66ab", "vhb"):
             setattr(d, k, L.dptr(a[k]))
+        d.nhb = len(a["hb"])
         e1, e2 = Q.eps_factors()
         for k in range(6):
             d.eps1[k], d.eps2[k] = e1[k + 1], e2[k + 1]
@@ -130,7 +132,7 @@ class QMDFFForceField:
         return e, g
 
     def schedule_info(self):
-        b = np.zeros(4, dtype=np.int32)
+        b = np.zeros(5, dtype=np.int32)
         c = C.c_int()
         L.check(L.lib().cr_qmdff_schedule_info(self._h, L.iptr(b), C.byref(c)), "schedule_info")
         return {"batches": b.tolist(), "colors": c.value}

@@ -29,13 +29,22 @@ from .units import BOHR_ANGSTROM
 
 F32 = lambda x: float(np.float32(x))  # noqa: E731  (REAL(4) literal widened to REAL(8))
 
-# published D3 values Caracal keeps in src/setnonb.f90 (r2r4) for H and C
-R2R4 = {1: F32(2.00734898), 6: F32(3.10492822)}
-# covalent radii (Mantina et al.), Angstrom, src/prepare.f90
-RAD_ANG = {1: 0.32, 6: 0.75}
+# published D3 values Caracal keeps in src/setnonb.f90 (r2r4) for H, C, N, O, Cl
+R2R4 = {1: F32(2.00734898), 6: F32(3.10492822), 7: F32(2.71175247), 8: F32(2.59361680),
+        17: F32(3.72932356)}
+# covalent radii, Angstrom (Caracal's rad table is in bohr, src/prepare.f90)
+RAD_ANG = {1: 0.32, 6: 0.75, 7: 0.71, 8: 0.63, 17: 0.99}
 # synthetic D3-like inputs (not Caracal's D3 tables)
-C6_PAIR = {(1, 1): 3.0898, (1, 6): 7.5916, (6, 6): 18.1368}
-R0AB_PAIR_ANG = {(1, 1): 2.1823, (1, 6): 2.5984, (6, 6): 2.9146}
+C6_PAIR = {(1, 1): 3.0898, (1, 6): 7.5916, (6, 6): 18.1368, (1, 7): 5.5, (1, 8): 4.6, (6, 7): 14.0,
+           (6, 8): 11.5, (7, 7): 11.0, (7, 8): 9.5, (8, 8): 8.0, (1, 17): 12.0, (6, 17): 30.0,
+           (7, 17): 24.0, (8, 17): 20.0, (17, 17): 50.0}
+R0AB_PAIR_ANG = {(1, 1): 2.1823, (1, 6): 2.5984, (6, 6): 2.9146, (1, 7): 2.47, (1, 8): 2.36,
+                 (6, 7): 2.77, (6, 8): 2.66, (7, 7): 2.63, (7, 8): 2.52, (8, 8): 2.41, (1, 17): 2.80,
+                 (6, 17): 3.10, (7, 17): 2.97, (8, 17): 2.86, (17, 17): 3.34}
+# H-bond / halogen-bond scaling of src/setnonb.f90:123-137 (REAL(4) literals)
+SCALE_HB = {7: F32(0.8), 8: F32(0.3), 9: F32(0.1), 15: F32(2.0), 16: F32(2.0), 17: F32(2.0),
+            34: F32(2.0), 35: F32(2.0)}
+SCALE_XB = {17: F32(0.30), 35: F32(0.60), 53: F32(0.80), 85: F32(1.00)}
 
 
 def element_radii():
@@ -47,12 +56,35 @@ def element_radii():
 
 
 def valence_charge(z):
-    """valel (src/valel.f90) for H and C: Z times the REAL(4) fit factor."""
+    """valel (src/valel.f90) for rows 1-3: valence count times the REAL(4) fit factor."""
     if z <= 2:
         return float(z) * F32(2.35)
     if z <= 10:
-        return float(z - 2) * F32(0.95)
-    raise ValueError("only H and C are tabulated")
+        return 1.7 if z == 3 else 5.5 if z == 4 else float(z - 2) * F32(0.95)
+    if z <= 18:
+        return 2.5 if z == 11 else 3.0 if z == 12 else float(z - 10) * F32(0.75)
+    raise ValueError("valence charges are tabulated up to Ar")
+
+
+def hbpara(a, b, q):
+    """src/hbpara.f90: exp(-a q) / (exp(-a q) + b)."""
+    return np.exp(-a * q) / (np.exp(-a * q) + b)
+
+
+def hb_parameters(ff):
+    """vhb(2, nhb) as rdsolvff computes it (src/rdsolvff.f90:142-152): for an H
+    bond (third atom H) ca, cb = hbpara(10, 5, q) * scalehb of atoms 1 and 2,
+    for a halogen bond ca = scalexb(X) * hbpara(-6.5, 1, q(X))."""
+    hb = np.asarray(ff.hb).reshape(-1, 3)
+    v = np.zeros((len(hb), 2))
+    for k, (a, b, h) in enumerate(hb):
+        a, b, h = a - 1, b - 1, h - 1
+        if ff.at[h] == 1:
+            v[k, 0] = hbpara(10.0, 5.0, ff.q[a]) * SCALE_HB.get(int(ff.at[a]), 0.0)
+            v[k, 1] = hbpara(10.0, 5.0, ff.q[b]) * SCALE_HB.get(int(ff.at[b]), 0.0)
+        else:
+            v[k, 0] = SCALE_XB.get(int(ff.at[h]), 0.0) * hbpara(-6.5, 1.0, ff.q[h])
+    return v
 
 
 @dataclass
@@ -63,7 +95,7 @@ class ElementTables:
     sr42: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))
 
     @classmethod
-    def d3_like(cls, elements=(1, 6)):
+    def d3_like(cls, elements=(1, 6, 7, 8, 17)):
         t = cls()
         a1, s8, a2 = F32(0.45), F32(2.7), 4.0
         for zi in elements:
@@ -92,6 +124,7 @@ class QMDFF:
     c6: np.ndarray            # (n, n) pair C6 (Caracal's c6xy)
     e_zero: float = 0.0
     method: str = "synthetic"
+    hb: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), int))  # (nhb, 3) A B H, 1-based
 
     @property
     def n(self):
@@ -99,6 +132,10 @@ class QMDFF:
 
     def rad_bohr(self):
         return np.array([RAD_ANG[int(z)] / BOHR_ANGSTROM for z in self.at])
+
+    @property
+    def nhb(self):
+        return len(np.asarray(self.hb).reshape(-1, 3))
 
 
 def _fmt(x):
@@ -111,7 +148,8 @@ def write_qmdff(ff: QMDFF, path):
         fh.write(f"{ff.n:4d}{1.0:10.4f}{0.0:10.4f}\n{ff.method}\n")
         for i in range(ff.n):
             fh.write(f"{int(ff.at[i]):5d}" + "".join(_fmt(v) for v in ff.xyz[i]) + _fmt(ff.q[i]) + f"{0:5d}\n")
-        fh.write("".join(f"{v:8d}" for v in (len(ff.bond), len(ff.angl), len(ff.tors), 0, len(ff.nci), 0)) + "\n")
+        fh.write("".join(f"{v:8d}" for v in (len(ff.bond), len(ff.angl), len(ff.tors), ff.nhb, len(ff.nci), 0))
+                 + "\n")
         for b, v in zip(ff.bond, ff.vbond):
             fh.write(f"{b[0]:5d}{b[1]:5d}" + "".join(_fmt(x) for x in v) + "\n")
         for a, v in zip(ff.angl, ff.vangl):
@@ -122,6 +160,9 @@ def write_qmdff(ff: QMDFF, path):
             for j in range(int(t[4])):
                 s += f"{v[2 + 3 * j]:4.1f}{v[3 + 3 * j] / np.pi:4.1f}{v[4 + 3 * j]:16.8E}"
             fh.write(s + "\n")
+        htrip = [f"{a:4d}{b:4d}{c:4d}  " for a, b, c in np.asarray(ff.hb).reshape(-1, 3)]
+        for k in range(0, len(htrip), 6):
+            fh.write("".join(htrip[k:k + 6]) + "\n")
         trip = [f"{a:4d}{b:4d}{c:4d}  " for a, b, c in ff.nci]
         for k in range(0, len(trip), 8):
             fh.write("".join(trip[k:k + 8]) + "\n")
@@ -154,8 +195,6 @@ def read_qmdff(path, c6=None):
         v = read(6)
         at[i], xyz[i], q[i] = int(v[0]), v[1:4], v[4]
     nbond, nangl, ntors, nhb, nnci = [int(x) for x in read(5)]
-    if nhb:
-        raise NotImplementedError("H/halogen-bond terms (ff_hb) are not supported yet")
     bond, vbond = np.zeros((nbond, 2), int), np.zeros((nbond, 3))
     for m in range(nbond):
         v = read(5)
@@ -177,11 +216,12 @@ def read_qmdff(path, c6=None):
             vtors[m, 2 + 3 * j] = vals[2 + 3 * j]
             vtors[m, 3 + 3 * j] = vals[3 + 3 * j] * np.pi
             vtors[m, 4 + 3 * j] = vals[4 + 3 * j]
+    hb = np.array(read(3 * nhb, int), dtype=int).reshape(nhb, 3) if nhb else np.zeros((0, 3), int)
     nci = np.array(read(3 * nnci, int), dtype=int).reshape(nnci, 3) if nnci else np.zeros((0, 3), int)
     if c6 is None:
         c6 = pair_c6(at)
     return QMDFF(at=at, xyz=xyz, q=q, bond=bond, vbond=vbond, angl=angl, vangl=vangl, tors=tors,
-                 vtors=vtors, nci=nci, c6=c6)
+                 vtors=vtors, nci=nci, c6=c6, hb=hb)
 
 
 def pair_c6(at):
@@ -272,7 +312,7 @@ def _adjacency(n, bonds):
 
 
 def from_topology(at, xyz, bonds, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002, r0=None,
-                  e_zero=0.0):
+                  e_zero=0.0, charges=None, hb=None):
     """QMDFF terms for a bond list (0-based pairs) on geometry xyz (bohr): bond
     curvature k_bond, angle curvature k_angle, torsion barrier v_tors (each
     drawn in +-20 % from the seed), reference values from the geometry (or
@@ -321,11 +361,38 @@ def from_topology(at, xyz, bonds, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors
         for j in range(i + 1, n):
             if dist[i, j] >= 3:
                 nci.append([i + 1, j + 1, min(int(dist[i, j]), 5)])
-    q = np.where(at == 6, -0.1, 0.1).astype(float)
-    q[at == 1] -= q.sum() / np.count_nonzero(at == 1)   # exact neutrality
-    return QMDFF(at=at, xyz=xyz.copy(), q=q, bond=bond, vbond=vbond, angl=np.array(angl),
-                 vangl=np.array(vangl), tors=np.array(tors).reshape(-1, 6),
-                 vtors=np.array(vtors).reshape(-1, 14), nci=np.array(nci), c6=pair_c6(at), e_zero=e_zero)
+    if charges is None:
+        q = np.where(at == 6, -0.1, 0.1).astype(float)
+        q[at == 1] -= q.sum() / np.count_nonzero(at == 1)   # exact neutrality
+    else:
+        q = np.asarray(charges, dtype=float)
+    hb = np.zeros((0, 3), int) if hb is None else np.asarray(hb, int).reshape(-1, 3)
+    return QMDFF(at=at, xyz=xyz.copy(), q=q, bond=bond, vbond=vbond, angl=np.array(angl).reshape(-1, 3),
+                 vangl=np.array(vangl).reshape(-1, 2), tors=np.array(tors).reshape(-1, 6),
+                 vtors=np.array(vtors).reshape(-1, 14), nci=np.array(nci).reshape(-1, 3), c6=pair_c6(at),
+                 e_zero=e_zero, hb=hb)
+
+
+def water_dimer():
+    """Synthetic QMDFF of a water dimer with one O-H...O hydrogen bond
+    (hb triple: acceptor O, donor O, bridging H), bohr."""
+    xa = np.array([[0.0, 0.0, 0.0], [0.96, 0.0, 0.0], [-0.24, 0.93, 0.0],
+                   [2.91, 0.0, 0.0], [3.23, 0.76, 0.47], [3.23, -0.76, 0.47]])
+    at = np.array([8, 1, 1, 8, 1, 1])
+    return from_topology(at, xa / BOHR_ANGSTROM, [(0, 1), (0, 2), (3, 4), (3, 5)], seed=11,
+                         charges=[-0.6, 0.3, 0.3, -0.6, 0.3, 0.3], hb=[[4, 1, 2]])
+
+
+def chloromethane_ammonia():
+    """Synthetic QMDFF of CH3Cl...NH3 with one C-Cl...N halogen bond (hb triple:
+    C, N, Cl), bohr."""
+    xa = np.array([[0.0, 0.0, 0.0], [-0.36, 1.03, 0.0], [-0.36, -0.51, 0.89], [-0.36, -0.51, -0.89],
+                   [1.78, 0.0, 0.0], [4.88, 0.0, 0.0], [5.26, 0.94, 0.0], [5.26, -0.47, 0.81],
+                   [5.26, -0.47, -0.81]])
+    at = np.array([6, 1, 1, 1, 17, 7, 1, 1, 1])
+    return from_topology(at, xa / BOHR_ANGSTROM, [(0, 1), (0, 2), (0, 3), (0, 4), (5, 6), (5, 7), (5, 8)],
+                         seed=12, charges=[-0.2, 0.12, 0.12, 0.12, -0.16, -0.9, 0.3, 0.3, 0.3],
+                         hb=[[1, 6, 5]])
 
 
 def alkane(nc=20, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors=0.002):

@@ -38,7 +38,7 @@ extern "C" {
 #define CR_PES_H3 1      /* ANA_H3: BKMP2, src/egrad_h3.f */
 #define CR_PES_CH4H 2    /* ANA_CH4H: src/egrad_ch4h.f + src/util_ch4h.f */
 #define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f + src/util_ch4oh.f */
-#define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90 (ff_hb not built yet) */
+#define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90, ff_hb.f90 */
 #define CR_PES_EVB 5     /* dE-EVB of two QMDFFs: src/gradient.f90:361-386, 1228-1304 */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
@@ -126,8 +126,8 @@ int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d
 /* ---- QMDFF force field ------------------------------------------------------
  * Replaces the QMDFF branch of `gradient` (src/gradient.f90:342-358):
  * `ff_eg(n,at,xyz,e,g)` (src/ff_eg.f90:41) + `ff_nonb(n,at,xyz,q,r0ab,zab,
- * r0094,sr42,c66ab,enb,g)` (src/ff_nonb.f90:34) + E_zero, one molecule, not
- * periodic, no H/halogen-bond terms (nhb = 0).  The arrays are those of module
+ * r0094,sr42,c66ab,enb,g)` (src/ff_nonb.f90:34) + `ff_hb(n,at,xyz,eh,g)`
+ * (src/ff_hb.f90:36) + E_zero, one molecule, not periodic.  The arrays are those of module
  * qmdff (src/qmdff.f90:52-57, 1-based atom indices, Fortran column-major) and
  * the ff_nonb arguments; they are copied to the device at creation. */
 typedef struct cr_qmdff_def {
@@ -153,6 +153,9 @@ typedef struct cr_qmdff_def {
   int zahn;               /* 1: Zahn Coulomb q q (erfc(a r)/r - par (r - cut)), no eps1 */
   double zahn_a, zahn_par;
   double e_zero;          /* E_zero1 shift */
+  int nhb;                /* H/halogen bonds (src/ff_hb.f90; one molecule: the listed triples) */
+  const int* hb;          /* hb(3,nhb): A, B, H (H bond if at(H) = 1, else halogen bond) */
+  const double* vhb;      /* vhb(2,nhb): rdsolvff's hbpara * scalehb / scalexb values */
 } cr_qmdff_def;
 typedef struct cr_qmdff cr_qmdff;
 int cr_qmdff_create(const cr_qmdff_def* def, cr_qmdff** out);
@@ -162,8 +165,8 @@ int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, doubl
 /* Same on device-resident arrays; stream may be 0. */
 int cr_qmdff_egrad_device(cr_qmdff* ff, const double* d_xyz, int nbeads, double* d_e, double* d_g,
                           int precision, void* stream);
-/* Term batches of the warp schedule (bonds, angles, torsions, NCI pairs) and
- * the colours they need (diagnostics). */
+/* Term batches of the warp schedule (batches[5]: bonds, angles, torsions,
+ * NCI pairs, H/halogen bonds) and the colours they need (diagnostics). */
 int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors);
 /* No counterpart in Caracal.  The force kernel comes in three occupancy
  * variants per form; the first launch of >= 2048 beads outside a stream

@@ -51,7 +51,8 @@ class QmdffDef(C.Structure):
                 ("vtors", C.POINTER(C.c_double)), ("nci", C.POINTER(C.c_int)),
                 ("pR0", C.POINTER(C.c_double)), ("pC6", C.POINTER(C.c_double)),
                 ("pSr42", C.POINTER(C.c_double)), ("pZab", C.POINTER(C.c_double)),
-                ("pAlpha", C.POINTER(C.c_double)), ("eps1", C.c_double * 7), ("eps2", C.c_double * 7),
+                ("pAlpha", C.POINTER(C.c_double)), ("nhb", C.c_int), ("hb", C.POINTER(C.c_int)),
+                ("vhb", C.POINTER(C.c_double)), ("eps1", C.c_double * 7), ("eps2", C.c_double * 7),
                 ("coul_cut", C.c_double), ("zahn", C.c_int), ("zahn_a", C.c_double),
                 ("zahn_par", C.c_double), ("e_zero", C.c_double)]
 
@@ -81,7 +82,9 @@ def set_qmdff(ff, tables, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
     from caracal_gb300 import qmdff as Q
     ip = lambda a: np.ascontiguousarray(a, dtype=np.int32)  # noqa: E731
     fp = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    hb = np.asarray(getattr(ff, "hb", np.zeros((0, 3), int))).reshape(-1, 3)
     arrs = dict(at=ip(ff.at), q=fp(ff.q), rad=fp(ff.rad_bohr()), bond=ip(ff.bond - 1),
+                hb=ip(hb - 1 if len(hb) else hb), vhb=fp(Q.hb_parameters(ff) if len(hb) else np.zeros((0, 2))),
                 vbond=fp(ff.vbond), angl=ip(ff.angl - 1), vangl=fp(ff.vangl),
                 tors=ip(np.column_stack([ff.tors[:, :4] - 1, ff.tors[:, 4:]])), vtors=fp(ff.vtors),
                 nci=ip(np.column_stack([ff.nci[:, :2] - 1, ff.nci[:, 2]])))
@@ -93,8 +96,10 @@ def set_qmdff(ff, tables, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
     d.nbond, d.nangl, d.ntors, d.nnci = len(ff.bond), len(ff.angl), len(ff.tors), len(ff.nci)
     for k in ("q", "rad", "vbond", "vangl", "vtors"):
         setattr(d, k, arrs[k].ctypes.data_as(C.POINTER(C.c_double)))
-    for k in ("at", "bond", "angl", "tors", "nci"):
+    for k in ("at", "bond", "angl", "tors", "nci", "hb"):
         setattr(d, k, arrs[k].ctypes.data_as(C.POINTER(C.c_int)))
+    d.vhb = arrs["vhb"].ctypes.data_as(C.POINTER(C.c_double))
+    d.nhb = len(hb)
     for k, a in zip(("pR0", "pC6", "pSr42", "pZab", "pAlpha"), pr):
         setattr(d, k, a.ctypes.data_as(C.POINTER(C.c_double)))
     for i in range(7):

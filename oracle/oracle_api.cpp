@@ -95,6 +95,11 @@ void orc_qmdff_set(const orc_qmdff_def* d) {
   f.pSr42.assign(d->pSr42, d->pSr42 + f.nnci);
   f.pZab.assign(d->pZab, d->pZab + f.nnci);
   f.pAlpha.assign(d->pAlpha, d->pAlpha + f.nnci);
+  f.nhb = d->nhb;
+  if (f.nhb > 0) {
+    f.hb.assign(d->hb, d->hb + 3 * f.nhb);
+    f.vhb.assign(d->vhb, d->vhb + 2 * f.nhb);
+  }
   for (int i = 0; i < 7; ++i) {
     f.eps1[i] = d->eps1[i];
     f.eps2[i] = d->eps2[i];

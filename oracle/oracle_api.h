@@ -66,6 +66,9 @@ typedef struct orc_qmdff_def {
   const double* vtors;/* 14 per torsion */
   const int* nci;     /* 3 per pair */
   const double *pR0, *pC6, *pSr42, *pZab, *pAlpha;
+  int nhb;
+  const int* hb;      /* 3 per triple: A, B, H (0-based) */
+  const double* vhb;  /* 2 per triple */
   double eps1[7], eps2[7];
   double coul_cut;
   int zahn;

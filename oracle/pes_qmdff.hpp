@@ -14,7 +14,13 @@
 //           Zahn form q q (erfc(a r)/r - b (r - coul_cut)) (:337-416); the
 //           dipole moment (:743-762) never reaches the outputs and is skipped
 //   gradient src/gradient.f90:342-358 e = ff_eg + ff_nonb (+ ff_hb) + E_zero
-// H/halogen-bond terms (ff_hb) are not restated yet (nhb must be 0).
+//   ff_hb   src/ff_hb.f90:36-93 (one molecule: the listed triples only)
+//           eabhag src/eabhag.f90:35-220 (analytic H bond), eabxag
+//           src/eabxag.f90:35-156 with eabx src/eabx.f90:34-111 (halogen
+//           bond, central-difference gradient).  Quirk reproduced: eabxag
+//           assigns the scalar difference quotient to the whole 3-vector in
+//           each of its j loops, so every component of each atom's gradient
+//           is the z derivative.
 // REAL(4) literals reproduced: abdamp's cutoff 3.0 * 3.5710642 (a float
 // product), eps1(3) = 0.85 (src/setnonb.f90:164-190).
 #pragma once
@@ -50,6 +56,9 @@ struct FF {
   std::vector<int> tors;        // i, j, k, l (0-based), nt, type
   std::vector<double> vtors;    // 14 per torsion: phi0, V, (rn, phase*pi, V_n) x 4
   std::vector<int> nci;         // i, j (0-based), category nk (1..6)
+  int nhb = 0;
+  std::vector<int> hb;          // A, B, H (0-based): H-bond if at(H) = 1, else halogen bond
+  std::vector<double> vhb;      // 2 per triple: ca, cb (rdsolvff's hbpara * scalehb / scalexb)
   // per nci pair parameters: R0 (r094), C6, sr42, zab, alpha (r0ab)
   std::vector<double> pR0, pC6, pSr42, pZab, pAlpha;
   double eps1[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -432,12 +441,161 @@ inline void ff_nonb(const FF& ff, const T* x, T* enb, T* g) {
   *enb = *enb + e;
 }
 
+// eabhag (src/eabhag.f90:35-220): one hydrogen bond A...H-B, energy and
+// analytic gradient accumulated into e, g; nothing if E > -1e-8.
+template <class T>
+inline void eabhag(const T* x, int A, int B, int H, double ca, double cb, T* e, T* g) {
+  const double longcut = 8.0, alp7 = 12.0, alp3 = 6.0;
+  T drah[3], drbh[3], drab[3];
+  for (int c = 0; c < 3; ++c) {
+    drah[c] = x[3 * A + c] - x[3 * H + c];
+    drbh[c] = x[3 * B + c] - x[3 * H + c];
+    drab[c] = x[3 * A + c] - x[3 * B + c];
+  }
+  T rab2 = drab[0] * drab[0] + drab[1] * drab[1] + drab[2] * drab[2];
+  T rab = sqrt(rab2);
+  T rah2 = drah[0] * drah[0] + drah[1] * drah[1] + drah[2] * drah[2];
+  T rah = sqrt(rah2);
+  T rbh2 = drbh[0] * drbh[0] + drbh[1] * drbh[1] + drbh[2] * drbh[2];
+  T rbh = sqrt(rbh2);
+  T ratio = pow(rab / longcut, T(alp7));
+  T rdampl = 1.0 / (1.0 + ratio);
+  rdampl = rdampl / rab2 / rab;
+  T cosabh, aprod;
+  const bool far_a = rah2 > rbh2;
+  if (far_a) {
+    aprod = 1.0 / rbh / rab;
+    cosabh = -(drbh[0] * drab[0] + drbh[1] * drab[1] + drbh[2] * drab[2]) * aprod;
+  } else {
+    aprod = 1.0 / rah / rab;
+    cosabh = (drah[0] * drab[0] + drah[1] * drab[1] + drah[2] * drab[2]) * aprod;
+  }
+  T aterm = 0.5 * (cosabh + 1.0);
+  T apref = pow(aterm, T(alp3 - 1));
+  aterm = aterm * apref;
+  apref = alp3 * 0.5 * apref;
+  T rah4 = rah2 * rah2, rbh4 = rbh2 * rbh2;
+  T denom = 1.0 / (rah4 + rbh4);
+  T da = (ca * rah4 + cb * rbh4) * denom;
+  T eabh = -da * rdampl * aterm;
+  if (eabh > -1.0e-8) return;
+  *e = *e + eabh;
+  T ga[3], gb[3], gh[3], dg[3], dg2[3];
+  T gi = 4.0 * (ca - cb) * rah2 * rbh4 * denom * denom;
+  gi = -gi * rdampl * aterm;
+  for (int c = 0; c < 3; ++c) ga[c] = gi * drah[c];
+  gi = 4.0 * (cb - ca) * rbh2 * rah4 * denom * denom;
+  gi = -gi * rdampl * aterm;
+  for (int c = 0; c < 3; ++c) {
+    gb[c] = gi * drbh[c];
+    gh[c] = -ga[c] - gb[c];
+  }
+  gi = rdampl * rdampl * rab * (3.0 + (3.0 + alp7) * ratio);
+  gi = gi * da * aterm;
+  for (int c = 0; c < 3; ++c) {
+    dg[c] = gi * drab[c];
+    ga[c] = ga[c] + dg[c];
+    gb[c] = gb[c] - dg[c];
+  }
+  gi = -da * rdampl * apref;
+  if (far_a) {
+    for (int c = 0; c < 3; ++c) {
+      dg[c] = -aprod * drbh[c] - cosabh * drab[c] / rab2;
+      dg2[c] = aprod * drab[c] + cosabh * drbh[c] / rbh2;
+      dg[c] = gi * dg[c];
+      dg2[c] = gi * dg2[c];
+      ga[c] = ga[c] + dg[c];
+      gh[c] = gh[c] + dg2[c];
+      gb[c] = gb[c] - dg[c] - dg2[c];
+    }
+  } else {
+    for (int c = 0; c < 3; ++c) {
+      dg[c] = -aprod * drah[c] + cosabh * drab[c] / rab2;
+      dg2[c] = -aprod * drab[c] + cosabh * drah[c] / rah2;
+      dg[c] = gi * dg[c];
+      dg2[c] = gi * dg2[c];
+      gb[c] = gb[c] + dg[c];
+      gh[c] = gh[c] + dg2[c];
+      ga[c] = ga[c] - dg[c] - dg2[c];
+    }
+  }
+  for (int c = 0; c < 3; ++c) {
+    g[3 * A + c] += ga[c];
+    g[3 * B + c] += gb[c];
+    g[3 * H + c] += gh[c];
+  }
+}
+
+// eabx (src/eabx.f90:34-111): halogen-bond energy of A...X-B (X = H arg).
+template <class T>
+inline T eabx(const T* x, int A, int B, int H, double ca) {
+  const double longcut = 120.0, alp7 = 6.0, alp3 = 6.0;
+  T rb[3];
+  for (int c = 0; c < 3; ++c) rb[c] = x[3 * A + c] - x[3 * B + c];
+  T rab2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+  T dampl = 1.0 / (1.0 + pow(rab2 / longcut, T(alp7)));
+  for (int c = 0; c < 3; ++c) rb[c] = x[3 * A + c] - x[3 * H + c];
+  T d2ik = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+  for (int c = 0; c < 3; ++c) rb[c] = x[3 * H + c] - x[3 * B + c];
+  T d2jk = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+  T xy, term;
+  if (d2ik > d2jk) {
+    xy = sqrt(rab2 * d2jk);
+    term = 0.5 * (rab2 + d2jk - d2ik) / xy;
+  } else {
+    xy = sqrt(rab2 * d2ik);
+    term = 0.5 * (rab2 + d2ik - d2jk) / xy;
+  }
+  T aterm = pow(0.5 * (term + 1.0), T(alp3));
+  return -ca * dampl * aterm / d2jk;
+}
+
+// eabxag (src/eabxag.f90:35-156): energy plus Caracal's difference quotients
+// (step 1e-6); each atom's three components all get the z-direction quotient.
+template <class T>
+inline void eabxag(const T* x0, int n, int A, int B, int H, double ca, T* e, T* g) {
+  std::vector<T> x(x0, x0 + 3 * n);
+  *e = *e + eabx<T>(x.data(), A, B, H, ca);
+  const double step = 1.0e-6;
+  const double dum = 1.0 / (2.0 * step);
+  const int atoms[3] = {A, B, H};
+  for (int ia = 0; ia < 3; ++ia) {
+    const int at = atoms[ia];
+    T last = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      x[3 * at + j] = x[3 * at + j] + step;
+      T er = eabx<T>(x.data(), A, B, H, ca);
+      x[3 * at + j] = x[3 * at + j] - step * 2.0;
+      T el = eabx<T>(x.data(), A, B, H, ca);
+      x[3 * at + j] = x[3 * at + j] + step;
+      last = (er - el) * dum;
+    }
+    for (int c = 0; c < 3; ++c) g[3 * at + c] += last;
+  }
+}
+
+// ff_hb (src/ff_hb.f90:36-93) for one molecule: the listed triples, skipped
+// beyond 15 bohr between A and B.
+template <class T>
+inline void ff_hb(const FF& ff, const T* x, T* eh, T* g) {
+  for (int k = 0; k < ff.nhb; ++k) {
+    const int i1 = ff.hb[3 * k], i2 = ff.hb[3 * k + 1], i = ff.hb[3 * k + 2];
+    T rb[3];
+    for (int c = 0; c < 3; ++c) rb[c] = x[3 * i1 + c] - x[3 * i2 + c];
+    T r = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
+    if (r > 15.0) continue;
+    if (ff.at[i] == 1) eabhag<T>(x, i1, i2, i, ff.vhb[2 * k], ff.vhb[2 * k + 1], eh, g);
+    else eabxag<T>(x, ff.n, i1, i2, i, ff.vhb[2 * k], eh, g);
+  }
+}
+
 // gradient dispatch for one QMDFF (src/gradient.f90:342-358)
 template <class T>
 inline void egrad(const FF& ff, const T* x, T* V, T* g) {
   T e;
   ff_eg(ff, x, &e, g);
   ff_nonb(ff, x, &e, g);
+  ff_hb(ff, x, &e, g);
   *V = e + ff.e_zero;
 }
 

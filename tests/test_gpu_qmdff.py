@@ -196,3 +196,23 @@ def test_recross_unsupported_on_qmdff(gpu_ff, alkane):
     with pytest.raises(CaracalError):
         eng.set_recross([1], [2], (1, 2), (1, 3), 2.0, 2.0, 10.0, max_steps=4)
     eng.close()
+
+
+@pytest.mark.parametrize("system,tol", [("water_dimer", 1e-12), ("chloromethane_ammonia", 1e-9)])
+def test_hbond_terms_match_oracle(require_gpu, system, tol):
+    # halogen bonds carry Caracal's difference-quotient gradient (step 1e-6):
+    # rounding differences of the two energies are amplified by 5e5, so their
+    # parity bound is 1e-9; hydrogen bonds are analytic (1e-12)
+    ff = getattr(Q, system)()
+    tab = Q.ElementTables.d3_like()
+    orc.set_qmdff(ff, tab)
+    gff = QMDFFForceField(ff, tab)
+    assert gff.schedule_info()["batches"][4] == 1
+    x = ff.xyz[None] + np.random.default_rng(4).normal(0, 0.03, (64,) + ff.xyz.shape)
+    e, g = gff.egrad(x, "fp64")
+    eo, go = orc.egrad("qmdff", x)
+    em, gm = gff.egrad(x, "mixed")
+    gff.close()
+    assert rel_err(e, eo) <= 1e-12
+    assert rel_err(g, go) <= tol
+    assert np.sqrt(np.sum((gm - g) ** 2) / np.sum(g ** 2)) <= 5e-6

@@ -89,3 +89,53 @@ def test_element_tables_real4_literals():
     assert Q.eps_factors()[0][3] == float(np.float32(0.85))
     r = Q.element_radii()
     assert r.shape == (94,) and r[0] > 0 and r[5] > 0
+
+
+def test_hbond_gradient_central_differences():
+    # eabhag (src/eabhag.f90) is analytic: its gradient is the derivative of
+    # its energy; the synthetic water dimer has one O-H...O triple
+    ff = Q.water_dimer()
+    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    x = ff.xyz + np.random.default_rng(0).normal(0, 0.03, ff.xyz.shape)
+    V, g = orc.egrad("qmdff", x)
+    ff0 = Q.QMDFF(**{**ff.__dict__, "hb": np.zeros((0, 3), int)})
+    orc.set_qmdff(ff0, Q.ElementTables.d3_like())
+    V0, _ = orc.egrad("qmdff", x)
+    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    assert V[0] < V0[0] - 1e-4          # the H bond is attractive here
+    h = 1e-5
+    for a in range(ff.n):
+        for d in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[a, d] += h
+            xm[a, d] -= h
+            fd = (orc.egrad("qmdff", xp)[0][0] - orc.egrad("qmdff", xm)[0][0]) / (2 * h)
+            assert abs(fd - g[0][a, d]) < 1e-9
+
+
+def test_halogen_bond_reproduces_reference_quirk():
+    # eabxag (src/eabxag.f90:111-134) assigns each scalar difference quotient
+    # to the whole 3-vector inside its j loop: every component of each of the
+    # three atoms' gradients equals that atom's z quotient
+    ff = Q.chloromethane_ammonia()
+    tab = Q.ElementTables.d3_like()
+    x = ff.xyz + np.random.default_rng(1).normal(0, 0.03, ff.xyz.shape)
+    orc.set_qmdff(ff, tab)
+    _, g = orc.egrad("qmdff", x)
+    orc.set_qmdff(Q.QMDFF(**{**ff.__dict__, "hb": np.zeros((0, 3), int)}), tab)
+    _, g0 = orc.egrad("qmdff", x)
+    dg = g[0] - g0[0]
+    for atom in (0, 4, 5):              # C, Cl, N of the triple
+        assert np.allclose(dg[atom], dg[atom][2], rtol=0, atol=1e-15)
+        assert abs(dg[atom][2]) > 1e-6
+    others = [i for i in range(ff.n) if i not in (0, 4, 5)]
+    assert np.max(np.abs(dg[others])) < 1e-15
+
+
+def test_qmdff_file_round_trip_with_hbonds(tmp_path):
+    ff = Q.water_dimer()
+    path = tmp_path / "w2.qmdff"
+    Q.write_qmdff(ff, path)
+    rd = Q.read_qmdff(path)
+    assert np.array_equal(rd.hb, ff.hb) and np.array_equal(rd.nci, ff.nci)
+    np.testing.assert_allclose(Q.hb_parameters(rd), Q.hb_parameters(ff), atol=1e-10)
