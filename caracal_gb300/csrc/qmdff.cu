@@ -308,64 +308,72 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   ff->nterm[3] = d->nnci;
   ff->nterm[4] = d->nhb;
 
-  // schedule: torsions grouped by (type, nt) so a batch runs one code path
-  std::vector<int> slot;
-  std::vector<unsigned char> color, ncol;
+  // schedules (plain, mixed): torsions grouped by (type, nt) so a batch runs
+  // one code path
+  std::vector<int> slot[2];
+  std::vector<unsigned char> color[2], ncol[2];
   cr::qmdff::Dev& D = ff->dev;
   D.n = n;
-  int boff = 0;
   bool distinct = true;
-  for (int kind = 0; kind < cr::qmdff::kKinds; ++kind) {
-    std::vector<int> order((size_t)ff->nterm[kind]);
-    for (int m = 0; m < ff->nterm[kind]; ++m) order[(size_t)m] = m;
-    std::vector<int> atoms;
-    int arity = 2;
-    if (kind == 0) atoms = bond;
-    if (kind == 1) {
-      arity = 3;
-      atoms = angl;
+  for (int form = 0; form < 2; ++form) {
+    int boff = 0;
+    for (int kind = 0; kind < cr::qmdff::kKinds; ++kind) {
+      std::vector<int> order((size_t)ff->nterm[kind]);
+      for (int m = 0; m < ff->nterm[kind]; ++m) order[(size_t)m] = m;
+      std::vector<int> atoms;
+      int arity = 2;
+      if (kind == 0) atoms = bond;
+      if (kind == 1) {
+        arity = 3;
+        atoms = angl;
+      }
+      if (kind == 2) {
+        arity = 4;
+        atoms.resize((size_t)4 * d->ntors);
+        for (int m = 0; m < d->ntors; ++m)
+          for (int a = 0; a < 4; ++a) atoms[(size_t)4 * m + a] = tors[(size_t)6 * m + a];
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+          const int kx = tors[(size_t)6 * x + 5] * 8 + tors[(size_t)6 * x + 4];
+          const int ky = tors[(size_t)6 * y + 5] * 8 + tors[(size_t)6 * y + 4];
+          return kx < ky;
+        });
+      }
+      if (kind == 3) atoms = pair;
+      if (kind == 4) {
+        arity = 3;
+        atoms.resize((size_t)3 * d->nhb);
+        for (int m = 0; m < d->nhb; ++m)
+          for (int a = 0; a < 3; ++a) atoms[(size_t)3 * m + a] = hb[(size_t)4 * m + a];
+      }
+      int nb = 0;
+      int* colours = form == 1 ? &ff->ncolors : &ff->ncolors_fp64;
+      if (form == 1 && kind == 3) {
+        schedule_pairs(ff->nterm[kind], atoms, n, slot[form], color[form], ncol[form], nb, *colours);
+      } else {
+        const int max_colours = form == 0 ? 255 : (kind == 0 ? 1 : 2);
+        schedule_kind(ff->nterm[kind], arity, max_colours, atoms, order, n, slot[form], color[form], ncol[form], nb,
+                      *colours);
+      }
+      if (form == 0)
+        for (int m = 0; m < ff->nterm[kind]; ++m)
+          for (int x = 0; x < arity; ++x)
+            for (int y = x + 1; y < arity; ++y)
+              if (atoms[(size_t)m * arity + x] == atoms[(size_t)m * arity + y]) distinct = false;
+      D.sched[form].nb[kind] = nb;
+      D.sched[form].boff[kind] = boff;
+      boff += nb;
     }
-    if (kind == 2) {
-      arity = 4;
-      atoms.resize((size_t)4 * d->ntors);
-      for (int m = 0; m < d->ntors; ++m)
-        for (int a = 0; a < 4; ++a) atoms[(size_t)4 * m + a] = tors[(size_t)6 * m + a];
-      std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        const int kx = tors[(size_t)6 * x + 5] * 8 + tors[(size_t)6 * x + 4];
-        const int ky = tors[(size_t)6 * y + 5] * 8 + tors[(size_t)6 * y + 4];
-        return kx < ky;
-      });
-    }
-    if (kind == 3) atoms = pair;
-    if (kind == 4) {
-      arity = 3;
-      atoms.resize((size_t)3 * d->nhb);
-      for (int m = 0; m < d->nhb; ++m)
-        for (int a = 0; a < 3; ++a) atoms[(size_t)3 * m + a] = hb[(size_t)4 * m + a];
-    }
-    int nb = 0;
-    if (kind == 3) {
-      schedule_pairs(ff->nterm[kind], atoms, n, slot, color, ncol, nb, ff->ncolors);
-    } else {
-      const int max_colours = (kind == 0) ? 1 : 2;
-      schedule_kind(ff->nterm[kind], arity, max_colours, atoms, order, n, slot, color, ncol, nb, ff->ncolors);
-    }
-    for (int m = 0; m < ff->nterm[kind]; ++m)
-      for (int x = 0; x < arity; ++x)
-        for (int y = x + 1; y < arity; ++y)
-          if (atoms[(size_t)m * arity + x] == atoms[(size_t)m * arity + y]) distinct = false;
-    D.nb[kind] = nb;
-    D.boff[kind] = boff;
-    boff += nb;
   }
 
   int rc = CR_OK;
   auto up = [&](auto& h, auto** dp) {
     if (rc == CR_OK) rc = upload(ff, h, dp);
   };
-  up(slot, &D.slot);
-  up(color, &D.color);
-  up(ncol, &D.ncol);
+  for (int form = 0; form < 2; ++form) {
+    up(slot[form], &D.sched[form].slot);
+    up(color[form], &D.sched[form].color);
+    up(ncol[form], &D.sched[form].ncol);
+  }
   up(bond, &D.bond);
   up(angl, &D.angl);
   up(tors, &D.tors);
@@ -401,7 +409,7 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
 int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors) {
   if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
   if (batches)
-    for (int k = 0; k < cr::qmdff::kKinds; ++k) batches[k] = ff->dev.nb[k];
+    for (int k = 0; k < cr::qmdff::kKinds; ++k) batches[k] = ff->dev.sched[1].nb[k];
   if (colors) *colors = ff->ncolors;
   return CR_OK;
 }

@@ -44,13 +44,22 @@ struct Tables {
 
 constexpr int kKinds = 5;  // bonds, angles, torsions, NCI pairs, H/halogen bonds
 
-struct Dev {
-  int n;
+// Warp schedule of the terms: batches of 32 slots (one term per lane) with
+// the colour of each slot; no atom appears twice within a colour.
+struct Schedule {
   int nb[kKinds];    // batches per kind
   int boff[kKinds];  // first batch of each kind
   const int* slot;             // [batches][32]: term index or -1
   const unsigned char* color;  // [batches][32]
   const unsigned char* ncol;   // [batches]
+};
+
+struct Dev {
+  int n;
+  // [0] plain form: full 32-term batches, as many colours as needed (an FP64
+  // term costs far more than a scatter round); [1] mixed form: NCI pairs in
+  // round-robin matchings (one colour), bonds one colour, others two.
+  Schedule sched[2];
   const int* bond;   // 2 per bond (0-based)
   const int* angl;   // 3 per angle (centre, i, k)
   const int* tors;   // 6 per torsion: i, j, k, l, nt, type
@@ -767,18 +776,23 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
                                     typename std::conditional<MIXED, float, double>::type& es,
                                     typename std::conditional<MIXED, float, double>::type& ec, int lane) {
   using F = typename std::conditional<MIXED, float, double>::type;
-  const int b0 = D.boff[KIND], nb = D.nb[KIND];
+  const Schedule& S = D.sched[MIXED ? 1 : 0];
+  const int b0 = S.boff[KIND], nb = S.nb[KIND];
   const bool distinct = D.distinct != 0;
   for (int b = b0; b < b0 + nb; ++b) {
-    const int m = D.slot[32 * b + lane];
-    const int col = D.color[32 * b + lane];
-    const int ncol = D.ncol[b];
+    const int m = S.slot[32 * b + lane];
+    const int col = S.color[32 * b + lane];
+    const int ncol = S.ncol[b];
     Contrib<F> c;
     if (m >= 0) {
       const F v = term<MIXED>(D, KIND, X, m, c);
-      const F t = es + v;
-      ec += (fabs(es) >= fabs(v)) ? ((es - t) + v) : ((v - t) + es);
-      es = t;
+      if constexpr (MIXED) {  // compensated FP32 lane sum
+        const F t = es + v;
+        ec += (fabs(es) >= fabs(v)) ? ((es - t) + v) : ((v - t) + es);
+        es = t;
+      } else {
+        es += v;
+      }
     }
     for (int k = 0; k < ncol; ++k) {
       if (m >= 0 && col == k) scatter<NA>(c, G, distinct);

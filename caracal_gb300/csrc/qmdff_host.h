@@ -10,7 +10,8 @@
 struct cr_qmdff {
   int n = 0;
   int nterm[cr::qmdff::kKinds] = {0, 0, 0, 0, 0};  // bonds, angles, torsions, NCI pairs, H/halogen bonds
-  int ncolors = 0;              // colours summed over batches
+  int ncolors = 0;              // colours summed over the mixed form's batches
+  int ncolors_fp64 = 0;         // the same for the plain form's schedule
   cr::qmdff::Dev dev{};
   std::vector<void*> allocs;    // device buffers owned by the force field
   int variant[2] = {-1, -1};    // autotuned kernel variant per form (FP64, mixed); -1: not yet

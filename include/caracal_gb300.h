@@ -165,8 +165,9 @@ int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, doubl
 /* Same on device-resident arrays; stream may be 0. */
 int cr_qmdff_egrad_device(cr_qmdff* ff, const double* d_xyz, int nbeads, double* d_e, double* d_g,
                           int precision, void* stream);
-/* Term batches of the warp schedule (batches[5]: bonds, angles, torsions,
- * NCI pairs, H/halogen bonds) and the colours they need (diagnostics). */
+/* Term batches of the mixed form's warp schedule (batches[5]: bonds, angles,
+ * torsions, NCI pairs, H/halogen bonds) and the colours they need
+ * (diagnostics; the plain form uses full 32-term batches). */
 int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors);
 /* No counterpart in Caracal.  The force kernel comes in three occupancy
  * variants per form; the first launch of >= 2048 beads outside a stream
