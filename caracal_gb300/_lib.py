@@ -25,6 +25,7 @@ CR_ERR_IO = 6
 
 CR_TRAJ_NONFINITE = 1
 CR_TRAJ_SINGULAR_INERTIA = 2
+CR_TRAJ_SHAKE_FAILED = 4
 
 CR_PES_H3 = 1
 CR_PES_CH4H = 2
@@ -119,6 +120,7 @@ def _sig(lib):
         "cr_engine_set_recross": ([eng, C.POINTER(CrRecross), C.c_int], C.c_int),
         "cr_engine_init_children": ([eng, d], C.c_int),
         "cr_engine_kappa": ([eng, d, d, d, i], C.c_int),
+        "cr_engine_set_parent": ([eng, C.POINTER(CrRecross)], C.c_int),
         "cr_qmdff_create": ([C.POINTER(CrQmdffDef), C.POINTER(C.c_void_p)], C.c_int),
         "cr_qmdff_destroy": ([v], C.c_int),
         "cr_qmdff_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),

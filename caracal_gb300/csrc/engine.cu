@@ -215,6 +215,11 @@ struct cr_engine {
   int* d_istep = nullptr;
   int h_istep = 0;
   double* d_vnh = nullptr;  // [T][4] Nose-Hoover chain velocities
+  // constrained parent (analytic surfaces through the graph path)
+  bool parent = false;
+  int step_launches = 5;  // kernels per step of the graph path
+  double *d_dxi = nullptr, *d_cq = nullptr;
+  int* d_shake_fail = nullptr;
   size_t smem_drift = 0, smem_kick = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -338,10 +343,52 @@ int launch_forces(cr_engine* e) {
 }
 
 // Forces of the large-molecule path: one QMDFF, or the dE-EVB of two.
+template <class PES>
+int egrad_launch(cr_engine* e, double* V, double* f) {
+  const int nb = e->T * e->P, bs = 128;
+  if (e->cfg.precision == CR_PREC_MIXED)
+    cr::egrad_kernel<PES, true><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, V, f);
+  else
+    cr::egrad_kernel<PES, false><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, V, f);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
 int split_forces(cr_engine* e, double* V, double* f) {
   if (e->evb)
     return evb_launch(e->evb, e->d_q, e->T * e->P, V, f, e->d_V2, e->d_f2, e->cfg.precision, e->stream);
-  return qmdff_launch(e->ff, e->d_q, e->T * e->P, V, f, e->cfg.precision, e->stream);
+  if (e->ff) return qmdff_launch(e->ff, e->d_q, e->T * e->P, V, f, e->cfg.precision, e->stream);
+  switch (e->cfg.pes) {
+    case CR_PES_H3: return egrad_launch<cr::PesH3>(e, V, f);
+    case CR_PES_CH4H: return egrad_launch<cr::PesCH4H>(e, V, f);
+    case CR_PES_CH4OH: return egrad_launch<cr::PesCH4OH>(e, V, f);
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+}
+
+// SHAKE / RATTLE of the constrained parent (template on the atom count)
+int parent_kernel(cr_engine* e, int which) {
+  const int T = e->T;
+  switch (e->N) {
+    case 3:
+      if (which == 0) cr::split_shake_kernel<3><<<T, 32, 0, e->stream>>>(e->sp);
+      else if (which == 1) cr::split_rattle_kernel<3><<<T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      else cr::split_parent_init_kernel<3><<<(T + 63) / 64, 64, 0, e->stream>>>(e->sp);
+      break;
+    case 6:
+      if (which == 0) cr::split_shake_kernel<6><<<T, 32, 0, e->stream>>>(e->sp);
+      else if (which == 1) cr::split_rattle_kernel<6><<<T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      else cr::split_parent_init_kernel<6><<<(T + 63) / 64, 64, 0, e->stream>>>(e->sp);
+      break;
+    case 7:
+      if (which == 0) cr::split_shake_kernel<7><<<T, 32, 0, e->stream>>>(e->sp);
+      else if (which == 1) cr::split_rattle_kernel<7><<<T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      else cr::split_parent_init_kernel<7><<<(T + 63) / 64, 64, 0, e->stream>>>(e->sp);
+      break;
+    default: return fail(CR_ERR_UNSUPPORTED, "constrained parents are built for the analytic surfaces");
+  }
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
 }
 
 // One step of the large-molecule path as kernel launches on e->stream
@@ -356,13 +403,30 @@ int split_step_launches(cr_engine* e) {
   }
   cr::split_drift_kernel<<<grid, cr::kSplitBlock, e->smem_drift, e->stream>>>(e->sp);
   CR_CUDA(cudaGetLastError());
-  int rc = split_forces(e, e->d_V, e->d_f);
+  int rc;
+  if (e->parent && (rc = parent_kernel(e, 0))) return rc;  // SHAKE (src/verlet.f90:746-757)
+  rc = split_forces(e, e->d_V, e->d_f);
   if (rc) return rc;
-  cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp);
-  CR_CUDA(cudaGetLastError());
-  if (nhc) {
-    cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+  if (e->parent) {
+    // 1/2 kick, RATTLE (src/verlet.f90:1080-1082), NHC, then Andersen / PILE
+    cr::split_kick_kernel<<<grid, cr::kSplitBlock, 0, e->stream>>>(e->sp, 1);
     CR_CUDA(cudaGetLastError());
+    if ((rc = parent_kernel(e, 1))) return rc;
+    if (nhc) {
+      cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      CR_CUDA(cudaGetLastError());
+    }
+    if (e->cfg.thermostat == CR_THERMO_ANDERSEN || e->cfg.thermostat == CR_THERMO_PILE) {
+      cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp, 2);
+      CR_CUDA(cudaGetLastError());
+    }
+  } else {
+    cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp, 0);
+    CR_CUDA(cudaGetLastError());
+    if (nhc) {
+      cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      CR_CUDA(cudaGetLastError());
+    }
   }
   cr::split_finish_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
   CR_CUDA(cudaGetLastError());
@@ -378,14 +442,15 @@ int split_run(cr_engine* e, int nsteps) {
     CR_CUDA(cudaFuncSetAttribute(cr::split_kick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)e->smem_kick));
     // the force kernels set their shared-memory limits outside the capture
-    int rc = e->evb ? evb_launch(e->evb, e->d_q, 0, e->d_V, e->d_f, e->d_V2, e->d_f2, e->cfg.precision, e->stream)
-                    : qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
+    int rc = CR_OK;
+    if (e->evb) rc = evb_launch(e->evb, e->d_q, 0, e->d_V, e->d_f, e->d_V2, e->d_f2, e->cfg.precision, e->stream);
+    else if (e->ff) rc = qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
     if (rc) return rc;
     // let the autotuner pick the force-kernel variant on this batch before it
     // is frozen into the graph; the gradient goes to scratch so f is untouched
     const size_t nall = (size_t)e->T * e->P * e->NC;
     double* scratch = nullptr;
-    if (cudaMalloc(&scratch, nall * sizeof(double)) == cudaSuccess) {
+    if (e->ff && cudaMalloc(&scratch, nall * sizeof(double)) == cudaSuccess) {
       rc = split_forces(e, e->d_V, scratch);
       cudaStreamSynchronize(e->stream);
       cudaFree(scratch);
@@ -401,6 +466,9 @@ int split_run(cr_engine* e, int nsteps) {
     }
     if (ce != cudaSuccess) return fail(CR_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ce));
     e->graph = g;
+    size_t nodes = 0;
+    CR_CUDA(cudaGraphGetNodes(e->graph, nullptr, &nodes));
+    e->step_launches = (int)nodes;
     CR_CUDA(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
   }
   e->h_istep = e->istep;
@@ -729,7 +797,9 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
     sig[(size_t)i] = (cfg->beta > 0.0 && std::isfinite(cfg->beta)) ? std::sqrt(e->mass[i] / (cfg->beta / e->P)) : 0.0;
   }
 
-  if (e->split) {
+  {
+    // graph-path parameters: always set up (a constrained parent of an
+    // analytic surface also steps through the graph path)
     cr::SplitParams& s = e->sp;
     s.M = pd.M;
     s.split = pd.split;
@@ -776,12 +846,15 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
     const int cw = cr::split_chunk(e->P), sp1 = e->P + 1;
     e->smem_drift = cr::split_smem_doubles(s, pl) * sizeof(double);
     e->smem_kick = pl ? ((size_t)3 * cw * sp1 + 2 * (size_t)e->P) * sizeof(double) : 0;
-    if (e->smem_drift > 200 * 1024) return cleanup_fail(fail(CR_ERR_UNSUPPORTED, "bead count too large for the split path"));
-    e->block = cr::kSplitBlock;
-    e->grid = ((e->NC + cw - 1) / cw) * e->T;
-    e->smem = e->smem_drift;
-    *out = e;
-    return CR_OK;
+    if (e->split && e->smem_drift > 200 * 1024)
+      return cleanup_fail(fail(CR_ERR_UNSUPPORTED, "bead count too large for the split path"));
+    if (e->split) {
+      e->block = cr::kSplitBlock;
+      e->grid = ((e->NC + cw - 1) / cw) * e->T;
+      e->smem = e->smem_drift;
+      *out = e;
+      return CR_OK;
+    }
   }
   if (N > cr::kMaxAtoms) return cleanup_fail(fail(CR_ERR_UNSUPPORTED, "too many atoms for the persistent kernel"));
 
@@ -859,6 +932,9 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_vnh);
   cudaFree(e->d_V2);
   cudaFree(e->d_f2);
+  cudaFree(e->d_dxi);
+  cudaFree(e->d_cq);
+  cudaFree(e->d_shake_fail);
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   if (e->ev0) cudaEventDestroy(e->ev0);
@@ -978,7 +1054,7 @@ static int engine_run_async(cr_engine* e, int nsteps) {
   if (rc) return rc;
   CR_CUDA(cudaEventRecord(e->ev1, e->stream));
   e->istep += nsteps;
-  e->launches = e->split ? (e->cfg.thermostat == CR_THERMO_NHC ? 7 : 5) * nsteps : 1;
+  e->launches = e->split ? e->step_launches * nsteps : 1;
   return CR_OK;
 }
 
@@ -1054,14 +1130,13 @@ int cr_host_free(void* ptr) {
   return CR_OK;
 }
 
-int cr_engine_set_recross(cr_engine* e, const cr_recross* rc, int max_steps) {
-  if (!e || !rc) return fail(CR_ERR_ARG, "NULL argument");
-  if (max_steps < 1) return fail(CR_ERR_ARG, "max_steps must be >= 1");
-  if (e->split) return fail(CR_ERR_UNSUPPORTED, "recrossing children are built for the analytic surfaces only");
+}  // extern "C"
+
+// BIMOLEC reaction coordinate of a cr_recross definition (1-based atoms).
+static int make_xidev(const cr_engine* e, const cr_recross* rc, cr::XiDev& x) {
   auto bad_atom = [&](int a) { return a < 1 || a > e->N; };
   if (rc->nreac1 < 1 || rc->nreac1 > 8 || rc->nreac2 < 1 || rc->nreac2 > 8)
     return fail(CR_ERR_ARG, "reactants need 1..8 atoms each");
-  cr::XiDev x{};
   x.nreac1 = rc->nreac1;
   x.nreac2 = rc->nreac2;
   x.mreac1 = 0.0;
@@ -1087,6 +1162,53 @@ int cr_engine_set_recross(cr_engine* e, const cr_recross* rc, int max_steps) {
   x.break_ref = rc->break_ref;
   x.r_inf = rc->r_inf;
   x.xi_ideal = rc->xi_ideal;
+  return CR_OK;
+}
+
+extern "C" {
+
+int cr_engine_set_parent(cr_engine* e, const cr_recross* rc) {
+  if (!e || !rc) return fail(CR_ERR_ARG, "NULL argument");
+  if (e->ff || e->evb) return fail(CR_ERR_UNSUPPORTED, "constrained parents are built for the analytic surfaces");
+  if (e->xi_on) return fail(CR_ERR_ARG, "a recrossing-children engine cannot be a parent");
+  cr::XiDev x{};
+  int rcode = make_xidev(e, rc, x);
+  if (rcode) return rcode;
+  if (!e->d_dxi) {
+    CR_CUDA(cudaMalloc(&e->d_dxi, (size_t)e->T * e->NC * sizeof(double)));
+    CR_CUDA(cudaMalloc(&e->d_cq, (size_t)e->T * e->NC * sizeof(double)));
+    CR_CUDA(cudaMalloc(&e->d_shake_fail, (size_t)e->T * sizeof(int)));
+  }
+  e->parent = true;
+  e->split = true;
+  e->sp.constrain = 1;
+  e->sp.xi = x;
+  e->sp.transrot = 0;  // verlet calls transrot only for constrain <= 0
+  e->sp.dxi = e->d_dxi;
+  e->sp.cq = e->d_cq;
+  e->sp.shake_fail = e->d_shake_fail;
+  if (e->graph_exec) {
+    cudaGraphExecDestroy(e->graph_exec);
+    e->graph_exec = nullptr;
+  }
+  if (e->graph) {
+    cudaGraphDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  rcode = parent_kernel(e, 2);
+  if (rcode) return rcode;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_set_recross(cr_engine* e, const cr_recross* rc, int max_steps) {
+  if (!e || !rc) return fail(CR_ERR_ARG, "NULL argument");
+  if (max_steps < 1) return fail(CR_ERR_ARG, "max_steps must be >= 1");
+  if (e->split) return fail(CR_ERR_UNSUPPORTED, "recrossing children are built for the analytic surfaces only");
+  cr::XiDev x{};
+  int rcode = make_xidev(e, rc, x);
+  if (rcode) return rcode;
+
   cudaFree(e->d_side);
   cudaFree(e->d_w);
   cudaFree(e->d_kappa);

@@ -56,6 +56,12 @@ struct SplitParams {
   int* istep;              // device step counter (last completed step)
   NhcParams nhc;
   double* vnh;             // [T][4] Nose-Hoover chain velocities
+  // constrained parent (verlet with constrain = 1)
+  int constrain;
+  XiDev xi;
+  double* dxi;             // [T][NC] dxi_act
+  double* cq;              // [T][NC] centroid before SHAKE
+  int* shake_fail;         // [T]
 };
 
 constexpr int kSplitBlock = 128;
@@ -71,6 +77,25 @@ __host__ __device__ inline size_t split_smem_doubles(const SplitParams& s, bool 
   n += (size_t)2 * cw * (s.su + s.sv);                 // u, v (q and p)
   if (pile) n += (size_t)2 * cw * sp + 2 * (size_t)s.P;  // eta, tmp, circulants
   return n;
+}
+
+// Deterministic block sum of NV values per thread (fixed tree); red holds
+// NV * blockDim.x doubles.  The result is returned on every thread.
+template <int NV>
+__device__ inline void block_sum(double (&v)[NV], double* red) {
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < NV; ++i) red[i * blockDim.x + threadIdx.x] = v[i];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w >= 1; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) red[i * blockDim.x + threadIdx.x] += red[i * blockDim.x + threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = red[i * blockDim.x];
 }
 
 // Normals of coordinates [c0, c0+cw) of every bead into eta[c][j] (row stride sp).
@@ -236,7 +261,9 @@ __global__ void __launch_bounds__(kSplitBlock) split_drift_kernel(SplitParams s)
   }
 }
 
-__global__ void __launch_bounds__(kSplitBlock) split_kick_kernel(SplitParams s) {
+// mode 0: 1/2 kick and thermostat; 1: 1/2 kick only; 2: thermostat only (the
+// constrained parent runs RATTLE between the two).
+__global__ void __launch_bounds__(kSplitBlock) split_kick_kernel(SplitParams s, int mode) {
   extern __shared__ double sm[];
   const int P = s.P, NC = s.NC, cw_max = split_chunk(P), sp = P + 1;
   const int t = blockIdx.y, c0 = blockIdx.x * cw_max;
@@ -244,6 +271,15 @@ __global__ void __launch_bounds__(kSplitBlock) split_kick_kernel(SplitParams s) 
   const int istep = *s.istep + 1;
   const size_t tb = (size_t)t * P * NC + c0;
   const uint32_t traj = s.traj0 + (uint32_t)t;
+  const double hdt = mode == 2 ? 0.0 : s.half_dt;
+  if (mode == 1) {
+    for (int idx = threadIdx.x; idx < P * cw; idx += blockDim.x) {
+      const int c = idx % cw, j = idx / cw;
+      const size_t g = tb + (size_t)j * NC + c;
+      s.p[g] = s.p[g] - s.half_dt * s.f[g];
+    }
+    return;
+  }
   if (s.thermostat == CR_THERMO_PILE) {
     double* xp = sm;
     double* eta = xp + cw_max * sp;
@@ -254,7 +290,7 @@ __global__ void __launch_bounds__(kSplitBlock) split_kick_kernel(SplitParams s) 
     for (int idx = threadIdx.x; idx < P * cw; idx += blockDim.x) {
       const int c = idx % cw, j = idx / cw;
       const size_t g = tb + (size_t)j * NC + c;
-      xp[c * sp + j] = s.p[g] - s.half_dt * s.f[g];
+      xp[c * sp + j] = s.p[g] - hdt * s.f[g];
     }
     __syncthreads();
     chunk_pile(s, traj, (uint32_t)istep, TAG_PILE_B, c0, cw, xp, eta, tmp, sa, sb, sp);
@@ -277,6 +313,7 @@ __global__ void __launch_bounds__(kSplitBlock) split_kick_kernel(SplitParams s) 
     }
     return;
   }
+  if (mode == 2) return;
   for (int idx = threadIdx.x; idx < P * cw; idx += blockDim.x) {
     const int c = idx % cw, j = idx / cw;
     const size_t g = tb + (size_t)j * NC + c;
@@ -284,23 +321,104 @@ __global__ void __launch_bounds__(kSplitBlock) split_kick_kernel(SplitParams s) 
   }
 }
 
-// Deterministic block sum of NV values per thread (fixed tree); red holds
-// NV * blockDim.x doubles.  The result is returned on every thread.
-template <int NV>
-__device__ inline void block_sum(double (&v)[NV], double* red) {
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < NV; ++i) red[i * blockDim.x + threadIdx.x] = v[i];
-  __syncthreads();
-  for (int w = blockDim.x / 2; w >= 1; w >>= 1) {
-    if ((int)threadIdx.x < w) {
-#pragma unroll
-      for (int i = 0; i < NV; ++i) red[i * blockDim.x + threadIdx.x] += red[i * blockDim.x + threadIdx.x + w];
-    }
-    __syncthreads();
+// ---- constrained parent (src/constrain_q.f90, src/constrain_p.f90) ----------
+// One block per trajectory.  SHAKE: the centroid c (kept for the next dxi),
+// Newton iterations for the multiplier on thread 0 (at most 200; the
+// tolerances 1.0E-8 and 1.0E-10 are REAL(4) literals), then every bead moves:
+// q by the coefficient of the last iteration's start, p by the updated
+// multiplier.  A failed SHAKE leaves q, p unchanged and is flagged.
+template <int N>
+__global__ void split_shake_kernel(SplitParams s) {
+  constexpr int NC = 3 * N;
+  __shared__ double cq[NC], dxa[NC], res[3];
+  const int t = blockIdx.x, P = s.P;
+  const size_t tb = (size_t)t * P * NC;
+  for (int c = threadIdx.x; c < NC; c += blockDim.x) {
+    double acc = 0.0;
+    for (int k = 0; k < P; ++k) acc = acc + s.q[tb + (size_t)k * NC + c];
+    cq[c] = acc / P;
+    dxa[c] = s.dxi[(size_t)t * NC + c];
+    s.cq[(size_t)t * NC + c] = cq[c];
   }
-#pragma unroll
-  for (int i = 0; i < NV; ++i) v[i] = red[i * blockDim.x];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double dt = 2.0 * s.half_dt;
+    double mult = 0.0, coeff = 0.0, qt[NC], dxn[NC];
+    int ok = 0;
+    for (int iter = 1; iter <= 200; ++iter) {
+      coeff = mult * dt * dt / P;
+      for (int c = 0; c < NC; ++c) qt[c] = cq[c] + coeff * dxa[c] / s.mass[c / 3];
+      const double sigma = xi_bimolec<N>(s.xi, qt, s.mass, dxn);
+      double dsigma = 0.0;
+      for (int c = 0; c < NC; ++c) dsigma = dsigma + dxn[c] * dt * dt * dxa[c] / (s.mass[c / 3] * P);
+      const double dx = sigma / dsigma;
+      mult = mult - dx;
+      if (fabs(dx) < (double)1.0E-8f || fabs(sigma) < (double)1.0E-10f) {
+        ok = 1;
+        break;
+      }
+    }
+    res[0] = coeff;
+    res[1] = mult;
+    res[2] = ok;
+    s.shake_fail[t] = ok ? 0 : 1;
+  }
+  __syncthreads();
+  if (res[2] == 0.0) return;
+  const double coeff = res[0], mult = res[1], dt = 2.0 * s.half_dt;
+  for (int idx = threadIdx.x; idx < P * NC; idx += blockDim.x) {
+    const int c = idx % NC;
+    const double m = s.mass[c / 3];
+    s.q[tb + idx] = s.q[tb + idx] + coeff / m * dxa[c];
+    s.p[tb + idx] = s.p[tb + idx] + mult * dt / P * dxa[c];
+  }
+}
+
+// dxi_act <- dxi at the pre-SHAKE centroid (umbrella mode 1, src/verlet.f90:
+// 1047-1049), then RATTLE: p -= (sum dxi.p/m) / (sum dxi^2/m) / P * dxi.
+template <int N>
+__global__ void split_rattle_kernel(SplitParams s) {
+  constexpr int NC = 3 * N;
+  __shared__ double dxa[NC], red[kFinishBlock];
+  const int t = blockIdx.x, P = s.P;
+  const size_t tb = (size_t)t * P * NC;
+  if (threadIdx.x == 0) {
+    double cq[NC], d[NC];
+    for (int c = 0; c < NC; ++c) cq[c] = s.cq[(size_t)t * NC + c];
+    xi_bimolec<N>(s.xi, cq, s.mass, d);
+    for (int c = 0; c < NC; ++c) {
+      dxa[c] = d[c];
+      s.dxi[(size_t)t * NC + c] = d[c];
+    }
+  }
+  __syncthreads();
+  double c1[1] = {0.0};
+  for (int idx = threadIdx.x; idx < P * NC; idx += blockDim.x) {
+    const int c = idx % NC;
+    c1[0] = c1[0] + dxa[c] * s.p[tb + idx] / s.mass[c / 3];
+  }
+  block_sum<1>(c1, red);
+  double c2 = 0.0;
+  for (int c = 0; c < NC; ++c) c2 = c2 + dxa[c] * dxa[c] / s.mass[c / 3];
+  const double lambdas = -c1[0] / c2 / P;
+  for (int idx = threadIdx.x; idx < P * NC; idx += blockDim.x) s.p[tb + idx] = s.p[tb + idx] + lambdas * dxa[idx % NC];
+}
+
+// initial dxi_act of each parent at its current centroid
+template <int N>
+__global__ void split_parent_init_kernel(SplitParams s) {
+  constexpr int NC = 3 * N;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.T) return;
+  double cq[NC], d[NC];
+  for (int c = 0; c < NC; ++c) {
+    double acc = 0.0;
+    for (int k = 0; k < s.P; ++k) acc = acc + s.q[((size_t)t * s.P + k) * NC + c];
+    cq[c] = acc / s.P;
+  }
+  xi_bimolec<N>(s.xi, cq, s.mass, d);
+  for (int c = 0; c < NC; ++c) s.dxi[(size_t)t * NC + c] = d[c];
+  s.shake_fail[t] = 0;
 }
 
 // NaN check (src/verlet.f90:1256-1275), transrot (src/transrot.f90:36-237,
@@ -334,7 +452,8 @@ __global__ void __launch_bounds__(kFinishBlock) split_finish_kernel(SplitParams 
   if (status) atomicOr(&sstat, status);
   __syncthreads();
   status = sstat;
-  if (threadIdx.x == 0) s.epot[t] = s1[6];
+  if (s.constrain && s.shake_fail[t]) status |= CR_TRAJ_SHAKE_FAILED;
+  if (threadIdx.x == 0) s.epot[t] = s1[6] + ((s.constrain && s.shake_fail[t]) ? 100000.0 : 0.0);
   if (s.transrot) {
     const double itm = 1.0 / s.totmass;
     const double vt[3] = {s1[0] * itm, s1[1] * itm, s1[2] * itm};

@@ -304,6 +304,25 @@ class RPMDEngine:
         ep = L.dptr(epot) if epot is not None else None
         L.check(L.lib().cr_engine_step_host(self._h, L.dptr(q), L.dptr(p), L.dptr(f), ep), "step_host")
 
+    @staticmethod
+    def _recross_def(reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf, xi_ideal):
+        rc = L.CrRecross()
+        rc.nreac1, rc.nreac2 = len(reac1), len(reac2)
+        for i, a in enumerate(reac1):
+            rc.reac1[i] = a
+        for i, a in enumerate(reac2):
+            rc.reac2[i] = a
+        rc.bond_form[0], rc.bond_form[1] = bond_form
+        rc.bond_break[0], rc.bond_break[1] = bond_break
+        rc.form_ref, rc.break_ref, rc.r_inf, rc.xi_ideal = form_ref, break_ref, r_inf, xi_ideal
+        return rc
+
+    def set_parent(self, reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf, xi_ideal=1.0):
+        """Constrained parent (SHAKE/RATTLE on xi = 0 of the BIMOLEC coordinate;
+        1-based atoms as in Caracal's MECHA block); call after the initial state."""
+        rc = self._recross_def(reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf, xi_ideal)
+        L.check(L.lib().cr_engine_set_parent(self._h, C.byref(rc)), "set_parent")
+
     def set_recross(self, reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf,
                     xi_ideal=1.0, max_steps=1):
         """BIMOLEC recrossing bookkeeping; atom indices 1-based as in Caracal's MECHA block."""

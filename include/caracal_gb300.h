@@ -33,6 +33,7 @@ extern "C" {
 /* per-trajectory status bits (cr_engine_get_state) */
 #define CR_TRAJ_NONFINITE 1        /* a coordinate became NaN/Inf (src/verlet.f90:1256-1275) */
 #define CR_TRAJ_SINGULAR_INERTIA 2 /* transrot could not invert the inertia tensor */
+#define CR_TRAJ_SHAKE_FAILED 4     /* constrained parent: SHAKE did not converge (src/verlet.f90:751-756) */
 
 /* ---- potentials (Caracal keyword PES) ----------------------------------- */
 #define CR_PES_H3 1      /* ANA_H3: BKMP2, src/egrad_h3.f */
@@ -266,6 +267,15 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent);
 /* num[nsteps] and denom summed over the engine's children (deterministic
  * order); weights (may be NULL) gets vs/fs per child. */
 int cr_engine_kappa(cr_engine* e, double* num, double* denom, double* weights, int* nsteps);
+
+/* Constrained parent trajectories (calc_rate part 3, src/recross.f90:240-290:
+ * verlet with constrain = 1): after each free ring-polymer step SHAKE moves
+ * the centroid onto xi = 0 of the BIMOLEC coordinate rc (src/constrain_q.f90),
+ * after the second half kick RATTLE removes the momentum along dxi
+ * (src/constrain_p.f90); no transrot.  Call once after the initial state is
+ * set (dxi starts at the current centroid); the engine then steps through its
+ * kernel-graph path.  Analytic surfaces only. */
+int cr_engine_set_parent(cr_engine* e, const cr_recross* rc);
 
 /* Device time of the last cr_engine_run / step kernel (CUDA events on the
  * engine's stream), launches issued by it, and the launch shape chosen. */

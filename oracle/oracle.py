@@ -156,6 +156,8 @@ def lib():
         _lib.orc_qmdff_set2.argtypes = [C.POINTER(QmdffDef)]
         _lib.orc_evb_set.argtypes = [C.c_int, d]
         _lib.orc_nhc_half.argtypes = [C.POINTER(Cfg), d, d]
+        _lib.orc_run_parent.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, C.c_int, C.c_int,
+                                        d, d, d, d, C.POINTER(C.c_int), d, d]
         _lib.orc_calc_xi.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d]
         _lib.orc_calc_xi.restype = C.c_double
         _lib.orc_recross_children.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, d,
@@ -321,3 +323,22 @@ def nhc_half(cfg: Config, vnh, p):
     pp = np.array(p, dtype=np.float64)
     lib().orc_nhc_half(C.byref(cfg.c), _dp(v), _dp(pp))
     return v, pp
+
+
+def run_parent(cfg: Config, xd, q, p, f, nsteps, istep0=0, traj0=0, dxi=None, vnh=None):
+    """Constrained parent trajectories (SHAKE/RATTLE on xi = 0): returns
+    (q, p, f, epot, status, dxi); dxi is the dxi_act state (zeros: start from
+    the current centroid)."""
+    q = np.array(q, dtype=np.float64)
+    p = np.array(p, dtype=np.float64)
+    f = np.array(f, dtype=np.float64)
+    T = q.shape[0]
+    e = np.zeros(T)
+    st = np.zeros(T, dtype=np.int32)
+    dxi = np.zeros((T, cfg.natoms * 3)) if dxi is None else np.array(dxi, dtype=np.float64)
+    if cfg.thermostat == 2 and vnh is None:
+        vnh = np.zeros((T, 4))
+    vp = _dp(vnh) if vnh is not None else None
+    lib().orc_run_parent(C.byref(cfg.c), C.byref(xd), T, traj0, istep0, nsteps, _dp(q), _dp(p), _dp(f), _dp(e),
+                         st.ctypes.data_as(C.POINTER(C.c_int)), _dp(dxi), vp)
+    return q, p, f, e, st, dxi

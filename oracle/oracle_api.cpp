@@ -222,6 +222,35 @@ static orc::XiDef to_xi(const orc_xidef* x) {
   return d;
 }
 
+int orc_run_parent(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t traj0, int istep0, int nsteps,
+                   double* q, double* p, double* f, double* epot, int* status, double* dxi, double* vnh) {
+  if (cf->thermostat == 2 && !vnh) return -1;
+  orc::StepConfig s = to_step(cf);
+  s.transrot = 0;
+  const orc::XiDef x = to_xi(xd);
+  BeadPES pes{cf->pes, cf->natoms};
+  const int n3 = 3 * cf->natoms;
+  const size_t per = (size_t)n3 * cf->nbeads;
+  for (int t = 0; t < ntraj; ++t) {
+    double* d = &dxi[(size_t)t * n3];
+    bool zero = true;
+    for (int k = 0; k < n3; ++k) zero = zero && d[k] == 0.0;
+    if (zero) {
+      std::vector<double> c(n3);
+      orc::centroid(cf->natoms, cf->nbeads, &q[t * per], c.data());
+      orc::calc_xi_mode2(x, cf->natoms, c.data(), cf->mass, d);
+    }
+    int st = 0;
+    double e = 0.0;
+    for (int n = 1; n <= nsteps; ++n)
+      st |= orc::parent_step(s, x, traj0 + t, istep0 + n, &q[t * per], &p[t * per], &f[t * per], &e, d, pes,
+                             vnh ? &vnh[4 * (size_t)t] : nullptr);
+    if (epot) epot[t] = e;
+    if (status) status[t] |= st;
+  }
+  return 0;
+}
+
 double orc_calc_xi(const orc_xidef* xd, int natoms, const double* coords, const double* mass,
                    double* dxi) {
   return orc::calc_xi_mode2(to_xi(xd), natoms, coords, mass, dxi);

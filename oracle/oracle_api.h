@@ -101,6 +101,13 @@ int orc_recross_children(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint
                          const double* q_parent, int nsteps, double* num, double* denom,
                          double* w_out, double* q_out, double* p_out, int nthreads);
 
+/* nsteps steps of ntraj constrained parent trajectories (verlet with
+ * constrain = 1: SHAKE/RATTLE on the xi(centroid) = 0 surface, no transrot);
+ * dxi[ntraj * 3 * natoms] in/out is each parent's dxi_act (zeros: computed
+ * from the current centroid first).  status bit 4: SHAKE did not converge. */
+int orc_run_parent(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t traj0, int istep0, int nsteps,
+                   double* q, double* p, double* f, double* epot, int* status, double* dxi, double* vnh);
+
 /* algorithmic operation tallies (add, mul, div, sqrt, exp, log, pow, sin, cos,
  * acos, erf, cmp, tanh, cosh) of one PES evaluation of one bead at geometry q. */
 void orc_pes_opcount(int pes, const double* q, uint64_t out[14]);

@@ -12,6 +12,9 @@
 // m / P, fs = sqrt(sum dxi^2 / m / (2 pi beta)), denominator += vs/fs if
 // vs > 0; then child_evol NVE steps (no thermostat, no transrot: verlet with
 // constrain = 2), numerator(t) += vs/fs whenever xi(centroid) > 0 after step t.
+// The parent trajectory (verlet with constrain = 1) is kept on the dividing
+// surface by SHAKE on the centroid (constrain_q, src/constrain_q.f90:35-113)
+// and RATTLE on the momenta (constrain_p, src/constrain_p.f90:36-76).
 #pragma once
 #include <cmath>
 #include <vector>
@@ -126,6 +129,97 @@ inline double recross_child(const StepConfig& cf, const XiDef& xd, uint32_t traj
     side[s - 1] = calc_xi_mode2(xd, N, c.data(), cf.mass, nullptr) > 0.0 ? 1 : 0;
   }
   return vs / fs;
+}
+
+// constrain_q (src/constrain_q.f90:35-113): Newton iterations (at most 200)
+// for the multiplier that moves the centroid c along dxi_act onto xi = 0,
+// then every bead is shifted.  As in the reference, q moves by the
+// coefficient of the last iteration's start and p by the updated multiplier.
+// Returns false when the iterations do not converge (q, p unchanged).
+inline bool constrain_q(const StepConfig& cf, const XiDef& xd, const double* c, const double* dxi_act, double* q,
+                        double* p) {
+  const int N = cf.natoms, P = cf.nbeads, nc = 3 * N;
+  const double dt = cf.dt;
+  double mult = 0.0, coeff = 0.0;
+  std::vector<double> qt(nc), dxn(nc);
+  const int maxiters = 200;
+  for (int iter = 1; iter <= maxiters; ++iter) {
+    coeff = mult * dt * dt / P;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < N; ++j) qt[3 * j + i] = c[3 * j + i] + coeff * dxi_act[3 * j + i] / cf.mass[j];
+    const double sigma = calc_xi_mode2(xd, N, qt.data(), cf.mass, dxn.data());
+    double dsigma = 0.0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < N; ++j)
+        dsigma = dsigma + dxn[3 * j + i] * dt * dt * dxi_act[3 * j + i] / (cf.mass[j] * P);
+    const double dx = sigma / dsigma;
+    mult = mult - dx;
+    if (std::fabs(dx) < (double)1.0E-8f || std::fabs(sigma) < (double)1.0E-10f) break;
+    if (iter == maxiters) return false;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < P; ++k) {
+        q[(size_t)k * nc + 3 * j + i] = q[(size_t)k * nc + 3 * j + i] + coeff / cf.mass[j] * dxi_act[3 * j + i];
+        p[(size_t)k * nc + 3 * j + i] = p[(size_t)k * nc + 3 * j + i] + mult * dt / P * dxi_act[3 * j + i];
+      }
+  return true;
+}
+
+// constrain_p (src/constrain_p.f90:36-76): removes the momentum along dxi_act.
+inline void constrain_p(const StepConfig& cf, const double* dxi_act, double* p) {
+  const int N = cf.natoms, P = cf.nbeads, nc = 3 * N;
+  double coeff1 = 0.0, coeff2 = 0.0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < P; ++k) coeff1 = coeff1 + dxi_act[3 * j + i] * p[(size_t)k * nc + 3 * j + i] / cf.mass[j];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < N; ++j) coeff2 = coeff2 + dxi_act[3 * j + i] * dxi_act[3 * j + i] / cf.mass[j];
+  const double lambdas = -coeff1 / coeff2 / P;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < P; ++k) p[(size_t)k * nc + 3 * j + i] = p[(size_t)k * nc + 3 * j + i] + lambdas * dxi_act[3 * j + i];
+}
+
+enum ParentStatus : int { TRAJ_SHAKE_FAILED = 4 };
+
+// One step of the constrained parent (verlet with constrain = 1): thermostat
+// as configured, no transrot; dxi_act carries dxi at the previous step's
+// centroid taken before its SHAKE (src/verlet.f90:649, 746-757, 1043-1049,
+// 1080-1082).  A failed SHAKE sets TRAJ_SHAKE_FAILED and, like the
+// reference, gives the step the 1e5 energy penalty.
+template <class EGrad>
+inline int parent_step(const StepConfig& cf, const XiDef& xd, uint32_t traj, int istep, double* q, double* p,
+                       double* f, double* epot, double* dxi_act, EGrad egrad, double* vnh = nullptr) {
+  const int N = cf.natoms, P = cf.nbeads, n3 = 3 * N;
+  const size_t nall = (size_t)n3 * P;
+  if (cf.thermostat == 2) nhc_half(cf, vnh, p);
+  if (cf.thermostat == 3) pile_half(cf, traj, (uint32_t)istep, TAG_PILE_A, p);
+  for (size_t x = 0; x < nall; ++x) p[x] = p[x] - 0.5 * cf.dt * f[x];
+  free_rp_step(cf, q, p);
+  std::vector<double> c(n3);
+  centroid(N, P, q, c.data());
+  int status = TRAJ_OK;
+  double e = 0.0;
+  if (!constrain_q(cf, xd, c.data(), dxi_act, q, p)) {
+    status |= TRAJ_SHAKE_FAILED;
+    e = 100000.0;
+  }
+  for (int k = 0; k < P; ++k) {
+    double v;
+    egrad(&q[(size_t)k * n3], &v, &f[(size_t)k * n3]);
+    e = e + v;
+  }
+  *epot = e;
+  calc_xi_mode2(xd, N, c.data(), cf.mass, dxi_act);
+  for (size_t x = 0; x < nall; ++x) p[x] = p[x] - 0.5 * cf.dt * f[x];
+  constrain_p(cf, dxi_act, p);
+  if (cf.thermostat == 2) nhc_half(cf, vnh, p);
+  if (cf.thermostat == 1 && istep % cf.andersen_step == 0) andersen(cf, traj, (uint32_t)istep, TAG_ANDERSEN, p);
+  if (cf.thermostat == 3) pile_half(cf, traj, (uint32_t)istep, TAG_PILE_B, p);
+  for (size_t x = 0; x < nall; ++x)
+    if (!std::isfinite(q[x])) status |= TRAJ_NONFINITE;
+  return status;
 }
 
 }  // namespace orc
