@@ -132,6 +132,7 @@ def _sig(lib):
         "cr_evb_destroy": ([v], C.c_int),
         "cr_evb_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
         "cr_engine_create_evb": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
+        "cr_evb_fit": ([C.c_int, d, C.c_int, C.c_int, d, d, d, d, d], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

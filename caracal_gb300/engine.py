@@ -200,6 +200,23 @@ class EVBPair:
             pass
 
 
+FIT_BASES = {"1g": 1, "2g": 2, "3g": 3, "sp": 4, "sd": 5, "sd2": 6, "sp2d": 7, "sp2d3": 8}
+
+
+def evb_fit(basis, x, e1, e2, eref, jacobian=True):
+    """Residuals of Caracal's dE-EVB coupling fit (lm_de_func) at parameters x
+    and, optionally, MINPACK's forward-difference Jacobian (fdjac2), shape
+    (npar, m); computed on the device."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    e1, e2, eref = (np.ascontiguousarray(a, dtype=np.float64) for a in (e1, e2, eref))
+    m = len(e1)
+    fvec = np.zeros(m)
+    fjac = np.zeros((len(x), m)) if jacobian else None
+    L.check(L.lib().cr_evb_fit(FIT_BASES[basis], L.dptr(x), len(x), m, L.dptr(e1), L.dptr(e2), L.dptr(eref),
+                               L.dptr(fvec), L.dptr(fjac) if jacobian else None), "cr_evb_fit")
+    return (fvec, fjac) if jacobian else fvec
+
+
 class RPMDEngine:
     """A batch of independent RPMD trajectories resident on one GPU.
 

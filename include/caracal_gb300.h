@@ -201,6 +201,25 @@ int cr_evb_destroy(cr_evb* evb);
 /* Host arrays xyz(3,natoms,nbeads) -> e(nbeads), g(3,natoms,nbeads). */
 int cr_evb_egrad(cr_evb* evb, const double* xyz, int nbeads, double* e, double* g, int precision);
 
+/* dE-EVB coupling fit (Caracal's EVB optimisation, src/optimize_de.f90 with
+ * lm_de_func src/lm_de_func.f90:35-181): for m reference points with QMDFF
+ * energies e1, e2 (E_zero included) and reference energies eref,
+ * fvec[i] = (eref_i - E_EVB,i(x))^2 with dE = |e1 - e2|, and, if fjac is not
+ * NULL, MINPACK's forward-difference Jacobian fdjac2 (src/lm_good.f:795-840,
+ * epsfcn = 0) as fjac[j * m + i] = d fvec_i / d x_j.  Parameters x per basis:
+ * 1g a b | 2g a b c d m | 3g a b c d e f m n | sp, sd a b c d | sd2 a b c d e f |
+ * sp2d a .. h | sp2d3 a .. l. */
+#define CR_FIT_1G 1
+#define CR_FIT_2G 2
+#define CR_FIT_3G 3
+#define CR_FIT_SP 4
+#define CR_FIT_SD 5
+#define CR_FIT_SD2 6
+#define CR_FIT_SP2D 7
+#define CR_FIT_SP2D3 8
+int cr_evb_fit(int basis, const double* x, int npar, int m, const double* e1, const double* e2, const double* eref,
+               double* fvec, double* fjac);
+
 /* ---- RPMD engine -----------------------------------------------------------
  * Replaces the stepping loop of `dynamic` (src/dynamic.f90:1569-1579) around
  * `verlet` (src/verlet.f90:65) and the initialisation of `mdinit`

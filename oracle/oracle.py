@@ -156,6 +156,7 @@ def lib():
         _lib.orc_qmdff_set2.argtypes = [C.POINTER(QmdffDef)]
         _lib.orc_evb_set.argtypes = [C.c_int, d]
         _lib.orc_nhc_half.argtypes = [C.POINTER(Cfg), d, d]
+        _lib.orc_evb_fit.argtypes = [C.c_int, d, C.c_int, C.c_int, d, d, d, d, d]
         _lib.orc_run_parent.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, C.c_int, C.c_int,
                                         d, d, d, d, C.POINTER(C.c_int), d, d]
         _lib.orc_calc_xi.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d]
@@ -342,3 +343,18 @@ def run_parent(cfg: Config, xd, q, p, f, nsteps, istep0=0, traj0=0, dxi=None, vn
     lib().orc_run_parent(C.byref(cfg.c), C.byref(xd), T, traj0, istep0, nsteps, _dp(q), _dp(p), _dp(f), _dp(e),
                          st.ctypes.data_as(C.POINTER(C.c_int)), _dp(dxi), vp)
     return q, p, f, e, st, dxi
+
+
+FIT_BASES = {"1g": 1, "2g": 2, "3g": 3, "sp": 4, "sd": 5, "sd2": 6, "sp2d": 7, "sp2d3": 8}
+
+
+def evb_fit(basis, x, e1, e2, eref, jacobian=True):
+    """lm_de_func residuals (and fdjac2's Jacobian, shape (npar, m))."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    e1, e2, eref = (np.ascontiguousarray(a, dtype=np.float64) for a in (e1, e2, eref))
+    m = len(e1)
+    fvec = np.zeros(m)
+    fjac = np.zeros((len(x), m)) if jacobian else None
+    lib().orc_evb_fit(FIT_BASES[basis], _dp(x), len(x), m, _dp(e1), _dp(e2), _dp(eref), _dp(fvec),
+                      _dp(fjac) if jacobian else None)
+    return (fvec, fjac) if jacobian else fvec

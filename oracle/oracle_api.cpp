@@ -12,6 +12,7 @@
 #include "pes_ch4h.hpp"
 #include "pes_ch4oh.hpp"
 #include "pes_h3.hpp"
+#include "evb_fit.hpp"
 #include "pes_evb.hpp"
 #include "pes_qmdff.hpp"
 #include "philox.hpp"
@@ -320,6 +321,14 @@ void orc_pes_opcount(int pes, const double* q, uint64_t out[14]) {
   uint64_t v[14] = {t.add, t.mul, t.div,  t.sqrt, t.exp, t.log,  t.pow,
                     t.sin, t.cos, t.acos, t.erf,  t.cmp, t.tanh, t.cosh};
   for (int i = 0; i < 14; ++i) out[i] = v[i];
+}
+
+int orc_evb_fit(int basis, const double* x, int npar, int m, const double* e1, const double* e2,
+                const double* eref, double* fvec, double* fjac) {
+  if (basis < 1 || basis > 8) return -1;
+  orc::evbfit::residual(basis, x, m, e1, e2, eref, fvec);
+  if (fjac) orc::evbfit::fdjac2(basis, std::vector<double>(x, x + npar), m, e1, e2, eref, fvec, 0.0, fjac);
+  return 0;
 }
 
 }  // extern "C"

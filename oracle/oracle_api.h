@@ -108,6 +108,12 @@ int orc_recross_children(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint
 int orc_run_parent(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t traj0, int istep0, int nsteps,
                    double* q, double* p, double* f, double* epot, int* status, double* dxi, double* vnh);
 
+/* dE-EVB coupling fit (src/lm_de_func.f90, src/lm_good.f fdjac2): fvec[m]
+ * and, if fjac is not NULL, the forward-difference Jacobian fjac[npar][m];
+ * basis 1..8 = 1g, 2g, 3g, sp, sd, sd2, sp2d, sp2d3. */
+int orc_evb_fit(int basis, const double* x, int npar, int m, const double* e1, const double* e2,
+                const double* eref, double* fvec, double* fjac);
+
 /* algorithmic operation tallies (add, mul, div, sqrt, exp, log, pow, sin, cos,
  * acos, erf, cmp, tanh, cosh) of one PES evaluation of one bead at geometry q. */
 void orc_pes_opcount(int pes, const double* q, uint64_t out[14]);

@@ -70,3 +70,14 @@ def test_argument_validation_precedes_device_use():
     assert lib.cr_engine_create(C.byref(cfg), C.byref(h)) == L.CR_ERR_ARG   # NVE with P > 1
     cfg = L.CrConfig(99, 3, 16, 1, 0, 70, 1, 0, 1, 0, 1.0, 1.0, 0.0, L.dptr(mass))
     assert lib.cr_engine_create(C.byref(cfg), C.byref(h)) == L.CR_ERR_UNSUPPORTED
+
+
+def test_evb_fit_argument_validation():
+    lib = L.lib()
+    x = np.zeros(4)
+    e = np.zeros(3)
+    f = np.zeros(3)
+    assert lib.cr_evb_fit(9, L.dptr(x), 4, 3, L.dptr(e), L.dptr(e), L.dptr(e), L.dptr(f), None) == L.CR_ERR_ARG
+    assert lib.cr_evb_fit(1, L.dptr(x), 4, 3, L.dptr(e), L.dptr(e), L.dptr(e), L.dptr(f), None) == L.CR_ERR_ARG
+    assert lib.cr_evb_fit(4, L.dptr(x), 4, -1, L.dptr(e), L.dptr(e), L.dptr(e), L.dptr(f), None) == L.CR_ERR_ARG
+    assert lib.cr_evb_fit(4, L.dptr(x), 4, 0, None, None, None, None, None) == 0

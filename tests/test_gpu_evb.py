@@ -68,3 +68,20 @@ def test_evb_engine_matches_oracle(fields):
     pair.close()
     qo, po, fo, eo, _ = orc.run(cfg, q, p, f, 10)
     assert rel_err(q10, qo) <= 1e-9 and rel_err(p10, po) <= 1e-9 and rel_err(e10, eo) <= 1e-9
+
+
+@pytest.mark.parametrize("basis", ["1g", "2g", "3g", "sp", "sd", "sd2", "sp2d", "sp2d3"])
+def test_evb_fit_matches_oracle(require_gpu, basis):
+    from caracal_gb300.engine import evb_fit
+    from test_oracle_evb import FIT, fit_data
+    e1, e2, eref = fit_data(m=4096)
+    fv, fj = evb_fit(basis, FIT[basis], e1, e2, eref)
+    fo, fjo = orc.evb_fit(basis, FIT[basis], e1, e2, eref)
+    assert rel_err(fv, fo) <= 1e-12
+    # forward differences with fdjac2's h = sqrt(eps) |x_j| amplify last-bit
+    # differences of the residuals by 1/h
+    x = np.asarray(FIT[basis])
+    for j in range(len(x)):
+        hj = np.sqrt(np.finfo(float).eps) * abs(x[j])
+        noise = 1e-15 * np.max(np.abs(eref)) ** 2 / hj
+        assert np.max(np.abs(fj[j] - fjo[j])) <= 1e-10 * np.max(np.abs(fjo[j])) + noise

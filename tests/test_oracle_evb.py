@@ -55,3 +55,43 @@ def test_evb_lower_root(pair):
     assert e < min(e1, e2)
     V12 = 0.02 * np.exp(-10.0 * (e1 - e2) ** 2)
     assert abs(e - 0.5 * (e1 + e2 - np.sqrt((e1 - e2) ** 2 + 4 * V12 ** 2))) < 1e-14
+
+
+FIT = {"1g": [0.01, 50.0], "2g": [0.01, 50.0, 0.005, 20.0, 0.01],
+       "3g": [0.01, 50.0, 0.005, 20.0, 0.002, 10.0, 0.01, -0.02], "sp": [0.01, 50.0, 0.02, 30.0],
+       "sd": [0.01, 50.0, 0.2, 30.0], "sd2": [0.01, 50.0, 0.2, 30.0, 0.1, 5.0],
+       "sp2d": [0.01, 50.0, 0.02, 30.0, 0.01, 5.0, 0.3, 40.0],
+       "sp2d3": [0.01, 50.0, 0.02, 30.0, 0.01, 5.0, 0.3, 40.0, 0.1, 8.0, 0.05, 12.0]}
+
+
+def fit_data(m=200, seed=3):
+    rng = np.random.default_rng(seed)
+    e1 = rng.normal(0.0, 0.03, m)
+    e2 = rng.normal(0.01, 0.03, m)
+    eref = np.minimum(e1, e2) - np.abs(rng.normal(0.0, 0.004, m))
+    return e1, e2, eref
+
+
+@pytest.mark.parametrize("basis", list(FIT))
+def test_fit_residual_and_jacobian(basis):
+    e1, e2, eref = fit_data()
+    x = np.array(FIT[basis])
+    fvec, fjac = orc.evb_fit(basis, x, e1, e2, eref)
+    # the residual is the squared deviation from the EVB lower root with |dE|
+    dE = np.abs(e1 - e2)
+    if basis == "1g":
+        v = x[0] * np.exp(-x[1] * dE ** 2)
+        np.testing.assert_allclose(fvec, (eref - 0.5 * (e1 + e2 - np.sqrt(dE ** 2 + 4 * v * v))) ** 2, rtol=1e-12)
+    # fdjac2's forward differences agree with central differences of the residual
+    for j in range(len(x)):
+        h = 1e-6 * max(abs(x[j]), 1e-3)
+        xp, xm = x.copy(), x.copy()
+        xp[j] += h
+        xm[j] -= h
+        cd = (orc.evb_fit(basis, xp, e1, e2, eref, jacobian=False) -
+              orc.evb_fit(basis, xm, e1, e2, eref, jacobian=False)) / (2 * h)
+        # forward differences carry O(h) truncation and rounding noise of
+        # about eps * |E|^2 / h with fdjac2's step h = sqrt(eps) |x_j|
+        hj = np.sqrt(np.finfo(float).eps) * abs(x[j])
+        noise = 1e-15 * np.max(np.abs(eref)) ** 2 / hj
+        assert np.max(np.abs(fjac[j] - cd)) <= 1e-5 * np.max(np.abs(cd)) + noise
