@@ -39,6 +39,8 @@ ALGO_PES_OPS = {
     "h3": {"add": 491, "mul": 738, "div": 82, "sqrt": 5, "exp": 11, "pow": 6},
     "ch4h": {"add": 3839, "mul": 7125, "div": 1812, "sqrt": 135, "exp": 54, "acos": 18, "tanh": 21,
              "cosh": 21},
+    "ch4oh": {"add": 4063, "mul": 7423, "div": 1850, "sqrt": 140, "exp": 72, "pow": 3, "acos": 22,
+              "tanh": 25, "cosh": 25},
     # synthetic C20H42 QMDFF (ff_eg + ff_nonb), thermal geometry (reference
     # geometry + N(0, 0.05 bohr) per coordinate, seed 0); asin counted with acos
     "qmdff": {"add": 92211, "mul": 117770, "div": 20592, "sqrt": 4525, "exp": 1415, "pow": 122,
@@ -208,7 +210,7 @@ def workload(name):
     if name == "qmdff":
         return W.qmdff_config(ntraj=1024, nbeads=64)
     if name == "qmdff_small":
-        return W.qmdff_config(ntraj=64, nbeads=16)
+        return W.qmdff_config(ntraj=512, nbeads=64)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -492,6 +494,196 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def class_list(name):
+    from caracal_gb300 import workloads as W
+    return W.mixed_classes(scale=1 if name == "classes" else 16)
+
+
+def reference_classes(args):
+    """`--impl reference` for the mixed-class workload: each class advanced by
+    the oracle on all host threads for a bounded sample; the rate is the total
+    bead-steps over the summed time (the classes run one after another)."""
+    rank, ws, dist = dist_setup()
+    classes = class_list(args.workload)
+    if rank != 0:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    cores = os.cpu_count()
+    per = max(1, min(args.ref_steps_per_sample // 4, 1000))
+    runs = [OracleRunner(wl) for wl in classes]
+    for _ in range(args.warmup):
+        for r in runs:
+            r.advance(per, cores)
+    el = 0.0
+    for _ in range(args.steps):
+        for r in runs:
+            t0 = time.perf_counter()
+            r.advance(per, cores)
+            el += time.perf_counter() - t0
+    units = sum(wl.ntraj * wl.nbeads for wl in classes) * per * args.steps
+    v = units / el
+    line = {"impl": "reference", "metric": "bead-steps/s", "value": v, "unit": "bead-steps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": el * 1e3 / (args.steps * per), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "classes": [wl.name for wl in classes],
+                       "ref_steps_per_sample": per},
+            "cpu_baseline": {"value": v, "unit": "bead-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{per} steps of every class per timed sample; Caracal's Fortran "
+                                       "is not buildable here, so its C++ restatement (oracle/) is timed"},
+            "e2e": {"value": v, "unit": "bead-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_classes(args):
+    """Trajectory classes of uneven atom and bead counts (H3, CH4H, CH4OH,
+    QMDFF) stepped together by one graph launch per chunk (cr_batch), against
+    the same engines run one after another (separate launches)."""
+    import torch
+    from caracal_gb300 import _lib as L
+    from caracal_gb300 import RPMDBatch
+
+    rank, ws, dist = dist_setup()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    classes = class_list(args.workload)
+    K, W = args.steps, args.warmup
+    cal = calibrate(L)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    engs = {prec: [make_engine(wl, prec, traj0=rank * wl.ntraj) for wl in classes] for prec in ("mixed", "fp64")}
+
+    def maxr(x):
+        if dist:
+            t = torch.tensor([x], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    def timed_batch(prec, sampler=None):
+        b = RPMDBatch(engs[prec], chunk_steps=args.chunk)
+        b.run(W)
+        flush.zero_()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        if sampler:
+            with sampler:
+                b.run(K)
+        else:
+            b.run(K)
+        torch.cuda.synchronize()
+        info = b.info()
+        b.close()
+        return maxr(info["ms"]), info
+
+    def timed_separate(prec):
+        per = []
+        for e in engs[prec]:
+            e.run(W)
+        for e in engs[prec]:
+            flush.zero_()
+            torch.cuda.synchronize()
+            e.run(K)
+            per.append(maxr(e.last_kernel_ms()))
+        return sum(per), per
+
+    clk = ClockSampler(dev)
+    ms_mx, info_mx = timed_batch("mixed", clk)
+    clocks = clk.summary()
+    ms_64, info_64 = timed_batch("fp64")
+    sep_mx, per_mx = timed_separate("mixed")
+    sep_64, per_64 = timed_separate("fp64")
+    units = [wl.ntraj * wl.nbeads * K for wl in classes]
+    total = sum(units)
+    value = ws * total / (ms_mx * 1e-3)
+
+    per_class = []
+    for i, wl in enumerate(classes):
+        q, p, f, e, st = engs["fp64"][i].get_state()
+        em = engs["mixed"][i]
+        em.set_state(q, p)
+        _, _, f_mx, _, _ = em.get_state()
+        ferr = float(np.max(np.abs(f_mx - f)) / np.max(np.abs(f)))
+        per_class.append({"workload": wl.name, "pes": wl.pes, "natoms": len(wl.mass), "nbeads": wl.nbeads,
+                          "ntraj": wl.ntraj, "thermostat": wl.thermostat,
+                          "separate_mixed": ws * units[i] / (per_mx[i] * 1e-3),
+                          "separate_fp64": ws * units[i] / (per_64[i] * 1e-3),
+                          "force_error_vs_fp64": ferr})
+
+    # end to end through the public API: every step the host state of every
+    # class goes in (set_state), the batch steps once, the state comes out
+    b = RPMDBatch(engs["mixed"], chunk_steps=1)
+    states = [e.get_state() for e in engs["mixed"]]
+    K_e2e = min(K, args.e2e_steps // 10 or 1)
+    b.run(1)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(K_e2e):
+        for e, (q, p, f, _, _) in zip(engs["mixed"], states):
+            e.set_state(q, p, f)
+        b.run(1)
+        states = [e.get_state() for e in engs["mixed"]]
+    el = maxr(time.perf_counter() - t0)
+    b.close()
+    nbytes = sum(wl.ntraj * wl.nbeads * len(wl.mass) * 3 * 8 for wl in classes)
+    e2e = ws * sum(wl.ntraj * wl.nbeads for wl in classes) * K_e2e / el
+
+    # roofline: the classes' algorithmic flops over the batched launch time
+    p64, p32 = cal["fp64"]["peak_tflops"], cal["fp32"]["peak_tflops"]
+    eq_mx = eq_64 = 0.0
+    for wl, u in zip(classes, units):
+        f64, pes64 = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat,
+                                              cal["fp64"]["w"], wl.transrot)
+        _, pes32 = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat,
+                                            cal["fp32"]["w"], wl.transrot)
+        eq_mx += (f64 + pes32 * p64 / p32) * u
+        eq_64 += (f64 + pes64) * u
+    ach = eq_mx / (ms_mx * 1e-3) / 1e12
+    ach64 = eq_64 / (ms_64 * 1e-3) / 1e12
+    line = {
+        "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": ws, "steps": K,
+        "warmup": W, "ms_per_step": ms_mx / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32 (mixed form)", "data": "synthetic",
+        "config": {"workload": args.workload, "classes": [c["workload"] for c in per_class],
+                   "chunk_steps": args.chunk, "parallelism": f"replicas x{ws}",
+                   "l2": "flushed (256 MB write) before each timed run"},
+        "plain_fp64": {"value": ws * total / (ms_64 * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms_64 / K},
+        "separate_launches": {"mixed": ws * total / (sep_mx * 1e-3), "fp64": ws * total / (sep_64 * 1e-3),
+                              "unit": "bead-steps/s"},
+        "batched_over_separate": {"mixed": sep_mx / ms_mx, "fp64": sep_64 / ms_64},
+        "mixed_over_plain": ms_64 / ms_mx,
+        "per_class": per_class,
+        "e2e": {"value": e2e, "unit": "bead-steps/s", "steps": K_e2e, "h2d_bytes_per_step": 3 * nbytes,
+                "d2h_bytes_per_step": 3 * nbytes + sum(8 * wl.ntraj + 4 * wl.ntraj for wl in classes)},
+        "gpu_launches": info_mx["launches"],
+        "launch": {"graph_kernels_per_chunk": info_mx["graph_nodes"], "chunk_steps": args.chunk},
+        "roofline": {"kernel": "cr_batch graph<mixed>", "bound": "fp64+fp32 (FP64-equivalent)",
+                     "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64, "traffic": None,
+                     "peak_source": "measured in this run (FP64/FP32 FMA microbenchmarks, cr_calibrate_op)"},
+        "roofline_plain_fp64": {"achieved": ach64, "peak": p64, "unit": "TFLOP/s", "frac": ach64 / p64},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = [cpu_baseline(wl, target_s=args.cpu_seconds / 4) for wl in classes]
+        rate = total / sum(u / c["value"] for u, c in zip(units, cb))
+        line["cpu_baseline"] = {"value": rate, "unit": "bead-steps/s", "cores": cb[0]["cores"], "kind": "port",
+                                "sample": "; ".join(c["sample"] for c in cb)}
+    if rank == 0:
+        print(json.dumps(line))
+    for prec in engs:
+        for e in engs[prec]:
+            e.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -501,16 +693,25 @@ def main():
     ap.add_argument("--workload", default="ch4h",
                     help="ch4h (CH4+H recrossing children, 4096 x 32 beads: the default), "
                          "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16), "
-                         "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (64 x 16)")
+                         "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (512 x 64), "
+                         "classes (H3 4096x8, CH4H 2048x32, CH4OH 512x64, QMDFF 128x128 in one batch), "
+                         "classes_small (the same with 1/16 of the trajectories)")
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-steps-per-sample", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="run only the engine launches (small ncu captures)")
+    ap.add_argument("--chunk", type=int, default=50, help="steps per batch graph (classes workloads)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload in ("classes", "classes_small"):
+        if args.impl == "reference":
+            reference_classes(args)
+        else:
+            run_classes(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

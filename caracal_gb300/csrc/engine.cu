@@ -223,6 +223,7 @@ struct cr_engine {
   size_t smem_drift = 0, smem_kick = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
+  bool split_ready = false;  // split_prepare done
 };
 
 namespace {
@@ -318,13 +319,34 @@ void build_pile(int P, double beta, double dt, double tau0, std::vector<double>&
   }
 }
 
+// Persistent run of nsteps steps.  dev_step: the first step index is read
+// from the device counter, which a second launch then advances (so the pair
+// can be replayed from a graph); the shared-memory limit is then set by the
+// caller before the capture.
 template <class PES>
-int launch_run(cr_engine* e, int nsteps) {
+int launch_run(cr_engine* e, int nsteps, bool dev_step = false) {
+  auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
+                                                  : cr::rpmd_run_kernel<PES, false>;
+  if (!dev_step) {
+    CR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
+    kern<<<e->grid, e->block, e->smem, e->stream>>>(e->prm, e->istep, nsteps);
+    CR_CUDA(cudaGetLastError());
+    return CR_OK;
+  }
+  cr::StepParams prm = e->prm;
+  prm.istep_dev = e->d_istep;
+  kern<<<e->grid, e->block, e->smem, e->stream>>>(prm, 0, nsteps);
+  CR_CUDA(cudaGetLastError());
+  cr::advance_by_kernel<<<1, 1, 0, e->stream>>>(e->d_istep, nsteps);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+template <class PES>
+int set_run_smem(cr_engine* e) {
   auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
                                                   : cr::rpmd_run_kernel<PES, false>;
   CR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
-  kern<<<e->grid, e->block, e->smem, e->stream>>>(e->prm, e->istep, nsteps);
-  CR_CUDA(cudaGetLastError());
   return CR_OK;
 }
 
@@ -435,27 +457,37 @@ int split_step_launches(cr_engine* e) {
   return CR_OK;
 }
 
+// Everything the graph path needs before its launches can be captured:
+// shared-memory limits and the force kernel's autotuned variant.
+int split_prepare(cr_engine* e) {
+  if (e->split_ready) return CR_OK;
+  CR_CUDA(cudaFuncSetAttribute(cr::split_drift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)e->smem_drift));
+  CR_CUDA(cudaFuncSetAttribute(cr::split_kick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)e->smem_kick));
+  // the force kernels set their shared-memory limits outside the capture
+  int rc = CR_OK;
+  if (e->evb) rc = evb_launch(e->evb, e->d_q, 0, e->d_V, e->d_f, e->d_V2, e->d_f2, e->cfg.precision, e->stream);
+  else if (e->ff) rc = qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
+  if (rc) return rc;
+  // let the autotuner pick the force-kernel variant on this batch before it
+  // is frozen into the graph; the gradient goes to scratch so f is untouched
+  const size_t nall = (size_t)e->T * e->P * e->NC;
+  double* scratch = nullptr;
+  if (e->ff && cudaMalloc(&scratch, nall * sizeof(double)) == cudaSuccess) {
+    rc = split_forces(e, e->d_V, scratch);
+    cudaStreamSynchronize(e->stream);
+    cudaFree(scratch);
+    if (rc) return rc;
+  }
+  e->split_ready = true;
+  return CR_OK;
+}
+
 int split_run(cr_engine* e, int nsteps) {
   if (!e->graph_exec) {
-    CR_CUDA(cudaFuncSetAttribute(cr::split_drift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)e->smem_drift));
-    CR_CUDA(cudaFuncSetAttribute(cr::split_kick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)e->smem_kick));
-    // the force kernels set their shared-memory limits outside the capture
-    int rc = CR_OK;
-    if (e->evb) rc = evb_launch(e->evb, e->d_q, 0, e->d_V, e->d_f, e->d_V2, e->d_f2, e->cfg.precision, e->stream);
-    else if (e->ff) rc = qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
+    int rc = split_prepare(e);
     if (rc) return rc;
-    // let the autotuner pick the force-kernel variant on this batch before it
-    // is frozen into the graph; the gradient goes to scratch so f is untouched
-    const size_t nall = (size_t)e->T * e->P * e->NC;
-    double* scratch = nullptr;
-    if (e->ff && cudaMalloc(&scratch, nall * sizeof(double)) == cudaSuccess) {
-      rc = split_forces(e, e->d_V, scratch);
-      cudaStreamSynchronize(e->stream);
-      cudaFree(scratch);
-      if (rc) return rc;
-    }
     CR_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     rc = split_step_launches(e);
     cudaGraph_t g = nullptr;
@@ -1301,6 +1333,197 @@ int cr_engine_kappa(cr_engine* e, double* num, double* denom, double* weights, i
   if (weights)
     CR_CUDA(cudaMemcpyAsync(weights, e->d_w, (size_t)e->T * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
   CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: several engines (trajectory classes of different atom and bead
+// counts, surfaces and precisions) stepped by one graph launch per chunk of
+// steps.  Each engine's chunk is a branch of the graph on its own stream:
+// a persistent analytic kernel (step index from the device counter) or the
+// graph path's per-step kernels, so the classes fill the GPU together.
+// ---------------------------------------------------------------------------
+struct cr_batch {
+  std::vector<cr_engine*> eng;
+  int chunk = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> join;
+  struct Chunk {
+    int len;
+    int nodes;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Chunk> graphs;
+  long long launches = 0;  // kernels of the last cr_batch_run
+  float last_ms = 0.f;
+};
+
+namespace {
+
+int batch_prepare(cr_engine* e) {
+  if (e->split) return split_prepare(e);
+  switch (e->cfg.pes) {
+    case CR_PES_H3: return set_run_smem<cr::PesH3>(e);
+    case CR_PES_CH4H: return set_run_smem<cr::PesCH4H>(e);
+    case CR_PES_CH4OH: return set_run_smem<cr::PesCH4OH>(e);
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+}
+
+int batch_branch(cr_engine* e, int len) {
+  if (e->split) {
+    for (int n = 0; n < len; ++n) {
+      int rc = split_step_launches(e);
+      if (rc) return rc;
+    }
+    return CR_OK;
+  }
+  switch (e->cfg.pes) {
+    case CR_PES_H3: return launch_run<cr::PesH3>(e, len, true);
+    case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, len, true);
+    case CR_PES_CH4OH: return launch_run<cr::PesCH4OH>(e, len, true);
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+}
+
+cr_batch::Chunk* batch_graph(cr_batch* b, int len) {
+  for (auto& c : b->graphs)
+    if (c.len == len) return &c;
+  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    fail(CR_ERR_CUDA, "batch capture could not start");
+    return nullptr;
+  }
+  int rc = cudaEventRecord(b->fork, b->stream) == cudaSuccess ? CR_OK
+                                                               : fail(CR_ERR_CUDA, "batch fork event failed");
+  for (size_t i = 0; i < b->eng.size() && rc == CR_OK; ++i) {
+    cr_engine* e = b->eng[i];
+    if (cudaStreamWaitEvent(e->stream, b->fork, 0) != cudaSuccess) {
+      rc = fail(CR_ERR_CUDA, "batch fork failed");
+      break;
+    }
+    rc = batch_branch(e, len);
+    if (rc == CR_OK && (cudaEventRecord(b->join[i], e->stream) != cudaSuccess ||
+                        cudaStreamWaitEvent(b->stream, b->join[i], 0) != cudaSuccess))
+      rc = fail(CR_ERR_CUDA, "batch join failed");
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  if (rc != CR_OK || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (rc == CR_OK) fail(CR_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(ce));
+    cudaGetLastError();
+    return nullptr;
+  }
+  cr_batch::Chunk c{len, 0, g, nullptr};
+  size_t nodes = 0;
+  if (cudaGraphGetNodes(g, nullptr, &nodes) != cudaSuccess || cudaGraphInstantiate(&c.exec, g, 0) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    fail(CR_ERR_CUDA, "batch graph instantiation failed");
+    return nullptr;
+  }
+  // kernels only: the fork/join leave no nodes of their own
+  c.nodes = (int)nodes;
+  b->graphs.push_back(c);
+  return &b->graphs.back();
+}
+
+}  // namespace
+
+extern "C" {
+
+int cr_batch_create(cr_engine* const* engines, int nengines, int chunk_steps, cr_batch** out) {
+  if (!out) return fail(CR_ERR_ARG, "NULL output handle");
+  *out = nullptr;
+  if (!engines || nengines < 1) return fail(CR_ERR_ARG, "a batch needs at least one engine");
+  if (chunk_steps < 1) return fail(CR_ERR_ARG, "chunk_steps must be >= 1");
+  for (int i = 0; i < nengines; ++i) {
+    if (!engines[i]) return fail(CR_ERR_ARG, "NULL engine in the batch");
+    for (int j = 0; j < i; ++j)
+      if (engines[j] == engines[i]) return fail(CR_ERR_ARG, "an engine appears twice in the batch");
+  }
+  cr_batch* b = new cr_batch();
+  b->eng.assign(engines, engines + nengines);
+  b->chunk = chunk_steps;
+  b->join.assign((size_t)nengines, nullptr);
+  bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreate(&b->ev0) == cudaSuccess && cudaEventCreate(&b->ev1) == cudaSuccess;
+  for (auto& ev : b->join) ok = ok && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cr_batch_destroy(b);
+    return fail(CR_ERR_CUDA, "batch stream or event creation failed");
+  }
+  *out = b;
+  return CR_OK;
+}
+
+int cr_batch_destroy(cr_batch* b) {
+  if (!b) return CR_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& c : b->graphs) {
+    if (c.exec) cudaGraphExecDestroy(c.exec);
+    if (c.graph) cudaGraphDestroy(c.graph);
+  }
+  for (auto ev : b->join)
+    if (ev) cudaEventDestroy(ev);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return CR_OK;
+}
+
+int cr_batch_run(cr_batch* b, int nsteps) {
+  if (!b) return fail(CR_ERR_ARG, "NULL batch");
+  if (nsteps < 0) return fail(CR_ERR_ARG, "nsteps must be >= 0");
+  for (cr_engine* e : b->eng)
+    if (e->xi_on && e->istep + nsteps - e->side_step0 > e->side_cap)
+      return fail(CR_ERR_ARG, "run exceeds the recrossing step capacity set by cr_engine_set_recross");
+  if (nsteps == 0) return CR_OK;
+  for (cr_engine* e : b->eng) {
+    CR_CUDA(cudaStreamSynchronize(e->stream));  // work queued on the engine before the batch
+    int rc = batch_prepare(e);
+    if (rc) return rc;
+    e->h_istep = e->istep;
+    CR_CUDA(cudaMemcpyAsync(e->d_istep, &e->h_istep, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  }
+  const int full = nsteps / b->chunk, rem = nsteps % b->chunk;
+  cr_batch::Chunk* cf = full ? batch_graph(b, b->chunk) : nullptr;
+  if (full && !cf) return CR_ERR_CUDA;
+  cr_batch::Chunk* cm = rem ? batch_graph(b, rem) : nullptr;
+  if (rem && !cm) return CR_ERR_CUDA;
+  CR_CUDA(cudaEventRecord(b->ev0, b->stream));
+  for (int n = 0; n < full; ++n) CR_CUDA(cudaGraphLaunch(cf->exec, b->stream));
+  if (rem) CR_CUDA(cudaGraphLaunch(cm->exec, b->stream));
+  CR_CUDA(cudaEventRecord(b->ev1, b->stream));
+  CR_CUDA(cudaStreamSynchronize(b->stream));
+  CR_CUDA(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+  b->launches = (long long)full * (cf ? cf->nodes : 0) + (cm ? cm->nodes : 0);
+  int bad = 0;
+  for (cr_engine* e : b->eng) {
+    e->istep += nsteps;
+    std::vector<int> st((size_t)e->T);
+    CR_CUDA(cudaMemcpy(st.data(), e->d_status, st.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int v : st) bad |= v;
+  }
+  if (bad) return fail(CR_ERR_TRAJECTORY, "a trajectory reported a non-finite coordinate or singular inertia");
+  return CR_OK;
+}
+
+int cr_batch_info(const cr_batch* b, long long* launches, int* graph_nodes, float* ms) {
+  if (!b) return fail(CR_ERR_ARG, "NULL batch");
+  if (launches) *launches = b->launches;
+  if (graph_nodes) {
+    *graph_nodes = 0;
+    for (auto& c : b->graphs)
+      if (c.len == b->chunk) *graph_nodes = c.nodes;
+  }
+  if (ms) *ms = b->last_ms;
   return CR_OK;
 }
 

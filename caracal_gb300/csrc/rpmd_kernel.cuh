@@ -201,6 +201,9 @@ struct StepParams {
   int side_stride;
   unsigned char* side;
   XiDev xi;
+  // step counter on the device (a launch replayed from a CUDA graph reads its
+  // first step index here); NULL: the launch argument
+  const int* istep_dev;
 };
 
 // Sum over the G lanes of a group (deterministic tree).  red: per-group
@@ -313,7 +316,8 @@ __host__ __device__ inline size_t step_smem_doubles(int P, int G, int NC, int gr
 }
 
 template <class PES, bool MIXED>
-__global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep0, int nsteps) {
+__global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep_arg, int nsteps) {
+  const int istep0 = prm.istep_dev ? *prm.istep_dev : istep_arg;
   constexpr int N = PES::N;
   constexpr int NC = 3 * N;
   extern __shared__ double smem[];

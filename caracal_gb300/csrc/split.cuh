@@ -547,6 +547,7 @@ __global__ void __launch_bounds__(kFinishBlock) split_nhc_kernel(SplitParams s) 
 }
 
 __global__ void split_advance_kernel(int* istep) { *istep += 1; }
+__global__ void advance_by_kernel(int* istep, int n) { *istep += n; }
 
 // mdinit-style initial state for any atom count: per (trajectory, bead, pair).
 __global__ void split_init_positions_kernel(int T, int P, int NC, uint32_t seed, uint32_t traj0, const double* q0,

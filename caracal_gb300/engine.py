@@ -377,3 +377,36 @@ class RPMDEngine:
         L.check(L.lib().cr_engine_launch_info(self._h, C.byref(g), C.byref(b), C.byref(s), C.byref(n)),
                 "launch_info")
         return {"grid": g.value, "block": b.value, "smem_bytes": s.value, "launches": n.value}
+
+
+class RPMDBatch:
+    """Several engines (trajectory classes of different surfaces, atom and
+    bead counts or precisions) advanced together, one graph launch per chunk
+    of steps (cr_batch).  run(n) gives every engine the state that its own
+    run(n) would give."""
+
+    def __init__(self, engines, chunk_steps=50):
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e._h for e in self.engines])
+        h = C.c_void_p()
+        L.check(L.lib().cr_batch_create(arr, len(self.engines), int(chunk_steps), C.byref(h)), "batch_create")
+        self._h = h
+
+    def run(self, nsteps, check=True):
+        rc = L.lib().cr_batch_run(self._h, int(nsteps))
+        if check:
+            L.check(rc, "batch_run")
+        return rc
+
+    def info(self):
+        n, g, ms = C.c_longlong(), C.c_int(), C.c_float()
+        L.check(L.lib().cr_batch_info(self._h, C.byref(n), C.byref(g), C.byref(ms)), "batch_info")
+        return {"launches": n.value, "graph_nodes": g.value, "ms": ms.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().cr_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -137,3 +137,36 @@ def ch4oh_geometry(r_ch_ang=1.09, r_ho_ang=1.3, r_oh_ang=0.97, angle_deg=100.0):
     a = np.radians(angle_deg)
     q[6] = q[5] + (-v[0] * np.cos(a) + perp * np.sin(a)) * r_oh_ang
     return angstrom_to_bohr(q)
+
+
+def ch4h_md_config(ntraj=2048, nbeads=32, nsteps=1000, kelvin=500.0, dt_fs=0.1):
+    """CH4 + H thermal trajectories (Andersen, ANDERSEN_STEP 70) from the
+    dividing-surface geometry with 0.01 A bead jitter."""
+    return Workload(name=f"ch4h_md_P{nbeads}_T{ntraj}", pes="ch4h",
+                    symbols=["H", "C", "H", "H", "H", "H"], q0=ch4h_dividing_surface(),
+                    nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs, nsteps=nsteps,
+                    thermostat="andersen", sigma_bohr=float(angstrom_to_bohr(0.01)))
+
+
+def ch4oh_md_config(ntraj=512, nbeads=64, nsteps=1000, kelvin=300.0, dt_fs=0.1):
+    """CH4 + OH thermal trajectories (Andersen, ANDERSEN_STEP 70), 7 atoms."""
+    return Workload(name=f"ch4oh_md_P{nbeads}_T{ntraj}", pes="ch4oh",
+                    symbols=["H", "C", "H", "H", "H", "O", "H"], q0=ch4oh_geometry(),
+                    nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs, nsteps=nsteps,
+                    thermostat="andersen", sigma_bohr=float(angstrom_to_bohr(0.01)))
+
+
+def mixed_classes(scale=1, nsteps=1000):
+    """Four trajectory classes of uneven atom and bead counts stepped together:
+    H3 (N=3) T=4096 P=8 (PILE), CH4H (N=6) T=2048 P=32, CH4OH (N=7) T=512
+    P=64, QMDFF C20H42 (N=62) T=128 P=128 (Andersen); 147.5 M bead-steps in
+    1000 steps.  Each class has its own noise seed; ``scale`` divides the
+    trajectory counts (tests)."""
+    t = lambda n: max(1, n // scale)  # noqa: E731
+    out = [h3_config(ntraj=t(4096), nbeads=8, nsteps=nsteps, thermostat="pile"),
+           ch4h_md_config(ntraj=t(2048), nbeads=32, nsteps=nsteps),
+           ch4oh_md_config(ntraj=t(512), nbeads=64, nsteps=nsteps),
+           qmdff_config(ntraj=t(128), nbeads=128, nsteps=nsteps)]
+    for i, w in enumerate(out):
+        w.seed = SEED + 1 + i
+    return out

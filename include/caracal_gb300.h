@@ -324,6 +324,21 @@ int cr_host_free(void* ptr);
 #define CR_CALIB_COSH 11
 int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s);
 
+/* ---- batches of trajectory classes -----------------------------------------
+ * One graph launch per chunk of steps advances several engines (classes with
+ * different surfaces, atom and bead counts, precisions) side by side: Caracal
+ * farms such runs over MPI ranks (src/dynamic.f90:1569-1579 per rank); here
+ * they share one GPU.  Each engine keeps its own state and step counter;
+ * cr_batch_run(b, n) is cr_engine_run(e, n) for every engine of the batch
+ * (the same results) with the classes overlapped on the device. */
+typedef struct cr_batch cr_batch;
+int cr_batch_create(cr_engine* const* engines, int nengines, int chunk_steps, cr_batch** out);
+int cr_batch_run(cr_batch* b, int nsteps);
+/* kernels launched by the last cr_batch_run, kernels per chunk graph, its
+ * device time in ms */
+int cr_batch_info(const cr_batch* b, long long* launches, int* graph_nodes, float* ms);
+int cr_batch_destroy(cr_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

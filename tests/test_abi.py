@@ -81,3 +81,13 @@ def test_evb_fit_argument_validation():
     assert lib.cr_evb_fit(1, L.dptr(x), 4, 3, L.dptr(e), L.dptr(e), L.dptr(e), L.dptr(f), None) == L.CR_ERR_ARG
     assert lib.cr_evb_fit(4, L.dptr(x), 4, -1, L.dptr(e), L.dptr(e), L.dptr(e), L.dptr(f), None) == L.CR_ERR_ARG
     assert lib.cr_evb_fit(4, L.dptr(x), 4, 0, None, None, None, None, None) == 0
+
+
+def test_batch_argument_validation():
+    lib = L.lib()
+    h = C.c_void_p()
+    assert lib.cr_batch_create(None, 0, 10, C.byref(h)) == L.CR_ERR_ARG
+    arr = (C.c_void_p * 1)(None)
+    assert lib.cr_batch_create(arr, 1, 10, C.byref(h)) == L.CR_ERR_ARG
+    assert lib.cr_batch_run(None, 1) == L.CR_ERR_ARG
+    assert lib.cr_batch_destroy(None) == 0

@@ -5,7 +5,7 @@ import os
 
 import numpy as np
 
-from caracal_gb300.workloads import ch4h_dividing_surface, h3_collinear
+from caracal_gb300.workloads import ch4h_dividing_surface, ch4oh_geometry, h3_collinear
 from conftest import ROOT
 from oracle import oracle as orc
 
@@ -19,7 +19,7 @@ def _bench():
 
 def test_algo_table_matches_oracle_counts():
     table = _bench().ALGO_PES_OPS
-    for pes, q in (("h3", h3_collinear()), ("ch4h", ch4h_dividing_surface())):
+    for pes, q in (("h3", h3_collinear()), ("ch4h", ch4h_dividing_surface()), ("ch4oh", ch4oh_geometry())):
         counted = {k: v for k, v in orc.pes_opcount(pes, q).items() if v and k != "cmp"}
         assert counted == table[pes], (pes, counted)
 
