@@ -132,7 +132,14 @@ def _sig(lib):
         "cr_evb_destroy": ([v], C.c_int),
         "cr_evb_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
         "cr_engine_create_evb": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
+        "cr_qmdff_nparams": ([v, i], C.c_int),
+        "cr_qmdff_hvp": ([v, d, d, C.c_int, d, d, d], C.c_int),
+        "cr_qmdff_param_vjp": ([v, d, d, C.c_int, d], C.c_int),
         "cr_evb_fit": ([C.c_int, d, C.c_int, C.c_int, d, d, d, d, d], C.c_int),
+        "cr_adjoint_create": ([v, C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+        "cr_adjoint_forward": ([v], C.c_int),
+        "cr_adjoint_backward": ([v, d, d, d, d, d], C.c_int),
+        "cr_adjoint_destroy": ([v], C.c_int),
         "cr_batch_create": ([C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
         "cr_batch_run": ([v, C.c_int], C.c_int),
         "cr_batch_info": ([v, C.POINTER(C.c_longlong), i, C.POINTER(C.c_float)], C.c_int),

@@ -1,4 +1,5 @@
 // Host side of the GB300 RPMD engine and its C-ABI (include/caracal_gb300.h).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1524,6 +1525,193 @@ int cr_batch_info(const cr_batch* b, long long* launches, int* graph_nodes, floa
       if (c.len == b->chunk) *graph_nodes = c.nodes;
   }
   if (ms) *ms = b->last_ms;
+  return CR_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Adjoint of the ring-polymer velocity-Verlet step (NVE, plain FP64, QMDFF):
+// gradients of a loss L(q_K, p_K) at step K with respect to the force field's
+// linear parameters and to the initial state, with checkpoints every `every`
+// steps and the positions of one segment recomputed at a time.
+//
+// Forward step n:  p' = p_{n-1} - h g(q_{n-1});  (q_n, p'') = A (q_{n-1}, p');
+//                  p_n = p'' - h g(q_n)          (h = dt/2, A the free ring
+// polymer).  Reverse, from (lq, lp) = dL/d(q_K, p_K):
+//   lq += -h H(q_K) lp                               (last half kick)
+//   for n = K .. 1:  (lq, lp) <- A^T (lq, lp);
+//                    lq += c H(q_{n-1}) lp,  c = -2h (n > 1: both half kicks
+//                    at q_{n-1}), -h (n = 1)
+// and the parameter gradient collects c d/dtheta (lp . g(q_m)) at each kick.
+// A^T: K1, K2, K3 are symmetric, so A^T applied to (lq, lp) is A applied to
+// (p := lq, q := lp) -- the forward drift kernel with swapped arrays and zero
+// forces.
+// ---------------------------------------------------------------------------
+namespace cr {
+__global__ void axpy_kernel(size_t n, double a, const double* x, double* y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = fma(a, x[i], y[i]);
+}
+}  // namespace cr
+
+struct cr_adjoint {
+  cr_engine* e = nullptr;
+  int nsteps = 0, every = 0, nseg = 0, nlin = 0, scratch_beads = 0;
+  size_t nall = 0;
+  int istep0 = 0;
+  bool forward_done = false;
+  double* ck = nullptr;   // [nseg][3][nall]: q, p, f at the segment starts
+  double* fin = nullptr;  // [3][nall]: the state after step K
+  double* seg = nullptr;  // [every][nall]: positions of the current segment
+  double *lq = nullptr, *lp = nullptr, *hw = nullptr, *zero = nullptr, *scratch = nullptr, *gacc = nullptr;
+};
+
+namespace {
+
+int adj_copy_state(cr_engine* e, double* dst, bool to_engine) {
+  const size_t b = (size_t)e->T * e->P * e->NC * sizeof(double);
+  double* eng[3] = {e->d_q, e->d_p, e->d_f};
+  for (int k = 0; k < 3; ++k) {
+    double* x = dst + (size_t)k * (b / sizeof(double));
+    CR_CUDA(cudaMemcpyAsync(to_engine ? eng[k] : x, to_engine ? x : eng[k], b, cudaMemcpyDeviceToDevice, e->stream));
+  }
+  return CR_OK;
+}
+
+int adj_axpy(cr_adjoint* a, double c, const double* x, double* y) {
+  cr::axpy_kernel<<<1024, 256, 0, a->e->stream>>>(a->nall, c, x, y);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+// lq += c H(q) lp;  gacc += c d/dtheta (lp . grad E(q))
+int adj_kick(cr_adjoint* a, const double* q, double c) {
+  cr_engine* e = a->e;
+  const int nb = e->T * e->P;
+  int rc = qmdff_hvp_launch(e->ff, q, a->lp, nb, nullptr, nullptr, a->hw, nullptr, e->stream);
+  if (rc) return rc;
+  if ((rc = adj_axpy(a, c, a->hw, a->lq))) return rc;
+  return qmdff_vjp_launch(e->ff, q, a->lp, nb, nullptr, nullptr, c, a->scratch, a->scratch_beads, a->gacc, e->stream);
+}
+
+int adj_drift(cr_adjoint* a) {
+  cr_engine* e = a->e;
+  cr::SplitParams sp = e->sp;
+  sp.p = a->lq;
+  sp.q = a->lp;
+  sp.f = a->zero;
+  sp.thermostat = CR_THERMO_NONE;
+  const int cw = cr::split_chunk(e->P);
+  const dim3 grid((e->NC + cw - 1) / cw, e->T);
+  cr::split_drift_kernel<<<grid, cr::kSplitBlock, e->smem_drift, e->stream>>>(sp);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cr_adjoint_create(cr_engine* e, int nsteps, int every, cr_adjoint** out) {
+  if (!out) return fail(CR_ERR_ARG, "NULL output handle");
+  *out = nullptr;
+  if (!e || nsteps < 1 || every < 1) return fail(CR_ERR_ARG, "adjoint needs an engine, nsteps >= 1, every >= 1");
+  if (!e->ff || e->evb || !e->split) return fail(CR_ERR_UNSUPPORTED, "the adjoint is built for QMDFF engines");
+  if (e->cfg.precision != CR_PREC_FP64) return fail(CR_ERR_UNSUPPORTED, "the adjoint runs the plain FP64 form");
+  if (e->cfg.thermostat != CR_THERMO_NONE || e->cfg.transrot || e->parent || e->xi_on)
+    return fail(CR_ERR_UNSUPPORTED, "the adjoint needs NVE steps without transrot, parent or recrossing");
+  if (e->ff->nterm[4] > 0) return fail(CR_ERR_UNSUPPORTED, "second derivatives of H/halogen-bond terms are not built");
+  cr_adjoint* a = new cr_adjoint();
+  a->e = e;
+  a->nsteps = nsteps;
+  a->every = every;
+  a->nseg = (nsteps + every - 1) / every;
+  a->nlin = qmdff_nlin(e->ff);
+  a->nall = (size_t)e->T * e->P * e->NC;
+  a->scratch_beads = std::min(e->T * e->P, 4096);
+  const size_t n = a->nall;
+  bool ok = cudaMalloc(&a->ck, (size_t)a->nseg * 3 * n * 8) == cudaSuccess &&
+            cudaMalloc(&a->fin, 3 * n * 8) == cudaSuccess && cudaMalloc(&a->seg, (size_t)every * n * 8) == cudaSuccess &&
+            cudaMalloc(&a->lq, n * 8) == cudaSuccess && cudaMalloc(&a->lp, n * 8) == cudaSuccess &&
+            cudaMalloc(&a->hw, n * 8) == cudaSuccess && cudaMalloc(&a->zero, n * 8) == cudaSuccess &&
+            cudaMalloc(&a->scratch, (size_t)a->scratch_beads * std::max(a->nlin, 1) * 8) == cudaSuccess &&
+            cudaMalloc(&a->gacc, (size_t)std::max(a->nlin, 1) * 8) == cudaSuccess &&
+            cudaMemset(a->zero, 0, n * 8) == cudaSuccess;
+  if (!ok) {
+    cr_adjoint_destroy(a);
+    return fail(CR_ERR_CUDA, "device allocation of the adjoint buffers failed");
+  }
+  *out = a;
+  return CR_OK;
+}
+
+int cr_adjoint_destroy(cr_adjoint* a) {
+  if (!a) return CR_OK;
+  cudaFree(a->ck);
+  cudaFree(a->fin);
+  cudaFree(a->seg);
+  cudaFree(a->lq);
+  cudaFree(a->lp);
+  cudaFree(a->hw);
+  cudaFree(a->zero);
+  cudaFree(a->scratch);
+  cudaFree(a->gacc);
+  delete a;
+  return CR_OK;
+}
+
+int cr_adjoint_forward(cr_adjoint* a) {
+  if (!a) return fail(CR_ERR_ARG, "NULL adjoint");
+  cr_engine* e = a->e;
+  a->istep0 = e->istep;
+  for (int k = 0; k < a->nseg; ++k) {
+    int rc = adj_copy_state(e, a->ck + (size_t)k * 3 * a->nall, false);
+    if (rc) return rc;
+    if ((rc = cr_engine_run(e, std::min(a->every, a->nsteps - k * a->every)))) return rc;
+  }
+  int rc = adj_copy_state(e, a->fin, false);
+  if (rc) return rc;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  a->forward_done = true;
+  return CR_OK;
+}
+
+int cr_adjoint_backward(cr_adjoint* a, const double* dl_dq, const double* dl_dp, double* grad, double* dl_dq0,
+                        double* dl_dp0) {
+  if (!a || !dl_dq || !dl_dp || !grad) return fail(CR_ERR_ARG, "NULL argument");
+  if (!a->forward_done) return fail(CR_ERR_ARG, "cr_adjoint_forward must run first");
+  cr_engine* e = a->e;
+  const size_t n = a->nall;
+  const double h = 0.5 * e->cfg.dt;
+  CR_CUDA(cudaMemcpyAsync(a->lq, dl_dq, n * 8, cudaMemcpyHostToDevice, e->stream));
+  CR_CUDA(cudaMemcpyAsync(a->lp, dl_dp, n * 8, cudaMemcpyHostToDevice, e->stream));
+  CR_CUDA(cudaMemsetAsync(a->gacc, 0, (size_t)std::max(a->nlin, 1) * 8, e->stream));
+  int rc = adj_kick(a, a->fin, -h);  // the last half kick, at q_K
+  if (rc) return rc;
+  for (int k = a->nseg - 1; k >= 0; --k) {
+    const int s0 = k * a->every, len = std::min(a->every, a->nsteps - s0);
+    // recompute the segment's positions q_{s0} .. q_{s0+len-1}
+    if ((rc = adj_copy_state(e, a->ck + (size_t)k * 3 * n, true))) return rc;
+    e->istep = a->istep0 + s0;
+    CR_CUDA(cudaMemcpyAsync(a->seg, e->d_q, n * 8, cudaMemcpyDeviceToDevice, e->stream));
+    for (int i = 1; i < len; ++i) {
+      if ((rc = cr_engine_run(e, 1))) return rc;
+      CR_CUDA(cudaMemcpyAsync(a->seg + (size_t)i * n, e->d_q, n * 8, cudaMemcpyDeviceToDevice, e->stream));
+    }
+    for (int st = s0 + len; st > s0; --st) {
+      if ((rc = adj_drift(a))) return rc;
+      const int m = st - 1;
+      if ((rc = adj_kick(a, a->seg + (size_t)(m - s0) * n, m > 0 ? -2.0 * h : -h))) return rc;
+    }
+  }
+  // leave the engine in its state after step K
+  if ((rc = adj_copy_state(e, a->fin, true))) return rc;
+  e->istep = a->istep0 + a->nsteps;
+  if (a->nlin) CR_CUDA(cudaMemcpyAsync(grad, a->gacc, (size_t)a->nlin * 8, cudaMemcpyDeviceToHost, e->stream));
+  if (dl_dq0) CR_CUDA(cudaMemcpyAsync(dl_dq0, a->lq, n * 8, cudaMemcpyDeviceToHost, e->stream));
+  if (dl_dp0) CR_CUDA(cudaMemcpyAsync(dl_dp0, a->lp, n * 8, cudaMemcpyDeviceToHost, e->stream));
+  CR_CUDA(cudaStreamSynchronize(e->stream));
   return CR_OK;
 }
 

@@ -135,7 +135,101 @@ __global__ void __launch_bounds__(kQmdffWarps * 32, MINB)
   }
 }
 
+// Energy, gradient and Hessian-vector product H w per bead (plain form, dual
+// coordinates); dew[b] = w . grad E.
+__global__ void __launch_bounds__(kQmdffWarps * 32)
+    qmdff_hvp_kernel(qmdff::Dev D, int nbeads, const double* q, const double* w, double* e, double* g, double* hw,
+                     double* dew) {
+  extern __shared__ double qsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n3 = 3 * D.n;
+  double* ws = qsm + (size_t)warp * (qmdff::warp_hvp_smem_bytes(D.n) / sizeof(double));
+  for (int b = blockIdx.x * kQmdffWarps + warp; b < nbeads; b += gridDim.x * kQmdffWarps) {
+    const double* qb = q + (size_t)b * n3;
+    const double* wb = w + (size_t)b * n3;
+    for (int a = lane; a < n3; a += 32) {
+      ws[a] = qb[a];
+      ws[n3 + a] = wb[a];
+    }
+    __syncwarp();
+    double de = 0.0;
+    const double v = qmdff::warp_hvp(D, ws, g ? g + (size_t)b * n3 : nullptr, hw + (size_t)b * n3, de, lane);
+    if (lane == 0) {
+      if (e) e[b] = v;
+      if (dew) dew[b] = de;
+    }
+    __syncwarp();
+  }
+}
+
+// Per bead b and linear parameter t: out[b][t] = alpha_b (v_b . grad E_t|unit)
+// + beta_b E_t|unit (alpha = 1, beta = 0 where the weights are NULL).
+__global__ void __launch_bounds__(kQmdffWarps * 32)
+    qmdff_vjp_kernel(qmdff::Dev D, qmdff::Tables<double> U, int nbeads, int nlin, const double* q, const double* v,
+                     const double* alpha, const double* beta, double* out) {
+  extern __shared__ double qsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n3 = 3 * D.n;
+  double* xs = qsm + (size_t)warp * 2 * n3;
+  double* vs = xs + n3;
+  for (int b = blockIdx.x * kQmdffWarps + warp; b < nbeads; b += gridDim.x * kQmdffWarps) {
+    for (int a = lane; a < n3; a += 32) {
+      xs[a] = q[(size_t)b * n3 + a];
+      vs[a] = v[(size_t)b * n3 + a];
+    }
+    __syncwarp();
+    qmdff::warp_param_vjp(D, U, xs, vs, alpha ? alpha[b] : 1.0, beta ? beta[b] : 0.0, out + (size_t)b * nlin, lane);
+    __syncwarp();
+  }
+}
+
+// acc[t] += scale * sum_b in[b][t], the beads summed in order (deterministic).
+__global__ void sum_rows_kernel(int nrows, int ncols, const double* in, double scale, double* acc) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncols) return;
+  double s = 0.0;
+  for (int r = 0; r < nrows; ++r) s += in[(size_t)r * ncols + t];
+  acc[t] += scale * s;
+}
+
 }  // namespace cr
+
+int qmdff_hvp_launch(const cr_qmdff* ff, const double* d_q, const double* d_w, int nbeads, double* d_e, double* d_g,
+                     double* d_hw, double* d_dew, cudaStream_t s) {
+  if (ff->nterm[4] > 0) return cr_set_error(CR_ERR_UNSUPPORTED, "second derivatives of H/halogen-bond terms are not built");
+  const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_hvp_smem_bytes(ff->n);
+  CR_TRY_CUDA(cudaFuncSetAttribute(cr::qmdff_hvp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nbeads == 0) return CR_OK;
+  int grid = (nbeads + kQmdffWarps - 1) / kQmdffWarps;
+  if (grid > 1 << 20) grid = 1 << 20;
+  cr::qmdff_hvp_kernel<<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, nbeads, d_q, d_w, d_e, d_g, d_hw, d_dew);
+  CR_TRY_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+int qmdff_nlin(const cr_qmdff* ff) { return ff->nterm[0] + ff->nterm[1] + ff->nterm[2] + ff->nterm[3]; }
+
+int qmdff_vjp_launch(const cr_qmdff* ff, const double* d_q, const double* d_v, int nbeads, const double* d_alpha,
+                     const double* d_beta, double scale, double* d_scratch, int scratch_beads, double* d_acc,
+                     cudaStream_t s) {
+  if (ff->nterm[4] > 0) return cr_set_error(CR_ERR_UNSUPPORTED, "parameter gradients of H/halogen-bond terms are not built");
+  const int nlin = qmdff_nlin(ff);
+  const size_t smem = (size_t)kQmdffWarps * 2 * 3 * ff->n * sizeof(double);
+  CR_TRY_CUDA(cudaFuncSetAttribute(cr::qmdff_vjp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nlin == 0) return CR_OK;
+  const size_t n3 = (size_t)3 * ff->n;
+  for (int b0 = 0; b0 < nbeads; b0 += scratch_beads) {
+    const int nb = std::min(scratch_beads, nbeads - b0);
+    const int grid = (nb + kQmdffWarps - 1) / kQmdffWarps;
+    cr::qmdff_vjp_kernel<<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, ff->unit, nb, nlin, d_q + b0 * n3, d_v + b0 * n3,
+                                                              d_alpha ? d_alpha + b0 : nullptr,
+                                                              d_beta ? d_beta + b0 : nullptr, d_scratch);
+    CR_TRY_CUDA(cudaGetLastError());
+    cr::sum_rows_kernel<<<(nlin + 127) / 128, 128, 0, s>>>(nb, nlin, d_scratch, scale, d_acc);
+    CR_TRY_CUDA(cudaGetLastError());
+  }
+  return CR_OK;
+}
 
 namespace {
 
@@ -402,6 +496,25 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   D.zahn_par = d->zahn_par;
   D.e_zero = d->e_zero;
   D.distinct = distinct ? 1 : 0;
+  for (int k = 0; k < cr::qmdff::kKinds; ++k) D.nterm[k] = ff->nterm[k];
+  // unit tables of the linear parameters (parameter gradients)
+  std::vector<double> ubond = vbond, uangl = vangl, utors = vtors, upair = vpair;
+  for (int m = 0; m < d->nbond; ++m) ubond[(size_t)3 * m + 1] = 1.0;
+  for (int m = 0; m < d->nangl; ++m) uangl[(size_t)kVAngl * m + 1] = 1.0;
+  for (int m = 0; m < d->ntors; ++m) utors[(size_t)14 * m + 1] = 1.0;
+  for (int m = 0; m < d->nnci; ++m) {
+    upair[(size_t)kVPair * m + 5] = 0.0;
+    upair[(size_t)kVPair * m + 6] = 1.0;
+  }
+  ff->unit.rad = D.d.rad;
+  up(ubond, &ff->unit.vbond);
+  up(uangl, &ff->unit.vangl);
+  up(utors, &ff->unit.vtors);
+  up(upair, &ff->unit.vpair);
+  if (rc != CR_OK) {
+    cr_qmdff_destroy(ff);
+    return rc;
+  }
   *out = ff;
   return CR_OK;
 }
@@ -453,6 +566,58 @@ int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, doubl
   cudaFree(d_q);
   cudaFree(d_e);
   cudaFree(d_g);
+  return rc;
+}
+
+int cr_qmdff_nparams(const cr_qmdff* ff, int* nlin) {
+  if (!ff || !nlin) return cr_set_error(CR_ERR_ARG, "NULL argument");
+  *nlin = qmdff_nlin(ff);
+  return CR_OK;
+}
+
+int cr_qmdff_hvp(cr_qmdff* ff, const double* xyz, const double* w, int nbeads, double* e, double* g, double* hw) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (nbeads < 0 || (nbeads > 0 && (!xyz || !w || !hw))) return cr_set_error(CR_ERR_ARG, "bad hvp arguments");
+  if (ff->nterm[4] > 0) return cr_set_error(CR_ERR_UNSUPPORTED, "second derivatives of H/halogen-bond terms are not built");
+  if (nbeads == 0) return CR_OK;
+  const size_t nq = (size_t)3 * ff->n * nbeads;
+  double* d = nullptr;
+  CR_TRY_CUDA(cudaMalloc(&d, (4 * nq + nbeads) * sizeof(double)));
+  double *dq = d, *dw = dq + nq, *dg = dw + nq, *dh = dg + nq, *de = dh + nq;
+  int rc = CR_OK;
+  if (cudaMemcpy(dq, xyz, nq * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dw, w, nq * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = cr_set_error(CR_ERR_CUDA, "copy of the hvp inputs failed");
+  else if ((rc = qmdff_hvp_launch(ff, dq, dw, nbeads, de, dg, dh, nullptr, nullptr)) == CR_OK &&
+           (cudaMemcpy(hw, dh, nq * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            (g && cudaMemcpy(g, dg, nq * 8, cudaMemcpyDeviceToHost) != cudaSuccess) ||
+            (e && cudaMemcpy(e, de, (size_t)nbeads * 8, cudaMemcpyDeviceToHost) != cudaSuccess)))
+    rc = cr_set_error(CR_ERR_CUDA, "copy of the hvp results failed");
+  cudaFree(d);
+  return rc;
+}
+
+int cr_qmdff_param_vjp(cr_qmdff* ff, const double* xyz, const double* v, int nbeads, double* grad) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (nbeads < 0 || !grad || (nbeads > 0 && (!xyz || !v))) return cr_set_error(CR_ERR_ARG, "bad vjp arguments");
+  if (ff->nterm[4] > 0) return cr_set_error(CR_ERR_UNSUPPORTED, "parameter gradients of H/halogen-bond terms are not built");
+  const int nlin = qmdff_nlin(ff);
+  for (int t = 0; t < nlin; ++t) grad[t] = 0.0;
+  if (nbeads == 0 || nlin == 0) return CR_OK;
+  const size_t nq = (size_t)3 * ff->n * nbeads;
+  const int chunk = std::min(nbeads, 4096);
+  double* d = nullptr;
+  CR_TRY_CUDA(cudaMalloc(&d, (2 * nq + (size_t)chunk * nlin + nlin) * sizeof(double)));
+  double *dq = d, *dv = dq + nq, *ds = dv + nq, *dacc = ds + (size_t)chunk * nlin;
+  int rc = CR_OK;
+  if (cudaMemcpy(dq, xyz, nq * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dv, v, nq * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(dacc, 0, (size_t)nlin * 8) != cudaSuccess)
+    rc = cr_set_error(CR_ERR_CUDA, "copy of the vjp inputs failed");
+  else if ((rc = qmdff_vjp_launch(ff, dq, dv, nbeads, nullptr, nullptr, 1.0, ds, chunk, dacc, nullptr)) == CR_OK &&
+           cudaMemcpy(grad, dacc, (size_t)nlin * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = cr_set_error(CR_ERR_CUDA, "copy of the vjp result failed");
+  cudaFree(d);
   return rc;
 }
 

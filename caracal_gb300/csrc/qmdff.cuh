@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "../../include/caracal_gb300.h"
+#include "dual.cuh"
 
 namespace cr {
 namespace qmdff {
@@ -71,6 +72,7 @@ struct Dev {
   double coul_cut, zahn_a, zahn_par, e_zero;
   int zahn;
   int distinct;  // 1: every term's atoms are pairwise distinct
+  int nterm[kKinds];  // terms per kind
 };
 
 template <class F> __device__ inline F q_sqrt(F x);
@@ -97,6 +99,23 @@ template <> __device__ inline float q_sin<float>(float x) { return sinf(x); }
 template <class F> __device__ inline F q_cos(F x);
 template <> __device__ inline double q_cos<double>(double x) { return cos(x); }
 template <> __device__ inline float q_cos<float>(float x) { return cosf(x); }
+template <class F> __device__ inline F q_pow(F x, double p);
+template <> __device__ inline double q_pow<double>(double x, double p) { return pow(x, p); }
+// dual coordinates (Hessian-vector products of the plain form)
+template <> __device__ inline Dual q_sqrt<Dual>(Dual x) { return sqrt(x); }
+template <> __device__ inline Dual q_exp<Dual>(Dual x) { return exp(x); }
+template <> __device__ inline Dual q_acos<Dual>(Dual x) { return acos(x); }
+template <> __device__ inline Dual q_asin<Dual>(Dual x) { return asin(x); }
+template <> __device__ inline Dual q_erf<Dual>(Dual x) { return erf(x); }
+template <> __device__ inline Dual q_erfc<Dual>(Dual x) { return erfc(x); }
+template <> __device__ inline Dual q_sin<Dual>(Dual x) { return sin(x); }
+template <> __device__ inline Dual q_cos<Dual>(Dual x) { return cos(x); }
+template <> __device__ inline Dual q_pow<Dual>(Dual x, double p) { return pow(x, p); }
+
+// Parameter type of a term evaluated in arithmetic type F (dual coordinates
+// read FP64 parameters).
+template <class F> struct ParamOf { using type = F; };
+template <> struct ParamOf<Dual> { using type = double; };
 
 template <class F>
 __device__ inline void cross(const F* a, const F* b, F* c) {
@@ -193,6 +212,7 @@ struct BeadPos {
   const double* x;
   const float* hi;
   const float* lo;
+  const double* w;  // tangent direction (dual coordinates only)
 };
 
 template <class F>
@@ -204,6 +224,11 @@ __device__ inline void disp<double>(const BeadPos& X, int a, int b, double* v) {
   v[2] = X.x[3 * a + 2] - X.x[3 * b + 2];
 }
 template <>
+__device__ inline void disp<Dual>(const BeadPos& X, int a, int b, Dual* v) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) v[d] = Dual(X.x[3 * a + d] - X.x[3 * b + d], X.w[3 * a + d] - X.w[3 * b + d]);
+}
+template <>
 __device__ inline void disp<float>(const BeadPos& X, int a, int b, float* v) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) v[d] = (X.hi[3 * a + d] - X.hi[3 * b + d]) + (X.lo[3 * a + d] - X.lo[3 * b + d]);
@@ -211,16 +236,18 @@ __device__ inline void disp<float>(const BeadPos& X, int a, int b, float* v) {
 
 // Bond stretch, generalised Lennard-Jones (src/ff_eg.f90:87-163):
 // e = k (1 + (r0/r)^a - 2 (r0/r)^(a/2)).
-__device__ inline double bond_f64(const Dev& D, const BeadPos& x, int m, Contrib<double>& c) {
+template <class F>
+__device__ inline F bond_plain(const Dev& D, const Tables<typename ParamOf<F>::type>& T, const BeadPos& x, int m,
+                               Contrib<F>& c) {
   const int i = D.bond[2 * m], j = D.bond[2 * m + 1];
-  double rb[3];
-  disp<double>(x, i, j, rb);
-  const double r2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
-  const double r = sqrt(r2);
-  const double* v = &D.d.vbond[3 * m];
+  F rb[3];
+  disp<F>(x, i, j, rb);
+  const F r2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
+  const F r = q_sqrt<F>(r2);
+  const auto* v = &T.vbond[3 * m];
   const double rij = v[0], kij = v[1], aai = v[2];
-  const double pa2 = pow(rij / r, aai / 2), pa = pa2 * pa2;
-  const double fac = aai * kij * (-pa + pa2) / r2;
+  const F pa2 = q_pow<F>(rij / r, aai / 2), pa = pa2 * pa2;
+  const F fac = aai * kij * (-pa + pa2) / r2;
   c.na = 2;
   c.a[0] = i;
   c.a[1] = j;
@@ -264,9 +291,10 @@ __device__ inline float bond_mixed(const Dev& D, const BeadPos& x, int m, Contri
 
 // Angle bend with abdamp damping (src/ff_eg.f90:167-299).
 template <class F>
-__device__ inline F angle_term(const Dev& D, const Tables<F>& T, const BeadPos& x, int m, Contrib<F>& c) {
+__device__ inline F angle_term(const Dev& D, const Tables<typename ParamOf<F>::type>& T, const BeadPos& x, int m,
+                               Contrib<F>& c) {
   const int j = D.angl[3 * m], i = D.angl[3 * m + 1], k = D.angl[3 * m + 2];
-  const F* v = &T.vangl[kVAngl * m];
+  const auto* v = &T.vangl[kVAngl * m];
   const F c0 = v[0], kijk = v[1], cc0 = v[2];
   F vab[3], vcb[3], vp[3];
   disp<F>(x, i, j, vab);
@@ -324,25 +352,25 @@ __device__ inline F dihedral(const F* ra, const F* rb, const F* rc, F* na, F* nb
   nan_ = q_sqrt<F>(dot3(na, na));
   nbn = q_sqrt<F>(dot3(nb, nb));
   F phi;
-  if constexpr (std::is_same<F, double>::value) {
-    double a[3] = {na[0], na[1], na[2]}, b[3] = {nb[0], nb[1], nb[2]};
-    if (fabs(nan_) > 1e-14) {
-      const double o = 1.0 / nan_;
+  if constexpr (!std::is_same<F, float>::value) {
+    F a[3] = {na[0], na[1], na[2]}, b[3] = {nb[0], nb[1], nb[2]};
+    if (fabs(ad::val(nan_)) > 1e-14) {
+      const F o = 1.0 / nan_;
       a[0] *= o;
       a[1] *= o;
       a[2] *= o;
     }
-    if (fabs(nbn) > 1e-14) {
-      const double o = 1.0 / nbn;
+    if (fabs(ad::val(nbn)) > 1e-14) {
+      const F o = 1.0 / nbn;
       b[0] *= o;
       b[1] *= o;
       b[2] *= o;
     }
-    double s = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-    if (fabs(fabs(s) - 1.0) < 1e-14) s = s >= 0 ? 1.0 : -1.0;
-    phi = acos(s);
-    cosphi = cos(phi);
-    sinphi = sin(phi);
+    F s = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    if (fabs(fabs(ad::val(s)) - 1.0) < 1e-14) s = ad::val(s) >= 0 ? F(1.0) : F(-1.0);
+    phi = q_acos<F>(s);
+    cosphi = q_cos<F>(phi);
+    sinphi = q_sin<F>(phi);
   } else {
     const float cn = dot3(na, nb);
     const float sn = sqrtf(dot3(rb, rb)) * fabsf(dot3(na, rc));
@@ -357,13 +385,14 @@ __device__ inline F dihedral(const F* ra, const F* rb, const F* rc, F* na, F* nb
 // Torsions (erf-blended cosine series, src/ff_eg.f90:303-440) and
 // inversions (tors type 2, src/ff_eg.f90:441-618).
 template <class F>
-__device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const BeadPos& x, int m, Contrib<F>& c) {
+__device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>::type>& T, const BeadPos& x, int m,
+                                 Contrib<F>& c) {
   const F pi = (F)3.1415926535897932384626433832795029;
   const F pi2 = (F)6.28318530717958623199592693708837;
   const F spi = (F)1.77245385090551599275151910313925;
   const int i = D.tors[6 * m], j = D.tors[6 * m + 1], k = D.tors[6 * m + 2], l = D.tors[6 * m + 3];
   const int nt = D.tors[6 * m + 4], type = D.tors[6 * m + 5];
-  const F* vt = &T.vtors[14 * m];
+  const auto* vt = &T.vtors[14 * m];
   const F phi0 = vt[0];
   F vab[3], vcb[3], vdc[3], dda[3], ddb[3], ddc[3], ddd[3];
   F et, dij, dampij, dampjk, dampX, d2ij, d2jk, d2X;
@@ -385,7 +414,7 @@ __device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const BeadPos
     F na[3], nb[3], nan_, nbn, cosphi, sinphi;
     const F phi = dihedral<F>(ra, rb, rc, na, nb, nan_, nbn, cosphi, sinphi);
     const F nenner = nan_ * nbn * sinphi;
-    if (fabs((double)nenner) < 1e-14) {
+    if (fabs((double)ad::val(nenner)) < 1e-14) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = F(0);
     } else {
@@ -456,21 +485,21 @@ __device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const BeadPos
   cross(re, rd, rn);
   const F rnn = q_sqrt<F>(dot3(rn, rn)), rvn = q_sqrt<F>(dot3(rv, rv));
   F om;
-  if constexpr (std::is_same<F, double>::value) {
-    double a[3] = {rn[0], rn[1], rn[2]}, b[3] = {rv[0], rv[1], rv[2]};
-    if (fabs(rnn) > 1e-14) {
-      const double o = 1.0 / rnn;
+  if constexpr (!std::is_same<F, float>::value) {
+    F a[3] = {rn[0], rn[1], rn[2]}, b[3] = {rv[0], rv[1], rv[2]};
+    if (fabs(ad::val(rnn)) > 1e-14) {
+      const F o = 1.0 / rnn;
       a[0] *= o;
       a[1] *= o;
       a[2] *= o;
     }
-    if (fabs(rvn) > 1e-14) {
-      const double o = 1.0 / rvn;
+    if (fabs(ad::val(rvn)) > 1e-14) {
+      const F o = 1.0 / rvn;
       b[0] *= o;
       b[1] *= o;
       b[2] *= o;
     }
-    om = asin(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+    om = q_asin<F>(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
   } else {
     om = q_asin<F>(fmin(F(1), fmax(F(-1), dot3(rn, rv) / (rnn * rvn))));
   }
@@ -484,7 +513,7 @@ __device__ inline F torsion_term(const Dev& D, const Tables<F>& T, const BeadPos
   cross(rv, rdme, rvdme);
   cross(rn, rdme, rndme);
   const F nenner = rnn * rvn * cosom;
-  if (fabs((double)nenner) > 1e-14) {
+  if (fabs((double)ad::val(nenner)) > 1e-14) {
     const F on = F(1) / nenner;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -535,12 +564,19 @@ __device__ inline void load_pair_params(const double* p, double* v) {
     v[2 * k + 1] = t.y;
   }
 }
+__device__ inline void load_pair_params(const double* p, Dual* v) {
+  double t[kVPair];
+  load_pair_params(p, t);
+#pragma unroll
+  for (int k = 0; k < kVPair; ++k) v[k] = Dual(t[k]);
+}
 
 // One NCI pair (src/ff_nonb.f90): BJ-damped C6/C8 dispersion and, for
 // r < 25 bohr, exponential repulsion, both times eps2 (:79-193); Coulomb
 // within coul_cut (:337-416), eps1 q_i q_j / r or the Zahn form.
 template <class F>
-__device__ inline F pair_term(const Dev& D, const Tables<F>& T, const BeadPos& x, int kp, Contrib<F>& c) {
+__device__ inline F pair_term(const Dev& D, const Tables<typename ParamOf<F>::type>& T, const BeadPos& x, int kp,
+                              Contrib<F>& c) {
   const int2 ij = __ldg(reinterpret_cast<const int2*>(D.pair) + kp);
   const int i1 = ij.x, i2 = ij.y;
   F v[kVPair];
@@ -759,7 +795,7 @@ __device__ inline typename std::conditional<MIXED, float, double>::type term(
     }
   } else {
     switch (kind) {
-      case 0: return bond_f64(D, x, m, c);
+      case 0: return bond_plain<double>(D, D.d, x, m, c);
       case 1: return angle_term<double>(D, D.d, x, m, c);
       case 2: return torsion_term<double>(D, D.d, x, m, c);
       case 3: return pair_term<double>(D, D.d, x, m, c);
@@ -845,6 +881,123 @@ __device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, doub
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
   return e + D.e_zero;
+}
+
+// ---------------------------------------------------------------------------
+// Derivatives for the adjoint (plain form only; bonds, angles, torsions and
+// NCI pairs).
+// ---------------------------------------------------------------------------
+
+// Gradient value and tangent (H w) of one bead in shared memory.
+struct GradDual {
+  double* g;
+  double* h;
+  __device__ inline void add(int i, const Dual& v) {
+    g[i] += v.v;
+    h[i] += v.d;
+  }
+};
+
+__device__ inline Dual term_dual(const Dev& D, int kind, const BeadPos& x, int m, Contrib<Dual>& c) {
+  switch (kind) {
+    case 0: return bond_plain<Dual>(D, D.d, x, m, c);
+    case 1: return angle_term<Dual>(D, D.d, x, m, c);
+    case 2: return torsion_term<Dual>(D, D.d, x, m, c);
+    default: return pair_term<Dual>(D, D.d, x, m, c);
+  }
+}
+
+// The plain form's schedule (sched[0]) with dual coordinates.
+template <int KIND, int NA>
+__device__ inline void kind_batches_dual(const Dev& D, const BeadPos& X, GradDual& G, Dual& es, int lane) {
+  const Schedule& S = D.sched[0];
+  const int b0 = S.boff[KIND], nb = S.nb[KIND];
+  for (int b = b0; b < b0 + nb; ++b) {
+    const int m = S.slot[32 * b + lane];
+    const int col = S.color[32 * b + lane];
+    const int ncol = S.ncol[b];
+    Contrib<Dual> c;
+    if (m >= 0) es += term_dual(D, KIND, X, m, c);
+    for (int k = 0; k < ncol; ++k) {
+      if (m >= 0 && col == k) {
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) G.add(3 * c.a[a] + d, c.g[a][d]);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Shared memory per warp of warp_hvp: x, w, gradient, H w (3n doubles each).
+__host__ __device__ inline size_t warp_hvp_smem_bytes(int n) { return (size_t)12 * n * sizeof(double); }
+
+// Energy (with E_zero), gradient and Hessian-vector product H w of one bead
+// by one warp.  ws: the warp's shared memory holding x (3n doubles) then w
+// (3n doubles).  dew receives the directional derivative w . grad E.
+__device__ inline double warp_hvp(const Dev& D, double* ws, double* gout, double* hout, double& dew, int lane) {
+  const int n3 = 3 * D.n;
+  double* xs = ws;
+  double* w = ws + n3;
+  GradDual G{w + n3, w + 2 * n3};
+  for (int a = lane; a < n3; a += 32) {
+    G.g[a] = 0.0;
+    G.h[a] = 0.0;
+  }
+  __syncwarp();
+  BeadPos X{xs, nullptr, nullptr, w};
+  Dual es(0.0);
+  kind_batches_dual<0, 2>(D, X, G, es, lane);
+  kind_batches_dual<1, 3>(D, X, G, es, lane);
+  kind_batches_dual<2, 4>(D, X, G, es, lane);
+  kind_batches_dual<3, 2>(D, X, G, es, lane);
+  for (int a = lane; a < n3; a += 32) {
+    if (gout) gout[a] = G.g[a];
+    hout[a] = G.h[a];
+  }
+  double e = es.v, de = es.d;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    de += __shfl_xor_sync(0xffffffffu, de, o);
+  }
+  dew = de;
+  return e + D.e_zero;
+}
+
+// Linear parameters of the force field (the loss gradients of the adjoint are
+// taken with respect to these): bond force constant k (vbond[1]), angle force
+// constant k (vangl[1]), torsion barrier V (vtors[1]) and the NCI pair's
+// Coulomb product qq (vpair[6]: eps1 q_i q_j, or q_i q_j in the Zahn form).
+// Every term is linear in its parameter, so d/dtheta_t (v . grad E) is v .
+// grad E_t evaluated with theta_t = 1; the tables U hold the parameters with
+// those entries set to 1 (and, for pairs, eps2 = 0: Coulomb only).
+// Per term, out receives alpha * (v . grad E_t|unit) + beta * E_t|unit.
+__device__ inline void warp_param_vjp(const Dev& D, const Tables<double>& U, const double* xs, const double* vs,
+                                      double alpha, double beta, double* out, int lane) {
+  const BeadPos X{xs, nullptr, nullptr, nullptr};
+  int off = 0;
+#pragma unroll 1
+  for (int kind = 0; kind < 4; ++kind) {
+    const int nt = D.nterm[kind];
+    for (int m = lane; m < nt; m += 32) {
+      Contrib<double> c;
+      double e;
+      switch (kind) {
+        case 0: e = bond_plain<double>(D, U, X, m, c); break;
+        case 1: e = angle_term<double>(D, U, X, m, c); break;
+        case 2: e = torsion_term<double>(D, U, X, m, c); break;
+        default: e = pair_term<double>(D, U, X, m, c); break;
+      }
+      double s = 0.0;
+      for (int a = 0; a < c.na; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) s += vs[3 * c.a[a] + d] * c.g[a][d];
+      out[off + m] = alpha * s + beta * e;
+    }
+    off += nt;
+  }
 }
 
 }  // namespace qmdff

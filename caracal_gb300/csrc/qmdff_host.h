@@ -15,6 +15,7 @@ struct cr_qmdff {
   cr::qmdff::Dev dev{};
   std::vector<void*> allocs;    // device buffers owned by the force field
   int variant[2] = {-1, -1};    // autotuned kernel variant per form (FP64, mixed); -1: not yet
+  cr::qmdff::Tables<double> unit{};  // linear parameters set to 1 (parameter gradients)
   float tune_ms[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 };
 
@@ -24,6 +25,18 @@ constexpr int kQmdffWarps = 4;
 // e[b] (with E_zero) and g = dV/dq for nbeads beads of d_q(3, n, nbeads).
 int qmdff_launch(const cr_qmdff* ff, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
                  cudaStream_t s);
+
+// Plain-form derivatives for the adjoint (bonds, angles, torsions, NCI pairs):
+// energy, gradient and H w per bead (d_e, d_g, d_dew may be NULL) ...
+int qmdff_hvp_launch(const cr_qmdff* ff, const double* d_q, const double* d_w, int nbeads, double* d_e, double* d_g,
+                     double* d_hw, double* d_dew, cudaStream_t s);
+// ... and d_acc[t] += scale * sum_b (alpha_b v_b . grad E_t|unit + beta_b E_t|unit)
+// over the linear parameters t (bond k, angle k, torsion V, pair qq; count
+// qmdff_nlin); d_scratch holds scratch_beads * nlin doubles.
+int qmdff_vjp_launch(const cr_qmdff* ff, const double* d_q, const double* d_v, int nbeads, const double* d_alpha,
+                     const double* d_beta, double scale, double* d_scratch, int scratch_beads, double* d_acc,
+                     cudaStream_t s);
+int qmdff_nlin(const cr_qmdff* ff);
 
 // dE-EVB of two force fields (csrc/evb.cu): e, g <- EVB energy and gradient;
 // e2, g2 are scratch of the same sizes for the second force field.

@@ -131,6 +131,34 @@ class QMDFFForceField:
                 "cr_qmdff_egrad")
         return e, g
 
+    @property
+    def nparams(self):
+        """Number of linear parameters (bond k, angle k, torsion V, pair qq)."""
+        n = C.c_int()
+        L.check(L.lib().cr_qmdff_nparams(self._h, C.byref(n)), "cr_qmdff_nparams")
+        return n.value
+
+    def hvp(self, xyz, w):
+        """Energies, gradients and Hessian-vector products H w (plain FP64)."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, self.n, 3)
+        w = np.ascontiguousarray(w, dtype=np.float64).reshape(x.shape)
+        e = np.zeros(x.shape[0])
+        g = np.zeros_like(x)
+        hw = np.zeros_like(x)
+        L.check(L.lib().cr_qmdff_hvp(self._h, L.dptr(x), L.dptr(w), x.shape[0], L.dptr(e), L.dptr(g), L.dptr(hw)),
+                "cr_qmdff_hvp")
+        return e, g, hw
+
+    def param_vjp(self, xyz, v):
+        """d/dtheta sum_b v_b . grad E(xyz_b) over the linear parameters
+        (bond k, angle k, torsion V, pair qq, in that order)."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, self.n, 3)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(x.shape)
+        grad = np.zeros(self.nparams)
+        L.check(L.lib().cr_qmdff_param_vjp(self._h, L.dptr(x), L.dptr(v), x.shape[0], L.dptr(grad)),
+                "cr_qmdff_param_vjp")
+        return grad
+
     def schedule_info(self):
         b = np.zeros(5, dtype=np.int32)
         c = C.c_int()

@@ -163,6 +163,23 @@ int cr_qmdff_create(const cr_qmdff_def* def, cr_qmdff** out);
 int cr_qmdff_destroy(cr_qmdff* ff);
 /* Host arrays xyz(3,natoms,nbeads) -> e(nbeads) (with E_zero), g(3,natoms,nbeads). */
 int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
+
+/* Derivatives for parameter fitting and adjoints (plain FP64 form; force
+ * fields without H/halogen bonds, else CR_ERR_UNSUPPORTED).  No reference
+ * counterpart: Caracal fits EVB couplings by finite differences (fdjac2) and
+ * has no QMDFF force-constant gradients.
+ * Linear parameters, in this order (count from cr_qmdff_nparams): bond force
+ * constants k (vbond(2,:) of src/qmdff.f90), angle force constants (vangl(2,:)),
+ * torsion barriers V (vtors(2,:)), NCI pair Coulomb products qq (eps1 q_i q_j,
+ * or q_i q_j in the Zahn form).  Every term of ff_eg/ff_nonb is linear in its
+ * parameter. */
+int cr_qmdff_nparams(const cr_qmdff* ff, int* nlin);
+/* hw[b] = Hessian of E at xyz[b] times w[b] (forward-mode dual numbers on the
+ * term formulas); e, g (may be NULL) as cr_qmdff_egrad. */
+int cr_qmdff_hvp(cr_qmdff* ff, const double* xyz, const double* w, int nbeads, double* e, double* g, double* hw);
+/* grad[t] = d/dtheta_t sum_b v[b] . grad E(xyz[b]): the parameter gradient of
+ * a force-matching loss with v = -dL/dF. */
+int cr_qmdff_param_vjp(cr_qmdff* ff, const double* xyz, const double* v, int nbeads, double* grad);
 /* Same on device-resident arrays; stream may be 0. */
 int cr_qmdff_egrad_device(cr_qmdff* ff, const double* d_xyz, int nbeads, double* d_e, double* d_g,
                           int precision, void* stream);
@@ -338,6 +355,23 @@ int cr_batch_run(cr_batch* b, int nsteps);
  * device time in ms */
 int cr_batch_info(const cr_batch* b, long long* launches, int* graph_nodes, float* ms);
 int cr_batch_destroy(cr_batch* b);
+
+/* ---- adjoint of the step (parameter fitting through trajectories) --------
+ * No reference counterpart.  For a QMDFF engine in the plain FP64 form with
+ * NVE steps (thermostat CR_THERMO_NONE, transrot 0): cr_adjoint_forward runs
+ * nsteps steps from the engine's current state, keeping (q, p, dV/dq) every
+ * `every` steps; cr_adjoint_backward takes dL/dq and dL/dp of a loss of the
+ * final state (host arrays shaped like the state) and returns dL/dtheta over
+ * the force field's linear parameters (order of cr_qmdff_param_vjp) and,
+ * if not NULL, dL/dq and dL/dp of the initial state.  Each segment's
+ * positions are recomputed from its checkpoint; the engine ends in its state
+ * after the forward run. */
+typedef struct cr_adjoint cr_adjoint;
+int cr_adjoint_create(cr_engine* e, int nsteps, int every, cr_adjoint** out);
+int cr_adjoint_forward(cr_adjoint* a);
+int cr_adjoint_backward(cr_adjoint* a, const double* dl_dq, const double* dl_dp, double* grad, double* dl_dq0,
+                        double* dl_dp0);
+int cr_adjoint_destroy(cr_adjoint* a);
 
 #ifdef __cplusplus
 }
