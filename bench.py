@@ -684,6 +684,105 @@ def run_classes(args):
         dist.destroy_process_group()
 
 
+def run_adjoint(args):
+    """Derivative workloads on the synthetic C20H42 QMDFF:
+    (1) force matching over 8192 bead geometries sampled from thermal RPMD
+        trajectories (128 x 64 beads after 100 steps): loss and dL/dtheta over
+        the bond, angle, torsion and charge parameters, plus the EVB coupling
+        and first-force-field gradient of the dE-EVB pair;
+    (2) the adjoint of a 200-step NVE trajectory (P=16, 64 trajectories,
+        checkpoints every 20 steps).
+    Timed on the device clock around the C-ABI calls (host arrays in and out)."""
+    import torch
+    from caracal_gb300 import qmdff as Q
+    from caracal_gb300.engine import EVBPair, QMDFFForceField
+    from caracal_gb300.fit import QMDFFParams, TrajectoryAdjoint, trajectory_engine
+    from caracal_gb300 import workloads as Wk
+
+    rank, ws, dist = dist_setup()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    K, W = args.steps, args.warmup
+    wl = Wk.qmdff_config(ntraj=128, nbeads=64)
+    eng = make_engine(wl, "fp64", traj0=rank * wl.ntraj)
+    eng.run(100)
+    q, _, _, _, _ = eng.get_state()
+    eng.close()
+    x = q.reshape(-1, len(wl.mass), 3)
+    ff = wl.extra["ff"]
+    params = QMDFFParams(ff)
+    gff = wl.extra["gpu_ff"]
+    _, g_ref = gff.egrad(x)
+    theta = params.theta() * np.random.default_rng(7).uniform(0.9, 1.1, params.size)
+    f1 = QMDFFForceField(params.with_theta(theta))
+    ff2 = QMDFFForceField(Q.alkane_evb_partner(ff))
+    pair = EVBPair(f1, ff2, "1g", a=0.01, b=50.0)
+
+    def fm_step():
+        _, g = f1.egrad(x)
+        G = x.shape[0]
+        v = (2.0 / G) * (g - g_ref)
+        raw = f1.param_vjp(x, v)
+        return float(np.sum((g - g_ref) ** 2) / G), params.chain(raw, theta)
+
+    def evb_step():
+        _, g = pair.egrad(x)
+        return pair.param_vjp(x, (2.0 / x.shape[0]) * (g - g_ref))
+
+    def timed(fn, n):
+        for _ in range(W):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            out = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / n, out
+
+    t_fm, (loss, grad) = timed(fm_step, K)
+    t_evb, _ = timed(evb_step, K)
+
+    # trajectory adjoint
+    mass = wl.mass
+    P, T, nst, every = 16, 64, 200, 20
+    rng = np.random.default_rng(11)
+    shape = (T, P, len(mass), 3)
+    q0 = ff.xyz[None, None] + rng.normal(0.0, 0.02, shape)
+    p0 = rng.normal(0.0, 1.0, shape) * np.sqrt(mass[None, None, :, None] * P / wl.beta)
+    e_t, g_t = trajectory_engine(params, theta, mass, P, T, wl.dt_au, wl.beta, q0, p0)
+    adj = TrajectoryAdjoint(e_t, nst, every)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    adj.forward()
+    t1 = time.perf_counter()
+    qk, _, _, _, _ = e_t.get_state()
+    raw, _, _ = adj.backward(qk - q0, np.zeros(shape))
+    t2 = time.perf_counter()
+    adj.close()
+    e_t.close()
+    g_t.close()
+    line = {
+        "metric": "geometries/s (force-matching loss + parameter gradient)", "value": x.shape[0] / t_fm,
+        "unit": "geometries/s", "n_gpus": ws, "steps": K, "warmup": W, "ms_per_step": t_fm * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "adjoint_c20h42", "geometries": int(x.shape[0]), "params": int(params.size),
+                   "trajectory": {"nbeads": P, "ntraj": T, "steps": nst, "checkpoint_every": every}},
+        "force_matching": {"loss": loss, "grad_norm": float(np.linalg.norm(grad)), "s_per_eval": t_fm},
+        "evb_force_matching": {"geometries_per_s": x.shape[0] / t_evb, "basis": "1g"},
+        "trajectory_adjoint": {"forward_s": t1 - t0, "backward_s": t2 - t1,
+                               "bead_steps_per_s_backward": P * T * nst / (t2 - t1),
+                               "backward_over_forward": (t2 - t1) / (t1 - t0)},
+        "e2e": {"value": x.shape[0] / t_fm, "unit": "geometries/s", "h2d_bytes_per_step": int(2 * x.nbytes),
+                "d2h_bytes_per_step": int(x.nbytes + 8 * params.size)},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    for o in (pair, f1, ff2, gff):
+        o.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -695,7 +794,8 @@ def main():
                          "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16), "
                          "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (512 x 64), "
                          "classes (H3 4096x8, CH4H 2048x32, CH4OH 512x64, QMDFF 128x128 in one batch), "
-                         "classes_small (the same with 1/16 of the trajectories)")
+                         "classes_small (the same with 1/16 of the trajectories), "
+                         "adjoint (force matching over 8192 C20H42 geometries and a 200-step trajectory adjoint)")
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-steps-per-sample", type=int, default=20)
@@ -706,6 +806,13 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "adjoint":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "Caracal has no parameter gradients of "
+                              "QMDFF losses (its EVB fit uses finite differences only)"}))
+        else:
+            run_adjoint(args)
+        return
     if args.workload in ("classes", "classes_small"):
         if args.impl == "reference":
             reference_classes(args)

@@ -136,6 +136,8 @@ def _sig(lib):
         "cr_qmdff_hvp": ([v, d, d, C.c_int, d, d, d], C.c_int),
         "cr_qmdff_param_vjp": ([v, d, d, C.c_int, d], C.c_int),
         "cr_evb_fit": ([C.c_int, d, C.c_int, C.c_int, d, d, d, d, d], C.c_int),
+        "cr_evb_fit_grad": ([C.c_int, d, C.c_int, C.c_int, d, d, d, d], C.c_int),
+        "cr_evb_param_vjp": ([v, d, d, C.c_int, d, d], C.c_int),
         "cr_adjoint_create": ([v, C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
         "cr_adjoint_forward": ([v], C.c_int),
         "cr_adjoint_backward": ([v, d, d, d, d, d], C.c_int),

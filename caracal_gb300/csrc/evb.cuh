@@ -8,6 +8,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "dual.cuh"
+
 namespace cr {
 namespace evb {
 
@@ -19,61 +21,70 @@ struct Coupling {
 };
 
 // V12(dE) and the factor K such that Caracal's deldiscr = K * (g1 - g2).
-__host__ __device__ inline void coupling(const Coupling& C, double ediff, double& offdiag, double& K) {
-  const double e2 = ediff * ediff;
-  switch (C.basis) {
+// p = (a, b, c, d, e, f, g, h, m, n); T is double or a dual number
+// (parameter gradients).
+template <class T>
+__host__ __device__ inline void coupling_t(int basis, const T* p, T ediff, T& offdiag, T& K) {
+  const T e2 = ediff * ediff;
+  const T &a = p[0], &b = p[1], &c = p[2], &d = p[3], &e = p[4], &f = p[5], &g = p[6], &h = p[7], &m = p[8], &n = p[9];
+  switch (basis) {
     case CONST:
-      offdiag = C.a;
+      offdiag = a;
       K = ediff;
       break;
     case G1:
-      offdiag = C.a * exp(-C.b * e2);
-      K = ediff * (1.0 - 2.0 * (4.0 * offdiag * offdiag) * C.b);
+      offdiag = a * exp(-b * e2);
+      K = ediff * (1.0 - 2.0 * (4.0 * offdiag * offdiag) * b);
       break;
     case G2: {
-      const double x1 = exp(-C.b * e2), x2 = exp(-C.d * (ediff + C.m) * (ediff + C.m));
-      offdiag = C.a * x1 + C.c * x2;
-      K = 1.0 * ediff + 4.0 * offdiag * (-2.0 * C.a * C.b * ediff * x1 - 2.0 * C.c * C.d * (C.m + ediff) * x2);
+      const T x1 = exp(-b * e2), x2 = exp(-d * (ediff + m) * (ediff + m));
+      offdiag = a * x1 + c * x2;
+      K = 1.0 * ediff + 4.0 * offdiag * (-2.0 * a * b * ediff * x1 - 2.0 * c * d * (m + ediff) * x2);
       break;
     }
     case G3: {
-      const double x1 = exp(-C.b * e2), x2 = exp(-C.d * (ediff + C.m) * (ediff + C.m));
-      const double x3 = exp(-C.f * (ediff + C.n) * (ediff + C.n));
-      offdiag = C.a * x1 + C.c * x2 + C.e * x3;
+      const T x1 = exp(-b * e2), x2 = exp(-d * (ediff + m) * (ediff + m));
+      const T x3 = exp(-f * (ediff + n) * (ediff + n));
+      offdiag = a * x1 + c * x2 + e * x3;
       K = 1.0 * ediff + 4.0 * offdiag *
-                            (-2.0 * C.a * C.b * ediff * x1 - 2.0 * C.c * C.d * (C.m + ediff) * x2 -
-                             2.0 * C.e * C.f * (C.n + ediff) * x3);
+                            (-2.0 * a * b * ediff * x1 - 2.0 * c * d * (m + ediff) * x2 -
+                             2.0 * e * f * (n + ediff) * x3);
       break;
     }
     case SP: {
-      const double x1 = exp(-C.b * e2), x2 = exp(-C.d * e2);
-      offdiag = C.a * x1 + C.c * ediff * x2;
-      K = 1.0 * ediff + 4.0 * offdiag * (-2.0 * C.a * C.b * ediff * x1 + C.c * (1.0 - 2.0 * e2 * C.d) * x2);
+      const T x1 = exp(-b * e2), x2 = exp(-d * e2);
+      offdiag = a * x1 + c * ediff * x2;
+      K = 1.0 * ediff + 4.0 * offdiag * (-2.0 * a * b * ediff * x1 + c * (1.0 - 2.0 * e2 * d) * x2);
       break;
     }
     case SD: {
-      const double x1 = exp(-C.b * e2), x2 = exp(-C.d * e2);
-      offdiag = C.a * x1 + C.c * e2 * x2;
-      K = 1.0 * ediff + 4.0 * offdiag * (-2.0 * C.a * C.b * ediff * x1 + C.c * (2.0 * ediff - 2.0 * e2 * ediff * C.d) * x2);
+      const T x1 = exp(-b * e2), x2 = exp(-d * e2);
+      offdiag = a * x1 + c * e2 * x2;
+      K = 1.0 * ediff + 4.0 * offdiag * (-2.0 * a * b * ediff * x1 + c * (2.0 * ediff - 2.0 * e2 * ediff * d) * x2);
       break;
     }
     case SD2: {
-      const double x1 = exp(-C.b * e2), x2 = exp(-C.d * e2), x3 = exp(-C.f * e2);
-      offdiag = C.a * x1 + C.c * e2 * x2 + C.e * e2 * x3;
+      const T x1 = exp(-b * e2), x2 = exp(-d * e2), x3 = exp(-f * e2);
+      offdiag = a * x1 + c * e2 * x2 + e * e2 * x3;
       K = 1.0 * ediff + 4.0 * offdiag *
-                            (-2.0 * C.a * C.b * ediff * x1 + C.c * (2.0 * ediff - 2.0 * e2 * ediff * C.d) * x2 +
-                             C.e * (2.0 * ediff - 2.0 * e2 * ediff * C.f) * x3);
+                            (-2.0 * a * b * ediff * x1 + c * (2.0 * ediff - 2.0 * e2 * ediff * d) * x2 +
+                             e * (2.0 * ediff - 2.0 * e2 * ediff * f) * x3);
       break;
     }
     default: {  // SP2D
-      const double x1 = exp(-C.b * e2), x2 = exp(-C.d * e2), x3 = exp(-C.f * e2), x4 = exp(-C.h * e2);
-      offdiag = C.a * x1 + C.c * ediff * x2 + C.e * ediff * x3 + e2 * C.g * x4;
+      const T x1 = exp(-b * e2), x2 = exp(-d * e2), x3 = exp(-f * e2), x4 = exp(-h * e2);
+      offdiag = a * x1 + c * ediff * x2 + e * ediff * x3 + e2 * g * x4;
       K = 1.0 * ediff + 4.0 * offdiag *
-                            (-2.0 * C.a * C.b * ediff * x1 + C.c * (1.0 - 2.0 * e2 * C.d) * x2 +
-                             C.e * (1.0 - 2.0 * e2 * C.f) * x3 + C.g * (2.0 * ediff - 2.0 * e2 * ediff * C.h) * x4);
+                            (-2.0 * a * b * ediff * x1 + c * (1.0 - 2.0 * e2 * d) * x2 +
+                             e * (1.0 - 2.0 * e2 * f) * x3 + g * (2.0 * ediff - 2.0 * e2 * ediff * h) * x4);
       break;
     }
   }
+}
+
+__host__ __device__ inline void coupling(const Coupling& C, double ediff, double& offdiag, double& K) {
+  const double p[10] = {C.a, C.b, C.c, C.d, C.e, C.f, C.g, C.h, C.m, C.n};
+  coupling_t<double>(C.basis, p, ediff, offdiag, K);
 }
 
 // One warp per bead: e[b] <- EVB energy, g[b] <- EVB gradient (g1 in place).

@@ -216,6 +216,19 @@ class EVBPair:
         L.check(L.lib().cr_evb_egrad(self._h, L.dptr(x), x.shape[0], L.dptr(e), L.dptr(g), prec), "cr_evb_egrad")
         return e, g
 
+    def param_vjp(self, xyz, v, ff1=True):
+        """d/dc sum_b v_b . grad E_EVB(xyz_b) over the coupling parameters
+        (dict a..h, m, n) and, with ff1, over the first force field's linear
+        parameters (plain FP64)."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, self.n, 3)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(x.shape)
+        gc = np.zeros(10)
+        gf = np.zeros(max(self.ff1.nparams, 1)) if ff1 else None
+        L.check(L.lib().cr_evb_param_vjp(self._h, L.dptr(x), L.dptr(v), x.shape[0], L.dptr(gc),
+                                         L.dptr(gf) if ff1 else None), "cr_evb_param_vjp")
+        out = dict(zip("abcdefghmn", gc))
+        return (out, gf[:self.ff1.nparams]) if ff1 else out
+
     def close(self):
         if getattr(self, "_h", None):
             L.lib().cr_evb_destroy(self._h)
@@ -243,6 +256,16 @@ def evb_fit(basis, x, e1, e2, eref, jacobian=True):
     L.check(L.lib().cr_evb_fit(FIT_BASES[basis], L.dptr(x), len(x), m, L.dptr(e1), L.dptr(e2), L.dptr(eref),
                                L.dptr(fvec), L.dptr(fjac) if jacobian else None), "cr_evb_fit")
     return (fvec, fjac) if jacobian else fvec
+
+
+def evb_fit_grad(basis, x, e1, e2, eref):
+    """Analytic gradient of sum_i fvec_i of the dE-EVB fit (device, dual numbers)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    e1, e2, eref = (np.ascontiguousarray(a, dtype=np.float64) for a in (e1, e2, eref))
+    grad = np.zeros(len(x))
+    L.check(L.lib().cr_evb_fit_grad(FIT_BASES[basis], L.dptr(x), len(x), len(e1), L.dptr(e1), L.dptr(e2),
+                                    L.dptr(eref), L.dptr(grad)), "cr_evb_fit_grad")
+    return grad
 
 
 class RPMDEngine:

@@ -236,6 +236,17 @@ int cr_evb_egrad(cr_evb* evb, const double* xyz, int nbeads, double* e, double* 
 #define CR_FIT_SP2D3 8
 int cr_evb_fit(int basis, const double* x, int npar, int m, const double* e1, const double* e2, const double* eref,
                double* fvec, double* fjac);
+/* grad[j] = d/dx_j sum_i fvec_i: the analytic gradient of the fit loss (dual
+ * numbers), against which the fdjac2 columns summed over the points are the
+ * reference's finite-difference counterpart. */
+int cr_evb_fit_grad(int basis, const double* x, int npar, int m, const double* e1, const double* e2,
+                    const double* eref, double* grad);
+/* Parameter gradient of sum_b v[b] . grad E_EVB(xyz[b]) (a force-matching loss
+ * with v = -dL/dF), plain FP64: grad_coupling[10] over the coupling
+ * parameters a..h, m, n of cr_evb_def, and, if grad_ff1 is not NULL, over the
+ * first force field's linear parameters (order of cr_qmdff_param_vjp). */
+int cr_evb_param_vjp(cr_evb* evb, const double* xyz, const double* v, int nbeads, double* grad_coupling,
+                     double* grad_ff1);
 
 /* ---- RPMD engine -----------------------------------------------------------
  * Replaces the stepping loop of `dynamic` (src/dynamic.f90:1569-1579) around

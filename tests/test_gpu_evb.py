@@ -85,3 +85,68 @@ def test_evb_fit_matches_oracle(require_gpu, basis):
         hj = np.sqrt(np.finfo(float).eps) * abs(x[j])
         noise = 1e-15 * np.max(np.abs(eref)) ** 2 / hj
         assert np.max(np.abs(fj[j] - fjo[j])) <= 1e-10 * np.max(np.abs(fjo[j])) + noise
+
+
+@pytest.mark.parametrize("basis", ["1g", "2g", "sp", "sp2d3"])
+def test_evb_fit_gradient_matches_fdjac2(require_gpu, basis):
+    """The analytic fit gradient against the reference's own route: MINPACK
+    fdjac2 columns (forward differences) summed over the points, and central
+    differences of the loss."""
+    from caracal_gb300.engine import evb_fit_grad
+    from test_oracle_evb import FIT, fit_data
+    e1, e2, eref = fit_data(m=2048)
+    x = np.asarray(FIT[basis])
+    grad = evb_fit_grad(basis, x, e1, e2, eref)
+    _, fjac = orc.evb_fit(basis, x, e1, e2, eref)
+    fd2 = fjac.sum(axis=1)
+    for j in range(len(x)):
+        hj = np.sqrt(np.finfo(float).eps) * abs(x[j])
+        noise = 1e-15 * np.max(np.abs(eref)) ** 2 / hj * len(e1)
+        assert abs(grad[j] - fd2[j]) <= 1e-5 * abs(grad[j]) + noise
+        h = 1e-6 * abs(x[j])
+        xp, xm = x.copy(), x.copy()
+        xp[j] += h
+        xm[j] -= h
+        cd = (orc.evb_fit(basis, xp, e1, e2, eref, jacobian=False).sum() -
+              orc.evb_fit(basis, xm, e1, e2, eref, jacobian=False).sum()) / (2 * h)
+        assert abs(grad[j] - cd) <= 1e-7 * abs(grad[j]) + noise
+
+
+@pytest.mark.parametrize("basis", ["1g", "sp"])
+def test_evb_param_vjp_matches_finite_differences(fields, basis):
+    from caracal_gb300.fit import QMDFFParams
+    ff, ff2, g1, g2 = fields
+    par = dict(BASES[basis])
+    x = ff.xyz[None] + np.random.default_rng(61).normal(0, 0.05, (12,) + ff.xyz.shape)
+    v = np.random.default_rng(62).normal(0, 1.0, x.shape)
+    pair = EVBPair(g1, g2, basis, **par)
+    gc, gf = pair.param_vjp(x, v)
+    pair.close()
+
+    def S_coupling(p):
+        pr = EVBPair(g1, g2, basis, **p)
+        _, g = pr.egrad(x)
+        pr.close()
+        return float(np.sum(v * g))
+    for k in ("a", "b"):
+        h = 1e-6 * abs(par[k])
+        pp, pm = dict(par), dict(par)
+        pp[k] += h
+        pm[k] -= h
+        fd = (S_coupling(pp) - S_coupling(pm)) / (2 * h)
+        assert abs(fd - gc[k]) <= 1e-6 * abs(fd) + 1e-12
+    params = QMDFFParams(ff)
+    theta = params.theta()
+    grad = params.chain(gf)
+
+    def S_ff1(th):
+        f1 = QMDFFForceField(params.with_theta(th))
+        pr = EVBPair(f1, g2, basis, **par)
+        _, g = pr.egrad(x)
+        pr.close()
+        f1.close()
+        return float(np.sum(v * g))
+    d = np.random.default_rng(63).normal(0, 1.0, theta.shape) * np.abs(theta)
+    h = 1e-6
+    fd = (S_ff1(theta + h * d) - S_ff1(theta - h * d)) / (2 * h)
+    assert abs(fd - grad @ d) <= 1e-6 * abs(fd)
