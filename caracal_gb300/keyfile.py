@@ -1,0 +1,203 @@
+"""Caracal's keyword input for `dynamic` (the subset on this engine's path).
+
+A key file is a list of lines; the first word of a line is the keyword
+(case-insensitive), the rest its values, and a line `NAME {` opens a block
+closed by `}`.  Read here, with Caracal's defaults and checks:
+
+  general (src/dynamic.f90:243-320): XYZSTART file, RPMD_BEADS n, ENSEMBLE NVE|NVT,
+    STEPS n, DELTAT dt_fs, TDUMP t_fs   (iwrite = nint(TDUMP / DELTAT))
+  NVT { TEMP K, THERMOSTAT ANDERSEN|NOSE-HOOVER, ANDERSEN_STEP n, NOSE_DAMP n }
+    (src/dynamic.f90:382-473; defaults TEMP 0, ANDERSEN_STEP 70, NOSE_DAMP 100)
+  PES ANA_H3 | ANA_CH4H | ANA_CH4OH | QMDFF | DE_EVB  (src/read_pes.f90:203)
+  QMDFF { FFNAMES file [file2], ESHIFT e1 [e2] }     (src/read_pes.f90:1760-1830)
+  DE_EVB { COUPLING basis }  with the parameters in evb_pars.dat
+    (src/read_pes.f90:1928-1975, 2557-2600)
+  E_CON (md_energies.dat), OUTPUT_SPARSE (no all-bead trajectory for P > 1)
+  and, for this engine only, GPU_TRAJECTORIES n (independent trajectories
+  stepped together; Caracal runs one) and SEED n.
+
+Keywords outside this subset are reported by `unsupported`; NPT, periodic
+boxes and the other surfaces are not on this engine's path.
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass, field
+
+ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh"}
+EVB_BASES = ("1g", "2g", "3g", "sp", "sd", "sd2", "sp2d")
+KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE",
+         "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "}"}
+
+
+class KeyError_(ValueError):
+    """A key file Caracal would stop on (its `fatal`)."""
+
+
+@dataclass
+class DynamicInput:
+    xyzstart: str = ""
+    nbeads: int = 1
+    ensemble: str = "NVE"
+    nstep: int = 0
+    dt_fs: float = 1.0
+    tdump_fs: float = 1.0
+    kelvin: float = 0.0
+    thermostat: str = "none"
+    andersen_step: int = 70
+    nose_damp: float = 100.0
+    pes: str = ""
+    ffnames: list = field(default_factory=list)
+    eshift: list = field(default_factory=list)
+    coupling: str = "1g"
+    ntraj: int = 1
+    seed: int = 0
+    energycon: bool = False      # E_CON: md_energies.dat (src/dynamic.f90:1130-1140)
+    output_sparse: bool = False  # OUTPUT_SPARSE: no all-bead trajectory (src/dynamic.f90:1145-1155)
+    unsupported: list = field(default_factory=list)
+    directory: str = "."
+
+    @property
+    def iwrite(self):
+        """Steps between trajectory frames: Fortran nint(TDUMP / DELTAT)."""
+        x = self.tdump_fs / self.dt_fs
+        return int(x + 0.5) if x >= 0 else -int(-x + 0.5)
+
+
+def _words(line):
+    return line.split()
+
+
+def _blocks(lines, name):
+    """Lines inside every `name {` ... `}` block."""
+    out = []
+    for i, ln in enumerate(lines):
+        head = ln.strip().upper().replace(" ", "")
+        if head == name + "{":
+            for ln2 in lines[i + 1:]:
+                w = _words(ln2)
+                if w and w[0] == "}":
+                    break
+                out.append(ln2)
+            else:
+                raise KeyError_(f"The {name} section has no second delimiter! (}})")
+    return out
+
+
+def parse(text, directory="."):
+    """DynamicInput from the text of a key file."""
+    lines = [ln.rstrip("\n") for ln in text.splitlines()]
+    d = DynamicInput(directory=directory)
+    inside = set()
+    for name in ("NVT", "NVE", "QMDFF", "DE_EVB", "NPT"):
+        for ln in _blocks(lines, name):
+            inside.add(ln)
+    for ln in lines:
+        w = _words(ln)
+        if not w or ln in inside:
+            continue
+        k = w[0].upper()
+        if k == "XYZSTART":
+            d.xyzstart = w[1]
+        elif k == "RPMD_BEADS":
+            d.nbeads = int(w[1])
+        elif k == "ENSEMBLE":
+            d.ensemble = w[1].upper()
+        elif k == "STEPS":
+            d.nstep = int(w[1])
+        elif k == "DELTAT":
+            d.dt_fs = float(w[1].replace("d", "e").replace("D", "E"))
+        elif k == "TDUMP":
+            d.tdump_fs = float(w[1].replace("d", "e").replace("D", "E"))
+        elif k == "PES":
+            d.pes = w[1].upper()
+        elif k == "GPU_TRAJECTORIES":
+            d.ntraj = int(w[1])
+        elif k == "SEED":
+            d.seed = int(w[1])
+        elif k == "E_CON":
+            d.energycon = True
+        elif k == "OUTPUT_SPARSE":
+            d.output_sparse = True
+        elif k.rstrip("{") not in KNOWN and not k.startswith("#") and not k.startswith("!"):
+            d.unsupported.append(k)
+    # checks of src/dynamic.f90:290-320
+    if d.nbeads < 1:
+        raise KeyError_("The number of RPMD beads must be positive!")
+    if d.ensemble not in ("NVE", "NVT", "NPT"):
+        raise KeyError_("No valid thermodynamic ensemble given! Choose either NVE, NVT or NPT.")
+    if d.ensemble == "NPT":
+        raise KeyError_("NPT (barostat, periodic box) is not on this engine's path")
+    if d.nstep < 1:
+        raise KeyError_("The number of MD timesteps must be greater than zero!")
+    if d.dt_fs < 1e-5:
+        raise KeyError_("The MD timestep is too small to be useful!")
+    if d.ensemble == "NVT":
+        thermo = "none"
+        for ln in _blocks(lines, "NVT"):
+            w = _words(ln)
+            k = w[0].upper()
+            if k == "TEMP":
+                d.kelvin = float(w[1])
+            elif k == "THERMOSTAT":
+                thermo = w[1].upper()
+            elif k == "ANDERSEN_STEP":
+                d.andersen_step = int(w[1])
+            elif k == "NOSE_DAMP":
+                d.nose_damp = float(w[1])
+        if d.kelvin < 0.0:
+            raise KeyError_("Give a positive temperature!")
+        if thermo == "ANDERSEN":
+            d.thermostat = "andersen"
+        elif thermo == "NOSE-HOOVER":
+            d.thermostat = "nhc"
+        else:
+            raise KeyError_("No availiable thermostat was chosen! Add the keyword THERMOSTAT!")
+    if d.pes in ("QMDFF", "DE_EVB"):
+        for ln in _blocks(lines, "QMDFF"):
+            w = _words(ln)
+            k = w[0].upper()
+            if k == "FFNAMES":
+                d.ffnames = w[1:3] if d.pes == "DE_EVB" else w[1:2]
+            elif k == "ESHIFT":
+                d.eshift = [float(x.replace("d", "e").replace("D", "E")) for x in w[1:3]]
+        if not d.ffnames:
+            raise KeyError_("Please check the QMDFFNAMES keyword!")
+    if d.pes == "DE_EVB":
+        for ln in _blocks(lines, "DE_EVB"):
+            w = _words(ln)
+            if w[0].upper() == "COUPLING":
+                d.coupling = w[1] if w[1] in EVB_BASES else "1g"
+    if d.pes not in ANALYTIC and d.pes not in ("QMDFF", "DE_EVB"):
+        raise KeyError_(f"PES {d.pes or '(none)'} is not on this engine's path")
+    return d
+
+
+def read(path):
+    with open(path) as f:
+        return parse(f.read(), directory=os.path.dirname(os.path.abspath(path)))
+
+
+def read_xyz(path):
+    """(symbols, coordinates in Angstrom) of the first frame of an xyz file."""
+    with open(path) as f:
+        n = int(f.readline().split()[0])
+        f.readline()
+        sym, xyz = [], []
+        for _ in range(n):
+            w = f.readline().split()
+            sym.append(w[0])
+            xyz.append([float(x) for x in w[1:4]])
+    return sym, xyz
+
+
+def read_evb_pars(path, basis):
+    """Coupling parameters from evb_pars.dat in the order of
+    src/read_pes.f90:2565-2590 (a name line, then one value per line)."""
+    order = {"1g": "ab", "2g": "abcdm", "3g": "abcdefmn", "sp": "abcd", "sd": "abcd", "sd2": "abcdef",
+             "sp2d": "abcdefgh"}[basis]
+    with open(path) as f:
+        vals = [ln.split()[0] for ln in f.read().splitlines()[1:] if ln.split()]
+    if len(vals) < len(order):
+        raise KeyError_("The evb_pars.dat file contains too few lines or has a wrong formate!")
+    return {k: float(v.replace("d", "e").replace("D", "E")) for k, v in zip(order, vals)}

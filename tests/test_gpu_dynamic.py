@@ -1,0 +1,71 @@
+"""GPU: `python -m caracal_gb300.dynamic` on Caracal key files (H3, QMDFF,
+dE-EVB): the output files Caracal writes, and the written frames equal the
+engine's own state after the same steps."""
+import numpy as np
+import pytest
+
+from caracal_gb300 import RPMDEngine
+from caracal_gb300 import qmdff as Q
+from caracal_gb300.dynamic import run
+from caracal_gb300.units import BOHR_ANGSTROM, angstrom_to_bohr, beta_from_kelvin, dt_fs_to_au, mass_au
+from caracal_gb300.workloads import h3_collinear
+
+pytestmark = pytest.mark.gpu
+
+
+def frames(path):
+    lines = open(path).read().splitlines()
+    out, i = [], 0
+    while i < len(lines):
+        n = int(lines[i])
+        out.append(np.array([[float(v) for v in ln.split()[1:4]] for ln in lines[i + 2:i + 2 + n]]))
+        i += 2 + n
+    return out
+
+
+def test_dynamic_h3_nvt(require_gpu, tmp_path):
+    xyz = h3_collinear() * BOHR_ANGSTROM
+    (tmp_path / "start.xyz").write_text("3\n\n" + "".join(f"H {a} {b} {c}\n" for a, b, c in xyz))
+    (tmp_path / "dynamic.key").write_text(
+        "XYZSTART start.xyz\nRPMD_BEADS 4\nENSEMBLE NVT\nSTEPS 20\nDELTAT 0.1\nTDUMP 0.5\nPES ANA_H3\n"
+        "E_CON\nSEED 3\nNVT {\n TEMP 300\n THERMOSTAT ANDERSEN\n ANDERSEN_STEP 7\n}\n")
+    run(str(tmp_path / "dynamic.key"), out_dir=str(tmp_path), quiet=True)
+    tr = frames(tmp_path / "trajectory.xyz")
+    ce = frames(tmp_path / "traj_centroid.xyz")
+    en = [ln for ln in open(tmp_path / "md_energies.dat").read().splitlines()[1:]]
+    assert len(tr) == 4 and all(f.shape == (12, 3) for f in tr)
+    assert len(ce) == 4 and len(en) == 4
+    assert [int(r.split()[0]) for r in en] == [5, 10, 15, 20]
+    mass = [mass_au("H")] * 3
+    eng = RPMDEngine("h3", mass, 4, 1, dt_fs_to_au(0.1), beta=beta_from_kelvin(300.0), thermostat="andersen",
+                     andersen_step=7, transrot=True, seed=3)
+    eng.init_positions(angstrom_to_bohr(xyz), 0.0)
+    eng.init_momenta()
+    eng.compute_forces()
+    eng.run(20)
+    q, _, _, e, _ = eng.get_state()
+    assert np.allclose(tr[-1], q[0].reshape(-1, 3) * BOHR_ANGSTROM, rtol=1e-15, atol=1e-15)
+    assert np.allclose(ce[-1], q[0].mean(axis=0) * BOHR_ANGSTROM, rtol=1e-15, atol=1e-15)
+    assert float(en[-1].split()[1]) == pytest.approx(e[0] / 4, rel=1e-15)
+
+
+def test_dynamic_qmdff_and_evb(require_gpu, tmp_path):
+    ff = Q.alkane(nc=3)
+    ff2 = Q.alkane_evb_partner(ff)
+    Q.write_qmdff(ff, tmp_path / "a.qmdff")
+    Q.write_qmdff(ff2, tmp_path / "b.qmdff")
+    sym = ["C" if z == 6 else "H" for z in ff.at]
+    (tmp_path / "start.xyz").write_text(f"{ff.n}\n\n" + "".join(
+        f"{s} {a} {b} {c}\n" for s, (a, b, c) in zip(sym, ff.xyz * BOHR_ANGSTROM)))
+    base = "XYZSTART start.xyz\nRPMD_BEADS 2\nENSEMBLE NVT\nSTEPS 6\nDELTAT 0.5\nTDUMP 1.0\nE_CON\n" \
+           "NVT {\n TEMP 300\n THERMOSTAT ANDERSEN\n}\n"
+    (tmp_path / "q.key").write_text(base + "PES QMDFF\nQMDFF {\n FFNAMES a.qmdff\n ESHIFT -0.25\n}\n")
+    run(str(tmp_path / "q.key"), out_dir=str(tmp_path), quiet=True)
+    en = [ln.split() for ln in open(tmp_path / "md_energies.dat").read().splitlines()[1:]]
+    assert len(en) == 3 and all(np.isfinite(float(v)) for r in en for v in r)
+    assert float(en[0][1]) < -0.2        # E_zero from ESHIFT is in the energy
+    (tmp_path / "evb_pars.dat").write_text("1g\n0.01\n50.0\n")
+    (tmp_path / "e.key").write_text(base + "PES DE_EVB\nQMDFF {\n FFNAMES a.qmdff b.qmdff\n ESHIFT 0.0 0.02\n}\n"
+                                    "DE_EVB {\n COUPLING 1g\n}\n")
+    run(str(tmp_path / "e.key"), out_dir=str(tmp_path), quiet=True)
+    assert len(frames(tmp_path / "trajectory.xyz")) == 3

@@ -1,0 +1,76 @@
+"""CPU: Caracal's keyword input (dynamic) and the list-directed output format."""
+import pytest
+
+from caracal_gb300 import keyfile as K
+from caracal_gb300.dynamic import fortran_int, fortran_real
+
+KEY = """XYZSTART start.xyz
+RPMD_BEADS 8
+ENSEMBLE nvt
+STEPS 40
+DELTAT 0.1
+TDUMP 0.5
+PES ana_ch4h
+E_CON
+NVT {
+  TEMP 300
+  THERMOSTAT nose-hoover
+  NOSE_DAMP 50
+}
+"""
+
+
+def test_parse_dynamic_key():
+    d = K.parse(KEY)
+    assert (d.xyzstart, d.nbeads, d.ensemble, d.nstep) == ("start.xyz", 8, "NVT", 40)
+    assert d.dt_fs == 0.1 and d.tdump_fs == 0.5 and d.iwrite == 5
+    assert d.kelvin == 300.0 and d.thermostat == "nhc" and d.nose_damp == 50.0 and d.andersen_step == 70
+    assert d.pes == "ANA_CH4H" and d.energycon and not d.unsupported
+
+
+def test_defaults_and_nve():
+    d = K.parse("XYZSTART a.xyz\nSTEPS 10\nPES ANA_H3\n")
+    assert d.ensemble == "NVE" and d.nbeads == 1 and d.dt_fs == 1.0 and d.iwrite == 1
+    assert d.thermostat == "none"
+
+
+def test_fortran_nint_of_dump_interval():
+    assert K.parse("STEPS 1\nDELTAT 0.4\nTDUMP 1.0\nPES ANA_H3\n").iwrite == 3   # nint(2.5) = 3
+    assert K.parse("STEPS 1\nDELTAT 0.3\nTDUMP 1.0\nPES ANA_H3\n").iwrite == 3
+
+
+@pytest.mark.parametrize("text,msg", [
+    ("RPMD_BEADS 0\nSTEPS 1\nPES ANA_H3\n", "beads"),
+    ("ENSEMBLE NVX\nSTEPS 1\nPES ANA_H3\n", "ensemble"),
+    ("STEPS 0\nPES ANA_H3\n", "timesteps"),
+    ("STEPS 1\nDELTAT 1e-7\nPES ANA_H3\n", "too small"),
+    ("ENSEMBLE NVT\nSTEPS 1\nPES ANA_H3\nNVT {\n TEMP 300\n}\n", "THERMOSTAT"),
+    ("ENSEMBLE NVT\nSTEPS 1\nPES ANA_H3\nNVT {\n TEMP 300\n THERMOSTAT ANDERSEN\n", "delimiter"),
+    ("ENSEMBLE NPT\nSTEPS 1\nPES ANA_H3\n", "NPT"),
+    ("STEPS 1\nPES ANA_O3\n", "not on this engine"),
+    ("STEPS 1\nPES QMDFF\n", "QMDFFNAMES"),
+])
+def test_fatal_inputs(text, msg):
+    with pytest.raises(K.KeyError_, match=msg):
+        K.parse(text)
+
+
+def test_qmdff_and_evb_blocks(tmp_path):
+    text = ("STEPS 5\nPES de_evb\nQMDFF {\n FFNAMES a.qmdff b.qmdff\n ESHIFT -1.5 -1.4\n}\n"
+            "DE_EVB {\n COUPLING sp\n}\nGPU_TRAJECTORIES 64\nSEED 9\nBOGUS 1\n")
+    d = K.parse(text)
+    assert d.ffnames == ["a.qmdff", "b.qmdff"] and d.eshift == [-1.5, -1.4] and d.coupling == "sp"
+    assert d.ntraj == 64 and d.seed == 9 and d.unsupported == ["BOGUS"]
+    (tmp_path / "evb_pars.dat").write_text("sp\n0.01\n50.0\n0.02\n30.0\n")
+    assert K.read_evb_pars(str(tmp_path / "evb_pars.dat"), "sp") == dict(a=0.01, b=50.0, c=0.02, d=30.0)
+    with pytest.raises(K.KeyError_):
+        K.read_evb_pars(str(tmp_path / "evb_pars.dat"), "sp2d")
+
+
+def test_list_directed_numbers_round_trip():
+    for x in (1.0, -1.0, 0.5, 0.74, 12345.6789, 0.01, -3.2e-7, 1e20, 0.0, 2.0 / 3.0):
+        s = fortran_real(x)
+        assert len(s) == 26 and float(s) == x
+    assert fortran_real(1.0) == "   1.0000000000000000     "
+    assert fortran_real(0.01) == "   1.0000000000000000E-002"
+    assert fortran_int(48) == "          48"
