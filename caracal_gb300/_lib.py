@@ -142,6 +142,9 @@ def _sig(lib):
         "cr_adjoint_forward": ([v], C.c_int),
         "cr_adjoint_backward": ([v, d, d, d, d, d], C.c_int),
         "cr_adjoint_destroy": ([v], C.c_int),
+        "cr_engine_set_umbrella": ([eng, C.POINTER(CrRecross), d, d, C.c_int, C.c_double, C.c_double], C.c_int),
+        "cr_engine_umbrella_sampling": ([eng, C.c_int], C.c_int),
+        "cr_engine_umbrella_stats": ([eng, d, d, d, C.c_int], C.c_int),
         "cr_batch_create": ([C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
         "cr_batch_run": ([v, C.c_int], C.c_int),
         "cr_batch_info": ([v, C.POINTER(C.c_longlong), i, C.POINTER(C.c_float)], C.c_int),

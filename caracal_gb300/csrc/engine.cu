@@ -225,6 +225,9 @@ struct cr_engine {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   bool split_ready = false;  // split_prepare done
+  // umbrella windows (graph path, analytic surfaces)
+  double *d_umb = nullptr;   // [T] centres, [T] force constants, [T] xsum, [T] xsum2, [T][nbins] histogram
+  int* d_umb_flag = nullptr; // sampling switch
 };
 
 namespace {
@@ -430,6 +433,15 @@ int split_step_launches(cr_engine* e) {
   if (e->parent && (rc = parent_kernel(e, 0))) return rc;  // SHAKE (src/verlet.f90:746-757)
   rc = split_forces(e, e->d_V, e->d_f);
   if (rc) return rc;
+  if (e->sp.umbrella) {  // src/verlet.f90:1043-1046
+    switch (e->N) {
+      case 3: cr::split_umbrella_kernel<3><<<e->T, 64, 0, e->stream>>>(e->sp); break;
+      case 6: cr::split_umbrella_kernel<6><<<e->T, 64, 0, e->stream>>>(e->sp); break;
+      case 7: cr::split_umbrella_kernel<7><<<e->T, 64, 0, e->stream>>>(e->sp); break;
+      default: return fail(CR_ERR_UNSUPPORTED, "umbrella windows are built for the analytic surfaces");
+    }
+    CR_CUDA(cudaGetLastError());
+  }
   if (e->parent) {
     // 1/2 kick, RATTLE (src/verlet.f90:1080-1082), NHC, then Andersen / PILE
     cr::split_kick_kernel<<<grid, cr::kSplitBlock, 0, e->stream>>>(e->sp, 1);
@@ -968,6 +980,8 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_dxi);
   cudaFree(e->d_cq);
   cudaFree(e->d_shake_fail);
+  cudaFree(e->d_umb);
+  cudaFree(e->d_umb_flag);
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   if (e->ev0) cudaEventDestroy(e->ev0);
@@ -1231,6 +1245,70 @@ int cr_engine_set_parent(cr_engine* e, const cr_recross* rc) {
   rcode = parent_kernel(e, 2);
   if (rcode) return rcode;
   CR_CUDA(cudaStreamSynchronize(e->stream));
+  return CR_OK;
+}
+
+int cr_engine_set_umbrella(cr_engine* e, const cr_recross* rc, const double* centers, const double* kforce,
+                           int nbins, double lo, double hi) {
+  if (!e || !rc || !centers || !kforce) return fail(CR_ERR_ARG, "NULL argument");
+  if (e->ff || e->evb) return fail(CR_ERR_UNSUPPORTED, "umbrella windows are built for the analytic surfaces");
+  if (e->xi_on || e->parent) return fail(CR_ERR_ARG, "an umbrella engine cannot be a parent or recrossing children");
+  if (!(e->cfg.beta > 0.0) || !std::isfinite(e->cfg.beta)) return fail(CR_ERR_ARG, "umbrella sampling needs a temperature");
+  if (nbins < 0 || (nbins > 0 && !(hi > lo))) return fail(CR_ERR_ARG, "bad histogram range");
+  cr::XiDev x{};
+  int rcode = make_xidev(e, rc, x);
+  if (rcode) return rcode;
+  const size_t T = (size_t)e->T, nh = T * (size_t)nbins;
+  cudaFree(e->d_umb);
+  e->d_umb = nullptr;
+  CR_CUDA(cudaMalloc(&e->d_umb, (4 * T + nh + 1) * sizeof(double)));
+  if (!e->d_umb_flag) CR_CUDA(cudaMalloc(&e->d_umb_flag, sizeof(int)));
+  CR_CUDA(cudaMemcpy(e->d_umb, centers, T * 8, cudaMemcpyHostToDevice));
+  CR_CUDA(cudaMemcpy(e->d_umb + T, kforce, T * 8, cudaMemcpyHostToDevice));
+  CR_CUDA(cudaMemset(e->d_umb + 2 * T, 0, (2 * T + nh) * 8));
+  CR_CUDA(cudaMemset(e->d_umb_flag, 0, sizeof(int)));
+  cr::UmbrellaDev u{};
+  u.center = e->d_umb;
+  u.kforce = e->d_umb + T;
+  u.beta = e->cfg.beta;
+  u.sampling = e->d_umb_flag;
+  u.xsum = e->d_umb + 2 * T;
+  u.xsum2 = e->d_umb + 3 * T;
+  u.nbins = nbins;
+  u.lo = lo;
+  u.hi = hi;
+  u.hist = e->d_umb + 4 * T;
+  e->split = true;
+  e->sp.umbrella = 1;
+  e->sp.umb = u;
+  e->sp.xi = x;
+  if (e->graph_exec) {
+    cudaGraphExecDestroy(e->graph_exec);
+    e->graph_exec = nullptr;
+  }
+  if (e->graph) {
+    cudaGraphDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  return CR_OK;
+}
+
+int cr_engine_umbrella_sampling(cr_engine* e, int on) {
+  if (!e || !e->d_umb_flag) return fail(CR_ERR_ARG, "no umbrella windows on this engine");
+  const int v = on ? 1 : 0;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  CR_CUDA(cudaMemcpy(e->d_umb_flag, &v, sizeof(int), cudaMemcpyHostToDevice));
+  return CR_OK;
+}
+
+int cr_engine_umbrella_stats(cr_engine* e, double* xsum, double* xsum2, double* hist, int reset) {
+  if (!e || !e->d_umb) return fail(CR_ERR_ARG, "no umbrella windows on this engine");
+  const size_t T = (size_t)e->T, nh = T * (size_t)e->sp.umb.nbins;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  if (xsum) CR_CUDA(cudaMemcpy(xsum, e->d_umb + 2 * T, T * 8, cudaMemcpyDeviceToHost));
+  if (xsum2) CR_CUDA(cudaMemcpy(xsum2, e->d_umb + 3 * T, T * 8, cudaMemcpyDeviceToHost));
+  if (hist && nh) CR_CUDA(cudaMemcpy(hist, e->d_umb + 4 * T, nh * 8, cudaMemcpyDeviceToHost));
+  if (reset) CR_CUDA(cudaMemset(e->d_umb + 2 * T, 0, (2 * T + nh) * 8));
   return CR_OK;
 }
 

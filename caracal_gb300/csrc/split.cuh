@@ -28,9 +28,23 @@
 #include <cuda_runtime.h>
 
 #include "cr_common.cuh"
+#include "dual.cuh"
 #include "rpmd_kernel.cuh"
 
 namespace cr {
+
+// Umbrella windows (verlet with constrain = 0, src/umbrella.f90 mode 0).
+struct UmbrellaDev {
+  const double* center;  // [T] xi of each trajectory's window
+  const double* kforce;  // [T] force constant (Eh)
+  double beta;           // 1 / (k_B T) of the fs term
+  const int* sampling;   // device flag: 1 while the statistics are collected
+  double* xsum;          // [T] sum of xi over the sampled steps
+  double* xsum2;         // [T] sum of xi^2
+  int nbins;             // histogram of xi over [lo, hi) (0: none)
+  double lo, hi;
+  double* hist;          // [T][nbins]
+};
 
 struct SplitParams {
   int T, P, N, NC;
@@ -62,6 +76,8 @@ struct SplitParams {
   double* dxi;             // [T][NC] dxi_act
   double* cq;              // [T][NC] centroid before SHAKE
   int* shake_fail;         // [T]
+  int umbrella;            // 1: bias towards the trajectory's window after the forces
+  UmbrellaDev umb;
 };
 
 constexpr int kSplitBlock = 128;
@@ -587,6 +603,110 @@ __global__ void split_sum_beads_kernel(int T, int P, const double* V, double* ep
   double s = 0.0;
   for (int k = 0; k < P; ++k) s += V[(size_t)t * P + k];
   epot[t] = s;
+}
+
+
+// BIMOLEC reaction coordinate of umbrella sampling (calc_xi mode 1,
+// src/calc_xi.f90:63-279): xi = s0 / (s0 - s1) and its gradient
+// (s0 ds1 - s1 ds0) / (s0 - s1)^2.  T = Dual gives, with dual coordinates
+// c + eps u, the Hessian-vector product in the eps parts of dxi.
+template <int N, class T>
+__device__ inline T xi_umbrella(const XiDev& x, const T* c, const double* mass, T* dxi) {
+  constexpr int NC = 3 * N;
+  T Rf[3], Rb[3];
+  for (int d = 0; d < 3; ++d) {
+    Rf[d] = c[3 * x.form0 + d] - c[3 * x.form1 + d];
+    Rb[d] = c[3 * x.brk0 + d] - c[3 * x.brk1 + d];
+  }
+  const T rf = sqrt(Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2]);
+  const T rb = sqrt(Rb[0] * Rb[0] + Rb[1] * Rb[1] + Rb[2] * Rb[2]);
+  T s1 = T(0.0);
+  s1 = s1 + (rb - x.break_ref) / 1.0;
+  s1 = s1 - (rf - x.form_ref) / 1.0;
+  T c1[3] = {T(0.0), T(0.0), T(0.0)}, c2[3] = {T(0.0), T(0.0), T(0.0)};
+  for (int k = 0; k < x.nreac1; ++k)
+    for (int d = 0; d < 3; ++d) c1[d] = c1[d] + mass[x.reac1[k]] * c[3 * x.reac1[k] + d] / x.mreac1;
+  for (int k = 0; k < x.nreac2; ++k)
+    for (int d = 0; d < 3; ++d) c2[d] = c2[d] + mass[x.reac2[k]] * c[3 * x.reac2[k] + d] / x.mreac2;
+  const T Red[3] = {c2[0] - c1[0], c2[1] - c1[1], c2[2] - c1[2]};
+  const T reds = sqrt(Red[0] * Red[0] + Red[1] * Red[1] + Red[2] * Red[2]);
+  T s0 = T(0.0);
+  s0 = s0 + (x.r_inf - reds);
+  s0 = s0 / 1.0;
+  T ds1[NC], ds0[NC];
+  for (int i = 0; i < NC; ++i) ds1[i] = ds0[i] = T(0.0);
+  T ri = 1.0 / rf;
+  for (int d = 0; d < 3; ++d) {
+    ds1[3 * x.form0 + d] = ds1[3 * x.form0 + d] - Rf[d] * ri / 1.0;
+    ds1[3 * x.form1 + d] = ds1[3 * x.form1 + d] + Rf[d] * ri / 1.0;
+  }
+  ri = 1.0 / rb;
+  for (int d = 0; d < 3; ++d) {
+    ds1[3 * x.brk0 + d] = ds1[3 * x.brk0 + d] + Rb[d] * ri / 1.0;
+    ds1[3 * x.brk1 + d] = ds1[3 * x.brk1 + d] - Rb[d] * ri / 1.0;
+  }
+  ri = 1.0 / reds;
+  for (int k = 0; k < x.nreac1; ++k) {
+    const int a = x.reac1[k];
+    for (int d = 0; d < 3; ++d) ds0[3 * a + d] = ds0[3 * a + d] + Red[d] * ri * mass[a] / x.mreac1 / 1.0;
+  }
+  for (int k = 0; k < x.nreac2; ++k) {
+    const int a = x.reac2[k];
+    for (int d = 0; d < 3; ++d) ds0[3 * a + d] = ds0[3 * a + d] + (-1.0) * Red[d] * ri * mass[a] / x.mreac2 / 1.0;
+  }
+  const T D = s0 - s1;
+  for (int i = 0; i < NC; ++i) dxi[i] = (s0 * ds1[i] - s1 * ds0[i]) / (D * D);
+  return s0 / D;
+}
+
+// Umbrella bias after the forces (src/umbrella.f90:100-176): at the centroid,
+// every bead's gradient gets k (xi - xi0) dxi, then the gradient of
+// -(1/beta) log fs, (-1/beta) / (2 pi beta fs^2) H dxi/m with H the Hessian
+// of xi (a dual-number pass along u = dxi/m).  One block per trajectory.
+template <int N>
+__global__ void split_umbrella_kernel(SplitParams s) {
+  constexpr int NC = 3 * N;
+  __shared__ double cq[NC], ka[NC], kb[NC];
+  const int t = blockIdx.x, P = s.P;
+  const size_t tb = (size_t)t * P * NC;
+  for (int c = threadIdx.x; c < NC; c += blockDim.x) {
+    double acc = 0.0;
+    for (int k = 0; k < P; ++k) acc = acc + s.q[tb + (size_t)k * NC + c];
+    cq[c] = acc / P;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double dxi[NC];
+    const double xi = xi_umbrella<N, double>(s.xi, cq, s.mass, dxi);
+    Dual cd[NC], hd[NC];
+    for (int c = 0; c < NC; ++c) cd[c] = Dual(cq[c], dxi[c] / s.mass[c / 3]);
+    xi_umbrella<N, Dual>(s.xi, cd, s.mass, hd);
+    const double delta = xi - s.umb.center[t], kf = s.umb.kforce[t];
+    const double pi = 3.1415926535897932384;
+    double fs2 = 0.0;
+    for (int l = 0; l < 3; ++l)
+      for (int m = 0; m < N; ++m) fs2 = fs2 + dxi[3 * m + l] * dxi[3 * m + l] / s.mass[m];
+    const double coeff1 = 2.0 * pi * s.umb.beta;
+    fs2 = fs2 / coeff1;
+    const double coeff2 = -1.0 / s.umb.beta;
+    for (int c = 0; c < NC; ++c) {
+      ka[c] = kf * delta * dxi[c];
+      kb[c] = hd[c].d * coeff2 / (coeff1 * fs2);
+    }
+    if (*s.umb.sampling) {
+      s.umb.xsum[t] = s.umb.xsum[t] + xi;
+      s.umb.xsum2[t] = s.umb.xsum2[t] + xi * xi;
+      if (s.umb.nbins > 0) {
+        const double u = (xi - s.umb.lo) / (s.umb.hi - s.umb.lo) * s.umb.nbins;
+        if (u >= 0.0 && u < s.umb.nbins) s.umb.hist[(size_t)t * s.umb.nbins + (int)u] += 1.0;
+      }
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < P * NC; idx += blockDim.x) {
+    const int c = idx % NC;
+    s.f[tb + idx] = (s.f[tb + idx] + ka[c]) + kb[c];
+  }
 }
 
 }  // namespace cr

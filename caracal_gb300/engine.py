@@ -391,6 +391,30 @@ class RPMDEngine:
         rc = self._recross_def(reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf, xi_ideal)
         L.check(L.lib().cr_engine_set_parent(self._h, C.byref(rc)), "set_parent")
 
+    def set_umbrella(self, reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf, centers, kforce,
+                     nbins=0, lo=0.0, hi=1.0, xi_ideal=1.0):
+        """Umbrella windows: trajectory t biased towards xi = centers[t] with
+        force constant kforce[t] (Eh), xi of calc_xi mode 1 on the MECHA
+        definition (1-based atoms); nbins > 0 also histograms xi over [lo, hi)."""
+        rc = self._recross_def(reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf, xi_ideal)
+        c = np.ascontiguousarray(np.broadcast_to(centers, (self.ntraj,)), dtype=np.float64)
+        k = np.ascontiguousarray(np.broadcast_to(kforce, (self.ntraj,)), dtype=np.float64)
+        self._umb_nbins = int(nbins)
+        L.check(L.lib().cr_engine_set_umbrella(self._h, C.byref(rc), L.dptr(c), L.dptr(k), int(nbins), float(lo),
+                                               float(hi)), "set_umbrella")
+
+    def umbrella_sampling(self, on=True):
+        L.check(L.lib().cr_engine_umbrella_sampling(self._h, int(bool(on))), "umbrella_sampling")
+
+    def umbrella_stats(self, reset=False):
+        """(xsum, xsum2, hist) of xi over the sampled steps per trajectory."""
+        xs = np.zeros(self.ntraj)
+        x2 = np.zeros(self.ntraj)
+        h = np.zeros((self.ntraj, max(getattr(self, "_umb_nbins", 0), 1)))
+        L.check(L.lib().cr_engine_umbrella_stats(self._h, L.dptr(xs), L.dptr(x2), L.dptr(h), int(bool(reset))),
+                "umbrella_stats")
+        return xs, x2, h[:, :getattr(self, "_umb_nbins", 0)]
+
     def set_recross(self, reac1, reac2, bond_form, bond_break, form_ref, break_ref, r_inf,
                     xi_ideal=1.0, max_steps=1):
         """BIMOLEC recrossing bookkeeping; atom indices 1-based as in Caracal's MECHA block."""

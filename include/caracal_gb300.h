@@ -352,6 +352,22 @@ int cr_host_free(void* ptr);
 #define CR_CALIB_COSH 11
 int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s);
 
+/* ---- umbrella windows (calc_rate's umbrella sampling) ----------------------
+ * Trajectory t samples the window centred at centers[t] with force constant
+ * kforce[t] (Eh; Caracal scales its UMBR_BONDS input by the temperature,
+ * src/calc_rate.f90:699): after the forces of every step, each bead's gradient
+ * gets k (xi - xi_t) dxi and the gradient of -(1/beta) log fs at the centroid
+ * (src/umbrella.f90:100-176, xi of calc_xi mode 1 on the MECHA definition rc).
+ * Analytic surfaces, finite temperature.  With sampling on, the xi of every
+ * step is summed (xsum, xsum2) and binned into nbins over [lo, hi): the
+ * averages and variances of umbrella integration and the histograms of WHAM
+ * (src/calc_rate.f90:1568-1700, 1936-2012). */
+int cr_engine_set_umbrella(cr_engine* e, const cr_recross* rc, const double* centers, const double* kforce,
+                           int nbins, double lo, double hi);
+int cr_engine_umbrella_sampling(cr_engine* e, int on);
+/* xsum[T], xsum2[T], hist[T][nbins] (each may be NULL); reset != 0 zeroes them */
+int cr_engine_umbrella_stats(cr_engine* e, double* xsum, double* xsum2, double* hist, int reset);
+
 /* ---- batches of trajectory classes -----------------------------------------
  * One graph launch per chunk of steps advances several engines (classes with
  * different surfaces, atom and bead counts, precisions) side by side: Caracal

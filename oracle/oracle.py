@@ -161,6 +161,13 @@ def lib():
                                         d, d, d, d, C.POINTER(C.c_int), d, d]
         _lib.orc_calc_xi.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d]
         _lib.orc_calc_xi.restype = C.c_double
+        _lib.orc_umbrella_bias.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_double, C.c_double, d, d]
+        _lib.orc_umbrella_bias.restype = C.c_double
+        _lib.orc_calc_xi_umbrella.argtypes = [C.POINTER(XiDef), C.c_int, d, d, d, d]
+        _lib.orc_calc_xi_umbrella.restype = C.c_double
+        _lib.orc_run_umbrella.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, C.c_int, C.c_int,
+                                          d, d, d, d, d, d, C.POINTER(C.c_int), d, C.c_int, d, d, C.c_int,
+                                          C.c_double, C.c_double, d]
         _lib.orc_recross_children.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, d,
                                               C.c_int, d, d, d, d, d, C.c_int]
         _lib.orc_pes_opcount.argtypes = [C.c_int, d, C.POINTER(C.c_uint64)]
@@ -343,6 +350,49 @@ def run_parent(cfg: Config, xd, q, p, f, nsteps, istep0=0, traj0=0, dxi=None, vn
     lib().orc_run_parent(C.byref(cfg.c), C.byref(xd), T, traj0, istep0, nsteps, _dp(q), _dp(p), _dp(f), _dp(e),
                          st.ctypes.data_as(C.POINTER(C.c_int)), _dp(dxi), vp)
     return q, p, f, e, st, dxi
+
+
+def run_umbrella(cfg: Config, xd, q, p, f, nsteps, centers, kforce, istep0=0, traj0=0, vnh=None, sampling=False,
+                 stats=None, nbins=0, lo=0.0, hi=1.0):
+    """Umbrella-window trajectories (bias towards centers[t] with kforce[t]):
+    returns (q, p, f, epot, status, stats) with stats = dict(xsum, xsum2, hist)
+    accumulated over the steps when sampling is set."""
+    q = np.array(q, dtype=np.float64)
+    p = np.array(p, dtype=np.float64)
+    f = np.array(f, dtype=np.float64)
+    T = q.shape[0]
+    e = np.zeros(T)
+    st = np.zeros(T, dtype=np.int32)
+    if stats is None:
+        stats = dict(xsum=np.zeros(T), xsum2=np.zeros(T), hist=np.zeros((T, max(nbins, 1))))
+    if cfg.thermostat == 2 and vnh is None:
+        vnh = np.zeros((T, 4))
+    c = np.ascontiguousarray(centers, dtype=np.float64)
+    k = np.ascontiguousarray(kforce, dtype=np.float64)
+    lib().orc_run_umbrella(C.byref(cfg.c), C.byref(xd), T, traj0, istep0, nsteps, _dp(c), _dp(k), _dp(q), _dp(p),
+                           _dp(f), _dp(e), st.ctypes.data_as(C.POINTER(C.c_int)),
+                           _dp(vnh) if vnh is not None else None, int(bool(sampling)), _dp(stats["xsum"]),
+                           _dp(stats["xsum2"]), int(nbins), float(lo), float(hi), _dp(stats["hist"]))
+    return q, p, f, e, st, stats
+
+
+def umbrella_bias(cfg: Config, xd, xi0, kforce, q, f):
+    """f (nbeads, N, 3) plus the umbrella bias of the ring polymer q; returns (xi, f)."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    f = np.array(f, dtype=np.float64)
+    xi = lib().orc_umbrella_bias(C.byref(cfg.c), C.byref(xd), float(xi0), float(kforce), _dp(q), _dp(f))
+    return xi, f
+
+
+def calc_xi_umbrella(xd, coords, mass):
+    """xi (calc_xi mode 1), dxi (N, 3) and the Hessian (3N, 3N)."""
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    m = np.ascontiguousarray(mass, dtype=np.float64)
+    n = c.shape[0]
+    d = np.zeros((n, 3))
+    h = np.zeros((3 * n, 3 * n))
+    x = lib().orc_calc_xi_umbrella(C.byref(xd), n, _dp(c), _dp(m), _dp(d), _dp(h))
+    return x, d, h
 
 
 FIT_BASES = {"1g": 1, "2g": 2, "3g": 3, "sp": 4, "sd": 5, "sd2": 6, "sp2d": 7, "sp2d3": 8}

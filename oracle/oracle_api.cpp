@@ -252,6 +252,52 @@ int orc_run_parent(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t t
   return 0;
 }
 
+// Umbrella sampling windows: trajectory t is biased towards centers[t] with
+// force constant kforce[t] (Eh); with sampling set, the xi of every step is
+// added to xsum, xsum2 and (nbins > 0) the histogram hist[t][nbins] over
+// [lo, hi).  Same step as orc_run otherwise.
+int orc_run_umbrella(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t traj0, int istep0, int nsteps,
+                     const double* centers, const double* kforce, double* q, double* p, double* f, double* epot,
+                     int* status, double* vnh, int sampling, double* xsum, double* xsum2, int nbins, double lo,
+                     double hi, double* hist) {
+  if (cf->thermostat == 2 && !vnh) return -1;
+  orc::StepConfig s = to_step(cf);
+  const orc::XiDef x = to_xi(xd);
+  BeadPES pes{cf->pes, cf->natoms};
+  const size_t per = (size_t)3 * cf->natoms * cf->nbeads;
+  for (int t = 0; t < ntraj; ++t) {
+    int st = 0;
+    double e = 0.0;
+    for (int n = 1; n <= nsteps; ++n) {
+      double xi = 0.0;
+      auto bias = [&](const double* qq, double* ff) { xi = orc::umbrella_bias(s, x, centers[t], kforce[t], qq, ff); };
+      st |= orc::verlet_step(s, traj0 + t, istep0 + n, &q[t * per], &p[t * per], &f[t * per], &e, pes,
+                             vnh ? &vnh[4 * (size_t)t] : nullptr, bias);
+      if (sampling) {
+        xsum[t] = xsum[t] + xi;
+        xsum2[t] = xsum2[t] + xi * xi;
+        if (nbins > 0) {
+          const double u = (xi - lo) / (hi - lo) * nbins;
+          if (u >= 0.0 && u < nbins) hist[(size_t)t * nbins + (int)u] += 1.0;
+        }
+      }
+    }
+    if (epot) epot[t] = e;
+    if (status) status[t] |= st;
+  }
+  return 0;
+}
+
+double orc_umbrella_bias(const orc_cfg* cf, const orc_xidef* xd, double xi0, double kforce, const double* q,
+                         double* f) {
+  return orc::umbrella_bias(to_step(cf), to_xi(xd), xi0, kforce, q, f);
+}
+
+double orc_calc_xi_umbrella(const orc_xidef* xd, int natoms, const double* coords, const double* mass, double* dxi,
+                            double* d2xi) {
+  return orc::calc_xi_mode1(to_xi(xd), natoms, coords, mass, dxi, d2xi);
+}
+
 double orc_calc_xi(const orc_xidef* xd, int natoms, const double* coords, const double* mass,
                    double* dxi) {
   return orc::calc_xi_mode2(to_xi(xd), natoms, coords, mass, dxi);

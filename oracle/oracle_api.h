@@ -90,6 +90,14 @@ typedef struct orc_xidef {
   double form_ref, break_ref, r_inf, xi_ideal;
 } orc_xidef;
 
+int orc_run_umbrella(const orc_cfg* cf, const orc_xidef* xd, int ntraj, uint32_t traj0, int istep0, int nsteps,
+                     const double* centers, const double* kforce, double* q, double* p, double* f, double* epot,
+                     int* status, double* vnh, int sampling, double* xsum, double* xsum2, int nbins, double lo,
+                     double hi, double* hist);
+double orc_umbrella_bias(const orc_cfg* cf, const orc_xidef* xd, double xi0, double kforce, const double* q,
+                         double* f);
+double orc_calc_xi_umbrella(const orc_xidef* xd, int natoms, const double* coords, const double* mass, double* dxi,
+                            double* d2xi);
 double orc_calc_xi(const orc_xidef* xd, int natoms, const double* coords, const double* mass,
                    double* dxi);
 /* ntraj recrossing children (pairs 2i, 2i+1 share momenta with opposite

@@ -222,4 +222,134 @@ inline int parent_step(const StepConfig& cf, const XiDef& xd, uint32_t traj, int
   return status;
 }
 
+// Umbrella sampling (calc_xi mode 1, src/calc_xi.f90:63-470; one forming and
+// one breaking bond, two reactants): xi = s0 / (s0 - s1),
+// dxi = (s0 ds1 - s1 ds0) / (s0 - s1)^2 and, if d2xi (3N x 3N, row-major over
+// (atom, dim)) is given, the reference's explicit Hessian from the bond and
+// centre-of-mass distance Hessians d2s1, d2s0.
+inline double calc_xi_mode1(const XiDef& x, int N, const double* c, const double* mass, double* dxi,
+                            double* d2xi) {
+  const int n3 = 3 * N;
+  double Rf[3], Rb[3];
+  for (int d = 0; d < 3; ++d) {
+    Rf[d] = c[3 * x.form[0] + d] - c[3 * x.form[1] + d];
+    Rb[d] = c[3 * x.brk[0] + d] - c[3 * x.brk[1] + d];
+  }
+  const double rf = std::sqrt(Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2]);
+  const double rb = std::sqrt(Rb[0] * Rb[0] + Rb[1] * Rb[1] + Rb[2] * Rb[2]);
+  double s1 = 0.0;
+  s1 = s1 + (rb - x.break_ref) / 1.0;
+  s1 = s1 - (rf - x.form_ref) / 1.0;
+  const int* rs[2] = {x.reac1, x.reac2};
+  const int nr[2] = {x.nreac1, x.nreac2};
+  double com[2][3] = {{0, 0, 0}, {0, 0, 0}}, mr[2] = {0, 0};
+  for (int r = 0; r < 2; ++r)
+    for (int k = 0; k < nr[r]; ++k) mr[r] += mass[rs[r][k]];
+  for (int r = 0; r < 2; ++r)
+    for (int k = 0; k < nr[r]; ++k)
+      for (int d = 0; d < 3; ++d) com[r][d] = com[r][d] + mass[rs[r][k]] * c[3 * rs[r][k] + d] / mr[r];
+  const double Red[3] = {com[1][0] - com[0][0], com[1][1] - com[0][1], com[1][2] - com[0][2]};
+  const double reds = std::sqrt(Red[0] * Red[0] + Red[1] * Red[1] + Red[2] * Red[2]);
+  double s0 = 0.0;
+  s0 = s0 + (x.r_inf - reds);
+  s0 = s0 / 1.0;
+  const double xi = s0 / (s0 - s1);
+  std::vector<double> ds1(n3, 0.0), ds0(n3, 0.0);
+  double ri = 1.0 / rf;
+  for (int d = 0; d < 3; ++d) {
+    ds1[3 * x.form[0] + d] = ds1[3 * x.form[0] + d] - Rf[d] * ri / 1.0;
+    ds1[3 * x.form[1] + d] = ds1[3 * x.form[1] + d] + Rf[d] * ri / 1.0;
+  }
+  ri = 1.0 / rb;
+  for (int d = 0; d < 3; ++d) {
+    ds1[3 * x.brk[0] + d] = ds1[3 * x.brk[0] + d] + Rb[d] * ri / 1.0;
+    ds1[3 * x.brk[1] + d] = ds1[3 * x.brk[1] + d] - Rb[d] * ri / 1.0;
+  }
+  ri = 1.0 / reds;
+  for (int r = 0; r < 2; ++r) {
+    const double sg = r == 0 ? 1.0 : -1.0;
+    for (int k = 0; k < nr[r]; ++k) {
+      const int a = rs[r][k];
+      for (int d = 0; d < 3; ++d) ds0[3 * a + d] = ds0[3 * a + d] + sg * Red[d] * ri * mass[a] / mr[r] / 1.0;
+    }
+  }
+  const double D = s0 - s1;
+  if (dxi)
+    for (int i = 0; i < n3; ++i) dxi[i] = (s0 * ds1[i] - s1 * ds0[i]) / (D * D);
+  if (d2xi) {
+    // second derivatives of the bond lengths and the COM distance: for a
+    // vector R of length r, d2 r / dR_a dR_b = (delta_ab r^2 - R_a R_b) / r^3
+    std::vector<double> d2s1((size_t)n3 * n3, 0.0), d2s0((size_t)n3 * n3, 0.0);
+    auto blk = [](const double* R, double r, double sgn, double h[3][3]) {
+      const double r3 = 1.0 / (r * r * r);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) h[a][b] = sgn * ((a == b ? r * r : 0.0) - R[a] * R[b]) * r3;
+    };
+    auto add2 = [&](std::vector<double>& H, int i, int j, double h[3][3], double w) {
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) H[(size_t)(3 * i + a) * n3 + 3 * j + b] += w * h[a][b];
+    };
+    double hf[3][3], hb[3][3], hr[3][3];
+    blk(Rf, rf, -1.0, hf);  // s1 contains -r_form
+    blk(Rb, rb, 1.0, hb);
+    blk(Red, reds, -1.0, hr);  // s0 contains -|Red|
+    const int fa = x.form[0], fb = x.form[1], ba = x.brk[0], bb = x.brk[1];
+    add2(d2s1, fa, fa, hf, 1.0);
+    add2(d2s1, fa, fb, hf, -1.0);
+    add2(d2s1, fb, fa, hf, -1.0);
+    add2(d2s1, fb, fb, hf, 1.0);
+    add2(d2s1, ba, ba, hb, 1.0);
+    add2(d2s1, ba, bb, hb, -1.0);
+    add2(d2s1, bb, ba, hb, -1.0);
+    add2(d2s1, bb, bb, hb, 1.0);
+    for (int r1 = 0; r1 < 2; ++r1)
+      for (int k = 0; k < nr[r1]; ++k)
+        for (int r2 = 0; r2 < 2; ++r2)
+          for (int l = 0; l < nr[r2]; ++l) {
+            const int a1 = rs[r1][k], a2 = rs[r2][l];
+            const double mf = mass[a1] / mr[r1] * mass[a2] / mr[r2];
+            add2(d2s0, a1, a2, hr, (r1 == r2 ? 1.0 : -1.0) * mf);
+          }
+    for (int i = 0; i < n3; ++i)
+      for (int j = 0; j < n3; ++j)
+        d2xi[(size_t)i * n3 + j] =
+            ((s0 * d2s1[(size_t)i * n3 + j] + ds0[j] * ds1[i] - ds1[j] * ds0[i] - s1 * d2s0[(size_t)i * n3 + j]) * D -
+             2.0 * (s0 * ds1[i] - s1 * ds0[i]) * (ds0[j] - ds1[j])) /
+            (D * D * D);
+  }
+  return xi;
+}
+
+// Umbrella bias of one ring polymer (umbrella mode 0, src/umbrella.f90:100-176):
+// at the centroid, every bead's gradient gets k (xi - xi0) dxi plus the
+// gradient of -(1/beta) log fs, fs^2 = sum dxi^2 / m / (2 pi beta):
+// (-1/beta) / (2 pi beta fs^2) * sum_j d2xi(j, i) dxi(j) / m(j).  Returns xi.
+inline double umbrella_bias(const StepConfig& cf, const XiDef& xd, double xi0, double kforce, const double* q,
+                            double* f) {
+  const int N = cf.natoms, P = cf.nbeads, n3 = 3 * N;
+  std::vector<double> c(n3), dxi(n3), d2xi((size_t)n3 * n3);
+  centroid(N, P, q, c.data());
+  const double xi = calc_xi_mode1(xd, N, c.data(), cf.mass, dxi.data(), d2xi.data());
+  const double delta = xi - xi0;
+  for (int k = 0; k < P; ++k)
+    for (int i = 0; i < n3; ++i) f[(size_t)k * n3 + i] = f[(size_t)k * n3 + i] + kforce * delta * dxi[i];
+  const double pi = 3.1415926535897932384;
+  double fs2 = 0.0;
+  for (int l = 0; l < 3; ++l)
+    for (int m = 0; m < N; ++m) fs2 = fs2 + dxi[3 * m + l] * dxi[3 * m + l] / cf.mass[m];
+  const double coeff1 = 2.0 * pi * cf.beta;
+  fs2 = fs2 / coeff1;
+  const double coeff2 = -1.0 / cf.beta;
+  for (int l = 0; l < 3; ++l)
+    for (int m = 0; m < N; ++m) {
+      double dh = 0.0;
+      for (int l2 = 0; l2 < 3; ++l2)
+        for (int m2 = 0; m2 < N; ++m2)
+          dh = dh + d2xi[(size_t)(3 * m2 + l2) * n3 + 3 * m + l] * dxi[3 * m2 + l2] / cf.mass[m2];
+      dh = dh * coeff2 / (coeff1 * fs2);
+      for (int k = 0; k < P; ++k) f[(size_t)k * n3 + 3 * m + l] = f[(size_t)k * n3 + 3 * m + l] + dh;
+    }
+  return xi;
+}
+
 }  // namespace orc

@@ -417,9 +417,21 @@ enum TrajStatus : int { TRAJ_OK = 0, TRAJ_NONFINITE = 1, TRAJ_SINGULAR_INERTIA =
 
 // One verlet step of one trajectory.  `egrad(q_bead, &V, g_bead)` evaluates a
 // bead; f holds dV/dq of the previous step on entry and of this step on exit.
+struct NoBias {
+  void operator()(const double*, double*) const {}
+};
+
 template <class EGrad>
 inline int verlet_step(const StepConfig& cf, uint32_t traj, int istep, double* q, double* p,
                        double* f, double* epot, EGrad egrad, double* vnh = nullptr) {
+  return verlet_step(cf, traj, istep, q, p, f, epot, egrad, vnh, NoBias());
+}
+
+// The same step with a bias added to the bead gradients after the forces
+// (umbrella sampling: src/verlet.f90:1043-1046, umbrella mode 0).
+template <class EGrad, class Bias>
+inline int verlet_step(const StepConfig& cf, uint32_t traj, int istep, double* q, double* p,
+                       double* f, double* epot, EGrad egrad, double* vnh, Bias bias) {
   const int N = cf.natoms, P = cf.nbeads, n3 = 3 * N;
   const size_t nall = (size_t)n3 * P;
   if (cf.thermostat == 2) nhc_half(cf, vnh, p);  // src/verlet.f90:186-208
@@ -433,6 +445,7 @@ inline int verlet_step(const StepConfig& cf, uint32_t traj, int istep, double* q
     e = e + v;
   }
   *epot = e;
+  bias(q, f);
   for (size_t x = 0; x < nall; ++x) p[x] = p[x] - 0.5 * cf.dt * f[x];
   if (cf.thermostat == 2) nhc_half(cf, vnh, p);  // src/verlet.f90:1085-1106
   if (cf.thermostat == 1 && istep % cf.andersen_step == 0)
