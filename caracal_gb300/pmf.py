@@ -73,3 +73,16 @@ def wham(hist, xi_windows, kforce, kelvin, xi_min, xi_max, tol=1e-5, max_iter=10
     pmin = np.max((1.0 / beta2) * np.log(pu))
     centres = xi_min + bin_size * (np.arange(1, nbins + 1) - 0.5)
     return centres, (-(1.0 / beta2) * np.log(pu) + pmin) * 627.509 * BOHR_ANGSTROM
+
+
+def bimolecular_rate(kappa, pmf_max, pmf_min, r_inf, beta, mass_reac1, mass_reac2, npaths=1):
+    """Caracal's BIMOLEC rate constant (src/calc_k_t.f90) in cm^3 mol^-1 s^-1:
+    k = npaths kappa 4 pi R_inf^2 sqrt(1/(2 pi beta mu)) exp(-beta (W_max - W_min))
+    in atomic units, converted with the reference's single-precision factor
+    1e6 (a0^3 / t_au) N_A (its literals carry no D exponent)."""
+    f32 = np.float32
+    mu = mass_reac1 * mass_reac2 / (mass_reac1 + mass_reac2)
+    k = npaths * kappa * 4.0 * np.pi * r_inf * r_inf * np.sqrt(1.0 / (2.0 * np.pi * beta * mu)) * \
+        np.exp(-beta * (pmf_max - pmf_min))
+    conv = f32(f32(5.2917721092e-11) ** 3) / f32(2.418884326505e-17)
+    return float(k * float(f32(1e6)) * float(f32(conv)) * float(f32(6.02214179e23)))
