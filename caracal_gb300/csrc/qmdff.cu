@@ -494,6 +494,9 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   D.zahn = d->zahn ? 1 : 0;
   D.zahn_a = d->zahn_a;
   D.zahn_par = d->zahn_par;
+  D.fcoul_cut = (float)d->coul_cut;
+  D.fzahn_a = (float)d->zahn_a;
+  D.fzahn_par = (float)d->zahn_par;
   D.e_zero = d->e_zero;
   D.distinct = distinct ? 1 : 0;
   for (int k = 0; k < cr::qmdff::kKinds; ++k) D.nterm[k] = ff->nterm[k];

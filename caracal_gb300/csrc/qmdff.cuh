@@ -70,6 +70,7 @@ struct Dev {
   Tables<double> d;
   Tables<float> f;
   double coul_cut, zahn_a, zahn_par, e_zero;
+  float fcoul_cut, fzahn_a, fzahn_par;  // the same in FP32 (mixed form)
   int zahn;
   int distinct;  // 1: every term's atoms are pairwise distinct
   int nterm[kKinds];  // terms per kind
@@ -112,6 +113,14 @@ template <> __device__ inline Dual q_sin<Dual>(Dual x) { return sin(x); }
 template <> __device__ inline Dual q_cos<Dual>(Dual x) { return cos(x); }
 template <> __device__ inline Dual q_pow<Dual>(Dual x, double p) { return pow(x, p); }
 
+// |x| < 1e-14 and |x| > 1e-14 as the reference tests its FP64 denominators;
+// for FP32 the same sets of values without a conversion (1e-14 is not a
+// float: |x| < 1e-14 holds exactly for |x| <= 1e-14f).
+template <class F> __device__ inline bool below_1em14(F x) { return fabs((double)ad::val(x)) < 1e-14; }
+template <> __device__ inline bool below_1em14<float>(float x) { return fabsf(x) <= 1e-14f; }
+template <class F> __device__ inline bool above_1em14(F x) { return fabs((double)ad::val(x)) > 1e-14; }
+template <> __device__ inline bool above_1em14<float>(float x) { return fabsf(x) > 1e-14f; }
+
 // Parameter type of a term evaluated in arithmetic type F (dual coordinates
 // read FP64 parameters).
 template <class F> struct ParamOf { using type = F; };
@@ -146,14 +155,15 @@ struct Grad<double> {
 };
 template <>
 struct Grad<float> {
-  float* s;
-  float* k;
+  float2* sk;  // (sum, compensation) per coordinate: one 8-byte access each
   __device__ inline void add(int i, float v) {
-    float a = s[i], t = a + v;
-    k[i] += (fabsf(a) >= fabsf(v)) ? ((a - t) + v) : ((v - t) + a);
-    s[i] = t;
+    float2 c = sk[i];
+    const float t = c.x + v;
+    c.y += (fabsf(c.x) >= fabsf(v)) ? ((c.x - t) + v) : ((v - t) + c.x);
+    c.x = t;
+    sk[i] = c;
   }
-  __device__ inline double get(int i) const { return (double)s[i] + (double)k[i]; }
+  __device__ inline double get(int i) const { return (double)sk[i].x + (double)sk[i].y; }
 };
 
 // Adds a term's gradient for its NA atoms (compile-time count).  Mixed form
@@ -171,21 +181,18 @@ __device__ inline void scatter(const Contrib<double>& c, Grad<double>& G, bool) 
 template <int NA>
 __device__ inline void scatter(const Contrib<float>& c, Grad<float>& G, bool distinct) {
   if (distinct) {
-    float a[NA][3], k[NA][3];
+    float2 a[NA][3];
+#pragma unroll
+    for (int m = 0; m < NA; ++m)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) a[m][d] = G.sk[3 * c.a[m] + d];
 #pragma unroll
     for (int m = 0; m < NA; ++m)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        a[m][d] = G.s[3 * c.a[m] + d];
-        k[m][d] = G.k[3 * c.a[m] + d];
-      }
-#pragma unroll
-    for (int m = 0; m < NA; ++m)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const float v = c.g[m][d], t = a[m][d] + v;
-        G.k[3 * c.a[m] + d] = k[m][d] + ((fabsf(a[m][d]) >= fabsf(v)) ? ((a[m][d] - t) + v) : ((v - t) + a[m][d]));
-        G.s[3 * c.a[m] + d] = t;
+        const float v = c.g[m][d], s0 = a[m][d].x, t = s0 + v;
+        const float k = a[m][d].y + ((fabsf(s0) >= fabsf(v)) ? ((s0 - t) + v) : ((v - t) + s0));
+        G.sk[3 * c.a[m] + d] = make_float2(t, k);
       }
   } else {
 #pragma unroll
@@ -210,9 +217,8 @@ __device__ inline void abdamp(F radi, F radj, F r2, F& damp, F& ddamp) {
 // A bead's coordinates: FP64, and (mixed form) the FP32 split x = hi + lo.
 struct BeadPos {
   const double* x;
-  const float* hi;
-  const float* lo;
-  const double* w;  // tangent direction (dual coordinates only)
+  const float2* hl;  // (hi, lo) per coordinate (mixed form only)
+  const double* w;   // tangent direction (dual coordinates only)
 };
 
 template <class F>
@@ -231,7 +237,10 @@ __device__ inline void disp<Dual>(const BeadPos& X, int a, int b, Dual* v) {
 template <>
 __device__ inline void disp<float>(const BeadPos& X, int a, int b, float* v) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) v[d] = (X.hi[3 * a + d] - X.hi[3 * b + d]) + (X.lo[3 * a + d] - X.lo[3 * b + d]);
+  for (int d = 0; d < 3; ++d) {
+    const float2 u = X.hl[3 * a + d], w = X.hl[3 * b + d];
+    v[d] = (u.x - w.x) + (u.y - w.y);
+  }
 }
 
 // Bond stretch, generalised Lennard-Jones (src/ff_eg.f90:87-163):
@@ -414,7 +423,7 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
     F na[3], nb[3], nan_, nbn, cosphi, sinphi;
     const F phi = dihedral<F>(ra, rb, rc, na, nb, nan_, nbn, cosphi, sinphi);
     const F nenner = nan_ * nbn * sinphi;
-    if (fabs((double)ad::val(nenner)) < 1e-14) {
+    if (below_1em14(nenner)) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = F(0);
     } else {
@@ -513,7 +522,7 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
   cross(rv, rdme, rvdme);
   cross(rn, rdme, rndme);
   const F nenner = rnn * rvn * cosom;
-  if (fabs((double)ad::val(nenner)) > 1e-14) {
+  if (above_1em14(nenner)) {
     const F on = F(1) / nenner;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -603,9 +612,14 @@ __device__ inline F pair_term(const Dev& D, const Tables<typename ParamOf<F>::ty
     e = e + t * oner * eps2;
     drij = drij - eps2 * t * (alpha * r + F(1)) * oner * ir2;
   }
-  if (!(r > (F)D.coul_cut)) {
+  const F cut = std::is_same<F, float>::value ? F(D.fcoul_cut) : F(D.coul_cut);
+  if (!(r > cut)) {
     F e0;
-    if (D.zahn) e0 = v[6] * ((q_erfc<F>((F)D.zahn_a * r) * oner) - (F)D.zahn_par * (r - (F)D.coul_cut));
+    if (D.zahn) {
+      const F za = std::is_same<F, float>::value ? F(D.fzahn_a) : F(D.zahn_a);
+      const F zp = std::is_same<F, float>::value ? F(D.fzahn_par) : F(D.zahn_par);
+      e0 = v[6] * ((q_erfc<F>(za * r) * oner) - zp * (r - cut));
+    }
     else e0 = v[6] * oner;
     e = e + e0;
     drij = drij - e0 * ir2;
@@ -838,8 +852,8 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
 }
 
 // Shared memory per warp (bytes): coordinates (3n doubles), the FP32 split
-// hi, lo (3n floats each) and the gradient (3n doubles, or sum and
-// compensation, 3n floats each).
+// (hi, lo) (3n float pairs) and the gradient (3n doubles, or (sum,
+// compensation) float pairs).
 __host__ __device__ inline size_t warp_smem_bytes(int n) { return (size_t)3 * n * (8 + 4 + 4 + 8); }
 
 // Energy (with E_zero) and gradient (times gscale) of one bead by one warp.
@@ -850,21 +864,18 @@ __device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, doub
   using F = typename std::conditional<MIXED, float, double>::type;
   const int n3 = 3 * D.n;
   double* xs = ws;
-  float* hi = (float*)(ws + n3);
-  float* lo = hi + n3;
-  void* gs = lo + n3;
-  BeadPos X{xs, hi, lo};
+  float2* hl = (float2*)(ws + n3);
+  void* gs = hl + n3;
+  BeadPos X{xs, hl, nullptr};
   Grad<F> G;
   if constexpr (MIXED) {
     for (int a = lane; a < n3; a += 32) {
       const double v = xs[a];
       const float h = __double2float_rn(v);
-      hi[a] = h;
-      lo[a] = __double2float_rn(v - (double)h);
+      hl[a] = make_float2(h, __double2float_rn(v - (double)h));
     }
-    G.s = (float*)gs;
-    G.k = (float*)gs + n3;
-    for (int a = lane; a < 2 * n3; a += 32) ((float*)gs)[a] = 0.f;
+    G.sk = (float2*)gs;
+    for (int a = lane; a < n3; a += 32) G.sk[a] = make_float2(0.f, 0.f);
   } else {
     G.g = (double*)gs;
     for (int a = lane; a < n3; a += 32) G.g[a] = 0.0;
@@ -946,7 +957,7 @@ __device__ inline double warp_hvp(const Dev& D, double* ws, double* gout, double
     G.h[a] = 0.0;
   }
   __syncwarp();
-  BeadPos X{xs, nullptr, nullptr, w};
+  BeadPos X{xs, nullptr, w};
   Dual es(0.0);
   kind_batches_dual<0, 2>(D, X, G, es, lane);
   kind_batches_dual<1, 3>(D, X, G, es, lane);
@@ -976,7 +987,7 @@ __device__ inline double warp_hvp(const Dev& D, double* ws, double* gout, double
 // Per term, out receives alpha * (v . grad E_t|unit) + beta * E_t|unit.
 __device__ inline void warp_param_vjp(const Dev& D, const Tables<double>& U, const double* xs, const double* vs,
                                       double alpha, double beta, double* out, int lane) {
-  const BeadPos X{xs, nullptr, nullptr, nullptr};
+  const BeadPos X{xs, nullptr, nullptr};
   int off = 0;
 #pragma unroll 1
   for (int kind = 0; kind < 4; ++kind) {
