@@ -50,6 +50,14 @@ class CrConfig(C.Structure):
                 ("mass", c_double_p), ("nose_q", C.c_double)]
 
 
+DUMP_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                      C.POINTER(C.c_double))
+
+
+class CrQmdffTables(C.Structure):
+    _fields_ = [(k, C.POINTER(C.c_double)) for k in ("rad", "r0ab", "zab", "r0094", "sr42", "c6ab")]
+
+
 class CrRecross(C.Structure):
     _fields_ = [("nreac1", C.c_int), ("reac1", C.c_int * 8), ("nreac2", C.c_int),
                 ("reac2", C.c_int * 8), ("bond_form", C.c_int * 2), ("bond_break", C.c_int * 2),
@@ -109,6 +117,7 @@ def _sig(lib):
         "cr_engine_set_state": ([eng, d, d, d], C.c_int),
         "cr_engine_get_state": ([eng, d, d, d, d, i], C.c_int),
         "cr_engine_run": ([eng, C.c_int], C.c_int),
+        "cr_engine_run_dump": ([eng, C.c_int, C.c_int, DUMP_FN, v, d, d, d], C.c_int),
         "cr_engine_step_host": ([eng, d, d, d, d], C.c_int),
         "cr_engine_last_kernel_ms": ([eng, C.POINTER(C.c_float)], C.c_int),
         "cr_engine_launch_info": ([eng, i, i, i, i], C.c_int),
@@ -133,6 +142,9 @@ def _sig(lib):
         "cr_evb_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
         "cr_engine_create_evb": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
         "cr_qmdff_nparams": ([v, i], C.c_int),
+        "cr_qmdff_load": ([C.c_char_p, C.POINTER(CrQmdffTables), C.c_double, C.c_int, C.c_double,
+                           C.POINTER(C.c_void_p)], C.c_int),
+        "cr_qmdff_file_counts": ([C.c_char_p, i, i], C.c_int),
         "cr_qmdff_hvp": ([v, d, d, C.c_int, d, d, d], C.c_int),
         "cr_qmdff_param_vjp": ([v, d, d, C.c_int, d], C.c_int),
         "cr_evb_fit": ([C.c_int, d, C.c_int, C.c_int, d, d, d, d, d], C.c_int),

@@ -1126,6 +1126,24 @@ int cr_engine_run(cr_engine* e, int nsteps) {
   return engine_finish(e);
 }
 
+int cr_engine_run_dump(cr_engine* e, int nsteps, int every, cr_dump_fn dump, void* user, double* q, double* p,
+                       double* epot) {
+  if (!e || !dump || !q || !p || !epot) return fail(CR_ERR_ARG, "NULL argument");
+  if (nsteps < 0 || every < 1) return fail(CR_ERR_ARG, "nsteps must be >= 0 and every >= 1");
+  int done = 0;
+  while (done < nsteps) {
+    const int n = std::min(every - e->istep % every, nsteps - done);
+    int rc = cr_engine_run(e, n);
+    if (rc) return rc;
+    done += n;
+    if (e->istep % every == 0) {
+      if ((rc = cr_engine_get_state(e, q, p, nullptr, epot, nullptr))) return rc;
+      if (dump(user, e->istep, q, p, epot) != 0) return fail(CR_ERR_ARG, "the dump callback stopped the run");
+    }
+  }
+  return CR_OK;
+}
+
 int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* epot) {
   if (!e || !q || !p || !f) return fail(CR_ERR_ARG, "NULL argument");
   if (e->xi_on && e->istep + 1 - e->side_step0 > e->side_cap)

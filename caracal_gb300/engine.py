@@ -131,6 +131,31 @@ class QMDFFForceField:
                 "cr_qmdff_egrad")
         return e, g
 
+    @classmethod
+    def load(cls, path, tables=None, e_zero=0.0, zahn=False, coul_cut=50.0):
+        """A device QMDFF read from a .qmdff file by the library's own reader
+        (cr_qmdff_load); the pair C6 from the element-pair table."""
+        from . import qmdff as Q
+        tables = tables if tables is not None else Q.ElementTables.d3_like()
+        fp = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+        c6 = np.zeros((94, 94))
+        for (a, b), val in Q.C6_PAIR.items():
+            c6[a - 1, b - 1] = c6[b - 1, a - 1] = val
+        arrs = dict(rad=fp(Q.element_radii()), r0ab=fp(tables.r0ab[1:, 1:].T), zab=fp(tables.zab[1:, 1:].T),
+                    r0094=fp(tables.r094[1:, 1:].T), sr42=fp(tables.sr42[1:, 1:].T), c6ab=fp(c6.T))
+        t = L.CrQmdffTables(*[L.dptr(arrs[k]) for k in ("rad", "r0ab", "zab", "r0094", "sr42", "c6ab")])
+        h = C.c_void_p()
+        L.check(L.lib().cr_qmdff_load(str(path).encode(), C.byref(t), float(e_zero), int(bool(zahn)),
+                                      float(coul_cut), C.byref(h)), "cr_qmdff_load")
+        obj = cls.__new__(cls)
+        obj._h = h
+        obj._arrs = arrs
+        counts = np.zeros(5, dtype=np.int32)
+        n = C.c_int()
+        L.check(L.lib().cr_qmdff_file_counts(str(path).encode(), C.byref(n), L.iptr(counts)), "file_counts")
+        obj.n = n.value
+        return obj
+
     @property
     def nparams(self):
         """Number of linear parameters (bond k, angle k, torsion V, pair qq)."""
@@ -366,6 +391,20 @@ class RPMDEngine:
         if check:
             L.check(rc, "run")
         return rc
+
+    def run_dump(self, nsteps, every, callback):
+        """Run nsteps steps; after every step whose index is a multiple of
+        `every`, callback(istep, q, p, epot) gets the state (numpy views of
+        host buffers, valid during the call); a truthy return stops the run."""
+        q = np.zeros(self.shape)
+        p = np.zeros(self.shape)
+        e = np.zeros(self.ntraj)
+
+        def cb(_user, istep, _q, _p, _e):
+            return 1 if callback(istep, q, p, e) else 0
+        fn = L.DUMP_FN(cb)
+        L.check(L.lib().cr_engine_run_dump(self._h, int(nsteps), int(every), fn, None, L.dptr(q), L.dptr(p),
+                                           L.dptr(e)), "run_dump")
 
     def step_host(self, q, p, f, epot=None):
         """One verlet step through host arrays (modified in place)."""

@@ -160,6 +160,24 @@ typedef struct cr_qmdff_def {
 } cr_qmdff_def;
 typedef struct cr_qmdff cr_qmdff;
 int cr_qmdff_create(const cr_qmdff_def* def, cr_qmdff** out);
+/* Element tables for reading a .qmdff file: the (94,94) arrays ff_nonb takes
+ * and, per element pair, the C6 that gives c6xy(i, j) = c6ab(at(i), at(j)). */
+typedef struct cr_qmdff_tables {
+  const double* rad;    /* rad(94), bohr */
+  const double* r0ab;   /* (94,94) */
+  const double* zab;
+  const double* r0094;
+  const double* sr42;
+  const double* c6ab;   /* (94,94) */
+} cr_qmdff_tables;
+/* rdsolvff (src/rdsolvff.f90:34-202) from a file: the force field with E_zero
+ * e_zero, the Zahn Coulomb switch and cutoff; H/halogen-bond strengths as
+ * rdsolvff derives them from the charges (src/rdsolvff.f90:142-152). */
+int cr_qmdff_load(const char* path, const cr_qmdff_tables* tab, double e_zero, int zahn, double coul_cut,
+                  cr_qmdff** out);
+/* natoms and the term counts (bonds, angles, torsions, H bonds, NCI pairs) of
+ * a .qmdff file; host only. */
+int cr_qmdff_file_counts(const char* path, int* natoms, int* counts);
 int cr_qmdff_destroy(cr_qmdff* ff);
 /* Host arrays xyz(3,natoms,nbeads) -> e(nbeads) (with E_zero), g(3,natoms,nbeads). */
 int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
@@ -282,6 +300,14 @@ int cr_engine_get_state(cr_engine* e, double* q, double* p, double* f, double* e
  * step counter continues from previous runs.  Returns CR_ERR_TRAJECTORY if a
  * trajectory reported a status bit (state is still returned). */
 int cr_engine_run(cr_engine* e, int nsteps);
+/* cr_engine_run with Caracal's trajectory dumps (src/verlet.f90:780-800,
+ * every iwrite steps): after each step whose index is a multiple of `every`
+ * the state is copied to the caller's q, p (3 x natoms x nbeads x ntraj) and
+ * epot (ntraj) and dump(user, istep, q, p, epot) is called; a nonzero return
+ * stops the run with CR_ERR_ARG. */
+typedef int (*cr_dump_fn)(void* user, int istep, const double* q, const double* p, const double* epot);
+int cr_engine_run_dump(cr_engine* e, int nsteps, int every, cr_dump_fn dump, void* user, double* q, double* p,
+                       double* epot);
 
 /* One `verlet` step through host buffers, as a Fortran caller holding
  * q_i, p_i, derivs would use it: copy in, one step, copy out (epot may be NULL). */

@@ -91,3 +91,16 @@ def test_batch_argument_validation():
     assert lib.cr_batch_create(arr, 1, 10, C.byref(h)) == L.CR_ERR_ARG
     assert lib.cr_batch_run(None, 1) == L.CR_ERR_ARG
     assert lib.cr_batch_destroy(None) == 0
+
+
+def test_qmdff_file_counts(tmp_path):
+    from caracal_gb300 import qmdff as Q
+    ff = Q.water_dimer()
+    Q.write_qmdff(ff, tmp_path / "w.qmdff")
+    n = C.c_int()
+    counts = np.zeros(5, dtype=np.int32)
+    assert L.lib().cr_qmdff_file_counts(str(tmp_path / "w.qmdff").encode(), C.byref(n), L.iptr(counts)) == 0
+    assert n.value == ff.n
+    assert counts.tolist() == [len(ff.bond), len(ff.angl), len(ff.tors), len(ff.hb), len(ff.nci)]
+    assert L.lib().cr_qmdff_file_counts(str(tmp_path / "missing.qmdff").encode(), C.byref(n),
+                                        L.iptr(counts)) == L.CR_ERR_ARG

@@ -69,3 +69,25 @@ def test_dynamic_qmdff_and_evb(require_gpu, tmp_path):
                                     "DE_EVB {\n COUPLING 1g\n}\n")
     run(str(tmp_path / "e.key"), out_dir=str(tmp_path), quiet=True)
     assert len(frames(tmp_path / "trajectory.xyz")) == 3
+
+
+def test_run_dump_callback(require_gpu):
+    mass = [mass_au("H")] * 3
+    kw = dict(beta=beta_from_kelvin(300.0), thermostat="andersen", andersen_step=7, seed=4)
+    a = RPMDEngine("h3", mass, 4, 2, dt_fs_to_au(0.1), **kw)
+    b = RPMDEngine("h3", mass, 4, 2, dt_fs_to_au(0.1), **kw)
+    for e in (a, b):
+        e.init_positions(h3_collinear(), 0.01)
+        e.init_momenta()
+        e.compute_forces()
+    seen = []
+
+    def cb(istep, q, p, epot):
+        b.run(5)
+        qb, pb, _, eb, _ = b.get_state()
+        seen.append((istep, np.array_equal(q, qb) and np.array_equal(p, pb) and np.array_equal(epot, eb)))
+        return istep >= 15          # stop after the third dump
+
+    with pytest.raises(Exception):
+        a.run_dump(40, 5, cb)
+    assert seen == [(5, True), (10, True), (15, True)]
