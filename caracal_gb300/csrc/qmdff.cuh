@@ -156,6 +156,10 @@ struct Grad<double> {
 template <>
 struct Grad<float> {
   float2* sk;  // (sum, compensation) per coordinate: one 8-byte access each
+  float* pr;   // NCI pair contributions, a plain FP32 sum: they are ~1 % of
+               // the valence forces, so their own rounding stays below the
+               // compensated sum's, and keeping them apart leaves that sum
+               // free of many small additions
   __device__ inline void add(int i, float v) {
     float2 c = sk[i];
     const float t = c.x + v;
@@ -163,7 +167,7 @@ struct Grad<float> {
     c.x = t;
     sk[i] = c;
   }
-  __device__ inline double get(int i) const { return (double)sk[i].x + (double)sk[i].y; }
+  __device__ inline double get(int i) const { return ((double)sk[i].x + (double)sk[i].y) + (double)pr[i]; }
 };
 
 // Adds a term's gradient for its NA atoms (compile-time count).  Mixed form
@@ -177,6 +181,18 @@ __device__ inline void scatter(const Contrib<double>& c, Grad<double>& G, bool) 
   for (int m = 0; m < NA; ++m)
 #pragma unroll
     for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
+}
+template <int NA>
+__device__ inline void scatter_pair(const Contrib<float>& c, Grad<float>& G) {
+  float a[NA][3];
+#pragma unroll
+  for (int m = 0; m < NA; ++m)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) a[m][d] = G.pr[3 * c.a[m] + d];
+#pragma unroll
+  for (int m = 0; m < NA; ++m)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) G.pr[3 * c.a[m] + d] = a[m][d] + c.g[m][d];
 }
 template <int NA>
 __device__ inline void scatter(const Contrib<float>& c, Grad<float>& G, bool distinct) {
@@ -593,22 +609,36 @@ __device__ inline F pair_term(const Dev& D, const Tables<typename ParamOf<F>::ty
   F vab[3];
   disp<F>(x, i1, i2, vab);
   const F r2 = dot3(vab, vab);
-  const F r = q_sqrt<F>(r2);
-  const F oner = F(1) / r;
-  const F ir2 = oner * oner;
+  F r, oner, it6, it8;
   const F R0 = v[0], c6 = v[1], eps2 = v[5];
   const F r4 = r2 * r2, r6 = r4 * r2;
   const F R02 = R0 * R0, r06 = R02 * R02 * R02;
   const F t6 = r6 + r06;
   const F t8 = r6 * r2 + r06 * R0 * R0;
-  const F it6 = F(1) / t6, it8 = F(1) / t8;
+  if constexpr (std::is_same<F, float>::value) {
+    // hardware approximations (a few ulp): the pair forces are ~1 % of the
+    // valence forces, far below the form's error budget
+    oner = rsqrtf(r2);
+    r = r2 * oner;
+    it6 = __fdividef(1.0f, t6);
+    it8 = __fdividef(1.0f, t8);
+  } else {
+    r = q_sqrt<F>(r2);
+    oner = F(1) / r;
+    it6 = F(1) / t6;
+    it8 = F(1) / t8;
+  }
+  const F ir2 = oner * oner;
   const F c6t6 = c6 * it6, c6t8 = c6 * it8;
   const F t27 = v[2] * c6t8;
   F e = -(c6t6 + t27) * eps2;
   F drij = eps2 * (c6t6 * F(6) * r4 * it6 + F(8) * t27 * r6 * it8);
   if (r < F(25)) {
     const F alpha = v[4];
-    const F t = v[3] * q_exp<F>(-alpha * r);
+    F ex;
+    if constexpr (std::is_same<F, float>::value) ex = __expf(-alpha * r);
+    else ex = q_exp<F>(-alpha * r);
+    const F t = v[3] * ex;
     e = e + t * oner * eps2;
     drij = drij - eps2 * t * (alpha * r + F(1)) * oner * ir2;
   }
@@ -845,7 +875,10 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
       }
     }
     for (int k = 0; k < ncol; ++k) {
-      if (m >= 0 && col == k) scatter<NA>(c, G, distinct);
+      if (m >= 0 && col == k) {
+        if constexpr (MIXED && KIND == 3) scatter_pair<NA>(c, G);
+        else scatter<NA>(c, G, distinct);
+      }
       __syncwarp();
     }
   }
@@ -853,8 +886,8 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
 
 // Shared memory per warp (bytes): coordinates (3n doubles), the FP32 split
 // (hi, lo) (3n float pairs) and the gradient (3n doubles, or (sum,
-// compensation) float pairs).
-__host__ __device__ inline size_t warp_smem_bytes(int n) { return (size_t)3 * n * (8 + 4 + 4 + 8); }
+// compensation) float pairs and the 3n floats of the pair sum).
+__host__ __device__ inline size_t warp_smem_bytes(int n) { return (size_t)3 * n * (8 + 4 + 4 + 8 + 4); }
 
 // Energy (with E_zero) and gradient (times gscale) of one bead by one warp.
 // ws: the warp's shared memory with the bead's FP64 coordinates in its first
@@ -875,7 +908,11 @@ __device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, doub
       hl[a] = make_float2(h, __double2float_rn(v - (double)h));
     }
     G.sk = (float2*)gs;
-    for (int a = lane; a < n3; a += 32) G.sk[a] = make_float2(0.f, 0.f);
+    G.pr = (float*)(G.sk + n3);
+    for (int a = lane; a < n3; a += 32) {
+      G.sk[a] = make_float2(0.f, 0.f);
+      G.pr[a] = 0.f;
+    }
   } else {
     G.g = (double*)gs;
     for (int a = lane; a < n3; a += 32) G.g[a] = 0.0;
