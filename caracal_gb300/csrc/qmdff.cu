@@ -500,6 +500,58 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   D.e_zero = d->e_zero;
   D.distinct = distinct ? 1 : 0;
   for (int k = 0; k < cr::qmdff::kKinds; ++k) D.nterm[k] = ff->nterm[k];
+  // mixed form bond polynomial: a k u (1 - u) / r^2 = t H(t), t = r^2/r0^2 - 1,
+  // H(t) = (a k / r0^2) [(1+t)^-(a/4+1) - (1+t)^-(a/2+1)] / t interpolated
+  // at 48 Chebyshev nodes of |t| <= kBondSerMaxT, truncated to degree 23 and
+  // written as a monomial in x = t / kBondSerMaxT; bonds with exponents
+  // outside (0, 20] keep the FP32 formula
+  {
+    using cr::qmdff::kBondPoly;
+    using cr::qmdff::kBondSer;
+    const double T = cr::qmdff::kBondSerMaxT;
+    const int nn = 48;
+    std::vector<float2> bser((size_t)kBondSer * std::max(d->nbond, 1), make_float2(0.f, 0.f));
+    auto split = [](double v) {
+      const float hi = (float)v;
+      return make_float2(hi, (float)(v - (double)hi));
+    };
+    for (int m = 0; m < d->nbond; ++m) {
+      const double r0 = vbond[(size_t)3 * m], kk = vbond[(size_t)3 * m + 1], aa = vbond[(size_t)3 * m + 2];
+      float2* row = &bser[(size_t)kBondSer * m];
+      row[0] = split(1.0 / (r0 * r0));
+      row[1] = split(r0 * r0);
+      if (!(aa > 0.0) || aa > 20.0 || !(r0 > 0.0)) continue;
+      const double p1 = aa / 4.0 + 1.0, p2 = aa / 2.0 + 1.0, scale = aa * kk / (r0 * r0);
+      std::vector<double> hv((size_t)nn), cheb((size_t)kBondPoly, 0.0);
+      for (int k = 0; k < nn; ++k) {
+        const double xk = std::cos(pi * (k + 0.5) / nn), tk = T * xk;
+        hv[(size_t)k] = (std::pow(1.0 + tk, -p1) - std::pow(1.0 + tk, -p2)) / tk;
+      }
+      for (int j = 0; j < kBondPoly; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < nn; ++k) acc += hv[(size_t)k] * std::cos(pi * j * (k + 0.5) / nn);
+        cheb[(size_t)j] = (j == 0 ? 1.0 : 2.0) * acc / nn;
+      }
+      // Chebyshev -> monomial in x: T_0 = 1, T_1 = x, T_{j+1} = 2x T_j - T_{j-1}
+      std::vector<double> tm1((size_t)kBondPoly, 0.0), t0((size_t)kBondPoly, 0.0), mono((size_t)kBondPoly, 0.0);
+      tm1[0] = 1.0;
+      if (kBondPoly > 1) t0[1] = 1.0;
+      for (int j = 0; j < kBondPoly; ++j) {
+        const std::vector<double>& tj = j == 0 ? tm1 : t0;
+        for (int n = 0; n < kBondPoly; ++n) mono[(size_t)n] += cheb[(size_t)j] * tj[(size_t)n];
+        if (j >= 1 && j + 1 < kBondPoly) {
+          std::vector<double> tn((size_t)kBondPoly, 0.0);
+          for (int n = 0; n + 1 < kBondPoly; ++n) tn[(size_t)n + 1] += 2.0 * t0[(size_t)n];
+          for (int n = 0; n < kBondPoly; ++n) tn[(size_t)n] -= tm1[(size_t)n];
+          tm1 = t0;
+          t0 = tn;
+        }
+      }
+      row[2] = make_float2(1.0f, 0.0f);
+      for (int n = 0; n < kBondPoly; ++n) row[3 + n] = split(scale * mono[(size_t)n]);
+    }
+    up(bser, &D.bser);
+  }
   // unit tables of the linear parameters (parameter gradients)
   std::vector<double> ubond = vbond, uangl = vangl, utors = vtors, upair = vpair;
   for (int m = 0; m < d->nbond; ++m) ubond[(size_t)3 * m + 1] = 1.0;

@@ -74,7 +74,38 @@ struct Dev {
   int zahn;
   int distinct;  // 1: every term's atoms are pairwise distinct
   int nterm[kKinds];  // terms per kind
+  // mixed form, bond stretch gradient as a double-FP32 polynomial (see
+  // bond_mixed): per bond kBondSer (hi, lo) pairs: 1/r0^2, r0^2, (use flag,
+  // 0), the kBondPoly coefficients
+  const float2* bser;
 };
+
+constexpr int kBondPoly = 24;             // polynomial of degree 23
+constexpr int kBondSer = kBondPoly + 3;
+constexpr double kBondSerMaxT = 0.45;     // used for |r^2/r0^2 - 1| <= this
+
+// Double-FP32 ("float-float") numbers hi + lo, |lo| <= ulp(hi)/2: about 44
+// bits of significand from FP32 operations (error-free sum of Knuth, product
+// split by FMA).  Used where FP32 rounding would set the mixed form's error.
+struct FF {
+  float hi, lo;
+};
+__device__ inline FF ff_norm(float s, float e) {
+  const float h = s + e;
+  return FF{h, e - (h - s)};
+}
+__device__ inline FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi, bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);
+  return ff_norm(s, e + (a.lo + b.lo));
+}
+__device__ inline FF ff_mul(FF a, FF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return ff_norm(p, e);
+}
+__device__ inline FF ff_of(float2 v) { return FF{v.x, v.y}; }
 
 template <class F> __device__ inline F q_sqrt(F x);
 template <> __device__ inline double q_sqrt<double>(double x) { return sqrt(x); }
@@ -182,6 +213,16 @@ __device__ inline void scatter(const Contrib<double>& c, Grad<double>& G, bool) 
 #pragma unroll
     for (int d = 0; d < 3; ++d) G.add(3 * c.a[m] + d, c.g[m][d]);
 }
+// bond of the mixed form: (hi, lo) parts in g[0..1] and g[2..3]
+__device__ inline void scatter_bond(const Contrib<float>& c, Grad<float>& G) {
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      G.add(3 * c.a[m] + d, c.g[m][d]);
+      G.add(3 * c.a[m] + d, c.g[m + 2][d]);
+    }
+}
 template <int NA>
 __device__ inline void scatter_pair(const Contrib<float>& c, Grad<float>& G) {
   float a[NA][3];
@@ -287,16 +328,38 @@ __device__ inline F bond_plain(const Dev& D, const Tables<typename ParamOf<F>::t
 // Mixed form: with u = (r0/r)^(a/2) = exp(-(a/2) log1p(x)), x = (r - r0)/r0
 // taken from the FP64 r^2 - r0^2, e = k (1 - u)^2 and the gradient factor
 // a k u (1 - u) / r^2 are free of the cancellation in 1 + u^2 - 2u.
+// Bond stretches carry the largest forces of a molecule, so FP32 roundings
+// of their gradient set the form's force error (~4e-7 of the largest force;
+// angles, torsions and pairs stay below 7e-8).  The gradient is therefore
+// taken in double-FP32 arithmetic without transcendentals: with
+// t = r^2/r0^2 - 1,
+// a k u (1 - u) / r^2 = (a k / r0^2) [(1+t)^-(a/4+1) - (1+t)^-(a/2+1)]
+//                     = t H(t),
+// H a degree-23 polynomial in t / kBondSerMaxT (Chebyshev interpolation of
+// H on |t| <= kBondSerMaxT, fitted per bond on the host, relative error
+// below 1e-10 for exponents a <= 16), summed by Horner; the displacement
+// comes exactly from the (hi, lo) coordinates and the gradient is scattered
+// as its (hi, lo) pair.  Beyond that range, and for the energy, the FP32
+// formula above (the FP64 pipe would cost more than the whole FP32 term).
 __device__ inline float bond_mixed(const Dev& D, const BeadPos& x, int m, Contrib<float>& c) {
   const int i = D.bond[2 * m], j = D.bond[2 * m + 1];
-  double rd[3];
-  disp<double>(x, i, j, rd);
-  const double r2d = rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2];
-  const double r0d = D.d.vbond[3 * m];
-  const float r2 = (float)r2d;
+  const float2* ser = D.bser + (size_t)kBondSer * m;
+  // displacement as double-FP32 from the (hi, lo) coordinates
+  FF dv[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float2 a = x.hl[3 * i + d], b = x.hl[3 * j + d];
+    dv[d] = ff_add(FF{a.x, a.y}, FF{-b.x, -b.y});
+  }
+  FF r2f = ff_mul(dv[0], dv[0]);
+  r2f = ff_add(r2f, ff_mul(dv[1], dv[1]));
+  r2f = ff_add(r2f, ff_mul(dv[2], dv[2]));
+  const FF r0sq = ff_of(__ldg(ser + 1));
+  const float r2 = r2f.hi;
   const float r = sqrtf(r2);
-  const float r0 = (float)r0d;
-  const float dr = (float)(r2d - r0d * r0d) / (r + r0);  // r - r0
+  const float r0 = D.f.vbond[3 * m];
+  const FF d2 = ff_add(r2f, FF{-r0sq.hi, -r0sq.lo});
+  const float dr = (d2.hi + d2.lo) / (r + r0);  // r - r0
   const float kij = D.f.vbond[3 * m + 1], aai = D.f.vbond[3 * m + 2];
   const float lg = -0.5f * aai * log1pf(dr / r0);
   const float omu = -expm1f(lg);  // 1 - u
@@ -305,11 +368,31 @@ __device__ inline float bond_mixed(const Dev& D, const BeadPos& x, int m, Contri
   c.na = 2;
   c.a[0] = i;
   c.a[1] = j;
+  const FF t = ff_add(ff_mul(r2f, ff_of(__ldg(ser))), FF{-1.0f, 0.0f});
+  if (__ldg(ser + 2).x != 0.0f && fabsf(t.hi) <= (float)kBondSerMaxT) {
+    // 1 / kBondSerMaxT = 20/9 as a double-FP32 constant
+    const FF xs = ff_mul(t, FF{2.22222232818603515625f, -1.0596381372e-07f});
+    FF h = ff_of(__ldg(ser + 3 + kBondPoly - 1));
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const float rb = (float)rd[d];
-    c.g[0][d] = fac * rb;
-    c.g[1][d] = -fac * rb;
+    for (int k = kBondPoly - 2; k >= 0; --k) h = ff_add(ff_mul(h, xs), ff_of(__ldg(ser + 3 + k)));
+    const FF f = ff_mul(t, h);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const FF g = ff_mul(f, dv[d]);
+      c.g[0][d] = g.hi;
+      c.g[1][d] = -g.hi;
+      c.g[2][d] = g.lo;
+      c.g[3][d] = -g.lo;
+    }
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float rb = dv[d].hi;
+      c.g[0][d] = fac * rb;
+      c.g[1][d] = -fac * rb;
+      c.g[2][d] = 0.0f;
+      c.g[3][d] = 0.0f;
+    }
   }
   return kij * omu * omu;
 }
@@ -877,6 +960,7 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
     for (int k = 0; k < ncol; ++k) {
       if (m >= 0 && col == k) {
         if constexpr (MIXED && KIND == 3) scatter_pair<NA>(c, G);
+        else if constexpr (MIXED && KIND == 0) scatter_bond(c, G);
         else scatter<NA>(c, G, distinct);
       }
       __syncwarp();
