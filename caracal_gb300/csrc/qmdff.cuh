@@ -267,7 +267,8 @@ __device__ inline void abdamp(F radi, F radj, F r2, F& damp, F& ddamp) {
   const F rcut = pre * (s * s);
   const F x = r2 / rcut;
   const F rr = x * x;
-  damp = F(1) / (F(1) + rr);
+  if constexpr (std::is_same<F, float>::value) damp = __frcp_rn(1.0f + rr);  // = 1/(1 + rr), correctly rounded
+  else damp = F(1) / (F(1) + rr);
   ddamp = F(-4) * rr * (damp * damp) / r2;
 }
 
@@ -414,7 +415,11 @@ __device__ inline F angle_term(const Dev& D, const Tables<typename ParamOf<F>::t
   const F al = q_sqrt<F>(rab2), bl = q_sqrt<F>(rcb2);
   F cosa = (al > F(0) && bl > F(0)) ? dot3(vab, vcb) / (al * bl) : F(0);
   cosa = fmin(F(1), fmax(F(-1), cosa));
-  const F theta = q_acos<F>(cosa);
+  // FP32: theta only for linear reference angles; sin(theta) of the
+  // harmonic-cosine form as sqrt((1 - c)(1 + c)), free of cancellation away
+  // from c = +-1 (where the linear form is used)
+  F theta = F(0);
+  if (!std::is_same<F, float>::value || v[3] != F(0)) theta = q_acos<F>(cosa);
   F dampij, damp2ij, dampjk, damp2jk;
   abdamp<F>(T.rad[i], T.rad[j], rab2, dampij, damp2ij);
   abdamp<F>(T.rad[k], T.rad[j], rcb2, dampjk, damp2jk);
@@ -427,7 +432,10 @@ __device__ inline F angle_term(const Dev& D, const Tables<typename ParamOf<F>::t
   } else {
     const F dd = cosa - cc0;
     ea = kijk * (dd * dd);
-    deddt = F(2) * kijk * q_sin<F>(theta) * (cc0 - cosa);
+    F sth;
+    if constexpr (std::is_same<F, float>::value) sth = sqrtf((1.0f - cosa) * (1.0f + cosa));
+    else sth = q_sin<F>(theta);
+    deddt = F(2) * kijk * sth * (cc0 - cosa);
   }
   F deda[3], dedc[3];
   cross(vab, vp, deda);
@@ -484,8 +492,9 @@ __device__ inline F dihedral(const F* ra, const F* rb, const F* rc, F* na, F* nb
     const float sn = sqrtf(dot3(rb, rb)) * fabsf(dot3(na, rc));
     phi = atan2f(sn, cn);
     const float den = nan_ * nbn;
-    cosphi = den > 0.f ? cn / den : 1.f;
-    sinphi = den > 0.f ? sn / den : 0.f;
+    const float id = den > 0.f ? __frcp_rn(den) : 0.f;
+    cosphi = den > 0.f ? cn * id : 1.f;
+    sinphi = den > 0.f ? sn * id : 0.f;
   }
   return phi;
 }
@@ -526,7 +535,16 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
 #pragma unroll
       for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = F(0);
     } else {
-      const F on = F(1) / nenner, rba_ = nbn / nan_, rab_ = nan_ / nbn;
+      F on, rba_, rab_;
+      if constexpr (std::is_same<F, float>::value) {
+        on = __frcp_rn(nenner);
+        rba_ = nbn * __frcp_rn(nan_);
+        rab_ = nan_ * __frcp_rn(nbn);
+      } else {
+        on = F(1) / nenner;
+        rba_ = nbn / nan_;
+        rab_ = nan_ / nbn;
+      }
       const F rapb[3] = {ra[0] + rb[0], ra[1] + rb[1], ra[2] + rb[2]};
       const F rbpc[3] = {rb[0] + rc[0], rb[1] + rc[1], rb[2] + rc[2]};
       F t_rab[3], t_rba[3], t_rac[3], t_rbb[3], t_rbc[3], t_raa[3], rapba[3], rapbb[3], rbpca[3], rbpcb[3];
@@ -552,12 +570,23 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
     dij = F(0);
     const F phipi = phi - pi;
     const F ef = q_erf<F>(phipi);
-    const F expo = q_exp<F>(-(phipi * phipi)) / spi;
+    F expo;
+    if constexpr (std::is_same<F, float>::value) expo = q_exp<F>(-(phipi * phipi)) * 0.564189583547756286948f;  // 1/sqrt(pi)
+    else expo = q_exp<F>(-(phipi * phipi)) / spi;
     for (int it = 0; it < nt; ++it) {
       const F rn = vt[2 + 3 * it], ph = vt[3 + 3 * it], vn = vt[4 + 3 * it];
       const F c1 = rn * (phi - phi0) + ph;
       const F c2 = rn * (phi + phi0 - pi2) + ph;
-      const F x1cos = q_cos<F>(c1), x2cos = q_cos<F>(c2), x1sin = q_sin<F>(c1), x2sin = q_sin<F>(c2);
+      F x1cos, x2cos, x1sin, x2sin;
+      if constexpr (std::is_same<F, float>::value) {
+        sincosf(c1, &x1sin, &x1cos);
+        sincosf(c2, &x2sin, &x2cos);
+      } else {
+        x1cos = q_cos<F>(c1);
+        x2cos = q_cos<F>(c2);
+        x1sin = q_sin<F>(c1);
+        x2sin = q_sin<F>(c2);
+      }
       const F e1 = vn * (F(1) + x1cos), e2 = vn * (F(1) + x2cos);
       et = et + F(0.5) * (F(1) - ef) * e1 + (F(0.5) + F(0.5) * ef) * e2;
       dij = dij - expo * e1 - F(0.5) * (F(1) - ef) * vn * x1sin * rn + expo * e2 -
