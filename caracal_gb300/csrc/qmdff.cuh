@@ -59,7 +59,8 @@ struct Dev {
   int n;
   // [0] plain form: full 32-term batches, as many colours as needed (an FP64
   // term costs far more than a scatter round); [1] mixed form: NCI pairs in
-  // round-robin matchings (one colour), bonds one colour, others two.
+  // round-robin matchings (one colour), bonds up to 3 colours, angles 4,
+  // torsions 6, H/halogen bonds 2.
   Schedule sched[2];
   const int* bond;   // 2 per bond (0-based)
   const int* angl;   // 3 per angle (centre, i, k)

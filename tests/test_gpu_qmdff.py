@@ -47,11 +47,11 @@ def geoms(ff, nb, sigma, seed):
 def test_schedule_covers_every_term(gpu_ff):
     info = gpu_ff.schedule_info()
     b = info["batches"]
-    # bonds and NCI pairs take one colour per batch (at most 31 terms on 62
-    # atoms), angles and torsions at most two
+    # mixed form: NCI pairs in matchings of one colour (at most 31 terms on 62
+    # atoms); bonds, angles, torsions with at most 3, 4, 6 colours per batch
     assert b[0] >= 2 and b[3] >= (1710 + 30) // 31
     assert b[1] >= 4 and b[2] >= 6
-    assert sum(b) <= info["colors"] <= b[0] + 2 * b[1] + 2 * b[2] + b[3]
+    assert sum(b) <= info["colors"] <= 3 * b[0] + 4 * b[1] + 6 * b[2] + b[3] + 2 * b[4]
 
 
 def test_egrad_fp64_matches_oracle(gpu_ff, alkane):
