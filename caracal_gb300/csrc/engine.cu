@@ -16,6 +16,7 @@
 #include "rpmd_kernel.cuh"
 #include "host_util.h"
 #include "qmdff_host.h"
+#include "water_host.h"
 #include "split.cuh"
 
 namespace {
@@ -186,6 +187,8 @@ __global__ void sum_beads_kernel(int T, int P, const double* V, double* epot) {
 // ---------------------------------------------------------------------------
 // Engine
 // ---------------------------------------------------------------------------
+constexpr int kHostGroups = 8;  // most trajectory groups of the pipelined host-buffer step
+
 struct cr_engine {
   cr_config cfg{};
   std::vector<double> mass;
@@ -209,6 +212,7 @@ struct cr_engine {
   // large-molecule path (QMDFF): state in HBM, a captured graph per step
   cr_qmdff* ff = nullptr;
   cr_evb* evb = nullptr;               // dE-EVB of two force fields (ff = the first)
+  cr_water* water = nullptr;           // flexible SPC water box
   double *d_V2 = nullptr, *d_f2 = nullptr;  // second force field's energies / gradients
   bool split = false;
   cr::SplitParams sp{};
@@ -228,6 +232,14 @@ struct cr_engine {
   // umbrella windows (graph path, analytic surfaces)
   double *d_umb = nullptr;   // [T] centres, [T] force constants, [T] xsum, [T] xsum2, [T][nbins] histogram
   int* d_umb_flag = nullptr; // sampling switch
+  double* d_fdrift = nullptr;  // split_drift_fast_kernel table (SplitParams::fdrift)
+  int fast_M = 0;              // P / 2 when the drift runs by fast cosine transforms, else 0
+  double *d_fsum = nullptr, *d_fmove = nullptr;  // split finish scratch (SplitParams::fsum, fmove)
+  int* d_fstat = nullptr;
+  // host-buffer step (cr_engine_step_host): trajectory groups whose copies in,
+  // step and copies out overlap on separate streams
+  cudaStream_t hs_in = nullptr, hs_out = nullptr, hs_c[kHostGroups] = {};
+  cudaEvent_t hev_in[kHostGroups] = {}, hev_c[kHostGroups] = {}, hev_out = nullptr;
 };
 
 namespace {
@@ -289,6 +301,27 @@ void build_split_propagator(int P, double beta, double dt, const cr::PropDims& d
     }
 }
 
+// Table of split_drift_fast_kernel for even P = 2M: per mode k = 0..M the
+// weights w_k / P (w_0 = w_M = 1, else 2) times pc, pd, pq of mode_tables,
+// then the factors 1 / (2 cos(pi (2k+1) / (2N))) of Lee's type-III recursion
+// for N = 2, 4, ..., M/2 at [N/2 - 1 + k].
+void build_fast_drift(int P, double beta, double dt, std::vector<double>& tab) {
+  const int M = P / 2;
+  std::vector<double> C, diag[3];
+  mode_tables(P, beta, dt, C, diag);
+  tab.assign((size_t)cr::fast_drift_doubles(M), 0.0);
+  for (int k = 0; k <= M; ++k) {
+    const double w = (k == 0 || k == M) ? 1.0 / P : 2.0 / P;
+    tab[(size_t)k] = w * diag[0][(size_t)k];
+    tab[(size_t)(M + 1) + k] = w * diag[2][(size_t)k];
+    tab[(size_t)2 * (M + 1) + k] = w * diag[1][(size_t)k];
+  }
+  for (int N = 2; N <= M / 2; N *= 2)
+    for (int k = 0; k < N / 2; ++k)
+      tab[(size_t)3 * (M + 1) + N / 2 - 1 + k] = 1.0 / (2.0 * std::cos(kPi * (2 * k + 1) / (2.0 * N)));
+}
+
+
 // PILE-L circulant vectors a (friction) and b (noise) of O^T diag(c) O with O
 // the orthonormal real normal-mode matrix; gamma_0 = 1/tau0, gamma_k = 2 w_k.
 void build_pile(int P, double beta, double dt, double tau0, std::vector<double>& out) {
@@ -346,6 +379,31 @@ int launch_run(cr_engine* e, int nsteps, bool dev_step = false) {
   return CR_OK;
 }
 
+// One step of trajectories [t0, t0 + tn) by the persistent kernel on stream
+// st (the shared-memory limit is set by the caller): per-trajectory arrays
+// offset, the noise key of trajectory t0, the step index from the host.
+template <class PES>
+int launch_group(cr_engine* e, int t0, int tn, cudaStream_t st) {
+  auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
+                                                  : cr::rpmd_run_kernel<PES, false>;
+  cr::StepParams prm = e->prm;
+  const size_t off = (size_t)t0 * e->P * e->NC;
+  prm.istep_dev = nullptr;
+  prm.T = tn;
+  prm.traj0 += (uint32_t)t0;
+  prm.q += off;
+  prm.p += off;
+  prm.f += off;
+  prm.epot += t0;
+  prm.status += t0;
+  prm.vnh += 4 * (size_t)t0;
+  if (prm.side) prm.side += (size_t)t0 * prm.side_stride;
+  const int groups = e->block / e->G;
+  kern<<<(tn + groups - 1) / groups, e->block, e->smem, st>>>(prm, e->istep, 1);
+  CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
 template <class PES>
 int set_run_smem(cr_engine* e) {
   auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
@@ -380,10 +438,17 @@ int egrad_launch(cr_engine* e, double* V, double* f) {
   return CR_OK;
 }
 
-int split_forces(cr_engine* e, double* V, double* f) {
+// Forces of trajectories [t0, t0 + tn) on stream st (V, f: that range's
+// outputs).  The analytic surfaces go through here only for constrained
+// parents, which always cover every trajectory.
+int split_forces_range(cr_engine* e, int t0, int tn, double* V, double* f, cudaStream_t st) {
+  const size_t off = (size_t)t0 * e->P * e->NC;
   if (e->evb)
-    return evb_launch(e->evb, e->d_q, e->T * e->P, V, f, e->d_V2, e->d_f2, e->cfg.precision, e->stream);
-  if (e->ff) return qmdff_launch(e->ff, e->d_q, e->T * e->P, V, f, e->cfg.precision, e->stream);
+    return evb_launch(e->evb, e->d_q + off, tn * e->P, V, f, e->d_V2 + (size_t)t0 * e->P, e->d_f2 + off,
+                      e->cfg.precision, st);
+  if (e->ff) return qmdff_launch(e->ff, e->d_q + off, tn * e->P, V, f, e->cfg.precision, st);
+  if (e->water) return water_launch(e->water, e->d_q + off, tn * e->P, V, f, e->cfg.precision, st);
+  if (t0 != 0 || tn != e->T || st != e->stream) return fail(CR_ERR_UNSUPPORTED, "analytic forces cover every trajectory");
   switch (e->cfg.pes) {
     case CR_PES_H3: return egrad_launch<cr::PesH3>(e, V, f);
     case CR_PES_CH4H: return egrad_launch<cr::PesCH4H>(e, V, f);
@@ -391,6 +456,8 @@ int split_forces(cr_engine* e, double* V, double* f) {
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
+
+int split_forces(cr_engine* e, double* V, double* f) { return split_forces_range(e, 0, e->T, V, f, e->stream); }
 
 // SHAKE / RATTLE of the constrained parent (template on the atom count)
 int parent_kernel(cr_engine* e, int which) {
@@ -417,54 +484,117 @@ int parent_kernel(cr_engine* e, int which) {
   return CR_OK;
 }
 
-// One step of the large-molecule path as kernel launches on e->stream
-// (recorded once into a CUDA graph).
-int split_step_launches(cr_engine* e) {
+// The engine's graph-path parameters restricted to trajectories
+// [t0, t0 + tn): per-trajectory arrays offset, the noise key of trajectory t0.
+cr::SplitParams split_params_range(const cr_engine* e, int t0, int tn) {
+  cr::SplitParams s = e->sp;
+  const size_t off = (size_t)t0 * e->P * e->NC;
+  s.T = tn;
+  s.traj0 += (uint32_t)t0;
+  s.q += off;
+  s.p += off;
+  s.f += off;
+  s.V += (size_t)t0 * e->P;
+  s.epot += t0;
+  s.status += t0;
+  s.vnh += 4 * (size_t)t0;
+  const int S = cr::finish_slices(e->P * e->N);
+  s.fsum += (size_t)t0 * S * cr::kFinishSums;
+  s.fstat += (size_t)t0 * S;
+  s.fmove += (size_t)t0 * cr::kMoveDoubles;
+  return s;
+}
+
+// The kernels of one step of the large-molecule path for the trajectories
+// of s (s = split_params_range(e, t0, tn)) on stream st; the caller advances
+// the device step counter.  Constrained parents and umbrella windows step
+// every trajectory at once on e->stream.  *nl counts the launches.
+int split_group_launches(cr_engine* e, const cr::SplitParams& s, int t0, int tn, cudaStream_t st, int* nl) {
+  const bool whole = t0 == 0 && tn == e->T && st == e->stream;
+  if ((e->parent || s.umbrella) && !whole)
+    return fail(CR_ERR_UNSUPPORTED, "constrained parents and umbrella windows step every trajectory at once");
   const int cw = cr::split_chunk(e->P);
-  const dim3 grid((e->NC + cw - 1) / cw, e->T);
+  const dim3 grid((e->NC + cw - 1) / cw, tn);
   const bool nhc = e->cfg.thermostat == CR_THERMO_NHC;
+  int n = 0;
   if (nhc) {
-    cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+    cr::split_nhc_kernel<<<tn, cr::kFinishBlock, 0, st>>>(s);
     CR_CUDA(cudaGetLastError());
+    ++n;
   }
-  cr::split_drift_kernel<<<grid, cr::kSplitBlock, e->smem_drift, e->stream>>>(e->sp);
+  switch (e->fast_M) {
+    case 4: cr::split_drift_fast_kernel<4><<<dim3((e->NC + 63) / 64, tn), 128, 0, st>>>(s); break;
+    case 8: cr::split_drift_fast_kernel<8><<<dim3((e->NC + 63) / 64, tn), 128, 0, st>>>(s); break;
+    case 16: cr::split_drift_fast_kernel<16><<<dim3((e->NC + 63) / 64, tn), 128, 0, st>>>(s); break;
+    case 32: cr::split_drift_fast_kernel<32><<<dim3((e->NC + 63) / 64, tn), 128, 0, st>>>(s); break;
+    default: cr::split_drift_kernel<<<grid, cr::kSplitBlock, e->smem_drift, st>>>(s);
+  }
   CR_CUDA(cudaGetLastError());
+  ++n;
   int rc;
   if (e->parent && (rc = parent_kernel(e, 0))) return rc;  // SHAKE (src/verlet.f90:746-757)
-  rc = split_forces(e, e->d_V, e->d_f);
+  rc = split_forces_range(e, t0, tn, s.V, s.f, st);
   if (rc) return rc;
-  if (e->sp.umbrella) {  // src/verlet.f90:1043-1046
+  n += e->evb ? 3 : 1;
+  if (s.umbrella) {  // src/verlet.f90:1043-1046
     switch (e->N) {
-      case 3: cr::split_umbrella_kernel<3><<<e->T, 64, 0, e->stream>>>(e->sp); break;
-      case 6: cr::split_umbrella_kernel<6><<<e->T, 64, 0, e->stream>>>(e->sp); break;
-      case 7: cr::split_umbrella_kernel<7><<<e->T, 64, 0, e->stream>>>(e->sp); break;
+      case 3: cr::split_umbrella_kernel<3><<<tn, 64, 0, st>>>(s); break;
+      case 6: cr::split_umbrella_kernel<6><<<tn, 64, 0, st>>>(s); break;
+      case 7: cr::split_umbrella_kernel<7><<<tn, 64, 0, st>>>(s); break;
       default: return fail(CR_ERR_UNSUPPORTED, "umbrella windows are built for the analytic surfaces");
     }
     CR_CUDA(cudaGetLastError());
+    ++n;
   }
   if (e->parent) {
     // 1/2 kick, RATTLE (src/verlet.f90:1080-1082), NHC, then Andersen / PILE
-    cr::split_kick_kernel<<<grid, cr::kSplitBlock, 0, e->stream>>>(e->sp, 1);
+    cr::split_kick_kernel<<<grid, cr::kSplitBlock, 0, st>>>(s, 1);
     CR_CUDA(cudaGetLastError());
     if ((rc = parent_kernel(e, 1))) return rc;
     if (nhc) {
-      cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      cr::split_nhc_kernel<<<tn, cr::kFinishBlock, 0, st>>>(s);
       CR_CUDA(cudaGetLastError());
     }
     if (e->cfg.thermostat == CR_THERMO_ANDERSEN || e->cfg.thermostat == CR_THERMO_PILE) {
-      cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp, 2);
+      cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, st>>>(s, 2);
       CR_CUDA(cudaGetLastError());
     }
   } else {
-    cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, e->stream>>>(e->sp, 0);
+    cr::split_kick_kernel<<<grid, cr::kSplitBlock, e->smem_kick, st>>>(s, 0);
     CR_CUDA(cudaGetLastError());
+    ++n;
     if (nhc) {
-      cr::split_nhc_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      cr::split_nhc_kernel<<<tn, cr::kFinishBlock, 0, st>>>(s);
       CR_CUDA(cudaGetLastError());
+      ++n;
     }
   }
-  cr::split_finish_kernel<<<e->T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
-  CR_CUDA(cudaGetLastError());
+  {
+    // NaN check, transrot, epot: moments per slice, a solve per trajectory,
+    // the momentum update per item
+    const int S = cr::finish_slices(e->P * e->N);
+    cr::split_moments_kernel<<<dim3(S, tn), cr::kMomentThreads, 0, st>>>(s);
+    CR_CUDA(cudaGetLastError());
+    cr::split_solve_kernel<<<(tn + 127) / 128, 128, 0, st>>>(s, S);
+    CR_CUDA(cudaGetLastError());
+    n += 2;
+    if (s.transrot) {
+      const long long items = (long long)tn * e->P * e->N;
+      const int grid = (int)std::min<long long>((items + cr::kMomentThreads - 1) / cr::kMomentThreads, 152LL * 16);
+      cr::split_apply_kernel<<<grid, cr::kMomentThreads, 0, st>>>(s);
+      CR_CUDA(cudaGetLastError());
+      ++n;
+    }
+  }
+  if (nl) *nl += n;
+  return CR_OK;
+}
+
+// One step of the large-molecule path as kernel launches on e->stream
+// (recorded once into a CUDA graph).
+int split_step_launches(cr_engine* e) {
+  int rc = split_group_launches(e, e->sp, 0, e->T, e->stream, nullptr);
+  if (rc) return rc;
   cr::split_advance_kernel<<<1, 1, 0, e->stream>>>(e->d_istep);
   CR_CUDA(cudaGetLastError());
   return CR_OK;
@@ -482,6 +612,7 @@ int split_prepare(cr_engine* e) {
   int rc = CR_OK;
   if (e->evb) rc = evb_launch(e->evb, e->d_q, 0, e->d_V, e->d_f, e->d_V2, e->d_f2, e->cfg.precision, e->stream);
   else if (e->ff) rc = qmdff_launch(e->ff, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
+  else if (e->water) rc = water_launch(e->water, e->d_q, 0, e->d_V, e->d_f, e->cfg.precision, e->stream);
   if (rc) return rc;
   // let the autotuner pick the force-kernel variant on this batch before it
   // is frozen into the graph; the gradient goes to scratch so f is untouched
@@ -713,11 +844,14 @@ int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq
 
 // Validation and set-up shared by both engine paths; ff != NULL selects the
 // large-molecule (QMDFF) path.
-static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_engine** out) {
+static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_water* water, cr_engine** out) {
   if (!cfg || !out) return fail(CR_ERR_ARG, "NULL argument");
   *out = nullptr;
   int N = -1;
-  if (evb) {
+  if (water) {
+    if (cfg->pes != CR_PES_WATER) return fail(CR_ERR_ARG, "cr_engine_create_water needs pes = CR_PES_WATER");
+    N = water->dev.n;
+  } else if (evb) {
     if (cfg->pes != CR_PES_EVB) return fail(CR_ERR_ARG, "cr_engine_create_evb needs pes = CR_PES_EVB");
     ff = evb_first(evb);
     N = ff->n;
@@ -725,16 +859,16 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
     if (cfg->pes != CR_PES_QMDFF) return fail(CR_ERR_ARG, "cr_engine_create_qmdff needs pes = CR_PES_QMDFF");
     N = ff->n;
   } else {
-    if (cfg->pes == CR_PES_QMDFF || cfg->pes == CR_PES_EVB)
-      return fail(CR_ERR_ARG, "force-field engines are created with cr_engine_create_qmdff / _evb");
+    if (cfg->pes == CR_PES_QMDFF || cfg->pes == CR_PES_EVB || cfg->pes == CR_PES_WATER)
+      return fail(CR_ERR_ARG, "force-field engines are created with cr_engine_create_qmdff / _evb / _water");
     N = pes_natoms(cfg->pes);
     if (N < 0) return fail(CR_ERR_UNSUPPORTED, "PES not available in this engine");
   }
   if (cfg->natoms != N) return fail(CR_ERR_ARG, "natoms does not match the PES");
   if (cfg->nbeads < 1 || cfg->nbeads > cr::kMaxBeads) return fail(CR_ERR_ARG, "nbeads must be 1..128");
   if (cfg->ntraj < 1) return fail(CR_ERR_ARG, "ntraj must be >= 1");
-  if (ff && (long long)cfg->ntraj * cfg->nbeads > (1LL << 26))
-    return fail(CR_ERR_ARG, "ntraj * nbeads must be <= 2^26 on the QMDFF path");
+  if ((ff || water) && (long long)cfg->ntraj * cfg->nbeads > (1LL << 26))
+    return fail(CR_ERR_ARG, "ntraj * nbeads must be <= 2^26 on the force-field path");
   if (!(cfg->dt > 0.0)) return fail(CR_ERR_ARG, "dt must be > 0");
   if (cfg->thermostat == CR_THERMO_NHC && !(cfg->nose_q > 0.0 && std::isfinite(cfg->nose_q)))
     return fail(CR_ERR_ARG, "the Nose-Hoover chain needs nose_q > 0");
@@ -766,7 +900,8 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
   e->cfg.mass = e->mass.data();
   e->ff = ff;
   e->evb = evb;
-  e->split = ff != nullptr;
+  e->water = water;
+  e->split = ff != nullptr || water != nullptr;
   e->N = N;
   e->NC = 3 * N;
   e->P = cfg->nbeads;
@@ -861,6 +996,22 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
         cudaMemcpy(e->d_sigma, sig.data(), (size_t)N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(e->d_istep, 0, sizeof(int)) != cudaSuccess)
       return cleanup_fail(fail(CR_ERR_CUDA, "upload of the split tables failed"));
+    const size_t nsl = (size_t)e->T * cr::finish_slices(e->P * N);
+    if (cudaMalloc(&e->d_fsum, nsl * cr::kFinishSums * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&e->d_fstat, nsl * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&e->d_fmove, (size_t)e->T * cr::kMoveDoubles * sizeof(double)) != cudaSuccess)
+      return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the finish scratch failed"));
+    // the free ring polymer by fast cosine transforms where P is 8..64, a
+    // power of two, and no PILE half step runs inside the drift
+    const int P = e->P;
+    if (pd.split && P >= 8 && P <= 64 && (P & (P - 1)) == 0 && cfg->thermostat != CR_THERMO_PILE) {
+      std::vector<double> tab;
+      build_fast_drift(P, cfg->beta, cfg->dt, tab);
+      if (cudaMalloc(&e->d_fdrift, tab.size() * 8) != cudaSuccess ||
+          cudaMemcpy(e->d_fdrift, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+        return cleanup_fail(fail(CR_ERR_CUDA, "upload of the fast drift table failed"));
+      e->fast_M = P / 2;
+    }
     s.T = e->T;
     s.P = e->P;
     s.N = N;
@@ -872,6 +1023,7 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
     s.traj0 = cfg->traj0;
     s.half_dt = 0.5 * cfg->dt;
     s.totmass = totmass;
+    s.wsum = tm;
     s.mass = e->d_mass;
     s.inv_mass = e->d_inv_mass;
     s.sigma = e->d_sigma;
@@ -887,6 +1039,10 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
     s.istep = e->d_istep;
     s.nhc = nhc;
     s.vnh = e->d_vnh;
+    s.fsum = e->d_fsum;
+    s.fdrift = e->d_fdrift;
+    s.fstat = e->d_fstat;
+    s.fmove = e->d_fmove;
     const bool pl = cfg->thermostat == CR_THERMO_PILE;
     const int cw = cr::split_chunk(e->P), sp1 = e->P + 1;
     e->smem_drift = cr::split_smem_doubles(s, pl) * sizeof(double);
@@ -940,16 +1096,21 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_eng
 
 extern "C" {
 
-int cr_engine_create(const cr_config* cfg, cr_engine** out) { return engine_create(cfg, nullptr, nullptr, out); }
+int cr_engine_create(const cr_config* cfg, cr_engine** out) { return engine_create(cfg, nullptr, nullptr, nullptr, out); }
 
 int cr_engine_create_qmdff(const cr_config* cfg, cr_qmdff* ff, cr_engine** out) {
   if (!ff) return fail(CR_ERR_ARG, "NULL force field");
-  return engine_create(cfg, ff, nullptr, out);
+  return engine_create(cfg, ff, nullptr, nullptr, out);
 }
 
 int cr_engine_create_evb(const cr_config* cfg, cr_evb* evb, cr_engine** out) {
   if (!evb) return fail(CR_ERR_ARG, "NULL EVB");
-  return engine_create(cfg, nullptr, evb, out);
+  return engine_create(cfg, nullptr, evb, nullptr, out);
+}
+
+int cr_engine_create_water(const cr_config* cfg, cr_water* w, cr_engine** out) {
+  if (!w) return fail(CR_ERR_ARG, "NULL water box");
+  return engine_create(cfg, nullptr, nullptr, w, out);
 }
 
 int cr_engine_destroy(cr_engine* e) {
@@ -982,10 +1143,27 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_shake_fail);
   cudaFree(e->d_umb);
   cudaFree(e->d_umb_flag);
+  cudaFree(e->d_fsum);
+  cudaFree(e->d_fdrift);
+  cudaFree(e->d_fstat);
+  cudaFree(e->d_fmove);
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->hs_in) {
+    cudaStreamSynchronize(e->hs_in);
+    cudaStreamSynchronize(e->hs_out);
+    cudaStreamDestroy(e->hs_in);
+    cudaStreamDestroy(e->hs_out);
+    cudaEventDestroy(e->hev_out);
+    for (int g = 0; g < kHostGroups; ++g) {
+      cudaStreamSynchronize(e->hs_c[g]);
+      cudaStreamDestroy(e->hs_c[g]);
+      cudaEventDestroy(e->hev_in[g]);
+      cudaEventDestroy(e->hev_c[g]);
+    }
+  }
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return CR_OK;
@@ -1144,20 +1322,115 @@ int cr_engine_run_dump(cr_engine* e, int nsteps, int every, cr_dump_fn dump, voi
   return CR_OK;
 }
 
+// Trajectory groups of the pipelined host-buffer step: about 2 MB of each
+// state array per group, at most kHostGroups; 1 (copy in, step, copy out in
+// sequence) where a group would be too small to pay for its launches, and
+// for constrained parents and umbrella windows.
+static int host_groups(const cr_engine* e) {
+  if (e->parent || (e->split && e->sp.umbrella)) return 1;
+  const size_t bytes = (size_t)e->T * e->P * e->NC * 8;
+  const size_t ng = bytes / (2u << 20);
+  return (int)std::max<size_t>(1, std::min<size_t>({ng, (size_t)kHostGroups, (size_t)e->T}));
+}
+
+static int host_pipeline_init(cr_engine* e) {
+  if (e->hs_in) return CR_OK;
+  CR_CUDA(cudaStreamCreateWithFlags(&e->hs_in, cudaStreamNonBlocking));
+  CR_CUDA(cudaStreamCreateWithFlags(&e->hs_out, cudaStreamNonBlocking));
+  CR_CUDA(cudaEventCreateWithFlags(&e->hev_out, cudaEventDisableTiming));
+  for (int g = 0; g < kHostGroups; ++g) {
+    CR_CUDA(cudaStreamCreateWithFlags(&e->hs_c[g], cudaStreamNonBlocking));
+    CR_CUDA(cudaEventCreateWithFlags(&e->hev_in[g], cudaEventDisableTiming));
+    CR_CUDA(cudaEventCreateWithFlags(&e->hev_c[g], cudaEventDisableTiming));
+  }
+  return CR_OK;
+}
+
+// The step of every group g: on hs_c[g] after its copies in, before its
+// copies out.
+static int host_group_step(cr_engine* e, int t0, int tn, cudaStream_t st, int* nl) {
+  if (e->split) return split_group_launches(e, split_params_range(e, t0, tn), t0, tn, st, nl);
+  ++*nl;
+  switch (e->cfg.pes) {
+    case CR_PES_H3: return launch_group<cr::PesH3>(e, t0, tn, st);
+    case CR_PES_CH4H: return launch_group<cr::PesCH4H>(e, t0, tn, st);
+    case CR_PES_CH4OH: return launch_group<cr::PesCH4OH>(e, t0, tn, st);
+    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  }
+}
+
 int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* epot) {
   if (!e || !q || !p || !f) return fail(CR_ERR_ARG, "NULL argument");
   if (e->xi_on && e->istep + 1 - e->side_step0 > e->side_cap)
     return fail(CR_ERR_ARG, "step exceeds the recrossing step capacity set by cr_engine_set_recross");
-  const size_t bytes = (size_t)e->T * e->P * e->NC * 8;
-  CR_CUDA(cudaMemcpyAsync(e->d_q, q, bytes, cudaMemcpyHostToDevice, e->stream));
-  CR_CUDA(cudaMemcpyAsync(e->d_p, p, bytes, cudaMemcpyHostToDevice, e->stream));
-  CR_CUDA(cudaMemcpyAsync(e->d_f, f, bytes, cudaMemcpyHostToDevice, e->stream));
-  int rc = engine_run_async(e, 1);
+  const int ng = host_groups(e);
+  const size_t per_traj = (size_t)e->P * e->NC;
+  if (ng <= 1) {
+    const size_t bytes = (size_t)e->T * per_traj * 8;
+    CR_CUDA(cudaMemcpyAsync(e->d_q, q, bytes, cudaMemcpyHostToDevice, e->stream));
+    CR_CUDA(cudaMemcpyAsync(e->d_p, p, bytes, cudaMemcpyHostToDevice, e->stream));
+    CR_CUDA(cudaMemcpyAsync(e->d_f, f, bytes, cudaMemcpyHostToDevice, e->stream));
+    int rc = engine_run_async(e, 1);
+    if (rc) return rc;
+    CR_CUDA(cudaMemcpyAsync(q, e->d_q, bytes, cudaMemcpyDeviceToHost, e->stream));
+    CR_CUDA(cudaMemcpyAsync(p, e->d_p, bytes, cudaMemcpyDeviceToHost, e->stream));
+    CR_CUDA(cudaMemcpyAsync(f, e->d_f, bytes, cudaMemcpyDeviceToHost, e->stream));
+    if (epot) CR_CUDA(cudaMemcpyAsync(epot, e->d_epot, (size_t)e->T * 8, cudaMemcpyDeviceToHost, e->stream));
+    return engine_finish(e);
+  }
+  // Pipelined: group g's copies in (hs_in), its step (hs_c[g]) and its
+  // copies out (hs_out) overlap the other groups' work; the device step
+  // counter is set before and advanced after every group.
+  int rc = host_pipeline_init(e);
   if (rc) return rc;
-  CR_CUDA(cudaMemcpyAsync(q, e->d_q, bytes, cudaMemcpyDeviceToHost, e->stream));
-  CR_CUDA(cudaMemcpyAsync(p, e->d_p, bytes, cudaMemcpyDeviceToHost, e->stream));
-  CR_CUDA(cudaMemcpyAsync(f, e->d_f, bytes, cudaMemcpyDeviceToHost, e->stream));
-  if (epot) CR_CUDA(cudaMemcpyAsync(epot, e->d_epot, (size_t)e->T * 8, cudaMemcpyDeviceToHost, e->stream));
+  if (e->split) {
+    if ((rc = split_prepare(e))) return rc;
+    e->h_istep = e->istep;
+    CR_CUDA(cudaMemcpyAsync(e->d_istep, &e->h_istep, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  } else {
+    switch (e->cfg.pes) {
+      case CR_PES_H3: rc = set_run_smem<cr::PesH3>(e); break;
+      case CR_PES_CH4H: rc = set_run_smem<cr::PesCH4H>(e); break;
+      case CR_PES_CH4OH: rc = set_run_smem<cr::PesCH4OH>(e); break;
+      default: rc = fail(CR_ERR_UNSUPPORTED, "PES not built");
+    }
+    if (rc) return rc;
+  }
+  CR_CUDA(cudaEventRecord(e->ev0, e->stream));
+  CR_CUDA(cudaStreamWaitEvent(e->hs_in, e->ev0, 0));
+  for (int g = 0; g < ng; ++g) {
+    const int t0 = (int)((long long)e->T * g / ng), t1 = (int)((long long)e->T * (g + 1) / ng);
+    const size_t off = (size_t)t0 * per_traj, bytes = (size_t)(t1 - t0) * per_traj * 8;
+    CR_CUDA(cudaMemcpyAsync(e->d_q + off, q + off, bytes, cudaMemcpyHostToDevice, e->hs_in));
+    CR_CUDA(cudaMemcpyAsync(e->d_p + off, p + off, bytes, cudaMemcpyHostToDevice, e->hs_in));
+    CR_CUDA(cudaMemcpyAsync(e->d_f + off, f + off, bytes, cudaMemcpyHostToDevice, e->hs_in));
+    CR_CUDA(cudaEventRecord(e->hev_in[g], e->hs_in));
+  }
+  int nl = 0;
+  for (int g = 0; g < ng; ++g) {
+    const int t0 = (int)((long long)e->T * g / ng), t1 = (int)((long long)e->T * (g + 1) / ng);
+    CR_CUDA(cudaStreamWaitEvent(e->hs_c[g], e->hev_in[g], 0));
+    if ((rc = host_group_step(e, t0, t1 - t0, e->hs_c[g], &nl))) return rc;
+    CR_CUDA(cudaEventRecord(e->hev_c[g], e->hs_c[g]));
+    CR_CUDA(cudaStreamWaitEvent(e->hs_out, e->hev_c[g], 0));
+    const size_t off = (size_t)t0 * per_traj, bytes = (size_t)(t1 - t0) * per_traj * 8;
+    CR_CUDA(cudaMemcpyAsync(q + off, e->d_q + off, bytes, cudaMemcpyDeviceToHost, e->hs_out));
+    CR_CUDA(cudaMemcpyAsync(p + off, e->d_p + off, bytes, cudaMemcpyDeviceToHost, e->hs_out));
+    CR_CUDA(cudaMemcpyAsync(f + off, e->d_f + off, bytes, cudaMemcpyDeviceToHost, e->hs_out));
+  }
+  // epot (often pageable: such a copy returns only when done) once, last
+  if (epot) CR_CUDA(cudaMemcpyAsync(epot, e->d_epot, (size_t)e->T * 8, cudaMemcpyDeviceToHost, e->hs_out));
+  for (int g = 0; g < ng; ++g) CR_CUDA(cudaStreamWaitEvent(e->stream, e->hev_c[g], 0));
+  if (e->split) {
+    cr::split_advance_kernel<<<1, 1, 0, e->stream>>>(e->d_istep);
+    CR_CUDA(cudaGetLastError());
+    ++nl;
+  }
+  CR_CUDA(cudaEventRecord(e->hev_out, e->hs_out));
+  CR_CUDA(cudaStreamWaitEvent(e->stream, e->hev_out, 0));
+  CR_CUDA(cudaEventRecord(e->ev1, e->stream));
+  e->istep += 1;
+  e->launches = nl;
   return engine_finish(e);
 }
 
@@ -1234,7 +1507,8 @@ extern "C" {
 
 int cr_engine_set_parent(cr_engine* e, const cr_recross* rc) {
   if (!e || !rc) return fail(CR_ERR_ARG, "NULL argument");
-  if (e->ff || e->evb) return fail(CR_ERR_UNSUPPORTED, "constrained parents are built for the analytic surfaces");
+  if (e->ff || e->evb || e->water)
+    return fail(CR_ERR_UNSUPPORTED, "constrained parents are built for the analytic surfaces");
   if (e->xi_on) return fail(CR_ERR_ARG, "a recrossing-children engine cannot be a parent");
   cr::XiDev x{};
   int rcode = make_xidev(e, rc, x);
@@ -1269,7 +1543,8 @@ int cr_engine_set_parent(cr_engine* e, const cr_recross* rc) {
 int cr_engine_set_umbrella(cr_engine* e, const cr_recross* rc, const double* centers, const double* kforce,
                            int nbins, double lo, double hi) {
   if (!e || !rc || !centers || !kforce) return fail(CR_ERR_ARG, "NULL argument");
-  if (e->ff || e->evb) return fail(CR_ERR_UNSUPPORTED, "umbrella windows are built for the analytic surfaces");
+  if (e->ff || e->evb || e->water)
+    return fail(CR_ERR_UNSUPPORTED, "umbrella windows are built for the analytic surfaces");
   if (e->xi_on || e->parent) return fail(CR_ERR_ARG, "an umbrella engine cannot be a parent or recrossing children");
   if (!(e->cfg.beta > 0.0) || !std::isfinite(e->cfg.beta)) return fail(CR_ERR_ARG, "umbrella sampling needs a temperature");
   if (nbins < 0 || (nbins > 0 && !(hi > lo))) return fail(CR_ERR_ARG, "bad histogram range");

@@ -489,6 +489,22 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   up(fvangl, &D.f.vangl);
   up(fvtors, &D.f.vtors);
   up(fvpair, &D.f.vpair);
+  // mixed-form pair constants (pair_mixed)
+  std::vector<float> fpair((size_t)kVPair * d->nnci);
+  for (int m = 0; m < d->nnci; ++m) {
+    const double* v = &vpair[(size_t)kVPair * m];
+    float* o = &fpair[(size_t)kVPair * m];
+    const double R02 = v[0] * v[0], R06 = R02 * R02 * R02;
+    o[0] = (float)R06;
+    o[1] = (float)(R06 * R02);
+    o[2] = (float)(v[5] * v[1]);
+    o[3] = (float)(v[5] * v[1] * v[2]);
+    o[4] = (float)(v[5] * v[3]);
+    o[5] = (float)(v[4] * 1.4426950408889634074);  // log2(e)
+    o[6] = (float)v[6];
+    o[7] = (float)v[4];
+  }
+  up(fpair, &D.fpair);
   if (rc != CR_OK) {
     cr_qmdff_destroy(ff);
     return rc;

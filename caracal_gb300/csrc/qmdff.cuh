@@ -79,6 +79,10 @@ struct Dev {
   // bond_mixed): per bond kBondSer (hi, lo) pairs: 1/r0^2, r0^2, (use flag,
   // 0), the kBondPoly coefficients
   const float2* bser;
+  // mixed form, NCI pairs with their constants folded (pair_mixed): per pair
+  // kVPair floats R0^6, R0^8, eps2 C6, eps2 C6 sr42, eps2 zab,
+  // alpha log2(e), qq, alpha, each rounded once from FP64
+  const float* fpair;
 };
 
 constexpr int kBondPoly = 24;             // polynomial of degree 23
@@ -778,6 +782,66 @@ __device__ inline F pair_term(const Dev& D, const Tables<typename ParamOf<F>::ty
   return e;
 }
 
+// FP32 hardware approximations (PTX rsqrt / rcp / ex2 .approx.ftz, relative
+// error about 2^-22): inputs here are normal numbers far from the limits.
+__device__ inline float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ inline float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ inline float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// One NCI pair in the mixed form: the formulas of pair_term with the
+// per-pair constants folded into the table Dev::fpair (R0^6 and R0^8 of the
+// BJ damping, eps2 into the C6 / C8 and repulsion prefactors, alpha log2(e)
+// for a base-2 exponential).  The pair forces are ~1 % of the valence
+// forces, so hardware approximations stay far below the form's error budget.
+__device__ inline float pair_mixed(const Dev& D, const BeadPos& x, int kp, Contrib<float>& c) {
+  const int2 ij = __ldg(reinterpret_cast<const int2*>(D.pair) + kp);
+  const int i1 = ij.x, i2 = ij.y;
+  float v[kVPair];
+  load_pair_params(&D.fpair[kVPair * kp], v);
+  float vab[3];
+  disp<float>(x, i1, i2, vab);
+  const float r2 = dot3(vab, vab);
+  const float oner = rsqrt_approx(r2), r = r2 * oner, ir2 = oner * oner;
+  const float r4 = r2 * r2, r6 = r4 * r2;
+  const float it6 = rcp_approx(r6 + v[0]), it8 = rcp_approx(r6 * r2 + v[1]);
+  const float d6 = v[2] * it6, d8 = v[3] * it8;
+  float e = -(d6 + d8);
+  float drij = 6.0f * d6 * (r4 * it6) + 8.0f * d8 * (r6 * it8);
+  if (r < 25.0f) {
+    const float t = v[4] * ex2_approx(-v[5] * r) * oner;
+    e += t;
+    drij = fmaf(-t * ir2, fmaf(v[7], r, 1.0f), drij);
+  }
+  if (!(r > D.fcoul_cut)) {
+    float e0;
+    if (D.zahn) e0 = v[6] * ((q_erfc<float>(D.fzahn_a * r) * oner) - D.fzahn_par * (r - D.fcoul_cut));
+    else e0 = v[6] * oner;
+    e += e0;
+    drij = fmaf(-e0, ir2, drij);
+  }
+  c.na = 2;
+  c.a[0] = i1;
+  c.a[1] = i2;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    c.g[0][d] = vab[d] * drij;
+    c.g[1][d] = -vab[d] * drij;
+  }
+  return e;
+}
+
 // x^5, x^6, x^12 by products (the reference's real-exponent ** operators)
 template <class F>
 __device__ inline F pow6(F x) {
@@ -947,7 +1011,7 @@ __device__ inline typename std::conditional<MIXED, float, double>::type term(
       case 0: return bond_mixed(D, x, m, c);
       case 1: return angle_term<float>(D, D.f, x, m, c);
       case 2: return torsion_term<float>(D, D.f, x, m, c);
-      case 3: return pair_term<float>(D, D.f, x, m, c);
+      case 3: return pair_mixed(D, x, m, c);
       default: return hb_term<float>(D, D.f, x, m, c);
     }
   } else {

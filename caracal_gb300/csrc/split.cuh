@@ -55,12 +55,14 @@ struct SplitParams {
   int thermostat, andersen_step, transrot;
   uint32_t seed, traj0;
   double half_dt, totmass;
+  double wsum;             // sum of the masses over beads and atoms (P sum m)
   const double* mass;      // [N]
   const double* inv_mass;  // [N]
   const double* sigma;     // [N] sqrt(m P / beta)
   const double* ke;        // [3][nr][nu]: K1, K2, K3 (unit mass), even-mode part (or full rows)
   const double* ko;        // [3][nr][nv]: odd-mode part
   const double* pile;      // [2][P] circulant a, b
+  const double* fdrift;    // split_drift_fast_kernel: [3][M+1] mode coefficients, then M Lee factors
   double* q;
   double* p;
   double* f;               // dV/dq
@@ -78,6 +80,10 @@ struct SplitParams {
   int* shake_fail;         // [T]
   int umbrella;            // 1: bias towards the trajectory's window after the forces
   UmbrellaDev umb;
+  // transrot / energy scratch of split_moments_kernel and split_solve_kernel
+  double* fsum;            // [T][S][16] partial sums per slice
+  int* fstat;              // [T][S] status bits per slice
+  double* fmove;           // [T][10] vt, xt, va, skip flag
 };
 
 constexpr int kSplitBlock = 128;
@@ -91,6 +97,7 @@ __host__ __device__ inline size_t split_smem_doubles(const SplitParams& s, bool 
   size_t n = (size_t)3 * s.nr * (s.nu + s.nv);        // tables
   n += (size_t)2 * cw * sp;                            // xq, xp
   n += (size_t)2 * cw * (s.su + s.sv);                 // u, v (q and p)
+  n += (size_t)cw;                                     // q shifts
   if (pile) n += (size_t)2 * cw * sp + 2 * (size_t)s.P;  // eta, tmp, circulants
   return n;
 }
@@ -172,7 +179,8 @@ __global__ void __launch_bounds__(kSplitBlock) split_drift_kernel(SplitParams s)
   double* up = uq + cw_max * s.su;
   double* vq = up + cw_max * s.su;
   double* vp = vq + cw_max * s.sv;
-  double* eta = vp + cw_max * s.sv;
+  double* shq = vp + cw_max * s.sv;  // per-coordinate q shift
+  double* eta = shq + cw_max;
   double* tmp = eta + cw_max * sp;
   double* sa = tmp + cw_max * sp;
   double* sb = sa + P;
@@ -196,6 +204,15 @@ __global__ void __launch_bounds__(kSplitBlock) split_drift_kernel(SplitParams s)
     }
     __syncthreads();
   }
+  // q relative to its bead-0 value (the constant vector is the centroid
+  // mode: K1 keeps it, K2 drops it; the products then round on bead spreads)
+  for (int c = threadIdx.x; c < cw; c += blockDim.x) shq[c] = xq[c * sp];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < P * cw; idx += blockDim.x) {
+    const int c = idx % cw, j = idx / cw;
+    xq[c * sp + j] -= shq[c];
+  }
+  __syncthreads();
   // fold into u (and v)
   const int M = s.M;
   for (int idx = threadIdx.x; idx < cw * s.nu; idx += blockDim.x) {
@@ -253,13 +270,13 @@ __global__ void __launch_bounds__(kSplitBlock) split_drift_kernel(SplitParams s)
     }
     const int atom = (c0 + c) / 3;
     const double m = s.mass[atom], im = s.inv_mass[atom];
-    const double qa = fma(im, e3p + o3p, e1q + o1q);
+    const double qa = fma(im, e3p + o3p, e1q + o1q) + shq[c];
     const double pa = fma(m, e2q + o2q, e1p + o1p);
     int rows[2] = {r, -1};
     double qv[2] = {qa, 0.0}, pv[2] = {pa, 0.0};
     if (s.split && 2 * r != M) {
       rows[1] = M - r;
-      qv[1] = fma(im, e3p - o3p, e1q - o1q);
+      qv[1] = fma(im, e3p - o3p, e1q - o1q) + shq[c];
       pv[1] = fma(m, e2q - o2q, e1p - o1p);
     }
     for (int k = 0; k < 2; ++k) {
@@ -274,6 +291,141 @@ __global__ void __launch_bounds__(kSplitBlock) split_drift_kernel(SplitParams s)
         s.p[g2] = pv[k];
       }
     }
+  }
+}
+
+// ---- free ring polymer by fast cosine transforms (even P = 2M, M = 4..32) ----
+// Caracal's map y = C D C x (C = sqrt(1/P) cos(2 pi j k / P)) depends on x
+// only through the fold s_0 = x_0, s_M = x_M, s_l = x_l + x_{P-l}, and
+// C x = T_M(s) / sqrt(P) with the type-I cosine transform
+//   T_M(s)_k = s_0 + (-1)^k s_M + sum_{l=1}^{M-1} s_l cos(pi k l / M),  k = 0..M.
+// The output is y_j = y_{P-j} = T_M(z)_j / sqrt(P), z_k = w_k D_k (C x)_k with
+// w_0 = w_M = 1, w_k = 2 otherwise.  T_M splits by the parity of k into
+// T_{M/2} of u_l = s_l + s_{M-l} (even k) and the type-III transform of size
+// M/2 of v_l = s_l - s_{M-l} (odd k); the type-III transform
+//   X_k = sum_{n<N} x_n cos(pi (2k+1) n / (2N))
+// follows Lee's recursion (B. G. Lee, IEEE Trans. ASSP 32 (1984) 1243):
+// G = (size N/2 of x_{2m}), H' = (size N/2 of x_{2m+1} + x_{2m-1}),
+// X_k = G_k + H'_k / (2 cos(pi (2k+1) / (2N))), X_{N-1-k} = G_k - (same).
+// For M = 32 that is ~210 FP64 operations per transform against 33^2 for the
+// matrix; the rounding error measured against extended precision is below
+// the matrix form's.
+template <int N>
+struct Dct3 {
+  __device__ static inline void run(const double (&x)[N], double (&X)[N], const double* lee) {
+    constexpr int H = N / 2;
+    double xe[H], z[H], G[H], Hh[H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      xe[m] = x[2 * m];
+      z[m] = m > 0 ? x[2 * m + 1] + x[2 * m - 1] : x[1];
+    }
+    Dct3<H>::run(xe, G, lee);
+    Dct3<H>::run(z, Hh, lee);
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+      const double h = Hh[k] * lee[H - 1 + k];  // 1 / (2 cos(pi (2k+1) / (2N)))
+      X[k] = G[k] + h;
+      X[N - 1 - k] = G[k] - h;
+    }
+  }
+};
+template <>
+struct Dct3<1> {
+  __device__ static inline void run(const double (&x)[1], double (&X)[1], const double*) { X[0] = x[0]; }
+};
+
+template <int M>
+struct Dct1 {
+  __device__ static inline void run(const double (&s)[M + 1], double (&y)[M + 1], const double* lee) {
+    constexpr int N = M / 2;
+    double u[N + 1], v[N], ye[N + 1], yo[N];
+    u[0] = s[0] + s[M];
+    v[0] = s[0] - s[M];
+#pragma unroll
+    for (int l = 1; l < N; ++l) {
+      u[l] = s[l] + s[M - l];
+      v[l] = s[l] - s[M - l];
+    }
+    u[N] = s[N];
+    Dct1<N>::run(u, ye, lee);
+    Dct3<N>::run(v, yo, lee);
+#pragma unroll
+    for (int k = 0; k <= N; ++k) y[2 * k] = ye[k];
+#pragma unroll
+    for (int k = 0; k < N; ++k) y[2 * k + 1] = yo[k];
+  }
+};
+template <>
+struct Dct1<2> {
+  __device__ static inline void run(const double (&s)[3], double (&y)[3], const double*) {
+    const double a = s[0] + s[2];
+    y[0] = a + s[1];
+    y[1] = s[0] - s[2];
+    y[2] = a - s[1];
+  }
+};
+
+// Entries of the fast-drift table for even P = 2M: A_k = w_k cos(w_k dt) / P,
+// B_k = w_k sin(w_k dt) / (w_k P) and C_k = -w_k w_k sin(w_k dt) / P per mode
+// k = 0..M (w the mode weight above), then the Lee factors of every size N
+// <= M/2 at [N/2 - 1 + k].
+__host__ __device__ inline int fast_drift_doubles(int M) { return 3 * (M + 1) + M; }
+
+// Free ring-polymer step of even P = 2M beads with the 1/2 kick before it
+// (no PILE): each warp takes 16 coordinates of one trajectory, lanes 0-15
+// transforming q and lanes 16-31 transforming p - dt/2 dV/dq of the same
+// coordinates; the 2x2 mode update exchanges the partner's coefficient by a
+// shuffle.  Block: 4 warps = 64 coordinates; grid (ceil(NC / 64), T).
+template <int M>
+__global__ void __launch_bounds__(128) split_drift_fast_kernel(SplitParams s) {
+  constexpr int P = 2 * M;
+  constexpr int kTab = 3 * (M + 1) + M;
+  __shared__ double tab[kTab];
+  for (int i = threadIdx.x; i < kTab; i += blockDim.x) tab[i] = s.fdrift[i];
+  __syncthreads();
+  const double* lee = tab + 3 * (M + 1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int NC = s.NC, t = blockIdx.y;
+  const int c = (blockIdx.x * 4 + warp) * 16 + (lane & 15);
+  const bool isp = lane >= 16, active = c < NC;
+  const int atom = active ? c / 3 : 0;
+  const size_t tb = (size_t)t * P * NC + c;
+  // q enters relative to its bead-0 value: the constant vector is mode 0
+  // (K1 keeps it, K2 drops it), and the transforms then round on bead
+  // spreads instead of absolute positions
+  double x[M + 1], shift = 0.0;
+#pragma unroll
+  for (int l = 0; l <= M; ++l) x[l] = 0.0;
+  if (active) {
+    const double* src = isp ? s.p : s.q;
+    const double hdt = isp ? s.half_dt : 0.0;
+    if (!isp) shift = src[tb];
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      const size_t g = tb + (size_t)j * NC;
+      const double v = fma(-hdt, s.f[g], src[g]) - shift;
+      x[j <= M ? j : P - j] += v;
+    }
+  }
+  double X[M + 1];
+  Dct1<M>::run(x, X, lee);
+  // q' = A q + B p / m (lanes 0-15), p' = A p + C m q (lanes 16-31)
+  const double msc = isp ? s.mass[atom] : s.inv_mass[atom];
+  const double* coef = tab + (isp ? 2 : 1) * (M + 1);
+#pragma unroll
+  for (int k = 0; k <= M; ++k) {
+    const double other = __shfl_xor_sync(0xffffffffu, X[k], 16);
+    X[k] = fma(coef[k] * msc, other, tab[k] * X[k]);
+  }
+  Dct1<M>::run(X, x, lee);
+  if (!active) return;
+  double* dst = isp ? s.p : s.q;
+#pragma unroll
+  for (int j = 0; j <= M; ++j) {
+    const double y = x[j] + shift;
+    dst[tb + (size_t)j * NC] = y;
+    if (j > 0 && j < M) dst[tb + (size_t)(P - j) * NC] = y;
   }
 }
 
@@ -439,102 +591,189 @@ __global__ void split_parent_init_kernel(SplitParams s) {
 
 // NaN check (src/verlet.f90:1256-1275), transrot (src/transrot.f90:36-237,
 // COM velocity and rotation centre with Caracal's total mass P^2 sum m) and
-// the potential energy summed over beads.  One block per trajectory.
-__global__ void __launch_bounds__(kFinishBlock) split_finish_kernel(SplitParams s) {
-  __shared__ double red[9 * kFinishBlock];
-  __shared__ double sva[4];
-  const int t = blockIdx.x, P = s.P, N = s.N, NC = s.NC;
-  const size_t tb = (size_t)t * P * NC;
+// the potential energy summed over beads, as three kernels:
+//   split_moments_kernel  grid (S, T): slice g of trajectory t's (bead, atom)
+//                         items -> 15 moment sums (sum w v, sum w x,
+//                         sum w x cross v, sum w x x^T), the bead energies
+//                         (slice 0), the NaN bits; fixed-order block sums
+//   split_solve_kernel    one thread per trajectory: the S partials summed in
+//                         order, epot, status, and the 3x3 system for the
+//                         angular velocity (Gauss-Jordan, full pivoting)
+//   split_apply_kernel    every item: p <- m (v - vt - va x (x - xt)),
+//                         evaluated as p - m (b + va x x), b = vt - va x xt
+// The second moments about Caracal's rotation centre xt come from the raw
+// ones by the parallel-axis identity C = S - xt Sx^T - Sx xt^T + W xt xt^T,
+// W = sum w.  Traffic: q and p read twice, p written once.
+constexpr int kMomentThreads = 256;
+constexpr int kFinishSums = 16;   // 15 moments + sum of bead energies
+constexpr int kMoveDoubles = 10;  // b = vt - va x xt, va, (unused), skip flag per trajectory
+
+// slices per trajectory of split_moments_kernel: about 4 items per thread
+__host__ __device__ inline int finish_slices(int items) {
+  const int s = (items + 4 * kMomentThreads - 1) / (4 * kMomentThreads);
+  return s < 1 ? 1 : (s > 16 ? 16 : s);
+}
+
+// Not NaN or infinite: exponent bits below all-ones (integer pipe only).
+__device__ inline bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
+
+// Moment sums of one (bead, atom) item.  On this GPU the FP64 pipe bounds the
+// finish, so the sums use w v = p (momentum) and w x once: 21 FP64
+// operations per item.
+__device__ inline void finish_accumulate(const SplitParams& s, int a, const double (&q)[3], const double (&p)[3],
+                                         double (&acc)[kFinishSums], int& status) {
+  const double w = s.mass[a];
+  const double wq[3] = {w * q[0], w * q[1], w * q[2]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (!finite_bits(q[d])) status |= CR_TRAJ_NONFINITE;
+    acc[d] += p[d];
+    acc[3 + d] += wq[d];
+  }
+  acc[6] = fma(q[1], p[2], fma(-q[2], p[1], acc[6]));
+  acc[7] = fma(q[2], p[0], fma(-q[0], p[2], acc[7]));
+  acc[8] = fma(q[0], p[1], fma(-q[1], p[0], acc[8]));
+  acc[9] = fma(wq[0], q[0], acc[9]);
+  acc[10] = fma(wq[0], q[1], acc[10]);
+  acc[11] = fma(wq[0], q[2], acc[11]);
+  acc[12] = fma(wq[1], q[1], acc[12]);
+  acc[13] = fma(wq[1], q[2], acc[13]);
+  acc[14] = fma(wq[2], q[2], acc[14]);
+}
+
+// Warp sum of 16 values per lane as a reduce-scatter butterfly: at each of
+// the first four levels a lane keeps half of its values and adds the
+// partner's copy of that half (8 + 4 + 2 + 1 FP64 adds instead of 16 x 5),
+// then one exchange finishes.  Lane l returns the warp sum of value l >> 1.
+// Fixed order: deterministic.
+__device__ inline double warp_sum16(double (&v)[16], int lane) {
+#pragma unroll
+  for (int level = 0; level < 4; ++level) {
+    const int half = 8 >> level;  // values kept per lane after this level
+    const bool up = (lane >> (4 - level)) & 1;
+#pragma unroll
+    for (int j = 0; j < half; ++j) {
+      const double keep = up ? v[half + j] : v[j];
+      const double give = up ? v[j] : v[half + j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, give, 16 >> level);
+    }
+  }
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+__global__ void __launch_bounds__(kMomentThreads) split_moments_kernel(SplitParams s) {
+  constexpr int kWarps = kMomentThreads / 32;
+  __shared__ double wpart[kWarps][kFinishSums];
+  __shared__ int wstat[kWarps];
+  const int S = gridDim.x, g = blockIdx.x, t = blockIdx.y, P = s.P, N = s.N;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t tb = (size_t)t * P * s.NC;
   const int items = P * N;
+  const int lo = (int)((long long)items * g / S), hi = (int)((long long)items * (g + 1) / S);
+  double acc[kFinishSums];
+#pragma unroll
+  for (int j = 0; j < kFinishSums; ++j) acc[j] = 0.0;
   int status = 0;
-  double s1[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
-    const int a = idx % N;
-    const double* qq = s.q + tb + 3 * (size_t)idx;
-    const double* pp = s.p + tb + 3 * (size_t)idx;
-    const double w = s.mass[a], iw = s.inv_mass[a];
+  for (int i = lo + threadIdx.x; i < hi; i += kMomentThreads) {
+    double q[3], p[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      if (!isfinite(qq[d])) status |= CR_TRAJ_NONFINITE;
-      s1[d] = fma(pp[d] * iw, w, s1[d]);
-      s1[3 + d] = fma(qq[d], w, s1[3 + d]);
+      q[d] = s.q[tb + 3 * (size_t)i + d];
+      p[d] = s.p[tb + 3 * (size_t)i + d];
     }
+    finish_accumulate(s, i % N, q, p, acc, status);
   }
-  for (int j = threadIdx.x; j < P; j += blockDim.x) s1[6] += s.V[(size_t)t * P + j];
-  block_sum<7>(s1, red);
-  __shared__ int sstat;
-  if (threadIdx.x == 0) sstat = 0;
+  if (g == 0)
+    for (int j = threadIdx.x; j < P; j += kMomentThreads) acc[15] += s.V[(size_t)t * P + j];
+  const double ws = warp_sum16(acc, lane);
+  status = __reduce_or_sync(0xffffffffu, status);
+  if ((lane & 1) == 0) wpart[warp][lane >> 1] = ws;
+  if (lane == 0) wstat[warp] = status;
   __syncthreads();
-  if (status) atomicOr(&sstat, status);
-  __syncthreads();
-  status = sstat;
-  if (s.constrain && s.shake_fail[t]) status |= CR_TRAJ_SHAKE_FAILED;
-  if (threadIdx.x == 0) s.epot[t] = s1[6] + ((s.constrain && s.shake_fail[t]) ? 100000.0 : 0.0);
+  const size_t slot = (size_t)t * S + g;
+  if (threadIdx.x < kFinishSums) {
+    double v = 0.0;
+    for (int w = 0; w < kWarps; ++w) v += wpart[w][threadIdx.x];
+    s.fsum[slot * kFinishSums + threadIdx.x] = v;
+  } else if (threadIdx.x == kFinishSums) {
+    int st = 0;
+    for (int w = 0; w < kWarps; ++w) st |= wstat[w];
+    s.fstat[slot] = st;
+  }
+}
+
+__global__ void split_solve_kernel(SplitParams s, int S) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.T) return;
+  double tot[kFinishSums];
+  int status = 0;
+#pragma unroll
+  for (int j = 0; j < kFinishSums; ++j) tot[j] = 0.0;
+  for (int g = 0; g < S; ++g) {
+    const size_t slot = (size_t)t * S + g;
+#pragma unroll
+    for (int j = 0; j < kFinishSums; ++j) tot[j] += s.fsum[slot * kFinishSums + j];
+    status |= s.fstat[slot];
+  }
+  const bool shake_fail = s.constrain && s.shake_fail[t];
+  if (shake_fail) status |= CR_TRAJ_SHAKE_FAILED;
+  s.epot[t] = tot[15] + (shake_fail ? 100000.0 : 0.0);
+  double* mv = s.fmove + (size_t)t * kMoveDoubles;
   if (s.transrot) {
-    const double itm = 1.0 / s.totmass;
-    const double vt[3] = {s1[0] * itm, s1[1] * itm, s1[2] * itm};
-    const double xt[3] = {s1[3] * itm, s1[4] * itm, s1[5] * itm};
-    double s2[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
-      const int a = idx % N;
-      const double* qq = s.q + tb + 3 * (size_t)idx;
-      const double* pp = s.p + tb + 3 * (size_t)idx;
-      const double w = s.mass[a], iw = s.inv_mass[a];
-      const double vv[3] = {pp[0] * iw, pp[1] * iw, pp[2] * iw};
-      s2[0] = fma(qq[1] * vv[2] - qq[2] * vv[1], w, s2[0]);
-      s2[1] = fma(qq[2] * vv[0] - qq[0] * vv[2], w, s2[1]);
-      s2[2] = fma(qq[0] * vv[1] - qq[1] * vv[0], w, s2[2]);
-      const double xd = qq[0] - xt[0], yd = qq[1] - xt[1], zd = qq[2] - xt[2];
-      s2[3] = fma(xd * xd, w, s2[3]);
-      s2[4] = fma(xd * yd, w, s2[4]);
-      s2[5] = fma(xd * zd, w, s2[5]);
-      s2[6] = fma(yd * yd, w, s2[6]);
-      s2[7] = fma(yd * zd, w, s2[7]);
-      s2[8] = fma(zd * zd, w, s2[8]);
+    const double itm = 1.0 / s.totmass, tm = s.totmass, W = s.wsum;
+    const double vt[3] = {tot[0] * itm, tot[1] * itm, tot[2] * itm};
+    const double xt[3] = {tot[3] * itm, tot[4] * itm, tot[5] * itm};
+    // centred second moments xx, xy, xz, yy, yz, zz
+    const double cxx = tot[9] - 2.0 * xt[0] * tot[3] + W * xt[0] * xt[0];
+    const double cxy = tot[10] - xt[0] * tot[4] - tot[3] * xt[1] + W * xt[0] * xt[1];
+    const double cxz = tot[11] - xt[0] * tot[5] - tot[3] * xt[2] + W * xt[0] * xt[2];
+    const double cyy = tot[12] - 2.0 * xt[1] * tot[4] + W * xt[1] * xt[1];
+    const double cyz = tot[13] - xt[1] * tot[5] - tot[4] * xt[2] + W * xt[1] * xt[2];
+    const double czz = tot[14] - 2.0 * xt[2] * tot[5] + W * xt[2] * xt[2];
+    const double mang[3] = {tot[6] - (xt[1] * vt[2] - xt[2] * vt[1]) * tm,
+                            tot[7] - (xt[2] * vt[0] - xt[0] * vt[2]) * tm,
+                            tot[8] - (xt[0] * vt[1] - xt[1] * vt[0]) * tm};
+    double ten[3][3] = {{cyy + czz, -cxy, -cxz}, {-cxy, cxx + czz, -cyz}, {-cxz, -cyz, cxx + cyy}};
+    if (s.N <= 2) {
+      ten[0][0] += 0.000001;
+      ten[1][1] += 0.000001;
+      ten[2][2] += 0.000001;
     }
-    block_sum<9>(s2, red);
-    if (threadIdx.x == 0) {
-      const double tm = s.totmass;
-      const double mang[3] = {s2[0] - (xt[1] * vt[2] - xt[2] * vt[1]) * tm,
-                              s2[1] - (xt[2] * vt[0] - xt[0] * vt[2]) * tm,
-                              s2[2] - (xt[0] * vt[1] - xt[1] * vt[0]) * tm};
-      double ten[3][3] = {{s2[6] + s2[8], -s2[4], -s2[5]},
-                          {-s2[4], s2[3] + s2[8], -s2[7]},
-                          {-s2[5], -s2[7], s2[3] + s2[6]}};
-      if (N <= 2) {
-        ten[0][0] += 0.000001;
-        ten[1][1] += 0.000001;
-        ten[2][2] += 0.000001;
-      }
-      if (!invert3(ten)) {
-        sva[3] = 1.0;
-      } else {
-        sva[3] = 0.0;
-        for (int a = 0; a < 3; ++a) sva[a] = ten[a][0] * mang[0] + ten[a][1] * mang[1] + ten[a][2] * mang[2];
-      }
-    }
-    __syncthreads();
-    if (sva[3] != 0.0) {
+    if (!invert3(ten)) {
       status |= CR_TRAJ_SINGULAR_INERTIA;
+      mv[9] = 1.0;
     } else {
-      const double va[3] = {sva[0], sva[1], sva[2]};
-      for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
-        const int a = idx % N;
-        const double* qq = s.q + tb + 3 * (size_t)idx;
-        double* pp = s.p + tb + 3 * (size_t)idx;
-        const double w = s.mass[a], iw = s.inv_mass[a];
-        double vv[3] = {pp[0] * iw - vt[0], pp[1] * iw - vt[1], pp[2] * iw - vt[2]};
-        const double xd = qq[0] - xt[0], yd = qq[1] - xt[1], zd = qq[2] - xt[2];
-        const double v0 = vv[0] - va[1] * zd + va[2] * yd;
-        const double v1 = vv[1] - va[2] * xd + va[0] * zd;
-        const double v2 = vv[2] - va[0] * yd + va[1] * xd;
-        pp[0] = v0 * w;
-        pp[1] = v1 * w;
-        pp[2] = v2 * w;
-      }
+      double va[3];
+      for (int a = 0; a < 3; ++a) va[a] = ten[a][0] * mang[0] + ten[a][1] * mang[1] + ten[a][2] * mang[2];
+      // p <- m (v - vt - va x (x - xt)) = p - m (b + va x x), b = vt - va x xt
+      mv[0] = vt[0] - (va[1] * xt[2] - va[2] * xt[1]);
+      mv[1] = vt[1] - (va[2] * xt[0] - va[0] * xt[2]);
+      mv[2] = vt[2] - (va[0] * xt[1] - va[1] * xt[0]);
+      for (int a = 0; a < 3; ++a) mv[3 + a] = va[a];
+      mv[9] = 0.0;
     }
   }
-  if (threadIdx.x == 0 && status) atomicOr(&s.status[t], status);
+  if (status) s.status[t] |= status;
+}
+
+__global__ void __launch_bounds__(kMomentThreads) split_apply_kernel(SplitParams s) {
+  const int N = s.N, items = s.P * N;
+  const size_t total = (size_t)s.T * items;
+  for (size_t idx = (size_t)blockIdx.x * kMomentThreads + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * kMomentThreads) {
+    const int t = (int)(idx / items), a = (int)(idx % items) % N;
+    const double* mv = s.fmove + (size_t)t * kMoveDoubles;
+    if (mv[9] != 0.0) continue;
+    const double* qq = s.q + 3 * idx;
+    double* pp = s.p + 3 * idx;
+    const double w = s.mass[a];
+    const double u0 = mv[0] + fma(mv[4], qq[2], -mv[5] * qq[1]);
+    const double u1 = mv[1] + fma(mv[5], qq[0], -mv[3] * qq[2]);
+    const double u2 = mv[2] + fma(mv[3], qq[1], -mv[4] * qq[0]);
+    pp[0] = fma(-w, u0, pp[0]);
+    pp[1] = fma(-w, u1, pp[1]);
+    pp[2] = fma(-w, u2, pp[2]);
+  }
 }
 
 // nhc (src/nhc.f90:35-171) on one trajectory per block: the kinetic sum

@@ -109,9 +109,15 @@ inline void free_rp_step(const StepConfig& cf, double* q, double* p) {
   for (int i = 0; i < N; ++i) {
     free_rp_poly(P, cf.beta, cf.dt, cf.mass[i], poly.data());
     for (int d = 0; d < 3; ++d) {
+      // q enters relative to its bead-0 value: a constant vector is the
+      // centroid mode, which poly keeps in q and leaves out of p
+      // (poly(2,0) = 0, poly(4,0) = 1), so the map is unchanged while the
+      // transforms round on bead spreads instead of absolute positions
+      // (otherwise ~1e-12 of |p| for heavy atoms at P = 64, dt = 0.5 fs)
+      const double shift = q[(0 * N + i) * 3 + d];
       for (int k = 0; k < P; ++k) {
         vp[k] = p[(k * N + i) * 3 + d];
-        vq[k] = q[(k * N + i) * 3 + d];
+        vq[k] = q[(k * N + i) * 3 + d] - shift;
       }
       caracal_cos_transform(vp.data(), P);
       caracal_cos_transform(vq.data(), P);
@@ -124,7 +130,7 @@ inline void free_rp_step(const StepConfig& cf, double* q, double* p) {
       caracal_cos_transform(vq.data(), P);
       for (int k = 0; k < P; ++k) {
         p[(k * N + i) * 3 + d] = vp[k];
-        q[(k * N + i) * 3 + d] = vq[k];
+        q[(k * N + i) * 3 + d] = vq[k] + shift;
       }
     }
   }

@@ -12,7 +12,7 @@ import pytest
 
 from caracal_gb300 import _lib as L
 from caracal_gb300 import RPMDEngine, egrad_h3
-from caracal_gb300.units import angstrom_to_bohr, beta_from_kelvin, dt_fs_to_au, mass_au
+from caracal_gb300.units import angstrom_to_bohr, beta_from_kelvin, dt_fs_to_au, mass_au, nose_q_to_au
 from caracal_gb300.workloads import h3_collinear
 from conftest import rel_err
 from oracle import oracle as orc
@@ -114,6 +114,33 @@ def test_step_host_equals_device_run(require_gpu):
         eng.step_host(qh, ph, fh, eh)
     qo, po, fo, eo, _ = orc.run(cfg, q, p, f, 3)
     assert rel_err(qh, qo) <= 1e-12 and rel_err(ph, po) <= 1e-12 and rel_err(eh, eo) <= 1e-12
+
+
+@pytest.mark.parametrize("thermostat", ["pile", "andersen", "nhc"])
+def test_step_host_pipelined_groups_equal_device_run(require_gpu, thermostat):
+    # 8192 trajectories x 16 beads: 9.4 MB per state array, so the host step
+    # runs as 4 trajectory groups whose copies overlap the other groups' steps
+    engs = []
+    for _ in range(2):
+        eng = RPMDEngine("h3", [MH] * 3, 16, 8192, dt_fs_to_au(0.1), beta=beta_from_kelvin(300.0),
+                         thermostat=thermostat, andersen_step=2, pile_tau0_au=dt_fs_to_au(100.0),
+                         nose_q_au=nose_q_to_au(20.0, 0.1), seed=20261203)
+        eng.init_positions(h3_collinear(), float(angstrom_to_bohr(0.01)))
+        eng.init_momenta()
+        eng.compute_forces()
+        engs.append(eng)
+    a, b = engs
+    q, p, f, e, _ = a.get_state()
+    for _ in range(3):
+        a.step_host(q, p, f, e)
+    assert a.launch_info()["launches"] == 4
+    b.run(3)
+    qb, pb, fb, eb, st = b.get_state()
+    a.close()
+    b.close()
+    assert not st.any()
+    assert rel_err(q, qb) <= 1e-15 and rel_err(p, pb) <= 1e-15
+    assert rel_err(f, fb) <= 1e-15 and rel_err(e, eb) <= 1e-15
 
 
 def test_nve_classical_energy_drift_no_larger_than_oracle(require_gpu):

@@ -14,7 +14,7 @@ import pytest
 from caracal_gb300 import RPMDEngine
 from caracal_gb300 import qmdff as Q
 from caracal_gb300.engine import QMDFFForceField
-from caracal_gb300.units import beta_from_kelvin, dt_fs_to_au
+from caracal_gb300.units import beta_from_kelvin, dt_fs_to_au, nose_q_to_au
 from caracal_gb300.workloads import qmdff_config
 from conftest import rel_err
 from oracle import oracle as orc
@@ -193,6 +193,39 @@ def test_step_host_matches_run(gpu_ff, alkane):
     eng2.close()
     assert rel_err(q, q2) <= 1e-15
     assert rel_err(p, p2) <= 1e-15
+
+
+@pytest.mark.parametrize("thermostat", ["andersen", "nhc", "pile"])
+def test_step_host_pipelined_groups_match_run(gpu_ff, alkane, thermostat):
+    # 384 trajectories x 8 beads x 62 atoms: 4.6 MB per state array, two
+    # trajectory groups in the pipelined host step (step kernels on offset
+    # trajectory ranges, noise keys of the global trajectory index)
+    engs = []
+    for _ in range(2):
+        eng = RPMDEngine(gpu_ff, qmdff_config().mass, 8, 384, dt_fs_to_au(0.5), beta=beta_from_kelvin(300.0),
+                         thermostat=thermostat, andersen_step=2, pile_tau0_au=dt_fs_to_au(100.0),
+                         nose_q_au=nose_q_to_au(20.0, 0.5), seed=77)
+        eng.init_positions(alkane.xyz, 0.02)
+        eng.init_momenta()
+        # twice: a first launch of >= 2048 beads may run the force kernel's
+        # autotuner, whose register variants can differ in the last bit
+        eng.compute_forces()
+        eng.compute_forces()
+        engs.append(eng)
+    a, b = engs
+    q, p, f, e, _ = a.get_state()
+    for _ in range(3):
+        a.step_host(q, p, f, e)
+    # drift, forces, kick, moments, solve, transrot apply (+ 2 NHC)
+    per_group = 6 + (2 if thermostat == "nhc" else 0)
+    assert a.launch_info()["launches"] == 2 * per_group + 1
+    b.run(3)
+    qb, pb, fb, eb, st = b.get_state()
+    a.close()
+    b.close()
+    assert not st.any()
+    assert rel_err(q, qb) <= 1e-15 and rel_err(p, pb) <= 1e-15
+    assert rel_err(f, fb) <= 1e-15 and rel_err(e, eb) <= 1e-15
 
 
 def test_mixed_engine_tracks_fp64(gpu_ff, alkane):
