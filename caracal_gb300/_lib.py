@@ -32,6 +32,7 @@ CR_PES_CH4H = 2
 CR_PES_CH4OH = 3
 CR_PES_QMDFF = 4
 CR_PES_EVB = 5
+CR_PES_WATER = 6
 
 CR_THERMO_NONE = 0
 CR_THERMO_ANDERSEN = 1
@@ -79,6 +80,11 @@ class CrQmdffDef(C.Structure):
 
 class CrEvbDef(C.Structure):
     _fields_ = [("basis", C.c_int)] + [(k, C.c_double) for k in "abcdefghmn"]
+
+
+class CrWaterDef(C.Structure):
+    _fields_ = [("nwater", C.c_int), ("periodic", C.c_int), ("box", C.c_double * 3), ("coul_cut", C.c_double),
+                ("zahn", C.c_int), ("zahn_a", C.c_double), ("zahn_par", C.c_double)]
 
 
 class CaracalError(RuntimeError):
@@ -161,6 +167,11 @@ def _sig(lib):
         "cr_batch_run": ([v, C.c_int], C.c_int),
         "cr_batch_info": ([v, C.POINTER(C.c_longlong), i, C.POINTER(C.c_float)], C.c_int),
         "cr_batch_destroy": ([v], C.c_int),
+        "cr_water_create": ([C.POINTER(CrWaterDef), C.POINTER(C.c_void_p)], C.c_int),
+        "cr_water_destroy": ([v], C.c_int),
+        "cr_water_natoms": ([v], C.c_int),
+        "cr_water_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
+        "cr_engine_create_water": ([C.POINTER(CrConfig), v, C.POINTER(C.c_void_p)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -72,6 +72,61 @@ def egrad_ch4oh(q):
     return V, g
 
 
+class WaterBox:
+    """Caracal's flexible SPC water box on the device (cr_water,
+    src/egrad_water.f90): ``nwater`` molecules, atoms ordered O, H, H.
+    ``box`` (Angstrom) makes it periodic, with the Coulomb cutoff
+    ``coul_cut`` (Angstrom) and the Zahn form set up as src/set_periodic.f90
+    does (:func:`caracal_gb300.water.periodic_setup`); without a box every
+    pair interacts."""
+
+    def __init__(self, nwater, box=None, coul_cut=0.0, zahn=False):
+        from . import water as W
+        d = L.CrWaterDef()
+        d.nwater = int(nwater)
+        if box is not None:
+            bb, cut, za, zp = W.periodic_setup(box, coul_cut, zahn)
+            d.periodic = 1
+            for k in range(3):
+                d.box[k] = bb[k]
+            d.coul_cut, d.zahn, d.zahn_a, d.zahn_par = cut, int(bool(zahn)), za, zp
+        self.nwater = int(nwater)
+        self.n = 3 * self.nwater
+        self.box_bohr = tuple(d.box) if box is not None else None
+        self.coul_cut = d.coul_cut
+        self.zahn, self.zahn_a, self.zahn_par = bool(d.zahn), d.zahn_a, d.zahn_par
+        h = C.c_void_p()
+        L.check(L.lib().cr_water_create(C.byref(d), C.byref(h)), "cr_water_create")
+        self._h = h
+
+    @property
+    def mass(self):
+        from . import water as W
+        return W.masses(self.nwater)
+
+    def egrad(self, xyz, precision="fp64"):
+        """Energies and gradients of xyz (nbeads, n, 3) bohr."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        if x.ndim == 2:
+            x = x[None]
+        if x.shape[1:] != (self.n, 3):
+            raise ValueError(f"xyz must be (nbeads, {self.n}, 3)")
+        V = np.zeros(x.shape[0])
+        g = np.zeros_like(x)
+        L.check(L.lib().cr_water_egrad(self._h, L.dptr(x), x.shape[0], L.dptr(V), L.dptr(g),
+                                       PRECISION[precision] if isinstance(precision, str) else int(precision)),
+                "cr_water_egrad")
+        return V, g
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().cr_water_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 class QMDFFForceField:
     """A QMDFF resident on the device (cr_qmdff): Caracal's ff_eg + ff_nonb +
     E_zero (src/gradient.f90:342-358) for one molecule, no H-bond terms.
@@ -303,7 +358,10 @@ class RPMDEngine:
                  andersen_step=70, pile_tau0_au=0.0, transrot=True, precision="fp64", seed=0,
                  traj0=0, nose_q_au=0.0):
         self.ff = pes if isinstance(pes, (QMDFFForceField, EVBPair)) else None
-        if isinstance(pes, EVBPair):
+        self.water = pes if isinstance(pes, WaterBox) else None
+        if isinstance(pes, WaterBox):
+            self.pes = L.CR_PES_WATER
+        elif isinstance(pes, EVBPair):
             self.pes = L.CR_PES_EVB
         elif self.ff is not None:
             self.pes = L.CR_PES_QMDFF
@@ -321,7 +379,10 @@ class RPMDEngine:
                               int(seed) & 0xFFFFFFFF, int(traj0) & 0xFFFFFFFF, float(dt_au),
                               self.beta, float(pile_tau0_au), L.dptr(self.mass), float(nose_q_au))
         h = C.c_void_p()
-        if isinstance(self.ff, EVBPair):
+        if self.water is not None:
+            L.check(L.lib().cr_engine_create_water(C.byref(self.cfg), self.water._h, C.byref(h)),
+                    "cr_engine_create_water")
+        elif isinstance(self.ff, EVBPair):
             L.check(L.lib().cr_engine_create_evb(C.byref(self.cfg), self.ff._h, C.byref(h)),
                     "cr_engine_create_evb")
         elif self.ff is not None:

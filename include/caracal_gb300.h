@@ -41,6 +41,7 @@ extern "C" {
 #define CR_PES_CH4OH 3   /* ANA_CH4OH: src/egrad_ch4oh.f + src/util_ch4oh.f */
 #define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90, ff_hb.f90 */
 #define CR_PES_EVB 5     /* dE-EVB of two QMDFFs: src/gradient.f90:361-386, 1228-1304 */
+#define CR_PES_WATER 6   /* flexible SPC water box: src/egrad_water.f90, src/water_init.f90 */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
 #define CR_THERMO_NONE 0      /* NVE */
@@ -69,6 +70,31 @@ typedef struct cr_config {
   const double* mass; /* natoms masses, a.u. (amu / 5.485799095e-4) */
   double nose_q;      /* NHC chain time, a.u.: NOSE_Q (in time steps) x dt (src/dynamic.f90:578) */
 } cr_config;
+
+/* ---- flexible SPC water box (water_spc: src/egrad_water.f90:36-333) -------
+ * nwater molecules with atoms ordered O, H, H (src/water_init.f90:53-72) and
+ * Caracal's fixed parameters (src/water_init.f90:74-103): Morse OH, harmonic
+ * HH, bond-angle and bond-bond couplings, point charges -0.82 / 0.41 e,
+ * Coulomb (or the Zahn form) between molecules and LJ 12-6 where the pair's
+ * first atom is an oxygen.  With periodic = 1 every distance vector takes
+ * the minimum image of the orthorhombic box (src/box_image.f90) and pairs at
+ * r >= coul_cut are skipped (src/set_periodic.f90 sets coul_cut and, for
+ * Zahn, zahn_a = 0.2 bohr and zahn_par from the cutoff). */
+typedef struct cr_water_def {
+  int nwater;
+  int periodic;
+  double box[3];     /* box lengths, bohr */
+  double coul_cut;   /* bohr */
+  int zahn;
+  double zahn_a, zahn_par;
+} cr_water_def;
+typedef struct cr_water cr_water;
+int cr_water_create(const cr_water_def* def, cr_water** out);
+int cr_water_destroy(cr_water* w);
+int cr_water_natoms(const cr_water* w);
+/* Energies V(nbeads) and gradients dVdq(3, natoms, nbeads) of host arrays
+ * q(3, natoms, nbeads), precision CR_PREC_FP64 or CR_PREC_MIXED. */
+int cr_water_egrad(const cr_water* w, const double* q, int nbeads, double* V, double* dVdq, int precision);
 
 typedef struct cr_engine cr_engine;
 
@@ -279,6 +305,9 @@ int cr_engine_create_qmdff(const cr_config* cfg, cr_qmdff* ff, cr_engine** out);
 /* Engine on a dE-EVB of two QMDFFs (cfg->pes = CR_PES_EVB); the EVB object
  * and its force fields must outlive the engine. */
 int cr_engine_create_evb(const cr_config* cfg, cr_evb* evb, cr_engine** out);
+/* Engine on a water box (cfg->pes = CR_PES_WATER, cfg->natoms = 3 nwater);
+ * the box must outlive the engine.  Steps run through the graph path. */
+int cr_engine_create_water(const cr_config* cfg, cr_water* w, cr_engine** out);
 int cr_engine_destroy(cr_engine* e);
 
 /* Initial positions: every bead of every trajectory = q0(3,natoms) plus

@@ -19,7 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-PES_IDS = {"h3": 1, "ch4h": 2, "ch4oh": 3, "qmdff": 4, "evb": 5}
+PES_IDS = {"h3": 1, "ch4h": 2, "ch4oh": 3, "qmdff": 4, "evb": 5, "water": 6}
 EVB_BASES = {"const": 0, "1g": 1, "2g": 2, "3g": 3, "sp": 4, "sd": 5, "sd2": 6, "sp2d": 7}
 THERMOSTATS = {"none": 0, "andersen": 1, "nose-hoover": 2, "nhc": 2, "pile": 3}
 OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",
@@ -75,6 +75,14 @@ def set_evb(ff1, ff2, tables, basis="1g", par=None, **kw):
 
 _keep2 = []
 _last_def = [None]
+
+
+def set_water(nwater, box=None, coul_cut=0.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
+    """PES 6: Caracal's flexible SPC water box of nwater molecules (O, H, H);
+    box = (Lx, Ly, Lz) in bohr for periodic boundaries, None for none."""
+    ln = (C.c_double * 3)(*(box if box is not None else (0.0, 0.0, 0.0)))
+    lib().orc_water_set(int(nwater), int(box is not None), ln, float(coul_cut), int(zahn), float(zahn_a),
+                        float(zahn_par))
 
 
 def set_qmdff(ff, tables, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
@@ -171,6 +179,7 @@ def lib():
         _lib.orc_recross_children.argtypes = [C.POINTER(Cfg), C.POINTER(XiDef), C.c_int, C.c_uint32, d,
                                               C.c_int, d, d, d, d, d, C.c_int]
         _lib.orc_pes_opcount.argtypes = [C.c_int, d, C.POINTER(C.c_uint64)]
+        _lib.orc_water_set.argtypes = [C.c_int, C.c_int, d, C.c_double, C.c_int, C.c_double, C.c_double]
     return _lib
 
 

@@ -15,6 +15,7 @@
 #include "evb_fit.hpp"
 #include "pes_evb.hpp"
 #include "pes_qmdff.hpp"
+#include "pes_water.hpp"
 #include "philox.hpp"
 #include "recross.hpp"
 #include "rpmd.hpp"
@@ -39,6 +40,7 @@ orc::StepConfig to_step(const orc_cfg* c) {
 
 orc::qmdff::FF g_qmdff, g_qmdff2;
 orc::evb::Coupling g_evb;
+orc::water::Box g_water;
 
 // Per-bead PES call, q(3,N) -> V, g(3,N).
 struct BeadPES {
@@ -51,6 +53,7 @@ struct BeadPES {
       case 3: orc::ch4oh::egrad_bead<double>(q, V, g); break;
       case 4: orc::qmdff::egrad(g_qmdff, q, V, g); break;
       case 5: orc::evb::egrad(g_qmdff, g_qmdff2, g_evb, q, V, g); break;
+      case 6: *V = orc::water::egrad<double>(g_water, q, g); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
   }
@@ -59,6 +62,18 @@ struct BeadPES {
 }  // namespace
 
 extern "C" {
+
+void orc_water_set(int nwater, int periodic, const double* len, double coul_cut, int zahn, double zahn_a,
+                   double zahn_par) {
+  orc::water::Box& b = g_water;
+  b.nwater = nwater;
+  b.periodic = periodic;
+  for (int k = 0; k < 3; ++k) b.len[k] = len ? len[k] : 0.0;
+  b.coul_cut = coul_cut;
+  b.zahn = zahn;
+  b.zahn_a = zahn_a;
+  b.zahn_par = zahn_par;
+}
 
 void orc_qmdff_set2(const orc_qmdff_def* d) {
   orc::qmdff::FF keep = g_qmdff;

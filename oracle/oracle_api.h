@@ -12,7 +12,8 @@ extern "C" {
 #endif
 
 typedef struct orc_cfg {
-  int pes;            /* 1 H3 (BKMP2), 2 CH4H, 3 CH4OH, 4 QMDFF (orc_qmdff_set), 5 dE-EVB of two QMDFFs */
+  int pes;            /* 1 H3 (BKMP2), 2 CH4H, 3 CH4OH, 4 QMDFF (orc_qmdff_set), 5 dE-EVB of two QMDFFs,
+                         6 flexible SPC water box (orc_water_set) */
   int natoms;
   int nbeads;
   int thermostat;     /* 0 none, 1 Andersen, 2 Nose-Hoover chain, 3 PILE */
@@ -80,6 +81,11 @@ void orc_qmdff_set(const orc_qmdff_def* d);
 /* The second force field and the coupling of PES id 5 (dE-EVB of the two):
  * basis 0..7 = const, 1g, 2g, 3g, sp, sd, sd2, sp2d; par = offa..offh, offm, offn. */
 void orc_qmdff_set2(const orc_qmdff_def* d);
+/* PES 6: Caracal's flexible SPC water box (src/egrad_water.f90): nwater
+ * molecules O, H, H; periodic boundaries with box lengths len[3] (bohr) and
+ * the Coulomb cutoff, Zahn form if zahn. */
+void orc_water_set(int nwater, int periodic, const double* len, double coul_cut, int zahn, double zahn_a,
+                   double zahn_par);
 void orc_evb_set(int basis, const double par[10]);
 
 /* BIMOLEC reaction coordinate of Caracal's recrossing (calc_xi mode 2). */
