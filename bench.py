@@ -45,6 +45,9 @@ ALGO_PES_OPS = {
     # geometry + N(0, 0.05 bohr) per coordinate, seed 0); asin counted with acos
     "qmdff": {"add": 92211, "mul": 117770, "div": 20592, "sqrt": 4525, "exp": 1415, "pow": 122,
               "sin": 633, "cos": 753, "acos": 291, "erf": 171},
+    # flexible SPC water, 64 molecules, periodic box 23.47 bohr, Coulomb
+    # cutoff 6 A, thermal geometry (grid geometry + N(0, 0.05 bohr), seed 0)
+    "water": {"add": 194295, "mul": 201198, "div": 9259, "sqrt": 18336, "exp": 128},
 }
 CALIB_OPS = {"fma": 0, "div": 1, "sqrt": 2, "exp": 3, "log": 4, "pow": 5, "sin": 6, "cos": 7,
              "acos": 8, "erf": 9, "tanh": 10, "cosh": 11}
@@ -100,7 +103,7 @@ def roofline(wl, mixed, ms, K, cal):
     _, pes32 = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w32, wl.transrot, rec)
     p64, p32 = cal["fp64"]["peak_tflops"], cal["fp32"]["peak_tflops"]
     units = wl.ntraj * wl.nbeads * K
-    step = "qmdff step graph" if wl.pes == "qmdff" else "rpmd_run_kernel"
+    step = "step graph" if wl.pes in ("qmdff", "water") else "rpmd_run_kernel"
     if mixed:
         eq = f64 + pes32 * p64 / p32
         kern, bound = f"{step}<{wl.pes}, mixed>", "fp64+fp32 (FP64-equivalent)"
@@ -211,6 +214,8 @@ def workload(name):
         return W.qmdff_config(ntraj=1024, nbeads=64)
     if name == "qmdff_small":
         return W.qmdff_config(ntraj=512, nbeads=64)
+    if name == "water":
+        return W.water_config(nwater=64, ntraj=64, nbeads=32)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -220,6 +225,12 @@ def make_pes(wl):
         from caracal_gb300.engine import QMDFFForceField
         if "gpu_ff" not in wl.extra:
             wl.extra["gpu_ff"] = QMDFFForceField(wl.extra["ff"])
+        return wl.extra["gpu_ff"]
+    if wl.pes == "water":
+        from caracal_gb300.engine import WaterBox
+        if "gpu_ff" not in wl.extra:
+            x = wl.extra
+            wl.extra["gpu_ff"] = WaterBox(x["nwater"], box=x["box"], coul_cut=x["coul_cut"], zahn=x["zahn"])
         return wl.extra["gpu_ff"]
     return wl.pes
 
@@ -254,6 +265,11 @@ class OracleRunner:
         if wl.pes == "qmdff":
             from caracal_gb300 import qmdff as Q
             orc.set_qmdff(wl.extra["ff"], Q.ElementTables.d3_like())
+        if wl.pes == "water":
+            from caracal_gb300 import water as Wt
+            x = wl.extra
+            box, cut, za, zp = Wt.periodic_setup(x["box"], x["coul_cut"], x["zahn"])
+            orc.set_water(x["nwater"], box, cut, x["zahn"], za, zp)
         self.cfg = orc.Config(wl.pes, wl.mass, wl.nbeads, wl.dt_au, wl.beta,
                               thermostat=wl.thermostat, andersen_step=wl.andersen_step,
                               pile_tau0=wl.pile_tau0_au, transrot=wl.transrot, seed=wl.seed)
@@ -459,8 +475,8 @@ def run_ours(args):
                    "natoms": len(wl.mass), "thermostat": wl.thermostat, "kelvin": wl.kelvin,
                    "dt_fs": wl.dt_fs, "parallelism": f"replicas x{ws}",
                    "l2": "flushed (256 MB write) before the timed launch"
-                         + ("; K steps in one launch" if wl.pes != "qmdff" else
-                            "; state (3 x 97.5 MB) larger than L2 is streamed every step")},
+                         + ("; K steps in one launch" if wl.pes not in ("qmdff", "water") else
+                            f"; state (3 x {nbytes / 1e6:.1f} MB) streamed every step (graph path)")},
         "plain_fp64": {"value": plain, "unit": "bead-steps/s", "ms_per_step": ms_64 / K},
         "mixed_over_plain": value / plain,
         "force_error_vs_fp64": ferr, "energy_error_vs_fp64": eerr,
@@ -793,6 +809,7 @@ def main():
                     help="ch4h (CH4+H recrossing children, 4096 x 32 beads: the default), "
                          "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16), "
                          "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (512 x 64), "
+                         "water (flexible SPC, 64 molecules, periodic, 64 x 32), "
                          "classes (H3 4096x8, CH4H 2048x32, CH4OH 512x64, QMDFF 128x128 in one batch), "
                          "classes_small (the same with 1/16 of the trajectories), "
                          "adjoint (force matching over 8192 C20H42 geometries and a 200-step trajectory adjoint)")

@@ -189,6 +189,53 @@ def generate_structures(r, pes, mass, beta, dt, q0, xw, kf, mech):
     return out
 
 
+def write_recross_restart(out_dir, bunches_done, num, den, qpar):
+    """The recrossing restart files after a bunch of children
+    (src/recross.f90:418-440): recross_num_tmp.dat (one numerator per child
+    step), recross_denom_tmp.dat, recross_parent_pos.dat (the parent's beads,
+    `x y z` bohr per atom) and recross_status (bunches done).  Caracal opens
+    the parent file with status="replace" and then reads from it, so its file
+    stays empty and its resume starts over; here the file holds the parent."""
+    with open(os.path.join(out_dir, "recross_num_tmp.dat"), "w") as fh:
+        for v in num:
+            fh.write(f"{v:26.16E}\n")
+    with open(os.path.join(out_dir, "recross_denom_tmp.dat"), "w") as fh:
+        fh.write(f"{den:26.16E}\n")
+    with open(os.path.join(out_dir, "recross_parent_pos.dat"), "w") as fh:
+        for bead in qpar:
+            for atom in bead:
+                fh.write("".join(f"{v:26.16E}" for v in atom) + "\n")
+    with open(os.path.join(out_dir, "recross_status"), "w") as fh:
+        fh.write(f"{int(bunches_done):12d}\n")
+
+
+def read_recross_restart(out_dir, child_steps, nbeads, natoms):
+    """(bunches done, numerators, denominator, parent beads or None) from the
+    restart files (src/recross.f90:124-228); missing or incomplete files give
+    a fresh start (0, zeros, 0, None), an incomplete parent file None."""
+    fresh = (0, np.zeros(child_steps), 0.0, None)
+    try:
+        with open(os.path.join(out_dir, "recross_status")) as fh:
+            k = int(fh.read().split()[0])
+        with open(os.path.join(out_dir, "recross_num_tmp.dat")) as fh:
+            num = np.array([float(x.replace("D", "E")) for x in fh.read().split()])
+        with open(os.path.join(out_dir, "recross_denom_tmp.dat")) as fh:
+            den = float(fh.read().split()[0].replace("D", "E"))
+    except (OSError, ValueError, IndexError):
+        return fresh
+    if k <= 0 or len(num) < child_steps:
+        return fresh
+    qpar = None
+    try:
+        with open(os.path.join(out_dir, "recross_parent_pos.dat")) as fh:
+            vals = np.array([float(x.replace("D", "E")) for x in fh.read().split()])
+        if len(vals) >= nbeads * natoms * 3:
+            qpar = vals[:nbeads * natoms * 3].reshape(nbeads, natoms, 3)
+    except (OSError, ValueError):
+        qpar = None
+    return k, num[:child_steps], den, qpar
+
+
 def run(path, out_dir=None, quiet=False):
     from .engine import RPMDEngine
     with open(path) as fh:
@@ -243,15 +290,26 @@ def run(path, out_dir=None, quiet=False):
     kappa_num = np.zeros(r.child_steps)
     kappa_den = 0.0
     if r.child_total > 0 and r.child_steps > 0:
+        nkids = max(2, r.child_perpoint - r.child_perpoint % 2)
+        bunches = -(-r.child_total // nkids)
+        point, kappa_num, kappa_den, qpar = read_recross_restart(out_dir, r.child_steps, r.nbeads, len(mass))
+        if point >= bunches and qpar is None:
+            point = bunches                    # every bunch done: the sums are final
+        elif point > 0 and qpar is None:
+            point, kappa_num, kappa_den = 0, np.zeros(r.child_steps), 0.0
+        done = point * nkids
         par = RPMDEngine(pes, mass, r.nbeads, 1, dt, beta=beta, thermostat=r.thermostat,
                          andersen_step=r.andersen_step, transrot=False, seed=r.seed + 1)
         par.init_positions(q0, 0.0)
         par.init_momenta()
-        par.compute_forces()
+        if qpar is not None and point > 0:     # resume from the saved parent, fresh momenta
+            _, p1, _, _, _ = par.get_state()
+            par.set_state(qpar[None], p1)
+        else:
+            par.compute_forces()
         par.set_parent(xi_ideal=xi_barrier, **mech)
-        par.run(max(r.rc_equi, 1))
-        nkids = max(2, r.child_perpoint - r.child_perpoint % 2)
-        done, point = 0, 0
+        if point == 0:
+            par.run(max(r.rc_equi, 1))
         while done < r.child_total:
             par.run(r.child_interval)
             qp, _, _, _, _ = par.get_state()
@@ -267,6 +325,7 @@ def run(path, out_dir=None, quiet=False):
             kappa_den += den
             done += nkids
             point += 1
+            write_recross_restart(out_dir, point, kappa_num, kappa_den, qp[0])
         par.close()
     kappa_t = kappa_num / kappa_den if kappa_den > 0 else np.ones(max(r.child_steps, 1))
     with open(os.path.join(out_dir, "recross.dat"), "w") as fh:
@@ -274,6 +333,8 @@ def run(path, out_dir=None, quiet=False):
         for i, v in enumerate(kappa_t):
             fh.write(f"{(i + 1) * r.dt_fs:24.16f}{v:26.16f}\n")
     kappa = float(kappa_t[-1])
+    with open(os.path.join(out_dir, "recross_finished"), "w") as fh:   # src/recross.f90:660-665
+        fh.write(f"{kappa:26.16E}\n")
     if kappa < 0.002:   # src/calc_rate.f90:2237-2252
         kappa = 1.0
 

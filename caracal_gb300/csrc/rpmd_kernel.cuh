@@ -114,10 +114,6 @@ __host__ __device__ inline PropDims prop_dims(int P) {
 __device__ inline double sym_at(const double* x, int l, int P) {
   return (l == 0 || 2 * l == P) ? x[l] : x[l] + x[P - l];
 }
-// the same of x - x0 (each difference first: exact for nearby values)
-__device__ inline double sym_at_shift(const double* x, int l, int P, double x0) {
-  return (l == 0 || 2 * l == P) ? x[l] - x0 : (x[l] - x0) + (x[P - l] - x0);
-}
 
 // Nose-Hoover chain constants of one engine (src/nhc.f90:35-171 with the
 // masses of src/mdinit.f90:128-147), precomputed on the host.
@@ -309,10 +305,10 @@ __device__ inline bool invert3(double (&a)[3][3]) {
 //   [0, 3 nr (nu + nv))            propagator blocks Ke, Ko of K1, K2, K3
 //   then 2P                        PILE circulant vectors a, b
 //   then per group: xs[2 NC][G] (reused as the outputs [2 NC][P/2+1]),
-//                   u[2 NC][su], v[2 NC][sv], red[(G/32) * 32], sq[NC]
+//                   u[2 NC][su], v[2 NC][sv], red[(G/32) * 32]
 __host__ __device__ inline size_t step_group_doubles(int P, int G, int NC) {
   const PropDims d = prop_dims(P);
-  return (size_t)2 * NC * G + (size_t)2 * NC * (d.su + d.sv) + (size_t)((G + 31) / 32) * 32 + (size_t)NC;
+  return (size_t)2 * NC * G + (size_t)2 * NC * (d.su + d.sv) + (size_t)((G + 31) / 32) * 32;
 }
 __host__ __device__ inline size_t step_smem_doubles(int P, int G, int NC, int groups) {
   const PropDims d = prop_dims(P);
@@ -342,7 +338,6 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
   double* su = xs + 2 * NC * G;            // [2 NC][su]
   double* sv = su + 2 * NC * pd.su;        // [2 NC][sv]
   double* red = sv + 2 * NC * pd.sv;       // [(G/32)][32]
-  double* sq = red + ((G + 31) / 32) * 32; // [NC] bead-0 q per coordinate (propagator shift)
 
   for (int x = threadIdx.x; x < nke; x += blockDim.x) s_ke[x] = prm.ke[x];
   for (int x = threadIdx.x; x < nko; x += blockDim.x) s_ko[x] = prm.ko[x];
@@ -442,18 +437,13 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
       xs[(NC + c) * G + j] = q[c];
     }
     group_sync(G);
-    // fold each coordinate's P values into u (and v): tasks (cc, l).  q
-    // enters relative to its bead-0 value x0 (the constant vector is the
-    // centroid mode: K1 keeps it, K2 drops it), so the products round on
-    // bead spreads; x0 is added back to the outputs.
+    // fold each coordinate's P values into u (and v): tasks (cc, l)
     for (int idx = j; idx < 2 * NC * pd.nu; idx += G) {
       const int cc = idx / pd.nu, l = idx - cc * pd.nu;
       const double* x = xs + cc * G;
-      const double x0 = cc >= NC ? x[0] : 0.0;
-      if (cc >= NC && l == 0) sq[cc - NC] = x0;
-      const double a = sym_at_shift(x, l, P, x0);
+      const double a = sym_at(x, l, P);
       if (pd.split && 2 * l != pd.M) {
-        const double b = sym_at_shift(x, pd.M - l, P, x0);
+        const double b = sym_at(x, pd.M - l, P);
         su[cc * pd.su + l] = a + b;
         if (l < pd.nv) sv[cc * pd.sv + l] = a - b;
       } else {
@@ -494,10 +484,10 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
       }
       const double m = prm.mass[c / 3], im = prm.inv_mass[c / 3];
       xs[c * H + r] = fma(m, e2q + o2q, e1p + o1p);
-      xs[(NC + c) * H + r] = fma(im, e3p + o3p, e1q + o1q) + sq[c];
+      xs[(NC + c) * H + r] = fma(im, e3p + o3p, e1q + o1q);
       if (pd.split && 2 * r != pd.M) {
         xs[c * H + pd.M - r] = fma(m, e2q - o2q, e1p - o1p);
-        xs[(NC + c) * H + pd.M - r] = fma(im, e3p - o3p, e1q - o1q) + sq[c];
+        xs[(NC + c) * H + pd.M - r] = fma(im, e3p - o3p, e1q - o1q);
       }
     }
     group_sync(G);

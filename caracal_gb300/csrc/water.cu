@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(water::kMaxAtoms)
     __syncthreads();
     if (tid < n) {
       double f[3] = {gi[3 * tid], gi[3 * tid + 1], gi[3 * tid + 2]};
-      en += MIXED ? water::pairs_mixed(D, hl, tid, f) : water::pairs_plain(D, xs, tid, f);
+      en += MIXED ? water::pairs_mixed(D, xs, hl, tid, f) : water::pairs_plain(D, xs, tid, f);
       double* gb = g + (size_t)b * n3 + 3 * tid;
       gb[0] = f[0];
       gb[1] = f[1];

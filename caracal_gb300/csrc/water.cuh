@@ -155,7 +155,11 @@ __device__ inline double pairs_plain(const Dev& D, const double* x, int i, doubl
 }
 
 // The same in FP32 from the (hi, lo) coordinates, forces summed in FP64.
-__device__ inline double pairs_mixed(const Dev& D, const float2* hl, int i, double (&f)[3]) {
+// The truncated Coulomb sum jumps by q_i q_j / r_cut where a pair crosses the
+// cutoff, so the cutoff decision must be the plain form's: where the FP32 r
+// lies within 1e-5 of the cutoff, the FP64 distance (same image loop, same
+// sqrt) decides.
+__device__ inline double pairs_mixed(const Dev& D, const double* x, const float2* hl, int i, double (&f)[3]) {
   const float qi = (i % 3 == 0) ? D.feo : D.feh;
   float2 xi[3];
 #pragma unroll
@@ -172,8 +176,20 @@ __device__ inline double pairs_mixed(const Dev& D, const float2* hl, int i, doub
     }
     if (D.periodic) image(D, d);
     const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-    const float oner = rsqrtf(r2), r = r2 * oner;
-    if (!(r < D.fcut || !D.periodic)) continue;
+    float oner = rsqrtf(r2);
+    oner = fmaf(0.5f * oner, fmaf(-r2 * oner, oner, 1.0f), oner);  // one Newton step
+    const float r = r2 * oner;
+    if (D.periodic) {
+      bool inside = r < D.fcut;
+      if (fabsf(r - D.fcut) < 1e-5f * D.fcut) {
+        double dd[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dd[k] = x[3 * i + k] - x[3 * j + k];
+        image(D, dd);
+        inside = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) < D.coul_cut;
+      }
+      if (!inside) continue;
+    }
     const float ir2 = oner * oner;
     float e0;
     if (D.zahn) e0 = qi * qj * ((erfcf(D.fzahn_a * r) * oner) - D.fzahn_par * (r - D.fcut));

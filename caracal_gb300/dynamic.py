@@ -2,7 +2,8 @@
 
 Reads the key file (``caracal_gb300.keyfile``), the XYZSTART geometry and the
 force fields, starts every bead on the input structure with mdinit's momenta
-(src/dynamic.f90:1307-1314, src/mdinit.f90:110-150), advances the engine
+(src/dynamic.f90:1307-1314, src/mdinit.f90:110-150; READ_VEL: velocity_start.dat),
+advances the engine
 TDUMP/DELTAT steps per launch and writes Caracal's output files at every dump
 step (src/verlet.f90:780-800, 666-676, 1170-1205; src/dynamic.f90:1458-1486, 1676):
 
@@ -58,6 +59,13 @@ def write_frame(f, names, xyz_ang):
     f.flush()
 
 
+def momenta_from_velocities(v, mass, shape):
+    """READ_VEL start momenta of every trajectory: bead 1 p = -v m, others 0."""
+    p = np.zeros(shape)
+    p[:, 0] = -np.asarray(v)[None] * np.asarray(mass)[None, :, None]
+    return p
+
+
 def build_pes(d, nve):
     """The engine's PES argument (and the objects that must stay alive)."""
     if d.pes in K.ANALYTIC:
@@ -97,6 +105,12 @@ def run(path, out_dir=None, quiet=False):
     eng.init_positions(q0, 0.0)
     eng.init_momenta(zero=nve)
     eng.compute_forces()
+    if d.read_vel and not nve and d.thermostat == "andersen":
+        # src/mdinit.f90:113-118: bead 1 gets p = -v m (sign as in the
+        # reference); the reference leaves the other beads unset, here zero
+        v = K.read_velocities(os.path.join(d.directory, "velocity_start.dat"), len(sym))
+        q, p, f, _, _ = eng.get_state()
+        eng.set_state(q, momenta_from_velocities(v, mass, p.shape), f)
     names = list(sym)
     P, N = d.nbeads, len(sym)
     traj = None if (d.output_sparse and P > 1) else open(os.path.join(out_dir, "trajectory.xyz"), "w")

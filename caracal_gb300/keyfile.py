@@ -24,10 +24,12 @@ from __future__ import annotations
 import os
 from dataclasses import dataclass, field
 
+import numpy as np
+
 ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh"}
 EVB_BASES = ("1g", "2g", "3g", "sp", "sd", "sd2", "sp2d")
 KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE",
-         "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "}"}
+         "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "READ_VEL", "}"}
 
 
 class KeyError_(ValueError):
@@ -54,6 +56,7 @@ class DynamicInput:
     seed: int = 0
     energycon: bool = False      # E_CON: md_energies.dat (src/dynamic.f90:1130-1140)
     output_sparse: bool = False  # OUTPUT_SPARSE: no all-bead trajectory (src/dynamic.f90:1145-1155)
+    read_vel: bool = False       # READ_VEL: start momenta from velocity_start.dat (src/dynamic.f90:1031-1059)
     unsupported: list = field(default_factory=list)
     directory: str = "."
 
@@ -119,6 +122,8 @@ def parse(text, directory="."):
             d.energycon = True
         elif k == "OUTPUT_SPARSE":
             d.output_sparse = True
+        elif k == "READ_VEL":
+            d.read_vel = True
         elif k.rstrip("{") not in KNOWN and not k.startswith("#") and not k.startswith("!"):
             d.unsupported.append(k)
     # checks of src/dynamic.f90:290-320
@@ -189,6 +194,21 @@ def read_xyz(path):
             sym.append(w[0])
             xyz.append([float(x) for x in w[1:4]])
     return sym, xyz
+
+
+def read_velocities(path, natoms):
+    """velocity_start.dat (src/dynamic.f90:1047-1059): two lines skipped, then
+    per atom `idum idum vx vy vz`; returns (natoms, 3)."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    v = np.zeros((natoms, 3))
+    rows = [ln for ln in lines[2:] if ln.strip()]
+    if len(rows) < natoms:
+        raise KeyError_("velocity_start.dat has fewer lines than atoms")
+    for i in range(natoms):
+        w = rows[i].replace("d", "e").replace("D", "E").split()
+        v[i] = [float(x) for x in w[2:5]]
+    return v
 
 
 def read_evb_pars(path, basis):

@@ -121,6 +121,23 @@ def qmdff_config(ntraj=1024, nbeads=64, nsteps=500, kelvin=300.0, dt_fs=0.5, nc=
                     sigma_bohr=float(angstrom_to_bohr(0.01)), transrot=True, extra={"ff": ff})
 
 
+def water_config(nwater=64, ntraj=64, nbeads=32, nsteps=500, kelvin=300.0, dt_fs=0.25, coul_cut_ang=6.0,
+                 thermostat="andersen", andersen_step=70, zahn=False):
+    """Periodic box of Caracal's flexible SPC water (water_spc): nwater
+    molecules at 1 g/cm^3 on a cubic grid, randomly oriented (seed), cubic box,
+    Coulomb cutoff coul_cut_ang (pulled below half the box as
+    src/set_periodic.f90 does); NVT 300 K, 0.25 fs, beads start on the grid
+    geometry with 0.01 A jitter."""
+    from . import water as Wt
+    x, length = Wt.water_box(nwater, seed=SEED)
+    sym = ["O", "H", "H"] * nwater
+    return Workload(name=f"water_spc_{nwater}_P{nbeads}_T{ntraj}", pes="water", symbols=sym, q0=x,
+                    nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs, nsteps=nsteps,
+                    thermostat=thermostat, andersen_step=andersen_step,
+                    sigma_bohr=float(angstrom_to_bohr(0.01)), transrot=True,
+                    extra={"nwater": nwater, "box": [length] * 3, "coul_cut": coul_cut_ang, "zahn": zahn})
+
+
 def ch4oh_geometry(r_ch_ang=1.09, r_ho_ang=1.3, r_oh_ang=0.97, angle_deg=100.0):
     """CH4 (tetrahedral, r(CH) = r_ch) + OH with O collinear with one C-H bond,
     r_ho beyond that bond's H, and the hydroxyl H at r_oh from O bent by angle_deg

@@ -377,6 +377,11 @@ void orc_pes_opcount(int pes, const double* q, uint64_t out[14]) {
     orc::OC V;
     for (int x = 0; x < n3; ++x) qq[(size_t)x] = orc::OC(q[x]);
     orc::qmdff::egrad<orc::OC>(g_qmdff, qq.data(), &V, g.data());
+  } else if (pes == 6) {
+    const int n3 = 9 * g_water.nwater;
+    std::vector<orc::OC> qq((size_t)n3), g((size_t)n3);
+    for (int x = 0; x < n3; ++x) qq[(size_t)x] = orc::OC(q[x]);
+    orc::water::egrad<orc::OC>(g_water, qq.data(), g.data());
   }
   const orc::OpTally& t = orc::tally();
   uint64_t v[14] = {t.add, t.mul, t.div,  t.sqrt, t.exp, t.log,  t.pow,

@@ -16,6 +16,8 @@
 #include <cmath>
 #include <vector>
 
+#include "opcount.hpp"
+
 namespace orc {
 namespace water {
 
@@ -56,16 +58,18 @@ struct Box {
 // the component exceeds half the box length.
 template <class T>
 inline void box_image(const Box& b, T* d) {
+  using std::fabs;
   for (int k = 0; k < 3; ++k) {
     const double L = b.len[k], L2 = 0.5 * b.len[k];
-    while (std::fabs(d[k]) > L2) d[k] = d[k] - std::copysign(L, d[k]);
+    while (fabs(d[k]) > T(L2)) d[k] = d[k] - T(std::copysign(L, val(d[k])));
   }
 }
 
 template <class T>
 inline T egrad(const Box& b, const T* x, T* g) {
-  using std::sqrt;
+  using std::erfc;
   using std::exp;
+  using std::sqrt;
   const Params P = params();
   const int n = 3 * b.nwater;
   T e = T(0);
@@ -142,10 +146,10 @@ inline T egrad(const Box& b, const T* x, T* g) {
       for (int k = 0; k < 3; ++k) d[k] = x[3 * i + k] - x[3 * j + k];
       if (b.periodic) box_image(b, d);
       const T r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-      if (!(r < b.coul_cut || !b.periodic)) continue;
+      if (!(r < T(b.coul_cut) || !b.periodic)) continue;
       const T oner = T(1) / r;
       T e0;
-      if (b.zahn) e0 = qi * qj * ((std::erfc(b.zahn_a * r) * oner) - b.zahn_par * (r - b.coul_cut));
+      if (b.zahn) e0 = qi * qj * ((erfc(b.zahn_a * r) * oner) - b.zahn_par * (r - b.coul_cut));
       else e0 = qi * qj * oner;
       e = e + e0;
       for (int k = 0; k < 3; ++k) {

@@ -37,3 +37,21 @@ def test_bimolecular_rate_formula():
     mu = m1 * m2 / (m1 + m2)
     au = 4 * np.pi * 100.0 * np.sqrt(1 / (2 * np.pi * beta * mu)) * np.exp(-beta * 0.01)
     assert k1 / au == pytest.approx(1e6 * 5.2917721092e-11 ** 3 / 2.418884326505e-17 * 6.02214179e23, rel=1e-6)
+
+
+def test_recross_restart_files_round_trip(tmp_path):
+    from caracal_gb300.calc_rate import read_recross_restart, write_recross_restart
+    num = np.linspace(0.1, 0.9, 7)
+    q = np.arange(2 * 3 * 3, dtype=float).reshape(2, 3, 3) * 0.1
+    write_recross_restart(str(tmp_path), 4, num, 2.5, q)
+    k, n2, d2, q2 = read_recross_restart(str(tmp_path), 7, 2, 3)
+    assert k == 4 and d2 == 2.5 and np.array_equal(n2, num) and np.array_equal(q2, q)
+    # an incomplete parent file: sums kept, no parent
+    (tmp_path / "recross_parent_pos.dat").write_text(" 1.0 2.0 3.0\n")
+    k, n2, d2, q2 = read_recross_restart(str(tmp_path), 7, 2, 3)
+    assert k == 4 and q2 is None
+    # too few numerators: a fresh start
+    (tmp_path / "recross_num_tmp.dat").write_text(" 0.5\n")
+    k, n2, d2, q2 = read_recross_restart(str(tmp_path), 7, 2, 3)
+    assert k == 0 and d2 == 0.0 and not n2.any() and q2 is None
+    assert read_recross_restart(str(tmp_path / "nothing"), 7, 2, 3)[0] == 0

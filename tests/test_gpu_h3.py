@@ -87,7 +87,12 @@ def test_single_step_matches_oracle(require_gpu, thermostat, nbeads):
     assert not st.any() and not so.any()
     assert rel_err(qg, qo) <= 1e-12
     assert rel_err(pg, po) <= 1e-12
-    assert rel_err(fg, fo) <= 1e-12
+    # forces of the step at its own new positions; against the oracle's step
+    # the positions may differ in the last bit, which moves BKMP2's gradient
+    # by ~1e-14 of its largest component (the bound's size at P = 3)
+    _, g_at = orc.egrad("h3", qg.reshape(-1, 3, 3))
+    assert rel_err(fg, g_at.reshape(fg.shape)) <= 1e-12
+    assert rel_err(fg, fo) <= 1e-11
     assert rel_err(eg, eo) <= 1e-12
 
 

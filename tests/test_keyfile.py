@@ -1,4 +1,5 @@
 """CPU: Caracal's keyword input (dynamic) and the list-directed output format."""
+import numpy as np
 import pytest
 
 from caracal_gb300 import keyfile as K
@@ -74,3 +75,18 @@ def test_list_directed_numbers_round_trip():
     assert fortran_real(1.0) == "   1.0000000000000000     "
     assert fortran_real(0.01) == "   1.0000000000000000E-002"
     assert fortran_int(48) == "          48"
+
+
+def test_read_vel_keyword_and_file(tmp_path):
+    from caracal_gb300.dynamic import momenta_from_velocities
+    key = "XYZSTART s.xyz\nRPMD_BEADS 2\nENSEMBLE NVT\nNVT {\n TEMP 300\n THERMOSTAT ANDERSEN\n}\n" \
+          "STEPS 10\nDELTAT 0.5\nTDUMP 1\nPES ana_h3\nREAD_VEL\n"
+    d = K.parse(key)
+    assert d.read_vel and not d.unsupported
+    (tmp_path / "velocity_start.dat").write_text(
+        " header\n\n 1 1  1.0d-4 -2.0E-4 3.0e-4\n 2 1 0.0 0.5d-3 0\n 3 1 1 2 3\n")
+    v = K.read_velocities(str(tmp_path / "velocity_start.dat"), 3)
+    assert np.allclose(v, [[1e-4, -2e-4, 3e-4], [0, 5e-4, 0], [1, 2, 3]])
+    m = np.array([1.0, 2.0, 3.0])
+    p = momenta_from_velocities(v, m, (4, 2, 3, 3))
+    assert np.allclose(p[:, 0], -v * m[:, None]) and not p[:, 1].any()

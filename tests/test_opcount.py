@@ -33,6 +33,18 @@ def test_qmdff_table_matches_oracle_counts():
     assert counted == _bench().ALGO_PES_OPS["qmdff"]
 
 
+def test_water_table_matches_oracle_counts():
+    from caracal_gb300 import water as Wt
+    from caracal_gb300.workloads import water_config
+    wl = water_config()
+    x = wl.extra
+    box, cut, za, zp = Wt.periodic_setup(x["box"], x["coul_cut"], x["zahn"])
+    orc.set_water(x["nwater"], box, cut)
+    q = wl.q0 + np.random.default_rng(0).normal(0, 0.05, wl.q0.shape)
+    counted = {k: v for k, v in orc.pes_opcount("water", q).items() if v and k != "cmp"}
+    assert counted == _bench().ALGO_PES_OPS["water"]
+
+
 def test_algo_flops_positive_and_monotone_in_beads():
     b = _bench()
     w = {k: 20.0 for k in ("div", "sqrt", "exp", "pow", "log", "sin", "cos", "acos", "erf", "tanh",
