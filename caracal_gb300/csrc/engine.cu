@@ -13,6 +13,7 @@
 #include "pes_ch4h.cuh"
 #include "pes_ch4oh.cuh"
 #include "pes_h3.cuh"
+#include "pes_oh3.cuh"
 #include "rpmd_kernel.cuh"
 #include "host_util.h"
 #include "qmdff_host.h"
@@ -48,6 +49,7 @@ int pes_natoms(int pes) {
     case CR_PES_H3: return 3;
     case CR_PES_CH4H: return 6;
     case CR_PES_CH4OH: return 7;
+    case CR_PES_OH3: return 4;
     default: return -1;
   }
 }
@@ -453,6 +455,7 @@ int split_forces_range(cr_engine* e, int t0, int tn, double* V, double* f, cudaS
     case CR_PES_H3: return egrad_launch<cr::PesH3>(e, V, f);
     case CR_PES_CH4H: return egrad_launch<cr::PesCH4H>(e, V, f);
     case CR_PES_CH4OH: return egrad_launch<cr::PesCH4OH>(e, V, f);
+    case CR_PES_OH3: return egrad_launch<cr::PesOH3>(e, V, f);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -477,6 +480,11 @@ int parent_kernel(cr_engine* e, int which) {
       if (which == 0) cr::split_shake_kernel<7><<<T, 32, 0, e->stream>>>(e->sp);
       else if (which == 1) cr::split_rattle_kernel<7><<<T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
       else cr::split_parent_init_kernel<7><<<(T + 63) / 64, 64, 0, e->stream>>>(e->sp);
+      break;
+    case 4:
+      if (which == 0) cr::split_shake_kernel<4><<<T, 32, 0, e->stream>>>(e->sp);
+      else if (which == 1) cr::split_rattle_kernel<4><<<T, cr::kFinishBlock, 0, e->stream>>>(e->sp);
+      else cr::split_parent_init_kernel<4><<<(T + 63) / 64, 64, 0, e->stream>>>(e->sp);
       break;
     default: return fail(CR_ERR_UNSUPPORTED, "constrained parents are built for the analytic surfaces");
   }
@@ -541,6 +549,7 @@ int split_group_launches(cr_engine* e, const cr::SplitParams& s, int t0, int tn,
       case 3: cr::split_umbrella_kernel<3><<<tn, 64, 0, st>>>(s); break;
       case 6: cr::split_umbrella_kernel<6><<<tn, 64, 0, st>>>(s); break;
       case 7: cr::split_umbrella_kernel<7><<<tn, 64, 0, st>>>(s); break;
+      case 4: cr::split_umbrella_kernel<4><<<tn, 64, 0, st>>>(s); break;
       default: return fail(CR_ERR_UNSUPPORTED, "umbrella windows are built for the analytic surfaces");
     }
     CR_CUDA(cudaGetLastError());
@@ -659,6 +668,7 @@ int dispatch_run(cr_engine* e, int nsteps) {
     case CR_PES_H3: return launch_run<cr::PesH3>(e, nsteps);
     case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, nsteps);
     case CR_PES_CH4OH: return launch_run<cr::PesCH4OH>(e, nsteps);
+    case CR_PES_OH3: return launch_run<cr::PesOH3>(e, nsteps);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -675,6 +685,7 @@ int dispatch_forces(cr_engine* e) {
     case CR_PES_H3: return launch_forces<cr::PesH3>(e);
     case CR_PES_CH4H: return launch_forces<cr::PesCH4H>(e);
     case CR_PES_CH4OH: return launch_forces<cr::PesCH4OH>(e);
+    case CR_PES_OH3: return launch_forces<cr::PesOH3>(e);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -791,6 +802,7 @@ int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d
     case CR_PES_H3: return egrad_device_impl<cr::PesH3>(d_q, npts, d_V, d_dVdq, precision, s);
     case CR_PES_CH4H: return egrad_device_impl<cr::PesCH4H>(d_q, npts, d_V, d_dVdq, precision, s);
     case CR_PES_CH4OH: return egrad_device_impl<cr::PesCH4OH>(d_q, npts, d_V, d_dVdq, precision, s);
+    case CR_PES_OH3: return egrad_device_impl<cr::PesOH3>(d_q, npts, d_V, d_dVdq, precision, s);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -811,6 +823,10 @@ int cr_egrad_ch4oh(const double* q, int natoms, int nbeads, double* V, double* d
 }
 
 int cr_initialize_ch4oh(void) { return CR_OK; }
+
+int cr_egrad_oh3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
+  return egrad_host(CR_PES_OH3, 4, q, natoms, nbeads, V, dVdq, info);
+}
 
 int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
   if (info) *info = 0;
@@ -1195,6 +1211,10 @@ int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
       cr::init_positions_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
       break;
+    case CR_PES_OH3:
+      cr::init_positions_kernel<12><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
+      break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
   CR_CUDA(cudaGetLastError());
@@ -1228,6 +1248,10 @@ int cr_engine_init_momenta(cr_engine* e, int zero) {
       break;
     case CR_PES_CH4OH:
       cr::init_momenta_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+      break;
+    case CR_PES_OH3:
+      cr::init_momenta_kernel<12><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
       break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
@@ -1355,6 +1379,7 @@ static int host_group_step(cr_engine* e, int t0, int tn, cudaStream_t st, int* n
     case CR_PES_H3: return launch_group<cr::PesH3>(e, t0, tn, st);
     case CR_PES_CH4H: return launch_group<cr::PesCH4H>(e, t0, tn, st);
     case CR_PES_CH4OH: return launch_group<cr::PesCH4OH>(e, t0, tn, st);
+    case CR_PES_OH3: return launch_group<cr::PesOH3>(e, t0, tn, st);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -1392,6 +1417,7 @@ int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* e
       case CR_PES_H3: rc = set_run_smem<cr::PesH3>(e); break;
       case CR_PES_CH4H: rc = set_run_smem<cr::PesCH4H>(e); break;
       case CR_PES_CH4OH: rc = set_run_smem<cr::PesCH4OH>(e); break;
+      case CR_PES_OH3: rc = set_run_smem<cr::PesOH3>(e); break;
       default: rc = fail(CR_ERR_UNSUPPORTED, "PES not built");
     }
     if (rc) return rc;
@@ -1661,6 +1687,10 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
       cr::init_children_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
       break;
+    case CR_PES_OH3:
+      cr::init_children_kernel<12><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
+      break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
   CR_CUDA(cudaGetLastError());
@@ -1676,6 +1706,9 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
       break;
     case CR_PES_CH4OH:
       cr::child_flux_kernel<7><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
+      break;
+    case CR_PES_OH3:
+      cr::child_flux_kernel<4><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
       break;
     default: break;
   }
@@ -1742,6 +1775,7 @@ int batch_prepare(cr_engine* e) {
     case CR_PES_H3: return set_run_smem<cr::PesH3>(e);
     case CR_PES_CH4H: return set_run_smem<cr::PesCH4H>(e);
     case CR_PES_CH4OH: return set_run_smem<cr::PesCH4OH>(e);
+    case CR_PES_OH3: return set_run_smem<cr::PesOH3>(e);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }
@@ -1758,6 +1792,7 @@ int batch_branch(cr_engine* e, int len) {
     case CR_PES_H3: return launch_run<cr::PesH3>(e, len, true);
     case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, len, true);
     case CR_PES_CH4OH: return launch_run<cr::PesCH4OH>(e, len, true);
+    case CR_PES_OH3: return launch_run<cr::PesOH3>(e, len, true);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
 }

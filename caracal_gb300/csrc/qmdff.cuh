@@ -805,11 +805,8 @@ __device__ inline float ex2_approx(float x) {
 // BJ damping, eps2 into the C6 / C8 and repulsion prefactors, alpha log2(e)
 // for a base-2 exponential).  The pair forces are ~1 % of the valence
 // forces, so hardware approximations stay far below the form's error budget.
-__device__ inline float pair_mixed(const Dev& D, const BeadPos& x, int kp, Contrib<float>& c) {
-  const int2 ij = __ldg(reinterpret_cast<const int2*>(D.pair) + kp);
-  const int i1 = ij.x, i2 = ij.y;
-  float v[kVPair];
-  load_pair_params(&D.fpair[kVPair * kp], v);
+__device__ inline float pair_mixed_v(const Dev& D, const BeadPos& x, int i1, int i2, const float (&v)[kVPair],
+                                     Contrib<float>& c) {
   float vab[3];
   disp<float>(x, i1, i2, vab);
   const float r2 = dot3(vab, vab);
@@ -840,6 +837,13 @@ __device__ inline float pair_mixed(const Dev& D, const BeadPos& x, int kp, Contr
     c.g[1][d] = -vab[d] * drij;
   }
   return e;
+}
+
+__device__ inline float pair_mixed(const Dev& D, const BeadPos& x, int kp, Contrib<float>& c) {
+  const int2 ij = __ldg(reinterpret_cast<const int2*>(D.pair) + kp);
+  float v[kVPair];
+  load_pair_params(&D.fpair[kVPair * kp], v);
+  return pair_mixed_v(D, x, ij.x, ij.y, v, c);
 }
 
 // x^5, x^6, x^12 by products (the reference's real-exponent ** operators)
@@ -1062,6 +1066,43 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
   }
 }
 
+// Mixed-form NCI pairs: every batch is one matching (one colour), so each
+// lane scatters right after its term; the next batch's slot, atom pair and
+// parameters are loaded before the current batch's arithmetic, so the L1
+// latency of the term tables overlaps the work.
+__device__ inline void pair_batches_mixed(const Dev& D, const BeadPos& X, Grad<float>& G, float& es, float& ec,
+                                          int lane) {
+  const Schedule& S = D.sched[1];
+  const int b0 = S.boff[3], nb = S.nb[3];
+  if (nb <= 0) return;
+  int m = S.slot[32 * b0 + lane];
+  int2 ij = m >= 0 ? __ldg(reinterpret_cast<const int2*>(D.pair) + m) : make_int2(0, 0);
+  float4 pa = m >= 0 ? __ldg(reinterpret_cast<const float4*>(&D.fpair[kVPair * m])) : make_float4(0, 0, 0, 0);
+  float4 pb = m >= 0 ? __ldg(reinterpret_cast<const float4*>(&D.fpair[kVPair * m]) + 1) : make_float4(0, 0, 0, 0);
+  for (int b = b0; b < b0 + nb; ++b) {
+    const int mc = m;
+    const int2 ijc = ij;
+    const float v[kVPair] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
+    if (b + 1 < b0 + nb) {
+      m = S.slot[32 * (b + 1) + lane];
+      if (m >= 0) {
+        ij = __ldg(reinterpret_cast<const int2*>(D.pair) + m);
+        pa = __ldg(reinterpret_cast<const float4*>(&D.fpair[kVPair * m]));
+        pb = __ldg(reinterpret_cast<const float4*>(&D.fpair[kVPair * m]) + 1);
+      }
+    }
+    if (mc >= 0) {
+      Contrib<float> c;
+      const float e = pair_mixed_v(D, X, ijc.x, ijc.y, v, c);
+      const float t = es + e;
+      ec += (fabsf(es) >= fabsf(e)) ? ((es - t) + e) : ((e - t) + es);
+      es = t;
+      scatter_pair<2>(c, G);
+    }
+    __syncwarp();
+  }
+}
+
 // Shared memory per warp (bytes): coordinates (3n doubles), the FP32 split
 // (hi, lo) (3n float pairs) and the gradient (3n doubles, or (sum,
 // compensation) float pairs and the 3n floats of the pair sum).
@@ -1100,7 +1141,8 @@ __device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, doub
   kind_batches<MIXED, 0, 2>(D, X, G, es, ec, lane);
   kind_batches<MIXED, 1, 3>(D, X, G, es, ec, lane);
   kind_batches<MIXED, 2, 4>(D, X, G, es, ec, lane);
-  kind_batches<MIXED, 3, 2>(D, X, G, es, ec, lane);
+  if constexpr (MIXED) pair_batches_mixed(D, X, G, es, ec, lane);
+  else kind_batches<MIXED, 3, 2>(D, X, G, es, ec, lane);
   kind_batches<MIXED, 4, 3>(D, X, G, es, ec, lane);
   for (int a = lane; a < n3; a += 32) gout[a] = gscale * G.get(a);
   double e = (double)es + (double)ec;

@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib as L
 from .units import beta_from_kelvin, dt_fs_to_au
 
-PES = {"h3": L.CR_PES_H3, "ana_h3": L.CR_PES_H3, "ch4h": L.CR_PES_CH4H, "ana_ch4h": L.CR_PES_CH4H,
+PES = {"h3": L.CR_PES_H3, "ana_h3": L.CR_PES_H3, "oh3": L.CR_PES_OH3, "ana_oh3": L.CR_PES_OH3, "ch4h": L.CR_PES_CH4H, "ana_ch4h": L.CR_PES_CH4H,
        "ch4oh": L.CR_PES_CH4OH, "ana_ch4oh": L.CR_PES_CH4OH}
 PES_NATOMS = {L.CR_PES_H3: 3, L.CR_PES_CH4H: 6, L.CR_PES_CH4OH: 7}
 THERMOSTAT = {"none": L.CR_THERMO_NONE, "nve": L.CR_THERMO_NONE, "andersen": L.CR_THERMO_ANDERSEN,
@@ -69,6 +69,22 @@ def egrad_ch4oh(q):
     g = np.zeros_like(q)
     info = C.c_int(0)
     L.check(L.lib().cr_egrad_ch4oh(L.dptr(q), 7, nb, L.dptr(V), L.dptr(g), C.byref(info)), "egrad_ch4oh")
+    return V, g
+
+
+def egrad_oh3(q):
+    """OH + H2 (Schatz-Elgersma, ANA_OH3) energies and gradients of q
+    (nbeads, 4, 3) bohr, atoms O, H, H, H."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    if q.ndim == 2:
+        q = q[None]
+    nb = q.shape[0]
+    if q.shape[1:] != (4, 3):
+        raise ValueError("egrad_oh3 expects q of shape (nbeads, 4, 3)")
+    V = np.zeros(nb)
+    g = np.zeros_like(q)
+    info = C.c_int(0)
+    L.check(L.lib().cr_egrad_oh3(L.dptr(q), 4, nb, L.dptr(V), L.dptr(g), C.byref(info)), "egrad_oh3")
     return V, g
 
 

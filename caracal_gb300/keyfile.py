@@ -26,7 +26,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh"}
+ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh", "ANA_OH3": "oh3"}
 EVB_BASES = ("1g", "2g", "3g", "sp", "sd", "sd2", "sp2d")
 KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE",
          "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "READ_VEL", "}"}

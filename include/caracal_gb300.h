@@ -42,6 +42,7 @@ extern "C" {
 #define CR_PES_QMDFF 4   /* QMDFF: src/ff_eg.f90, ff_nonb.f90, ff_hb.f90 */
 #define CR_PES_EVB 5     /* dE-EVB of two QMDFFs: src/gradient.f90:361-386, 1228-1304 */
 #define CR_PES_WATER 6   /* flexible SPC water box: src/egrad_water.f90, src/water_init.f90 */
+#define CR_PES_OH3 7     /* ANA_OH3: OH + H2 (Schatz-Elgersma), src/egrad_oh3.f */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
 #define CR_THERMO_NONE 0      /* NVE */
@@ -142,6 +143,8 @@ int cr_initialize_ch4h(void);
  * called from src/gradient.f90:180): natoms = 7 in Caracal's order H, C, H, H, H, O, H(O)
  * (methane H = atoms 3,4,5,1; O abstracts), bohr -> Hartree. */
 int cr_egrad_ch4oh(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+/* egrad_oh3 (src/egrad_oh3.f:33-189): atoms O, H, H, H; natoms must be 4. */
+int cr_egrad_oh3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
 /* Replaces `subroutine initialize_ch4oh()` (src/egrad_ch4oh.f:33, called from
  * src/read_pes.f90:591); constants are compiled in, always CR_OK. */
 int cr_initialize_ch4oh(void);

@@ -16,6 +16,7 @@
 #include "pes_evb.hpp"
 #include "pes_qmdff.hpp"
 #include "pes_water.hpp"
+#include "pes_oh3.hpp"
 #include "philox.hpp"
 #include "recross.hpp"
 #include "rpmd.hpp"
@@ -54,6 +55,7 @@ struct BeadPES {
       case 4: orc::qmdff::egrad(g_qmdff, q, V, g); break;
       case 5: orc::evb::egrad(g_qmdff, g_qmdff2, g_evb, q, V, g); break;
       case 6: *V = orc::water::egrad<double>(g_water, q, g); break;
+      case 7: orc::oh3::egrad_bead<double>(q, V, g); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
   }
@@ -377,6 +379,10 @@ void orc_pes_opcount(int pes, const double* q, uint64_t out[14]) {
     orc::OC V;
     for (int x = 0; x < n3; ++x) qq[(size_t)x] = orc::OC(q[x]);
     orc::qmdff::egrad<orc::OC>(g_qmdff, qq.data(), &V, g.data());
+  } else if (pes == 7) {
+    orc::OC qq[12], V, g[12];
+    for (int x = 0; x < 12; ++x) qq[x] = orc::OC(q[x]);
+    orc::oh3::egrad_bead<orc::OC>(qq, &V, g);
   } else if (pes == 6) {
     const int n3 = 9 * g_water.nwater;
     std::vector<orc::OC> qq((size_t)n3), g((size_t)n3);
