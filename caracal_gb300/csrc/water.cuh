@@ -17,7 +17,8 @@
 // r >= coul_cut skipped.  Each pair's energy counts once (thread min(i, j)).
 //
 // Mixed form: the pairs in FP32 from the (hi, lo) split of the coordinates,
-// their forces accumulated in FP64; the intramolecular terms stay FP64.
+// their forces and energies accumulated as compensated FP32 sums; the
+// intramolecular terms stay FP64.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -154,7 +155,16 @@ __device__ inline double pairs_plain(const Dev& D, const double* x, int i, doubl
   return e;
 }
 
-// The same in FP32 from the (hi, lo) coordinates, forces summed in FP64.
+// Error-free FP32 sum (Knuth's TwoSum): s + e == a + b exactly.
+__device__ inline void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// The same in FP32 from the (hi, lo) coordinates; forces and energy summed
+// as compensated FP32 pairs (sum + compensation, TwoSum per term), which
+// keeps the FP64-quality sums on the FP32 pipes.
 // The truncated Coulomb sum jumps by q_i q_j / r_cut where a pair crosses the
 // cutoff, so the cutoff decision must be the plain form's: where the FP32 r
 // lies within 1e-5 of the cutoff, the FP64 distance (same image loop, same
@@ -164,7 +174,7 @@ __device__ inline double pairs_mixed(const Dev& D, const double* x, const float2
   float2 xi[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) xi[k] = hl[3 * i + k];
-  double e = 0.0;
+  float es = 0.f, ec = 0.f, fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
   for (int j = 0; j < D.n; ++j) {
     if (j / 3 == i / 3) continue;
     const float qj = (j % 3 == 0) ? D.feo : D.feh;
@@ -201,11 +211,23 @@ __device__ inline double pairs_mixed(const Dev& D, const double* x, const float2
       ep += 4.0f * D.feps * (s6 * s6 - s6);
       s += 24.0f * D.feps * ir2 * s6 * (2.0f * s6 - 1.0f);
     }
-    if (j > i) e += (double)ep;
+    if (j > i) {
+      float t, r;
+      two_sum(es, ep, t, r);
+      es = t;
+      ec += r;
+    }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) f[k] -= (double)(s * d[k]);
+    for (int k = 0; k < 3; ++k) {
+      float t, r;
+      two_sum(fs[k], -(s * d[k]), t, r);
+      fs[k] = t;
+      fc[k] += r;
+    }
   }
-  return e;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) f[k] += (double)fs[k] + (double)fc[k];
+  return (double)es + (double)ec;
 }
 
 }  // namespace water
