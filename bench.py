@@ -45,6 +45,8 @@ ALGO_PES_OPS = {
     # geometry + N(0, 0.05 bohr) per coordinate, seed 0); asin counted with acos
     "qmdff": {"add": 92211, "mul": 117770, "div": 20592, "sqrt": 4525, "exp": 1415, "pow": 122,
               "sin": 633, "cos": 753, "acos": 291, "erf": 171},
+    # OH + H2 (Schatz-Elgersma), the reactant approach of workloads.oh3_geometry
+    "oh3": {"add": 218, "mul": 199, "div": 43, "sqrt": 7, "exp": 14, "tanh": 6, "cosh": 6},
     # flexible SPC water, 64 molecules, periodic box 23.47 bohr, Coulomb
     # cutoff 6 A, thermal geometry (grid geometry + N(0, 0.05 bohr), seed 0)
     "water": {"add": 194295, "mul": 201198, "div": 9259, "sqrt": 18336, "exp": 128},
@@ -216,6 +218,8 @@ def workload(name):
         return W.qmdff_config(ntraj=512, nbeads=64)
     if name == "water":
         return W.water_config(nwater=64, ntraj=64, nbeads=32)
+    if name == "oh3":
+        return W.oh3_config(ntraj=4096, nbeads=32)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -809,7 +813,7 @@ def main():
                     help="ch4h (CH4+H recrossing children, 4096 x 32 beads: the default), "
                          "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16), "
                          "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (512 x 64), "
-                         "water (flexible SPC, 64 molecules, periodic, 64 x 32), "
+                         "water (flexible SPC, 64 molecules, periodic, 64 x 32), oh3 (OH + H2, 4096 x 32), "
                          "classes (H3 4096x8, CH4H 2048x32, CH4OH 512x64, QMDFF 128x128 in one batch), "
                          "classes_small (the same with 1/16 of the trajectories), "
                          "adjoint (force matching over 8192 C20H42 geometries and a 200-step trajectory adjoint)")

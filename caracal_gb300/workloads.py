@@ -121,6 +121,21 @@ def qmdff_config(ntraj=1024, nbeads=64, nsteps=500, kelvin=300.0, dt_fs=0.5, nc=
                     sigma_bohr=float(angstrom_to_bohr(0.01)), transrot=True, extra={"ff": ff})
 
 
+def oh3_geometry():
+    """OH + H2 approach in Caracal's ANA_OH3 atom order (O, H of OH, H, H):
+    r(OH) = 0.97 A, H2 at 1.4 bohr, its near H 2.9 bohr from O (bohr)."""
+    return np.array([[0.0, 0.0, 0.0], [1.83, 0.0, 0.0], [-0.6, 2.9, 0.1], [-0.8, 4.3, 0.2]])
+
+
+def oh3_config(ntraj=4096, nbeads=32, nsteps=500, kelvin=300.0, dt_fs=0.1, thermostat="andersen",
+               andersen_step=70):
+    """OH + H2 on the Schatz-Elgersma surface (ANA_OH3): T trajectories of P beads
+    near the reactant approach, NVT 300 K, 0.1 fs, 0.01 A bead jitter."""
+    return Workload(name=f"oh3_P{nbeads}_T{ntraj}", pes="oh3", symbols=["O", "H", "H", "H"], q0=oh3_geometry(),
+                    nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs, nsteps=nsteps, thermostat=thermostat,
+                    andersen_step=andersen_step, sigma_bohr=float(angstrom_to_bohr(0.01)), transrot=True)
+
+
 def water_config(nwater=64, ntraj=64, nbeads=32, nsteps=500, kelvin=300.0, dt_fs=0.25, coul_cut_ang=6.0,
                  thermostat="andersen", andersen_step=70, zahn=False):
     """Periodic box of Caracal's flexible SPC water (water_spc): nwater
