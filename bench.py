@@ -199,6 +199,11 @@ def calibrate(L):
         fma = rates["fma"]
         out[tag] = {"fma_per_s": fma, "peak_tflops": 2 * fma / 1e12,
                     "w": {k: 2.0 * fma / v for k, v in rates.items() if k != "fma"}}
+    # FP64 tensor-core MMA (m8n8k4) multiply-adds per second, for the bead
+    # transform as a dense contraction against DFMA code
+    r = np.zeros(1)
+    L.check(L.lib().cr_calibrate_op(1, 12, 2000, L.dptr(r)), "calibrate dmma")
+    out["fp64"]["dmma_fma_per_s"] = float(r[0])
     return out
 
 
@@ -268,7 +273,7 @@ class OracleRunner:
         self.orc, self.wl = orc, wl
         if wl.pes == "qmdff":
             from caracal_gb300 import qmdff as Q
-            orc.set_qmdff(wl.extra["ff"], Q.ElementTables.d3_like())
+            orc.set_qmdff(wl.extra["ff"], Q.ElementTables.caracal())
         if wl.pes == "water":
             from caracal_gb300 import water as Wt
             x = wl.extra
@@ -410,9 +415,28 @@ def run_ours(args):
             ms = float(t.item())
         return ms
 
-    ms_64 = timed_run(eng_64)
+    # the plain FP64 arm: at least 200 timed steps (one launch, a few hundred
+    # ms), so its rate -- the denominator of mixed/plain -- is stable
+    K64 = max(K, 200)
+
+    def timed_plain():
+        eng_64.run(W)
+        flush.zero_()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        eng_64.run(K64)
+        torch.cuda.synchronize()
+        ms = eng_64.last_kernel_ms()
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
     with ClockSampler(dev) as clk:
         ms_mx = timed_run(eng_mx)
+        ms_64 = timed_plain()
         # keep the sampler alive over at least a few samples
         if ms_mx < 500:
             extra = max(1, int(500 / max(ms_mx, 1e-3)))
@@ -421,7 +445,7 @@ def run_ours(args):
     clocks = clk.summary()
     bead_steps = wl.ntraj * wl.nbeads * K
     value = ws * bead_steps / (ms_mx * 1e-3)
-    plain = ws * bead_steps / (ms_64 * 1e-3)
+    plain = ws * wl.ntraj * wl.nbeads * K64 / (ms_64 * 1e-3)
 
     # force error of the mixed form against FP64 at the same positions
     q, p, f, e, st = eng_64.get_state()
@@ -463,13 +487,41 @@ def run_ours(args):
     for ptr, _ in bufs:
         L.lib().cr_host_free(ptr)
 
+    # the same with the caller's own (pageable) numpy arrays, as Caracal's
+    # module arrays are: staged by the driver, then page-locked in place by
+    # cr_host_register (PinnedHost), which is how a Fortran caller would use it
+    from caracal_gb300.engine import PinnedHost
+    aq, ap, af, ae = q.copy(), p.copy(), f.copy(), np.zeros(wl.ntraj)
+
+    def e2e_loop():
+        for _ in range(min(W, 3)):
+            eng_mx.step_host(aq, ap, af, ae)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(K_e2e):
+            eng_mx.step_host(aq, ap, af, ae)
+        el = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([el], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        return ws * wl.ntraj * wl.nbeads * K_e2e / el
+
+    e2e_pageable = e2e_loop()
+    with PinnedHost(aq, ap, af):
+        e2e_registered = e2e_loop()
+
     # rooflines of the step kernel (headline: the mixed form, whose launch `value` times)
     roof = roofline(wl, True, ms_mx, K, cal)
-    roof_plain = roofline(wl, False, ms_64, K, cal)
+    roof_plain = roofline(wl, False, ms_64, K64, cal)
     kappa = None
     if wl.extra.get("recross") is not None:
+        from caracal_gb300.replicas import allreduce_kappa
         num, den, _ = eng_64.kappa(cap)
-        kappa = {"steps": len(num), "kappa_last": float(num[-1] / den) if den else None}
+        num, den = allreduce_kappa(num, den, dist)      # the replicas' children together
+        kappa = {"steps": len(num), "kappa_last": float(num[-1] / den) if den else None,
+                 "children": ws * wl.ntraj}
     info = eng_mx.launch_info()
     line = {
         "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": ws, "steps": K,
@@ -481,17 +533,21 @@ def run_ours(args):
                    "l2": "flushed (256 MB write) before the timed launch"
                          + ("; K steps in one launch" if wl.pes not in ("qmdff", "water") else
                             f"; state (3 x {nbytes / 1e6:.1f} MB) streamed every step (graph path)")},
-        "plain_fp64": {"value": plain, "unit": "bead-steps/s", "ms_per_step": ms_64 / K},
+        "plain_fp64": {"value": plain, "unit": "bead-steps/s", "ms_per_step": ms_64 / K64, "steps": K64},
         "mixed_over_plain": value / plain,
         "force_error_vs_fp64": ferr, "energy_error_vs_fp64": eerr,
         "e2e": {"value": e2e, "unit": "bead-steps/s", "steps": K_e2e,
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": 3 * nbytes + 8 * wl.ntraj},
+        "e2e_caller_arrays": {"pageable": e2e_pageable, "registered": e2e_registered, "unit": "bead-steps/s",
+                              "note": "the same loop on the caller's numpy arrays: pageable, then page-locked "
+                                      "in place by cr_host_register"},
         "gpu_launches": info["launches"],
         "launch": info,
         "roofline": roof,
         "roofline_plain_fp64": roof_plain,
         "recross": kappa,
         "calibration": {"fp64_peak_tflops": cal["fp64"]["peak_tflops"],
+                        "fp64_dmma_over_dfma": cal["fp64"]["dmma_fma_per_s"] / cal["fp64"]["fma_per_s"],
                         "fp32_peak_tflops": cal["fp32"]["peak_tflops"],
                         "fp64_op_cost_flops": cal["fp64"]["w"], "fp32_op_cost_flops": cal["fp32"]["w"]},
         "clocks": clocks,
@@ -827,6 +883,15 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # N replicas need N ranks: start them with torch.distributed.run (one
+        # process per GPU, rendezvous on 127.0.0.1), as the driver would
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", os.environ.get("MASTER_PORT", "29531"),
+               os.path.abspath(__file__)] + sys.argv[1:]
+        raise SystemExit(subprocess.call(cmd))
+    if args.gpus != int(os.environ.get("WORLD_SIZE", "1")):
+        raise SystemExit(f"--gpus {args.gpus} but WORLD_SIZE={os.environ.get('WORLD_SIZE', '1')}")
     if args.workload == "adjoint":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "Caracal has no parameter gradients of "

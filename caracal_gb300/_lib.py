@@ -49,7 +49,7 @@ class CrConfig(C.Structure):
                 ("thermostat", C.c_int), ("andersen_step", C.c_int), ("transrot", C.c_int),
                 ("precision", C.c_int), ("seed", C.c_uint), ("traj0", C.c_uint),
                 ("dt", C.c_double), ("beta", C.c_double), ("pile_tau0", C.c_double),
-                ("mass", c_double_p), ("nose_q", C.c_double)]
+                ("mass", c_double_p), ("nose_q", C.c_double), ("nm_mode", C.c_int)]
 
 
 DUMP_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -58,6 +58,10 @@ DUMP_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POI
 
 class CrQmdffTables(C.Structure):
     _fields_ = [(k, C.POINTER(C.c_double)) for k in ("rad", "r0ab", "zab", "r0094", "sr42", "c6ab")]
+
+
+class CrD3Reference(C.Structure):
+    _fields_ = [("c6ab", C.POINTER(C.c_double)), ("maxci", C.POINTER(C.c_int)), ("rcov", C.POINTER(C.c_double))]
 
 
 class CrRecross(C.Structure):
@@ -133,6 +137,8 @@ def _sig(lib):
                                     C.POINTER(C.c_void_p)], C.c_int),
         "cr_host_alloc": ([C.POINTER(C.c_void_p), C.c_ulonglong], C.c_int),
         "cr_host_free": ([v], C.c_int),
+        "cr_host_register": ([v, C.c_ulonglong], C.c_int),
+        "cr_host_unregister": ([v], C.c_int),
         "cr_calibrate_op": ([C.c_int, C.c_int, C.c_int, d], C.c_int),
         "cr_engine_set_recross": ([eng, C.POINTER(CrRecross), C.c_int], C.c_int),
         "cr_engine_init_children": ([eng, d], C.c_int),
@@ -153,6 +159,11 @@ def _sig(lib):
         "cr_qmdff_load": ([C.c_char_p, C.POINTER(CrQmdffTables), C.c_double, C.c_int, C.c_double,
                            C.POINTER(C.c_void_p)], C.c_int),
         "cr_qmdff_file_counts": ([C.c_char_p, i, i], C.c_int),
+        "cr_qmdff_eg": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
+        "cr_qmdff_nonb": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
+        "cr_qmdff_hb": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
+        "cr_qmdff_load_d3": ([C.c_char_p, C.POINTER(CrQmdffTables), C.POINTER(CrD3Reference), C.c_double, C.c_int,
+                              C.c_double, C.POINTER(C.c_void_p)], C.c_int),
         "cr_qmdff_hvp": ([v, d, d, C.c_int, d, d, d], C.c_int),
         "cr_qmdff_param_vjp": ([v, d, d, C.c_int, d], C.c_int),
         "cr_evb_fit": ([C.c_int, d, C.c_int, C.c_int, d, d, d, d, d], C.c_int),
@@ -165,6 +176,8 @@ def _sig(lib):
         "cr_engine_set_umbrella": ([eng, C.POINTER(CrRecross), d, d, C.c_int, C.c_double, C.c_double], C.c_int),
         "cr_engine_umbrella_sampling": ([eng, C.c_int], C.c_int),
         "cr_engine_umbrella_stats": ([eng, d, d, d, C.c_int], C.c_int),
+        "cr_engine_mdinit": ([eng, C.c_uint], C.c_int),
+        "cr_engine_set_andersen_step": ([eng, C.c_int], C.c_int),
         "cr_batch_create": ([C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
         "cr_batch_run": ([v, C.c_int], C.c_int),
         "cr_batch_info": ([v, C.POINTER(C.c_longlong), i, C.POINTER(C.c_float)], C.c_int),

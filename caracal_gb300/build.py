@@ -41,7 +41,11 @@ def _stale() -> bool:
 
 def _compile(src: str, verbose: bool) -> tuple[str, str]:
     obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
-    cmd = [nvcc_path(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
+    # host code without FMA contraction: its set-up arithmetic (the QMDFF
+    # reader's coordination numbers and C6) then rounds as the Python host
+    # does on both x86_64 and aarch64
+    cmd = [nvcc_path(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
+           "-ffp-contract=off", "-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, capture_output=True, text=True)

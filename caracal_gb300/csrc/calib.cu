@@ -66,6 +66,29 @@ __global__ void calib_kernel(F* out, int iters) {
   if (s == F(-12345)) out[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the work alive
 }
 
+// FP64 tensor-core throughput: kChains independent m8n8k4 accumulations per
+// warp (A 8x4 row, B 4x8 col: one double of each per thread, D 8x8: two).
+__global__ void calib_dmma_kernel(double* out, int iters) {
+  const double a = 1e-3 + 1e-9 * threadIdx.x, b = 1e-3;
+  double d0[kChains], d1[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) {
+    d0[c] = 1e-3 * c;
+    d1[c] = 0.0;
+  }
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
+                   : "+d"(d0[c]), "+d"(d1[c])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) s += d0[c] + d1[c];
+  if (s == -12345.0) out[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the work alive
+}
+
 template <class F>
 int run_one(int op, int iters, float* ms) {
   int dev = 0, sms = 0;
@@ -91,6 +114,9 @@ int run_one(int op, int iters, float* ms) {
       case CR_CALIB_ERF: calib_kernel<F, CR_CALIB_ERF><<<grid, block>>>(out, iters); break;
       case CR_CALIB_TANH: calib_kernel<F, CR_CALIB_TANH><<<grid, block>>>(out, iters); break;
       case CR_CALIB_COSH: calib_kernel<F, CR_CALIB_COSH><<<grid, block>>>(out, iters); break;
+      case CR_CALIB_DMMA:
+        if constexpr (sizeof(F) == 8) calib_dmma_kernel<<<grid, block>>>(out, iters);
+        break;
       default: break;
     }
   };
@@ -109,7 +135,8 @@ int run_one(int op, int iters, float* ms) {
 }  // namespace
 
 extern "C" int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s) {
-  if (!ops_per_s || op < CR_CALIB_FMA || op > CR_CALIB_COSH || iters < 1) return CR_ERR_ARG;
+  if (!ops_per_s || op < CR_CALIB_FMA || op > CR_CALIB_DMMA || iters < 1) return CR_ERR_ARG;
+  if (op == CR_CALIB_DMMA && !fp64) return CR_ERR_ARG;
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CR_ERR_NO_DEVICE;
   float ms = 0.f;
@@ -118,7 +145,8 @@ extern "C" int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const double total = (double)sms * 8 * 256 * kChains * (double)iters;
+  double total = (double)sms * 8 * 256 * kChains * (double)iters;
+  if (op == CR_CALIB_DMMA) total = total / 32.0 * 256.0;  // per warp instruction: 8 x 8 x 4 multiply-adds
   *ops_per_s = total / (ms * 1e-3);
   return CR_OK;
 }

@@ -21,7 +21,12 @@
 //  * the first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (set-up, once per device, with that device
 //    current); make that first call before any stream capture.
-#include <cstdio>
+//  * the copies and the kernel run on the legacy default stream with
+//    blocking cudaMemcpy, so a call waits for, and holds up, work on every
+//    blocking stream of the device (streams created without
+//    cudaStreamNonBlocking), and returns once the results are on the host.
+//  * errors return a CR_ERR_* status and set the text of
+//    cr_last_error_detail, as the other entry points do.
 #include <mutex>
 #include <string>
 #include <vector>
@@ -29,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/caracal_gb300.h"
+#include "host_util.h"
 #include "pes_h3.cuh"
 
 namespace {
@@ -61,17 +67,25 @@ __global__ void egrad_h3_noalloc_kernel(int nbeads, double* scratch) {
 // Address of the scratch array on the current device (set-up on first use).
 int scratch_for_current_device(double** out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return CR_ERR_NO_DEVICE;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess)
+    return cr_set_error(CR_ERR_NO_DEVICE, std::string("cr_egrad_h3_noalloc: cudaGetDevice: ") + cudaGetErrorString(err));
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if ((int)g_scratch_addr.size() <= dev) g_scratch_addr.resize((size_t)dev + 1, nullptr);
   if (!g_scratch_addr[(size_t)dev]) {
     double* ptr = nullptr;
-    cudaError_t err = cudaGetSymbolAddress((void**)&ptr, g_egrad_noalloc_scratch);
-    if (err != cudaSuccess || !ptr) return CR_ERR_CUDA;
+    err = cudaGetSymbolAddress((void**)&ptr, g_egrad_noalloc_scratch);
+    if (err != cudaSuccess || !ptr)
+      return cr_set_error(CR_ERR_CUDA, std::string("cr_egrad_h3_noalloc: cudaGetSymbolAddress: ") +
+                                           cudaGetErrorString(err));
     g_scratch_addr[(size_t)dev] = ptr;
   }
   *out = g_scratch_addr[(size_t)dev];
   return CR_OK;
+}
+
+int cuda_fail(const char* what, cudaError_t err) {
+  return cr_set_error(CR_ERR_CUDA, std::string("cr_egrad_h3_noalloc: ") + what + ": " + cudaGetErrorString(err));
 }
 
 }  // namespace
@@ -79,16 +93,17 @@ int scratch_for_current_device(double** out) {
 extern "C" int cr_egrad_h3_noalloc(const double* q, int natoms, int nbeads, double* V, double* dVdq,
                                    int* info) {
   if (info) *info = 0;
-  if (natoms != 3) return CR_ERR_ARG;
-  if (nbeads < 0 || (nbeads > 0 && (!q || !V || !dVdq))) return CR_ERR_ARG;
-  if (nbeads > kNoAllocMaxBeads) {
-    std::fprintf(stderr, "cr_egrad_h3_noalloc: %d beads exceed the fixed maximum of %d per call\n",
-                 nbeads, kNoAllocMaxBeads);
-    return CR_ERR_ARG;
-  }
+  if (natoms != 3) return cr_set_error(CR_ERR_ARG, "cr_egrad_h3_noalloc: natoms must be 3");
+  if (nbeads < 0 || (nbeads > 0 && (!q || !V || !dVdq)))
+    return cr_set_error(CR_ERR_ARG, "cr_egrad_h3_noalloc: negative bead count or NULL array");
+  if (nbeads > kNoAllocMaxBeads)
+    return cr_set_error(CR_ERR_ARG, "cr_egrad_h3_noalloc: " + std::to_string(nbeads) +
+                                        " beads exceed the fixed maximum of " + std::to_string(kNoAllocMaxBeads) +
+                                        " per call");
   if (nbeads == 0) return CR_OK;
   int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CR_ERR_NO_DEVICE;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return cr_set_error(CR_ERR_NO_DEVICE, "cr_egrad_h3_noalloc: no CUDA device");
   double* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc) return rc;
@@ -96,12 +111,14 @@ extern "C" int cr_egrad_h3_noalloc(const double* q, int natoms, int nbeads, doub
   double* d_g = scratch + (size_t)kNoAllocMaxBeads * kQ;
   double* d_V = scratch + (size_t)kNoAllocMaxBeads * 2 * kQ;
   const size_t nq = (size_t)kQ * nbeads;
-  if (cudaMemcpy(d_q, q, nq * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) return CR_ERR_CUDA;
+  cudaError_t err = cudaMemcpy(d_q, q, nq * sizeof(double), cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) return cuda_fail("copy of q", err);
   const int bs = 128;
   egrad_h3_noalloc_kernel<<<(nbeads + bs - 1) / bs, bs>>>(nbeads, scratch);
-  if (cudaGetLastError() != cudaSuccess) return CR_ERR_CUDA;
-  if (cudaMemcpy(V, d_V, (size_t)nbeads * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
-      cudaMemcpy(dVdq, d_g, nq * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return CR_ERR_CUDA;
+  if ((err = cudaGetLastError()) != cudaSuccess) return cuda_fail("kernel launch", err);
+  if ((err = cudaMemcpy(V, d_V, (size_t)nbeads * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_fail("copy of V", err);
+  if ((err = cudaMemcpy(dVdq, d_g, nq * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_fail("copy of dVdq", err);
   return CR_OK;
 }

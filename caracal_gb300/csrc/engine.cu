@@ -76,10 +76,11 @@ __global__ void init_positions_kernel(int T, int P, uint32_t seed, uint32_t traj
   for (int c = 0; c < NC; ++c) q[(size_t)idx * NC + c] = q0[c] + sigma * z[c];
 }
 
-// mdinit Andersen draw: p = sqrt(m P / beta) N(0,1) (tag TAG_INIT_MOMENTA)
+// mdinit Andersen draw: p = sqrt(m P / beta) N(0,1) (tag TAG_INIT_MOMENTA,
+// counter `draw`: 0 for the first mdinit of a run, then one per later call)
 template <int NC>
 __global__ void init_momenta_kernel(int T, int P, uint32_t seed, uint32_t traj0, StepParams prm,
-                                    int zero, double* p) {
+                                    int zero, uint32_t draw, double* p) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= T * P) return;
   int t = idx / P, k = idx % P;
@@ -89,7 +90,7 @@ __global__ void init_momenta_kernel(int T, int P, uint32_t seed, uint32_t traj0,
     return;
   }
   double z[NC];
-  normals_bead<NC>(seed, traj0 + t, (uint32_t)k, 0u, TAG_INIT_MOMENTA, z);
+  normals_bead<NC>(seed, traj0 + t, (uint32_t)k, draw, TAG_INIT_MOMENTA, z);
 #pragma unroll
   for (int c = 0; c < NC; ++c) p[(size_t)idx * NC + c] = z[c] * prm.sigma[c / 3];
 }
@@ -204,6 +205,7 @@ struct cr_engine {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double *d_q = nullptr, *d_p = nullptr, *d_f = nullptr, *d_epot = nullptr, *d_V = nullptr;
   double *d_pile = nullptr, *d_q0 = nullptr;
+  double* d_circ = nullptr;  // [3][P] circulant propagator rows (nm_mode 1)
   int* d_status = nullptr;
   // recrossing children
   int xi_on = 0, side_cap = 0, side_step0 = 0;
@@ -233,7 +235,8 @@ struct cr_engine {
   bool split_ready = false;  // split_prepare done
   // umbrella windows (graph path, analytic surfaces)
   double *d_umb = nullptr;   // [T] centres, [T] force constants, [T] xsum, [T] xsum2, [T][nbins] histogram
-  int* d_umb_flag = nullptr; // sampling switch
+  int* d_umb_flag = nullptr; // [2]: sampling switch, constant 0
+  int umb_sampling = 0;      // host copy of the sampling switch
   double* d_fdrift = nullptr;  // split_drift_fast_kernel table (SplitParams::fdrift)
   int fast_M = 0;              // P / 2 when the drift runs by fast cosine transforms, else 0
   double *d_fsum = nullptr, *d_fmove = nullptr;  // split finish scratch (SplitParams::fsum, fmove)
@@ -289,6 +292,24 @@ double kentry(const std::vector<double>& C, const std::vector<double>& D, int P,
 // Parity-split propagator blocks (both step paths): for even P, Ke[w][r][l]
 // (even modes, l < nu) and Ko[w][r][l] (odd modes, l < nv), r < nr; for odd P
 // the unique rows of K (nr = nu = P/2+1, nv = 0).
+// Orthonormal normal modes (nm_mode 1): K_w = O^T diag(D_w) O is circulant,
+// K_w[j][l] = circ[w][(j - l) mod P] = (1/P) sum_k D_w[k] cos(2 pi k (j - l) / P)
+// with Caracal's per-mode coefficients D (mode k and P - k share a frequency).
+void build_circulant(int P, double beta, double dt, std::vector<double>& circ) {
+  std::vector<double> C, diag[3];
+  mode_tables(P, beta, dt, C, diag);
+  circ.assign((size_t)3 * P, 0.0);
+  for (int w = 0; w < 3; ++w)
+    for (int d = 0; d < P; ++d) {
+      double acc = 0.0;
+      for (int k = 0; k < P; ++k) {
+        const long long m = ((long long)k * d) % P;
+        acc += diag[w][(size_t)k] * std::cos(2.0 * kPi * (double)m / P);
+      }
+      circ[(size_t)w * P + d] = acc / P;
+    }
+}
+
 void build_split_propagator(int P, double beta, double dt, const cr::PropDims& d, std::vector<double>& ke,
                             std::vector<double>& ko) {
   std::vector<double> C, diag[3];
@@ -893,6 +914,7 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_wat
     return fail(CR_ERR_ARG, "unknown thermostat");
   if (cfg->precision != CR_PREC_FP64 && cfg->precision != CR_PREC_MIXED)
     return fail(CR_ERR_ARG, "unknown precision");
+  if (cfg->nm_mode != 0 && cfg->nm_mode != 1) return fail(CR_ERR_ARG, "nm_mode must be 0 or 1");
   // P > 1 needs a finite beta for the free ring-polymer frequencies.  Caracal's
   // dynamic.x in NVE sets kelvin = 0 (src/dynamic.f90:338), making beta = +Inf
   // and the P > 1 propagator 0/0; the engine refuses that instead.
@@ -955,12 +977,16 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_wat
   build_split_propagator(e->P, cfg->beta, cfg->dt, pd, ke, ko);
   if (cfg->thermostat == CR_THERMO_PILE) build_pile(e->P, cfg->beta, cfg->dt, cfg->pile_tau0, pile);
   else pile.assign((size_t)2 * e->P, 0.0);
+  std::vector<double> circ;
+  if (cfg->nm_mode == 1) build_circulant(e->P, cfg->beta, cfg->dt, circ);
+  else circ.assign((size_t)3 * e->P, 0.0);
   if (cudaMalloc(&e->d_ke, ke.size() * 8) != cudaSuccess || cudaMalloc(&e->d_ko, ko.size() * 8) != cudaSuccess ||
-      cudaMalloc(&e->d_pile, pile.size() * 8) != cudaSuccess)
+      cudaMalloc(&e->d_pile, pile.size() * 8) != cudaSuccess || cudaMalloc(&e->d_circ, circ.size() * 8) != cudaSuccess)
     return cleanup_fail(fail(CR_ERR_CUDA, "device allocation of the tables failed"));
   if (cudaMemcpyAsync(e->d_ke, ke.data(), ke.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
       cudaMemcpyAsync(e->d_ko, ko.data(), ko.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
       cudaMemcpyAsync(e->d_pile, pile.data(), pile.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(e->d_circ, circ.data(), circ.size() * 8, cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return cleanup_fail(fail(CR_ERR_CUDA, "upload of the tables failed"));
 
@@ -1020,7 +1046,8 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_wat
     // the free ring polymer by fast cosine transforms where P is 8..64, a
     // power of two, and no PILE half step runs inside the drift
     const int P = e->P;
-    if (pd.split && P >= 8 && P <= 64 && (P & (P - 1)) == 0 && cfg->thermostat != CR_THERMO_PILE) {
+    if (pd.split && P >= 8 && P <= 64 && (P & (P - 1)) == 0 && cfg->thermostat != CR_THERMO_PILE &&
+        cfg->nm_mode == 0) {
       std::vector<double> tab;
       build_fast_drift(P, cfg->beta, cfg->dt, tab);
       if (cudaMalloc(&e->d_fdrift, tab.size() * 8) != cudaSuccess ||
@@ -1032,6 +1059,8 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_wat
     s.P = e->P;
     s.N = N;
     s.NC = e->NC;
+    s.nm_mode = cfg->nm_mode;
+    s.circ = e->d_circ;
     s.thermostat = cfg->thermostat;
     s.andersen_step = cfg->andersen_step > 0 ? cfg->andersen_step : 1;
     s.transrot = cfg->transrot ? 1 : 0;
@@ -1098,6 +1127,10 @@ static int engine_create(const cr_config* cfg, cr_qmdff* ff, cr_evb* evb, cr_wat
   s.nhc = nhc;
   s.vnh = e->d_vnh;
   s.pd = pd;
+  s.pow2_P = (e->P & (e->P - 1)) == 0 ? 1 : 0;
+  s.inv_P = 1.0 / e->P;
+  s.nm_mode = cfg->nm_mode;
+  s.circ = e->d_circ;
   s.ke = e->d_ke;
   s.ko = e->d_ko;
   s.pile = e->d_pile;
@@ -1150,6 +1183,7 @@ int cr_engine_destroy(cr_engine* e) {
   cudaFree(e->d_sigma);
   cudaFree(e->d_ke);
   cudaFree(e->d_ko);
+  cudaFree(e->d_circ);
   cudaFree(e->d_istep);
   cudaFree(e->d_vnh);
   cudaFree(e->d_V2);
@@ -1222,8 +1256,8 @@ int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
   return CR_OK;
 }
 
-int cr_engine_init_momenta(cr_engine* e, int zero) {
-  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+// Momenta of mdinit with Gaussian stream `draw` (see init_momenta_kernel).
+static int init_momenta_draw(cr_engine* e, int zero, uint32_t draw) {
   if (!zero && !(e->cfg.beta > 0.0 && std::isfinite(e->cfg.beta)))
     return fail(CR_ERR_ARG, "Andersen momenta need a finite temperature");
   // mdinit also starts the Nose-Hoover chain at rest (src/mdinit.f90:140-145)
@@ -1232,31 +1266,37 @@ int cr_engine_init_momenta(cr_engine* e, int zero) {
   if (e->split) {
     const long long n = (long long)nb * ((e->NC + 1) / 2);
     cr::split_init_momenta_kernel<<<(unsigned)((n + 127) / 128), 128, 0, e->stream>>>(
-        e->T, e->P, e->NC, e->cfg.seed, e->cfg.traj0, e->d_sigma, zero, e->d_p);
+        e->T, e->P, e->NC, e->cfg.seed, e->cfg.traj0, e->d_sigma, zero, draw, e->d_p);
     CR_CUDA(cudaGetLastError());
-    CR_CUDA(cudaStreamSynchronize(e->stream));
     return CR_OK;
   }
   switch (e->cfg.pes) {
     case CR_PES_H3:
       cr::init_momenta_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
-          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, draw, e->d_p);
       break;
     case CR_PES_CH4H:
       cr::init_momenta_kernel<18><<<(nb + 127) / 128, 128, 0, e->stream>>>(
-          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, draw, e->d_p);
       break;
     case CR_PES_CH4OH:
       cr::init_momenta_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
-          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, draw, e->d_p);
       break;
     case CR_PES_OH3:
       cr::init_momenta_kernel<12><<<(nb + 127) / 128, 128, 0, e->stream>>>(
-          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, e->d_p);
+          e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, draw, e->d_p);
       break;
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
   CR_CUDA(cudaGetLastError());
+  return CR_OK;
+}
+
+int cr_engine_init_momenta(cr_engine* e, int zero) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  int rc = init_momenta_draw(e, zero, 0u);
+  if (rc) return rc;
   CR_CUDA(cudaStreamSynchronize(e->stream));
   return CR_OK;
 }
@@ -1494,6 +1534,17 @@ int cr_host_free(void* ptr) {
   return CR_OK;
 }
 
+int cr_host_register(void* ptr, unsigned long long bytes) {
+  if (!ptr || bytes == 0) return fail(CR_ERR_ARG, "NULL pointer or zero size");
+  CR_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+  return CR_OK;
+}
+
+int cr_host_unregister(void* ptr) {
+  if (ptr) CR_CUDA(cudaHostUnregister(ptr));
+  return CR_OK;
+}
+
 }  // extern "C"
 
 // BIMOLEC reaction coordinate of a cr_recross definition (1-based atoms).
@@ -1526,6 +1577,10 @@ static int make_xidev(const cr_engine* e, const cr_recross* rc, cr::XiDev& x) {
   x.break_ref = rc->break_ref;
   x.r_inf = rc->r_inf;
   x.xi_ideal = rc->xi_ideal;
+  for (int k = 0; k < 8; ++k) {
+    x.w1[k] = k < x.nreac1 ? e->mass[(size_t)x.reac1[k]] / x.mreac1 : 0.0;
+    x.w2[k] = k < x.nreac2 ? e->mass[(size_t)x.reac2[k]] / x.mreac2 : 0.0;
+  }
   return CR_OK;
 }
 
@@ -1581,11 +1636,13 @@ int cr_engine_set_umbrella(cr_engine* e, const cr_recross* rc, const double* cen
   cudaFree(e->d_umb);
   e->d_umb = nullptr;
   CR_CUDA(cudaMalloc(&e->d_umb, (4 * T + nh + 1) * sizeof(double)));
-  if (!e->d_umb_flag) CR_CUDA(cudaMalloc(&e->d_umb_flag, sizeof(int)));
+  // [0] the sampling switch, [1] always 0 (the switch mdinit's bias reads)
+  if (!e->d_umb_flag) CR_CUDA(cudaMalloc(&e->d_umb_flag, 2 * sizeof(int)));
   CR_CUDA(cudaMemcpy(e->d_umb, centers, T * 8, cudaMemcpyHostToDevice));
   CR_CUDA(cudaMemcpy(e->d_umb + T, kforce, T * 8, cudaMemcpyHostToDevice));
   CR_CUDA(cudaMemset(e->d_umb + 2 * T, 0, (2 * T + nh) * 8));
-  CR_CUDA(cudaMemset(e->d_umb_flag, 0, sizeof(int)));
+  CR_CUDA(cudaMemset(e->d_umb_flag, 0, 2 * sizeof(int)));
+  e->umb_sampling = 0;
   cr::UmbrellaDev u{};
   u.center = e->d_umb;
   u.kforce = e->d_umb + T;
@@ -1617,6 +1674,55 @@ int cr_engine_umbrella_sampling(cr_engine* e, int on) {
   const int v = on ? 1 : 0;
   CR_CUDA(cudaStreamSynchronize(e->stream));
   CR_CUDA(cudaMemcpy(e->d_umb_flag, &v, sizeof(int), cudaMemcpyHostToDevice));
+  e->umb_sampling = v;
+  return CR_OK;
+}
+
+// Drops the captured step graph (it holds the step parameters by value).
+static void drop_graph(cr_engine* e) {
+  if (e->graph_exec) {
+    cudaGraphExecDestroy(e->graph_exec);
+    e->graph_exec = nullptr;
+  }
+  if (e->graph) {
+    cudaGraphDestroy(e->graph);
+    e->graph = nullptr;
+  }
+}
+
+int cr_engine_set_andersen_step(cr_engine* e, int andersen_step) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (andersen_step < 1) return fail(CR_ERR_ARG, "andersen_step must be >= 1");
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  e->cfg.andersen_step = andersen_step;
+  e->prm.andersen_step = andersen_step;
+  e->sp.andersen_step = andersen_step;
+  drop_graph(e);
+  return CR_OK;
+}
+
+int cr_engine_mdinit(cr_engine* e, unsigned draw) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  const bool umb = e->split && e->sp.umbrella;
+  if (umb && e->umb_sampling) return fail(CR_ERR_ARG, "switch umbrella sampling off before mdinit");
+  int rc = dispatch_forces(e);
+  if (rc) return rc;
+  if (umb) {  // src/mdinit.f90:96-100: umbrella(..., mode 0) on the initial forces
+    cr::SplitParams s = e->sp;
+    s.umb.sampling = e->d_umb_flag + 1;
+    switch (e->N) {
+      case 3: cr::split_umbrella_kernel<3><<<e->T, 64, 0, e->stream>>>(s); break;
+      case 6: cr::split_umbrella_kernel<6><<<e->T, 64, 0, e->stream>>>(s); break;
+      case 7: cr::split_umbrella_kernel<7><<<e->T, 64, 0, e->stream>>>(s); break;
+      case 4: cr::split_umbrella_kernel<4><<<e->T, 64, 0, e->stream>>>(s); break;
+      default: return fail(CR_ERR_UNSUPPORTED, "umbrella windows are built for the analytic surfaces");
+    }
+    CR_CUDA(cudaGetLastError());
+  }
+  // NVT: Andersen draw (src/mdinit.f90:118-121); NVE: zero momenta (:125)
+  const int nve = e->cfg.thermostat == CR_THERMO_NONE;
+  if ((rc = init_momenta_draw(e, nve, (uint32_t)draw))) return rc;
+  CR_CUDA(cudaStreamSynchronize(e->stream));
   return CR_OK;
 }
 

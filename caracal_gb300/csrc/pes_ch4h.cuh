@@ -26,6 +26,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
+#include "ff32.cuh"
+
 namespace cr {
 namespace ch4h {
 
@@ -92,13 +96,43 @@ __device__ inline void egrad(const double (&qb)[18], double& Vout, double (&gout
 #pragma unroll
   for (int x = 0; x < 18; ++x) qa[x] = qb[x] * 0.52918;
   Geo<F> G;
+  // mixed form: every position as a float pair (hi + lo = the FP64 value to
+  // ~2^-48), displacements and the stretch distances as float pairs; the
+  // FP32 geometry is their rounding (the same FP64-pipe cost as rounding
+  // FP64 differences)
+  constexpr bool kPair = std::is_same<F, float>::value;
+  ff Xtcb[3], Xtch[4][3], Xtbh[4][3], Xrch[4];
+  if constexpr (kPair) {
+    ff X[18];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    G.tcb[d] = (F)(qa[3 * NC + d] - qa[3 * NB + d]);
+    for (int x = 0; x < 18; ++x) {
+      const float h = __double2float_rn(qa[x]);
+      X[x] = ff{h, __double2float_rn(qa[x] - (double)h)};
+    }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      G.tch[i][d] = (F)(qa[3 * NC + d] - qa[3 * NH(i) + d]);
-      G.tbh[i][d] = (F)(qa[3 * NB + d] - qa[3 * NH(i) + d]);
+    for (int d = 0; d < 3; ++d) {
+      Xtcb[d] = X[3 * NC + d] - X[3 * NB + d];
+      G.tcb[d] = ff_float(Xtcb[d]);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        Xtch[i][d] = X[3 * NC + d] - X[3 * NH(i) + d];
+        Xtbh[i][d] = X[3 * NB + d] - X[3 * NH(i) + d];
+        G.tch[i][d] = ff_float(Xtch[i][d]);
+        G.tbh[i][d] = ff_float(Xtbh[i][d]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      Xrch[i] = ff_sqrt(Xtch[i][0] * Xtch[i][0] + Xtch[i][1] * Xtch[i][1] + Xtch[i][2] * Xtch[i][2]);
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      G.tcb[d] = (F)(qa[3 * NC + d] - qa[3 * NB + d]);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        G.tch[i][d] = (F)(qa[3 * NC + d] - qa[3 * NH(i) + d]);
+        G.tbh[i][d] = (F)(qa[3 * NB + d] - qa[3 * NH(i) + d]);
+      }
     }
   }
   G.rcb = t_sqrt<F>(G.tcb[0] * G.tcb[0] + G.tcb[1] * G.tcb[1] + G.tcb[2] * G.tcb[2]);
@@ -115,6 +149,11 @@ __device__ inline void egrad(const double (&qb)[18], double& Vout, double (&gout
   F pdot[18];
 #pragma unroll
   for (int x = 0; x < 18; ++x) pdot[x] = F(0);
+  // mixed form: the stretch gradient, summed as float pairs (its terms are
+  // large and cancel on each atom); the bends add into pdot in FP32
+  ff psx[kPair ? 18 : 1];
+#pragma unroll
+  for (int x = 0; x < (kPair ? 18 : 1); ++x) psx[x] = ff{0.f, 0.f};
 
   // ---- switching functions (switchf_ch4h)
   F s1[4], ds1[4], s2[4], ds2[4], s3[4], ds3[4], sphi[4], dsphi[4], sth[4], dsth[4];
@@ -155,6 +194,7 @@ __device__ inline void egrad(const double (&qb)[18], double& Vout, double (&gout
   const double pi = 3.141592653589793;
   const F A = F(tau - 0.5 * pi), B = F(tau - 2.0 * pi / 3.0);
   F th0[4][4], dth0[4][4][4];
+  F th0m[4][4];  // th0 - tau, without the rounding of tau (the mixed form's bend differences)
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -175,9 +215,12 @@ __device__ inline void egrad(const double (&qb)[18], double& Vout, double (&gout
           if (m < 0) m = k;
           else n = k;
         }
-      F t = F(tau) + A * (sphi[i] * sphi[j] - F(1)) + B * (sth[m] * sth[n] - F(1));
+      const F tm = A * (sphi[i] * sphi[j] - F(1)) + B * (sth[m] * sth[n] - F(1));
+      F t = F(tau) + tm;
       th0[i][j] = t;
       th0[j][i] = t;
+      th0m[i][j] = tm;
+      th0m[j][i] = tm;
       F di = A * dsphi[i] * sphi[j], dj = A * sphi[i] * dsphi[j];
       F dm = B * dsth[m] * sth[n], dn = B * sth[m] * dsth[n];
       dth0[i][j][i] = di; dth0[j][i][i] = di;
@@ -188,6 +231,93 @@ __device__ inline void egrad(const double (&qb)[18], double& Vout, double (&gout
 
   // ---- stretching (stretch_ch4h)
   F vstr = F(0);
+  if constexpr (kPair) {
+    // Mixed form.  Per C-H bond i the LEPS gradient collapses onto three
+    // scalars: T_i (along the C-H_i stretch, Q and exchange terms together),
+    // U_i (C-H_b) and W_i (H_b-H_i).  T_i is a small difference of large Q
+    // and J derivatives near the bond minimum, so the scalars are formed in
+    // float-pair arithmetic (distances, exponentials, the LEPS root) and
+    // rounded once; the vectors they multiply are the FP32 geometry.
+    const F rav = (G.rch[0] + G.rch[1] + G.rch[2] + G.rch[3]) * F(0.25);
+    const F arga = F(c1ch) * (rav - F(r0ch));
+    F ach, dumach;
+    if (arga < F(19.0)) {
+      ach = F(a1ch) + F(b1ch) * (t_tanh<F>(arga) + F(1)) * F(0.5);
+      const F ch = t_cosh<F>(arga);
+      dumach = F(b1ch * c1ch) / (F(2) * (ch * ch));
+    } else {
+      ach = F(a1ch + b1ch);
+      dumach = F(0);
+    }
+    constexpr ff D1ch = ff_const(d1ch), D3ch = ff_const(d3ch), D1hh = ff_const(d1hh), D3hh = ff_const(d3hh);
+    constexpr ff D1cb = ff_const(d1cb), D3cb = ff_const(d3cb);
+    constexpr ff Sqch = ff_const(d1ch + d3ch), Dfch = ff_const(d1ch - d3ch);
+    constexpr ff Sqhh = ff_const(d1hh + d3hh), Dfhh = ff_const(d1hh - d3hh);
+    constexpr ff Sqcb = ff_const(d1cb + d3cb), Dfcb = ff_const(d1cb - d3cb);
+    constexpr ff R0ch = ff_const(r0ch), R0hh = ff_const(r0hh), R0cb = ff_const(r0cb);
+    constexpr ff Acb = ff_const(acb), Ahh = ff_const(ahh);
+    auto norm3 = [](const ff (&v)[3]) { return ff_sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+    const ff rcb = norm3(Xtcb);
+    const ff ecb1 = ff_exp(-(Acb * (rcb - R0cb))), ecb2 = ecb1 * ecb1;
+    const ff vqcb = (D1cb * (ecb2 - ecb1 * 2.f) + D3cb * (ecb2 + ecb1 * 2.f)) * 0.5f;
+    const ff vjcb = (D1cb * (ecb2 - ecb1 * 2.f) - D3cb * (ecb2 + ecb1 * 2.f)) * 0.5f;
+    const ff dqcb = -(Acb * (Sqcb * ecb2 - Dfcb * ecb1));  // d vqcb / d rcb
+    const ff djcb = -(Acb * (Dfcb * ecb2 - Sqcb * ecb1));  // d vjcb / d rcb
+    // ach = a1 + b1 (tanh(arga) + 1) / 2 = a1 + b1 / (1 + exp(-2 arga)) as a
+    // float pair: its rounding enters every exponent -ach xch of the
+    // cancelling Q and J derivatives
+    ff achx = ff_const(a1ch + b1ch);
+    if (arga < F(19.0)) {
+      constexpr ff A1 = ff_const(a1ch), B1 = ff_const(b1ch), C1 = ff_const(c1ch);
+      const ff ravx = (Xrch[0] + Xrch[1] + Xrch[2] + Xrch[3]) * 0.25f;
+      const ff e2 = ff_exp(-(C1 * (ravx - R0ch)) * 2.f);
+      achx = A1 + B1 / (ff_from(1.f) + e2);
+    }
+    ach = ff_float(achx);
+    ff vsum = ff_from(0.f);
+    F achdc[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) achdc[d] = dumach * (G.uch[0][d] + G.uch[1][d] + G.uch[2][d] + G.uch[3][d]) * F(0.25);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const ff rch = Xrch[i], rbh = norm3(Xtbh[i]);
+      const ff xch = rch - R0ch;
+      const ff ec1 = ff_exp(-(achx * xch)), ec2 = ec1 * ec1;
+      const ff vqch = (D1ch * (ec2 - ec1 * 2.f) + D3ch * (ec2 + ec1 * 2.f)) * 0.5f;
+      const ff vjch = (D1ch * (ec2 - ec1 * 2.f) - D3ch * (ec2 + ec1 * 2.f)) * 0.5f;
+      const ff eh1 = ff_exp(-(Ahh * (rbh - R0hh))), eh2 = eh1 * eh1;
+      const ff vqbh = (D1hh * (eh2 - eh1 * 2.f) + D3hh * (eh2 + eh1 * 2.f)) * 0.5f;
+      const ff vjbh = (D1hh * (eh2 - eh1 * 2.f) - D3hh * (eh2 + eh1 * 2.f)) * 0.5f;
+      const ff e12 = vjch - vjcb, e23 = vjcb - vjbh, e31 = vjbh - vjch;
+      const ff vj = -ff_sqrt((e12 * e12 + e23 * e23 + e31 * e31) * 0.5f);
+      vsum += vqch + vqcb + vqbh + vj;
+      const ff factj = ff_recip(vj) * 0.5f;  // d vj / d J_k = (its two differences) * 0.5 / vj
+      const ff brq = Sqch * ec2 - Dfch * ec1, brj = Dfch * ec2 - Sqch * ec1;
+      const ff dqbh = -(Ahh * (Sqhh * eh2 - Dfhh * eh1)), djbh = -(Ahh * (Dfhh * eh2 - Sqhh * eh1));
+      // T: -(d V / d (ach * xch)); U: d V / d rcb (per unit rcb); W: d V / d rbh
+      const ff T = brq + (e12 - e31) * factj * brj;
+      const ff U = (-dqcb + (e12 - e23) * factj * djcb) / rcb;
+      const ff W = (dqbh + (e31 - e23) * factj * djbh) / rbh;
+      const ff irch = ff_recip(rch);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const ff u = Xtch[i][d] * irch;
+        const ff tcb = Xtcb[d], tbh = Xtbh[i][d];
+        const ff gc = achx * u + xch * achdc[d];
+        const ff gh = achx * u + xch * (dumach * G.uch[i][d] * F(0.25));
+        psx[3 * NC + d] -= gc * T + tcb * U;
+        psx[3 * NH(i) + d] += gh * T - tbh * W;
+        psx[3 * NB + d] += tcb * U + tbh * W;
+        const ff xT = xch * T;
+#pragma unroll
+        for (int k = 1; k <= 3; ++k) {
+          const int j = (i + k) & 3;
+          psx[3 * NH(j) + d] += xT * (dumach * G.uch[j][d] * F(0.25));
+        }
+      }
+    }
+    vstr = ff_float(vsum);
+  } else
   {
     F rav = (G.rch[0] + G.rch[1] + G.rch[2] + G.rch[3]) * F(0.25);
     F arga = F(c1ch) * (rav - F(r0ch));
@@ -413,8 +543,23 @@ __device__ inline void egrad(const double (&qb)[18], double& Vout, double (&gout
         dfk0[m] = g0 * ds2[m] * s2[n];
         dfk0[n] = g0 * s2[m] * ds2[n];
         const F kf = fk0 * f1[i] * f1[j];
-        F costh = (G.uch[i][0] * G.uch[j][0] + G.uch[i][1] * G.uch[j][1] + G.uch[i][2] * G.uch[j][2]);
-        F dth = t_acos<F>(costh) - th0[i][j];
+        F costh, dth;
+        if constexpr (kPair) {
+          // theta - tau as asin(sin(theta - tau)) from a float-pair cosine:
+          // theta - th0 is a small difference of two ~1.9 rad angles, which
+          // acosf of an FP32 cosine would leave with ~1e-7 rad of error
+          const ff c = (Xtch[i][0] * Xtch[j][0] + Xtch[i][1] * Xtch[j][1] + Xtch[i][2] * Xtch[j][2]) /
+                       (Xrch[i] * Xrch[j]);
+          constexpr ff kCosTau = ff_const(-1.0 / 3.0), kSinTau = ff_const(0.94280904158206336587);
+          const ff y = ff_sqrt(ff_from(1.f) - c * c) * kCosTau - c * kSinTau;
+          costh = ff_float(c);
+          const float dtau = fabsf(y.hi) < 0.9f ? asinf(y.hi) + y.lo / sqrtf(1.f - y.hi * y.hi)
+                                                : acosf(costh) - F(tau);
+          dth = dtau - th0m[i][j];
+        } else {
+          costh = (G.uch[i][0] * G.uch[j][0] + G.uch[i][1] * G.uch[j][1] + G.uch[i][2] * G.uch[j][2]);
+          dth = t_acos<F>(costh) - th0[i][j];
+        }
         vip += F(0.5) * kf * dth * dth;
         const F termth = F(-1) / t_sqrt<F>(F(1) - costh * costh);
         const F half_d2 = F(0.5) * dth * dth;
@@ -445,6 +590,10 @@ __device__ inline void egrad(const double (&qb)[18], double& Vout, double (&gout
   }
 
   Vout = (double)((vstr + vop + vip) * F(0.03812));
+  if constexpr (kPair) {
+#pragma unroll
+    for (int x = 0; x < 18; ++x) pdot[x] = ff_float(psx[x] + pdot[x]);
+  }
 #pragma unroll
   for (int x = 0; x < 18; ++x) gout[x] = (double)pdot[x] * 0.0201723;
 }

@@ -245,14 +245,81 @@ const QmdffKernel kKernels[2][kVariants] = {
 constexpr int kDefaultVariant = 1;
 constexpr int kTuneMinBeads = 2048;  // smaller batches keep the default
 
-int launch_variant(const cr_qmdff* ff, int prec, int v, const double* d_q, int nbeads, double* d_e, double* d_g,
-                   cudaStream_t s) {
-  const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(ff->n);
+int launch_dev(const cr::qmdff::Dev& D, int prec, int v, const double* d_q, int nbeads, double* d_e, double* d_g,
+               cudaStream_t s) {
+  const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(D.n);
   int grid = (nbeads + kQmdffWarps - 1) / kQmdffWarps;
   if (grid > 1 << 20) grid = 1 << 20;
-  kKernels[prec][v]<<<grid, kQmdffWarps * 32, smem, s>>>(ff->dev, nbeads, d_q, d_e, d_g);
+  kKernels[prec][v]<<<grid, kQmdffWarps * 32, smem, s>>>(D, nbeads, d_q, d_e, d_g);
   CR_TRY_CUDA(cudaGetLastError());
   return CR_OK;
+}
+
+int launch_variant(const cr_qmdff* ff, int prec, int v, const double* d_q, int nbeads, double* d_e, double* d_g,
+                   cudaStream_t s) {
+  return launch_dev(ff->dev, prec, v, d_q, nbeads, d_e, d_g, s);
+}
+
+// The force kernel over a subset of the term kinds (bit k of mask: kind k =
+// bonds, angles, torsions, NCI pairs, H/halogen bonds), with or without
+// E_zero: the pieces of Caracal's QMDFF call site (src/gradient.f90:341-358).
+// The masked kinds' batch counts are set to zero in a copy of the schedule.
+int qmdff_launch_kinds(const cr_qmdff* ff, unsigned mask, bool ezero, const double* d_q, int nbeads, double* d_e,
+                       double* d_g, int precision, cudaStream_t s) {
+  if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
+  const int prec = precision == CR_PREC_MIXED ? 1 : 0;
+  const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(ff->n);
+  if (smem > 48 * 1024)
+    for (int v = 0; v < kVariants; ++v)
+      CR_TRY_CUDA(cudaFuncSetAttribute(kKernels[prec][v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nbeads <= 0) return CR_OK;
+  cr::qmdff::Dev D = ff->dev;
+  for (int p = 0; p < 2; ++p)
+    for (int k = 0; k < cr::qmdff::kKinds; ++k)
+      if (!((mask >> k) & 1u)) D.sched[p].nb[k] = 0;
+  if (!ezero) D.e_zero = 0.0;
+  const int v = ff->variant[prec] >= 0 ? ff->variant[prec] : kDefaultVariant;
+  return launch_dev(D, prec, v, d_q, nbeads, d_e, d_g, s);
+}
+
+// Host-array call of a kind subset: e, g overwritten, or accumulated into.
+int qmdff_host_kinds(cr_qmdff* ff, unsigned mask, bool ezero, bool accumulate, const double* xyz, int nbeads,
+                     double* e, double* g, int precision) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (nbeads < 0 || (nbeads > 0 && (!xyz || !e || !g))) return cr_set_error(CR_ERR_ARG, "bad egrad arguments");
+  if (nbeads == 0) return CR_OK;
+  const size_t nq = (size_t)3 * ff->n * nbeads;
+  double *d_q = nullptr, *d_e = nullptr, *d_g = nullptr;
+  CR_TRY_CUDA(cudaMalloc(&d_q, nq * sizeof(double)));
+  cudaError_t e1 = cudaMalloc(&d_e, (size_t)nbeads * sizeof(double));
+  cudaError_t e2 = cudaMalloc(&d_g, nq * sizeof(double));
+  std::vector<double> pe, pg;
+  int rc = CR_OK;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    rc = cr_set_error(CR_ERR_CUDA, "cudaMalloc failed in the QMDFF term call");
+  } else if (cudaMemcpy(d_q, xyz, nq * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = cr_set_error(CR_ERR_CUDA, "copy of xyz failed");
+  } else if ((rc = qmdff_launch_kinds(ff, mask, ezero, d_q, nbeads, d_e, d_g, precision, nullptr)) == CR_OK) {
+    double* oe = e;
+    double* og = g;
+    if (accumulate) {
+      pe.resize((size_t)nbeads);
+      pg.resize(nq);
+      oe = pe.data();
+      og = pg.data();
+    }
+    if (cudaMemcpy(oe, d_e, (size_t)nbeads * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(og, d_g, nq * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+      rc = cr_set_error(CR_ERR_CUDA, "copy of results failed");
+    } else if (accumulate) {
+      for (int b = 0; b < nbeads; ++b) e[b] += pe[(size_t)b];
+      for (size_t x = 0; x < nq; ++x) g[x] += pg[x];
+    }
+  }
+  cudaFree(d_q);
+  cudaFree(d_e);
+  cudaFree(d_g);
+  return rc;
 }
 
 }  // namespace
@@ -650,6 +717,18 @@ int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, doubl
   cudaFree(d_e);
   cudaFree(d_g);
   return rc;
+}
+
+int cr_qmdff_eg(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision) {
+  return qmdff_host_kinds(ff, 0x7u, false, false, xyz, nbeads, e, g, precision);
+}
+
+int cr_qmdff_nonb(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision) {
+  return qmdff_host_kinds(ff, 0x8u, false, true, xyz, nbeads, e, g, precision);
+}
+
+int cr_qmdff_hb(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision) {
+  return qmdff_host_kinds(ff, 0x10u, false, true, xyz, nbeads, e, g, precision);
 }
 
 int cr_qmdff_nparams(const cr_qmdff* ff, int* nlin) {

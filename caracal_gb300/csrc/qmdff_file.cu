@@ -40,7 +40,7 @@ struct Records {
 struct FileFF {
   int n = 0, nbond = 0, nangl = 0, ntors = 0, nhb = 0, nnci = 0;
   std::vector<int> at, bond, angl, tors, hb, nci;
-  std::vector<double> q, vbond, vangl, vtors;
+  std::vector<double> q, xyz, vbond, vangl, vtors;  // xyz(3, n): reference geometry, bohr
 };
 
 int parse(const char* path, FileFF& f) {
@@ -59,6 +59,7 @@ int parse(const char* path, FileFF& f) {
   for (int i = 0; i < f.n; ++i) {
     if (!r.read(6, v)) return cr_set_error(CR_ERR_ARG, "truncated atom block");
     f.at.push_back(toi(v[0]));
+    for (int k = 1; k < 4; ++k) f.xyz.push_back(tod(v[(size_t)k]));
     f.q.push_back(tod(v[4]));
   }
   if (!r.read(5, v)) return cr_set_error(CR_ERR_ARG, "missing term counts");
@@ -139,6 +140,58 @@ double scale_xb(int z) {
 }
 double hbpara(double a, double b, double q) { return std::exp(-a * q) / (std::exp(-a * q) + b); }
 
+// Coordination numbers of the reference geometry (src/ncoord_qmdff.f90:36-76):
+// cn_i = sum_j 1 / (1 + exp(-16 ((rcov_i + rcov_j) / r_ij - 1))), pairs with
+// r^2 > cn_thr bohr^2 skipped.
+void ncoord(const FileFF& f, const double* rcov, double cn_thr, std::vector<double>& cn) {
+  const int n = f.n;
+  cn.assign((size_t)n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    double xn = 0.0;
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      const double dx = f.xyz[3 * (size_t)j] - f.xyz[3 * (size_t)i];
+      const double dy = f.xyz[3 * (size_t)j + 1] - f.xyz[3 * (size_t)i + 1];
+      const double dz = f.xyz[3 * (size_t)j + 2] - f.xyz[3 * (size_t)i + 2];
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 > cn_thr) continue;
+      const double r = std::sqrt(r2);
+      const double rr = (rcov[f.at[(size_t)i] - 1] + rcov[f.at[(size_t)j] - 1]) / r;
+      xn = xn + 1.0 / (1.0 + std::exp(-16.0 * (rr - 1.0)));
+    }
+    cn[(size_t)i] = xn;
+  }
+}
+
+// CN-interpolated pair C6 (src/getc6.f90:35-83) from the D3 reference table
+// c6ab(94,94,5,5,3) (column-major, as copyc6 leaves module qmdff).
+double getc6(const cr_d3_reference* d3, int iat, int jat, double nci, double ncj) {
+  auto at5 = [&](int i, int j, int a, int b, int m) {
+    return d3->c6ab[(size_t)(i - 1) + 94 * ((size_t)(j - 1) + 94 * ((size_t)a + 5 * ((size_t)b + 5 * (size_t)m)))];
+  };
+  double c6mem = -1e99, rsum = 0.0, csum = 0.0, r_save = 10000.0;
+  for (int a = 0; a < d3->maxci[iat - 1]; ++a)
+    for (int b = 0; b < d3->maxci[jat - 1]; ++b) {
+      const double c6 = at5(iat, jat, a, b, 0);
+      if (c6 > 0) {
+        const double cn1 = at5(iat, jat, a, b, 1), cn2 = at5(iat, jat, a, b, 2);
+        const double r = (cn1 - nci) * (cn1 - nci) + (cn2 - ncj) * (cn2 - ncj);
+        if (r < r_save) {
+          r_save = r;
+          c6mem = c6;
+        }
+        const double tmp1 = std::exp(-4.0 * r);
+        rsum = rsum + tmp1;
+        csum = csum + tmp1 * c6;
+      }
+    }
+  return rsum > 1e-99 ? csum / rsum : c6mem;
+}
+
+// Common tail of the loaders: H-bond strengths, eps scalings, the device force field.
+int build_from_file(const FileFF& f, const cr_qmdff_tables* tab, const std::vector<double>& c6, double e_zero,
+                    int zahn, double coul_cut, cr_qmdff** out);
+
 }  // namespace
 
 extern "C" {
@@ -171,6 +224,43 @@ int cr_qmdff_load(const char* path, const cr_qmdff_tables* tab, double e_zero, i
   std::vector<double> c6((size_t)n * n);
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) c6[(size_t)i + (size_t)n * j] = tab->c6ab[(size_t)(f.at[i] - 1) + 94 * (size_t)(f.at[j] - 1)];
+  return build_from_file(f, tab, c6, e_zero, zahn, coul_cut, out);
+}
+
+int cr_qmdff_load_d3(const char* path, const cr_qmdff_tables* tab, const cr_d3_reference* d3, double e_zero,
+                     int zahn, double coul_cut, cr_qmdff** out) {
+  if (!path || !tab || !d3 || !out || !tab->rad || !tab->r0ab || !tab->zab || !tab->r0094 || !tab->sr42 ||
+      !d3->c6ab || !d3->maxci || !d3->rcov)
+    return cr_set_error(CR_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  for (int z = 0; z < 94; ++z)
+    if (d3->maxci[z] < 0 || d3->maxci[z] > 5) return cr_set_error(CR_ERR_ARG, "maxci out of 0..5");
+  FileFF f;
+  int rc = parse(path, f);
+  if (rc) return rc;
+  for (int z : f.at)
+    if (z < 1 || z > 94) return cr_set_error(CR_ERR_ARG, "element number out of 1..94");
+  // prepare (src/prepare.f90:121-129): CN of the file's geometry, pair C6
+  std::vector<double> cn;
+  ncoord(f, d3->rcov, 5000.0, cn);
+  const int n = f.n;
+  std::vector<double> c6((size_t)n * n);
+  for (int i1 = 0; i1 < n; ++i1)
+    for (int i2 = 0; i2 <= i1; ++i2) {
+      const double v = getc6(d3, f.at[(size_t)i1], f.at[(size_t)i2], cn[(size_t)i1], cn[(size_t)i2]);
+      c6[(size_t)i2 + (size_t)n * i1] = v;
+      c6[(size_t)i1 + (size_t)n * i2] = v;
+    }
+  return build_from_file(f, tab, c6, e_zero, zahn, coul_cut, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+int build_from_file(const FileFF& f, const cr_qmdff_tables* tab, const std::vector<double>& c6, double e_zero,
+                    int zahn, double coul_cut, cr_qmdff** out) {
+  const int n = f.n;
   std::vector<double> vhb((size_t)2 * f.nhb, 0.0);
   for (int k = 0; k < f.nhb; ++k) {
     const int a = f.hb[(size_t)3 * k] - 1, b = f.hb[(size_t)3 * k + 1] - 1, h = f.hb[(size_t)3 * k + 2] - 1;
@@ -221,4 +311,4 @@ int cr_qmdff_load(const char* path, const cr_qmdff_tables* tab, double e_zero, i
   return cr_qmdff_create(&d, out);
 }
 
-}  // extern "C"
+}  // namespace

@@ -45,6 +45,7 @@ struct XiDev {
   int form0, form1, brk0, brk1;
   double form_ref, break_ref, r_inf, xi_ideal;
   double mreac1, mreac2;
+  double w1[8], w2[8];  // mass / mreac of each reactant atom (the step kernel's xi)
 };
 
 template <int N>
@@ -81,6 +82,29 @@ __host__ __device__ inline double xi_bimolec(const XiDev& x, const double* c, co
       for (int d = 0; d < 3; ++d) dxi[3 * x.reac2[k] + d] -= b * Red[d] / reds * mass[x.reac2[k]] / x.mreac2;
   }
   return x.xi_ideal * s1 + (1.0 - x.xi_ideal) * s0;
+}
+
+// xi alone (no derivative) for the side bit of a recrossing child: the same
+// formula as xi_bimolec with the reactant weights m / m_reac precomputed, so
+// the COMs cost multiplications only (FP64 divisions take ~10 FP64-pipe
+// instructions each on this GPU).
+template <int N>
+__device__ inline double xi_bimolec_value(const XiDev& x, const double* c) {
+  double Rf[3], Rb[3], c1[3] = {0, 0, 0}, c2[3] = {0, 0, 0};
+  for (int d = 0; d < 3; ++d) {
+    Rf[d] = c[3 * x.form0 + d] - c[3 * x.form1 + d];
+    Rb[d] = c[3 * x.brk0 + d] - c[3 * x.brk1 + d];
+  }
+  for (int k = 0; k < x.nreac1; ++k)
+    for (int d = 0; d < 3; ++d) c1[d] = fma(x.w1[k], c[3 * x.reac1[k] + d], c1[d]);
+  for (int k = 0; k < x.nreac2; ++k)
+    for (int d = 0; d < 3; ++d) c2[d] = fma(x.w2[k], c[3 * x.reac2[k] + d], c2[d]);
+  const double Red[3] = {c2[0] - c1[0], c2[1] - c1[1], c2[2] - c1[2]};
+  const double rf = sqrt(Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2]);
+  const double rb = sqrt(Rb[0] * Rb[0] + Rb[1] * Rb[1] + Rb[2] * Rb[2]);
+  const double reds = sqrt(Red[0] * Red[0] + Red[1] * Red[1] + Red[2] * Red[2]);
+  const double s1 = (rb - x.break_ref) - (rf - x.form_ref);
+  return x.xi_ideal * s1 + (1.0 - x.xi_ideal) * (x.r_inf - reds);
 }
 
 // Shape of the parity-split propagator blocks for P beads.
@@ -204,6 +228,12 @@ struct StepParams {
   // step counter on the device (a launch replayed from a CUDA graph reads its
   // first step index here); NULL: the launch argument
   const int* istep_dev;
+  int pow2_P;     // P is a power of two: centroids multiply by inv_P (exact)
+  double inv_P;
+  // nm_mode 1 (orthonormal normal modes): K1, K2, K3 are circulant, row j
+  // holds circ[w][(j - l) mod P] (unit mass); loaded where Ke sits in shared memory
+  int nm_mode;
+  const double* circ;  // [3][P]
 };
 
 // Sum over the G lanes of a group (deterministic tree).  red: per-group
@@ -234,6 +264,80 @@ __device__ inline void group_sum(double (&v)[NV], int G, double* red, int lane_i
     }
   }
 }
+
+// Allreduce over a group of G <= 32 lanes by reduce-scatter and all-gather:
+// at each butterfly level (offset O = G/2 .. 1) a lane keeps half of the
+// values it holds (the lower half if its bit O is clear) and adds the
+// partner's copy of that half, so the FP64 adds per lane total about NV
+// instead of NV log2(G); each sum is then read from the lane holding it.
+// The summation order is fixed (deterministic), not that of group_sum.
+template <int N, int O, int NV>
+__device__ __forceinline__ void rs_levels(double (&v)[NV], int lane) {
+  if constexpr (O >= 1) {
+    constexpr int H = (N + 1) / 2;
+    const bool b = (lane & O) != 0;
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      const double hi = (i < N - H) ? v[H + i] : 0.0;
+      const double send = b ? v[i] : hi;
+      const double keep = b ? hi : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+    }
+    rs_levels<H, O / 2, NV>(v, lane);
+  }
+}
+
+struct RsSrc {
+  int lane, idx;
+};
+// Which lane (within the group) ends up holding the sum of value c, and at
+// which slot, after rs_levels<NV, G/2>.  Every level halves the held set to
+// ceil(n/2) slots on both sides of the split (the upper half of an odd set
+// carries one empty slot), as rs_levels does.
+__host__ __device__ constexpr RsSrc rs_src(int NV, int G, int c) {
+  int n = NV, lo = 0, lane = 0;
+  for (int o = G / 2; o >= 1; o /= 2) {
+    const int h = (n + 1) / 2;
+    if (c - lo >= h) {
+      lane |= o;
+      lo += h;
+    }
+    n = h;
+  }
+  return RsSrc{lane, c - lo};
+}
+
+template <int NV, int G>
+__device__ inline void rs_allreduce(double (&v)[NV], int lane_in_group) {
+  rs_levels<NV, G / 2, NV>(v, lane_in_group);
+  const int base = (int)(threadIdx.x & 31u) & ~(G - 1);
+  double out[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    const RsSrc src = rs_src(NV, G, c);
+    out[c] = __shfl_sync(0xffffffffu, v[src.idx], base + src.lane);
+  }
+#pragma unroll
+  for (int c = 0; c < NV; ++c) v[c] = out[c];
+}
+
+// Sum over the G lanes of a group, on every lane: reduce-scatter for groups
+// inside one warp, the tree of group_sum for groups spanning warps.
+template <int NV>
+__device__ inline void group_allreduce(double (&v)[NV], int G, double* red, int lane_in_group) {
+  switch (G) {
+    case 32: rs_allreduce<NV, 32>(v, lane_in_group); return;
+    case 16: rs_allreduce<NV, 16>(v, lane_in_group); return;
+    case 8: rs_allreduce<NV, 8>(v, lane_in_group); return;
+    case 4: rs_allreduce<NV, 4>(v, lane_in_group); return;
+    case 2: rs_allreduce<NV, 2>(v, lane_in_group); return;
+    case 1: return;
+    default: group_sum<NV>(v, G, red, lane_in_group);
+  }
+}
+
+// Non-finite test on the exponent bits (integer pipe, no FP64 compare).
+__device__ inline bool nonfinite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) == 0x7ff00000; }
 
 __device__ inline void group_sync(int G) {
   if (G > 32) __syncthreads();
@@ -339,8 +443,12 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
   double* sv = su + 2 * NC * pd.su;        // [2 NC][sv]
   double* red = sv + 2 * NC * pd.sv;       // [(G/32)][32]
 
-  for (int x = threadIdx.x; x < nke; x += blockDim.x) s_ke[x] = prm.ke[x];
-  for (int x = threadIdx.x; x < nko; x += blockDim.x) s_ko[x] = prm.ko[x];
+  if (prm.nm_mode) {
+    for (int x = threadIdx.x; x < 3 * P; x += blockDim.x) s_ke[x] = prm.circ[x];  // 3 P <= nke
+  } else {
+    for (int x = threadIdx.x; x < nke; x += blockDim.x) s_ke[x] = prm.ke[x];
+    for (int x = threadIdx.x; x < nko; x += blockDim.x) s_ko[x] = prm.ko[x];
+  }
   if (prm.thermostat == CR_THERMO_PILE)
     for (int x = threadIdx.x; x < 2 * P; x += blockDim.x) s_pile[x] = prm.pile[x];
 
@@ -429,7 +537,8 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 #pragma unroll
     for (int c = 0; c < NC; ++c) p[c] = p[c] - prm.half_dt * f[c];
 
-    // free ring polymer in Caracal's cosine modes (src/verlet.f90:377-463)
+    // free ring polymer (src/verlet.f90:377-463): Caracal's cosine modes, or
+    // orthonormal normal modes where nm_mode is set
     group_sync(G);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
@@ -437,66 +546,90 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
       xs[(NC + c) * G + j] = q[c];
     }
     group_sync(G);
-    // fold each coordinate's P values into u (and v): tasks (cc, l)
-    for (int idx = j; idx < 2 * NC * pd.nu; idx += G) {
-      const int cc = idx / pd.nu, l = idx - cc * pd.nu;
-      const double* x = xs + cc * G;
-      const double a = sym_at(x, l, P);
-      if (pd.split && 2 * l != pd.M) {
-        const double b = sym_at(x, pd.M - l, P);
-        su[cc * pd.su + l] = a + b;
-        if (l < pd.nv) sv[cc * pd.sv + l] = a - b;
-      } else {
-        su[cc * pd.su + l] = a;
-      }
-    }
-    group_sync(G);
-    // row pairs (r, M - r) of every coordinate: tasks (c, r); outputs into xs
-    for (int idx = j; idx < NC * pd.nr; idx += G) {
-      const int c = idx / pd.nr, r = idx - c * pd.nr;
-      const double* k1e = s_ke + (0 * pd.nr + r) * pd.nu;
-      const double* k2e = s_ke + (1 * pd.nr + r) * pd.nu;
-      const double* k3e = s_ke + (2 * pd.nr + r) * pd.nu;
-      const double* up = su + c * pd.su;
-      const double* uq = su + (NC + c) * pd.su;
-      double e1q = 0.0, e1p = 0.0, e2q = 0.0, e3p = 0.0;
-      for (int l = 0; l < pd.nu; ++l) {
-        const double a1 = k1e[l], a2 = k2e[l], a3 = k3e[l], xq = uq[l], xp = up[l];
-        e1q = fma(a1, xq, e1q);
-        e1p = fma(a1, xp, e1p);
-        e2q = fma(a2, xq, e2q);
-        e3p = fma(a3, xp, e3p);
-      }
-      double o1q = 0.0, o1p = 0.0, o2q = 0.0, o3p = 0.0;
-      if (pd.nv > 0) {
-        const double* k1o = s_ko + (0 * pd.nr + r) * pd.nv;
-        const double* k2o = s_ko + (1 * pd.nr + r) * pd.nv;
-        const double* k3o = s_ko + (2 * pd.nr + r) * pd.nv;
-        const double* vp = sv + c * pd.sv;
-        const double* vq = sv + (NC + c) * pd.sv;
-        for (int l = 0; l < pd.nv; ++l) {
-          const double a1 = k1o[l], a2 = k2o[l], a3 = k3o[l], xq = vq[l], xp = vp[l];
-          o1q = fma(a1, xq, o1q);
-          o1p = fma(a1, xp, o1p);
-          o2q = fma(a2, xq, o2q);
-          o3p = fma(a3, xp, o3p);
+    if (prm.nm_mode) {
+      // orthonormal normal modes: bead j's row of the circulant K1, K2, K3
+      if (j < P) {
+        const double* c1 = s_ke;
+        const double* c2 = s_ke + P;
+        const double* c3 = s_ke + 2 * P;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          double a1p = 0.0, a1q = 0.0, a2q = 0.0, a3p = 0.0;
+          int m = j;  // (j - l) mod P
+          for (int l = 0; l < P; ++l) {
+            const double xp = xs[c * G + l], xq = xs[(NC + c) * G + l];
+            a1p = fma(c1[m], xp, a1p);
+            a1q = fma(c1[m], xq, a1q);
+            a2q = fma(c2[m], xq, a2q);
+            a3p = fma(c3[m], xp, a3p);
+            m = (m == 0) ? P - 1 : m - 1;
+          }
+          p[c] = fma(prm.mass[c / 3], a2q, a1p);
+          q[c] = fma(prm.inv_mass[c / 3], a3p, a1q);
         }
       }
-      const double m = prm.mass[c / 3], im = prm.inv_mass[c / 3];
-      xs[c * H + r] = fma(m, e2q + o2q, e1p + o1p);
-      xs[(NC + c) * H + r] = fma(im, e3p + o3p, e1q + o1q);
-      if (pd.split && 2 * r != pd.M) {
-        xs[c * H + pd.M - r] = fma(m, e2q - o2q, e1p - o1p);
-        xs[(NC + c) * H + pd.M - r] = fma(im, e3p - o3p, e1q - o1q);
+    } else {
+      // Caracal's transform: fold each coordinate's P values into u (and v): tasks (cc, l)
+      for (int idx = j; idx < 2 * NC * pd.nu; idx += G) {
+        const int cc = idx / pd.nu, l = idx - cc * pd.nu;
+        const double* x = xs + cc * G;
+        const double a = sym_at(x, l, P);
+        if (pd.split && 2 * l != pd.M) {
+          const double b = sym_at(x, pd.M - l, P);
+          su[cc * pd.su + l] = a + b;
+          if (l < pd.nv) sv[cc * pd.sv + l] = a - b;
+        } else {
+          su[cc * pd.su + l] = a;
+        }
       }
-    }
-    group_sync(G);
-    if (j < P) {
-      const int row = (j <= P - j) ? j : P - j;
+      group_sync(G);
+      // row pairs (r, M - r) of every coordinate: tasks (c, r); outputs into xs
+      for (int idx = j; idx < NC * pd.nr; idx += G) {
+        const int c = idx / pd.nr, r = idx - c * pd.nr;
+        const double* k1e = s_ke + (0 * pd.nr + r) * pd.nu;
+        const double* k2e = s_ke + (1 * pd.nr + r) * pd.nu;
+        const double* k3e = s_ke + (2 * pd.nr + r) * pd.nu;
+        const double* up = su + c * pd.su;
+        const double* uq = su + (NC + c) * pd.su;
+        double e1q = 0.0, e1p = 0.0, e2q = 0.0, e3p = 0.0;
+        for (int l = 0; l < pd.nu; ++l) {
+          const double a1 = k1e[l], a2 = k2e[l], a3 = k3e[l], xq = uq[l], xp = up[l];
+          e1q = fma(a1, xq, e1q);
+          e1p = fma(a1, xp, e1p);
+          e2q = fma(a2, xq, e2q);
+          e3p = fma(a3, xp, e3p);
+        }
+        double o1q = 0.0, o1p = 0.0, o2q = 0.0, o3p = 0.0;
+        if (pd.nv > 0) {
+          const double* k1o = s_ko + (0 * pd.nr + r) * pd.nv;
+          const double* k2o = s_ko + (1 * pd.nr + r) * pd.nv;
+          const double* k3o = s_ko + (2 * pd.nr + r) * pd.nv;
+          const double* vp = sv + c * pd.sv;
+          const double* vq = sv + (NC + c) * pd.sv;
+          for (int l = 0; l < pd.nv; ++l) {
+            const double a1 = k1o[l], a2 = k2o[l], a3 = k3o[l], xq = vq[l], xp = vp[l];
+            o1q = fma(a1, xq, o1q);
+            o1p = fma(a1, xp, o1p);
+            o2q = fma(a2, xq, o2q);
+            o3p = fma(a3, xp, o3p);
+          }
+        }
+        const double m = prm.mass[c / 3], im = prm.inv_mass[c / 3];
+        xs[c * H + r] = fma(m, e2q + o2q, e1p + o1p);
+        xs[(NC + c) * H + r] = fma(im, e3p + o3p, e1q + o1q);
+        if (pd.split && 2 * r != pd.M) {
+          xs[c * H + pd.M - r] = fma(m, e2q - o2q, e1p - o1p);
+          xs[(NC + c) * H + pd.M - r] = fma(im, e3p - o3p, e1q - o1q);
+        }
+      }
+      group_sync(G);
+      if (j < P) {
+        const int row = (j <= P - j) ? j : P - j;
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        p[c] = xs[c * H + row];
-        q[c] = xs[(NC + c) * H + row];
+        for (int c = 0; c < NC; ++c) {
+          p[c] = xs[c * H + row];
+          q[c] = xs[(NC + c) * H + row];
+        }
       }
     }
 
@@ -514,11 +647,12 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
       double cq[NC];
 #pragma unroll
       for (int c = 0; c < NC; ++c) cq[c] = active ? q[c] : 0.0;
-      group_sum<NC>(cq, G, red, j);
-#pragma unroll
-      for (int c = 0; c < NC; ++c) cq[c] = cq[c] / P;
+      group_allreduce<NC>(cq, G, red, j);
       if (active && j == 0) {
-        const double xi = xi_bimolec<N>(prm.xi, cq, prm.mass, nullptr);
+        // centroid: a multiplication by 1/P where P is a power of two (exact), else the division
+#pragma unroll
+        for (int c = 0; c < NC; ++c) cq[c] = prm.pow2_P ? cq[c] * prm.inv_P : cq[c] / P;
+        const double xi = xi_bimolec_value<N>(prm.xi, cq);
         prm.side[(size_t)t * prm.side_stride + (istep - prm.side_step0 - 1)] = xi > 0.0 ? 1 : 0;
       }
     }
@@ -541,7 +675,7 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
     // NaN / Inf check (src/verlet.f90:1256-1275)
 #pragma unroll
     for (int c = 0; c < NC; ++c)
-      if (!isfinite(q[c])) status |= CR_TRAJ_NONFINITE;
+      if (nonfinite_bits(q[c])) status |= CR_TRAJ_NONFINITE;
 
     // transrot (src/transrot.f90:36-237): removed COM velocity and rotation
     // centre both carry Caracal's extra 1/P (total mass P^2 sum m).
@@ -563,7 +697,7 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 #pragma unroll
         for (int k = 0; k < 6; ++k) s1[k] = 0.0;
       }
-      group_sum<6>(s1, G, red, j);
+      group_allreduce<6>(s1, G, red, j);
       const double itm = 1.0 / prm.totmass;
       const double vt[3] = {s1[0] * itm, s1[1] * itm, s1[2] * itm};
       const double xt[3] = {s1[3] * itm, s1[4] * itm, s1[5] * itm};
@@ -588,7 +722,7 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 #pragma unroll
         for (int k = 0; k < 9; ++k) s2[k] = 0.0;
       }
-      group_sum<9>(s2, G, red, j);
+      group_allreduce<9>(s2, G, red, j);
       const double tm = prm.totmass;
       double mang[3] = {s2[0] - (xt[1] * vt[2] - xt[2] * vt[1]) * tm,
                         s2[1] - (xt[2] * vt[0] - xt[0] * vt[2]) * tm,

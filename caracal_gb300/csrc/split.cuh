@@ -80,6 +80,9 @@ struct SplitParams {
   int* shake_fail;         // [T]
   int umbrella;            // 1: bias towards the trajectory's window after the forces
   UmbrellaDev umb;
+  // nm_mode 1: orthonormal normal modes, K1, K2, K3 circulant: circ[w][(j - l) mod P]
+  int nm_mode;
+  const double* circ;      // [3][P]
   // transrot / energy scratch of split_moments_kernel and split_solve_kernel
   double* fsum;            // [T][S][16] partial sums per slice
   int* fstat;              // [T][S] status bits per slice
@@ -184,8 +187,12 @@ __global__ void __launch_bounds__(kSplitBlock) split_drift_kernel(SplitParams s)
   double* tmp = eta + cw_max * sp;
   double* sa = tmp + cw_max * sp;
   double* sb = sa + P;
-  for (int x = threadIdx.x; x < nke; x += blockDim.x) ske[x] = s.ke[x];
-  for (int x = threadIdx.x; x < nko; x += blockDim.x) sko[x] = s.ko[x];
+  if (s.nm_mode) {
+    for (int x = threadIdx.x; x < 3 * P; x += blockDim.x) ske[x] = s.circ[x];  // 3 P <= nke
+  } else {
+    for (int x = threadIdx.x; x < nke; x += blockDim.x) ske[x] = s.ke[x];
+    for (int x = threadIdx.x; x < nko; x += blockDim.x) sko[x] = s.ko[x];
+  }
   if (pile)
     for (int x = threadIdx.x; x < 2 * P; x += blockDim.x) sa[x] = s.pile[x];
   const size_t tb = (size_t)t * P * NC + c0;
@@ -213,6 +220,30 @@ __global__ void __launch_bounds__(kSplitBlock) split_drift_kernel(SplitParams s)
     xq[c * sp + j] -= shq[c];
   }
   __syncthreads();
+  if (s.nm_mode) {
+    // orthonormal normal modes: row j of the circulant K1, K2, K3 (the
+    // constant vector is an eigenvector of all three, so the q shift holds)
+    for (int idx = threadIdx.x; idx < P * cw; idx += blockDim.x) {
+      const int c = idx % cw, j = idx / cw;
+      const double* xqc = xq + c * sp;
+      const double* xpc = xp + c * sp;
+      double a1p = 0.0, a1q = 0.0, a2q = 0.0, a3p = 0.0;
+      int m = j;  // (j - l) mod P
+      for (int l = 0; l < P; ++l) {
+        const double c1 = ske[m], c2 = ske[P + m], c3 = ske[2 * P + m];
+        a1p = fma(c1, xpc[l], a1p);
+        a1q = fma(c1, xqc[l], a1q);
+        a2q = fma(c2, xqc[l], a2q);
+        a3p = fma(c3, xpc[l], a3p);
+        m = (m == 0) ? P - 1 : m - 1;
+      }
+      const int atom = (c0 + c) / 3;
+      const size_t g = tb + (size_t)j * NC + c;
+      s.q[g] = fma(s.inv_mass[atom], a3p, a1q) + shq[c];
+      s.p[g] = fma(s.mass[atom], a2q, a1p);
+    }
+    return;
+  }
   // fold into u (and v)
   const int M = s.M;
   for (int idx = threadIdx.x; idx < cw * s.nu; idx += blockDim.x) {
@@ -821,7 +852,7 @@ __global__ void split_init_positions_kernel(int T, int P, int NC, uint32_t seed,
 }
 
 __global__ void split_init_momenta_kernel(int T, int P, int NC, uint32_t seed, uint32_t traj0, const double* sig,
-                                          int zero, double* p) {
+                                          int zero, uint32_t draw, double* p) {
   const int npair = (NC + 1) / 2;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)T * P * npair) return;
@@ -830,7 +861,7 @@ __global__ void split_init_momenta_kernel(int T, int P, int NC, uint32_t seed, u
   const int t = (int)(b / P), k = (int)(b % P);
   const int c = 2 * ip;
   double z0 = 0.0, z1 = 0.0;
-  if (!zero) normal_pair_f64(seed, traj0 + (uint32_t)t, (uint32_t)ip, (uint32_t)k, 0u, TAG_INIT_MOMENTA, z0, z1);
+  if (!zero) normal_pair_f64(seed, traj0 + (uint32_t)t, (uint32_t)ip, (uint32_t)k, draw, TAG_INIT_MOMENTA, z0, z1);
   p[(size_t)b * NC + c] = z0 * sig[c / 3];
   if (c + 1 < NC) p[(size_t)b * NC + c + 1] = z1 * sig[(c + 1) / 3];
 }

@@ -156,7 +156,7 @@ class QMDFFForceField:
 
     def __init__(self, ff, tables=None, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
         from . import qmdff as Q
-        tables = tables if tables is not None else Q.ElementTables.d3_like()
+        tables = tables if tables is not None else Q.ElementTables.caracal()
         ip = lambda a: np.ascontiguousarray(a, dtype=np.int32)  # noqa: E731
         fp = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
         self.n = int(ff.n)
@@ -202,22 +202,41 @@ class QMDFFForceField:
                 "cr_qmdff_egrad")
         return e, g
 
+    def _piece(self, fn, xyz, e, g, precision):
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, self.n, 3)
+        prec = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        L.check(fn(self._h, L.dptr(x), x.shape[0], L.dptr(e), L.dptr(g), prec), fn.__name__)
+
+    def ff_eg(self, xyz, e, g, precision="fp64"):
+        """Caracal's ff_eg: bonded terms into e (nbeads,), g (nbeads, n, 3), overwritten."""
+        self._piece(L.lib().cr_qmdff_eg, xyz, e, g, precision)
+
+    def ff_nonb(self, xyz, e, g, precision="fp64"):
+        """Caracal's ff_nonb: the NCI-pair terms added to e, g."""
+        self._piece(L.lib().cr_qmdff_nonb, xyz, e, g, precision)
+
+    def ff_hb(self, xyz, e, g, precision="fp64"):
+        """Caracal's ff_hb: the hydrogen- and halogen-bond terms added to e, g."""
+        self._piece(L.lib().cr_qmdff_hb, xyz, e, g, precision)
+
     @classmethod
     def load(cls, path, tables=None, e_zero=0.0, zahn=False, coul_cut=50.0):
         """A device QMDFF read from a .qmdff file by the library's own reader
-        (cr_qmdff_load); the pair C6 from the element-pair table."""
+        with Caracal's set-up (cr_qmdff_load_d3: coordination numbers of the
+        file's geometry, CN-interpolated D3 pair C6)."""
         from . import qmdff as Q
-        tables = tables if tables is not None else Q.ElementTables.d3_like()
+        tables = tables if tables is not None else Q.ElementTables.caracal()
         fp = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
-        c6 = np.zeros((94, 94))
-        for (a, b), val in Q.C6_PAIR.items():
-            c6[a - 1, b - 1] = c6[b - 1, a - 1] = val
+        c6ab, maxci = Q.d3_reference()
         arrs = dict(rad=fp(Q.element_radii()), r0ab=fp(tables.r0ab[1:, 1:].T), zab=fp(tables.zab[1:, 1:].T),
-                    r0094=fp(tables.r094[1:, 1:].T), sr42=fp(tables.sr42[1:, 1:].T), c6ab=fp(c6.T))
-        t = L.CrQmdffTables(*[L.dptr(arrs[k]) for k in ("rad", "r0ab", "zab", "r0094", "sr42", "c6ab")])
+                    r0094=fp(tables.r094[1:, 1:].T), sr42=fp(tables.sr42[1:, 1:].T),
+                    c6ref=fp(np.ravel(c6ab, order="F")), maxci=np.ascontiguousarray(maxci, dtype=np.int32),
+                    rcov=fp(Q.element_data()["rcov"]))
+        t = L.CrQmdffTables(*[L.dptr(arrs[k]) for k in ("rad", "r0ab", "zab", "r0094", "sr42")], None)
+        d3 = L.CrD3Reference(L.dptr(arrs["c6ref"]), L.iptr(arrs["maxci"]), L.dptr(arrs["rcov"]))
         h = C.c_void_p()
-        L.check(L.lib().cr_qmdff_load(str(path).encode(), C.byref(t), float(e_zero), int(bool(zahn)),
-                                      float(coul_cut), C.byref(h)), "cr_qmdff_load")
+        L.check(L.lib().cr_qmdff_load_d3(str(path).encode(), C.byref(t), C.byref(d3), float(e_zero),
+                                         int(bool(zahn)), float(coul_cut), C.byref(h)), "cr_qmdff_load_d3")
         obj = cls.__new__(cls)
         obj._h = h
         obj._arrs = arrs
@@ -364,6 +383,32 @@ def evb_fit_grad(basis, x, e1, e2, eref):
     return grad
 
 
+class PinnedHost:
+    """Page-lock numpy arrays the caller owns (cr_host_register) for the
+    duration of a with-block, so host-buffer steps copy them at pinned speed."""
+
+    def __init__(self, *arrays):
+        self.arrays = [a for a in arrays if a is not None]
+
+    def __enter__(self):
+        done = []
+        try:
+            for a in self.arrays:
+                if not a.flags.c_contiguous:
+                    raise ValueError("only contiguous arrays can be registered")
+                L.check(L.lib().cr_host_register(a.ctypes.data_as(C.c_void_p), a.nbytes), "cr_host_register")
+                done.append(a)
+        except Exception:
+            for a in done:
+                L.lib().cr_host_unregister(a.ctypes.data_as(C.c_void_p))
+            raise
+        return self
+
+    def __exit__(self, *exc):
+        for a in self.arrays:
+            L.lib().cr_host_unregister(a.ctypes.data_as(C.c_void_p))
+
+
 class RPMDEngine:
     """A batch of independent RPMD trajectories resident on one GPU.
 
@@ -372,7 +417,7 @@ class RPMDEngine:
 
     def __init__(self, pes, mass, nbeads, ntraj, dt_au, beta=None, thermostat="none",
                  andersen_step=70, pile_tau0_au=0.0, transrot=True, precision="fp64", seed=0,
-                 traj0=0, nose_q_au=0.0):
+                 traj0=0, nose_q_au=0.0, nm_mode=0):
         self.ff = pes if isinstance(pes, (QMDFFForceField, EVBPair)) else None
         self.water = pes if isinstance(pes, WaterBox) else None
         if isinstance(pes, WaterBox):
@@ -393,7 +438,7 @@ class RPMDEngine:
                               int(andersen_step), int(bool(transrot)),
                               PRECISION[precision] if isinstance(precision, str) else int(precision),
                               int(seed) & 0xFFFFFFFF, int(traj0) & 0xFFFFFFFF, float(dt_au),
-                              self.beta, float(pile_tau0_au), L.dptr(self.mass), float(nose_q_au))
+                              self.beta, float(pile_tau0_au), L.dptr(self.mass), float(nose_q_au), int(nm_mode))
         h = C.c_void_p()
         if self.water is not None:
             L.check(L.lib().cr_engine_create_water(C.byref(self.cfg), self.water._h, C.byref(h)),
@@ -443,6 +488,15 @@ class RPMDEngine:
 
     def compute_forces(self):
         L.check(L.lib().cr_engine_compute_forces(self._h), "compute_forces")
+
+    def mdinit(self, draw=0):
+        """Caracal's mdinit: forces (plus the umbrella bias where the engine
+        has windows), momenta from Gaussian stream `draw` (NVT) or zero
+        (NVE), chain at rest."""
+        L.check(L.lib().cr_engine_mdinit(self._h, int(draw) & 0xFFFFFFFF), "mdinit")
+
+    def set_andersen_step(self, n):
+        L.check(L.lib().cr_engine_set_andersen_step(self._h, int(n)), "set_andersen_step")
 
     def set_state(self, q, p, f=None):
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.shape)

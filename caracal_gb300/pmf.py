@@ -30,13 +30,11 @@ def umbrella_integration(xi_windows, kforce, average, variance, beta, xi_min, xi
     av = np.asarray(average, dtype=float)
     va = np.asarray(variance, dtype=float)
     bin_size = (xi_max - xi_min) / (nbins - 1)
-    dA = np.zeros(nbins)
-    for j in range(nbins):
-        x = xi_min + bin_size * j
-        p = 1.0 / np.sqrt(2.0 * np.pi * va) * np.exp(-0.5 * (x - av) ** 2 / va)
-        da = (1.0 / beta) * (x - av) / va - k * (x - xw)
-        w = nsamples * p
-        dA[j] = np.sum(w * da) / np.sum(w)
+    x = xi_min + bin_size * np.arange(nbins)[:, None]          # (bins, windows)
+    p = 1.0 / np.sqrt(2.0 * np.pi * va) * np.exp(-0.5 * (x - av) ** 2 / va)
+    da = (1.0 / beta) * (x - av) / va - k * (x - xw)
+    w = nsamples * p
+    dA = np.sum(w * da, axis=1) / np.sum(w, axis=1)
     coord = np.zeros(nbins)
     pmf = np.zeros(nbins)
     acc = 0.0

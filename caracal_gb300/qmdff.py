@@ -1,26 +1,36 @@
-"""QMDFF force-field data on the host: `.qmdff` files and the synthetic alkane.
+"""QMDFF force-field data on the host: `.qmdff` files, Caracal's element tables
+and D3 dispersion set-up, and the synthetic alkane.
 
 * ``read_qmdff`` / ``write_qmdff`` follow Caracal's file format: the reader of
   src/rdsolvff.f90:34-202 (header ``n q d``, method line, ``at x y z q mol``
   per atom, ``nbond nangl ntors nhb nnci``, the term lines, H-bond triples six
   per line, NCI triples eight per line; torsion phases are stored over pi) and
   the writer of src/main_gen.f90:825-847.
-* ``ElementTables`` are the per-element-pair non-bonded tables Caracal's
-  ``prepare`` hands to ``ff_nonb`` (src/setnonb.f90): sr42 = 3 s8 r2r4_i r2r4_j,
-  r094 = a1 sqrt(3 r2r4_i r2r4_j) + a2, zab = vz_i vz_j, r0ab = 16.5/R0AB^1.5,
-  with Caracal's REAL(4) literals (a1 = 0.45, s8 = 2.7, the valel factors).
-  The engine takes these tables (and the C6 pair matrix) from its caller, as
-  ff_nonb does.  For the synthetic alkane the C6 pair values and the D3 pair
-  radii R0AB are D3-like constants chosen here (Caracal's D3 reference data is
-  not reproduced), so that workload is "QMDFF-shaped", not a Caracal fit.
+* ``prepare`` is Caracal's QMDFF set-up (src/prepare.f90:100-127): the D3
+  reference C6 table as ``copyc6`` lays it out (src/copyc6.f90:35674-35744,
+  element codes split by ``limit``, src/limit.f90:34-60), coordination numbers
+  of the reference geometry (``ncoord_qmdff``, src/ncoord_qmdff.f90:36-76) and
+  the CN-interpolated pair C6 (``getc6``, src/getc6.f90:35-83).
+* ``ElementTables.caracal`` are the per-element-pair tables ``setnonb`` makes
+  (src/setnonb.f90:35-192): sr42 = 3 s8 r2r4_i r2r4_j, r094 = a1 sqrt(3
+  r2r4_i r2r4_j) + a2, zab = vz_i vz_j (``valel``, src/valel.f90:35-115),
+  r0ab = 16.5 / R0AB^1.5 with the D3 cut-off radii of ``setr0``
+  (src/setr0.f90), with Caracal's REAL(4) literals (a1 = 0.45, s8 = 2.7, the
+  r2r4 / rcov / R0AB arrays, the valel factors).  The element data come from
+  ``data/qmdff_tables.npz`` (made by ``data/make_qmdff_tables.py`` from the
+  reference's source files).
 * ``alkane`` builds the synthetic C_nH_2n+2 QMDFF of the benchmark: zig-zag
   chain, r(CC) = 1.53 A, r(CH) = 1.09 A, tetrahedral angles, bond / angle /
   torsion force constants drawn in +-20 % of 0.3 Eh/bohr^2, 0.1 Eh/rad^2,
   0.002 Eh from the seed, charges +-0.1 e with exact neutrality, NCI = all
-  pairs three or more bonds apart (categories 3, 4, >=5 -> 5).
+  pairs three or more bonds apart (categories 3, 4, >=5 -> 5), C6 from
+  Caracal's D3 set-up on its geometry.
 """
 from __future__ import annotations
 
+import functools
+import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -28,42 +38,183 @@ import numpy as np
 from .units import BOHR_ANGSTROM
 
 F32 = lambda x: float(np.float32(x))  # noqa: E731  (REAL(4) literal widened to REAL(8))
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "qmdff_tables.npz")
 
-# published D3 values Caracal keeps in src/setnonb.f90 (r2r4) for H, C, N, O, Cl
-R2R4 = {1: F32(2.00734898), 6: F32(3.10492822), 7: F32(2.71175247), 8: F32(2.59361680),
-        17: F32(3.72932356)}
-# covalent radii, Angstrom (Caracal's rad table is in bohr, src/prepare.f90)
-RAD_ANG = {1: 0.32, 6: 0.75, 7: 0.71, 8: 0.63, 17: 0.99}
-# synthetic D3-like inputs (not Caracal's D3 tables)
-C6_PAIR = {(1, 1): 3.0898, (1, 6): 7.5916, (6, 6): 18.1368, (1, 7): 5.5, (1, 8): 4.6, (6, 7): 14.0,
-           (6, 8): 11.5, (7, 7): 11.0, (7, 8): 9.5, (8, 8): 8.0, (1, 17): 12.0, (6, 17): 30.0,
-           (7, 17): 24.0, (8, 17): 20.0, (17, 17): 50.0}
-R0AB_PAIR_ANG = {(1, 1): 2.1823, (1, 6): 2.5984, (6, 6): 2.9146, (1, 7): 2.47, (1, 8): 2.36,
-                 (6, 7): 2.77, (6, 8): 2.66, (7, 7): 2.63, (7, 8): 2.52, (8, 8): 2.41, (1, 17): 2.80,
-                 (6, 17): 3.10, (7, 17): 2.97, (8, 17): 2.86, (17, 17): 3.34}
 # H-bond / halogen-bond scaling of src/setnonb.f90:123-137 (REAL(4) literals)
 SCALE_HB = {7: F32(0.8), 8: F32(0.3), 9: F32(0.1), 15: F32(2.0), 16: F32(2.0), 17: F32(2.0),
             34: F32(2.0), 35: F32(2.0)}
 SCALE_XB = {17: F32(0.30), 35: F32(0.60), 53: F32(0.80), 85: F32(1.00)}
 
 
-def element_radii():
-    """rad(94) of module qmdff: covalent radius per element in bohr (H and C set)."""
-    r = np.zeros(94)
-    for z, v in RAD_ANG.items():
-        r[z - 1] = v / BOHR_ANGSTROM
-    return r
+@functools.lru_cache(maxsize=1)
+def element_data():
+    """The element arrays of data/qmdff_tables.npz (read once)."""
+    with np.load(DATA) as d:
+        return {k: d[k].copy() for k in d.files}
+
+
+def valence_charges():
+    """vz(94) of valel (src/valel.f90:35-115), index 0 = element 1: the
+    valence-shell counts times the REAL(4) fit factors, then the fitted
+    group-1/2 values (REAL(4) literals widened)."""
+    z = np.zeros(95)
+    for i in range(1, 55):
+        at = float(i)
+        z[i] = at
+        if 2 < i <= 10:
+            z[i] = at - 2
+        if 10 < i <= 13:
+            z[i] = at - 10
+        if 13 < i <= 18:
+            z[i] = at - 10
+        if (30 <= i <= 36) or i in (19, 20):
+            z[i] = at - 18
+            if i >= 30:
+                z[i] = at - 28
+        if 21 <= i <= 29:
+            z[i] = at - 18
+        if 37 <= i <= 47:
+            z[i] = at - 36
+        if 47 < i <= 54:
+            z[i] = at - 46
+    z[57:81] = 4.0
+    for i in range(81, 87):
+        z[i] = float(i) - 78.0
+    z[1:3] *= F32(2.35)
+    z[3:11] *= F32(0.95)
+    z[11:19] *= F32(0.75)
+    z[19:55] *= F32(0.65)
+    z[55:95] *= F32(0.60)
+    for i, v in ((3, 1.7), (11, 2.5), (19, 3.0), (37, 3.0), (55, 3.0), (87, 3.0), (4, 5.5), (12, 3.0), (20, 2.8),
+                 (38, 2.6), (56, 2.4), (88, 2.4)):
+        z[i] = F32(v)
+    return z[1:]
 
 
 def valence_charge(z):
-    """valel (src/valel.f90) for rows 1-3: valence count times the REAL(4) fit factor."""
-    if z <= 2:
-        return float(z) * F32(2.35)
-    if z <= 10:
-        return 1.7 if z == 3 else 5.5 if z == 4 else float(z - 2) * F32(0.95)
-    if z <= 18:
-        return 2.5 if z == 11 else 3.0 if z == 12 else float(z - 10) * F32(0.75)
-    raise ValueError("valence charges are tabulated up to Ar")
+    return float(valence_charges()[int(z) - 1])
+
+
+def _limit(iat):
+    """src/limit.f90: element code above 100 -> (element, CN-reference index)."""
+    iadr = 1
+    while iat > 100:
+        iat -= 100
+        iadr += 1
+    return iat, iadr
+
+
+@functools.lru_cache(maxsize=1)
+def d3_reference():
+    """(c6ab (94, 94, 5, 5, 3), maxci (94,)) as copyc6 leaves module qmdff:
+    c6ab[i, j, a, b] = (C6, CN_i, CN_j) of the reference pair (element i+1,
+    CN index a+1; element j+1, CN index b+1), -1 where none exists; the
+    alkali and alkaline-earth C6 copied from the preceding rare gas."""
+    pars = element_data()["d3_pars"]
+    c6ab = np.full((94, 94, 5, 5, 3), -1.0)
+    maxci = np.zeros(94, dtype=np.int64)
+    for c6, a, b, cn1, cn2 in pars:
+        iat, iadr = _limit(int(a))
+        jat, jadr = _limit(int(b))
+        maxci[iat - 1] = max(maxci[iat - 1], iadr)
+        maxci[jat - 1] = max(maxci[jat - 1], jadr)
+        c6ab[iat - 1, jat - 1, iadr - 1, jadr - 1] = (c6, cn1, cn2)
+        c6ab[jat - 1, iat - 1, jadr - 1, iadr - 1] = (c6, cn2, cn1)
+    for iat in (3, 11, 19, 37, 55, 87):       # src/copyc6.f90:35702-35740
+        i, g = iat - 1, iat - 2               # 0-based alkali, rare gas
+        for j in range(94):
+            mj = maxci[j]
+            for ii in range(maxci[i]):
+                c6ab[i, j, ii, :mj, 0] = c6ab[g, j, 0, :mj, 0]
+                c6ab[j, i, :mj, ii, 0] = c6ab[j, g, :mj, 0, 0]
+            for ii in range(maxci[i + 1]):
+                c6ab[i + 1, j, ii, :mj, 0] = c6ab[g, j, 0, :mj, 0]
+                c6ab[j, i + 1, :mj, ii, 0] = c6ab[j, g, :mj, 0, 0]
+    return c6ab, maxci
+
+
+def ncoord(at, xyz, cn_thr=5000.0):
+    """Coordination numbers (src/ncoord_qmdff.f90:36-76): sum over the other
+    atoms of 1 / (1 + exp(-16 (rcov_i + rcov_j) / r - 1)), pairs with
+    r^2 > cn_thr bohr^2 skipped; xyz in bohr."""
+    rcov = element_data()["rcov"]
+    n = len(at)
+    cn = np.zeros(n)
+    for i in range(n):
+        xn = 0.0
+        for j in range(n):
+            if j == i:
+                continue
+            dx, dy, dz = xyz[j, 0] - xyz[i, 0], xyz[j, 1] - xyz[i, 1], xyz[j, 2] - xyz[i, 2]
+            r2 = dx * dx + dy * dy + dz * dz
+            if r2 > cn_thr:
+                continue
+            r = math.sqrt(r2)
+            rr = (rcov[at[i] - 1] + rcov[at[j] - 1]) / r
+            xn = xn + 1.0 / (1.0 + math.exp(-16.0 * (rr - 1.0)))
+        cn[i] = xn
+    return cn
+
+
+def getc6(iat, jat, nci, ncj):
+    """CN-interpolated C6 of elements iat, jat (src/getc6.f90:35-83): the
+    exp(-4 r) weighted mean over the reference pairs, r = (CN1 - nci)^2 +
+    (CN2 - ncj)^2; the nearest reference where every weight underflows."""
+    c6ab, maxci = d3_reference()
+    c6mem, rsum, csum, r_save = -1e99, 0.0, 0.0, 10000.0
+    for i in range(maxci[iat - 1]):
+        for j in range(maxci[jat - 1]):
+            c6, cn1, cn2 = c6ab[iat - 1, jat - 1, i, j]
+            if c6 > 0:
+                r = (cn1 - nci) * (cn1 - nci) + (cn2 - ncj) * (cn2 - ncj)   # Fortran ** 2: a product
+                if r < r_save:
+                    r_save, c6mem = r, c6
+                tmp1 = math.exp(-4.0 * r)
+                rsum = rsum + tmp1
+                csum = csum + tmp1 * c6
+    return csum / rsum if rsum > 1e-99 else c6mem
+
+
+def pair_c6(at, xyz):
+    """c6xy (n, n) of prepare (src/prepare.f90:121-129) for the reference
+    geometry xyz (bohr)."""
+    at = np.asarray(at, dtype=int)
+    cn = ncoord(at, np.asarray(xyz, dtype=float))
+    n = len(at)
+    c6 = np.zeros((n, n))
+    for i1 in range(n):
+        for i2 in range(i1 + 1):
+            c6[i2, i1] = c6[i1, i2] = getc6(int(at[i1]), int(at[i2]), cn[i1], cn[i2])
+    return c6
+
+
+SYMBOLS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br Kr "
+           "Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb "
+           "Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn Fr Ra Ac Th Pa U Np Pu").split()
+
+
+def element_number(symbol):
+    """Atomic number of an element symbol (case-insensitive)."""
+    return SYMBOLS.index(symbol.strip().capitalize()) + 1
+
+
+def read_xyz_frames(path):
+    """Every frame of an xyz file, coordinates converted to bohr:
+    (nframes, natoms, 3)."""
+    with open(path) as fh:
+        lines = fh.read().splitlines()
+    frames, k = [], 0
+    while k < len(lines) and lines[k].strip():
+        n = int(lines[k].split()[0])
+        frames.append([[float(x) for x in lines[k + 2 + i].split()[1:4]] for i in range(n)])
+        k += n + 2
+    return np.array(frames) / BOHR_ANGSTROM
+
+
+def element_radii():
+    """rad(94) of module qmdff after prepare: covalent radii (Mantina et al.,
+    src/prepare.f90:177-192) converted to bohr."""
+    return element_data()["rad_angstrom"] / BOHR_ANGSTROM
 
 
 def hbpara(a, b, q):
@@ -89,23 +240,37 @@ def hb_parameters(ff):
 
 @dataclass
 class ElementTables:
+    """Per-element-pair tables of ff_nonb, 1-based [iz1, iz2] as Caracal's
+    arrays (iz1, iz2) (index 0 unused)."""
     r0ab: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))   # alpha of the repulsion
     zab: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))
     r094: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))
     sr42: np.ndarray = field(default_factory=lambda: np.zeros((95, 95)))
 
     @classmethod
-    def d3_like(cls, elements=(1, 6, 7, 8, 17)):
+    @functools.lru_cache(maxsize=1)
+    def caracal(cls):
+        """setnonb's tables (src/setnonb.f90:138-161), term by term in the
+        reference's evaluation order: sr42(j,i) = 3 s8 r2r4(i) r2r4(j),
+        r094(j,i) = a1 sqrt(3 r2r4(i) r2r4(j)) + a2, zab(j,i) = vz(i) vz(j),
+        r0ab = 16.5 / (R0AB / 0.52917726)^1.5 (src/setr0.f90:810-819)."""
+        d = element_data()
+        r2r4 = d["r2r4"]
+        vz = valence_charges()
         t = cls()
         a1, s8, a2 = F32(0.45), F32(2.7), 4.0
-        for zi in elements:
-            for zj in elements:
-                t.sr42[zi, zj] = 3.0 * s8 * R2R4[zi] * R2R4[zj]
-                t.r094[zi, zj] = a1 * np.sqrt(3.0 * R2R4[zi] * R2R4[zj]) + a2
-                t.zab[zi, zj] = valence_charge(zi) * valence_charge(zj)
-                key = (min(zi, zj), max(zi, zj))
-                r0 = R0AB_PAIR_ANG[key] / BOHR_ANGSTROM
-                t.r0ab[zi, zj] = F32(16.5) / r0 ** 1.5
+        for i in range(94):
+            for j in range(94):
+                t.sr42[j + 1, i + 1] = 3.0 * s8 * r2r4[i] * r2r4[j]
+                t.r094[j + 1, i + 1] = a1 * math.sqrt(3.0 * r2r4[i] * r2r4[j]) + a2
+                t.zab[j + 1, i + 1] = vz[i] * vz[j]
+        r0 = d["r0ab_ref"]
+        k = 0
+        for i in range(94):
+            for j in range(i + 1):
+                v = 16.5 / (r0[k] / 0.52917726) ** 1.5
+                t.r0ab[i + 1, j + 1] = t.r0ab[j + 1, i + 1] = v
+                k += 1
         return t
 
 
@@ -131,7 +296,7 @@ class QMDFF:
         return len(self.at)
 
     def rad_bohr(self):
-        return np.array([RAD_ANG[int(z)] / BOHR_ANGSTROM for z in self.at])
+        return element_radii()[np.asarray(self.at, dtype=int) - 1]
 
     @property
     def nhb(self):
@@ -219,18 +384,9 @@ def read_qmdff(path, c6=None):
     hb = np.array(read(3 * nhb, int), dtype=int).reshape(nhb, 3) if nhb else np.zeros((0, 3), int)
     nci = np.array(read(3 * nnci, int), dtype=int).reshape(nnci, 3) if nnci else np.zeros((0, 3), int)
     if c6 is None:
-        c6 = pair_c6(at)
+        c6 = pair_c6(at, xyz)
     return QMDFF(at=at, xyz=xyz, q=q, bond=bond, vbond=vbond, angl=angl, vangl=vangl, tors=tors,
                  vtors=vtors, nci=nci, c6=c6, hb=hb)
-
-
-def pair_c6(at):
-    n = len(at)
-    c6 = np.zeros((n, n))
-    for i in range(n):
-        for j in range(n):
-            c6[i, j] = C6_PAIR[(min(at[i], at[j]), max(at[i], at[j]))]
-    return c6
 
 
 def alkane_geometry(nc=20, r_cc=1.53, r_ch=1.09):
@@ -369,7 +525,7 @@ def from_topology(at, xyz, bonds, seed=20261203, k_bond=0.3, k_angle=0.1, v_tors
     hb = np.zeros((0, 3), int) if hb is None else np.asarray(hb, int).reshape(-1, 3)
     return QMDFF(at=at, xyz=xyz.copy(), q=q, bond=bond, vbond=vbond, angl=np.array(angl).reshape(-1, 3),
                  vangl=np.array(vangl).reshape(-1, 2), tors=np.array(tors).reshape(-1, 6),
-                 vtors=np.array(vtors).reshape(-1, 14), nci=np.array(nci).reshape(-1, 3), c6=pair_c6(at),
+                 vtors=np.array(vtors).reshape(-1, 14), nci=np.array(nci).reshape(-1, 3), c6=pair_c6(at, xyz),
                  e_zero=e_zero, hb=hb)
 
 

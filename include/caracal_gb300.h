@@ -70,6 +70,10 @@ typedef struct cr_config {
   double pile_tau0;   /* PILE centroid time constant, a.u. */
   const double* mass; /* natoms masses, a.u. (amu / 5.485799095e-4) */
   double nose_q;      /* NHC chain time, a.u.: NOSE_Q (in time steps) x dt (src/dynamic.f90:578) */
+  int nm_mode;        /* normal-mode transform of the free ring polymer: 0 = Caracal's (rfft/irfft
+                         both keep sqrt(1/P) Re DFT, src/rfft.f90, src/irfft.f90: every step projects
+                         onto bead-reflection-symmetric configurations); 1 = orthonormal real normal
+                         modes (standard RPMD; not Caracal's code path, an engine option) */
 } cr_config;
 
 /* ---- flexible SPC water box (water_spc: src/egrad_water.f90:36-333) -------
@@ -122,7 +126,9 @@ int cr_egrad_h3(const double* q, int natoms, int nbeads, double* V, double* dVdq
  * nothing.  At most 16384 beads per call (more: CR_ERR_ARG).  All calls share
  * that array, so calls that overlap on the GPU race; serialise them.  The
  * first call on a device resolves the array's address (set-up), so make it
- * before any stream capture. */
+ * before any stream capture.  Runs on the legacy default stream with
+ * blocking copies: a call waits for, and holds up, work on every blocking
+ * stream of the device, and returns with the results on the host. */
 int cr_egrad_h3_noalloc(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
 
 /* Same surface on device-resident arrays with an explicit precision form
@@ -204,12 +210,42 @@ typedef struct cr_qmdff_tables {
  * rdsolvff derives them from the charges (src/rdsolvff.f90:142-152). */
 int cr_qmdff_load(const char* path, const cr_qmdff_tables* tab, double e_zero, int zahn, double coul_cut,
                   cr_qmdff** out);
+/* Grimme's D3 reference data as Caracal's module qmdff holds it after
+ * copyc6 (src/copyc6.f90, src/qmdff.f90:91): c6ab(94,94,5,5,3) column-major
+ * (C6, CN of the first element, CN of the second per reference pair; -1
+ * where none), maxci(94) reference CNs per element, rcov(94) the D3
+ * covalent radii of the coordination number (src/setnonb.f90:80-101). */
+typedef struct cr_d3_reference {
+  const double* c6ab;
+  const int* maxci;
+  const double* rcov;
+} cr_d3_reference;
+/* rdsolvff + prepare (src/rdsolvff.f90:34-202, src/prepare.f90:100-129):
+ * reads the .qmdff file, computes the coordination numbers of its reference
+ * geometry (ncoord_qmdff, src/ncoord_qmdff.f90:36-76) and the CN-interpolated
+ * pair C6 (getc6, src/getc6.f90:35-83), and builds the device force field
+ * with the element tables of tab (its c6ab is not used; may be NULL). */
+int cr_qmdff_load_d3(const char* path, const cr_qmdff_tables* tab, const cr_d3_reference* d3, double e_zero,
+                     int zahn, double coul_cut, cr_qmdff** out);
 /* natoms and the term counts (bonds, angles, torsions, H bonds, NCI pairs) of
  * a .qmdff file; host only. */
 int cr_qmdff_file_counts(const char* path, int* natoms, int* counts);
 int cr_qmdff_destroy(cr_qmdff* ff);
 /* Host arrays xyz(3,natoms,nbeads) -> e(nbeads) (with E_zero), g(3,natoms,nbeads). */
 int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
+/* The three pieces of Caracal's QMDFF call site (src/gradient.f90:341-358),
+ * for a caller that redirects them one by one; same arrays as
+ * cr_qmdff_egrad, E_zero in none of them.
+ *   cr_qmdff_eg:   bonds, angles, torsions and inversions; OVERWRITES e, g
+ *                  (ff_eg, src/ff_eg.f90:41-72).
+ *   cr_qmdff_nonb: dispersion, repulsion and Coulomb over the NCI pairs;
+ *                  ADDS to e, g (ff_nonb, src/ff_nonb.f90:34, 886).
+ *   cr_qmdff_hb:   hydrogen and halogen bonds; ADDS to e, g (ff_hb,
+ *                  src/ff_hb.f90:36-280).
+ * eg + nonb + hb + E_zero equals cr_qmdff_egrad to rounding. */
+int cr_qmdff_eg(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
+int cr_qmdff_nonb(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
+int cr_qmdff_hb(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
 
 /* Derivatives for parameter fitting and adjoints (plain FP64 form; force
  * fields without H/halogen bonds, else CR_ERR_UNSUPPORTED).  No reference
@@ -391,6 +427,12 @@ int cr_engine_device_state(cr_engine* e, double** q, double** p, double** f);
 /* Page-locked host buffers for fast host<->device copies. */
 int cr_host_alloc(void** ptr, unsigned long long bytes);
 int cr_host_free(void* ptr);
+/* Page-lock memory the caller already owns (cudaHostRegister), e.g. the
+ * module arrays q_i, p_i, derivs of Caracal's Fortran host (src/evb_mod.f90:246),
+ * so that cr_engine_step_host copies them at pinned-memory speed instead of
+ * staging pageable memory; unregister before the memory is freed. */
+int cr_host_register(void* ptr, unsigned long long bytes);
+int cr_host_unregister(void* ptr);
 
 /* ---- pipe calibration (no reference counterpart) ---------------------------
  * Device throughput (operations per second over the whole GPU) of one
@@ -408,6 +450,10 @@ int cr_host_free(void* ptr);
 #define CR_CALIB_ERF 9
 #define CR_CALIB_TANH 10
 #define CR_CALIB_COSH 11
+/* FP64 tensor-core MMA (mma.sync m8n8k4 f64, 256 multiply-adds per warp
+ * instruction), reported in multiply-adds per second (fp64 must be 1): the
+ * A/B of the bead transform as a dense contraction against DFMA code. */
+#define CR_CALIB_DMMA 12
 int cr_calibrate_op(int fp64, int op, int iters, double* ops_per_s);
 
 /* ---- umbrella windows (calc_rate's umbrella sampling) ----------------------
@@ -425,6 +471,22 @@ int cr_engine_set_umbrella(cr_engine* e, const cr_recross* rc, const double* cen
 int cr_engine_umbrella_sampling(cr_engine* e, int on);
 /* xsum[T], xsum2[T], hist[T][nbins] (each may be NULL); reset != 0 zeroes them */
 int cr_engine_umbrella_stats(cr_engine* e, double* xsum, double* xsum2, double* hist, int reset);
+
+/* Caracal's mdinit (src/mdinit.f90:40-173) as calc_rate calls it before
+ * every window trajectory and every parent segment (src/calc_rate.f90:966,
+ * 1536; src/recross.f90:251,462): forces of the current positions, plus the
+ * umbrella bias of mode 0 where the engine has umbrella windows
+ * (src/mdinit.f90:96-100; sampling must be off), then Andersen momenta (NVT,
+ * src/mdinit.f90:118-121) or zeros (NVE, :125), the Nose-Hoover chain at
+ * rest.  `draw` numbers the Gaussian stream of the momenta: draw 0 is the
+ * stream of cr_engine_init_momenta, and a later call with a new draw gives
+ * fresh momenta, as each of Caracal's mdinit calls does. */
+int cr_engine_mdinit(cr_engine* e, unsigned draw);
+/* ANDERSEN_STEP of an existing engine.  Caracal's recrossing sets it per
+ * phase of the parent trajectory: int(sqrt(equi_steps)) for the
+ * equilibration, int(sqrt(child_interval)) between child batches
+ * (src/recross.f90:239-242, 456-458). */
+int cr_engine_set_andersen_step(cr_engine* e, int andersen_step);
 
 /* ---- batches of trajectory classes -----------------------------------------
  * One graph launch per chunk of steps advances several engines (classes with

@@ -39,7 +39,8 @@ class Cfg(C.Structure):
     _fields_ = [("pes", C.c_int), ("natoms", C.c_int), ("nbeads", C.c_int),
                 ("thermostat", C.c_int), ("andersen_step", C.c_int), ("transrot", C.c_int),
                 ("seed", C.c_uint32), ("dt", C.c_double), ("beta", C.c_double),
-                ("pile_tau0", C.c_double), ("mass", C.POINTER(C.c_double)), ("nose_q", C.c_double)]
+                ("pile_tau0", C.c_double), ("mass", C.POINTER(C.c_double)), ("nose_q", C.c_double),
+                ("nm_mode", C.c_int)]
 
 
 class QmdffDef(C.Structure):
@@ -157,6 +158,8 @@ def lib():
         _lib.orc_transrot.argtypes = [C.POINTER(Cfg), d, d]
         _lib.orc_init_positions.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, d, C.c_double, d]
         _lib.orc_init_momenta.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, d]
+        _lib.orc_init_momenta_draw.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_uint32, d]
+        _lib.orc_d3_pair_c6.argtypes = [d, C.c_int, C.c_int, C.POINTER(C.c_int), d, d, d, d]
         _lib.orc_init_forces.argtypes = [C.POINTER(Cfg), C.c_int, d, d, d]
         _lib.orc_run.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_int, C.c_int, d, d, d, d,
                                  C.POINTER(C.c_int), C.c_int, d]
@@ -192,7 +195,7 @@ class Config:
     """Step configuration for the oracle (all quantities in atomic units)."""
 
     def __init__(self, pes, mass, nbeads, dt, beta, thermostat="none", andersen_step=70,
-                 pile_tau0=0.0, transrot=True, seed=0, nose_q=0.0):
+                 pile_tau0=0.0, transrot=True, seed=0, nose_q=0.0, nm_mode=0):
         self.mass = np.ascontiguousarray(mass, dtype=np.float64)
         self.natoms = len(self.mass)
         self.nbeads = int(nbeads)
@@ -200,7 +203,7 @@ class Config:
         self.c = Cfg(PES_IDS[pes] if isinstance(pes, str) else int(pes), self.natoms,
                      self.nbeads, self.thermostat, int(andersen_step), int(bool(transrot)),
                      int(seed) & 0xFFFFFFFF, float(dt), float(beta), float(pile_tau0),
-                     _dp(self.mass), float(nose_q))
+                     _dp(self.mass), float(nose_q), int(nm_mode))
 
     def shape(self, ntraj):
         return (ntraj, self.nbeads, self.natoms, 3)
@@ -270,10 +273,25 @@ def init_positions(cfg: Config, ntraj, q0, sigma, traj0=0):
     return q
 
 
-def init_momenta(cfg: Config, ntraj, traj0=0):
+def init_momenta(cfg: Config, ntraj, traj0=0, draw=0):
     p = np.zeros(cfg.shape(ntraj))
-    lib().orc_init_momenta(C.byref(cfg.c), ntraj, traj0, _dp(p))
+    lib().orc_init_momenta_draw(C.byref(cfg.c), ntraj, traj0, int(draw) & 0xFFFFFFFF, _dp(p))
     return p
+
+
+def d3_pair_c6(pars, at, xyz, rcov):
+    """prepare's pair C6 (n, n) and coordination numbers (n,) restated in C++
+    from the D3 reference lines pars (nlines, 5)."""
+    pars = np.ascontiguousarray(pars, dtype=np.float64)
+    at = np.ascontiguousarray(at, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    rcov = np.ascontiguousarray(rcov, dtype=np.float64)
+    n = len(at)
+    c6 = np.zeros((n, n))
+    cn = np.zeros(n)
+    lib().orc_d3_pair_c6(_dp(pars), pars.shape[0], n, at.ctypes.data_as(C.POINTER(C.c_int)), _dp(xyz), _dp(rcov),
+                         _dp(c6), _dp(cn))
+    return c6, cn
 
 
 def init_forces(cfg: Config, q):

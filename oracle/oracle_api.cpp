@@ -8,6 +8,7 @@
 #include <omp.h>
 #endif
 
+#include "d3.hpp"
 #include "opcount.hpp"
 #include "pes_ch4h.hpp"
 #include "pes_ch4oh.hpp"
@@ -36,6 +37,7 @@ orc::StepConfig to_step(const orc_cfg* c) {
   s.transrot = c->transrot;
   s.seed = c->seed;
   s.mass = c->mass;
+  s.nm_mode = c->nm_mode;
   return s;
 }
 
@@ -172,10 +174,14 @@ void orc_init_positions(const orc_cfg* cf, int ntraj, uint32_t traj0, const doub
     }
 }
 
-void orc_init_momenta(const orc_cfg* cf, int ntraj, uint32_t traj0, double* p) {
+void orc_init_momenta_draw(const orc_cfg* cf, int ntraj, uint32_t traj0, uint32_t draw, double* p) {
   orc::StepConfig s = to_step(cf);
   const size_t per = (size_t)3 * cf->natoms * cf->nbeads;
-  for (int t = 0; t < ntraj; ++t) orc::andersen(s, traj0 + t, 0, orc::TAG_INIT_MOMENTA, &p[t * per]);
+  for (int t = 0; t < ntraj; ++t) orc::andersen(s, traj0 + t, draw, orc::TAG_INIT_MOMENTA, &p[t * per]);
+}
+
+void orc_init_momenta(const orc_cfg* cf, int ntraj, uint32_t traj0, double* p) {
+  orc_init_momenta_draw(cf, ntraj, traj0, 0u, p);
 }
 
 int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, double* epot) {
@@ -404,3 +410,10 @@ int orc_evb_fit(int basis, const double* x, int npar, int m, const double* e1, c
 }
 
 }  // extern "C"
+
+extern "C" void orc_d3_pair_c6(const double* pars, int nlines, int n, const int* at, const double* xyz,
+                               const double* rcov, double* c6xy, double* cn) {
+  orc::D3Ref d;
+  orc::copyc6(pars, nlines, d);
+  orc::pair_c6(d, n, at, xyz, rcov, c6xy, cn);
+}

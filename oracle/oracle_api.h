@@ -25,6 +25,7 @@ typedef struct orc_cfg {
   double pile_tau0;   /* a.u. */
   const double* mass; /* natoms, a.u. */
   double nose_q;      /* a.u.: NOSE_Q (time steps) x dt */
+  int nm_mode;        /* 0: Caracal's cosine transform; 1: orthonormal real normal modes */
 } orc_cfg;
 
 void orc_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]);
@@ -42,6 +43,12 @@ void orc_init_positions(const orc_cfg* cf, int ntraj, uint32_t traj0, const doub
                         double sigma, double* q);
 /* mdinit: Andersen draw at step 0 (tag 0) */
 void orc_init_momenta(const orc_cfg* cf, int ntraj, uint32_t traj0, double* p);
+/* prepare's D3 pair C6 (copyc6 + ncoord_qmdff + getc6) of n atoms at xyz(3, n) bohr:
+ * c6xy (n x n), cn (n) */
+void orc_d3_pair_c6(const double* pars, int nlines, int n, const int* at, const double* xyz,
+                    const double* rcov, double* c6xy, double* cn);
+/* mdinit's Andersen draw number `draw` (Gaussian stream counter; 0 as above) */
+void orc_init_momenta_draw(const orc_cfg* cf, int ntraj, uint32_t traj0, uint32_t draw, double* p);
 /* mdinit: forces of the initial positions; epot[t] = sum over beads */
 int orc_init_forces(const orc_cfg* cf, int ntraj, const double* q, double* f, double* epot);
 /* nsteps verlet steps (istep0+1 .. istep0+nsteps) of ntraj trajectories;

@@ -47,6 +47,7 @@ struct StepConfig {
   int transrot = 1;       // 1: remove COM translation/rotation (constrain <= 0)
   uint32_t seed = 0;
   const double* mass = nullptr;  // natoms, a.u.
+  int nm_mode = 0;        // 0: Caracal's cosine transform; 1: orthonormal real normal modes
 };
 
 constexpr double kPi = 3.1415926535897932384626433832795029;
@@ -70,6 +71,39 @@ inline void caracal_cos_transform(double* x, int P) {
     y[k] = factor * s;
   }
   for (int k = 0; k < P; ++k) x[k] = y[k];
+}
+
+// Orthonormal real normal modes (the RPMD transform Caracal's rfft/irfft are
+// meant to be; not the reference's code path -- an engine option for runs
+// that compare with results of a correct transform): forward y = O x with
+// O[0][j] = 1/sqrt(P), O[k][j] = sqrt(2/P) cos(2 pi j k/P) for 0 < k < P/2,
+// O[P/2][j] = (-1)^j/sqrt(P), O[k][j] = sqrt(2/P) sin(2 pi j k/P) for k > P/2;
+// inverse x = O^T y.  Mode k and P - k share the frequency of poly.
+inline double nm_matrix(int P, int k, int j) {
+  const long long m = ((long long)j * k) % P;
+  const double a = 2.0 * kPi * (double)m / P;
+  if (k == 0) return std::sqrt(1.0 / P);
+  if (2 * k == P) return (j % 2 ? -1.0 : 1.0) * std::sqrt(1.0 / P);
+  if (2 * k < P) return std::sqrt(2.0 / P) * std::cos(a);
+  return std::sqrt(2.0 / P) * std::sin(a);
+}
+inline void nm_forward(double* x, int P) {
+  std::vector<double> y(P, 0.0);
+  for (int k = 0; k < P; ++k) {
+    double s = 0.0;
+    for (int j = 0; j < P; ++j) s += nm_matrix(P, k, j) * x[j];
+    y[k] = s;
+  }
+  for (int k = 0; k < P; ++k) x[k] = y[k];
+}
+inline void nm_inverse(double* x, int P) {
+  std::vector<double> y(P, 0.0);
+  for (int j = 0; j < P; ++j) {
+    double s = 0.0;
+    for (int k = 0; k < P; ++k) s += nm_matrix(P, k, j) * x[k];
+    y[j] = s;
+  }
+  for (int j = 0; j < P; ++j) x[j] = y[j];
 }
 
 // poly(1:4,k) of src/verlet.f90:405-429 for one atom of mass m.
@@ -119,15 +153,25 @@ inline void free_rp_step(const StepConfig& cf, double* q, double* p) {
         vp[k] = p[(k * N + i) * 3 + d];
         vq[k] = q[(k * N + i) * 3 + d] - shift;
       }
-      caracal_cos_transform(vp.data(), P);
-      caracal_cos_transform(vq.data(), P);
+      if (cf.nm_mode == 1) {
+        nm_forward(vp.data(), P);
+        nm_forward(vq.data(), P);
+      } else {
+        caracal_cos_transform(vp.data(), P);
+        caracal_cos_transform(vq.data(), P);
+      }
       for (int k = 0; k < P; ++k) {
         double pn = vp[k] * poly[4 * k + 0] + vq[k] * poly[4 * k + 1];
         vq[k] = vp[k] * poly[4 * k + 2] + vq[k] * poly[4 * k + 3];
         vp[k] = pn;
       }
-      caracal_cos_transform(vp.data(), P);
-      caracal_cos_transform(vq.data(), P);
+      if (cf.nm_mode == 1) {
+        nm_inverse(vp.data(), P);
+        nm_inverse(vq.data(), P);
+      } else {
+        caracal_cos_transform(vp.data(), P);
+        caracal_cos_transform(vq.data(), P);
+      }
       for (int k = 0; k < P; ++k) {
         p[(k * N + i) * 3 + d] = vp[k];
         q[(k * N + i) * 3 + d] = vq[k] + shift;

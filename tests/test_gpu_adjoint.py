@@ -42,7 +42,7 @@ def test_hvp_matches_finite_differences(require_gpu, zahn):
 
 def test_hvp_matches_oracle_finite_differences(require_gpu):
     ff = Q.alkane(nc=3)
-    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
     gff = QMDFFForceField(ff)
     x = thermal(ff, 3, seed=4)
     w = np.random.default_rng(5).normal(0.0, 1.0, x.shape)

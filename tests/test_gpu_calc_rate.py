@@ -1,11 +1,23 @@
-"""GPU: the calc_rate pipeline on H + H2 (umbrella windows, umbrella
-integration, constrained parent, recrossing children, k(T)) on a small
-input: every stage runs and writes Caracal's files with finite values."""
+"""GPU: the calc_rate pipeline on H + H2 (start structures, umbrella windows,
+umbrella integration, constrained parent, recrossing children, k(T)).
+
+* A small case run through the CUDA engine and through the oracle from the
+  same seeds: the profile and kappa(t) agree.
+* The reference's own examples/calc_rate/h+h2/rate.key, unmodified, against
+  the values the reference publishes for it (manual/figures/kappa_h3.png and
+  pmf_h3.png, read off the plots): kappa(t = 50 fs) = 0.767 and a PMF
+  maximum of 48.5 kJ/mol at xi = 1.0.  The tolerance is three jackknife
+  standard errors of this run plus the reading error of the plots
+  (0.005 in kappa, 0.5 kJ/mol in the PMF).
+"""
+import os
+import shutil
+
 import numpy as np
 import pytest
 
 from caracal_gb300.calc_rate import run
-from caracal_gb300.units import BOHR_ANGSTROM
+from conftest import ROOT
 
 pytestmark = pytest.mark.gpu
 
@@ -13,7 +25,7 @@ KEY = """TS_STRUC ts.xyz
 RPMD_BEADS 4
 DELTAT 0.1
 PES ANA_H3
-SEED 11
+RANDOM_SEED 11
 NVT {
  TEMP 300
  THERMOSTAT ANDERSEN
@@ -24,42 +36,76 @@ MECHA {
  REACTANT1 1 2
  REACTANT2 3
  DIST_INF 10.0
- BOND_FORM 2 3
- BOND_BREAK 1 2
+ BOND_FORM 2-3
+ BOND_BREAK 1-2
 }
 UMBRELLA {
- BIAS 0.15
- BONDS -0.05 1.05
+ BIAS 0.005
+ BONDS -0.1 1.1
  DIST 0.1
- GEN_STEPS 100
- EQUI_STEPS 100
- SAMPLE_STEPS 200
+ GEN_STEPS 40
+ EQUI_STEPS 60
+ SAMPLE_STEPS 120
  SAMPLE_TRAJS 2
 }
 PMF {
- XI_RANGE 0.0 1.0
- BINS 50
+ XI_RANGE -0.1 1.1
+ BINS 60
 }
 RECROSS {
- EQUI_STEPS 50
+ EQUI_STEPS 40
  CHILD_TOTAL 8
  CHILD_INTERVAL 20
  CHILD_PERPOINT 4
- CHILD_STEPS 60
+ CHILD_STEPS 50
 }
 """
 
+H_H2 = os.path.join(ROOT, "tests", "golden", "reference", "calc_rate", "h+h2")
 
-def test_calc_rate_h3(require_gpu, tmp_path):
-    # symmetric H-H-H transition state, r = 0.93 Angstrom
+
+def write_inputs(d):
+    """The small case: a symmetric H-H-H transition state (r = 0.93 A)."""
     xyz = np.array([[0.0, 0.0, -0.93], [0.0, 0.0, 0.0], [0.0, 0.0, 0.93]])
-    (tmp_path / "ts.xyz").write_text("3\n\n" + "".join(f"H {a} {b} {c}\n" for a, b, c in xyz))
-    (tmp_path / "calc_rate.key").write_text(KEY)
-    res = run(str(tmp_path / "calc_rate.key"), out_dir=str(tmp_path), quiet=True)
-    pmf = np.loadtxt(tmp_path / "pmf_integration.dat")
-    kap = np.loadtxt(tmp_path / "recross.dat")
-    assert pmf.shape == (49, 2) and np.all(np.isfinite(pmf)) and pmf[:, 1].min() == 0.0
-    assert kap.shape == (60, 2) and np.all(np.isfinite(kap))
-    assert res["windows"] == 12 and res["trajectories"] == 24
-    assert np.isfinite(res["k_t"]) and res["k_t"] > 0.0
-    assert 0.0 < res["kappa"] <= 1.5
+    (d / "ts.xyz").write_text("3\n\n" + "".join(f"H {a} {b} {c}\n" for a, b, c in xyz))
+    (d / "calc_rate.key").write_text(KEY)
+    return str(d / "calc_rate.key")
+
+
+@pytest.mark.parametrize("options", [{}, {"nm_mode": 1, "transrot": False}])
+def test_calc_rate_gpu_matches_oracle(require_gpu, tmp_path, options):
+    from oracle_engine import OracleEngine
+    dg, do = tmp_path / "gpu", tmp_path / "oracle"
+    dg.mkdir()
+    do.mkdir()
+    rg = run(write_inputs(dg), out_dir=str(dg), quiet=True, **options)
+    ro = run(write_inputs(do), out_dir=str(do), quiet=True, engine=OracleEngine, **options)
+    pg, po = np.loadtxt(dg / "pmf_integration.dat"), np.loadtxt(do / "pmf_integration.dat")
+    kg, ko = np.loadtxt(dg / "recross.dat"), np.loadtxt(do / "recross.dat")
+    assert pg.shape == po.shape == (59, 2)
+    # a few hundred steps of chaotic dynamics amplify 1e-16 roundings: 1e-7
+    assert np.max(np.abs(pg[:, 1] - po[:, 1])) <= 1e-7 * max(1.0, np.abs(po[:, 1]).max())
+    assert np.max(np.abs(kg[:, 1] - ko[:, 1])) <= 1e-7
+    assert rg["xi_barrier"] == ro["xi_barrier"]
+    assert rg["k_t"] == pytest.approx(ro["k_t"], rel=1e-6)
+
+
+def test_h_h2_reference_example(require_gpu, tmp_path):
+    """examples/calc_rate/h+h2/rate.key end to end (110 windows x 10 ring
+    polymers x 30 000 steps, 8 beads; 100 parent snapshots x 100 children x
+    500 steps) with the algorithm the published values were made with: the
+    orthonormal normal-mode transform and no COM/rotation removal in the
+    windows.  (Caracal's current source applies its cosine transform and
+    transrot every window step; transrot removes the total angular
+    momentum, which drops the 2 kT ln R rise of the profile.)"""
+    for n in ("rate.key", "ts.xyz"):
+        shutil.copyfile(os.path.join(H_H2, n), tmp_path / n)
+    res = run(str(tmp_path / "rate.key"), out_dir=str(tmp_path), quiet=True, nm_mode=1, transrot=False)
+    kap, kerr = res["kappa_t"][-1], res["kappa_t_stderr"][-1]
+    pmax, perr = res["pmf_max_kjmol"], res["pmf_max_stderr_kjmol"]
+    print(f"kappa(50 fs) = {kap:.4f} +- {kerr:.4f}; PMF max = {pmax:.2f} +- {perr:.2f} kJ/mol "
+          f"at xi = {res['xi_barrier']:.4f}; k(T) = {res['k_t']:.4e} cm^3/mol/s")
+    assert len(res["kappa_t"]) == 500
+    assert abs(kap - 0.767) <= 3.0 * kerr + 0.005
+    assert abs(pmax - 48.5) <= 3.0 * perr + 0.5
+    assert abs(res["xi_barrier"] - 1.0) <= 0.02

@@ -29,7 +29,7 @@ def fields(require_gpu):
 @pytest.mark.parametrize("basis", list(BASES))
 def test_evb_egrad_matches_oracle(fields, basis):
     ff, ff2, g1, g2 = fields
-    orc.set_evb(ff, ff2, Q.ElementTables.d3_like(), basis, BASES[basis])
+    orc.set_evb(ff, ff2, Q.ElementTables.caracal(), basis, BASES[basis])
     pair = EVBPair(g1, g2, basis, **BASES[basis])
     x = ff.xyz[None] + np.random.default_rng(3).normal(0, 0.05, (96,) + ff.xyz.shape)
     e, g = pair.egrad(x, "fp64")
@@ -44,7 +44,7 @@ def test_evb_egrad_matches_oracle(fields, basis):
 def test_evb_engine_matches_oracle(fields):
     ff, ff2, g1, g2 = fields
     par = BASES["1g"]
-    orc.set_evb(ff, ff2, Q.ElementTables.d3_like(), "1g", par)
+    orc.set_evb(ff, ff2, Q.ElementTables.caracal(), "1g", par)
     pair = EVBPair(g1, g2, "1g", **par)
     mass = qmdff_config().mass
     beta, dt = beta_from_kelvin(300.0), dt_fs_to_au(0.5)

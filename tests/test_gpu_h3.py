@@ -23,15 +23,16 @@ MH = mass_au("H")
 
 
 def make_pair(nbeads, ntraj, thermostat="andersen", kelvin=300.0, andersen_step=20,
-              transrot=True, precision="fp64", seed=20261203, dt_fs=0.1):
+              transrot=True, precision="fp64", seed=20261203, dt_fs=0.1, nm_mode=0):
     beta = beta_from_kelvin(kelvin) if kelvin else float("inf")
     dt = dt_fs_to_au(dt_fs)
     tau0 = dt_fs_to_au(100.0)
     eng = RPMDEngine("h3", [MH] * 3, nbeads, ntraj, dt, beta=beta, thermostat=thermostat,
                      andersen_step=andersen_step, pile_tau0_au=tau0, transrot=transrot,
-                     precision=precision, seed=seed)
+                     precision=precision, seed=seed, nm_mode=nm_mode)
     cfg = orc.Config("h3", [MH] * 3, nbeads, dt, beta, thermostat=thermostat,
-                     andersen_step=andersen_step, pile_tau0=tau0, transrot=transrot, seed=seed)
+                     andersen_step=andersen_step, pile_tau0=tau0, transrot=transrot, seed=seed,
+                     nm_mode=nm_mode)
     return eng, cfg
 
 
@@ -108,6 +109,30 @@ def test_100_steps_match_oracle(require_gpu, thermostat, nbeads):
     assert rel_err(qg, qo) <= 1e-9
     assert rel_err(pg, po) <= 1e-9
     assert rel_err(eg, eo) <= 1e-9
+
+
+@pytest.mark.parametrize("thermostat,nbeads", [("andersen", 4), ("andersen", 8), ("pile", 16), ("none", 32),
+                                               ("andersen", 64), ("andersen", 3)])
+def test_orthonormal_modes_match_oracle(require_gpu, thermostat, nbeads):
+    """nm_mode 1 (orthonormal normal modes, the circulant propagator): one
+    step <= 1e-12 and 100 steps <= 1e-9 against the oracle's transform-based
+    restatement."""
+    eng, cfg = make_pair(nbeads, 5, thermostat=thermostat, andersen_step=7, nm_mode=1)
+    q, p, f, e = start(eng, cfg)
+    eng.run(1)
+    qg, pg, _, _, st = eng.get_state()
+    q1, p1, f1, _, so = orc.run(cfg, q, p, f, 1)
+    assert not st.any() and not so.any()
+    assert rel_err(qg, q1) <= 1e-12 and rel_err(pg, p1) <= 1e-12
+    eng.run(99)
+    qg, pg, _, eg, st = eng.get_state()
+    eng.close()
+    qo, po, _, eo, so = orc.run(cfg, q1, p1, f1, 99, istep0=1)
+    assert not st.any() and not so.any()
+    assert rel_err(qg, qo) <= 1e-9 and rel_err(pg, po) <= 1e-9 and rel_err(eg, eo) <= 1e-9
+    # the orthonormal transform keeps beads j and P - j distinct; Caracal's does not
+    if nbeads >= 4:
+        assert np.max(np.abs(qg[:, 1] - qg[:, nbeads - 1])) > 1e-6
 
 
 def test_step_host_equals_device_run(require_gpu):

@@ -67,7 +67,7 @@ def test_nhc_needs_nose_q(require_gpu):
 @pytest.mark.parametrize("nbeads", [4, 8])
 def test_nhc_qmdff_path(require_gpu, nbeads):
     ff = Q.alkane()
-    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
     gff = QMDFFForceField(ff)
     mass = qmdff_config().mass
     dt_fs = 0.5

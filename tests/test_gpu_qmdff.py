@@ -36,7 +36,7 @@ def gpu_ff(alkane, require_gpu):
 
 @pytest.fixture(autouse=True)
 def oracle_ff(alkane):
-    orc.set_qmdff(alkane, Q.ElementTables.d3_like())
+    orc.set_qmdff(alkane, Q.ElementTables.caracal())
 
 
 def geoms(ff, nb, sigma, seed):
@@ -105,7 +105,7 @@ def test_mixed_force_error_within_1e7_on_thermal_ring_polymers(gpu_ff, alkane):
 
 def test_egrad_zahn_matches_oracle(alkane, require_gpu):
     ff = QMDFFForceField(alkane, coul_cut=10.0, zahn=True)
-    orc.set_qmdff(alkane, Q.ElementTables.d3_like(), coul_cut=10.0, zahn=True)
+    orc.set_qmdff(alkane, Q.ElementTables.caracal(), coul_cut=10.0, zahn=True)
     x = geoms(alkane, 64, 0.1, 3)
     e, g = ff.egrad(x, "fp64")
     eo, go = orc.egrad("qmdff", x)
@@ -115,16 +115,17 @@ def test_egrad_zahn_matches_oracle(alkane, require_gpu):
 
 
 def make_pair(gpu_ff, alkane, nbeads, ntraj, thermostat, andersen_step=5, precision="fp64",
-              transrot=True, kelvin=300.0, dt_fs=0.5, seed=77):
+              transrot=True, kelvin=300.0, dt_fs=0.5, seed=77, nm_mode=0):
     mass = qmdff_config().mass
     beta = beta_from_kelvin(kelvin)
     dt = dt_fs_to_au(dt_fs)
     tau0 = dt_fs_to_au(100.0)
     eng = RPMDEngine(gpu_ff, mass, nbeads, ntraj, dt, beta=beta, thermostat=thermostat,
                      andersen_step=andersen_step, pile_tau0_au=tau0, transrot=transrot,
-                     precision=precision, seed=seed)
+                     precision=precision, seed=seed, nm_mode=nm_mode)
     cfg = orc.Config("qmdff", mass, nbeads, dt, beta, thermostat=thermostat,
-                     andersen_step=andersen_step, pile_tau0=tau0, transrot=transrot, seed=seed)
+                     andersen_step=andersen_step, pile_tau0=tau0, transrot=transrot, seed=seed,
+                     nm_mode=nm_mode)
     return eng, cfg
 
 
@@ -163,6 +164,19 @@ def test_single_step_matches_oracle(gpu_ff, alkane, thermostat, nbeads):
     assert rel_err(fg, fo) <= 1e-12
     assert rel_err(eg, eo) <= 1e-12
     assert not st.any() and not sto.any()
+
+
+@pytest.mark.parametrize("thermostat,nbeads", [("andersen", 8), ("pile", 6), ("none", 4)])
+def test_orthonormal_modes_step_matches_oracle(gpu_ff, alkane, thermostat, nbeads):
+    """nm_mode 1 on the graph path (circulant drift of split_drift_kernel)."""
+    eng, cfg = make_pair(gpu_ff, alkane, nbeads, 2, thermostat, andersen_step=3, nm_mode=1)
+    q, p, f, e = start(eng, cfg, alkane)
+    eng.run(5)
+    qg, pg, fg, eg, st = eng.get_state()
+    eng.close()
+    qo, po, fo, eo, sto = orc.run(cfg, q, p, f, 5)
+    assert not st.any() and not sto.any()
+    assert rel_err(qg, qo) <= 1e-11 and rel_err(pg, po) <= 1e-11 and rel_err(eg, eo) <= 1e-11
 
 
 @pytest.mark.parametrize("thermostat,nbeads", [("andersen", 8), ("pile", 6), ("none", 4)])
@@ -256,7 +270,7 @@ def test_hbond_terms_match_oracle(require_gpu, system, tol):
     # rounding differences of the two energies are amplified by 5e5, so their
     # parity bound is 1e-9; hydrogen bonds are analytic (1e-12)
     ff = getattr(Q, system)()
-    tab = Q.ElementTables.d3_like()
+    tab = Q.ElementTables.caracal()
     orc.set_qmdff(ff, tab)
     gff = QMDFFForceField(ff, tab)
     assert gff.schedule_info()["batches"][4] == 1
@@ -288,3 +302,129 @@ def test_qmdff_load_matches_python_reader(require_gpu, tmp_path, which):
         assert np.array_equal(ea, eb) and np.array_equal(ga, gb)
     a.close()
     b.close()
+
+
+# ---- the reference's own QMDFF inputs -------------------------------------
+import os  # noqa: E402
+
+from conftest import ROOT  # noqa: E402
+
+REF = os.path.join(ROOT, "tests", "golden", "reference")
+GLUT = os.path.join(REF, "dynamic", "glutathione")
+EVB = os.path.join(REF, "evbopt", "dE-EVB")
+GLUT_ESHIFT = -1403.0282384116763   # ESHIFT of examples/dynamic/glutathione/glutathione.key
+
+
+@pytest.fixture(scope="module")
+def glutathione():
+    ff = Q.read_qmdff(os.path.join(GLUT, "glutathione.qmdff"))
+    ff.e_zero = GLUT_ESHIFT
+    return ff
+
+
+def test_glutathione_egrad_matches_oracle(require_gpu, glutathione):
+    """examples/dynamic/glutathione/glutathione.qmdff with Caracal's set-up
+    (D3 pair C6 from the coordination numbers of its geometry, 148 H-bond
+    terms): the device force field against the oracle; the library's own
+    reader (cr_qmdff_load_d3) against the Python reader."""
+    ff = glutathione
+    tab = Q.ElementTables.caracal()
+    orc.set_qmdff(ff, tab)
+    gff = QMDFFForceField(ff, tab)
+    x = ff.xyz[None] + np.random.default_rng(21).normal(0, 0.05, (64,) + ff.xyz.shape)
+    x[0] = ff.xyz
+    e, g = gff.egrad(x, "fp64")
+    eo, go = orc.egrad("qmdff", x)
+    assert rel_err(e, eo) <= 1e-12
+    assert rel_err(g, go) <= 1e-12
+    em, gm = gff.egrad(x, "mixed")
+    assert rel_err(gm, g) <= 2e-6
+    ld = QMDFFForceField.load(os.path.join(GLUT, "glutathione.qmdff"), e_zero=GLUT_ESHIFT)
+    el, gl = ld.egrad(x, "fp64")
+    ld.close()
+    gff.close()
+    assert np.array_equal(el, e) and np.array_equal(gl, g)
+
+
+def test_glutathione_nvt_100_steps_matches_oracle(require_gpu, glutathione):
+    """glutathione.key's dynamics (1 bead, NVT 500 K, Nose-Hoover chain with
+    the default NOSE_DAMP 100, dt 1 fs) from start.xyz: 100 steps of 4
+    trajectories against the oracle."""
+    from caracal_gb300 import keyfile as K
+    from caracal_gb300.units import angstrom_to_bohr, mass_au
+    ff = glutathione
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
+    gff = QMDFFForceField(ff)
+    sym, xyz = K.read_xyz(os.path.join(GLUT, "start.xyz"))
+    q0 = angstrom_to_bohr(np.array(xyz))
+    mass = np.array([mass_au(s) for s in sym])
+    dt, beta, nq = dt_fs_to_au(1.0), beta_from_kelvin(500.0), nose_q_to_au(100.0, 1.0)
+    eng = RPMDEngine(gff, mass, 1, 4, dt, beta=beta, thermostat="nhc", nose_q_au=nq, seed=5)
+    eng.init_positions(q0, 0.0)
+    eng.init_momenta()
+    eng.compute_forces()
+    cfg = orc.Config("qmdff", mass, 1, dt, beta, thermostat="nhc", nose_q=nq, seed=5)
+    q = orc.init_positions(cfg, 4, q0, 0.0)
+    p = orc.init_momenta(cfg, 4)
+    f, _ = orc.init_forces(cfg, q)
+    eng.run(60)
+    eng.run(40)
+    qg, pg, fg, eg, st = eng.get_state()
+    eng.close()
+    gff.close()
+    qo, po, fo, eo, sto = orc.run(cfg, q, p, f, 100)
+    assert not st.any() and not sto.any()
+    assert rel_err(qg, qo) <= 1e-9
+    assert rel_err(pg, po) <= 1e-9
+    assert rel_err(eg, eo) <= 1e-9
+
+
+def test_reference_de_evb_example_evaluates(require_gpu):
+    """examples/evbopt/dE-EVB: both QMDFFs (with the ESHIFT energies of
+    evbopt.key) on every reference structure, and the SP-coupling fit
+    residuals and fdjac2 Jacobian at a starting guess, device against
+    oracle."""
+    from caracal_gb300.engine import evb_fit
+    e1s, e2s = -272.22659664700754, -272.16798367875066
+    ff1 = Q.read_qmdff(os.path.join(EVB, "min1.qmdff"))
+    ff2 = Q.read_qmdff(os.path.join(EVB, "min2.qmdff"))
+    ff1.e_zero, ff2.e_zero = e1s, e2s
+    x = Q.read_xyz_frames(os.path.join(EVB, "struc.xyz"))
+    eref = np.loadtxt(os.path.join(EVB, "ref.dat"))
+    tab = Q.ElementTables.caracal()
+    es = []
+    for ff in (ff1, ff2):
+        orc.set_qmdff(ff, tab)
+        gff = QMDFFForceField(ff, tab)
+        e, _ = gff.egrad(x, "fp64")
+        eo, _ = orc.egrad("qmdff", x)
+        gff.close()
+        assert rel_err(e, eo) <= 1e-12
+        es.append(e)
+    par = np.array([0.02, 0.5, 0.01, 0.1])           # SP basis: a, b, c, d
+    fv, fj = evb_fit("sp", par, es[0], es[1], eref)
+    fvo, fjo = orc.evb_fit("sp", par, es[0], es[1], eref)
+    assert rel_err(fv, fvo) <= 1e-12
+    assert rel_err(fj, fjo) <= 1e-9
+    assert np.all(np.isfinite(fv)) and fv.shape == eref.shape
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("mixed", 1e-6)])
+def test_call_site_pieces_sum_to_egrad(require_gpu, glutathione, prec, tol):
+    """cr_qmdff_eg (overwrite) + cr_qmdff_nonb + cr_qmdff_hb (accumulate) +
+    E_zero, the pieces of Caracal's call site (src/gradient.f90:341-358),
+    against the fused cr_qmdff_egrad."""
+    gff = QMDFFForceField(glutathione)
+    x = glutathione.xyz[None] + np.random.default_rng(9).normal(0, 0.05, (16,) + glutathione.xyz.shape)
+    e = np.full(16, np.nan)
+    g = np.full_like(x, np.nan)
+    gff.ff_eg(x, e, g, prec)
+    e_cov = e.copy()
+    gff.ff_nonb(x, e, g, prec)
+    gff.ff_hb(x, e, g, prec)
+    ef, gf = gff.egrad(x, prec)
+    gff.close()
+    assert np.all(np.isfinite(e)) and np.all(np.isfinite(g))
+    assert not np.allclose(e_cov, e)                       # the non-bonded pieces add
+    assert rel_err(e, ef - glutathione.e_zero) <= tol
+    assert rel_err(g, gf) <= tol

@@ -29,7 +29,7 @@ def test_algo_table_matches_oracle_counts():
 def test_qmdff_table_matches_oracle_counts():
     from caracal_gb300 import qmdff as Q
     ff = Q.alkane()
-    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
     x = ff.xyz + np.random.default_rng(0).normal(0, 0.05, ff.xyz.shape)
     counted = {k: v for k, v in orc.pes_opcount("qmdff", x).items() if v and k != "cmp"}
     assert counted == _bench().ALGO_PES_OPS["qmdff"]

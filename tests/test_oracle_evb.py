@@ -23,7 +23,7 @@ BASES = {
 @pytest.fixture(scope="module")
 def pair():
     ff = Q.alkane()
-    return ff, Q.alkane_evb_partner(ff), Q.ElementTables.d3_like()
+    return ff, Q.alkane_evb_partner(ff), Q.ElementTables.caracal()
 
 
 @pytest.mark.parametrize("basis", list(BASES))

@@ -12,7 +12,7 @@ from oracle import oracle as orc
 @pytest.fixture(scope="module")
 def alkane():
     ff = Q.alkane()
-    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
     return ff
 
 
@@ -32,9 +32,9 @@ def test_reference_geometry_is_valence_minimum(alkane):
     # non-bonded pairs contribute: a copy without NCI pairs has E = 0, g = 0
     ff0 = Q.QMDFF(at=ff.at, xyz=ff.xyz, q=ff.q, bond=ff.bond, vbond=ff.vbond, angl=ff.angl,
                   vangl=ff.vangl, tors=ff.tors, vtors=ff.vtors, nci=ff.nci[:0], c6=ff.c6)
-    orc.set_qmdff(ff0, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff0, Q.ElementTables.caracal())
     V, g = orc.egrad("qmdff", ff.xyz)
-    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
     assert abs(V[0]) < 1e-20
     assert np.max(np.abs(g)) < 1e-12
 
@@ -57,13 +57,13 @@ def test_gradient_matches_central_differences(alkane):
 def test_zahn_coulomb_gradient(alkane):
     # NVE form: q q (erfc(a r)/r - par (r - cut)) within 10 bohr
     ff = alkane
-    orc.set_qmdff(ff, Q.ElementTables.d3_like(), coul_cut=10.0, zahn=True)
+    orc.set_qmdff(ff, Q.ElementTables.caracal(), coul_cut=10.0, zahn=True)
     try:
         x = ff.xyz + np.random.default_rng(6).normal(0, 0.05, ff.xyz.shape)
         V, g = orc.egrad("qmdff", x)
         assert np.isfinite(V).all() and np.isfinite(g).all()
     finally:
-        orc.set_qmdff(ff, Q.ElementTables.d3_like())
+        orc.set_qmdff(ff, Q.ElementTables.caracal())
 
 
 def test_qmdff_file_round_trip(alkane, tmp_path):
@@ -82,10 +82,12 @@ def test_qmdff_file_round_trip(alkane, tmp_path):
 
 
 def test_element_tables_real4_literals():
-    t = Q.ElementTables.d3_like()
-    # setnonb's a1 = 0.45 and s8 = 2.7 are REAL(4) literals widened to REAL(8)
+    t = Q.ElementTables.caracal()
+    # setnonb's a1 = 0.45, s8 = 2.7 and the r2r4 array are REAL(4) literals widened to REAL(8)
     s8 = float(np.float32(2.7))
-    assert t.sr42[6, 6] == 3.0 * s8 * Q.R2R4[6] * Q.R2R4[6]
+    r2r4 = Q.element_data()["r2r4"]
+    assert r2r4[5] == float(np.float32(3.10492822))
+    assert t.sr42[6, 6] == 3.0 * s8 * r2r4[5] * r2r4[5]
     assert Q.eps_factors()[0][3] == float(np.float32(0.85))
     r = Q.element_radii()
     assert r.shape == (94,) and r[0] > 0 and r[5] > 0
@@ -95,13 +97,13 @@ def test_hbond_gradient_central_differences():
     # eabhag (src/eabhag.f90) is analytic: its gradient is the derivative of
     # its energy; the synthetic water dimer has one O-H...O triple
     ff = Q.water_dimer()
-    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
     x = ff.xyz + np.random.default_rng(0).normal(0, 0.03, ff.xyz.shape)
     V, g = orc.egrad("qmdff", x)
     ff0 = Q.QMDFF(**{**ff.__dict__, "hb": np.zeros((0, 3), int)})
-    orc.set_qmdff(ff0, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff0, Q.ElementTables.caracal())
     V0, _ = orc.egrad("qmdff", x)
-    orc.set_qmdff(ff, Q.ElementTables.d3_like())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
     assert V[0] < V0[0] - 1e-4          # the H bond is attractive here
     h = 1e-5
     for a in range(ff.n):
@@ -118,7 +120,7 @@ def test_halogen_bond_reproduces_reference_quirk():
     # to the whole 3-vector inside its j loop: every component of each of the
     # three atoms' gradients equals that atom's z quotient
     ff = Q.chloromethane_ammonia()
-    tab = Q.ElementTables.d3_like()
+    tab = Q.ElementTables.caracal()
     x = ff.xyz + np.random.default_rng(1).normal(0, 0.03, ff.xyz.shape)
     orc.set_qmdff(ff, tab)
     _, g = orc.egrad("qmdff", x)

@@ -6,8 +6,10 @@ device-wide synchronisation, or a host whose device memory is a pre-sized
 pool).  Both entry points are called through the C-ABI on the same
 geometries, twice in a row with different sizes so that stale contents of
 the shared device array would show; they must agree within the plain-form
-tolerance used elsewhere (1e-12 norm-wise relative).  This file is collected
-last so a failure here never hides another test's result.
+tolerance used elsewhere (1e-12 norm-wise relative), and both must agree
+with the oracle (the CPU restatement of egrad_h3) to the same tolerance.
+This file is collected last so a failure here never hides another test's
+result.
 """
 import ctypes as C
 
@@ -17,6 +19,7 @@ import pytest
 from caracal_gb300 import _lib as L
 from caracal_gb300.workloads import h3_collinear
 from conftest import rel_err
+from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
@@ -51,9 +54,16 @@ def test_noalloc_matches_allocating_entry_point_twice(require_gpu):
         assert info_a == 0 and info_n == 0
         assert rel_err(V_n, V_a) <= 1e-12
         assert rel_err(g_n, g_a) <= 1e-12
+        sub = slice(0, 256)                  # the oracle on a sample of the geometries
+        V_o, g_o = orc.egrad_h3(q[sub])
+        assert rel_err(V_n[sub], V_o) <= 1e-12
+        assert rel_err(g_n[sub], g_o) <= 1e-12
 
 
 def test_noalloc_rejects_more_than_the_fixed_maximum(require_gpu):
     q = np.zeros((MAX_BEADS + 1, 3, 3))
     rc, _, _, _ = _call(_noalloc_fn(), q)
     assert rc == L.CR_ERR_ARG
+    buf = C.create_string_buffer(512)
+    L.lib().cr_last_error_detail(buf, 512)
+    assert b"fixed maximum" in buf.value
