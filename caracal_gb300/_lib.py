@@ -130,6 +130,7 @@ def _sig(lib):
         "cr_engine_get_state": ([eng, d, d, d, d, i], C.c_int),
         "cr_engine_run": ([eng, C.c_int], C.c_int),
         "cr_engine_run_dump": ([eng, C.c_int, C.c_int, DUMP_FN, v, d, d, d], C.c_int),
+        "cr_engine_run_dump_async": ([eng, C.c_int, C.c_int, DUMP_FN, v], C.c_int),
         "cr_engine_step_host": ([eng, d, d, d, d], C.c_int),
         "cr_engine_last_kernel_ms": ([eng, C.POINTER(C.c_float)], C.c_int),
         "cr_engine_launch_info": ([eng, i, i, i, i], C.c_int),
@@ -178,6 +179,9 @@ def _sig(lib):
         "cr_engine_umbrella_stats": ([eng, d, d, d, C.c_int], C.c_int),
         "cr_engine_mdinit": ([eng, C.c_uint], C.c_int),
         "cr_engine_set_andersen_step": ([eng, C.c_int], C.c_int),
+        "cr_engine_set_launch": ([eng, C.c_int], C.c_int),
+        "cr_engine_get_launch": ([eng, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+        "cr_engine_autotune": ([eng, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)], C.c_int),
         "cr_batch_create": ([C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
         "cr_batch_run": ([v, C.c_int], C.c_int),
         "cr_batch_info": ([v, C.POINTER(C.c_longlong), i, C.POINTER(C.c_float)], C.c_int),

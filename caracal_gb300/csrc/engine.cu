@@ -244,6 +244,13 @@ struct cr_engine {
   // host-buffer step (cr_engine_step_host): trajectory groups whose copies in,
   // step and copies out overlap on separate streams
   cudaStream_t hs_in = nullptr, hs_out = nullptr, hs_c[kHostGroups] = {};
+  // asynchronous trajectory dumps (cr_engine_run_dump_async): two snapshot
+  // slots, each a device copy of q, p, epot and the status words, and its
+  // page-locked host copy
+  cudaStream_t ds = nullptr;
+  char* d_snap[2] = {nullptr, nullptr};
+  char* h_snap[2] = {nullptr, nullptr};
+  cudaEvent_t ev_snap[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
   cudaEvent_t hev_in[kHostGroups] = {}, hev_c[kHostGroups] = {}, hev_out = nullptr;
 };
 
@@ -709,6 +716,19 @@ int dispatch_forces(cr_engine* e) {
     case CR_PES_OH3: return launch_forces<cr::PesOH3>(e);
     default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
   }
+}
+
+// Launch shape for `block` threads per block (a multiple of G, at most 256):
+// false if the group scratch of block/G trajectories does not fit.
+bool set_launch_shape(cr_engine* e, int block) {
+  const int G = e->G;
+  if (block < G || block % G || block > 256) return false;
+  const size_t smem = cr::step_smem_doubles(e->P, G, e->NC, block / G) * sizeof(double);
+  if (smem > 200 * 1024) return false;
+  e->block = block;
+  e->grid = (e->T + block / G - 1) / (block / G);
+  e->smem = smem;
+  return true;
 }
 
 // Launch shape: a tiny batch is latency-bound, so it is spread one warp per
@@ -1214,6 +1234,16 @@ int cr_engine_destroy(cr_engine* e) {
       cudaEventDestroy(e->hev_c[g]);
     }
   }
+  if (e->ds) {
+    cudaStreamSynchronize(e->ds);
+    cudaStreamDestroy(e->ds);
+    for (int k = 0; k < 2; ++k) {
+      cudaFree(e->d_snap[k]);
+      cudaFreeHost(e->h_snap[k]);
+      cudaEventDestroy(e->ev_snap[k]);
+      cudaEventDestroy(e->ev_copied[k]);
+    }
+  }
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return CR_OK;
@@ -1384,6 +1414,82 @@ int cr_engine_run_dump(cr_engine* e, int nsteps, int every, cr_dump_fn dump, voi
     }
   }
   return CR_OK;
+}
+
+// Bytes of one dump snapshot: q and p (T P 3N doubles each), epot (T
+// doubles), the status words (T ints).
+static size_t dump_snapshot_bytes(const cr_engine* e) {
+  return (2 * (size_t)e->T * e->P * e->NC + (size_t)e->T) * sizeof(double) + (size_t)e->T * sizeof(int);
+}
+
+static int dump_slots_init(cr_engine* e) {
+  if (e->ds) return CR_OK;
+  const size_t n = dump_snapshot_bytes(e);
+  CR_CUDA(cudaStreamCreateWithFlags(&e->ds, cudaStreamNonBlocking));
+  for (int k = 0; k < 2; ++k) {
+    CR_CUDA(cudaMalloc(&e->d_snap[k], n));
+    CR_CUDA(cudaMallocHost(&e->h_snap[k], n));
+    CR_CUDA(cudaEventCreateWithFlags(&e->ev_snap[k], cudaEventDisableTiming));
+    CR_CUDA(cudaEventCreateWithFlags(&e->ev_copied[k], cudaEventDisableTiming));
+  }
+  return CR_OK;
+}
+
+int cr_engine_run_dump_async(cr_engine* e, int nsteps, int every, cr_dump_fn dump, void* user) {
+  if (!e || !dump) return fail(CR_ERR_ARG, "NULL argument");
+  if (nsteps < 0 || every < 1) return fail(CR_ERR_ARG, "nsteps must be >= 0 and every >= 1");
+  if (e->xi_on && e->istep + nsteps - e->side_step0 > e->side_cap)
+    return fail(CR_ERR_ARG, "run exceeds the recrossing step capacity set by cr_engine_set_recross");
+  if (nsteps == 0) return CR_OK;
+  int rc = dump_slots_init(e);
+  if (rc) return rc;
+  const size_t nq = (size_t)e->T * e->P * e->NC;
+  const size_t nbytes = dump_snapshot_bytes(e);
+  // hand the host the snapshot of slot k once its copy has landed; a
+  // trajectory that went non-finite by then ends the run before its frame
+  // is written
+  auto deliver = [&](int k, int istep) -> int {
+    CR_CUDA(cudaEventSynchronize(e->ev_copied[k]));
+    const double* h = reinterpret_cast<const double*>(e->h_snap[k]);
+    const int* st = reinterpret_cast<const int*>(h + 2 * nq + e->T);
+    for (int t = 0; t < e->T; ++t)
+      if (st[t]) return fail(CR_ERR_TRAJECTORY, "a trajectory reported a non-finite coordinate or singular inertia");
+    if (dump(user, istep, h, h + nq, h + 2 * nq) != 0) return fail(CR_ERR_ARG, "the dump callback stopped the run");
+    return CR_OK;
+  };
+  int pending = -1, pending_step = 0, slot = 0, done = 0;
+  while (done < nsteps) {
+    const int n = std::min(every - e->istep % every, nsteps - done);
+    if ((rc = engine_run_async(e, n))) return rc;
+    done += n;
+    if (e->istep % every != 0) continue;
+    // snapshot on the engine stream, copy out on the dump stream: the next
+    // steps are queued behind the snapshot while the host writes the frame
+    // before it.  Slot `slot` was last read by the callback two dumps ago,
+    // which returned before this point.
+    char* d = e->d_snap[slot];
+    CR_CUDA(cudaMemcpyAsync(d, e->d_q, nq * 8, cudaMemcpyDeviceToDevice, e->stream));
+    CR_CUDA(cudaMemcpyAsync(d + nq * 8, e->d_p, nq * 8, cudaMemcpyDeviceToDevice, e->stream));
+    CR_CUDA(cudaMemcpyAsync(d + 2 * nq * 8, e->d_epot, (size_t)e->T * 8, cudaMemcpyDeviceToDevice, e->stream));
+    CR_CUDA(cudaMemcpyAsync(d + (2 * nq + e->T) * 8, e->d_status, (size_t)e->T * sizeof(int),
+                            cudaMemcpyDeviceToDevice, e->stream));
+    CR_CUDA(cudaEventRecord(e->ev_snap[slot], e->stream));
+    CR_CUDA(cudaStreamWaitEvent(e->ds, e->ev_snap[slot], 0));
+    CR_CUDA(cudaMemcpyAsync(e->h_snap[slot], d, nbytes, cudaMemcpyDeviceToHost, e->ds));
+    CR_CUDA(cudaEventRecord(e->ev_copied[slot], e->ds));
+    if (pending >= 0 && (rc = deliver(pending, pending_step))) {
+      cudaStreamSynchronize(e->stream);
+      return rc;
+    }
+    pending = slot;
+    pending_step = e->istep;
+    slot ^= 1;
+  }
+  if (pending >= 0 && (rc = deliver(pending, pending_step))) {
+    cudaStreamSynchronize(e->stream);
+    return rc;
+  }
+  return engine_finish(e);
 }
 
 // Trajectory groups of the pipelined host-buffer step: about 2 MB of each
@@ -1688,6 +1794,103 @@ static void drop_graph(cr_engine* e) {
     cudaGraphDestroy(e->graph);
     e->graph = nullptr;
   }
+}
+
+int cr_engine_set_launch(cr_engine* e, int threads_per_block) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (e->split) return fail(CR_ERR_UNSUPPORTED, "this engine steps through the graph path, which has no launch shape to set");
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  if (threads_per_block == 0) {
+    choose_launch(e);
+  } else if (!set_launch_shape(e, threads_per_block)) {
+    return fail(CR_ERR_ARG, "threads_per_block must be a multiple of the bead group (next power of two of nbeads), "
+                            "at most 256, with the group scratch within 200 KB");
+  }
+  drop_graph(e);
+  return CR_OK;
+}
+
+int cr_engine_get_launch(cr_engine* e, int* threads_per_block, int* blocks) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (threads_per_block) *threads_per_block = e->split ? 0 : e->block;
+  if (blocks) *blocks = e->split ? 0 : e->grid;
+  return CR_OK;
+}
+
+int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, float* ms_per_step) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (e->split) return fail(CR_ERR_UNSUPPORTED, "this engine steps through the graph path, which has no launch shape to tune");
+  if (nsteps < 1) return fail(CR_ERR_ARG, "nsteps must be >= 1");
+  if (e->xi_on && e->istep + nsteps - e->side_step0 > e->side_cap)
+    return fail(CR_ERR_ARG, "the trial run exceeds the recrossing step capacity set by cr_engine_set_recross");
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  // every trial starts from the same state: q, p, f, epot, status, the
+  // chain velocities and the step counter are saved and put back after it
+  const size_t nq = (size_t)e->T * e->P * e->NC, T = (size_t)e->T;
+  const size_t nsave = 3 * nq + T + 4 * T;
+  double* save = nullptr;
+  int* save_st = nullptr;
+  CR_CUDA(cudaMalloc(&save, nsave * sizeof(double)));
+  if (cudaMalloc(&save_st, T * sizeof(int)) != cudaSuccess) {
+    cudaFree(save);
+    return fail(CR_ERR_CUDA, "cudaMalloc failed for the autotuner's state copy");
+  }
+  auto copy_state = [&](bool out) -> cudaError_t {
+    double* dst[5] = {save, save + nq, save + 2 * nq, save + 3 * nq, save + 3 * nq + T};
+    double* src[5] = {e->d_q, e->d_p, e->d_f, e->d_epot, e->d_vnh};
+    const size_t n[5] = {nq, nq, nq, T, 4 * T};
+    cudaError_t err = cudaSuccess;
+    for (int k = 0; k < 5 && err == cudaSuccess; ++k)
+      err = cudaMemcpyAsync(out ? dst[k] : src[k], out ? src[k] : dst[k], n[k] * 8, cudaMemcpyDeviceToDevice, e->stream);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(out ? save_st : e->d_status, out ? e->d_status : save_st, T * sizeof(int),
+                            cudaMemcpyDeviceToDevice, e->stream);
+    return err;
+  };
+  const int block0 = e->block, istep0 = e->istep;
+  int best = block0, rc = CR_OK;
+  float best_ms = 0.f;
+  const int cand[] = {e->G, 32, 64, 128, 256};
+  cudaError_t err = copy_state(true);
+  for (int k = 0; k < 5 && rc == CR_OK && err == cudaSuccess; ++k) {
+    const int b = cand[k];
+    bool seen = false;
+    for (int i = 0; i < k; ++i) seen |= cand[i] == b;
+    if (seen || !set_launch_shape(e, b)) continue;
+    // one untimed step (first launch of this shape), then the timed run
+    for (int rep = 0; rep < 2 && rc == CR_OK; ++rep) {
+      if ((rc = engine_run_async(e, rep == 0 ? 1 : nsteps))) break;
+      err = cudaStreamSynchronize(e->stream);
+      if (err != cudaSuccess) break;
+      if (rep == 1) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+        if (best_ms == 0.f || ms < best_ms) {
+          best_ms = ms;
+          best = b;
+        }
+      }
+      e->istep = istep0;
+      if ((err = copy_state(false)) != cudaSuccess) break;
+    }
+  }
+  cudaStreamSynchronize(e->stream);
+  cudaFree(save);
+  cudaFree(save_st);
+  e->istep = istep0;
+  if (rc) {
+    set_launch_shape(e, block0);
+    return rc;
+  }
+  if (err != cudaSuccess) {
+    set_launch_shape(e, block0);
+    return fail(CR_ERR_CUDA, cudaGetErrorString(err));
+  }
+  set_launch_shape(e, best);
+  drop_graph(e);
+  if (threads_per_block) *threads_per_block = best;
+  if (ms_per_step) *ms_per_step = best_ms / nsteps;
+  return CR_OK;
 }
 
 int cr_engine_set_andersen_step(cr_engine* e, int andersen_step) {

@@ -536,7 +536,34 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
     F na[3], nb[3], nan_, nbn, cosphi, sinphi;
     const F phi = dihedral<F>(ra, rb, rc, na, nb, nan_, nbn, cosphi, sinphi);
     const F nenner = nan_ * nbn * sinphi;
-    if (below_1em14(nenner)) {
+    if constexpr (std::is_same<F, float>::value) {
+      // FP32: dphi/dr without the division by sin(phi) of dphidr.f90, whose
+      // numerator cancels as phi -> 0 or pi (planar groups); the same
+      // derivative, written with the plane normals (Blondel and Karplus,
+      // J. Comput. Chem. 17, 1132 (1996)):
+      //   dphi/dr_i = -s |rb| na / |na|^2,  dphi/dr_l = s |rb| nb / |nb|^2,
+      //   dphi/dr_j = -dphi/dr_i + s (u + v),  dphi/dr_k = -dphi/dr_l - s (u + v),
+      //   u = (ra.rb) na / (|na|^2 |rb|),  v = (rc.rb) nb / (|nb|^2 |rb|),
+      // s = sign(na.rc) (phi is the unsigned angle)
+      const float a2 = dot3(na, na), b2 = dot3(nb, nb), tr = dot3(na, rc);
+      const float sg = (tr > 0.f) ? 1.f : ((tr < 0.f) ? -1.f : 0.f);
+      if (!(a2 > 0.f) || !(b2 > 0.f)) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = 0.f;
+      } else {
+        const float L = sqrtf(dot3(rb, rb)), ia2 = __frcp_rn(a2), ib2 = __frcp_rn(b2), iL = __frcp_rn(L);
+        const float fa = sg * L * ia2, fb = sg * L * ib2;
+        const float fu = sg * dot3(ra, rb) * ia2 * iL, fv = sg * dot3(rc, rb) * ib2 * iL;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const float uv = fu * na[d] + fv * nb[d];
+          dda[d] = -fa * na[d];
+          ddd[d] = fb * nb[d];
+          ddb[d] = fa * na[d] + uv;
+          ddc[d] = -fb * nb[d] - uv;
+        }
+      }
+    } else if (below_1em14(nenner)) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = F(0);
     } else {
@@ -669,7 +696,22 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
     for (int d = 0; d < 3; ++d) dda[d] = ddb[d] = ddc[d] = ddd[d] = F(0);
   }
   const F damp = dampjk * dampij * dampX;
-  if (vt[2] > F(1e-6)) {
+  if constexpr (std::is_same<F, float>::value) {
+    // FP32: the differences of cosines as products of sines, cos a - cos b
+    // = -2 sin((a+b)/2) sin((a-b)/2) and 1 - cos a = 2 sin^2(a/2): near
+    // omega = phi0 the reference's forms cancel to a few bits in float,
+    // which the large inversion barriers of planar centres (tens of Eh)
+    // turn into force errors of 1e-6
+    const float h = 0.5f * (om - phi0), sh = sinf(h);
+    if (vt[2] > 1e-6f) {
+      et = 2.f * sh * sh * vt[1];
+      dij = sinf(om - phi0) * vt[1] * damp;
+    } else {
+      const float dd = -2.f * sinf(0.5f * (om + phi0)) * sh;  // cos(om) - cos(phi0)
+      et = vt[1] * (dd * dd);
+      dij = -2.f * vt[1] * sinf(om) * dd * damp;
+    }
+  } else if (vt[2] > F(1e-6)) {
     const F c1 = (om - phi0) + pi;
     et = (F(1) + q_cos<F>(c1)) * vt[1];
     dij = -q_sin<F>(c1) * vt[1] * damp;

@@ -5,7 +5,9 @@ force fields, starts every bead on the input structure with mdinit's momenta
 (src/dynamic.f90:1307-1314, src/mdinit.f90:110-150; READ_VEL: velocity_start.dat),
 advances the engine
 TDUMP/DELTAT steps per launch and writes Caracal's output files at every dump
-step (src/verlet.f90:780-800, 666-676, 1170-1205; src/dynamic.f90:1458-1486, 1676):
+step (src/verlet.f90:780-800, 666-676, 1170-1205; src/dynamic.f90:1458-1486, 1676),
+each frame from a page-locked snapshot while the GPU runs the next steps
+(cr_engine_run_dump_async):
 
   trajectory.xyz       natoms*nbeads, a blank line, `name x y z` (Angstrom) for
                        every bead (not with OUTPUT_SPARSE and nbeads > 1)
@@ -119,31 +121,29 @@ def run(path, out_dir=None, quiet=False):
     if ener:
         ener.write(" #   MD step   pot.energy    kin.energy   total energy \n")
     iw = max(d.iwrite, 1)
-    istep = 0
+
+    def dump(istep, q, p, epot):
+        ekin = float(np.mean(np.sum(p * p / (2.0 * mass[None, None, :, None]), axis=(1, 2, 3))))
+        ep = float(np.mean(epot))
+        if traj:
+            write_frame(traj, names * P, q[0].reshape(-1, 3) * BOHR_ANGSTROM)
+        if cen:
+            write_frame(cen, names, q[0].mean(axis=0) * BOHR_ANGSTROM)
+        if ener:
+            ener.write(fortran_int(istep) + fortran_real(ep / P) + fortran_real(ekin / P) +
+                       fortran_real((ep + ekin) / P) + "\n")
+        if not quiet:
+            if nve:
+                print(f" Step: {istep:8d}  --  pot. energy: {ep / P:12.5f} Hartree ")
+            else:
+                t = temperature_from_ekin(ekin, N, P)
+                print(f" Step: {istep:8d}  --  pot. energy: {ep / P:12.5f} Hartree  --  temperature: "
+                      f"{t:10.4f} K")
+        return False
+
     try:
-        while istep < d.nstep:
-            n = min(iw - istep % iw, d.nstep - istep)
-            eng.run(n)
-            istep += n
-            if istep % iw:
-                continue
-            q, p, f, epot, status = eng.get_state()
-            ekin = float(np.mean(np.sum(p * p / (2.0 * mass[None, None, :, None]), axis=(1, 2, 3))))
-            ep = float(np.mean(epot))
-            if traj:
-                write_frame(traj, names * P, q[0].reshape(-1, 3) * BOHR_ANGSTROM)
-            if cen:
-                write_frame(cen, names, q[0].mean(axis=0) * BOHR_ANGSTROM)
-            if ener:
-                ener.write(fortran_int(istep) + fortran_real(ep / P) + fortran_real(ekin / P) +
-                           fortran_real((ep + ekin) / P) + "\n")
-            if not quiet:
-                if nve:
-                    print(f" Step: {istep:8d}  --  pot. energy: {ep / P:12.5f} Hartree ")
-                else:
-                    t = temperature_from_ekin(ekin, N, P)
-                    print(f" Step: {istep:8d}  --  pot. energy: {ep / P:12.5f} Hartree  --  temperature: "
-                          f"{t:10.4f} K")
+        # frames are written from page-locked snapshots while the GPU steps on
+        eng.run_dump_async(d.nstep, iw, dump)
     finally:
         for fh in (traj, cen, ener):
             if fh:

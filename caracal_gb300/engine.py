@@ -498,6 +498,25 @@ class RPMDEngine:
     def set_andersen_step(self, n):
         L.check(L.lib().cr_engine_set_andersen_step(self._h, int(n)), "set_andersen_step")
 
+    def set_launch(self, threads_per_block=0):
+        """Threads per block of the persistent step kernel (0: built-in choice)."""
+        L.check(L.lib().cr_engine_set_launch(self._h, int(threads_per_block)), "set_launch")
+
+    def launch(self):
+        """(threads per block, blocks) of the persistent step kernel; (0, 0)
+        on the graph path."""
+        b, g = C.c_int(0), C.c_int(0)
+        L.check(L.lib().cr_engine_get_launch(self._h, C.byref(b), C.byref(g)), "get_launch")
+        return b.value, g.value
+
+    def autotune(self, nsteps=20):
+        """Time nsteps steps at each launch shape from the same state (put
+        back afterwards), keep the fastest; returns (threads per block, ms per
+        step)."""
+        b, ms = C.c_int(0), C.c_float(0.0)
+        L.check(L.lib().cr_engine_autotune(self._h, int(nsteps), C.byref(b), C.byref(ms)), "autotune")
+        return b.value, ms.value
+
     def set_state(self, q, p, f=None):
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.shape)
         p = np.ascontiguousarray(p, dtype=np.float64).reshape(self.shape)
@@ -536,6 +555,21 @@ class RPMDEngine:
         fn = L.DUMP_FN(cb)
         L.check(L.lib().cr_engine_run_dump(self._h, int(nsteps), int(every), fn, None, L.dptr(q), L.dptr(p),
                                            L.dptr(e)), "run_dump")
+
+    def run_dump_async(self, nsteps, every, callback):
+        """run_dump with the frames copied out behind the stepping: the GPU
+        runs on while callback(istep, q, p, epot) writes the previous frame.
+        The arrays are views of the library's page-locked snapshot buffers,
+        valid during the call only (copy what must be kept)."""
+        n = int(np.prod(self.shape))
+
+        def cb(_user, istep, q, p, e):
+            qa = np.ctypeslib.as_array(q, shape=(n,)).reshape(self.shape)
+            pa = np.ctypeslib.as_array(p, shape=(n,)).reshape(self.shape)
+            ea = np.ctypeslib.as_array(e, shape=(self.ntraj,))
+            return 1 if callback(istep, qa, pa, ea) else 0
+        fn = L.DUMP_FN(cb)
+        L.check(L.lib().cr_engine_run_dump_async(self._h, int(nsteps), int(every), fn, None), "run_dump_async")
 
     def step_host(self, q, p, f, epot=None):
         """One verlet step through host arrays (modified in place)."""

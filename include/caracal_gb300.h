@@ -376,6 +376,18 @@ int cr_engine_run(cr_engine* e, int nsteps);
 typedef int (*cr_dump_fn)(void* user, int istep, const double* q, const double* p, const double* epot);
 int cr_engine_run_dump(cr_engine* e, int nsteps, int every, cr_dump_fn dump, void* user, double* q, double* p,
                        double* epot);
+/* The same dumps without holding up the stepping (replaces the synchronous
+ * dumps of src/verlet.f90:780-800): at each dump step the state is copied to
+ * one of two device snapshot slots on the engine's stream and from there to
+ * page-locked host memory on a second stream, while the next steps run.
+ * dump() receives a snapshot (pointers into the library's page-locked
+ * buffers, valid during the call) one dump late, so writing frames to disk
+ * overlaps the dynamics; the last snapshot is delivered before the call
+ * returns.  A trajectory whose status word is set by a dump step ends the
+ * run with CR_ERR_TRAJECTORY before that frame is handed over.  The slots
+ * (2 x (2 T P 3N + T) doubles + 2 T ints, device and host) are allocated on
+ * the first call and kept until cr_engine_destroy. */
+int cr_engine_run_dump_async(cr_engine* e, int nsteps, int every, cr_dump_fn dump, void* user);
 
 /* One `verlet` step through host buffers, as a Fortran caller holding
  * q_i, p_i, derivs would use it: copy in, one step, copy out (epot may be NULL). */
@@ -487,6 +499,23 @@ int cr_engine_mdinit(cr_engine* e, unsigned draw);
  * equilibration, int(sqrt(child_interval)) between child batches
  * (src/recross.f90:239-242, 456-458). */
 int cr_engine_set_andersen_step(cr_engine* e, int andersen_step);
+
+/* Launch shape of the persistent step kernel (analytic surfaces; the graph
+ * path of force fields has none and returns CR_ERR_UNSUPPORTED).  A
+ * trajectory's beads sit on G = next_pow2(nbeads) consecutive threads;
+ * threads_per_block (a multiple of G, <= 256) sets how many trajectories
+ * share a block, and so how the batch spreads over the SMs and their four
+ * schedulers.  0 restores the built-in choice (32 threads for a batch of at
+ * most 128 threads per SM, else 128).  No counterpart in the reference,
+ * which steps one trajectory at a time on the host. */
+int cr_engine_set_launch(cr_engine* e, int threads_per_block);
+int cr_engine_get_launch(cr_engine* e, int* threads_per_block, int* blocks);
+/* Autotuner: times nsteps steps at each launch shape (G, 32, 64, 128, 256
+ * threads per block, those that fit), each from the same saved state, which
+ * is then put back (q, p, f, epot, status, chain velocities, step counter);
+ * keeps the fastest and returns it with its time per step.  The noise is a
+ * function of the step index, so the trials leave no trace in the run. */
+int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, float* ms_per_step);
 
 /* ---- batches of trajectory classes -----------------------------------------
  * One graph launch per chunk of steps advances several engines (classes with

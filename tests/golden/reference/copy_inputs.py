@@ -7,6 +7,7 @@ the few files the tests read are committed here, verbatim, by this script:
   calc_rate/h+h2/       rate.key, ts.xyz          (H + H2 rate at 300 K)
   dynamic/glutathione/  glutathione.key, .qmdff, start.xyz
   evbopt/dE-EVB/        evbopt.key, min1/min2.qmdff, ref.dat, struc.xyz
+  explore/ts_irc_ch4oh/ ts.key, irc.key, ts_start.xyz (CH4 + OH saddle and IRC)
 
 Run: python tests/golden/reference/copy_inputs.py [path of the Caracal tree]
 """
@@ -19,6 +20,7 @@ FILES = {
     "calc_rate/h+h2": ["rate.key", "ts.xyz"],
     "dynamic/glutathione": ["glutathione.key", "glutathione.qmdff", "start.xyz"],
     "evbopt/dE-EVB": ["evbopt.key", "min1.qmdff", "min2.qmdff", "ref.dat", "struc.xyz"],
+    "explore/ts_irc_ch4oh": ["ts.key", "irc.key", "ts_start.xyz"],
 }
 
 

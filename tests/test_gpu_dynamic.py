@@ -91,3 +91,42 @@ def test_run_dump_callback(require_gpu):
     with pytest.raises(Exception):
         a.run_dump(40, 5, cb)
     assert seen == [(5, True), (10, True), (15, True)]
+
+
+@pytest.mark.parametrize("kind", ["h3", "qmdff"])
+def test_run_dump_async_frames_match_run_dump(require_gpu, kind):
+    """cr_engine_run_dump_async hands over the same frames at the same steps
+    as the synchronous cr_engine_run_dump and leaves the same final state,
+    on the persistent kernel (H3, 4 beads) and on the graph path of a force
+    field (QMDFF alkane, 8 beads)."""
+    from caracal_gb300.engine import QMDFFForceField
+    kw = dict(beta=beta_from_kelvin(300.0), thermostat="andersen", andersen_step=7, seed=11)
+    if kind == "h3":
+        mass, nb, q0, ffs = [mass_au("H")] * 3, 4, h3_collinear(), [None, None]
+    else:
+        ff = Q.alkane()
+        mass, nb, q0 = [mass_au(Q.SYMBOLS[z - 1]) for z in ff.at], 8, ff.xyz
+        ffs = [QMDFFForceField(ff), QMDFFForceField(ff)]
+    engines = [RPMDEngine(f or "h3", mass, nb, 8, dt_fs_to_au(0.1), **kw) for f in ffs]
+    for e in engines:
+        e.init_positions(q0, 0.01)
+        e.init_momenta()
+        e.compute_forces()
+    frames = ([], [])
+    engines[0].run_dump(23, 4, lambda i, q, p, ep: frames[0].append((i, q.copy(), p.copy(), ep.copy())))
+    engines[1].run_dump_async(23, 4, lambda i, q, p, ep: frames[1].append((i, q.copy(), p.copy(), ep.copy())))
+    assert [f[0] for f in frames[0]] == [4, 8, 12, 16, 20] == [f[0] for f in frames[1]]
+    for a, b in zip(*frames):
+        assert all(np.array_equal(x, y) for x, y in zip(a[1:], b[1:]))
+    sa, sb = engines[0].get_state(), engines[1].get_state()
+    assert all(np.array_equal(x, y) for x, y in zip(sa, sb))
+    # a truthy return stops the run with an error after that frame
+    seen = []
+    with pytest.raises(Exception):
+        engines[1].run_dump_async(20, 2, lambda i, *_: seen.append(i) or len(seen) == 2)
+    assert len(seen) == 2
+    for e in engines:
+        e.close()
+    for f in ffs:
+        if f is not None:
+            f.close()
