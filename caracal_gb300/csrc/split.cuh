@@ -132,7 +132,7 @@ __device__ inline void chunk_normals(const SplitParams& s, uint32_t traj, uint32
     const int j = idx / npair, ip = idx % npair;
     const int c = 2 * ip;
     double z0, z1;
-    normal_pair_f64(s.seed, traj, (uint32_t)((c0 + c) / 2), (uint32_t)j, step, tag, z0, z1);
+    normal_pair(s.seed, traj, (uint32_t)((c0 + c) / 2), (uint32_t)j, step, tag, z0, z1);
     eta[c * sp + j] = z0;
     if (c + 1 < cw) eta[(c + 1) * sp + j] = z1;
   }
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kSplitBlock) split_kick_kernel(SplitParams s, 
       const int j = idx / npair, ip = idx % npair;
       const int c = 2 * ip;
       double z0, z1;
-      normal_pair_f64(s.seed, traj, (uint32_t)((c0 + c) / 2), (uint32_t)j, (uint32_t)istep, TAG_ANDERSEN, z0, z1);
+      normal_pair(s.seed, traj, (uint32_t)((c0 + c) / 2), (uint32_t)j, (uint32_t)istep, TAG_ANDERSEN, z0, z1);
       s.p[tb + (size_t)j * NC + c] = z0 * s.sigma[(c0 + c) / 3];
       if (c + 1 < cw) s.p[tb + (size_t)j * NC + c + 1] = z1 * s.sigma[(c0 + c + 1) / 3];
     }
@@ -845,7 +845,7 @@ __global__ void split_init_positions_kernel(int T, int P, int NC, uint32_t seed,
   const long long b = idx / npair;
   const int t = (int)(b / P), k = (int)(b % P);
   double z0, z1;
-  normal_pair_f64(seed, traj0 + (uint32_t)t, (uint32_t)ip, (uint32_t)k, 0u, TAG_BEAD_JITTER, z0, z1);
+  normal_pair(seed, traj0 + (uint32_t)t, (uint32_t)ip, (uint32_t)k, 0u, TAG_BEAD_JITTER, z0, z1);
   const int c = 2 * ip;
   q[(size_t)b * NC + c] = q0[c] + sigma * z0;
   if (c + 1 < NC) q[(size_t)b * NC + c + 1] = q0[c + 1] + sigma * z1;
@@ -861,7 +861,7 @@ __global__ void split_init_momenta_kernel(int T, int P, int NC, uint32_t seed, u
   const int t = (int)(b / P), k = (int)(b % P);
   const int c = 2 * ip;
   double z0 = 0.0, z1 = 0.0;
-  if (!zero) normal_pair_f64(seed, traj0 + (uint32_t)t, (uint32_t)ip, (uint32_t)k, draw, TAG_INIT_MOMENTA, z0, z1);
+  if (!zero) normal_pair(seed, traj0 + (uint32_t)t, (uint32_t)ip, (uint32_t)k, draw, TAG_INIT_MOMENTA, z0, z1);
   p[(size_t)b * NC + c] = z0 * sig[c / 3];
   if (c + 1 < NC) p[(size_t)b * NC + c + 1] = z1 * sig[(c + 1) / 3];
 }

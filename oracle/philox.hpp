@@ -19,6 +19,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 namespace orc {
 
@@ -64,22 +65,77 @@ enum NoiseTag : uint32_t {
   TAG_CHILD_MOMENTA = 5,  // recrossing child momenta
 };
 
-// Two standard normals for (traj, bead, step, tag, pair).
-inline void normal_pair(uint32_t seed, uint32_t traj, uint32_t pair, uint32_t bead,
-                        uint32_t step, uint32_t tag, double* z0, double* z1) {
-  uint32_t c[4] = {pair, bead, step, tag};
-  Philox4 r = philox4x32_10(c, seed, traj);
-  uint64_t a = ((uint64_t)r.v[1] << 32) | r.v[0];
-  uint64_t b = ((uint64_t)r.v[3] << 32) | r.v[2];
-  double ua = (double)(a >> 11) * 0x1.0p-53;
-  double ub = (double)(b >> 11) * 0x1.0p-53;
-  double rad = std::sqrt(-2.0 * std::log(1.0 - ua));
-  double th = 2.0 * M_PI * ub;
-  *z0 = rad * std::cos(th);
-  *z1 = rad * std::sin(th);
+// Gaussian deviates as the engine draws them: Box-Muller in FP32 on two
+// 24-bit uniforms, with ln and sin/cos as explicit polynomials in single
+// rounded FP32 operations (std::fma where the engine uses an FMA; this file
+// is compiled with -ffp-contract=off), so the deviates match the GPU's bit
+// for bit.  ln m = 2 atanh((m-1)/(m+1)) for m in [sqrt(1/2), sqrt(2)), odd
+// series to t^9; sin/cos by quadrant and Taylor series to theta^9 / theta^10.
+inline float bm_log(float u) {
+  int32_t i;
+  std::memcpy(&i, &u, 4);
+  int e = ((i >> 23) & 0xff) - 127;
+  const int32_t mb = (i & 0x7fffff) | 0x3f800000;
+  float m;
+  std::memcpy(&m, &mb, 4);
+  if (m > 0x1.6a09e6p+0f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float t = (m - 1.f) / (m + 1.f);
+  const float t2 = t * t;
+  float p = std::fma(t2, 0x1.c71c72p-4f, 0x1.24924ap-3f);
+  p = std::fma(t2, p, 0x1.99999ap-3f);
+  p = std::fma(t2, p, 0x1.555556p-2f);
+  p = std::fma(t2, p, 1.f);
+  const float lnm = (2.f * t) * p;
+  const float fe = (float)e;
+  return std::fma(fe, 0x1.62ep-1f, std::fma(fe, 0x1.0bfbe8p-15f, lnm));
 }
 
-// Normals for all 3*natoms coordinates of one bead.
+inline void bm_sincos2pi(float v, float* sn, float* cs) {
+  const float x = 4.f * v;
+  const int q = (int)std::nearbyint(x);
+  const float th = (x - (float)q) * 0x1.921fb6p+0f;
+  const float t2 = th * th;
+  float ps = std::fma(t2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
+  ps = std::fma(t2, ps, 0x1.111112p-7f);
+  ps = std::fma(t2, ps, -0x1.555556p-3f);
+  const float s = std::fma(th * t2, ps, th);
+  float pc = std::fma(t2, -0x1.27e4fcp-22f, 0x1.a01a02p-16f);
+  pc = std::fma(t2, pc, -0x1.6c16c2p-10f);
+  pc = std::fma(t2, pc, 0x1.555556p-5f);
+  pc = std::fma(t2, pc, -0.5f);
+  const float c = std::fma(t2, pc, 1.f);
+  switch (q & 3) {
+    case 0: *sn = s; *cs = c; break;
+    case 1: *sn = c; *cs = -s; break;
+    case 2: *sn = -s; *cs = -c; break;
+    default: *sn = -c; *cs = s; break;
+  }
+}
+
+inline void bm_pair(uint32_t wa, uint32_t wb, double* z0, double* z1) {
+  const float u = (float)((wa >> 8) + 1u) * 0x1.0p-24f;
+  const float v = (float)(wb >> 8) * 0x1.0p-24f;
+  const float rad = std::sqrt(-2.f * bm_log(u));
+  float sn, cs;
+  bm_sincos2pi(v, &sn, &cs);
+  *z0 = (double)(rad * cs);
+  *z1 = (double)(rad * sn);
+}
+
+// Deviates 2 pair and 2 pair + 1 of (traj, bead, step, tag); Philox block
+// pair / 2, words 0-1 for an even pair, 2-3 for an odd one.
+inline void normal_pair(uint32_t seed, uint32_t traj, uint32_t pair, uint32_t bead,
+                        uint32_t step, uint32_t tag, double* z0, double* z1) {
+  uint32_t c[4] = {pair >> 1, bead, step, tag};
+  Philox4 r = philox4x32_10(c, seed, traj);
+  if (pair & 1u) bm_pair(r.v[2], r.v[3], z0, z1);
+  else bm_pair(r.v[0], r.v[1], z0, z1);
+}
+
+// Deviates for all 3*natoms coordinates of one bead (coordinate c = deviate c).
 inline void normals_bead(uint32_t seed, uint32_t traj, uint32_t bead, uint32_t step,
                          uint32_t tag, int ncoord, double* z) {
   for (int i = 0; 2 * i < ncoord; ++i) {

@@ -22,7 +22,7 @@ def test_parse_calc_rate_key():
     assert (r.nbeads, r.pes, r.kelvin, r.andersen_step) == (4, "ANA_H3", 300.0, 20)
     assert (r.reac1, r.reac2, r.bond_form, r.bond_break) == ([1, 2], [3], (2, 3), (1, 2))
     assert r.r_inf == 10.0 / BOHR_ANGSTROM        # DIST_INF is read in Angstrom
-    assert (r.bias, r.umbr_lo, r.umbr_hi, r.umbr_dist) == (0.005, -0.1, 1.1, 0.1)
+    assert (r.bias, r.umbr_lo, r.umbr_hi, r.umbr_dist) == (0.05, -0.1, 1.1, 0.1)
     assert (r.gen_steps, r.equi_steps, r.sample_steps, r.sample_trajs) == (40, 60, 120, 2)
     assert (r.xi_lo, r.xi_hi, r.nbins) == (-0.1, 1.1, 60)
     assert (r.rc_equi, r.child_total, r.child_interval, r.child_perpoint, r.child_steps) == (40, 8, 20, 4, 50)

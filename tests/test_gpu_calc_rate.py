@@ -40,7 +40,7 @@ MECHA {
  BOND_BREAK 1-2
 }
 UMBRELLA {
- BIAS 0.005
+ BIAS 0.05
  BONDS -0.1 1.1
  DIST 0.1
  GEN_STEPS 40
@@ -109,3 +109,18 @@ def test_h_h2_reference_example(require_gpu, tmp_path):
     assert abs(kap - 0.767) <= 3.0 * kerr + 0.005
     assert abs(pmax - 48.5) <= 3.0 * perr + 0.5
     assert abs(res["xi_barrier"] - 1.0) <= 0.02
+    # the whole curves of the manual's figures (digitised, reading error
+    # ~0.001 in kappa and ~0.1 kJ/mol on flat parts): kappa(t) within 3
+    # standard errors of this run at each time, the PMF along xi within 3
+    # standard errors of its maximum (the integrated error grows with xi)
+    fk = np.loadtxt(os.path.join(ROOT, "tests", "golden", "reference", "figure_kappa_h3.txt"))
+    fp = np.loadtxt(os.path.join(ROOT, "tests", "golden", "reference", "figure_pmf_h3.txt"))
+    dt_fs = 0.1
+    for t in (5.0, 10.0, 20.0, 30.0, 40.0):
+        i = int(round(t / dt_fs)) - 1
+        want = np.interp(t, fk[:, 0], fk[:, 1])
+        assert abs(res["kappa_t"][i] - want) <= 3.0 * res["kappa_t_stderr"][i] + 0.005, (t, res["kappa_t"][i], want)
+    for xi in (0.2, 0.4, 0.6, 0.8, 0.9):
+        got = np.interp(xi, res["coord"], res["pmf_kjmol"])
+        want = np.interp(xi, fp[:, 0], fp[:, 1])
+        assert abs(got - want) <= 3.0 * perr + 0.5, (xi, got, want)

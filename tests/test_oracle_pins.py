@@ -30,9 +30,28 @@ def test_philox_known_answers():
 
 
 def test_normals_are_standard():
-    z = np.array([orc.normal_pair(7, t, i, b, 3, 1) for t in range(20) for i in range(5)
-                  for b in range(20)]).ravel()
-    assert abs(z.mean()) < 0.05 and abs(z.std() - 1.0) < 0.05
+    z = np.array([orc.normal_pair(7, t, i, b, 3, 1) for t in range(40) for i in range(10)
+                  for b in range(40)]).ravel()
+    n = len(z)
+    assert abs(z.mean()) < 4 / np.sqrt(n) and abs(z.var() - 1.0) < 5 * np.sqrt(2.0 / n)
+    assert abs(np.mean(z ** 4) - 3.0) < 5 * np.sqrt(96.0 / n)          # Gaussian kurtosis
+
+
+def test_normals_follow_box_muller_of_the_philox_words():
+    """Each deviate pair is Box-Muller of 24-bit uniforms from two Philox
+    words: u = (w0 >> 8) + 1, v = w1 >> 8 (times 2^-24); the FP32 polynomial
+    log and sin/cos agree with FP64 libm to a few float ulps."""
+    worst = 0.0
+    for pair in range(64):
+        w = orc.philox([pair >> 1, 5, 9, 2], 11, 3)
+        wa, wb = (w[2], w[3]) if pair & 1 else (w[0], w[1])
+        u = ((wa >> 8) + 1) * 2.0 ** -24
+        v = (wb >> 8) * 2.0 ** -24
+        r = np.sqrt(-2.0 * np.log(u))
+        ref = np.array([r * np.cos(2 * np.pi * v), r * np.sin(2 * np.pi * v)])
+        z = orc.normal_pair(11, 3, pair, 5, 9, 2)
+        worst = max(worst, np.abs(z - ref).max() / max(1.0, r))
+    assert worst < 1e-6
 
 
 def test_bkmp2_published_properties():
