@@ -59,7 +59,8 @@ TRANSCENDENTALS = ("exp", "log", "pow", "sin", "cos", "acos", "erf", "tanh", "co
 
 
 def algo_flops_per_bead_step(pes, natoms, nbeads, thermostat, w, transrot=True, recross=False):
-    """Algorithmic FP work of one bead-step, (FP64 part, PES part) in flops.
+    """Algorithmic FP work of one bead-step, (FP64 part, PES part, Gaussian
+    pairs drawn) in flops and pairs.
 
     Counting: add, mul, div and sqrt are 1 flop each (as counted in the
     reference formulas by the oracle's op-counting instantiation);
@@ -69,8 +70,10 @@ def algo_flops_per_bead_step(pes, natoms, nbeads, thermostat, w, transrot=True, 
     Caracal's propagator as four length-P real FFTs per coordinate
     (2.5 P log2 P flops each) plus the 2x2 mode update (6 flops), two half
     kicks (4 flops per coordinate), transrot (30 flops per coordinate), PILE
-    (per half step two FFT pairs and the Gaussian draws), and for recrossing
-    children the centroid and xi (3 flops per coordinate).
+    (per half step two FFT pairs), and for recrossing children the centroid
+    and xi (3 flops per coordinate).  The Gaussian deviates (Box-Muller: a
+    log, a sqrt, a sine and a cosine per pair) run in FP32 in both forms and
+    are returned as a pair count, weighted on the FP32 pipe by the caller.
     """
     ops = ALGO_PES_OPS[pes]
     pes_f = sum(ops.get(k, 0) for k in ("add", "mul", "div", "sqrt"))
@@ -80,14 +83,15 @@ def algo_flops_per_bead_step(pes, natoms, nbeads, thermostat, w, transrot=True, 
     f64 = nc * (4 * 2.5 * lg + 6) + nc * 4
     if transrot:
         f64 += nc * 30
+    pairs = 0.0
     if thermostat == "andersen":
-        # a full resample every ANDERSEN_STEP steps (70): the Gaussian draws
-        f64 += (nc / 2) * (w["log"] + 1 + w["sin"] + w["cos"]) / 70.0
+        pairs = (nc / 2) / 70.0      # a full resample every ANDERSEN_STEP steps (70)
     if thermostat == "pile":
-        f64 += 2 * (nc * (2 * 2 * 2.5 * lg + 4) + (nc / 2) * (w["log"] + 1 + w["sin"] + w["cos"]))
+        f64 += 2 * nc * (2 * 2 * 2.5 * lg + 4)
+        pairs = 2 * (nc / 2)
     if recross:
         f64 += nc * 3
-    return f64, pes_f
+    return f64, pes_f, pairs
 
 
 def roofline(wl, mixed, ms, K, cal):
@@ -101,16 +105,17 @@ def roofline(wl, mixed, ms, K, cal):
     w64, w32 = cal["fp64"]["w"], cal["fp32"]["w"]
     n = len(wl.mass)
     rec = wl.extra.get("recross") is not None
-    f64, pes64 = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w64, wl.transrot, rec)
-    _, pes32 = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w32, wl.transrot, rec)
+    f64, pes64, pairs = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w64, wl.transrot, rec)
+    _, pes32, _ = algo_flops_per_bead_step(wl.pes, n, wl.nbeads, wl.thermostat, w32, wl.transrot, rec)
     p64, p32 = cal["fp64"]["peak_tflops"], cal["fp32"]["peak_tflops"]
+    draws32 = pairs * (w32["log"] + 1 + w32["sin"] + w32["cos"])   # FP32 Box-Muller, both forms
     units = wl.ntraj * wl.nbeads * K
     step = "step graph" if wl.pes in ("qmdff", "water") else "rpmd_run_kernel"
     if mixed:
-        eq = f64 + pes32 * p64 / p32
+        eq = f64 + (pes32 + draws32) * p64 / p32
         kern, bound = f"{step}<{wl.pes}, mixed>", "fp64+fp32 (FP64-equivalent)"
     else:
-        eq = f64 + pes64
+        eq = f64 + pes64 + draws32 * p64 / p32
         kern, bound = f"{step}<{wl.pes}, fp64>", "fp64"
     ach = eq * units / (ms * 1e-3) / 1e12
     return {"kernel": kern, "bound": bound, "achieved": ach, "peak": p64, "unit": "TFLOP/s",
@@ -118,7 +123,7 @@ def roofline(wl, mixed, ms, K, cal):
             "peak_source": "measured in this run (FP64/FP32 FMA microbenchmarks, cr_calibrate_op); "
                            "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
             "algo_flops_per_bead_step": {"fp64": f64, "pes_fp64": pes64, "pes_fp32": pes32,
-                                         "fp64_equivalent": eq}}
+                                         "gaussian_fp32": draws32, "fp64_equivalent": eq}}
 
 
 class ClockSampler:
@@ -398,6 +403,13 @@ def run_ours(args):
     cal = calibrate(L)
     eng_mx = make_engine(wl, "mixed", traj0=rank * wl.ntraj, max_steps=cap)
     eng_64 = make_engine(wl, "fp64", traj0=rank * wl.ntraj, max_steps=cap)
+    # the launch-shape autotuner (threads per block and per bead) of the
+    # persistent kernel, before any timing; it puts the state back
+    tuned = {}
+    if wl.pes not in ("qmdff", "water"):
+        for name, eng in (("mixed", eng_mx), ("fp64", eng_64)):
+            b, tpb, ms = eng.autotune(min(max(K, 10), 50))
+            tuned[name] = {"threads_per_block": b, "threads_per_bead": tpb, "trial_ms_per_step": ms}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def timed_run(eng):
@@ -523,6 +535,9 @@ def run_ours(args):
         kappa = {"steps": len(num), "kappa_last": float(num[-1] / den) if den else None,
                  "children": ws * wl.ntraj}
     info = eng_mx.launch_info()
+    if tuned:
+        info["threads_per_bead"] = eng_mx.launch()[2]
+        info["autotuned"] = tuned
     line = {
         "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": ws, "steps": K,
         "warmup": W, "ms_per_step": ms_mx / K, "higher_is_better": True, "scaling": "weak",
@@ -654,6 +669,7 @@ def run_classes(args):
             b.run(K)
         torch.cuda.synchronize()
         info = b.info()
+        info["timeline"] = b.timeline()
         b.close()
         return maxr(info["ms"]), info
 
@@ -691,35 +707,56 @@ def run_classes(args):
                           "separate_fp64": ws * units[i] / (per_64[i] * 1e-3),
                           "force_error_vs_fp64": ferr})
 
-    # end to end through the public API: every step the host state of every
-    # class goes in (set_state), the batch steps once, the state comes out
-    b = RPMDBatch(engs["mixed"], chunk_steps=1)
-    states = [e.get_state() for e in engs["mixed"]]
-    K_e2e = min(K, args.e2e_steps // 10 or 1)
-    b.run(1)
+    # end to end through the C-ABI each class's caller would use: every step
+    # one cr_engine_step_host per class on its page-locked q, p, f (the
+    # copies in and out of each class overlap with its own trajectory
+    # groups' steps)
+    import ctypes as C
+    pinned, hostbufs = [], []
+    for wl, eng in zip(classes, engs["mixed"]):
+        shape = (wl.ntraj, wl.nbeads, len(wl.mass), 3)
+        nb = int(np.prod(shape)) * 8
+        arrs = []
+        for _ in range(3):
+            ptr = C.c_void_p()
+            L.check(L.lib().cr_host_alloc(C.byref(ptr), nb), "host_alloc")
+            pinned.append(ptr)
+            arrs.append(np.ctypeslib.as_array((C.c_double * (nb // 8)).from_address(ptr.value)).reshape(shape))
+        q, p, f, e, st = eng.get_state()
+        arrs[0][...], arrs[1][...], arrs[2][...] = q, p, f
+        hostbufs.append(arrs + [np.zeros(wl.ntraj)])
+    K_e2e = min(K, max(1, args.e2e_steps // 10))
+    for eng, (hq, hp, hf, he) in zip(engs["mixed"], hostbufs):
+        eng.step_host(hq, hp, hf, he)
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(K_e2e):
-        for e, (q, p, f, _, _) in zip(engs["mixed"], states):
-            e.set_state(q, p, f)
-        b.run(1)
-        states = [e.get_state() for e in engs["mixed"]]
+        for eng, (hq, hp, hf, he) in zip(engs["mixed"], hostbufs):
+            eng.step_host(hq, hp, hf, he)
     el = maxr(time.perf_counter() - t0)
-    b.close()
+    for ptr in pinned:
+        L.lib().cr_host_free(ptr)
     nbytes = sum(wl.ntraj * wl.nbeads * len(wl.mass) * 3 * 8 for wl in classes)
     e2e = ws * sum(wl.ntraj * wl.nbeads for wl in classes) * K_e2e / el
+    # concurrency of the classes inside one graph launch: the sum of the
+    # branches' busy intervals over the span they cover (> 1: overlap)
+    tl = info_mx["timeline"]
+    span = max(e for _, e in tl) - min(b for b, _ in tl)
+    busy = sum(e - b for b, e in tl)
 
     # roofline: the classes' algorithmic flops over the batched launch time
     p64, p32 = cal["fp64"]["peak_tflops"], cal["fp32"]["peak_tflops"]
     eq_mx = eq_64 = 0.0
     for wl, u in zip(classes, units):
-        f64, pes64 = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat,
-                                              cal["fp64"]["w"], wl.transrot)
-        _, pes32 = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat,
-                                            cal["fp32"]["w"], wl.transrot)
-        eq_mx += (f64 + pes32 * p64 / p32) * u
-        eq_64 += (f64 + pes64) * u
+        f64, pes64, pairs = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat,
+                                                     cal["fp64"]["w"], wl.transrot)
+        _, pes32, _ = algo_flops_per_bead_step(wl.pes, len(wl.mass), wl.nbeads, wl.thermostat,
+                                               cal["fp32"]["w"], wl.transrot)
+        w32 = cal["fp32"]["w"]
+        draws = pairs * (w32["log"] + 1 + w32["sin"] + w32["cos"]) * p64 / p32
+        eq_mx += (f64 + pes32 * p64 / p32 + draws) * u
+        eq_64 += (f64 + pes64 + draws) * u
     ach = eq_mx / (ms_mx * 1e-3) / 1e12
     ach64 = eq_64 / (ms_64 * 1e-3) / 1e12
     line = {
@@ -736,7 +773,12 @@ def run_classes(args):
         "mixed_over_plain": ms_64 / ms_mx,
         "per_class": per_class,
         "e2e": {"value": e2e, "unit": "bead-steps/s", "steps": K_e2e, "h2d_bytes_per_step": 3 * nbytes,
-                "d2h_bytes_per_step": 3 * nbytes + sum(8 * wl.ntraj + 4 * wl.ntraj for wl in classes)},
+                "d2h_bytes_per_step": 3 * nbytes + sum(8 * wl.ntraj for wl in classes),
+                "path": "cr_engine_step_host per class, page-locked q, p, f"},
+        "graph_timeline_ms": {"per_class": [{"workload": wl.name, "begin": b0, "end": b1}
+                                            for wl, (b0, b1) in zip(classes, tl)],
+                              "busy_over_span": busy / span if span > 0 else None,
+                              "note": "one chunk's graph launch: each class branch's first and last node"},
         "gpu_launches": info_mx["launches"],
         "launch": {"graph_kernels_per_chunk": info_mx["graph_nodes"], "chunk_steps": args.chunk},
         "roofline": {"kernel": "cr_batch graph<mixed>", "bound": "fp64+fp32 (FP64-equivalent)",

@@ -146,6 +146,7 @@ def _sig(lib):
         "cr_engine_kappa": ([eng, d, d, d, i], C.c_int),
         "cr_engine_set_parent": ([eng, C.POINTER(CrRecross)], C.c_int),
         "cr_qmdff_create": ([C.POINTER(CrQmdffDef), C.POINTER(C.c_void_p)], C.c_int),
+        "cr_qmdff_set_periodic": ([v, d, C.c_double, C.c_double, d], C.c_int),
         "cr_qmdff_destroy": ([v], C.c_int),
         "cr_qmdff_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
         "cr_qmdff_egrad_device": ([v, v, C.c_int, v, v, C.c_int, v], C.c_int),
@@ -179,12 +180,14 @@ def _sig(lib):
         "cr_engine_umbrella_stats": ([eng, d, d, d, C.c_int], C.c_int),
         "cr_engine_mdinit": ([eng, C.c_uint], C.c_int),
         "cr_engine_set_andersen_step": ([eng, C.c_int], C.c_int),
-        "cr_engine_set_launch": ([eng, C.c_int], C.c_int),
-        "cr_engine_get_launch": ([eng, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
-        "cr_engine_autotune": ([eng, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)], C.c_int),
+        "cr_engine_set_launch": ([eng, C.c_int, C.c_int], C.c_int),
+        "cr_engine_get_launch": ([eng, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+        "cr_engine_autotune": ([eng, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)],
+                               C.c_int),
         "cr_batch_create": ([C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
         "cr_batch_run": ([v, C.c_int], C.c_int),
         "cr_batch_info": ([v, C.POINTER(C.c_longlong), i, C.POINTER(C.c_float)], C.c_int),
+        "cr_batch_timeline": ([v, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
         "cr_batch_destroy": ([v], C.c_int),
         "cr_water_create": ([C.POINTER(CrWaterDef), C.POINTER(C.c_void_p)], C.c_int),
         "cr_water_destroy": ([v], C.c_int),

@@ -10,10 +10,7 @@
 
 #include "../../include/caracal_gb300.h"
 #include "cr_common.cuh"
-#include "pes_ch4h.cuh"
-#include "pes_ch4oh.cuh"
-#include "pes_h3.cuh"
-#include "pes_oh3.cuh"
+#include "pes_runs.h"
 #include "rpmd_kernel.cuh"
 #include "host_util.h"
 #include "qmdff_host.h"
@@ -93,22 +90,6 @@ __global__ void init_momenta_kernel(int T, int P, uint32_t seed, uint32_t traj0,
   normals_bead<NC>(seed, traj0 + t, (uint32_t)k, draw, TAG_INIT_MOMENTA, z);
 #pragma unroll
   for (int c = 0; c < NC; ++c) p[(size_t)idx * NC + c] = z[c] * prm.sigma[c / 3];
-}
-
-// One thread per bead: V and dV/dq.
-template <class PES, bool MIXED>
-__global__ void egrad_kernel(int nbeads_total, const double* q, double* V, double* g) {
-  constexpr int NC = 3 * PES::N;
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbeads_total) return;
-  double qq[NC], gg[NC], v;
-#pragma unroll
-  for (int c = 0; c < NC; ++c) qq[c] = q[(size_t)b * NC + c];
-  if (MIXED) PES::template egrad<float>(qq, v, gg);
-  else PES::template egrad<double>(qq, v, gg);
-  V[b] = v;
-#pragma unroll
-  for (int c = 0; c < NC; ++c) g[(size_t)b * NC + c] = gg[c];
 }
 
 // Recrossing children (src/recross.f90:540-561): q = parent ring polymer,
@@ -197,6 +178,7 @@ struct cr_engine {
   std::vector<double> mass;
   int N = 0, NC = 0, P = 0, T = 0, G = 1, H = 1;
   int block = 32, grid = 1;
+  int tpb = 1;  // threads per bead of the persistent step kernel
   size_t smem = 0;
   int istep = 0;
   int launches = 0;
@@ -390,20 +372,18 @@ void build_pile(int P, double beta, double dt, double tau0, std::vector<double>&
 // from the device counter, which a second launch then advances (so the pair
 // can be replayed from a graph); the shared-memory limit is then set by the
 // caller before the capture.
-template <class PES>
 int launch_run(cr_engine* e, int nsteps, bool dev_step = false) {
-  auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
-                                                  : cr::rpmd_run_kernel<PES, false>;
+  const cr::PesRuns* r = cr::pes_runs(e->cfg.pes);
+  if (!r) return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  const bool mixed = e->cfg.precision == CR_PREC_MIXED;
   if (!dev_step) {
-    CR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
-    kern<<<e->grid, e->block, e->smem, e->stream>>>(e->prm, e->istep, nsteps);
-    CR_CUDA(cudaGetLastError());
+    CR_CUDA(r->set_smem(mixed, e->tpb, e->smem));
+    CR_CUDA(r->run(e->prm, mixed, e->tpb, e->grid, e->block, e->smem, e->stream, e->istep, nsteps));
     return CR_OK;
   }
   cr::StepParams prm = e->prm;
   prm.istep_dev = e->d_istep;
-  kern<<<e->grid, e->block, e->smem, e->stream>>>(prm, 0, nsteps);
-  CR_CUDA(cudaGetLastError());
+  CR_CUDA(r->run(prm, mixed, e->tpb, e->grid, e->block, e->smem, e->stream, 0, nsteps));
   cr::advance_by_kernel<<<1, 1, 0, e->stream>>>(e->d_istep, nsteps);
   CR_CUDA(cudaGetLastError());
   return CR_OK;
@@ -412,10 +392,9 @@ int launch_run(cr_engine* e, int nsteps, bool dev_step = false) {
 // One step of trajectories [t0, t0 + tn) by the persistent kernel on stream
 // st (the shared-memory limit is set by the caller): per-trajectory arrays
 // offset, the noise key of trajectory t0, the step index from the host.
-template <class PES>
 int launch_group(cr_engine* e, int t0, int tn, cudaStream_t st) {
-  auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
-                                                  : cr::rpmd_run_kernel<PES, false>;
+  const cr::PesRuns* r = cr::pes_runs(e->cfg.pes);
+  if (!r) return fail(CR_ERR_UNSUPPORTED, "PES not built");
   cr::StepParams prm = e->prm;
   const size_t off = (size_t)t0 * e->P * e->NC;
   prm.istep_dev = nullptr;
@@ -428,43 +407,34 @@ int launch_group(cr_engine* e, int t0, int tn, cudaStream_t st) {
   prm.status += t0;
   prm.vnh += 4 * (size_t)t0;
   if (prm.side) prm.side += (size_t)t0 * prm.side_stride;
-  const int groups = e->block / e->G;
-  kern<<<(tn + groups - 1) / groups, e->block, e->smem, st>>>(prm, e->istep, 1);
-  CR_CUDA(cudaGetLastError());
+  const int groups = e->block / (e->G * e->tpb);
+  CR_CUDA(r->run(prm, e->cfg.precision == CR_PREC_MIXED, e->tpb, (tn + groups - 1) / groups, e->block, e->smem, st,
+                 e->istep, 1));
   return CR_OK;
 }
 
-template <class PES>
 int set_run_smem(cr_engine* e) {
-  auto kern = (e->cfg.precision == CR_PREC_MIXED) ? cr::rpmd_run_kernel<PES, true>
-                                                  : cr::rpmd_run_kernel<PES, false>;
-  CR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem));
+  const cr::PesRuns* r = cr::pes_runs(e->cfg.pes);
+  if (!r) return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  CR_CUDA(r->set_smem(e->cfg.precision == CR_PREC_MIXED, e->tpb, e->smem));
   return CR_OK;
 }
 
-template <class PES>
 int launch_forces(cr_engine* e) {
-  const int nb = e->T * e->P;
-  const int bs = 128;
-  if (e->cfg.precision == CR_PREC_MIXED)
-    cr::egrad_kernel<PES, true><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, e->d_V, e->d_f);
-  else
-    cr::egrad_kernel<PES, false><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, e->d_V, e->d_f);
-  CR_CUDA(cudaGetLastError());
+  const cr::PesRuns* r = cr::pes_runs(e->cfg.pes);
+  if (!r) return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  CR_CUDA(r->egrad(e->cfg.precision == CR_PREC_MIXED, e->T * e->P, e->d_q, e->d_V, e->d_f, e->stream));
   cr::sum_beads_kernel<<<(e->T + 127) / 128, 128, 0, e->stream>>>(e->T, e->P, e->d_V, e->d_epot);
   CR_CUDA(cudaGetLastError());
   return CR_OK;
 }
 
-// Forces of the large-molecule path: one QMDFF, or the dE-EVB of two.
-template <class PES>
+// Forces of the large-molecule path from an analytic surface (constrained
+// parents and umbrella windows step through the graph path).
 int egrad_launch(cr_engine* e, double* V, double* f) {
-  const int nb = e->T * e->P, bs = 128;
-  if (e->cfg.precision == CR_PREC_MIXED)
-    cr::egrad_kernel<PES, true><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, V, f);
-  else
-    cr::egrad_kernel<PES, false><<<(nb + bs - 1) / bs, bs, 0, e->stream>>>(nb, e->d_q, V, f);
-  CR_CUDA(cudaGetLastError());
+  const cr::PesRuns* r = cr::pes_runs(e->cfg.pes);
+  if (!r) return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  CR_CUDA(r->egrad(e->cfg.precision == CR_PREC_MIXED, e->T * e->P, e->d_q, V, f, e->stream));
   return CR_OK;
 }
 
@@ -479,13 +449,7 @@ int split_forces_range(cr_engine* e, int t0, int tn, double* V, double* f, cudaS
   if (e->ff) return qmdff_launch(e->ff, e->d_q + off, tn * e->P, V, f, e->cfg.precision, st);
   if (e->water) return water_launch(e->water, e->d_q + off, tn * e->P, V, f, e->cfg.precision, st);
   if (t0 != 0 || tn != e->T || st != e->stream) return fail(CR_ERR_UNSUPPORTED, "analytic forces cover every trajectory");
-  switch (e->cfg.pes) {
-    case CR_PES_H3: return egrad_launch<cr::PesH3>(e, V, f);
-    case CR_PES_CH4H: return egrad_launch<cr::PesCH4H>(e, V, f);
-    case CR_PES_CH4OH: return egrad_launch<cr::PesCH4OH>(e, V, f);
-    case CR_PES_OH3: return egrad_launch<cr::PesOH3>(e, V, f);
-    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
-  }
+  return egrad_launch(e, V, f);
 }
 
 int split_forces(cr_engine* e, double* V, double* f) { return split_forces_range(e, 0, e->T, V, f, e->stream); }
@@ -692,13 +656,7 @@ int split_run(cr_engine* e, int nsteps) {
 
 int dispatch_run(cr_engine* e, int nsteps) {
   if (e->split) return split_run(e, nsteps);
-  switch (e->cfg.pes) {
-    case CR_PES_H3: return launch_run<cr::PesH3>(e, nsteps);
-    case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, nsteps);
-    case CR_PES_CH4OH: return launch_run<cr::PesCH4OH>(e, nsteps);
-    case CR_PES_OH3: return launch_run<cr::PesOH3>(e, nsteps);
-    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
-  }
+  return launch_run(e, nsteps);
 }
 
 int dispatch_forces(cr_engine* e) {
@@ -709,30 +667,29 @@ int dispatch_forces(cr_engine* e) {
     CR_CUDA(cudaGetLastError());
     return CR_OK;
   }
-  switch (e->cfg.pes) {
-    case CR_PES_H3: return launch_forces<cr::PesH3>(e);
-    case CR_PES_CH4H: return launch_forces<cr::PesCH4H>(e);
-    case CR_PES_CH4OH: return launch_forces<cr::PesCH4OH>(e);
-    case CR_PES_OH3: return launch_forces<cr::PesOH3>(e);
-    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
-  }
+  return launch_forces(e);
 }
 
-// Launch shape for `block` threads per block (a multiple of G, at most 256):
-// false if the group scratch of block/G trajectories does not fit.
-bool set_launch_shape(cr_engine* e, int block) {
-  const int G = e->G;
-  if (block < G || block % G || block > 256) return false;
-  const size_t smem = cr::step_smem_doubles(e->P, G, e->NC, block / G) * sizeof(double);
+// Launch shape for `block` threads per block and `tpb` threads per bead
+// (block a multiple of G tpb, at most 256): false if the surface has no such
+// variant or the group scratch of block/(G tpb) trajectories does not fit.
+bool set_launch_shape(cr_engine* e, int block, int tpb) {
+  const cr::PesRuns* r = cr::pes_runs(e->cfg.pes);
+  if (!r || (tpb != 1 && tpb != 2 && tpb != 4) || tpb > r->max_tpb) return false;
+  const int GT = e->G * tpb;
+  if (block < GT || block % GT || block > 256) return false;
+  const size_t smem = cr::step_smem_doubles(e->P, e->G, e->NC, block / GT, tpb) * sizeof(double);
   if (smem > 200 * 1024) return false;
   e->block = block;
-  e->grid = (e->T + block / G - 1) / (block / G);
+  e->tpb = tpb;
+  e->grid = (e->T + block / GT - 1) / (block / GT);
   e->smem = smem;
   return true;
 }
 
 // Launch shape: a tiny batch is latency-bound, so it is spread one warp per
-// SM; a large batch uses 128-thread blocks, shrunk until the shared memory fits.
+// SM; a large batch uses 128-thread blocks, shrunk until the shared memory
+// fits; one thread per bead.
 void choose_launch(cr_engine* e) {
   const int G = e->G;
   int sms = 152;
@@ -744,6 +701,7 @@ void choose_launch(cr_engine* e) {
   if (block > 256) block = 256;
   while (block > G && cr::step_smem_doubles(e->P, G, e->NC, block / G) * 8 > 200 * 1024) block /= 2;
   e->block = block;
+  e->tpb = 1;
   const int groups = block / G;
   e->grid = (e->T + groups - 1) / groups;
   e->smem = cr::step_smem_doubles(e->P, G, e->NC, groups) * sizeof(double);
@@ -754,17 +712,12 @@ void choose_launch(cr_engine* e) {
 // ---------------------------------------------------------------------------
 // C-ABI
 // ---------------------------------------------------------------------------
-template <class PES>
-static int egrad_device_impl(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
+static int egrad_device_impl(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
                              cudaStream_t s) {
-  const int bs = 128;
-  if (precision == CR_PREC_MIXED)
-    cr::egrad_kernel<PES, true><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
-  else if (precision == CR_PREC_FP64)
-    cr::egrad_kernel<PES, false><<<(npts + bs - 1) / bs, bs, 0, s>>>(npts, d_q, d_V, d_dVdq);
-  else
-    return fail(CR_ERR_ARG, "unknown precision");
-  CR_CUDA(cudaGetLastError());
+  const cr::PesRuns* r = cr::pes_runs(pes);
+  if (!r) return fail(CR_ERR_UNSUPPORTED, "PES not built");
+  if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return fail(CR_ERR_ARG, "unknown precision");
+  CR_CUDA(r->egrad(precision == CR_PREC_MIXED, npts, d_q, d_V, d_dVdq, s));
   return CR_OK;
 }
 
@@ -839,13 +792,7 @@ int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d
   if (npts < 0 || (npts > 0 && (!d_q || !d_V || !d_dVdq))) return fail(CR_ERR_ARG, "bad egrad arguments");
   if (npts == 0) return CR_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  switch (pes) {
-    case CR_PES_H3: return egrad_device_impl<cr::PesH3>(d_q, npts, d_V, d_dVdq, precision, s);
-    case CR_PES_CH4H: return egrad_device_impl<cr::PesCH4H>(d_q, npts, d_V, d_dVdq, precision, s);
-    case CR_PES_CH4OH: return egrad_device_impl<cr::PesCH4OH>(d_q, npts, d_V, d_dVdq, precision, s);
-    case CR_PES_OH3: return egrad_device_impl<cr::PesOH3>(d_q, npts, d_V, d_dVdq, precision, s);
-    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
-  }
+  return egrad_device_impl(pes, d_q, npts, d_V, d_dVdq, precision, s);
 }
 
 int cr_egrad_h3_device(const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,
@@ -1521,13 +1468,7 @@ static int host_pipeline_init(cr_engine* e) {
 static int host_group_step(cr_engine* e, int t0, int tn, cudaStream_t st, int* nl) {
   if (e->split) return split_group_launches(e, split_params_range(e, t0, tn), t0, tn, st, nl);
   ++*nl;
-  switch (e->cfg.pes) {
-    case CR_PES_H3: return launch_group<cr::PesH3>(e, t0, tn, st);
-    case CR_PES_CH4H: return launch_group<cr::PesCH4H>(e, t0, tn, st);
-    case CR_PES_CH4OH: return launch_group<cr::PesCH4OH>(e, t0, tn, st);
-    case CR_PES_OH3: return launch_group<cr::PesOH3>(e, t0, tn, st);
-    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
-  }
+  return launch_group(e, t0, tn, st);
 }
 
 int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* epot) {
@@ -1559,13 +1500,7 @@ int cr_engine_step_host(cr_engine* e, double* q, double* p, double* f, double* e
     e->h_istep = e->istep;
     CR_CUDA(cudaMemcpyAsync(e->d_istep, &e->h_istep, sizeof(int), cudaMemcpyHostToDevice, e->stream));
   } else {
-    switch (e->cfg.pes) {
-      case CR_PES_H3: rc = set_run_smem<cr::PesH3>(e); break;
-      case CR_PES_CH4H: rc = set_run_smem<cr::PesCH4H>(e); break;
-      case CR_PES_CH4OH: rc = set_run_smem<cr::PesCH4OH>(e); break;
-      case CR_PES_OH3: rc = set_run_smem<cr::PesOH3>(e); break;
-      default: rc = fail(CR_ERR_UNSUPPORTED, "PES not built");
-    }
+    rc = set_run_smem(e);
     if (rc) return rc;
   }
   CR_CUDA(cudaEventRecord(e->ev0, e->stream));
@@ -1796,33 +1731,35 @@ static void drop_graph(cr_engine* e) {
   }
 }
 
-int cr_engine_set_launch(cr_engine* e, int threads_per_block) {
+int cr_engine_set_launch(cr_engine* e, int threads_per_block, int threads_per_bead) {
   if (!e) return fail(CR_ERR_ARG, "NULL engine");
   if (e->split) return fail(CR_ERR_UNSUPPORTED, "this engine steps through the graph path, which has no launch shape to set");
   CR_CUDA(cudaStreamSynchronize(e->stream));
   if (threads_per_block == 0) {
     choose_launch(e);
-  } else if (!set_launch_shape(e, threads_per_block)) {
-    return fail(CR_ERR_ARG, "threads_per_block must be a multiple of the bead group (next power of two of nbeads), "
-                            "at most 256, with the group scratch within 200 KB");
+  } else if (!set_launch_shape(e, threads_per_block, threads_per_bead)) {
+    return fail(CR_ERR_ARG, "threads_per_bead must be 1, 2 or 4 (as built for the surface: 4 for H3 and OH3, "
+                            "1 for CH4H and CH4OH) and threads_per_block a multiple of threads_per_bead x the bead "
+                            "group (next power of two of nbeads), at most 256, with the group scratch within 200 KB");
   }
   drop_graph(e);
   return CR_OK;
 }
 
-int cr_engine_get_launch(cr_engine* e, int* threads_per_block, int* blocks) {
+int cr_engine_get_launch(cr_engine* e, int* threads_per_block, int* blocks, int* threads_per_bead) {
   if (!e) return fail(CR_ERR_ARG, "NULL engine");
   if (threads_per_block) *threads_per_block = e->split ? 0 : e->block;
   if (blocks) *blocks = e->split ? 0 : e->grid;
+  if (threads_per_bead) *threads_per_bead = e->split ? 0 : e->tpb;
   return CR_OK;
 }
 
-int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, float* ms_per_step) {
+int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, int* threads_per_bead, float* ms_per_step) {
   if (!e) return fail(CR_ERR_ARG, "NULL engine");
   if (e->split) return fail(CR_ERR_UNSUPPORTED, "this engine steps through the graph path, which has no launch shape to tune");
   if (nsteps < 1) return fail(CR_ERR_ARG, "nsteps must be >= 1");
-  if (e->xi_on && e->istep + nsteps - e->side_step0 > e->side_cap)
-    return fail(CR_ERR_ARG, "the trial run exceeds the recrossing step capacity set by cr_engine_set_recross");
+  if (e->xi_on && e->istep + nsteps + 1 - e->side_step0 > e->side_cap)
+    return fail(CR_ERR_ARG, "the trial runs exceed the recrossing step capacity set by cr_engine_set_recross");
   CR_CUDA(cudaStreamSynchronize(e->stream));
   // every trial starts from the same state: q, p, f, epot, status, the
   // chain velocities and the step counter are saved and put back after it
@@ -1847,31 +1784,34 @@ int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, float* 
                             cudaMemcpyDeviceToDevice, e->stream);
     return err;
   };
-  const int block0 = e->block, istep0 = e->istep;
-  int best = block0, rc = CR_OK;
+  const int block0 = e->block, tpb0 = e->tpb, istep0 = e->istep;
+  int best = block0, best_tpb = tpb0, rc = CR_OK;
   float best_ms = 0.f;
-  const int cand[] = {e->G, 32, 64, 128, 256};
   cudaError_t err = copy_state(true);
-  for (int k = 0; k < 5 && rc == CR_OK && err == cudaSuccess; ++k) {
-    const int b = cand[k];
-    bool seen = false;
-    for (int i = 0; i < k; ++i) seen |= cand[i] == b;
-    if (seen || !set_launch_shape(e, b)) continue;
-    // one untimed step (first launch of this shape), then the timed run
-    for (int rep = 0; rep < 2 && rc == CR_OK; ++rep) {
-      if ((rc = engine_run_async(e, rep == 0 ? 1 : nsteps))) break;
-      err = cudaStreamSynchronize(e->stream);
-      if (err != cudaSuccess) break;
-      if (rep == 1) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e->ev0, e->ev1);
-        if (best_ms == 0.f || ms < best_ms) {
-          best_ms = ms;
-          best = b;
+  for (int tpb = 1; tpb <= 4 && rc == CR_OK && err == cudaSuccess; tpb *= 2) {
+    const int cand[] = {e->G * tpb, 32, 64, 128, 256};
+    for (int k = 0; k < 5 && rc == CR_OK && err == cudaSuccess; ++k) {
+      const int b = cand[k];
+      bool seen = false;
+      for (int i = 0; i < k; ++i) seen |= cand[i] == b;
+      if (seen || !set_launch_shape(e, b, tpb)) continue;
+      // one untimed step (first launch of this shape), then the timed run
+      for (int rep = 0; rep < 2 && rc == CR_OK; ++rep) {
+        if ((rc = engine_run_async(e, rep == 0 ? 1 : nsteps))) break;
+        err = cudaStreamSynchronize(e->stream);
+        if (err != cudaSuccess) break;
+        if (rep == 1) {
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+          if (best_ms == 0.f || ms < best_ms) {
+            best_ms = ms;
+            best = b;
+            best_tpb = tpb;
+          }
         }
+        e->istep = istep0;
+        if ((err = copy_state(false)) != cudaSuccess) break;
       }
-      e->istep = istep0;
-      if ((err = copy_state(false)) != cudaSuccess) break;
     }
   }
   cudaStreamSynchronize(e->stream);
@@ -1879,16 +1819,17 @@ int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, float* 
   cudaFree(save_st);
   e->istep = istep0;
   if (rc) {
-    set_launch_shape(e, block0);
+    set_launch_shape(e, block0, tpb0);
     return rc;
   }
   if (err != cudaSuccess) {
-    set_launch_shape(e, block0);
+    set_launch_shape(e, block0, tpb0);
     return fail(CR_ERR_CUDA, cudaGetErrorString(err));
   }
-  set_launch_shape(e, best);
+  set_launch_shape(e, best, best_tpb);
   drop_graph(e);
   if (threads_per_block) *threads_per_block = best;
+  if (threads_per_bead) *threads_per_bead = best_tpb;
   if (ms_per_step) *ms_per_step = best_ms / nsteps;
   return CR_OK;
 }
@@ -2065,6 +2006,10 @@ struct cr_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> join;
+  // timeline of a graph launch: t0 before the fork, each branch's first and
+  // last node (timing events recorded inside the captured graph)
+  cudaEvent_t t0 = nullptr;
+  std::vector<cudaEvent_t> tb, te;
   struct Chunk {
     int len;
     int nodes;
@@ -2080,13 +2025,7 @@ namespace {
 
 int batch_prepare(cr_engine* e) {
   if (e->split) return split_prepare(e);
-  switch (e->cfg.pes) {
-    case CR_PES_H3: return set_run_smem<cr::PesH3>(e);
-    case CR_PES_CH4H: return set_run_smem<cr::PesCH4H>(e);
-    case CR_PES_CH4OH: return set_run_smem<cr::PesCH4OH>(e);
-    case CR_PES_OH3: return set_run_smem<cr::PesOH3>(e);
-    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
-  }
+  return set_run_smem(e);
 }
 
 int batch_branch(cr_engine* e, int len) {
@@ -2097,13 +2036,7 @@ int batch_branch(cr_engine* e, int len) {
     }
     return CR_OK;
   }
-  switch (e->cfg.pes) {
-    case CR_PES_H3: return launch_run<cr::PesH3>(e, len, true);
-    case CR_PES_CH4H: return launch_run<cr::PesCH4H>(e, len, true);
-    case CR_PES_CH4OH: return launch_run<cr::PesCH4OH>(e, len, true);
-    case CR_PES_OH3: return launch_run<cr::PesOH3>(e, len, true);
-    default: return fail(CR_ERR_UNSUPPORTED, "PES not built");
-  }
+  return launch_run(e, len, true);
 }
 
 cr_batch::Chunk* batch_graph(cr_batch* b, int len) {
@@ -2113,16 +2046,22 @@ cr_batch::Chunk* batch_graph(cr_batch* b, int len) {
     fail(CR_ERR_CUDA, "batch capture could not start");
     return nullptr;
   }
-  int rc = cudaEventRecord(b->fork, b->stream) == cudaSuccess ? CR_OK
-                                                               : fail(CR_ERR_CUDA, "batch fork event failed");
+  // timing events as record nodes of the graph (External: recorded when the
+  // graph runs, not turned into capture dependencies)
+  int rc = (cudaEventRecordWithFlags(b->t0, b->stream, cudaEventRecordExternal) == cudaSuccess &&
+            cudaEventRecord(b->fork, b->stream) == cudaSuccess)
+               ? CR_OK
+               : fail(CR_ERR_CUDA, "batch fork event failed");
   for (size_t i = 0; i < b->eng.size() && rc == CR_OK; ++i) {
     cr_engine* e = b->eng[i];
-    if (cudaStreamWaitEvent(e->stream, b->fork, 0) != cudaSuccess) {
+    if (cudaStreamWaitEvent(e->stream, b->fork, 0) != cudaSuccess ||
+        cudaEventRecordWithFlags(b->tb[i], e->stream, cudaEventRecordExternal) != cudaSuccess) {
       rc = fail(CR_ERR_CUDA, "batch fork failed");
       break;
     }
     rc = batch_branch(e, len);
-    if (rc == CR_OK && (cudaEventRecord(b->join[i], e->stream) != cudaSuccess ||
+    if (rc == CR_OK && (cudaEventRecordWithFlags(b->te[i], e->stream, cudaEventRecordExternal) != cudaSuccess ||
+                        cudaEventRecord(b->join[i], e->stream) != cudaSuccess ||
                         cudaStreamWaitEvent(b->stream, b->join[i], 0) != cudaSuccess))
       rc = fail(CR_ERR_CUDA, "batch join failed");
   }
@@ -2141,8 +2080,9 @@ cr_batch::Chunk* batch_graph(cr_batch* b, int len) {
     fail(CR_ERR_CUDA, "batch graph instantiation failed");
     return nullptr;
   }
-  // kernels only: the fork/join leave no nodes of their own
-  c.nodes = (int)nodes;
+  // kernels only: the fork/join leave no nodes of their own; the timing
+  // events are 1 + 2 per engine record nodes
+  c.nodes = (int)nodes - (1 + 2 * (int)b->eng.size());
   b->graphs.push_back(c);
   return &b->graphs.back();
 }
@@ -2165,10 +2105,15 @@ int cr_batch_create(cr_engine* const* engines, int nengines, int chunk_steps, cr
   b->eng.assign(engines, engines + nengines);
   b->chunk = chunk_steps;
   b->join.assign((size_t)nengines, nullptr);
+  b->tb.assign((size_t)nengines, nullptr);
+  b->te.assign((size_t)nengines, nullptr);
   bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
-            cudaEventCreate(&b->ev0) == cudaSuccess && cudaEventCreate(&b->ev1) == cudaSuccess;
+            cudaEventCreate(&b->ev0) == cudaSuccess && cudaEventCreate(&b->ev1) == cudaSuccess &&
+            cudaEventCreate(&b->t0) == cudaSuccess;
   for (auto& ev : b->join) ok = ok && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+  for (auto& ev : b->tb) ok = ok && cudaEventCreate(&ev) == cudaSuccess;
+  for (auto& ev : b->te) ok = ok && cudaEventCreate(&ev) == cudaSuccess;
   if (!ok) {
     cr_batch_destroy(b);
     return fail(CR_ERR_CUDA, "batch stream or event creation failed");
@@ -2186,6 +2131,11 @@ int cr_batch_destroy(cr_batch* b) {
   }
   for (auto ev : b->join)
     if (ev) cudaEventDestroy(ev);
+  for (auto ev : b->tb)
+    if (ev) cudaEventDestroy(ev);
+  for (auto ev : b->te)
+    if (ev) cudaEventDestroy(ev);
+  if (b->t0) cudaEventDestroy(b->t0);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
@@ -2228,6 +2178,16 @@ int cr_batch_run(cr_batch* b, int nsteps) {
     for (int v : st) bad |= v;
   }
   if (bad) return fail(CR_ERR_TRAJECTORY, "a trajectory reported a non-finite coordinate or singular inertia");
+  return CR_OK;
+}
+
+int cr_batch_timeline(const cr_batch* b, float* begin_ms, float* end_ms) {
+  if (!b || !begin_ms || !end_ms) return fail(CR_ERR_ARG, "NULL argument");
+  if (b->graphs.empty()) return fail(CR_ERR_ARG, "the batch has not run");
+  for (size_t i = 0; i < b->eng.size(); ++i) {
+    CR_CUDA(cudaEventElapsedTime(&begin_ms[i], b->t0, b->tb[i]));
+    CR_CUDA(cudaEventElapsedTime(&end_ms[i], b->t0, b->te[i]));
+  }
   return CR_OK;
 }
 
@@ -2431,3 +2391,15 @@ int cr_adjoint_backward(cr_adjoint* a, const double* dl_dq, const double* dl_dp,
 }
 
 }  // extern "C"
+
+namespace cr {
+const PesRuns* pes_runs(int pes) {
+  switch (pes) {
+    case CR_PES_H3: return &kRunsH3;
+    case CR_PES_CH4H: return &kRunsCH4H;
+    case CR_PES_CH4OH: return &kRunsCH4OH;
+    case CR_PES_OH3: return &kRunsOH3;
+    default: return nullptr;
+  }
+}
+}  // namespace cr

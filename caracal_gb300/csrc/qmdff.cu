@@ -669,6 +669,55 @@ int cr_qmdff_create(const cr_qmdff_def* d, cr_qmdff** out) {
   return CR_OK;
 }
 
+int cr_qmdff_set_periodic(cr_qmdff* ff, const double* box_ang, double coul_cut_ang, double vdw_cut_ang,
+                          double* cuts) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  cr::qmdff::Dev& D = ff->dev;
+  if (!box_ang) {
+    D.periodic = 0;
+    return CR_OK;
+  }
+  for (int k = 0; k < 3; ++k)
+    if (!(box_ang[k] > 0.0)) return cr_set_error(CR_ERR_ARG, "box edges must be positive (Angstrom)");
+  if (!(coul_cut_ang > 0.0) || !(vdw_cut_ang > 0.0)) return cr_set_error(CR_ERR_ARG, "cutoffs must be positive");
+  // set_periodic (src/set_periodic.f90:67-113)
+  const double bohr = 0.52917721092;
+  for (int k = 0; k < 3; ++k) {
+    D.len[k] = box_ang[k] / bohr;
+    D.half[k] = D.len[k] * 0.5;
+  }
+  const double hmin = std::min(D.half[0], std::min(D.half[1], D.half[2]));
+  double coul = coul_cut_ang / bohr;
+  if (coul < 5.0) coul = hmin - 0.1;
+  if (D.zahn) {
+    const double spi = std::sqrt(3.14159265358979323846);
+    D.zahn_a = 0.2 * bohr;
+    coul = 10.0 / bohr;
+    const double acut = D.zahn_a * coul;
+    D.zahn_par = std::erfc(acut) / (coul * coul) + 2 * D.zahn_a / spi * std::exp(-acut * acut) / coul;
+  }
+  if (coul > hmin) coul = hmin - 0.1;
+  D.coul_cut = coul;
+  D.vdw_cut = vdw_cut_ang / bohr;
+  for (int k = 0; k < 3; ++k) {
+    D.flen[k] = (float)D.len[k];
+    D.flen_lo[k] = (float)(D.len[k] - (double)D.flen[k]);
+    D.fhalf[k] = (float)D.half[k];
+  }
+  D.fcoul_cut = (float)D.coul_cut;
+  D.fvdw_cut = (float)D.vdw_cut;
+  D.fzahn_a = (float)D.zahn_a;
+  D.fzahn_par = (float)D.zahn_par;
+  D.periodic = 1;
+  if (cuts) {
+    cuts[0] = D.coul_cut;
+    cuts[1] = D.vdw_cut;
+    cuts[2] = D.zahn_a;
+    cuts[3] = D.zahn_par;
+  }
+  return CR_OK;
+}
+
 int cr_qmdff_schedule_info(const cr_qmdff* ff, int* batches, int* colors) {
   if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
   if (batches)

@@ -73,6 +73,11 @@ struct Dev {
   double coul_cut, zahn_a, zahn_par, e_zero;
   float fcoul_cut, fzahn_a, fzahn_par;  // the same in FP32 (mixed form)
   int zahn;
+  // periodic box (src/set_periodic.f90, src/box_image.f90): edge lengths,
+  // halves and the dispersion/repulsion cutoff, bohr
+  int periodic;
+  double len[3], half[3], vdw_cut;
+  float flen[3], flen_lo[3], fhalf[3], fvdw_cut;  // edges as (hi, lo) float pairs
   int distinct;  // 1: every term's atoms are pairwise distinct
   int nterm[kKinds];  // terms per kind
   // mixed form, bond stretch gradient as a double-FP32 polynomial (see
@@ -282,7 +287,28 @@ struct BeadPos {
   const double* x;
   const float2* hl;  // (hi, lo) per coordinate (mixed form only)
   const double* w;   // tangent direction (dual coordinates only)
+  const Dev* pbc;    // the force field where the box is periodic, else NULL
 };
+
+// box_image (src/box_image.f90:36-63): subtract the edge while a component
+// exceeds half of it; bounded (a non-finite or absurd vector stops after
+// kImageIters subtractions and the step's NaN check reports it).  In FP32
+// the vector is a (hi, lo) pair and the edge is subtracted as one.
+constexpr int kImageIters = 64;
+__device__ inline double image1(double v, double len, double half) {
+  for (int it = 0; it < kImageIters && fabs(v) > half; ++it) v = v - copysign(len, v);
+  return v;
+}
+// FP32: the difference of two (hi, lo) coordinates as an exact float pair
+// first (atoms a box edge apart are not close enough for the hi parts to
+// subtract exactly), the edge subtracted as a pair, then rounded once.
+__device__ inline float image1(FF d, float len, float len_lo, float half) {
+  for (int it = 0; it < kImageIters && fabsf(d.hi) > half; ++it) {
+    const float s = copysignf(1.0f, d.hi);
+    d = ff_add(d, FF{-s * len, -s * len_lo});
+  }
+  return d.hi + d.lo;
+}
 
 template <class F>
 __device__ inline void disp(const BeadPos& X, int a, int b, F* v);
@@ -291,18 +317,27 @@ __device__ inline void disp<double>(const BeadPos& X, int a, int b, double* v) {
   v[0] = X.x[3 * a] - X.x[3 * b];
   v[1] = X.x[3 * a + 1] - X.x[3 * b + 1];
   v[2] = X.x[3 * a + 2] - X.x[3 * b + 2];
+  if (X.pbc) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] = image1(v[d], X.pbc->len[d], X.pbc->half[d]);
+  }
 }
 template <>
 __device__ inline void disp<Dual>(const BeadPos& X, int a, int b, Dual* v) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) v[d] = Dual(X.x[3 * a + d] - X.x[3 * b + d], X.w[3 * a + d] - X.w[3 * b + d]);
+  for (int d = 0; d < 3; ++d) {
+    double x = X.x[3 * a + d] - X.x[3 * b + d];
+    if (X.pbc) x = image1(x, X.pbc->len[d], X.pbc->half[d]);
+    v[d] = Dual(x, X.w[3 * a + d] - X.w[3 * b + d]);
+  }
 }
 template <>
 __device__ inline void disp<float>(const BeadPos& X, int a, int b, float* v) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float2 u = X.hl[3 * a + d], w = X.hl[3 * b + d];
-    v[d] = (u.x - w.x) + (u.y - w.y);
+    if (X.pbc) v[d] = image1(ff_add(FF{u.x, u.y}, FF{-w.x, -w.y}), X.pbc->flen[d], X.pbc->flen_lo[d], X.pbc->fhalf[d]);
+    else v[d] = (u.x - w.x) + (u.y - w.y);
   }
 }
 
@@ -356,6 +391,12 @@ __device__ inline float bond_mixed(const Dev& D, const BeadPos& x, int m, Contri
   for (int d = 0; d < 3; ++d) {
     const float2 a = x.hl[3 * i + d], b = x.hl[3 * j + d];
     dv[d] = ff_add(FF{a.x, a.y}, FF{-b.x, -b.y});
+    if (x.pbc) {
+      for (int it = 0; it < kImageIters && fabsf(dv[d].hi) > x.pbc->fhalf[d]; ++it) {
+        const float sg = copysignf(1.0f, dv[d].hi);
+        dv[d] = ff_add(dv[d], FF{-sg * x.pbc->flen[d], -sg * x.pbc->flen_lo[d]});
+      }
+    }
   }
   FF r2f = ff_mul(dv[0], dv[0]);
   r2f = ff_add(r2f, ff_mul(dv[1], dv[1]));
@@ -790,9 +831,11 @@ __device__ inline F pair_term(const Dev& D, const Tables<typename ParamOf<F>::ty
   const F ir2 = oner * oner;
   const F c6t6 = c6 * it6, c6t8 = c6 * it8;
   const F t27 = v[2] * c6t8;
-  F e = -(c6t6 + t27) * eps2;
-  F drij = eps2 * (c6t6 * F(6) * r4 * it6 + F(8) * t27 * r6 * it8);
-  if (r < F(25)) {
+  // periodic: dispersion and repulsion only within vdw_cut (src/ff_nonb.f90:107)
+  const bool vdw = !D.periodic || !(r > (std::is_same<F, float>::value ? F(D.fvdw_cut) : F(D.vdw_cut)));
+  F e = vdw ? -(c6t6 + t27) * eps2 : F(0);
+  F drij = vdw ? eps2 * (c6t6 * F(6) * r4 * it6 + F(8) * t27 * r6 * it8) : F(0);
+  if (vdw && r < F(25)) {
     const F alpha = v[4];
     F ex;
     if constexpr (std::is_same<F, float>::value) ex = __expf(-alpha * r);
@@ -856,9 +899,10 @@ __device__ inline float pair_mixed_v(const Dev& D, const BeadPos& x, int i1, int
   const float r4 = r2 * r2, r6 = r4 * r2;
   const float it6 = rcp_approx(r6 + v[0]), it8 = rcp_approx(r6 * r2 + v[1]);
   const float d6 = v[2] * it6, d8 = v[3] * it8;
-  float e = -(d6 + d8);
-  float drij = 6.0f * d6 * (r4 * it6) + 8.0f * d8 * (r6 * it8);
-  if (r < 25.0f) {
+  const bool vdw = !D.periodic || !(r > D.fvdw_cut);
+  float e = vdw ? -(d6 + d8) : 0.0f;
+  float drij = vdw ? 6.0f * d6 * (r4 * it6) + 8.0f * d8 * (r6 * it8) : 0.0f;
+  if (vdw && r < 25.0f) {
     const float t = v[4] * ex2_approx(-v[5] * r) * oner;
     e += t;
     drij = fmaf(-t * ir2, fmaf(v[7], r, 1.0f), drij);
@@ -1031,9 +1075,13 @@ __device__ inline F xbond_term(const BeadPos& X, int A, int B, int H, double ca,
 template <class F>
 __device__ __noinline__ F hb_term(const Dev& D, const Tables<F>&, const BeadPos& X, int k, Contrib<F>& c) {
   const int4 t = __ldg(reinterpret_cast<const int4*>(D.hb) + k);
-  const double r2 = (X.x[3 * t.x] - X.x[3 * t.y]) * (X.x[3 * t.x] - X.x[3 * t.y]) +
-                    (X.x[3 * t.x + 1] - X.x[3 * t.y + 1]) * (X.x[3 * t.x + 1] - X.x[3 * t.y + 1]) +
-                    (X.x[3 * t.x + 2] - X.x[3 * t.y + 2]) * (X.x[3 * t.x + 2] - X.x[3 * t.y + 2]);
+  double rb[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    rb[d] = X.x[3 * t.x + d] - X.x[3 * t.y + d];
+    if (X.pbc) rb[d] = image1(rb[d], X.pbc->len[d], X.pbc->half[d]);  // src/ff_hb.f90:64-66
+  }
+  const double r2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
   c.a[0] = t.x;
   c.a[1] = t.y;
   c.a[2] = t.z;
@@ -1160,7 +1208,7 @@ __device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, doub
   double* xs = ws;
   float2* hl = (float2*)(ws + n3);
   void* gs = hl + n3;
-  BeadPos X{xs, hl, nullptr};
+  BeadPos X{xs, hl, nullptr, D.periodic ? &D : nullptr};
   Grad<F> G;
   if constexpr (MIXED) {
     for (int a = lane; a < n3; a += 32) {
@@ -1256,7 +1304,7 @@ __device__ inline double warp_hvp(const Dev& D, double* ws, double* gout, double
     G.h[a] = 0.0;
   }
   __syncwarp();
-  BeadPos X{xs, nullptr, w};
+  BeadPos X{xs, nullptr, w, D.periodic ? &D : nullptr};
   Dual es(0.0);
   kind_batches_dual<0, 2>(D, X, G, es, lane);
   kind_batches_dual<1, 3>(D, X, G, es, lane);
@@ -1286,7 +1334,7 @@ __device__ inline double warp_hvp(const Dev& D, double* ws, double* gout, double
 // Per term, out receives alpha * (v . grad E_t|unit) + beta * E_t|unit.
 __device__ inline void warp_param_vjp(const Dev& D, const Tables<double>& U, const double* xs, const double* vs,
                                       double alpha, double beta, double* out, int lane) {
-  const BeadPos X{xs, nullptr, nullptr};
+  const BeadPos X{xs, nullptr, nullptr, D.periodic ? &D : nullptr};
   int off = 0;
 #pragma unroll 1
   for (int kind = 0; kind < 4; ++kind) {

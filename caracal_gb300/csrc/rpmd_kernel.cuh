@@ -409,39 +409,61 @@ __device__ inline bool invert3(double (&a)[3][3]) {
 //   [0, 3 nr (nu + nv))            propagator blocks Ke, Ko of K1, K2, K3
 //   then 2P                        PILE circulant vectors a, b
 //   then per group: xs[2 NC][G] (reused as the outputs [2 NC][P/2+1]),
-//                   u[2 NC][su], v[2 NC][sv], red[(G/32) * 32]
-__host__ __device__ inline size_t step_group_doubles(int P, int G, int NC) {
+//                   u[2 NC][su], v[2 NC][sv], red[(GT/32) * 32] with GT = G TPB
+__host__ __device__ inline size_t step_group_doubles(int P, int G, int NC, int tpb = 1) {
   const PropDims d = prop_dims(P);
-  return (size_t)2 * NC * G + (size_t)2 * NC * (d.su + d.sv) + (size_t)((G + 31) / 32) * 32;
+  return (size_t)2 * NC * G + (size_t)2 * NC * (d.su + d.sv) + (size_t)((G * tpb + 31) / 32) * 32;
 }
-__host__ __device__ inline size_t step_smem_doubles(int P, int G, int NC, int groups) {
+__host__ __device__ inline size_t step_smem_doubles(int P, int G, int NC, int groups, int tpb = 1) {
   const PropDims d = prop_dims(P);
-  return (size_t)3 * d.nr * (d.nu + d.nv) + 2 * (size_t)P + step_group_doubles(P, G, NC) * groups;
+  return (size_t)3 * d.nr * (d.nu + d.nv) + 2 * (size_t)P + step_group_doubles(P, G, NC, tpb) * groups;
 }
 
-template <class PES, bool MIXED>
+// Threads per bead (TPB = 1, 2, 4).  A trajectory owns GT = G TPB
+// consecutive threads: thread l of the group serves bead j = l mod G as its
+// sub-thread s = l / G.  Sub-thread s owns the atoms a with a mod TPB = s:
+// their q, p, f stay in its registers (slot 3 (a / TPB) + d), and it does
+// their share of every per-coordinate stage (kicks, the PILE convolutions,
+// the propagator's output rows, Andersen, the NaN check, the transrot moment
+// sums), so those stages cost 1/TPB per thread; the propagator's
+// (coordinate, row) tasks are shared by all GT threads.  The surface needs
+// the whole bead, so every sub-thread gathers the bead's coordinates
+// through shared memory and evaluates it (the same instructions side by
+// side; no exchange of forces).  Worth it where the batch is too small to
+// fill the GPU and the integrator dominates the bead's work (H3, OH + H2);
+// TPB = 1 is the one-thread-per-bead kernel.
+template <int TPB>
+__host__ __device__ constexpr int own_slot(int c) { return 3 * ((c / 3) / TPB) + c % 3; }
+
+template <class PES, bool MIXED, int TPB>
 __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep_arg, int nsteps) {
   const int istep0 = prm.istep_dev ? *prm.istep_dev : istep_arg;
   constexpr int N = PES::N;
   constexpr int NC = 3 * N;
+  constexpr int NL = 3 * ((N + TPB - 1) / TPB);  // coordinate slots per sub-thread
   extern __shared__ double smem[];
   const int P = prm.P, G = prm.G, H = prm.H;
-  const int groups = blockDim.x / G;
-  const int grp = threadIdx.x / G;
-  const int j = threadIdx.x % G;  // bead
+  const int GT = G * TPB;
+  const int groups = blockDim.x / GT;
+  const int grp = threadIdx.x / GT;
+  const int lg = threadIdx.x % GT;          // thread within the group
+  const int j = (TPB == 1) ? lg : lg % G;   // bead
+  const int sub = (TPB == 1) ? 0 : lg / G;  // sub-thread
   const int t = blockIdx.x * groups + grp;
   const bool active = (t < prm.T) && (j < P);
+  // does this sub-thread own coordinate c (c a compile-time loop index)
+  auto mine = [&](int c) { return TPB == 1 || (c / 3) % TPB == sub; };
 
   const PropDims pd = prm.pd;
   const int nke = 3 * pd.nr * pd.nu, nko = 3 * pd.nr * pd.nv;
   double* s_ke = smem;
   double* s_ko = s_ke + nke;
   double* s_pile = s_ko + nko;
-  double* s_grp = s_pile + 2 * P + step_group_doubles(P, G, NC) * grp;
+  double* s_grp = s_pile + 2 * P + step_group_doubles(P, G, NC, TPB) * grp;
   double* xs = s_grp;                      // [2][NC][G]; after the fold: outputs [2][NC][H]
   double* su = xs + 2 * NC * G;            // [2 NC][su]
   double* sv = su + 2 * NC * pd.su;        // [2 NC][sv]
-  double* red = sv + 2 * NC * pd.sv;       // [(G/32)][32]
+  double* red = sv + 2 * NC * pd.sv;       // [(GT/32)][32]
 
   if (prm.nm_mode) {
     for (int x = threadIdx.x; x < 3 * P; x += blockDim.x) s_ke[x] = prm.circ[x];  // 3 P <= nke
@@ -452,18 +474,18 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
   if (prm.thermostat == CR_THERMO_PILE)
     for (int x = threadIdx.x; x < 2 * P; x += blockDim.x) s_pile[x] = prm.pile[x];
 
-  double q[NC], p[NC], f[NC];
+  double q[NL], p[NL], f[NL];
+#pragma unroll
+  for (int k = 0; k < NL; ++k) { q[k] = 0.0; p[k] = 0.0; f[k] = 0.0; }
   const size_t base = ((size_t)t * P + j) * NC;
   if (active) {
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      q[c] = prm.q[base + c];
-      p[c] = prm.p[base + c];
-      f[c] = prm.f[base + c];
+      if (!mine(c)) continue;
+      q[own_slot<TPB>(c)] = prm.q[base + c];
+      p[own_slot<TPB>(c)] = prm.p[base + c];
+      f[own_slot<TPB>(c)] = prm.f[base + c];
     }
-  } else {
-#pragma unroll
-    for (int c = 0; c < NC; ++c) { q[c] = 0.0; p[c] = 0.0; f[c] = 0.0; }
   }
   const uint32_t traj_key = prm.traj0 + (uint32_t)t;
   int status = 0;
@@ -482,49 +504,54 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
     if (active) {
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        const double pp = p[3 * i] * p[3 * i] + p[3 * i + 1] * p[3 * i + 1] + p[3 * i + 2] * p[3 * i + 2];
+        if (!mine(3 * i)) continue;
+        const int k = own_slot<TPB>(3 * i);
+        const double pp = p[k] * p[k] + p[k + 1] * p[k + 1] + p[k + 2] * p[k + 2];
         ek[0] = ek[0] + pp / (2.0 * prm.mass[i]) / P / P;
       }
     }
-    group_sum<1>(ek, G, red, j);
+    group_sum<1>(ek, GT, red, lg);
     const double sc = nhc_scale(prm.nhc, ek[0], vnh);
 #pragma unroll
-    for (int c = 0; c < NC; ++c) p[c] = sc * p[c];
+    for (int k = 0; k < NL; ++k) p[k] = sc * p[k];
   };
 
   // PILE half step on p (in place); eta from the per-bead Gaussian stream.
   auto pile_half = [&](uint32_t step, uint32_t tag) {
     double eta[NC];
     normals_bead<NC>(prm.seed, traj_key, (uint32_t)j, step, tag, eta);
-    if (!active) {
-#pragma unroll
-      for (int c = 0; c < NC; ++c) eta[c] = 0.0;
-    }
-    group_sync(G);
+    group_sync(GT);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      xs[c * G + j] = p[c];
-      xs[(NC + c) * G + j] = eta[c];
+      if (!mine(c)) continue;
+      xs[c * G + j] = p[own_slot<TPB>(c)];
+      xs[(NC + c) * G + j] = active ? eta[c] : 0.0;
     }
-    group_sync(G);
+    group_sync(GT);
     const double* a = s_pile;
     const double* b = s_pile + P;
     if (j < P) {
-      double acc_p[NC], acc_e[NC];
+      double acc_p[NL], acc_e[NL];
 #pragma unroll
-      for (int c = 0; c < NC; ++c) { acc_p[c] = 0.0; acc_e[c] = 0.0; }
+      for (int k = 0; k < NL; ++k) { acc_p[k] = 0.0; acc_e[k] = 0.0; }
       int m = j;  // (j - l) mod P
       for (int l = 0; l < P; ++l) {
         const double al = a[m], bl = b[m];
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-          acc_p[c] = fma(al, xs[c * G + l], acc_p[c]);
-          acc_e[c] = fma(bl, xs[(NC + c) * G + l], acc_e[c]);
+          if (!mine(c)) continue;
+          const int k = own_slot<TPB>(c);
+          acc_p[k] = fma(al, xs[c * G + l], acc_p[k]);
+          acc_e[k] = fma(bl, xs[(NC + c) * G + l], acc_e[k]);
         }
         m = (m == 0) ? P - 1 : m - 1;
       }
 #pragma unroll
-      for (int c = 0; c < NC; ++c) p[c] = acc_p[c] + prm.sigma[c / 3] * acc_e[c];
+      for (int c = 0; c < NC; ++c) {
+        if (!mine(c)) continue;
+        const int k = own_slot<TPB>(c);
+        p[k] = acc_p[k] + prm.sigma[c / 3] * acc_e[k];
+      }
     }
   };
 
@@ -535,17 +562,18 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 
     // 1/2 kick (src/verlet.f90:216-218)
 #pragma unroll
-    for (int c = 0; c < NC; ++c) p[c] = p[c] - prm.half_dt * f[c];
+    for (int k = 0; k < NL; ++k) p[k] = p[k] - prm.half_dt * f[k];
 
     // free ring polymer (src/verlet.f90:377-463): Caracal's cosine modes, or
     // orthonormal normal modes where nm_mode is set
-    group_sync(G);
+    group_sync(GT);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      xs[c * G + j] = p[c];
-      xs[(NC + c) * G + j] = q[c];
+      if (!mine(c)) continue;
+      xs[c * G + j] = p[own_slot<TPB>(c)];
+      xs[(NC + c) * G + j] = q[own_slot<TPB>(c)];
     }
-    group_sync(G);
+    group_sync(GT);
     if (prm.nm_mode) {
       // orthonormal normal modes: bead j's row of the circulant K1, K2, K3
       if (j < P) {
@@ -554,6 +582,7 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
         const double* c3 = s_ke + 2 * P;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
+          if (!mine(c)) continue;
           double a1p = 0.0, a1q = 0.0, a2q = 0.0, a3p = 0.0;
           int m = j;  // (j - l) mod P
           for (int l = 0; l < P; ++l) {
@@ -564,13 +593,13 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
             a3p = fma(c3[m], xp, a3p);
             m = (m == 0) ? P - 1 : m - 1;
           }
-          p[c] = fma(prm.mass[c / 3], a2q, a1p);
-          q[c] = fma(prm.inv_mass[c / 3], a3p, a1q);
+          p[own_slot<TPB>(c)] = fma(prm.mass[c / 3], a2q, a1p);
+          q[own_slot<TPB>(c)] = fma(prm.inv_mass[c / 3], a3p, a1q);
         }
       }
     } else {
       // Caracal's transform: fold each coordinate's P values into u (and v): tasks (cc, l)
-      for (int idx = j; idx < 2 * NC * pd.nu; idx += G) {
+      for (int idx = lg; idx < 2 * NC * pd.nu; idx += GT) {
         const int cc = idx / pd.nu, l = idx - cc * pd.nu;
         const double* x = xs + cc * G;
         const double a = sym_at(x, l, P);
@@ -582,9 +611,9 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
           su[cc * pd.su + l] = a;
         }
       }
-      group_sync(G);
+      group_sync(GT);
       // row pairs (r, M - r) of every coordinate: tasks (c, r); outputs into xs
-      for (int idx = j; idx < NC * pd.nr; idx += G) {
+      for (int idx = lg; idx < NC * pd.nr; idx += GT) {
         const int c = idx / pd.nr, r = idx - c * pd.nr;
         const double* k1e = s_ke + (0 * pd.nr + r) * pd.nu;
         const double* k2e = s_ke + (1 * pd.nr + r) * pd.nu;
@@ -622,23 +651,42 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
           xs[(NC + c) * H + pd.M - r] = fma(im, e3p - o3p, e1q - o1q);
         }
       }
-      group_sync(G);
+      group_sync(GT);
       if (j < P) {
         const int row = (j <= P - j) ? j : P - j;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-          p[c] = xs[c * H + row];
-          q[c] = xs[(NC + c) * H + row];
+          if (!mine(c)) continue;
+          p[own_slot<TPB>(c)] = xs[c * H + row];
+          q[own_slot<TPB>(c)] = xs[(NC + c) * H + row];
         }
       }
     }
 
-    // per-bead forces (src/verlet.f90:772-777)
+    // per-bead forces (src/verlet.f90:772-777); with TPB > 1 the bead's
+    // coordinates are first gathered from its sub-threads
     double g[NC];
-    if (MIXED) PES::template egrad<float>(q, vbead, g);
-    else PES::template egrad<double>(q, vbead, g);
+    if constexpr (TPB == 1) {
+      if (MIXED) PES::template egrad<float>(q, vbead, g);
+      else PES::template egrad<double>(q, vbead, g);
 #pragma unroll
-    for (int c = 0; c < NC; ++c) f[c] = active ? g[c] : 0.0;
+      for (int c = 0; c < NC; ++c) f[c] = active ? g[c] : 0.0;
+    } else {
+      group_sync(GT);
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (mine(c)) xs[c * G + j] = q[own_slot<TPB>(c)];
+      group_sync(GT);
+      double qb[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) qb[c] = xs[c * G + j];
+      if (MIXED) PES::template egrad<float>(qb, vbead, g);
+      else PES::template egrad<double>(qb, vbead, g);
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (mine(c)) f[own_slot<TPB>(c)] = active ? g[c] : 0.0;
+      if (sub != 0) vbead = 0.0;  // the bead's energy counts once
+    }
     if (!active) vbead = 0.0;
 
     // reaction coordinate of the centroid (umbrella mode 1 of a child step,
@@ -646,9 +694,9 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
     if (prm.xi_on) {
       double cq[NC];
 #pragma unroll
-      for (int c = 0; c < NC; ++c) cq[c] = active ? q[c] : 0.0;
-      group_allreduce<NC>(cq, G, red, j);
-      if (active && j == 0) {
+      for (int c = 0; c < NC; ++c) cq[c] = (active && mine(c)) ? q[own_slot<TPB>(c)] : 0.0;
+      group_allreduce<NC>(cq, GT, red, lg);
+      if (active && lg == 0) {
         // centroid: a multiplication by 1/P where P is a power of two (exact), else the division
 #pragma unroll
         for (int c = 0; c < NC; ++c) cq[c] = prm.pow2_P ? cq[c] * prm.inv_P : cq[c] / P;
@@ -659,7 +707,7 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 
     // 1/2 kick (src/verlet.f90:1060-1062)
 #pragma unroll
-    for (int c = 0; c < NC; ++c) p[c] = p[c] - prm.half_dt * f[c];
+    for (int k = 0; k < NL; ++k) p[k] = p[k] - prm.half_dt * f[k];
 
     if (nhc) nhc_half();  // src/verlet.f90:1085-1106
 
@@ -668,45 +716,51 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
       double z[NC];
       normals_bead<NC>(prm.seed, traj_key, (uint32_t)j, (uint32_t)istep, TAG_ANDERSEN, z);
 #pragma unroll
-      for (int c = 0; c < NC; ++c) p[c] = active ? z[c] * prm.sigma[c / 3] : 0.0;
+      for (int c = 0; c < NC; ++c)
+        if (mine(c)) p[own_slot<TPB>(c)] = active ? z[c] * prm.sigma[c / 3] : 0.0;
     }
     if (prm.thermostat == CR_THERMO_PILE) pile_half((uint32_t)istep, TAG_PILE_B);
 
     // NaN / Inf check (src/verlet.f90:1256-1275)
 #pragma unroll
-    for (int c = 0; c < NC; ++c)
-      if (nonfinite_bits(q[c])) status |= CR_TRAJ_NONFINITE;
+    for (int k = 0; k < NL; ++k)
+      if (nonfinite_bits(q[k])) status |= CR_TRAJ_NONFINITE;
 
     // transrot (src/transrot.f90:36-237): removed COM velocity and rotation
     // centre both carry Caracal's extra 1/P (total mass P^2 sum m).
     if (prm.transrot) {
-      double vel[NC];
+      double vel[NL];
 #pragma unroll
-      for (int c = 0; c < NC; ++c) vel[c] = p[c] * prm.inv_mass[c / 3];
+      for (int c = 0; c < NC; ++c)
+        if (mine(c)) vel[own_slot<TPB>(c)] = p[own_slot<TPB>(c)] * prm.inv_mass[c / 3];
       double s1[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
       for (int i = 0; i < N; ++i) {
+        if (!mine(3 * i)) continue;
+        const int k = own_slot<TPB>(3 * i);
         const double w = prm.mass[i];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          s1[d] = fma(vel[3 * i + d], w, s1[d]);
-          s1[3 + d] = fma(q[3 * i + d], w, s1[3 + d]);
+          s1[d] = fma(vel[k + d], w, s1[d]);
+          s1[3 + d] = fma(q[k + d], w, s1[3 + d]);
         }
       }
       if (!active) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) s1[k] = 0.0;
       }
-      group_allreduce<6>(s1, G, red, j);
+      group_allreduce<6>(s1, GT, red, lg);
       const double itm = 1.0 / prm.totmass;
       const double vt[3] = {s1[0] * itm, s1[1] * itm, s1[2] * itm};
       const double xt[3] = {s1[3] * itm, s1[4] * itm, s1[5] * itm};
       double s2[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
       for (int i = 0; i < N; ++i) {
+        if (!mine(3 * i)) continue;
+        const int k = own_slot<TPB>(3 * i);
         const double w = prm.mass[i];
-        const double* qq = &q[3 * i];
-        const double* vv = &vel[3 * i];
+        const double* qq = &q[k];
+        const double* vv = &vel[k];
         s2[0] = fma(qq[1] * vv[2] - qq[2] * vv[1], w, s2[0]);
         s2[1] = fma(qq[2] * vv[0] - qq[0] * vv[2], w, s2[1]);
         s2[2] = fma(qq[0] * vv[1] - qq[1] * vv[0], w, s2[2]);
@@ -722,7 +776,7 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
 #pragma unroll
         for (int k = 0; k < 9; ++k) s2[k] = 0.0;
       }
-      group_allreduce<9>(s2, G, red, j);
+      group_allreduce<9>(s2, GT, red, lg);
       const double tm = prm.totmass;
       double mang[3] = {s2[0] - (xt[1] * vt[2] - xt[2] * vt[1]) * tm,
                         s2[1] - (xt[2] * vt[0] - xt[0] * vt[2]) * tm,
@@ -743,38 +797,58 @@ __global__ void __launch_bounds__(256) rpmd_run_kernel(StepParams prm, int istep
         for (int a = 0; a < 3; ++a) va[a] = ten[a][0] * mang[0] + ten[a][1] * mang[1] + ten[a][2] * mang[2];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          double* vv = &vel[3 * i];
+          if (!mine(3 * i)) continue;
+          double* vv = &vel[own_slot<TPB>(3 * i)];
+          const double* qq = &q[own_slot<TPB>(3 * i)];
           vv[0] -= vt[0];
           vv[1] -= vt[1];
           vv[2] -= vt[2];
-          const double xd = q[3 * i] - xt[0], yd = q[3 * i + 1] - xt[1], zd = q[3 * i + 2] - xt[2];
+          const double xd = qq[0] - xt[0], yd = qq[1] - xt[1], zd = qq[2] - xt[2];
           vv[0] = vv[0] - va[1] * zd + va[2] * yd;
           vv[1] = vv[1] - va[2] * xd + va[0] * zd;
           vv[2] = vv[2] - va[0] * yd + va[1] * xd;
         }
 #pragma unroll
-        for (int c = 0; c < NC; ++c) p[c] = active ? vel[c] * prm.mass[c / 3] : 0.0;
+        for (int c = 0; c < NC; ++c)
+          if (mine(c)) p[own_slot<TPB>(c)] = active ? vel[own_slot<TPB>(c)] * prm.mass[c / 3] : 0.0;
       }
     }
   }
 
   // potential energy of the last step, summed over beads
   double e[1] = {vbead};
-  group_sum<1>(e, G, red, j);
+  group_sum<1>(e, GT, red, lg);
   if (active) {
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      prm.q[base + c] = q[c];
-      prm.p[base + c] = p[c];
-      prm.f[base + c] = f[c];
+      if (!mine(c)) continue;
+      prm.q[base + c] = q[own_slot<TPB>(c)];
+      prm.p[base + c] = p[own_slot<TPB>(c)];
+      prm.f[base + c] = f[own_slot<TPB>(c)];
     }
-    if (j == 0) prm.epot[t] = e[0];
-    if (j == 0 && nhc) {
+    if (lg == 0) prm.epot[t] = e[0];
+    if (lg == 0 && nhc) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) prm.vnh[4 * (size_t)t + k] = vnh[k];
     }
     if (status) atomicOr(&prm.status[t], status);
   }
+}
+
+// One thread per bead: V and dV/dq.
+template <class PES, bool MIXED>
+__global__ void egrad_kernel(int nbeads_total, const double* q, double* V, double* g) {
+  constexpr int NC = 3 * PES::N;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbeads_total) return;
+  double qq[NC], gg[NC], v;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) qq[c] = q[(size_t)b * NC + c];
+  if (MIXED) PES::template egrad<float>(qq, v, gg);
+  else PES::template egrad<double>(qq, v, gg);
+  V[b] = v;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) g[(size_t)b * NC + c] = gg[c];
 }
 
 }  // namespace cr

@@ -280,6 +280,19 @@ class QMDFFForceField:
         L.check(L.lib().cr_qmdff_schedule_info(self._h, L.iptr(b), C.byref(c)), "schedule_info")
         return {"batches": b.tolist(), "colors": c.value}
 
+    def set_periodic(self, box_ang, coul_cut_ang=50.0, vdw_cut_ang=10.0):
+        """Periodic box (edges in Angstrom) with set_periodic's cutoff rules;
+        returns (coul_cut, vdw_cut, zahn_a, zahn_par) in bohr as set.  box_ang
+        None switches it off.  Before creating an engine on the force field."""
+        cuts = np.zeros(4)
+        if box_ang is None:
+            L.check(L.lib().cr_qmdff_set_periodic(self._h, None, 0.0, 0.0, None), "qmdff_set_periodic")
+            return None
+        box = np.ascontiguousarray(box_ang, dtype=np.float64)
+        L.check(L.lib().cr_qmdff_set_periodic(self._h, L.dptr(box), float(coul_cut_ang), float(vdw_cut_ang),
+                                              L.dptr(cuts)), "qmdff_set_periodic")
+        return tuple(cuts)
+
     def tuning(self, precision="fp64"):
         """The autotuner's choice and timings of the force-kernel variants."""
         v = C.c_int()
@@ -498,24 +511,27 @@ class RPMDEngine:
     def set_andersen_step(self, n):
         L.check(L.lib().cr_engine_set_andersen_step(self._h, int(n)), "set_andersen_step")
 
-    def set_launch(self, threads_per_block=0):
-        """Threads per block of the persistent step kernel (0: built-in choice)."""
-        L.check(L.lib().cr_engine_set_launch(self._h, int(threads_per_block)), "set_launch")
+    def set_launch(self, threads_per_block=0, threads_per_bead=1):
+        """Threads per block and per bead of the persistent step kernel
+        (threads_per_block 0: the built-in choice)."""
+        L.check(L.lib().cr_engine_set_launch(self._h, int(threads_per_block), int(threads_per_bead)),
+                "set_launch")
 
     def launch(self):
-        """(threads per block, blocks) of the persistent step kernel; (0, 0)
-        on the graph path."""
-        b, g = C.c_int(0), C.c_int(0)
-        L.check(L.lib().cr_engine_get_launch(self._h, C.byref(b), C.byref(g)), "get_launch")
-        return b.value, g.value
+        """(threads per block, blocks, threads per bead) of the persistent step
+        kernel; zeros on the graph path."""
+        b, g, tpb = C.c_int(0), C.c_int(0), C.c_int(0)
+        L.check(L.lib().cr_engine_get_launch(self._h, C.byref(b), C.byref(g), C.byref(tpb)), "get_launch")
+        return b.value, g.value, tpb.value
 
     def autotune(self, nsteps=20):
         """Time nsteps steps at each launch shape from the same state (put
-        back afterwards), keep the fastest; returns (threads per block, ms per
-        step)."""
-        b, ms = C.c_int(0), C.c_float(0.0)
-        L.check(L.lib().cr_engine_autotune(self._h, int(nsteps), C.byref(b), C.byref(ms)), "autotune")
-        return b.value, ms.value
+        back afterwards), keep the fastest; returns (threads per block,
+        threads per bead, ms per step)."""
+        b, tpb, ms = C.c_int(0), C.c_int(0), C.c_float(0.0)
+        L.check(L.lib().cr_engine_autotune(self._h, int(nsteps), C.byref(b), C.byref(tpb), C.byref(ms)),
+                "autotune")
+        return b.value, tpb.value, ms.value
 
     def set_state(self, q, p, f=None):
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.shape)
@@ -681,6 +697,14 @@ class RPMDBatch:
         n, g, ms = C.c_longlong(), C.c_int(), C.c_float()
         L.check(L.lib().cr_batch_info(self._h, C.byref(n), C.byref(g), C.byref(ms)), "batch_info")
         return {"launches": n.value, "graph_nodes": g.value, "ms": ms.value}
+
+    def timeline(self):
+        """Per engine (begin, end) in ms of its branch within the last graph
+        launch; overlapping intervals ran concurrently."""
+        n = len(self.engines)
+        b, e = (C.c_float * n)(), (C.c_float * n)()
+        L.check(L.lib().cr_batch_timeline(self._h, b, e), "batch_timeline")
+        return [(b[i], e[i]) for i in range(n)]
 
     def close(self):
         if getattr(self, "_h", None):

@@ -195,6 +195,22 @@ typedef struct cr_qmdff_def {
 } cr_qmdff_def;
 typedef struct cr_qmdff cr_qmdff;
 int cr_qmdff_create(const cr_qmdff_def* def, cr_qmdff** out);
+/* Periodic boundaries for the force field (PERIODIC x y z in Caracal's key
+ * file; set_periodic, src/set_periodic.f90:67-113, and box_image,
+ * src/box_image.f90:36-63): box edges and the Coulomb and dispersion
+ * cutoffs in Angstrom (Caracal's defaults 50 and 10); a Coulomb cutoff below
+ * 5 bohr becomes half the shortest edge minus 0.1 bohr, the Zahn form (as
+ * the force field was created) fixes it at 10 A with its parameters, and no
+ * Coulomb cutoff exceeds half the shortest edge.  Dispersion and repulsion
+ * then act within the dispersion cutoff only.  Every distance vector of
+ * every term is minimum-image (Caracal images the bond, angle, damping,
+ * pair and H-bond vectors, and takes dihedrals from raw coordinates, which
+ * agree for molecules not split across the box).  cuts (may be NULL)
+ * receives coul_cut, vdw_cut, zahn_a, zahn_par as set (bohr).
+ * box_ang NULL switches periodicity off.  Call it before an engine using
+ * the force field is created. */
+int cr_qmdff_set_periodic(cr_qmdff* ff, const double* box_ang, double coul_cut_ang, double vdw_cut_ang,
+                          double* cuts);
 /* Element tables for reading a .qmdff file: the (94,94) arrays ff_nonb takes
  * and, per element pair, the C6 that gives c6xy(i, j) = c6ab(at(i), at(j)). */
 typedef struct cr_qmdff_tables {
@@ -502,20 +518,25 @@ int cr_engine_set_andersen_step(cr_engine* e, int andersen_step);
 
 /* Launch shape of the persistent step kernel (analytic surfaces; the graph
  * path of force fields has none and returns CR_ERR_UNSUPPORTED).  A
- * trajectory's beads sit on G = next_pow2(nbeads) consecutive threads;
- * threads_per_block (a multiple of G, <= 256) sets how many trajectories
- * share a block, and so how the batch spreads over the SMs and their four
- * schedulers.  0 restores the built-in choice (32 threads for a batch of at
- * most 128 threads per SM, else 128).  No counterpart in the reference,
- * which steps one trajectory at a time on the host. */
-int cr_engine_set_launch(cr_engine* e, int threads_per_block);
-int cr_engine_get_launch(cr_engine* e, int* threads_per_block, int* blocks);
-/* Autotuner: times nsteps steps at each launch shape (G, 32, 64, 128, 256
- * threads per block, those that fit), each from the same saved state, which
- * is then put back (q, p, f, epot, status, chain velocities, step counter);
- * keeps the fastest and returns it with its time per step.  The noise is a
- * function of the step index, so the trials leave no trace in the run. */
-int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, float* ms_per_step);
+ * trajectory's beads sit on G = next_pow2(nbeads) threads, each served by
+ * threads_per_bead (1, 2 or 4; 4 is built for H3 and OH + H2, 1 for CH4 + H
+ * and CH4 + OH) threads that split the bead's atoms between them for the
+ * integrator's per-coordinate work; threads_per_block (a multiple of
+ * G x threads_per_bead, <= 256) sets how many trajectories share a block.
+ * threads_per_block = 0 restores the built-in choice (one thread per bead,
+ * 32 threads per block for a batch of at most 128 threads per SM, else 128).
+ * No counterpart in the reference, which steps one trajectory at a time on
+ * the host. */
+int cr_engine_set_launch(cr_engine* e, int threads_per_block, int threads_per_bead);
+int cr_engine_get_launch(cr_engine* e, int* threads_per_block, int* blocks, int* threads_per_bead);
+/* Autotuner: times nsteps steps at each launch shape (threads per bead 1, 2,
+ * 4 as built; G x threads_per_bead, 32, 64, 128, 256 threads per block, those
+ * that fit), each from the same saved state, which is then put back (q, p,
+ * f, epot, status, chain velocities, step counter); keeps the fastest and
+ * returns it with its time per step.  The noise is a function of the step
+ * index, so the trials leave no trace in the run. */
+int cr_engine_autotune(cr_engine* e, int nsteps, int* threads_per_block, int* threads_per_bead,
+                       float* ms_per_step);
 
 /* ---- batches of trajectory classes -----------------------------------------
  * One graph launch per chunk of steps advances several engines (classes with
@@ -530,6 +551,10 @@ int cr_batch_run(cr_batch* b, int nsteps);
 /* kernels launched by the last cr_batch_run, kernels per chunk graph, its
  * device time in ms */
 int cr_batch_info(const cr_batch* b, long long* launches, int* graph_nodes, float* ms);
+/* Timeline of the last graph launch of cr_batch_run: per engine, when its
+ * branch began and ended, in ms after the launch began (events recorded
+ * inside the graph).  Branches whose intervals overlap ran concurrently. */
+int cr_batch_timeline(const cr_batch* b, float* begin_ms, float* end_ms);
 int cr_batch_destroy(cr_batch* b);
 
 /* ---- adjoint of the step (parameter fitting through trajectories) --------

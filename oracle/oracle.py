@@ -118,6 +118,15 @@ def set_qmdff(ff, tables, coul_cut=50.0, zahn=False, zahn_a=0.0, zahn_par=0.0):
     lib().orc_qmdff_set(C.byref(d))
 
 
+def set_qmdff_periodic(box_ang, coul_cut_ang=50.0, vdw_cut_ang=10.0):
+    """set_periodic for the current QMDFF: returns (coul_cut, vdw_cut,
+    zahn_a, zahn_par) in bohr as set."""
+    box = np.ascontiguousarray(box_ang, dtype=np.float64)
+    out = np.zeros(4)
+    lib().orc_qmdff_set_periodic(_dp(box), float(coul_cut_ang), float(vdw_cut_ang), _dp(out))
+    return tuple(out)
+
+
 class XiDef(C.Structure):
     _fields_ = [("nreac1", C.c_int), ("reac1", C.c_int * 8), ("nreac2", C.c_int),
                 ("reac2", C.c_int * 8), ("form", C.c_int * 2), ("brk", C.c_int * 2),
@@ -165,6 +174,7 @@ def lib():
                                  C.POINTER(C.c_int), C.c_int, d]
         _lib.orc_qmdff_set.argtypes = [C.POINTER(QmdffDef)]
         _lib.orc_qmdff_set2.argtypes = [C.POINTER(QmdffDef)]
+        _lib.orc_qmdff_set_periodic.argtypes = [d, C.c_double, C.c_double, d]
         _lib.orc_evb_set.argtypes = [C.c_int, d]
         _lib.orc_nhc_half.argtypes = [C.POINTER(Cfg), d, d]
         _lib.orc_evb_fit.argtypes = [C.c_int, d, C.c_int, C.c_int, d, d, d, d, d]

@@ -79,6 +79,16 @@ void orc_water_set(int nwater, int periodic, const double* len, double coul_cut,
   b.zahn_par = zahn_par;
 }
 
+void orc_qmdff_set_periodic(const double* box_ang, double coul_cut_ang, double vdw_cut_ang, double* cuts) {
+  orc::qmdff::set_periodic(g_qmdff, box_ang, coul_cut_ang, vdw_cut_ang);
+  if (cuts) {
+    cuts[0] = g_qmdff.coul_cut;
+    cuts[1] = g_qmdff.vdw_cut;
+    cuts[2] = g_qmdff.zahn_a;
+    cuts[3] = g_qmdff.zahn_par;
+  }
+}
+
 void orc_qmdff_set2(const orc_qmdff_def* d) {
   orc::qmdff::FF keep = g_qmdff;
   orc_qmdff_set(d);

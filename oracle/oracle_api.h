@@ -85,6 +85,10 @@ typedef struct orc_qmdff_def {
 
 /* Sets the force field used by PES id 4 (QMDFF) in all oracle entry points. */
 void orc_qmdff_set(const orc_qmdff_def* d);
+/* set_periodic for the current force field: box edges and cutoffs in
+ * Angstrom; cuts (may be NULL) receives coul_cut, vdw_cut, zahn_a, zahn_par
+ * as set (bohr). */
+void orc_qmdff_set_periodic(const double* box_ang, double coul_cut_ang, double vdw_cut_ang, double* cuts);
 /* The second force field and the coupling of PES id 5 (dE-EVB of the two):
  * basis 0..7 = const, 1g, 2g, 3g, sp, sd, sd2, sp2d; par = offa..offh, offm, offn. */
 void orc_qmdff_set2(const orc_qmdff_def* d);

@@ -24,6 +24,7 @@
 // REAL(4) literals reproduced: abdamp's cutoff 3.0 * 3.5710642 (a float
 // product), eps1(3) = 0.85 (src/setnonb.f90:164-190).
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -67,7 +68,48 @@ struct FF {
   bool zahn = false;
   double zahn_a = 0.0, zahn_par = 0.0;
   double e_zero = 0.0;
+  // periodic box (src/set_periodic.f90, pbc_mod): edges and halves (bohr),
+  // dispersion/repulsion cutoff
+  bool periodic = false;
+  double len[3] = {0, 0, 0}, half[3] = {0, 0, 0};
+  double vdw_cut = 0.0;
 };
+
+// box_image (src/box_image.f90:36-63): subtract the edge while a component
+// exceeds half of it (bounded here at 64 subtractions).
+template <class T>
+inline void box_image(const FF& ff, T* v) {
+  if (!ff.periodic) return;
+  for (int k = 0; k < 3; ++k)
+    for (int it = 0; it < 64 && (v[k] > T(ff.half[k]) || v[k] < T(-ff.half[k])); ++it)
+      v[k] = v[k] - T(v[k] > T(0.0) ? ff.len[k] : -ff.len[k]);
+}
+
+// set_periodic (src/set_periodic.f90:67-113): box edges and the Coulomb and
+// dispersion cutoffs from Angstrom; a Coulomb cutoff below 5 bohr becomes
+// half the shortest edge minus 0.1 bohr, the Zahn form fixes it at 10 A and
+// sets its parameters, and no cutoff may exceed half the shortest edge.
+inline void set_periodic(FF& ff, const double box_ang[3], double coul_cut_ang, double vdw_cut_ang) {
+  const double bohr = 0.52917721092;
+  ff.periodic = true;
+  for (int k = 0; k < 3; ++k) {
+    ff.len[k] = box_ang[k] / bohr;
+    ff.half[k] = ff.len[k] * 0.5;
+  }
+  const double hmin = std::min(ff.half[0], std::min(ff.half[1], ff.half[2]));
+  ff.coul_cut = coul_cut_ang / bohr;
+  ff.vdw_cut = vdw_cut_ang / bohr;
+  if (ff.coul_cut < 5.0) ff.coul_cut = hmin - 0.1;
+  if (ff.zahn) {
+    const double spi = std::sqrt(3.14159265358979323846);
+    ff.zahn_a = 0.2 * bohr;
+    ff.coul_cut = 10.0 / bohr;
+    const double acut = ff.zahn_a * ff.coul_cut;
+    ff.zahn_par = std::erfc(acut) / (ff.coul_cut * ff.coul_cut) +
+                  2 * ff.zahn_a / spi * std::exp(-acut * acut) / ff.coul_cut;
+  }
+  if (ff.coul_cut > hmin) ff.coul_cut = hmin - 0.1;
+}
 
 template <class T>
 inline T vlen(const T* a) {
@@ -228,6 +270,7 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
     int i = ff.bond[2 * m], j = ff.bond[2 * m + 1];
     T rb[3];
     for (int c = 0; c < 3; ++c) rb[c] = x[3 * i + c] - x[3 * j + c];
+    box_image(ff, rb);
     T r2 = rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2];
     T r = sqrt(r2);
     T rij = ff.vbond[3 * m], kij = ff.vbond[3 * m + 1], aai = ff.vbond[3 * m + 2];
@@ -248,6 +291,8 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
       vab[c] = x[3 * i + c] - x[3 * j + c];
       vcb[c] = x[3 * k + c] - x[3 * j + c];
     }
+    box_image(ff, vab);
+    box_image(ff, vcb);
     T rab2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
     T rcb2 = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
     crprod(vcb, vab, vp);
@@ -300,6 +345,9 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
         vcb[c] = x[3 * j + c] - x[3 * k + c];
         vdc[c] = x[3 * k + c] - x[3 * l + c];
       }
+      box_image(ff, vab);
+      box_image(ff, vcb);
+      box_image(ff, vdc);
       T rij = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
       T rjk = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
       T rkl = vdc[0] * vdc[0] + vdc[1] * vdc[1] + vdc[2] * vdc[2];
@@ -347,6 +395,9 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
         vcb[c] = x[3 * j + c] - x[3 * k + c];
         vdc[c] = x[3 * j + c] - x[3 * l + c];
       }
+      box_image(ff, vab);
+      box_image(ff, vcb);
+      box_image(ff, vdc);
       T rij = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
       T rjk = vcb[0] * vcb[0] + vcb[1] * vcb[1] + vcb[2] * vcb[2];
       T rjl = vdc[0] * vdc[0] + vdc[1] * vdc[1] + vdc[2] * vdc[2];
@@ -390,8 +441,10 @@ inline void ff_nonb(const FF& ff, const T* x, T* enb, T* g) {
     int i1 = ff.nci[3 * kp], i2 = ff.nci[3 * kp + 1], nk = ff.nci[3 * kp + 2];
     T vab[3];
     for (int c = 0; c < 3; ++c) vab[c] = x[3 * i1 + c] - x[3 * i2 + c];
+    box_image(ff, vab);
     T r2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
     T r = sqrt(r2);
+    if (ff.periodic && r > T(ff.vdw_cut)) continue;
     T oner = 1.0 / r;
     T R0 = ff.pR0[kp], c6 = ff.pC6[kp];
     T r4 = r2 * r2, r6 = r4 * r2;
@@ -421,6 +474,7 @@ inline void ff_nonb(const FF& ff, const T* x, T* enb, T* g) {
     int i1 = ff.nci[3 * kp], i2 = ff.nci[3 * kp + 1], nk = ff.nci[3 * kp + 2];
     T vab[3];
     for (int c = 0; c < 3; ++c) vab[c] = x[3 * i1 + c] - x[3 * i2 + c];
+    box_image(ff, vab);
     T r2 = vab[0] * vab[0] + vab[1] * vab[1] + vab[2] * vab[2];
     T r = sqrt(r2);
     if (r > ff.coul_cut) continue;
@@ -444,7 +498,7 @@ inline void ff_nonb(const FF& ff, const T* x, T* enb, T* g) {
 // eabhag (src/eabhag.f90:35-220): one hydrogen bond A...H-B, energy and
 // analytic gradient accumulated into e, g; nothing if E > -1e-8.
 template <class T>
-inline void eabhag(const T* x, int A, int B, int H, double ca, double cb, T* e, T* g) {
+inline void eabhag(const FF& ff, const T* x, int A, int B, int H, double ca, double cb, T* e, T* g) {
   const double longcut = 8.0, alp7 = 12.0, alp3 = 6.0;
   T drah[3], drbh[3], drab[3];
   for (int c = 0; c < 3; ++c) {
@@ -452,6 +506,7 @@ inline void eabhag(const T* x, int A, int B, int H, double ca, double cb, T* e, 
     drbh[c] = x[3 * B + c] - x[3 * H + c];
     drab[c] = x[3 * A + c] - x[3 * B + c];
   }
+  box_image(ff, drah);  // as src/eabhag.f90:60-62 (the A-H vector only)
   T rab2 = drab[0] * drab[0] + drab[1] * drab[1] + drab[2] * drab[2];
   T rab = sqrt(rab2);
   T rah2 = drah[0] * drah[0] + drah[1] * drah[1] + drah[2] * drah[2];
@@ -582,9 +637,10 @@ inline void ff_hb(const FF& ff, const T* x, T* eh, T* g) {
     const int i1 = ff.hb[3 * k], i2 = ff.hb[3 * k + 1], i = ff.hb[3 * k + 2];
     T rb[3];
     for (int c = 0; c < 3; ++c) rb[c] = x[3 * i1 + c] - x[3 * i2 + c];
+    box_image(ff, rb);
     T r = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
     if (r > 15.0) continue;
-    if (ff.at[i] == 1) eabhag<T>(x, i1, i2, i, ff.vhb[2 * k], ff.vhb[2 * k + 1], eh, g);
+    if (ff.at[i] == 1) eabhag<T>(ff, x, i1, i2, i, ff.vhb[2 * k], ff.vhb[2 * k + 1], eh, g);
     else eabxag<T>(x, ff.n, i1, i2, i, ff.vhb[2 * k], eh, g);
   }
 }

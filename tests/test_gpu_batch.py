@@ -52,6 +52,10 @@ def test_batch_equals_separate_runs(require_gpu, precision):
         assert not sa[4].any()
     info = batch.info()
     assert info["launches"] > 0 and info["graph_nodes"] > 0
+    # each class branch's first and last node of the last graph launch
+    tl = batch.timeline()
+    assert len(tl) == len(a)
+    assert all(0.0 <= t0 <= t1 <= info["ms"] + 1e-3 for t0, t1 in tl), tl
     batch.close()
 
 

@@ -105,22 +105,30 @@ def test_h_h2_reference_example(require_gpu, tmp_path):
     pmax, perr = res["pmf_max_kjmol"], res["pmf_max_stderr_kjmol"]
     print(f"kappa(50 fs) = {kap:.4f} +- {kerr:.4f}; PMF max = {pmax:.2f} +- {perr:.2f} kJ/mol "
           f"at xi = {res['xi_barrier']:.4f}; k(T) = {res['k_t']:.4e} cm^3/mol/s")
+    # The figures are one run of Caracal with the example's sample sizes, so
+    # their statistical error equals this run's: the difference of the two
+    # estimates has sqrt(2) times this run's standard error, held here to 3 of
+    # those, plus the reading error of the figure (0.005 in kappa, 0.5 kJ/mol).
+    z = 3.0 * np.sqrt(2.0)
     assert len(res["kappa_t"]) == 500
-    assert abs(kap - 0.767) <= 3.0 * kerr + 0.005
-    assert abs(pmax - 48.5) <= 3.0 * perr + 0.5
+    assert abs(kap - 0.767) <= z * kerr + 0.005
+    assert abs(pmax - 48.5) <= z * perr + 0.5
     assert abs(res["xi_barrier"] - 1.0) <= 0.02
-    # the whole curves of the manual's figures (digitised, reading error
-    # ~0.001 in kappa and ~0.1 kJ/mol on flat parts): kappa(t) within 3
-    # standard errors of this run at each time, the PMF along xi within 3
-    # standard errors of its maximum (the integrated error grows with xi)
+    # the whole curves (digitised): kappa(t) against this run's error at each
+    # time, the PMF against the error of its maximum (the integrated error
+    # grows along xi)
     fk = np.loadtxt(os.path.join(ROOT, "tests", "golden", "reference", "figure_kappa_h3.txt"))
     fp = np.loadtxt(os.path.join(ROOT, "tests", "golden", "reference", "figure_pmf_h3.txt"))
     dt_fs = 0.1
-    for t in (5.0, 10.0, 20.0, 30.0, 40.0):
+    rows = []
+    for t in (2.5, 5.0, 10.0, 20.0, 30.0, 40.0):
         i = int(round(t / dt_fs)) - 1
-        want = np.interp(t, fk[:, 0], fk[:, 1])
-        assert abs(res["kappa_t"][i] - want) <= 3.0 * res["kappa_t_stderr"][i] + 0.005, (t, res["kappa_t"][i], want)
-    for xi in (0.2, 0.4, 0.6, 0.8, 0.9):
-        got = np.interp(xi, res["coord"], res["pmf_kjmol"])
-        want = np.interp(xi, fp[:, 0], fp[:, 1])
-        assert abs(got - want) <= 3.0 * perr + 0.5, (xi, got, want)
+        rows.append((t, res["kappa_t"][i], np.interp(t, fk[:, 0], fk[:, 1]), res["kappa_t_stderr"][i]))
+    pm = [(xi, np.interp(xi, res["coord"], res["pmf_kjmol"]), np.interp(xi, fp[:, 0], fp[:, 1]))
+          for xi in (0.2, 0.4, 0.6, 0.8, 0.9)]
+    print("kappa(t): t, run, figure, stderr", rows)
+    print("PMF(xi): xi, run, figure", pm)
+    for t, got, want, err in rows:
+        assert abs(got - want) <= z * err + 0.005, (t, got, want, err)
+    for xi, got, want in pm:
+        assert abs(got - want) <= z * perr + 0.5, (xi, got, want)

@@ -151,7 +151,7 @@ def test_init_matches_oracle(gpu_ff, alkane):
 
 
 @pytest.mark.parametrize("thermostat", ["andersen", "pile", "none"])
-@pytest.mark.parametrize("nbeads", [1, 2, 3, 4, 6, 8, 16, 64])
+@pytest.mark.parametrize("nbeads", [1, 2, 3, 4, 6, 8, 16, 32, 64])
 def test_single_step_matches_oracle(gpu_ff, alkane, thermostat, nbeads):
     eng, cfg = make_pair(gpu_ff, alkane, nbeads, 2, thermostat, andersen_step=1)
     q, p, f, e = start(eng, cfg, alkane)
@@ -179,15 +179,18 @@ def test_orthonormal_modes_step_matches_oracle(gpu_ff, alkane, thermostat, nbead
     assert rel_err(qg, qo) <= 1e-11 and rel_err(pg, po) <= 1e-11 and rel_err(eg, eo) <= 1e-11
 
 
-@pytest.mark.parametrize("thermostat,nbeads", [("andersen", 8), ("pile", 6), ("none", 4)])
+@pytest.mark.parametrize("thermostat,nbeads", [("andersen", 8), ("pile", 6), ("none", 4), ("andersen", 64),
+                                               ("none", 32)])
 def test_trajectory_matches_oracle(gpu_ff, alkane, thermostat, nbeads):
+    """100 steps (two runs) against the oracle; P = 32 and 64 take the fast
+    cosine-transform drift."""
     eng, cfg = make_pair(gpu_ff, alkane, nbeads, 2, thermostat, andersen_step=5)
     q, p, f, e = start(eng, cfg, alkane)
-    eng.run(12)
-    eng.run(8)
+    eng.run(37)
+    eng.run(63)
     qg, pg, fg, eg, st = eng.get_state()
     eng.close()
-    qo, po, fo, eo, sto = orc.run(cfg, q, p, f, 20)
+    qo, po, fo, eo, sto = orc.run(cfg, q, p, f, 100)
     assert rel_err(qg, qo) <= 1e-9
     assert rel_err(pg, po) <= 1e-9
     assert rel_err(eg, eo) <= 1e-9
@@ -452,3 +455,40 @@ def test_call_site_pieces_sum_to_egrad(require_gpu, glutathione, prec, tol):
     ez = glutathione.e_zero
     assert np.abs(e + ez - ef).max() <= tol * np.abs(e).max() + 4.0 * np.spacing(abs(ez))
     assert rel_err(g, gf) <= tol
+
+
+@pytest.mark.parametrize("zahn", [False, True])
+def test_periodic_box_matches_oracle(require_gpu, glutathione, zahn):
+    """PERIODIC: glutathione (about 15 A long) in a 24 A box with a 6 A
+    dispersion cutoff (Coulomb at half the box, or the Zahn form at 10 A), so
+    long intramolecular pairs take their nearest image: the device against
+    the oracle (Caracal's box_image at its call sites); the same geometries
+    with atoms moved by box edges: the device unchanged (every vector is
+    imaged; Caracal's raw-coordinate dihedrals would not be)."""
+    ff = glutathione
+    tab = Q.ElementTables.caracal()
+    box = np.array([24.0, 24.0, 24.0])
+    orc.set_qmdff(ff, tab, zahn=zahn)
+    oc = orc.set_qmdff_periodic(box, 50.0, 6.0)
+    gff = QMDFFForceField(ff, tab, zahn=zahn)
+    dc = gff.set_periodic(box, 50.0, 6.0)
+    assert np.allclose(dc, oc, rtol=0, atol=0)
+    x = ff.xyz[None] + np.random.default_rng(8).normal(0, 0.05, (16,) + ff.xyz.shape)
+    e, g = gff.egrad(x, "fp64")
+    eo, go = orc.egrad("qmdff", x)
+    assert rel_err(e, eo) <= 1e-12 and rel_err(g, go) <= 1e-11
+    gff.set_periodic(None)
+    en, _ = gff.egrad(x, "fp64")
+    assert np.abs(en - e).min() > 1e-6                 # the cutoffs and images act
+    gff.set_periodic(box, 50.0, 6.0)
+    L = box / 0.52917721092
+    xw = x.copy()
+    shift = np.random.default_rng(9).integers(-1, 2, xw.shape[:2] + (3,))
+    shift[:, 0] = 0                                    # atom 0 stays
+    xw += shift * L
+    ew, gw = gff.egrad(xw, "fp64")
+    assert rel_err(ew, e) <= 1e-12 and rel_err(gw, g) <= 1e-11
+    em, gm = gff.egrad(xw, "mixed")
+    assert rel_err(gm, g) <= 1e-6 and rel_err(em, e) <= 1e-6
+    gff.close()
+    orc.set_qmdff(ff, tab)

@@ -141,3 +141,37 @@ def test_qmdff_file_round_trip_with_hbonds(tmp_path):
     rd = Q.read_qmdff(path)
     assert np.array_equal(rd.hb, ff.hb) and np.array_equal(rd.nci, ff.nci)
     np.testing.assert_allclose(Q.hb_parameters(rd), Q.hb_parameters(ff), atol=1e-10)
+
+
+def test_periodic_rules_and_large_box_limit():
+    """set_periodic's cutoff rules (src/set_periodic.f90:67-113), and a box
+    far larger than the molecule with cutoffs beyond every pair: the same
+    energy and gradient as the non-periodic force field."""
+    from caracal_gb300 import qmdff as Q
+    ff = Q.alkane()
+    tab = Q.ElementTables.caracal()
+    bohr = 0.52917721092
+    x = ff.xyz[None] + np.random.default_rng(3).normal(0, 0.05, (4,) + ff.xyz.shape)
+    orc.set_qmdff(ff, tab)
+    e0, g0 = orc.egrad("qmdff", x)
+    cuts = orc.set_qmdff_periodic([400.0, 400.0, 400.0], 150.0, 150.0)
+    assert cuts[0] == 150.0 / bohr and cuts[1] == 150.0 / bohr
+    e1, g1 = orc.egrad("qmdff", x)
+    assert np.array_equal(e0, e1) and np.array_equal(g0, g1)
+    # a Coulomb cutoff beyond half the shortest edge: half of it minus 0.1 bohr;
+    # one below 5 bohr: the same
+    assert orc.set_qmdff_periodic([30.0, 24.0, 40.0], 50.0, 10.0)[0] == 12.0 / bohr - 0.1
+    assert orc.set_qmdff_periodic([30.0, 24.0, 40.0], 2.0, 10.0)[0] == 12.0 / bohr - 0.1
+    # the dispersion cutoff removes pairs: the energy changes
+    orc.set_qmdff_periodic([400.0, 400.0, 400.0], 150.0, 4.0)
+    e2, _ = orc.egrad("qmdff", x)
+    assert not np.allclose(e2, e0)
+    # Zahn: the cutoff is fixed at 10 A with its parameters
+    orc.set_qmdff(ff, tab, zahn=True)
+    c = orc.set_qmdff_periodic([30.0, 30.0, 30.0], 50.0, 10.0)
+    a = 0.2 * bohr
+    rc = 10.0 / bohr
+    from math import erfc, exp, pi, sqrt
+    assert c[0] == rc and c[2] == a
+    assert abs(c[3] - (erfc(a * rc) / rc ** 2 + 2 * a / sqrt(pi) * exp(-(a * rc) ** 2) / rc)) < 1e-15
+    orc.set_qmdff(ff, tab)
