@@ -390,10 +390,13 @@ def run_ours(args):
     wl = workload(args.workload)
     K, W = args.steps, args.warmup
     cap = W + K * 52 + args.e2e_steps + 16  # every step the engines take in this process
+    shape = [int(v) for v in args.launch.split(",")] if args.launch else None
     if args.profile:
         # only the engine launches (for ncu): W warm-up steps and K timed steps per form
         for prec in ("fp64", "mixed"):
             eng = make_engine(wl, prec, traj0=rank * wl.ntraj, max_steps=cap)
+            if shape:
+                eng.set_launch(*shape)
             eng.run(W)
             eng.run(K)
             print(json.dumps({"profile": wl.name, "precision": prec, "steps": K,
@@ -408,6 +411,10 @@ def run_ours(args):
     tuned = {}
     if wl.pes not in ("qmdff", "water"):
         for name, eng in (("mixed", eng_mx), ("fp64", eng_64)):
+            if shape:
+                eng.set_launch(*shape)
+                tuned[name] = {"threads_per_block": shape[0], "threads_per_bead": shape[1], "given": True}
+                continue
             b, tpb, ms = eng.autotune(min(max(K, 10), 50))
             tuned[name] = {"threads_per_block": b, "threads_per_bead": tpb, "trial_ms_per_step": ms}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -922,6 +929,9 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="run only the engine launches (small ncu captures)")
     ap.add_argument("--chunk", type=int, default=50, help="steps per batch graph (classes workloads)")
+    ap.add_argument("--launch", default="",
+                    help="threads_per_block,threads_per_bead of the persistent kernel instead of the autotuner "
+                         "(analytic workloads; used by the profiling commands)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

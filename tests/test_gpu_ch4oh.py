@@ -100,4 +100,4 @@ def test_ch4oh_mixed_force_error(require_gpu):
     _, _, f32, v32, _ = e32.get_state()
     err = rel_err(f32, f64)
     print(f"CH4OH mixed-form force error {err:.3e}, energy error {rel_err(v32, v64):.3e}")
-    assert err < 5e-6 and rel_err(v32, v64) < 5e-6
+    assert err < 1.5e-6 and rel_err(v32, v64) < 1.5e-6      # measured 6.8e-7 to 7.5e-7

@@ -1,8 +1,8 @@
 """GPU: Caracal's ANA_OH3 surface (OH + H2, src/egrad_oh3.f) through the
 C-ABI and in the persistent step kernel against the oracle.  Tolerances
 (norm-wise relative): FP64 energies and gradients <= 1e-12; one step
-<= 1e-12 (forces at the step's own positions), 20 steps <= 1e-9; mixed
-form force error <= 1e-5 of the largest force (FP32 surface, FP64
+<= 1e-12 (forces at the step's own positions), 100 steps <= 1e-9; mixed
+form force error <= 1.5e-6 of the largest force (FP32 surface, FP64
 distances and gradient assembly)."""
 import numpy as np
 import pytest
@@ -45,11 +45,11 @@ def test_engine_steps_match_oracle(require_gpu, nbeads):
     assert rel_err(q1, qo) <= 1e-12 and rel_err(p1, po) <= 1e-12
     _, g_at = orc.egrad("oh3", q1.reshape(-1, 4, 3))
     assert rel_err(f1, g_at.reshape(f1.shape)) <= 1e-12
-    eng.run(19)
-    q20, p20, _, e20, _ = eng.get_state()
-    qo, po, fo, eo, so = orc.run(cfg, q, p, f, 20)
+    eng.run(99)
+    q100, p100, _, e100, _ = eng.get_state()
+    qo, po, fo, eo, so = orc.run(cfg, q, p, f, 100)
     eng.close()
-    assert rel_err(q20, qo) <= 1e-9 and rel_err(p20, po) <= 1e-9 and rel_err(e20, eo) <= 1e-9
+    assert rel_err(q100, qo) <= 1e-9 and rel_err(p100, po) <= 1e-9 and rel_err(e100, eo) <= 1e-9
 
 
 def test_mixed_force_error(require_gpu):
@@ -64,4 +64,4 @@ def test_mixed_force_error(require_gpu):
         eng.close()
     err = np.max(np.abs(out["mixed"] - out["fp64"])) / np.max(np.abs(out["fp64"]))
     print(f"oh3 mixed force error {err:.3e}")
-    assert err <= 1e-5
+    assert err <= 1.5e-6           # measured 5.6e-7 (FP32 surface, FP64 distances)
