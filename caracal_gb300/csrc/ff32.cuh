@@ -60,6 +60,7 @@ __device__ __forceinline__ ff operator/(ff a, ff b) {
 }
 __device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
 __device__ __forceinline__ ff& operator-=(ff& a, ff b) { return a = a - b; }
+__device__ __forceinline__ ff& operator+=(ff& a, float b) { return a = a + b; }
 
 __device__ __forceinline__ ff ff_sqrt(ff a) {
   if (!(a.hi > 0.f)) return ff{0.f, 0.f};

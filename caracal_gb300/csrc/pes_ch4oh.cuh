@@ -20,8 +20,18 @@
 // away at compile time.  GPU restructuring as for CH4 + H (unrolled loops,
 // shared reciprocals, the opbend k <-> l swap as a sign); the energy and
 // gradient unit factors 0.03812 and 0.0201723 are the reference's.
+//
+// Mixed form (F = float): as for CH4 + H, positions enter as float pairs
+// (ff32.cuh), the LEPS stretch block -- whose Q and exchange derivatives are
+// large and cancel near the bond minima -- and the in-plane bends' angle
+// differences from their references are formed in float-pair arithmetic,
+// and the stretch gradient is summed as float pairs; the rest is FP32.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "ff32.cuh"
 
 namespace cr {
 namespace ch4oh {
@@ -95,14 +105,42 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
 #pragma unroll
   for (int x = 0; x < 21; ++x) qa[x] = qb[x] * 0.52918;
   Geo<F> G;
+  constexpr bool kPair = std::is_same<F, float>::value;
+  ff Xtcb[3], Xtno[3], Xtch[4][3], Xtbh[4][3], Xrch[4];
+  if constexpr (kPair) {
+    ff X[21];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    G.tcb[d] = (F)(qa[3 * NC + d] - qa[3 * NB + d]);
-    G.tno[d] = (F)(qa[3 * NO + d] - qa[3 * NB + d]);
+    for (int x = 0; x < 21; ++x) {
+      const float h = __double2float_rn(qa[x]);
+      X[x] = ff{h, __double2float_rn(qa[x] - (double)h)};
+    }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      G.tch[i][d] = (F)(qa[3 * NC + d] - qa[3 * NH(i) + d]);
-      G.tbh[i][d] = (F)(qa[3 * NB + d] - qa[3 * NH(i) + d]);
+    for (int d = 0; d < 3; ++d) {
+      Xtcb[d] = X[3 * NC + d] - X[3 * NB + d];
+      G.tcb[d] = ff_float(Xtcb[d]);
+      Xtno[d] = X[3 * NO + d] - X[3 * NB + d];
+      G.tno[d] = ff_float(Xtno[d]);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        Xtch[i][d] = X[3 * NC + d] - X[3 * NH(i) + d];
+        Xtbh[i][d] = X[3 * NB + d] - X[3 * NH(i) + d];
+        G.tch[i][d] = ff_float(Xtch[i][d]);
+        G.tbh[i][d] = ff_float(Xtbh[i][d]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      Xrch[i] = ff_sqrt(Xtch[i][0] * Xtch[i][0] + Xtch[i][1] * Xtch[i][1] + Xtch[i][2] * Xtch[i][2]);
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      G.tcb[d] = (F)(qa[3 * NC + d] - qa[3 * NB + d]);
+      G.tno[d] = (F)(qa[3 * NO + d] - qa[3 * NB + d]);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        G.tch[i][d] = (F)(qa[3 * NC + d] - qa[3 * NH(i) + d]);
+        G.tbh[i][d] = (F)(qa[3 * NB + d] - qa[3 * NH(i) + d]);
+      }
     }
   }
   G.rcb = t_sqrt<F>(G.tcb[0] * G.tcb[0] + G.tcb[1] * G.tcb[1] + G.tcb[2] * G.tcb[2]);
@@ -121,6 +159,11 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
   F pdot[21];
 #pragma unroll
   for (int x = 0; x < 21; ++x) pdot[x] = F(0);
+  // mixed form: the stretch gradient, summed as float pairs (its terms are
+  // large and cancel on each atom); the other terms add into pdot in FP32
+  ff psx[kPair ? 21 : 1];
+#pragma unroll
+  for (int x = 0; x < (kPair ? 21 : 1); ++x) psx[x] = ff{0.f, 0.f};
 
   // ---- switching functions (switchf_ch4oh)
   F s1[4], ds1[4], s2[4], ds2[4], s3[4], ds3[4], sphi[4], dsphi[4], sth[4], dsth[4];
@@ -161,11 +204,13 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
   const double pi = 3.141592653589793;
   const F A = F(tau - 0.5 * pi), B = F(tau - 2.0 * pi / 3.0);
   F th0[4][4], dth0[4][4][4];
+  F th0m[4][4];  // th0 - tau, without the rounding of tau (the mixed form's bend differences)
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       th0[i][j] = F(0);
+      th0m[i][j] = F(0);
 #pragma unroll
       for (int k = 0; k < 4; ++k) dth0[i][j][k] = F(0);
     }
@@ -181,9 +226,12 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
           if (m < 0) m = k;
           else n = k;
         }
-      F t = F(tau) + A * (sphi[i] * sphi[j] - F(1)) + B * (sth[m] * sth[n] - F(1));
+      const F tm = A * (sphi[i] * sphi[j] - F(1)) + B * (sth[m] * sth[n] - F(1));
+      F t = F(tau) + tm;
       th0[i][j] = t;
       th0[j][i] = t;
+      th0m[i][j] = tm;
+      th0m[j][i] = tm;
       F di = A * dsphi[i] * sphi[j], dj = A * sphi[i] * dsphi[j];
       F dm = B * dsth[m] * sth[n], dn = B * sth[m] * dsth[n];
       dth0[i][j][i] = di; dth0[j][i][i] = di;
@@ -194,6 +242,98 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
 
   // ---- stretching (stretch_ch4oh)
   F vstr = F(0);
+  if constexpr (kPair) {
+    // Mixed form.  Per C-H bond i the LEPS gradient collapses onto three
+    // scalars: T_i (along the C-H_i stretch, Q and exchange terms together),
+    // U_i (C-O) and W_i (O-H_i), formed in float-pair arithmetic and rounded
+    // once; the vectors they multiply are float pairs too.
+    const F rav = (G.rch[0] + G.rch[1] + G.rch[2] + G.rch[3]) * F(0.25);
+    const F arga = F(c1ch) * (rav - F(r0ch));
+    F dumach;
+    if (arga < F(19.0)) {
+      const F ch = t_cosh<F>(arga);
+      dumach = F(b1ch * c1ch) / (F(2) * (ch * ch));
+    } else {
+      dumach = F(0);
+    }
+    constexpr ff D1ch = ff_const(d1ch), D3ch = ff_const(d3ch), D1hh = ff_const(d1hh), D3hh = ff_const(d3hh);
+    constexpr ff D1cb = ff_const(d1cb), D3cb = ff_const(d3cb);
+    constexpr ff Sqch = ff_const(d1ch + d3ch), Dfch = ff_const(d1ch - d3ch);
+    constexpr ff Sqhh = ff_const(d1hh + d3hh), Dfhh = ff_const(d1hh - d3hh);
+    constexpr ff Sqcb = ff_const(d1cb + d3cb), Dfcb = ff_const(d1cb - d3cb);
+    constexpr ff R0ch = ff_const(r0ch), R0hh = ff_const(r0hh), R0cb = ff_const(r0cb);
+    constexpr ff Acb = ff_const(acb), Ahh = ff_const(ahh);
+    auto norm3 = [](const ff (&v)[3]) { return ff_sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+    const ff rcb = norm3(Xtcb);
+    const ff ecb1 = ff_exp(-(Acb * (rcb - R0cb))), ecb2 = ecb1 * ecb1;
+    const ff vqcb = (D1cb * (ecb2 - ecb1 * 2.f) + D3cb * (ecb2 + ecb1 * 2.f)) * 0.5f;
+    const ff vjcb = (D1cb * (ecb2 - ecb1 * 2.f) - D3cb * (ecb2 + ecb1 * 2.f)) * 0.5f;
+    const ff dqcb = -(Acb * (Sqcb * ecb2 - Dfcb * ecb1));  // d vqcb / d rcb
+    const ff djcb = -(Acb * (Dfcb * ecb2 - Sqcb * ecb1));  // d vjcb / d rcb
+    // ach = a1 + b1 (tanh(arga) + 1) / 2 = a1 + b1 / (1 + exp(-2 arga))
+    ff achx = ff_const(a1ch + b1ch);
+    if (arga < F(19.0)) {
+      constexpr ff A1 = ff_const(a1ch), B1 = ff_const(b1ch), C1 = ff_const(c1ch);
+      const ff ravx = (Xrch[0] + Xrch[1] + Xrch[2] + Xrch[3]) * 0.25f;
+      const ff e2 = ff_exp(-(C1 * (ravx - R0ch)) * 2.f);
+      achx = A1 + B1 / (ff_from(1.f) + e2);
+    }
+    ff vsum = ff_from(0.f);
+    F achdc[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) achdc[d] = dumach * (G.uch[0][d] + G.uch[1][d] + G.uch[2][d] + G.uch[3][d]) * F(0.25);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const ff rch = Xrch[i], rbh = norm3(Xtbh[i]);
+      const ff xch = rch - R0ch;
+      const ff ec1 = ff_exp(-(achx * xch)), ec2 = ec1 * ec1;
+      const ff vqch = (D1ch * (ec2 - ec1 * 2.f) + D3ch * (ec2 + ec1 * 2.f)) * 0.5f;
+      const ff vjch = (D1ch * (ec2 - ec1 * 2.f) - D3ch * (ec2 + ec1 * 2.f)) * 0.5f;
+      const ff eh1 = ff_exp(-(Ahh * (rbh - R0hh))), eh2 = eh1 * eh1;
+      const ff vqbh = (D1hh * (eh2 - eh1 * 2.f) + D3hh * (eh2 + eh1 * 2.f)) * 0.5f;
+      const ff vjbh = (D1hh * (eh2 - eh1 * 2.f) - D3hh * (eh2 + eh1 * 2.f)) * 0.5f;
+      const ff e12 = vjch - vjcb, e23 = vjcb - vjbh, e31 = vjbh - vjch;
+      const ff vj = -ff_sqrt((e12 * e12 + e23 * e23 + e31 * e31) * 0.5f);
+      vsum += vqch + vqcb + vqbh + vj;
+      const ff factj = ff_recip(vj) * 0.5f;
+      const ff brq = Sqch * ec2 - Dfch * ec1, brj = Dfch * ec2 - Sqch * ec1;
+      const ff dqbh = -(Ahh * (Sqhh * eh2 - Dfhh * eh1)), djbh = -(Ahh * (Dfhh * eh2 - Sqhh * eh1));
+      // T: -(d V / d (ach * xch)); U: d V / d rcb (per unit rcb); W: d V / d rbh
+      const ff T = brq + (e12 - e31) * factj * brj;
+      const ff U = (-dqcb + (e12 - e23) * factj * djcb) / rcb;
+      const ff W = (dqbh + (e31 - e23) * factj * djbh) / rbh;
+      const ff irch = ff_recip(rch);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const ff u = Xtch[i][d] * irch;
+        const ff tcb = Xtcb[d], tbh = Xtbh[i][d];
+        const ff gc = achx * u + xch * achdc[d];
+        const ff gh = achx * u + xch * (dumach * G.uch[i][d] * F(0.25));
+        psx[3 * NC + d] -= gc * T + tcb * U;
+        psx[3 * NH(i) + d] += gh * T - tbh * W;
+        psx[3 * NB + d] += tcb * U + tbh * W;
+        const ff xT = xch * T;
+#pragma unroll
+        for (int k = 1; k <= 3; ++k) {
+          const int j = (i + k) & 3;
+          psx[3 * NH(j) + d] += xT * (dumach * G.uch[j][d] * F(0.25));
+        }
+      }
+    }
+    // O-H Morse stretch (stretch_ch4oh :602-605, :620-632, :711-716), its
+    // 1 - exp(-a (r - r0)) near the minimum in float pairs too
+    const ff rno = norm3(Xtno);
+    const ff eoh = ff_exp(-(Ahh * (rno - R0hh)));
+    const ff omo = ff_from(1.f) - eoh;
+    vsum += D1hh * (omo * omo);
+    const ff de = (ff_const(2.0 * ahh * d1hh) * omo * eoh) / rno;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      psx[3 * NB + d] -= de * Xtno[d];
+      psx[3 * NO + d] += de * Xtno[d];
+    }
+    vstr = ff_float(vsum);
+  } else
   {
     F rav = (G.rch[0] + G.rch[1] + G.rch[2] + G.rch[3]) * F(0.25);
     F arga = F(c1ch) * (rav - F(r0ch));
@@ -429,8 +569,22 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
         dfk0[m] = g0 * ds2[m] * s2[n];
         dfk0[n] = g0 * s2[m] * ds2[n];
         const F kf = fk0 * f1[i] * f1[j];
-        F costh = (G.uch[i][0] * G.uch[j][0] + G.uch[i][1] * G.uch[j][1] + G.uch[i][2] * G.uch[j][2]);
-        F dth = t_acos<F>(costh) - th0[i][j];
+        F costh, dth;
+        if constexpr (kPair) {
+          // theta - tau as asin(sin(theta - tau)) from a float-pair cosine:
+          // theta - th0 is a small difference of two ~1.9 rad angles
+          const ff c = (Xtch[i][0] * Xtch[j][0] + Xtch[i][1] * Xtch[j][1] + Xtch[i][2] * Xtch[j][2]) /
+                       (Xrch[i] * Xrch[j]);
+          constexpr ff kCosTau = ff_const(-1.0 / 3.0), kSinTau = ff_const(0.94280904158206336587);
+          const ff y = ff_sqrt(ff_from(1.f) - c * c) * kCosTau - c * kSinTau;
+          costh = ff_float(c);
+          const float dtau = fabsf(y.hi) < 0.9f ? asinf(y.hi) + y.lo / sqrtf(1.f - y.hi * y.hi)
+                                                : acosf(costh) - F(tau);
+          dth = dtau - th0m[i][j];
+        } else {
+          costh = (G.uch[i][0] * G.uch[j][0] + G.uch[i][1] * G.uch[j][1] + G.uch[i][2] * G.uch[j][2]);
+          dth = t_acos<F>(costh) - th0[i][j];
+        }
         vip += F(0.5) * kf * dth * dth;
         const F termth = F(-1) / t_sqrt<F>(F(1) - costh * costh);
         const F half_d2 = F(0.5) * dth * dth;
@@ -465,9 +619,25 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const F* tb = G.tbh[i];
-      F cosine = -(G.tno[0] * tb[0] + G.tno[1] * tb[1] + G.tno[2] * tb[2]) * (G.irno * G.irbh[i]);
-      cosine = fmin(F(1), fmax(F(-1), cosine));
-      const F dang = t_acos<F>(cosine) - F(anh2oeq);
+      F cosine, dang;
+      if constexpr (kPair) {
+        // angle - anh2oeq as asin(sin(angle - anh2oeq)) from a float-pair
+        // cosine: a small difference of two ~1.8 rad angles
+        const ff rno = ff_sqrt(Xtno[0] * Xtno[0] + Xtno[1] * Xtno[1] + Xtno[2] * Xtno[2]);
+        const ff rbh = ff_sqrt(Xtbh[i][0] * Xtbh[i][0] + Xtbh[i][1] * Xtbh[i][1] + Xtbh[i][2] * Xtbh[i][2]);
+        ff c = -((Xtno[0] * Xtbh[i][0] + Xtno[1] * Xtbh[i][1] + Xtno[2] * Xtbh[i][2]) / (rno * rbh));
+        if (c.hi > 1.f) c = ff_from(1.f);
+        if (c.hi < -1.f) c = ff_from(-1.f);
+        constexpr ff kCosEq = ff_const(-0.25398078034139054), kSinEq = ff_const(0.9672092654731852);
+        const ff y = ff_sqrt(ff_from(1.f) - c * c) * kCosEq - c * kSinEq;  // sin(angle - anh2oeq)
+        cosine = ff_float(c);
+        dang = fabsf(y.hi) < 0.9f ? asinf(y.hi) + y.lo / sqrtf(1.f - y.hi * y.hi)
+                                  : t_acos<F>(cosine) - F(anh2oeq);
+      } else {
+        cosine = -(G.tno[0] * tb[0] + G.tno[1] * tb[1] + G.tno[2] * tb[2]) * (G.irno * G.irbh[i]);
+        cosine = fmin(F(1), fmax(F(-1), cosine));
+        dang = t_acos<F>(cosine) - F(anh2oeq);
+      }
       const F arga = F(alph2o) * (G.rbh[i] - F(r0hh));
       const F fk = (arga < F(19.0)) ? F(fkh2oeq) * (F(1) - t_tanh<F>(arga)) : F(0);
       vip += F(0.5) * fk * dang * dang;
@@ -497,6 +667,10 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
   }
 
   Vout = (double)((vstr + vop + vip) * F(0.03812));
+  if constexpr (kPair) {
+#pragma unroll
+    for (int x = 0; x < 21; ++x) pdot[x] = ff_float(psx[x] + pdot[x]);
+  }
 #pragma unroll
   for (int x = 0; x < 21; ++x) gout[x] = (double)pdot[x] * 0.0201723;
 }

@@ -8,9 +8,16 @@
 // constants are the BLOCK DATA PTPACM_oh3 (V4POT reads ALP, CLAM, ACON and
 // VH2O reads CON through their COMMON layouts).  F is the arithmetic type of
 // the surface (double, or float in the mixed form); the distances are formed
-// in FP64 and the gradient is assembled in FP64.
+// in FP64 and the gradient is assembled in FP64.  Mixed form: the O-H Morse
+// of R1 (1 - exp(-b (R - Re)) cancels near its minimum) and the H2 LEPS term
+// (its Coulomb and exchange parts cancel) in double-FP32 arithmetic
+// (ff32.cuh) from the FP64 distances split into float pairs, the rest FP32.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "ff32.cuh"
 
 namespace cr {
 namespace oh3 {
@@ -66,6 +73,44 @@ __device__ inline F v3pot(const F (&r)[3], F (&dedr)[3]) {
     dedr[i] = b * x[i] * ((F(3) * exch[i] - s) * is2 * (op3z * x[i] - zp3) / rad - zp3 * x[i] + op3z);
   }
   return e;
+}
+
+// The same two terms in float-pair arithmetic (mixed form), rounded once.
+__device__ inline void morse_ff(double d, double b, double t, ff r, float& v, ff& dv) {
+  const ff bb = ff_const(b), dd = ff_const(d);
+  const ff ex = ff_exp(-(bb * (r - ff_const(t))));
+  const ff u = ff_from(1.f) - ex;
+  v = ff_float(dd * (u * u));
+  dv = bb * dd * u * ex * 2.f;
+}
+__device__ inline float v3pot_ff(const ff (&r)[3], ff (&dedr)[3]) {
+  constexpr double z = K::sato, zpo = 1.0 + z, op3z = 1.0 + 3.0 * z, top3z = 2.0 * op3z, zp3 = z + 3.0,
+                   tzp3 = 2.0 * zp3;
+  constexpr double de[3] = {K::de[0], K::de[0], K::de[2]};
+  constexpr double be[3] = {K::beta[0], K::beta[0], K::beta[2]};
+  constexpr double re[3] = {K::re[0], K::re[0], K::re[2]};
+  ff x[3], exch[3], do4z[3], e = ff_from(0.f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    do4z[i] = ff_const(de[i] / 4.0 / zpo);
+    x[i] = ff_exp(-(ff_const(be[i]) * (r[i] - ff_const(re[i]))));
+    e += do4z[i] * (ff_const(zp3) * x[i] - ff_const(top3z)) * x[i];
+    exch[i] = do4z[i] * (ff_const(op3z) * x[i] - ff_const(tzp3)) * x[i];
+  }
+  const ff d01 = exch[0] - exch[1], d12 = exch[1] - exch[2], d20 = exch[2] - exch[0];
+  const ff rad = ff_sqrt(d01 * d01 + d12 * d12 + d20 * d20);
+  constexpr ff is2 = ff_const(0.70710678118654752440);
+  e -= rad * is2;
+  const ff sx = exch[0] + exch[1] + exch[2];
+  const ff irad = ff_recip(rad);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const ff b = ff_const(be[i]) * do4z[i] * 2.f;
+    dedr[i] = b * x[i] *
+              ((exch[i] * 3.f - sx) * is2 * (ff_const(op3z) * x[i] - ff_const(zp3)) * irad - ff_const(zp3) * x[i] +
+               ff_const(op3z));
+  }
+  return ff_float(e);
 }
 
 // Gaussians of (R2, R3, R4, R5)
@@ -169,6 +214,61 @@ __device__ inline F pot(const F (&R)[6], F (&dv)[6]) {
   return v - F(2) * F(K::de[1]) + F(K::de[2]);
 }
 
+// Mixed form of pot: the R1 Morse and the H2 LEPS term in float pairs (from
+// the FP64 distances), the rest FP32, and dV/dR_k summed as float pairs (the
+// terms of one distance can be large and opposite).
+__device__ inline float pot_mixed(const float (&R)[6], const double (&Rd)[6], ff (&dv)[6]) {
+  ff Rp[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const float h = __double2float_rn(Rd[k]);
+    Rp[k] = ff{h, __double2float_rn(Rd[k] - (double)h)};
+  }
+  float v, m3, m4, d3, d4;
+  constexpr double d1 = K::de[0], b1 = K::beta[0], t1 = K::re[0];
+  morse_ff(d1, b1, t1, Rp[0], v, dv[0]);
+  constexpr float d2 = (float)K::de[1], b2 = (float)K::beta[1], t2 = (float)K::re[1];
+  morse(d2, b2, t2, R[3], m3, d3);
+  morse(d2, b2, t2, R[4], m4, d4);
+  dv[3] = ff_from(d3);
+  dv[4] = ff_from(d4);
+  v = v + m3 + m4;
+  {
+    const ff r3[3] = {Rp[1], Rp[2], Rp[5]};
+    ff d[3];
+    v = v + v3pot_ff(r3, d);
+    dv[1] = d[0];
+    dv[2] = d[1];
+    dv[5] = d[2];
+  }
+  {
+    const float r3[3] = {R[0], R[1], R[3]};
+    float d[3];
+    v = v + vh2o(r3, d);
+    dv[0] += d[0];
+    dv[1] += d[1];
+    dv[3] += d[2];
+  }
+  {
+    const float r3[3] = {R[0], R[2], R[4]};
+    float d[3];
+    v = v + vh2o(r3, d);
+    dv[0] += d[0];
+    dv[2] += d[1];
+    dv[4] += d[2];
+  }
+  {
+    const float r4[4] = {R[1], R[2], R[3], R[4]};
+    float d[4];
+    v = v + v4pot(r4, d);
+    dv[1] += d[0];
+    dv[2] += d[1];
+    dv[3] += d[2];
+    dv[4] += d[3];
+  }
+  return v - 2.0f * (float)K::de[1] + (float)K::de[2];
+}
+
 }  // namespace oh3
 
 struct PesOH3 {
@@ -185,12 +285,22 @@ struct PesOH3 {
       Rd[k] = sqrt(d[k][0] * d[k][0] + d[k][1] * d[k][1] + d[k][2] * d[k][2]);
       R[k] = (F)Rd[k];
     }
-    V = (double)oh3::pot<F>(R, dv);
+    double dvd[6];
+    if constexpr (std::is_same<F, float>::value) {
+      ff dvp[6];
+      V = (double)oh3::pot_mixed(R, Rd, dvp);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) dvd[k] = (double)dvp[k].hi + (double)dvp[k].lo;
+    } else {
+      V = (double)oh3::pot<F>(R, dv);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) dvd[k] = (double)dv[k];
+    }
 #pragma unroll
     for (int x = 0; x < 12; ++x) g[x] = 0.0;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      const double u = (double)dv[k] / Rd[k];
+      const double u = dvd[k] / Rd[k];
 #pragma unroll
       for (int x = 0; x < 3; ++x) {
         g[3 * pa[k] + x] -= u * d[k][x];

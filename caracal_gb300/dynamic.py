@@ -74,13 +74,16 @@ def build_pes(d, nve):
         return K.ANALYTIC[d.pes], []
     from . import qmdff as Q
     from .engine import EVBPair, QMDFFForceField
-    kw = dict(zahn=True, coul_cut=10.0) if nve else dict(coul_cut=50.0)
+    kw = dict(zahn=True, coul_cut=10.0) if nve else dict(zahn=d.zahn, coul_cut=50.0)
     ffs = []
     for i, name in enumerate(d.ffnames):
         ff = Q.read_qmdff(os.path.join(d.directory, name))
         if i < len(d.eshift):
             ff.e_zero = d.eshift[i]
         ffs.append(QMDFFForceField(ff, **kw))
+        if d.box:
+            # set_periodic with the cutoffs of the key file (Angstrom)
+            ffs[-1].set_periodic(d.box, 10.0 if nve else d.coul_cut, 10.0 if nve else d.vdw_cut)
     if d.pes == "QMDFF":
         return ffs[0], ffs
     if len(ffs) != 2:

@@ -9,15 +9,17 @@ closed by `}`.  Read here, with Caracal's defaults and checks:
   NVT { TEMP K, THERMOSTAT ANDERSEN|NOSE-HOOVER, ANDERSEN_STEP n, NOSE_DAMP n }
     (src/dynamic.f90:382-473; defaults TEMP 0, ANDERSEN_STEP 70, NOSE_DAMP 100)
   PES ANA_H3 | ANA_CH4H | ANA_CH4OH | QMDFF | DE_EVB  (src/read_pes.f90:203)
-  QMDFF { FFNAMES file [file2], ESHIFT e1 [e2] }     (src/read_pes.f90:1760-1830)
+  QMDFF { FFNAMES file [file2], ESHIFT e1 [e2], COULOMB ZAHN, COUL_CUTOFF A,
+    VDW_CUTOFF A }  (src/read_pes.f90:1745-1863; defaults 50 and 10)
+  PERIODIC x y z (box edges, Angstrom; src/read_pes.f90:164-170) for QMDFF / DE_EVB
   DE_EVB { COUPLING basis }  with the parameters in evb_pars.dat
     (src/read_pes.f90:1928-1975, 2557-2600)
   E_CON (md_energies.dat), OUTPUT_SPARSE (no all-bead trajectory for P > 1)
   and, for this engine only, GPU_TRAJECTORIES n (independent trajectories
   stepped together; Caracal runs one) and SEED n.
 
-Keywords outside this subset are reported by `unsupported`; NPT, periodic
-boxes and the other surfaces are not on this engine's path.
+Keywords outside this subset are reported by `unsupported`; NPT and the
+other surfaces are not on this engine's path.
 """
 from __future__ import annotations
 
@@ -29,7 +31,7 @@ import numpy as np
 ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh", "ANA_OH3": "oh3"}
 EVB_BASES = ("1g", "2g", "3g", "sp", "sd", "sd2", "sp2d")
 KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE",
-         "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "READ_VEL", "}"}
+         "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "READ_VEL", "PERIODIC", "}"}
 
 
 class KeyError_(ValueError):
@@ -57,6 +59,10 @@ class DynamicInput:
     energycon: bool = False      # E_CON: md_energies.dat (src/dynamic.f90:1130-1140)
     output_sparse: bool = False  # OUTPUT_SPARSE: no all-bead trajectory (src/dynamic.f90:1145-1155)
     read_vel: bool = False       # READ_VEL: start momenta from velocity_start.dat (src/dynamic.f90:1031-1059)
+    box: list = field(default_factory=list)  # PERIODIC x y z (Angstrom); empty: not periodic
+    zahn: bool = False           # QMDFF { COULOMB ZAHN }
+    coul_cut: float = 50.0       # QMDFF { COUL_CUTOFF } (Angstrom where periodic)
+    vdw_cut: float = 10.0        # QMDFF { VDW_CUTOFF } (Angstrom)
     unsupported: list = field(default_factory=list)
     directory: str = "."
 
@@ -124,6 +130,13 @@ def parse(text, directory="."):
             d.output_sparse = True
         elif k == "READ_VEL":
             d.read_vel = True
+        elif k == "PERIODIC":
+            try:
+                d.box = [float(x) for x in w[1:4]]
+            except ValueError:
+                d.box = []
+            if len(d.box) != 3:
+                raise KeyError_("Correct format: PERIODIC [xlen,ylen,zlen (A)]")
         elif k.rstrip("{") not in KNOWN and not k.startswith("#") and not k.startswith("!"):
             d.unsupported.append(k)
     # checks of src/dynamic.f90:290-320
@@ -166,6 +179,18 @@ def parse(text, directory="."):
                 d.ffnames = w[1:3] if d.pes == "DE_EVB" else w[1:2]
             elif k == "ESHIFT":
                 d.eshift = [float(x.replace("d", "e").replace("D", "E")) for x in w[1:3]]
+            elif k == "COULOMB":
+                # only ZAHN changes the Coulomb treatment; PPPME stops the run
+                # (src/read_pes.f90:1832-1849), other names are just recorded
+                if len(w) < 2:
+                    raise KeyError_("Correct format: COULOMB [method]")
+                if w[1].upper() == "PPPME":
+                    raise KeyError_("The Particle Particle Particle Mesh Ewald (PPPME) method is not complete")
+                d.zahn = w[1].upper() == "ZAHN"
+            elif k == "COUL_CUTOFF":
+                d.coul_cut = float(w[1])
+            elif k == "VDW_CUTOFF":
+                d.vdw_cut = float(w[1])
         if not d.ffnames:
             raise KeyError_("Please check the QMDFFNAMES keyword!")
     if d.pes == "DE_EVB":
@@ -175,6 +200,8 @@ def parse(text, directory="."):
                 d.coupling = w[1] if w[1] in EVB_BASES else "1g"
     if d.pes not in ANALYTIC and d.pes not in ("QMDFF", "DE_EVB"):
         raise KeyError_(f"PES {d.pes or '(none)'} is not on this engine's path")
+    if d.box and d.pes in ANALYTIC:
+        raise KeyError_("PERIODIC applies to QMDFF force fields on this engine")
     return d
 
 

@@ -1,7 +1,8 @@
 """GPU: CH4 + OH (egrad_ch4oh) through the C-ABI against the oracle.
 
 Plain FP64 form: forces <= 1e-12, one NVE step <= 1e-12, 100 steps <= 1e-9
-(norm-wise relative); mixed form: force error against FP64 bounded.
+(norm-wise relative); mixed form: force error against FP64 <= 1.5e-7, the
+energy (summed in FP32) <= 1.5e-6.
 """
 import ctypes as C
 
@@ -100,4 +101,6 @@ def test_ch4oh_mixed_force_error(require_gpu):
     _, _, f32, v32, _ = e32.get_state()
     err = rel_err(f32, f64)
     print(f"CH4OH mixed-form force error {err:.3e}, energy error {rel_err(v32, v64):.3e}")
-    assert err < 1.5e-6 and rel_err(v32, v64) < 1.5e-6      # measured 6.8e-7 to 7.5e-7
+    # the O-H Morse, the stretches and the bends in float pairs: 3.6e-8 on
+    # the host restatement of the mixed form
+    assert err < 1.5e-7 and rel_err(v32, v64) < 1.5e-6

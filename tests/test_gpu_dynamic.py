@@ -130,3 +130,36 @@ def test_run_dump_async_frames_match_run_dump(require_gpu, kind):
     for f in ffs:
         if f is not None:
             f.close()
+
+
+def test_dynamic_periodic_qmdff(require_gpu, tmp_path):
+    """PERIODIC with a QMDFF key file: the dumped energies are the periodic
+    force field's at the dumped frames (set_periodic with the key file's
+    cutoffs: a 6 A dispersion cutoff removes pairs of the 11-carbon chain),
+    not the free molecule's."""
+    from caracal_gb300.engine import QMDFFForceField
+    ff = Q.alkane(nc=11)
+    Q.write_qmdff(ff, tmp_path / "a.qmdff")
+    sym = ["C" if z == 6 else "H" for z in ff.at]
+    (tmp_path / "start.xyz").write_text(f"{ff.n}\n\n" + "".join(
+        f"{s} {a} {b} {c}\n" for s, (a, b, c) in zip(sym, ff.xyz * BOHR_ANGSTROM)))
+    key = ("XYZSTART start.xyz\nRPMD_BEADS 1\nENSEMBLE NVT\nSTEPS 2\nDELTAT 0.5\nTDUMP 0.5\nE_CON\n"
+           "NVT {\n TEMP 300\n THERMOSTAT ANDERSEN\n}\nPES QMDFF\nPERIODIC 40.0 40.0 40.0\n"
+           "QMDFF {\n FFNAMES a.qmdff\n VDW_CUTOFF 6.0\n}\n")
+    (tmp_path / "p.key").write_text(key)
+    run(str(tmp_path / "p.key"), out_dir=str(tmp_path), quiet=True)
+    en = [ln.split() for ln in open(tmp_path / "md_energies.dat").read().splitlines()[1:]]
+    tr = frames(tmp_path / "trajectory.xyz")
+    assert len(en) == 2 and len(tr) == 2
+    free = QMDFFForceField(Q.read_qmdff(str(tmp_path / "a.qmdff")))
+    per = QMDFFForceField(Q.read_qmdff(str(tmp_path / "a.qmdff")))
+    per.set_periodic([40.0] * 3, 50.0, 6.0)
+    x = np.stack([angstrom_to_bohr(f) for f in tr])
+    ef, _ = free.egrad(x, "fp64")
+    ep, _ = per.egrad(x, "fp64")
+    free.close()
+    per.close()
+    e_dump = np.array([float(r[1]) for r in en])
+    # the frames are written with 17 digits: the energies agree to ~1e-12
+    assert np.abs(e_dump - ep).max() < 1e-9 * max(1.0, np.abs(ep).max())
+    assert np.abs(ep - ef).min() > 1e-6          # the cutoff acts on this chain

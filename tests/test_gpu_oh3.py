@@ -2,8 +2,9 @@
 C-ABI and in the persistent step kernel against the oracle.  Tolerances
 (norm-wise relative): FP64 energies and gradients <= 1e-12; one step
 <= 1e-12 (forces at the step's own positions), 100 steps <= 1e-9; mixed
-form force error <= 1.5e-6 of the largest force (FP32 surface, FP64
-distances and gradient assembly)."""
+form force error <= 1.5e-7 of the largest force (the R1 Morse and the H2
+LEPS term in float pairs, the rest FP32; FP64 distances and gradient
+assembly)."""
 import numpy as np
 import pytest
 
@@ -64,4 +65,4 @@ def test_mixed_force_error(require_gpu):
         eng.close()
     err = np.max(np.abs(out["mixed"] - out["fp64"])) / np.max(np.abs(out["fp64"]))
     print(f"oh3 mixed force error {err:.3e}")
-    assert err <= 1.5e-6           # measured 5.6e-7 (FP32 surface, FP64 distances)
+    assert err <= 1.5e-7           # 4.3e-8 over the 4096 x 32 bench ensemble

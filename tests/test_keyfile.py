@@ -90,3 +90,23 @@ def test_read_vel_keyword_and_file(tmp_path):
     m = np.array([1.0, 2.0, 3.0])
     p = momenta_from_velocities(v, m, (4, 2, 3, 3))
     assert np.allclose(p[:, 0], -v * m[:, None]) and not p[:, 1].any()
+
+
+def test_periodic_and_coulomb_keywords():
+    """PERIODIC x y z (src/read_pes.f90:164-170) and the QMDFF block's
+    COULOMB / COUL_CUTOFF / VDW_CUTOFF (src/read_pes.f90:1832-1863): only
+    ZAHN switches the Coulomb treatment, PPPME stops the run."""
+    d = K.parse("STEPS 5\nPES qmdff\nPERIODIC 27.0 27.0 30.5\nQMDFF {\n FFNAMES box.qmdff\n COULOMB zahn\n"
+                " COUL_CUTOFF 9.0\n VDW_CUTOFF 8.0\n}\n")
+    assert d.box == [27.0, 27.0, 30.5] and d.zahn and d.coul_cut == 9.0 and d.vdw_cut == 8.0
+    assert not d.unsupported
+    d = K.parse("STEPS 5\nPES qmdff\nQMDFF {\n FFNAMES a.qmdff\n}\n")
+    assert d.box == [] and not d.zahn and d.coul_cut == 50.0 and d.vdw_cut == 10.0
+    with pytest.raises(K.KeyError_, match="PERIODIC"):
+        K.parse("STEPS 5\nPES qmdff\nPERIODIC 27.0\nQMDFF {\n FFNAMES a.qmdff\n}\n")
+    d = K.parse("STEPS 5\nPES qmdff\nQMDFF {\n FFNAMES a.qmdff\n COULOMB ewald\n}\n")
+    assert not d.zahn and not d.unsupported
+    with pytest.raises(K.KeyError_, match="PPPME"):
+        K.parse("STEPS 5\nPES qmdff\nQMDFF {\n FFNAMES a.qmdff\n COULOMB pppme\n}\n")
+    with pytest.raises(K.KeyError_, match="QMDFF force fields"):
+        K.parse("STEPS 5\nPES ana_h3\nPERIODIC 20 20 20\n")
