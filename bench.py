@@ -45,6 +45,10 @@ ALGO_PES_OPS = {
     # geometry + N(0, 0.05 bohr) per coordinate, seed 0); asin counted with acos
     "qmdff": {"add": 92211, "mul": 117770, "div": 20592, "sqrt": 4525, "exp": 1415, "pow": 122,
               "sin": 633, "cos": 753, "acos": 291, "erf": 171},
+    # GeH4 + OH: the CH4 + OH code with its own constants (the same counts at
+    # workloads.geh4oh_geometry)
+    "geh4oh": {"add": 4063, "mul": 7423, "div": 1850, "sqrt": 140, "exp": 72, "pow": 3, "acos": 22,
+               "tanh": 25, "cosh": 25},
     # OH + H2 (Schatz-Elgersma), the reactant approach of workloads.oh3_geometry
     "oh3": {"add": 218, "mul": 199, "div": 43, "sqrt": 7, "exp": 14, "tanh": 6, "cosh": 6},
     # flexible SPC water, 64 molecules, periodic box 23.47 bohr, Coulomb
@@ -230,6 +234,8 @@ def workload(name):
         return W.water_config(nwater=64, ntraj=64, nbeads=32)
     if name == "oh3":
         return W.oh3_config(ntraj=4096, nbeads=32)
+    if name == "geh4oh":
+        return W.geh4oh_md_config(ntraj=2048, nbeads=32)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -919,6 +925,7 @@ def main():
                          "ch4h_small, h3 (H+H2, 64 x 16), h3_large (4096 x 16), "
                          "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (512 x 64), "
                          "water (flexible SPC, 64 molecules, periodic, 64 x 32), oh3 (OH + H2, 4096 x 32), "
+                         "geh4oh (GeH4 + OH, 2048 x 32, Andersen 300 K), "
                          "classes (H3 4096x8, CH4H 2048x32, CH4OH 512x64, QMDFF 128x128 in one batch), "
                          "classes_small (the same with 1/16 of the trajectories), "
                          "adjoint (force matching over 8192 C20H42 geometries and a 200-step trajectory adjoint)")

@@ -34,6 +34,7 @@ CR_PES_QMDFF = 4
 CR_PES_EVB = 5
 CR_PES_WATER = 6
 CR_PES_OH3 = 7
+CR_PES_GEH4OH = 8
 
 CR_THERMO_NONE = 0
 CR_THERMO_ANDERSEN = 1
@@ -120,6 +121,8 @@ def _sig(lib):
         "cr_egrad_ch4oh": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
         "cr_egrad_oh3": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
         "cr_initialize_ch4oh": ([], C.c_int),
+        "cr_egrad_geh4oh": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
+        "cr_initialize_geh4oh": ([], C.c_int),
         "cr_egrad_device": ([C.c_int, v, C.c_int, v, v, C.c_int, v], C.c_int),
         "cr_engine_create": ([C.POINTER(CrConfig), C.POINTER(C.c_void_p)], C.c_int),
         "cr_engine_destroy": ([eng], C.c_int),

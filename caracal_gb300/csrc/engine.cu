@@ -45,7 +45,8 @@ int pes_natoms(int pes) {
   switch (pes) {
     case CR_PES_H3: return 3;
     case CR_PES_CH4H: return 6;
-    case CR_PES_CH4OH: return 7;
+    case CR_PES_CH4OH:
+    case CR_PES_GEH4OH: return 7;
     case CR_PES_OH3: return 4;
     default: return -1;
   }
@@ -812,6 +813,12 @@ int cr_egrad_ch4oh(const double* q, int natoms, int nbeads, double* V, double* d
 
 int cr_initialize_ch4oh(void) { return CR_OK; }
 
+int cr_egrad_geh4oh(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
+  return egrad_host(CR_PES_GEH4OH, 7, q, natoms, nbeads, V, dVdq, info);
+}
+
+int cr_initialize_geh4oh(void) { return CR_OK; }
+
 int cr_egrad_oh3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
   return egrad_host(CR_PES_OH3, 4, q, natoms, nbeads, V, dVdq, info);
 }
@@ -1219,6 +1226,7 @@ int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
       break;
     case CR_PES_CH4OH:
+    case CR_PES_GEH4OH:
       cr::init_positions_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
       break;
@@ -1257,6 +1265,7 @@ static int init_momenta_draw(cr_engine* e, int zero, uint32_t draw) {
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, draw, e->d_p);
       break;
     case CR_PES_CH4OH:
+    case CR_PES_GEH4OH:
       cr::init_momenta_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, draw, e->d_p);
       break;
@@ -1934,6 +1943,7 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
       break;
     case CR_PES_CH4OH:
+    case CR_PES_GEH4OH:
       cr::init_children_kernel<21><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
       break;
@@ -1955,6 +1965,7 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
       cr::child_flux_kernel<6><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
       break;
     case CR_PES_CH4OH:
+    case CR_PES_GEH4OH:
       cr::child_flux_kernel<7><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
       break;
     case CR_PES_OH3:
@@ -2399,6 +2410,7 @@ const PesRuns* pes_runs(int pes) {
     case CR_PES_CH4H: return &kRunsCH4H;
     case CR_PES_CH4OH: return &kRunsCH4OH;
     case CR_PES_OH3: return &kRunsOH3;
+    case CR_PES_GEH4OH: return &kRunsGeH4OH;
     default: return nullptr;
   }
 }

@@ -2,7 +2,10 @@
 // (2000)) as GB300 device code: a drop-in for Caracal's egrad_ch4oh
 // (src/egrad_ch4oh.f:69-124) with its POTLIB wrapper in Caracal's settings
 // (bohr/Hartree user units, no relabelling: the routines of
-// src/util_ch4oh.f are identities).
+// src/util_ch4oh.f are identities).  The same code with the constants of
+// src/egrad_geh4oh.f is the GeH4 + OH surface (egrad_geh4oh :33-67): its
+// routines differ from CH4 + OH's only in the pyramid angle of refangles and
+// the uncut sphi of switchf (ParCH4OH / ParGeH4OH below).
 //
 // One thread evaluates one bead.  Routines restated (src/egrad_ch4oh.f):
 // POT_ch4oh :157, coorden :288, refangles :374, stretch :517, opbend :782,
@@ -36,26 +39,51 @@
 namespace cr {
 namespace ch4oh {
 
-// BLOCK DATA PTPACM_ch4oh (src/egrad_ch4oh.f:2064-2106) after PREPOT_ch4oh
-// (src/egrad_ch4oh.f:1987-2003): d's * 0.041840, force constants * 6.022045,
-// anh2oeq * 2 pi / 360.
-constexpr double r0ch = 1.09397, a1ch = 1.78000, b1ch = 0.15000, c1ch = 15.00000;
-constexpr double r0hh = 0.97060, ahh = 2.15000, r0cb = 1.49092, acb = 2.98688;
-constexpr double d1ch = 112.17000 * 0.041840, d3ch = 32.65328 * 0.041840;
-constexpr double d1hh = 125.44000 * 0.041840, d3hh = 20.41017 * 0.041840;
-constexpr double d1cb = 91.47526 * 0.041840, d3cbi = 112.69509 * 0.041840;
+// The constants of BLOCK DATA PTPACM_ch4oh (src/egrad_ch4oh.f:2064-2106) and
+// PTPACM_geh4oh (src/egrad_geh4oh.f:2001-2045) after PREPOT's / initialize's
+// conversions (src/egrad_ch4oh.f:1987-2003): d's * 0.041840, force constants
+// * 6.022045, anh2oeq * 2 pi / 360.  The two surfaces share these:
+constexpr double r0hh = 0.97060;
 constexpr double a3cb = 0.000000 * 0.041840, b3cb = 0.900000, rcbsp = 2.606485;
-constexpr double a3s = 0.1419100, b3s = -0.3068400, aphi = 0.5287900, bphi = 0.4006600;
-constexpr double cphi = 1.9209900, atheta = 0.9078700, btheta = 0.3548900, ctheta = 1.8915500;
-constexpr double fch3 = 0.0740000 * 6.022045, hch3 = 0.1915000 * 6.022045;
-constexpr double fkinf = 0.4400000 * 6.022045, ak = 0.1260000 * 6.022045;
-constexpr double aa1 = 0.303746, aa2 = 1.599960, aa3 = 3.216595, aa4 = 11.569980;
+constexpr double aphi = 0.5287900, bphi = 0.4006600;
+constexpr double atheta = 0.9078700, btheta = 0.3548900, ctheta = 1.8915500;
+constexpr double hch3 = 0.1915000 * 6.022045, ak = 0.1260000 * 6.022045;
+constexpr double aa2 = 1.599960, aa4 = 11.569980;
 constexpr double fkh2oeq = 0.7300000 * 6.022045, alph2o = 1.1080000;
 constexpr double anh2oeq = 104.7132000 * (2.0 * 3.141592653589793 / 360.0);
 static_assert(a3cb == 0.0, "the d3cb(rav) switch is folded away for a3cb = 0");
-constexpr double d3cb = d3cbi - a3cb;
-// switchf_ch4oh local constants (the original POTLIB values)
+// switchf local constants (the original POTLIB values)
 constexpr double a1s = 1.5313681e-7, b1s = -4.6696246, a2s = 1.0147402e-7, b2s = -12.363798;
+
+// The constants that differ.  tau_py is the pyramid angle of refangles'
+// sphi term (pi/2: planar CH3; 0.678 pi: pyramidal GeH3,
+// src/egrad_geh4oh.f:368-392); sphi_cut keeps switchf's rch < 3.8 condition
+// on sphi (CH4 + OH; GeH4 + OH evaluates sphi at every distance,
+// src/egrad_geh4oh.f:1792-1804).
+struct ParCH4OH {
+  static constexpr double r0ch = 1.09397, a1ch = 1.78000, b1ch = 0.15000, c1ch = 15.00000;
+  static constexpr double ahh = 2.15000, r0cb = 1.49092, acb = 2.98688;
+  static constexpr double d1ch = 112.17000 * 0.041840, d3ch = 32.65328 * 0.041840;
+  static constexpr double d1hh = 125.44000 * 0.041840, d3hh = 20.41017 * 0.041840;
+  static constexpr double d1cb = 91.47526 * 0.041840, d3cbi = 112.69509 * 0.041840;
+  static constexpr double a3s = 0.1419100, b3s = -0.3068400, cphi = 1.9209900;
+  static constexpr double fch3 = 0.0740000 * 6.022045, fkinf = 0.4400000 * 6.022045;
+  static constexpr double aa1 = 0.303746, aa3 = 3.216595;
+  static constexpr double tau_py = 0.5 * 3.141592653589793;
+  static constexpr bool sphi_cut = true;
+};
+struct ParGeH4OH {
+  static constexpr double r0ch = 1.52500, a1ch = 1.43925, b1ch = 0.12330, c1ch = 2.00400;
+  static constexpr double ahh = 2.18200, r0cb = 1.90035, acb = 0.67621;
+  static constexpr double d1ch = 86.50000 * 0.041840, d3ch = 41.50000 * 0.041840;
+  static constexpr double d1hh = 120.94800 * 0.041840, d3hh = 31.86417 * 0.041840;
+  static constexpr double d1cb = 41.50283 * 0.041840, d3cbi = 10.50589 * 0.041840;
+  static constexpr double a3s = 0.2019100, b3s = -0.6068400, cphi = 11.8809900;
+  static constexpr double fch3 = 0.0150000 * 6.022045, fkinf = 0.3060000 * 6.022045;
+  static constexpr double aa1 = 0.173746, aa3 = 2.166595;
+  static constexpr double tau_py = 0.678 * 3.141592653589793;
+  static constexpr bool sphi_cut = false;
+};
 
 template <class F> __device__ inline F t_exp(F x);
 template <> __device__ inline double t_exp<double>(double x) { return exp(x); }
@@ -98,8 +126,14 @@ __device__ inline void switch_fn(F arg, F darg_num, F& s, F& ds) {
   }
 }
 
-template <class F>
+template <class F, class K>
 __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout)[21]) {
+  constexpr double r0ch = K::r0ch, a1ch = K::a1ch, b1ch = K::b1ch, c1ch = K::c1ch;
+  constexpr double ahh = K::ahh, r0cb = K::r0cb, acb = K::acb;
+  constexpr double d1ch = K::d1ch, d3ch = K::d3ch, d1hh = K::d1hh, d3hh = K::d3hh;
+  constexpr double d1cb = K::d1cb, d3cb = K::d3cbi - a3cb;
+  constexpr double a3s = K::a3s, b3s = K::b3s, cphi = K::cphi;
+  constexpr double fch3 = K::fch3, fkinf = K::fkinf, aa1 = K::aa1, aa3 = K::aa3;
   // ---- positions in Angstrom (POT_ch4oh: q = R * 0.52918) and coorden
   double qa[21];
 #pragma unroll
@@ -178,13 +212,21 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
     switch_fn<F>(F(a3s) * x * (y3 * y3),
                  F(a3s) * (F(3) * r * r - F(2) * r * F(r0ch + 2.0 * b3s) + F(b3s * (b3s + 2.0 * r0ch))),
                  s3[i], ds3[i]);
-    if (r < F(3.8)) {
+    sphi[i] = F(0);
+    dsphi[i] = F(0);
+    if (!K::sphi_cut || r < F(3.8)) {
       F xc = r - F(cphi);
       F e = t_exp<F>(F(bphi) * xc * xc * xc);
       F arg = F(aphi) * x * e;
-      F ch = t_cosh<F>(arg);
-      sphi[i] = F(1) - t_tanh<F>(arg);
-      dsphi[i] = -(F(aphi) * (F(1) + F(3) * F(bphi) * x * xc * xc) * e) / (ch * ch);
+      // FP32 only: past arg = 19, 1 - tanh is 0 in float and exp or cosh
+      // overflows first (GeH4 + OH, r > 17.9 A); FP64 follows the reference
+      if (!kPair || arg < F(19.0)) {
+        F ch = t_cosh<F>(arg);
+        sphi[i] = F(1) - t_tanh<F>(arg);
+        dsphi[i] = -(F(aphi) * (F(1) + F(3) * F(bphi) * x * xc * xc) * e) / (ch * ch);
+      }
+    }
+    if (r < F(3.8)) {
       F xt = r - F(ctheta);
       F et = t_exp<F>(F(btheta) * xt * xt * xt);
       F argt = F(atheta) * x * et;
@@ -192,8 +234,6 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
       sth[i] = F(1) - t_tanh<F>(argt);
       dsth[i] = -(F(atheta) * (F(1) + F(3) * F(btheta) * x * xt * xt) * et) / (cht * cht);
     } else {
-      sphi[i] = F(0);
-      dsphi[i] = F(0);
       sth[i] = F(0);
       dsth[i] = F(0);
     }
@@ -202,7 +242,7 @@ __device__ inline void egrad(const double (&qb)[21], double& Vout, double (&gout
   // ---- reference angles (refangles_ch4oh): theta0[i][j], dtheta0[i][j][k]
   const double tau = 1.9106332362490186;  // acos(-1/3)
   const double pi = 3.141592653589793;
-  const F A = F(tau - 0.5 * pi), B = F(tau - 2.0 * pi / 3.0);
+  const F A = F(tau - K::tau_py), B = F(tau - 2.0 * pi / 3.0);
   F th0[4][4], dth0[4][4][4];
   F th0m[4][4];  // th0 - tau, without the rounding of tau (the mixed form's bend differences)
 #pragma unroll
@@ -681,7 +721,18 @@ struct PesCH4OH {
   static constexpr int N = 7;
   template <class F>
   __device__ static inline void egrad(const double (&q)[21], double& V, double (&g)[21]) {
-    ch4oh::egrad<F>(q, V, g);
+    ch4oh::egrad<F, ch4oh::ParCH4OH>(q, V, g);
+  }
+};
+
+// GeH4 + OH (src/egrad_geh4oh.f, Espinosa-Garcia, Rangel, Corchado, Phys.
+// Chem. Chem. Phys. 18, 16941 (2016)): the CH4 + OH functional forms and atom
+// roles (Ge in C's place) with its own constants.
+struct PesGeH4OH {
+  static constexpr int N = 7;
+  template <class F>
+  __device__ static inline void egrad(const double (&q)[21], double& V, double (&g)[21]) {
+    ch4oh::egrad<F, ch4oh::ParGeH4OH>(q, V, g);
   }
 };
 

@@ -8,7 +8,8 @@ closed by `}`.  Read here, with Caracal's defaults and checks:
     STEPS n, DELTAT dt_fs, TDUMP t_fs   (iwrite = nint(TDUMP / DELTAT))
   NVT { TEMP K, THERMOSTAT ANDERSEN|NOSE-HOOVER, ANDERSEN_STEP n, NOSE_DAMP n }
     (src/dynamic.f90:382-473; defaults TEMP 0, ANDERSEN_STEP 70, NOSE_DAMP 100)
-  PES ANA_H3 | ANA_CH4H | ANA_CH4OH | QMDFF | DE_EVB  (src/read_pes.f90:203)
+  PES ANA_H3 | ANA_CH4H | ANA_CH4OH | ANA_OH3 | ANA_GEH4OH | QMDFF | DE_EVB
+    (src/read_pes.f90:203, 413-631)
   QMDFF { FFNAMES file [file2], ESHIFT e1 [e2], COULOMB ZAHN, COUL_CUTOFF A,
     VDW_CUTOFF A }  (src/read_pes.f90:1745-1863; defaults 50 and 10)
   PERIODIC x y z (box edges, Angstrom; src/read_pes.f90:164-170) for QMDFF / DE_EVB
@@ -28,7 +29,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh", "ANA_OH3": "oh3"}
+ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh", "ANA_OH3": "oh3", "ANA_GEH4OH": "geh4oh"}
 EVB_BASES = ("1g", "2g", "3g", "sp", "sd", "sd2", "sp2d")
 KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE",
          "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "READ_VEL", "PERIODIC", "}"}

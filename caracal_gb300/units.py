@@ -17,7 +17,7 @@ EMASS_AMU = 5.485799095e-4
 
 # element masses used on this path (src/atommass.f90:58-129)
 AMU = {"H": 1.00782503207, "D": 2.0141017778, "C": 12.0, "O": 15.99491461956,
-       "N": 14.0030740048, "F": 18.9984, "S": 32.06, "Cl": 34.96885268, "Br": 78.9183371}
+       "N": 14.0030740048, "F": 18.9984, "S": 32.06, "Cl": 34.96885268, "Ge": 72.61, "Br": 78.9183371}
 
 
 def dt_fs_to_au(dt_fs: float) -> float:

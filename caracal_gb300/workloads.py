@@ -188,6 +188,20 @@ def ch4oh_md_config(ntraj=512, nbeads=64, nsteps=1000, kelvin=300.0, dt_fs=0.1):
                     thermostat="andersen", sigma_bohr=float(angstrom_to_bohr(0.01)))
 
 
+def geh4oh_geometry(r_geh_ang=1.525, r_ho_ang=1.5, r_oh_ang=0.97, angle_deg=100.0):
+    """GeH4 + OH in Caracal's atom order for ANA_GEH4OH (H attacked, Ge, H, H,
+    H, O, H(O)): the CH4 + OH arrangement with r(Ge-H) = 1.525 A."""
+    return ch4oh_geometry(r_ch_ang=r_geh_ang, r_ho_ang=r_ho_ang, r_oh_ang=r_oh_ang, angle_deg=angle_deg)
+
+
+def geh4oh_md_config(ntraj=512, nbeads=64, nsteps=1000, kelvin=300.0, dt_fs=0.1):
+    """GeH4 + OH thermal trajectories (Andersen, ANDERSEN_STEP 70), 7 atoms."""
+    return Workload(name=f"geh4oh_md_P{nbeads}_T{ntraj}", pes="geh4oh",
+                    symbols=["H", "Ge", "H", "H", "H", "O", "H"], q0=geh4oh_geometry(),
+                    nbeads=nbeads, ntraj=ntraj, kelvin=kelvin, dt_fs=dt_fs, nsteps=nsteps,
+                    thermostat="andersen", sigma_bohr=float(angstrom_to_bohr(0.01)))
+
+
 def mixed_classes(scale=1, nsteps=1000):
     """Four trajectory classes of uneven atom and bead counts stepped together:
     H3 (N=3) T=4096 P=8 (PILE), CH4H (N=6) T=2048 P=32, CH4OH (N=7) T=512

@@ -43,6 +43,7 @@ extern "C" {
 #define CR_PES_EVB 5     /* dE-EVB of two QMDFFs: src/gradient.f90:361-386, 1228-1304 */
 #define CR_PES_WATER 6   /* flexible SPC water box: src/egrad_water.f90, src/water_init.f90 */
 #define CR_PES_OH3 7     /* ANA_OH3: OH + H2 (Schatz-Elgersma), src/egrad_oh3.f */
+#define CR_PES_GEH4OH 8  /* ANA_GEH4OH: GeH4 + OH, src/egrad_geh4oh.f + src/util_geh4oh.f */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
 #define CR_THERMO_NONE 0      /* NVE */
@@ -56,7 +57,7 @@ extern "C" {
 
 typedef struct cr_config {
   int pes;            /* CR_PES_* */
-  int natoms;         /* must match the PES (H3: 3, CH4H: 6, CH4OH: 7, QMDFF: the force field's n) */
+  int natoms;         /* must match the PES (H3: 3, CH4H: 6, CH4OH and GeH4OH: 7, OH3: 4, QMDFF: the force field's n) */
   int nbeads;         /* 1..128 (RPMD_BEADS) */
   int ntraj;          /* independent trajectories in this engine */
   int thermostat;     /* CR_THERMO_* */
@@ -154,6 +155,15 @@ int cr_egrad_oh3(const double* q, int natoms, int nbeads, double* V, double* dVd
 /* Replaces `subroutine initialize_ch4oh()` (src/egrad_ch4oh.f:33, called from
  * src/read_pes.f90:591); constants are compiled in, always CR_OK. */
 int cr_initialize_ch4oh(void);
+
+/* Replaces `subroutine egrad_geh4oh(q,Natoms,Nbeads,V,dVdq,info)` (src/egrad_geh4oh.f:33-67;
+ * called from src/gradient.f90:192-193 with Nbeads = 1): natoms = 7 in Caracal's order
+ * H, Ge, H, H, H, O, H(O) (the CH4 + OH roles with Ge for C).  The reference routine reads
+ * bead 1 only; this one evaluates every bead. */
+int cr_egrad_geh4oh(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+/* Replaces `subroutine initialize_geh4oh()` (src/egrad_geh4oh.f:1823, called from
+ * src/read_pes.f90:629); constants are compiled in, always CR_OK. */
+int cr_initialize_geh4oh(void);
 
 /* Any built PES (CR_PES_*) on device-resident arrays q(3,natoms,npts). */
 int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,

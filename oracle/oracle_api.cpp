@@ -58,6 +58,7 @@ struct BeadPES {
       case 5: orc::evb::egrad(g_qmdff, g_qmdff2, g_evb, q, V, g); break;
       case 6: *V = orc::water::egrad<double>(g_water, q, g); break;
       case 7: orc::oh3::egrad_bead<double>(q, V, g); break;
+      case 8: orc::ch4oh::egrad_bead<double>(q, V, g, true); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
   }
@@ -385,10 +386,10 @@ void orc_pes_opcount(int pes, const double* q, uint64_t out[14]) {
     orc::OC qq[18], V, g[18];
     for (int x = 0; x < 18; ++x) qq[x] = orc::OC(q[x]);
     orc::ch4h::egrad_bead<orc::OC>(qq, &V, g);
-  } else if (pes == 3) {
+  } else if (pes == 3 || pes == 8) {
     orc::OC qq[21], V, g[21];
     for (int x = 0; x < 21; ++x) qq[x] = orc::OC(q[x]);
-    orc::ch4oh::egrad_bead<orc::OC>(qq, &V, g);
+    orc::ch4oh::egrad_bead<orc::OC>(qq, &V, g, pes == 8);
   } else if (pes == 4) {
     const int n3 = 3 * g_qmdff.n;
     std::vector<orc::OC> qq((size_t)n3), g((size_t)n3);

@@ -19,6 +19,11 @@
 //   PREPOT  :1888 unit conversions (fact1, fact2, fact3 = 2 pi/360 for anh2oeq)
 // Atom roles (BLOCK DATA): nnc = 2 (C), nnb = 6 (O), nnh = (3,4,5,1),
 // nno = 7 (the hydroxyl H).  All constants are REAL(8).
+// GeH4 + OH (src/egrad_geh4oh.f, Espinosa-Garcia, Rangel, Corchado, Phys.
+// Chem. Chem. Phys. 18, 16941 (2016)) is the same code with its own BLOCK
+// DATA (Ge in C's place), refangles' pyramid angle taugeh = 0.678 pi in place
+// of halfpi (:368-392) and switchf's sphi without the rch < 3.8 condition
+// (:1792-1804): params(true).
 // Loop and accumulation orders follow the Fortran.
 #pragma once
 #include <cmath>
@@ -39,11 +44,26 @@ struct Params {
   double r0ch, d1ch, d3ch, a1ch, b1ch, c1ch, r0hh, d1hh, d3hh, ahh, r0cb, d1cb, d3cbi, acb;
   double a3s, b3s, aphi, bphi, cphi, atheta, btheta, ctheta, fch3, hch3, fkinf, ak, bk;
   double aa1, aa2, aa3, aa4, fkh2oeq, alph2o, anh2oeq, a3cb, b3cb, rcbsp;
+  double tau_py;   // refangles' pyramid angle: halfpi (CH4 + OH), taugeh = 0.678 pi (GeH4 + OH)
+  bool sphi_cut;   // switchf's rch < 3.8 condition on sphi (absent in GeH4 + OH)
 };
 
-// BLOCK DATA PTPACM_ch4oh values after PREPOT_ch4oh's conversions.
-inline const Params& params() {
-  static const Params p = [] {
+// PREPOT_ch4oh's unit conversions (src/egrad_ch4oh.f:1987-2003).
+inline Params convert(Params q) {
+  const double pi = 3.141592653589793;
+  const double fact1 = 0.041840, fact2 = 6.022045, fact3 = 2.0 * pi / 360.0;
+  q.d1ch *= fact1; q.d3ch *= fact1; q.d1cb *= fact1; q.d3cbi *= fact1; q.a3cb *= fact1;
+  q.d1hh *= fact1; q.d3hh *= fact1;
+  q.fch3 *= fact2; q.hch3 *= fact2; q.fkinf *= fact2; q.ak *= fact2; q.fkh2oeq *= fact2;
+  q.anh2oeq *= fact3;
+  return q;
+}
+
+// BLOCK DATA PTPACM_ch4oh values after PREPOT_ch4oh's conversions, or with
+// geh4oh those of PTPACM_geh4oh (src/egrad_geh4oh.f:2001-2045) after
+// initialize_geh4oh's (the same conversions).
+inline const Params& params(bool geh4oh = false) {
+  static const Params p_ch4oh = [] {
     Params q;
     q.r0ch = 1.09397;  q.d1ch = 112.17000; q.d3ch = 32.65328;  q.a1ch = 1.78000;
     q.b1ch = 0.15000;  q.c1ch = 15.00000;  q.r0hh = 0.97060;   q.d1hh = 125.44000;
@@ -55,20 +75,33 @@ inline const Params& params() {
     q.aa2 = 1.599960; q.aa3 = 3.216595; q.aa4 = 11.569980; q.fkh2oeq = 0.7300000;
     q.alph2o = 1.1080000; q.anh2oeq = 104.7132000; q.a3cb = 0.000000; q.b3cb = 0.900000;
     q.rcbsp = 2.606485;
-    const double pi = 3.141592653589793;
-    const double fact1 = 0.041840, fact2 = 6.022045, fact3 = 2.0 * pi / 360.0;
-    q.d1ch *= fact1; q.d3ch *= fact1; q.d1cb *= fact1; q.d3cbi *= fact1; q.a3cb *= fact1;
-    q.d1hh *= fact1; q.d3hh *= fact1;
-    q.fch3 *= fact2; q.hch3 *= fact2; q.fkinf *= fact2; q.ak *= fact2; q.fkh2oeq *= fact2;
-    q.anh2oeq *= fact3;
-    return q;
+    q.tau_py = 0.5 * 3.141592653589793;
+    q.sphi_cut = true;
+    return convert(q);
   }();
-  return p;
+  static const Params p_geh4oh = [] {
+    Params q;
+    q.r0ch = 1.52500;  q.d1ch = 86.50000;  q.d3ch = 41.50000;  q.a1ch = 1.43925;
+    q.b1ch = 0.12330;  q.c1ch = 2.00400;   q.r0hh = 0.97060;   q.d1hh = 120.94800;
+    q.d3hh = 31.86417; q.ahh = 2.18200;    q.r0cb = 1.90035;   q.d1cb = 41.50283;
+    q.d3cbi = 10.50589; q.acb = 0.67621;   q.a3s = 0.2019100;  q.b3s = -0.6068400;
+    q.aphi = 0.5287900; q.bphi = 0.4006600; q.cphi = 11.8809900; q.atheta = 0.9078700;
+    q.btheta = 0.3548900; q.ctheta = 1.8915500; q.fch3 = 0.0150000; q.hch3 = 0.1915000;
+    q.fkinf = 0.3060000; q.ak = 0.1260000; q.bk = 50.7132; q.aa1 = 0.173746;
+    q.aa2 = 1.599960; q.aa3 = 2.166595; q.aa4 = 11.569980; q.fkh2oeq = 0.7300000;
+    q.alph2o = 1.1080000; q.anh2oeq = 104.7132000; q.a3cb = 0.000000; q.b3cb = 0.900000;
+    q.rcbsp = 2.606485;
+    q.tau_py = 0.678 * 3.141592653589793;
+    q.sphi_cut = false;
+    return convert(q);
+  }();
+  return geh4oh ? p_geh4oh : p_ch4oh;
 }
 
 // Working state of one evaluation (Caracal keeps it in COMMON blocks).
 template <class T>
 struct State {
+  const Params* P;        // the surface's constants
   T q[22];                // q(1..21), Angstrom (1-based)
   T pdot[22];             // dE/dq(1..21)
   int nc[4], nhb[4], nh[5][4], no[4];  // coordinate indices, 1-based
@@ -103,7 +136,7 @@ inline void coorden(State<T>& s) {
 
 template <class T>
 inline void switchf(State<T>& s) {
-  const Params& P = params();
+  const Params& P = *s.P;
   const double a1s = 1.5313681e-7, b1s = -4.6696246, a2s = 1.0147402e-7, b2s = -12.363798;
   const double argmax = 19.0;
   for (int i = 1; i <= 4; ++i) {
@@ -140,7 +173,7 @@ inline void switchf(State<T>& s) {
       s.s3[i] = 0.0;
       s.ds3[i] = 0.0;
     }
-    if (r < 3.8) {
+    if (!P.sphi_cut || r < 3.8) {
       T xc = r - P.cphi;
       T e = exp(P.bphi * xc * xc * xc);
       T arg = P.aphi * (r - P.r0ch) * e;
@@ -173,8 +206,8 @@ template <class T>
 inline void refangles(State<T>& s) {
   const double pi = 3.141592653589793;
   const double tau = std::acos(-1.0 / 3.0);
-  const double halfpi = 0.5 * pi, twopi = 2.0 * pi;
-  const double A = tau - halfpi, B = tau - twopi / 3.0;
+  const double twopi = 2.0 * pi;
+  const double A = tau - s.P->tau_py, B = tau - twopi / 3.0;
   for (int i = 1; i <= 4; ++i) {
     s.theta0[i][i] = 0.0;
     for (int k = 1; k <= 4; ++k) s.dtheta0[i][i][k] = 0.0;
@@ -226,7 +259,7 @@ inline void refangles(State<T>& s) {
 
 template <class T>
 inline void stretch(State<T>& s, T* vstr_out) {
-  const Params& P = params();
+  const Params& P = *s.P;
   T vqch[5], vjch[5], vqbh[5], vjbh[5], vq[5], vj[5], achdc[4], achdh[5][4];
   T rav = (s.rch[1] + s.rch[2] + s.rch[3] + s.rch[4]) / 4.0;
   T vstr = 0.0;
@@ -331,7 +364,7 @@ inline void stretch(State<T>& s, T* vstr_out) {
 
 template <class T>
 inline void opforce(State<T>& s) {
-  const Params& P = params();
+  const Params& P = *s.P;
   T* s3 = s.s3;
   T* ds3 = s.ds3;
   T sw[5], dsw[5][5];
@@ -505,7 +538,7 @@ inline void opbend(State<T>& s, T* vop_out) {
 
 template <class T>
 inline void ipforce(State<T>& s) {
-  const Params& P = params();
+  const Params& P = *s.P;
   T dfk0[5][5][5], df1dc[5], df1dh[5];
   T* s1 = s.s1;
   T* s2 = s.s2;
@@ -608,7 +641,7 @@ inline void ipbend(State<T>& s, T* vip_out) {
       }
     }
   // H(i)-O-H(O) harmonic bends (src/egrad_ch4oh.f:1061-1172)
-  const Params& P = params();
+  const Params& P = *s.P;
   T angh2o[5], fkh2o[5], dkdr[5], dkdx[5][4];
   for (int i = 1; i <= 4; ++i) {
     T dot = 0.0;
@@ -666,10 +699,12 @@ inline void ipbend(State<T>& s, T* vip_out) {
   *vip_out = vip;
 }
 
-// egrad_ch4oh for one bead: q(3,7) column-major in bohr -> V (Eh), g (Eh/bohr).
+// egrad_ch4oh for one bead: q(3,7) column-major in bohr -> V (Eh), g (Eh/bohr);
+// with geh4oh, egrad_geh4oh (src/egrad_geh4oh.f:33-67 -> pot_geh4oh).
 template <class T>
-inline void egrad_bead(const T* qb, T* V, T* g) {
+inline void egrad_bead(const T* qb, T* V, T* g, bool geh4oh = false) {
   State<T> s;
+  s.P = &params(geh4oh);
   const int nnc = 2, nnb = 6, nnh[5] = {0, 3, 4, 5, 1}, nno = 7;
   for (int ind = 1; ind <= 3; ++ind) {
     int icount = ind - 3;

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from oracle import oracle as orc  # noqa: E402
-from caracal_gb300.workloads import ch4h_dividing_surface, ch4oh_geometry, h3_collinear  # noqa: E402
+from caracal_gb300.workloads import ch4h_dividing_surface, ch4oh_geometry, geh4oh_geometry, h3_collinear  # noqa: E402
 from caracal_gb300.units import angstrom_to_bohr, beta_from_kelvin, dt_fs_to_au, mass_au  # noqa: E402
 
 
@@ -62,6 +62,13 @@ def ch4oh_egrad():
     return {"q": q.tolist(), "V": V.tolist(), "dVdq": g.tolist()}
 
 
+def geh4oh_egrad():
+    rng = np.random.default_rng(20261206)
+    q = np.array([geh4oh_geometry() + rng.normal(0, 0.08, (7, 3)) for _ in range(12)])
+    V, g = orc.egrad("geh4oh", q)
+    return {"q": q.tolist(), "V": V.tolist(), "dVdq": g.tolist()}
+
+
 if __name__ == "__main__":
     with open(os.path.join(HERE, "h3_egrad.json"), "w") as fh:
         json.dump(h3_egrad(), fh)
@@ -73,4 +80,6 @@ if __name__ == "__main__":
         json.dump(ch4h_egrad(), fh)
     with open(os.path.join(HERE, "ch4oh_egrad.json"), "w") as fh:
         json.dump(ch4oh_egrad(), fh)
+    with open(os.path.join(HERE, "geh4oh_egrad.json"), "w") as fh:
+        json.dump(geh4oh_egrad(), fh)
     print("golden fixtures written")

@@ -110,3 +110,14 @@ def test_periodic_and_coulomb_keywords():
         K.parse("STEPS 5\nPES qmdff\nQMDFF {\n FFNAMES a.qmdff\n COULOMB pppme\n}\n")
     with pytest.raises(K.KeyError_, match="QMDFF force fields"):
         K.parse("STEPS 5\nPES ana_h3\nPERIODIC 20 20 20\n")
+
+
+@pytest.mark.parametrize("name,pes", [("ANA_H3", "h3"), ("ANA_CH4H", "ch4h"), ("ANA_CH4OH", "ch4oh"),
+                                      ("ANA_OH3", "oh3"), ("ana_geh4oh", "geh4oh")])
+def test_analytic_surfaces(name, pes):
+    """The analytic PES keywords built on this engine (src/read_pes.f90:413-631);
+    the others stop with an error."""
+    d = K.parse(f"STEPS 5\nPES {name}\n")
+    assert K.ANALYTIC[d.pes] == pes
+    with pytest.raises(K.KeyError_, match="not on this engine's path"):
+        K.parse("STEPS 5\nPES ANA_BRH2\n")

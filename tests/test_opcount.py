@@ -19,9 +19,9 @@ def _bench():
 
 def test_algo_table_matches_oracle_counts():
     table = _bench().ALGO_PES_OPS
-    from caracal_gb300.workloads import oh3_geometry
+    from caracal_gb300.workloads import geh4oh_geometry, oh3_geometry
     for pes, q in (("h3", h3_collinear()), ("ch4h", ch4h_dividing_surface()), ("ch4oh", ch4oh_geometry()),
-                   ("oh3", oh3_geometry())):
+                   ("oh3", oh3_geometry()), ("geh4oh", geh4oh_geometry())):
         counted = {k: v for k, v in orc.pes_opcount(pes, q).items() if v and k != "cmp"}
         assert counted == table[pes], (pes, counted)
 
