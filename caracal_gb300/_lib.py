@@ -152,6 +152,7 @@ def _sig(lib):
         "cr_qmdff_set_periodic": ([v, d, C.c_double, C.c_double, d], C.c_int),
         "cr_qmdff_destroy": ([v], C.c_int),
         "cr_qmdff_egrad": ([v, d, C.c_int, d, d, C.c_int], C.c_int),
+        "cr_qmdff_egrad_virial": ([v, d, C.c_int, d, d, d, d, C.c_int], C.c_int),
         "cr_qmdff_egrad_device": ([v, v, C.c_int, v, v, C.c_int, v], C.c_int),
         "cr_qmdff_schedule_info": ([v, i, i], C.c_int),
         "cr_qmdff_tuning": ([v, C.c_int, i, C.POINTER(C.c_float)], C.c_int),
@@ -184,6 +185,8 @@ def _sig(lib):
         "cr_engine_mdinit": ([eng, C.c_uint], C.c_int),
         "cr_engine_set_andersen_step": ([eng, C.c_int], C.c_int),
         "cr_engine_set_launch": ([eng, C.c_int, C.c_int], C.c_int),
+        "cr_engine_set_npt": ([eng, C.c_double, d], C.c_int),
+        "cr_engine_get_npt": ([eng, d, d], C.c_int),
         "cr_engine_get_launch": ([eng, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
         "cr_engine_autotune": ([eng, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)],
                                C.c_int),

@@ -235,6 +235,12 @@ struct cr_engine {
   char* h_snap[2] = {nullptr, nullptr};
   cudaEvent_t ev_snap[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
   cudaEvent_t hev_in[kHostGroups] = {}, hev_c[kHostGroups] = {}, hev_out = nullptr;
+  // NpT with the Berendsen barostat (periodic QMDFF): per-trajectory box
+  // edges [T][3] (bohr), the last step's pressure [T] (a.u.) and the beads'
+  // virial traces [T][P]
+  bool npt = false;
+  double npt_pressure = 0.0, npt_rate = 0.0;
+  double *d_box = nullptr, *d_press = nullptr, *d_vir = nullptr;
 };
 
 namespace {
@@ -447,6 +453,10 @@ int split_forces_range(cr_engine* e, int t0, int tn, double* V, double* f, cudaS
   if (e->evb)
     return evb_launch(e->evb, e->d_q + off, tn * e->P, V, f, e->d_V2 + (size_t)t0 * e->P, e->d_f2 + off,
                       e->cfg.precision, st);
+  if (e->ff && e->npt) {
+    const QmdffNpt np{e->d_box + 3 * (size_t)t0, e->P, e->d_vir + (size_t)t0 * e->P};
+    return qmdff_launch(e->ff, e->d_q + off, tn * e->P, V, f, e->cfg.precision, st, &np);
+  }
   if (e->ff) return qmdff_launch(e->ff, e->d_q + off, tn * e->P, V, f, e->cfg.precision, st);
   if (e->water) return water_launch(e->water, e->d_q + off, tn * e->P, V, f, e->cfg.precision, st);
   if (t0 != 0 || tn != e->T || st != e->stream) return fail(CR_ERR_UNSUPPORTED, "analytic forces cover every trajectory");
@@ -516,7 +526,9 @@ int split_group_launches(cr_engine* e, const cr::SplitParams& s, int t0, int tn,
     return fail(CR_ERR_UNSUPPORTED, "constrained parents and umbrella windows step every trajectory at once");
   const int cw = cr::split_chunk(e->P);
   const dim3 grid((e->NC + cw - 1) / cw, tn);
-  const bool nhc = e->cfg.thermostat == CR_THERMO_NHC;
+  // under the Berendsen barostat the reference applies no Nose-Hoover chain
+  // (src/verlet.f90:189-208, 1088-1106)
+  const bool nhc = e->cfg.thermostat == CR_THERMO_NHC && !e->npt;
   int n = 0;
   if (nhc) {
     cr::split_nhc_kernel<<<tn, cr::kFinishBlock, 0, st>>>(s);
@@ -570,6 +582,13 @@ int split_group_launches(cr_engine* e, const cr::SplitParams& s, int t0, int tn,
       CR_CUDA(cudaGetLastError());
       ++n;
     }
+  }
+  if (e->npt) {  // pressure and Berendsen scaling (src/verlet.f90:1111-1151)
+    const cr::NptStep np{e->d_box + 3 * (size_t)t0, e->d_press + t0, e->d_vir + (size_t)t0 * e->P, e->npt_pressure,
+                         e->npt_rate};
+    cr::split_berendsen_kernel<<<tn, 128, 0, st>>>(s, np);
+    CR_CUDA(cudaGetLastError());
+    ++n;
   }
   {
     // NaN check, transrot, epot: moments per slice, a solve per trajectory,
@@ -1139,6 +1158,9 @@ int cr_engine_create_water(const cr_config* cfg, cr_water* w, cr_engine** out) {
 int cr_engine_destroy(cr_engine* e) {
   if (!e) return CR_OK;
   if (e->stream) cudaStreamSynchronize(e->stream);
+  cudaFree(e->d_box);
+  cudaFree(e->d_press);
+  cudaFree(e->d_vir);
   cudaFree(e->d_q);
   cudaFree(e->d_p);
   cudaFree(e->d_f);
@@ -1738,6 +1760,48 @@ static void drop_graph(cr_engine* e) {
     cudaGraphDestroy(e->graph);
     e->graph = nullptr;
   }
+}
+
+int cr_engine_set_npt(cr_engine* e, double pressure_atm, const double* box_bohr) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (!e->ff || e->evb || !e->ff->dev.periodic)
+    return fail(CR_ERR_UNSUPPORTED, "NpT is built for one periodic QMDFF force field (cr_qmdff_set_periodic)");
+  if (e->parent || e->sp.umbrella) return fail(CR_ERR_UNSUPPORTED, "NpT with constrained parents or umbrella windows");
+  if (!(pressure_atm >= 0.0)) return fail(CR_ERR_ARG, "Give a positive pressure!");
+  const size_t T = (size_t)e->T;
+  std::vector<double> box(3 * T);
+  for (size_t t = 0; t < T; ++t)
+    for (int k = 0; k < 3; ++k) {
+      const double L = box_bohr ? box_bohr[3 * t + k] : e->ff->dev.box.len[k];
+      if (!(L > 0.0) || !std::isfinite(L)) return fail(CR_ERR_ARG, "box edges must be positive");
+      box[3 * t + k] = L;
+    }
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  if (!e->d_box) {
+    CR_CUDA(cudaMalloc(&e->d_box, 3 * T * sizeof(double)));
+    CR_CUDA(cudaMalloc(&e->d_press, T * sizeof(double)));
+    CR_CUDA(cudaMalloc(&e->d_vir, T * (size_t)e->P * sizeof(double)));
+  }
+  CR_CUDA(cudaMemcpy(e->d_box, box.data(), 3 * T * sizeof(double), cudaMemcpyHostToDevice));
+  CR_CUDA(cudaMemset(e->d_press, 0, T * sizeof(double)));
+  CR_CUDA(cudaMemset(e->d_vir, 0, T * (size_t)e->P * sizeof(double)));
+  // mdinit's Berendsen constants (src/mdinit.f90:155-158) and the pressure
+  // unit (src/general.f90:263, src/dynamic.f90:1331-1335)
+  const double prescon = 290371576.61, taupres = 2.0, compress = 0.000046 * prescon / 1000.0;
+  e->npt = true;
+  e->npt_pressure = pressure_atm / prescon;
+  e->npt_rate = e->cfg.dt * compress / taupres;
+  drop_graph(e);
+  return CR_OK;
+}
+
+int cr_engine_get_npt(cr_engine* e, double* box_bohr, double* pressure_au) {
+  if (!e) return fail(CR_ERR_ARG, "NULL engine");
+  if (!e->npt) return fail(CR_ERR_ARG, "NpT is not set (cr_engine_set_npt)");
+  CR_CUDA(cudaStreamSynchronize(e->stream));
+  if (box_bohr) CR_CUDA(cudaMemcpy(box_bohr, e->d_box, 3 * (size_t)e->T * sizeof(double), cudaMemcpyDeviceToHost));
+  if (pressure_au) CR_CUDA(cudaMemcpy(pressure_au, e->d_press, (size_t)e->T * sizeof(double), cudaMemcpyDeviceToHost));
+  return CR_OK;
 }
 
 int cr_engine_set_launch(cr_engine* e, int threads_per_block, int threads_per_bead) {

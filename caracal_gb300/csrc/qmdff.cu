@@ -121,7 +121,7 @@ namespace cr {
 // MINB: blocks of kQmdffWarps warps kept resident per SM (the register cap
 // follows: 65536 / (MINB * 128) per thread).  The FP64 form trades spills for
 // occupancy differently from the mixed form; the autotuner below picks.
-template <bool MIXED, int MINB>
+template <bool MIXED, int MINB, int MODE = qmdff::kFree>
 __global__ void __launch_bounds__(kQmdffWarps * 32, MINB)
     qmdff_egrad_kernel(qmdff::Dev D, int nbeads, const double* q, double* e, double* g) {
   extern __shared__ double qsm[];
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kQmdffWarps * 32, MINB)
     const double* qb = q + (size_t)b * n3;
     for (int a = lane; a < n3; a += 32) ws[a] = qb[a];
     __syncwarp();
-    const double v = qmdff::warp_egrad<MIXED>(D, ws, g + (size_t)b * n3, 1.0, lane);
+    const double v = qmdff::warp_egrad<MIXED, MODE>(D, ws, g + (size_t)b * n3, 1.0, lane, b);
     if (lane == 0) e[b] = v;
     __syncwarp();
   }
@@ -243,6 +243,12 @@ const QmdffKernel kKernels[2][kVariants] = {
     {cr::qmdff_egrad_kernel<false, 2>, cr::qmdff_egrad_kernel<false, 3>, cr::qmdff_egrad_kernel<false, 4>},
     {cr::qmdff_egrad_kernel<true, 4>, cr::qmdff_egrad_kernel<true, 5>, cr::qmdff_egrad_kernel<true, 6>}};
 constexpr int kDefaultVariant = 1;
+// the force field's periodic box, and NpT (per-trajectory boxes and the
+// virial): one variant per form each
+const QmdffKernel kBoxKernels[2] = {cr::qmdff_egrad_kernel<false, 3, cr::qmdff::kBox>,
+                                    cr::qmdff_egrad_kernel<true, 5, cr::qmdff::kBox>};
+const QmdffKernel kNptKernels[2] = {cr::qmdff_egrad_kernel<false, 3, cr::qmdff::kNpt>,
+                                    cr::qmdff_egrad_kernel<true, 5, cr::qmdff::kNpt>};
 constexpr int kTuneMinBeads = 2048;  // smaller batches keep the default
 
 int launch_dev(const cr::qmdff::Dev& D, int prec, int v, const double* d_q, int nbeads, double* d_e, double* d_g,
@@ -250,7 +256,8 @@ int launch_dev(const cr::qmdff::Dev& D, int prec, int v, const double* d_q, int 
   const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(D.n);
   int grid = (nbeads + kQmdffWarps - 1) / kQmdffWarps;
   if (grid > 1 << 20) grid = 1 << 20;
-  kKernels[prec][v]<<<grid, kQmdffWarps * 32, smem, s>>>(D, nbeads, d_q, d_e, d_g);
+  const QmdffKernel k = D.periodic ? kBoxKernels[prec] : kKernels[prec][v];
+  k<<<grid, kQmdffWarps * 32, smem, s>>>(D, nbeads, d_q, d_e, d_g);
   CR_TRY_CUDA(cudaGetLastError());
   return CR_OK;
 }
@@ -258,6 +265,24 @@ int launch_dev(const cr::qmdff::Dev& D, int prec, int v, const double* d_q, int 
 int launch_variant(const cr_qmdff* ff, int prec, int v, const double* d_q, int nbeads, double* d_e, double* d_g,
                    cudaStream_t s) {
   return launch_dev(ff->dev, prec, v, d_q, nbeads, d_e, d_g, s);
+}
+
+// The NpT instantiation with the launch's boxes and virial array.
+int launch_npt(const cr_qmdff* ff, int prec, const QmdffNpt& npt, const double* d_q, int nbeads, double* d_e,
+               double* d_g, cudaStream_t s) {
+  cr::qmdff::Dev D = ff->dev;
+  D.tbox = npt.tbox;
+  D.tbox_beads = npt.beads_per_box;
+  D.vir = npt.vir;
+  const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(D.n);
+  if (smem > 48 * 1024)
+    CR_TRY_CUDA(cudaFuncSetAttribute(kNptKernels[prec], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nbeads <= 0) return CR_OK;
+  int grid = (nbeads + kQmdffWarps - 1) / kQmdffWarps;
+  if (grid > 1 << 20) grid = 1 << 20;
+  kNptKernels[prec]<<<grid, kQmdffWarps * 32, smem, s>>>(D, nbeads, d_q, d_e, d_g);
+  CR_TRY_CUDA(cudaGetLastError());
+  return CR_OK;
 }
 
 // The force kernel over a subset of the term kinds (bit k of mask: kind k =
@@ -269,9 +294,11 @@ int qmdff_launch_kinds(const cr_qmdff* ff, unsigned mask, bool ezero, const doub
   if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
   const int prec = precision == CR_PREC_MIXED ? 1 : 0;
   const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(ff->n);
-  if (smem > 48 * 1024)
+  if (smem > 48 * 1024) {
     for (int v = 0; v < kVariants; ++v)
       CR_TRY_CUDA(cudaFuncSetAttribute(kKernels[prec][v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CR_TRY_CUDA(cudaFuncSetAttribute(kBoxKernels[prec], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
   if (nbeads <= 0) return CR_OK;
   cr::qmdff::Dev D = ff->dev;
   for (int p = 0; p < 2; ++p)
@@ -329,16 +356,19 @@ int qmdff_host_kinds(cr_qmdff* ff, unsigned mask, bool ezero, bool accumulate, c
 // once on the caller's data (each writes the same outputs) and keeps the
 // fastest for this force field and form.
 int qmdff_launch(const cr_qmdff* ff_c, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
-                 cudaStream_t s) {
+                 cudaStream_t s, const QmdffNpt* npt) {
   cr_qmdff* ff = const_cast<cr_qmdff*>(ff_c);
   if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
   const int prec = precision == CR_PREC_MIXED ? 1 : 0;
+  if (npt) return launch_npt(ff, prec, *npt, d_q, nbeads, d_e, d_g, s);
   const size_t smem = (size_t)kQmdffWarps * cr::qmdff::warp_smem_bytes(ff->n);
   // the attribute is set even for nbeads = 0, so a caller can prepare the
   // kernels before a stream capture
-  if (smem > 48 * 1024)
+  if (smem > 48 * 1024) {
     for (int v = 0; v < kVariants; ++v)
       CR_TRY_CUDA(cudaFuncSetAttribute(kKernels[prec][v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CR_TRY_CUDA(cudaFuncSetAttribute(kBoxKernels[prec], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
   if (nbeads <= 0) return CR_OK;
   int choice = ff->variant[prec];
   if (choice < 0) {
@@ -682,11 +712,10 @@ int cr_qmdff_set_periodic(cr_qmdff* ff, const double* box_ang, double coul_cut_a
   if (!(coul_cut_ang > 0.0) || !(vdw_cut_ang > 0.0)) return cr_set_error(CR_ERR_ARG, "cutoffs must be positive");
   // set_periodic (src/set_periodic.f90:67-113)
   const double bohr = 0.52917721092;
-  for (int k = 0; k < 3; ++k) {
-    D.len[k] = box_ang[k] / bohr;
-    D.half[k] = D.len[k] * 0.5;
-  }
-  const double hmin = std::min(D.half[0], std::min(D.half[1], D.half[2]));
+  double len[3];
+  for (int k = 0; k < 3; ++k) len[k] = box_ang[k] / bohr;
+  D.box = cr::qmdff::make_box(len);
+  const double hmin = std::min(D.box.half[0], std::min(D.box.half[1], D.box.half[2]));
   double coul = coul_cut_ang / bohr;
   if (coul < 5.0) coul = hmin - 0.1;
   if (D.zahn) {
@@ -699,11 +728,6 @@ int cr_qmdff_set_periodic(cr_qmdff* ff, const double* box_ang, double coul_cut_a
   if (coul > hmin) coul = hmin - 0.1;
   D.coul_cut = coul;
   D.vdw_cut = vdw_cut_ang / bohr;
-  for (int k = 0; k < 3; ++k) {
-    D.flen[k] = (float)D.len[k];
-    D.flen_lo[k] = (float)(D.len[k] - (double)D.flen[k]);
-    D.fhalf[k] = (float)D.half[k];
-  }
   D.fcoul_cut = (float)D.coul_cut;
   D.fvdw_cut = (float)D.vdw_cut;
   D.fzahn_a = (float)D.zahn_a;
@@ -765,6 +789,42 @@ int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, doubl
   cudaFree(d_q);
   cudaFree(d_e);
   cudaFree(d_g);
+  return rc;
+}
+
+int cr_qmdff_egrad_virial(cr_qmdff* ff, const double* xyz, int nbeads, const double* box, double* e, double* g,
+                          double* vir, int precision) {
+  if (!ff) return cr_set_error(CR_ERR_ARG, "NULL force field");
+  if (!ff->dev.periodic) return cr_set_error(CR_ERR_ARG, "the virial is formed for periodic force fields (NpT)");
+  if (nbeads < 0 || (nbeads > 0 && (!xyz || !e || !g || !vir))) return cr_set_error(CR_ERR_ARG, "bad egrad arguments");
+  if (precision != CR_PREC_MIXED && precision != CR_PREC_FP64) return cr_set_error(CR_ERR_ARG, "unknown precision");
+  if (nbeads == 0) return CR_OK;
+  const size_t nq = (size_t)3 * ff->n * nbeads, nb = (size_t)nbeads;
+  std::vector<double> hb(3 * nb);
+  for (size_t b = 0; b < nb; ++b)
+    for (int k = 0; k < 3; ++k) hb[3 * b + k] = box ? box[3 * b + k] : ff->dev.box.len[k];
+  double *d_q = nullptr, *d_e = nullptr, *d_g = nullptr, *d_b = nullptr, *d_w = nullptr;
+  int rc = CR_OK;
+  if (cudaMalloc(&d_q, nq * sizeof(double)) != cudaSuccess || cudaMalloc(&d_e, nb * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_g, nq * sizeof(double)) != cudaSuccess || cudaMalloc(&d_b, 3 * nb * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_w, nb * sizeof(double)) != cudaSuccess) {
+    rc = cr_set_error(CR_ERR_CUDA, "cudaMalloc failed in cr_qmdff_egrad_virial");
+  } else if (cudaMemcpy(d_q, xyz, nq * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(d_b, hb.data(), 3 * nb * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = cr_set_error(CR_ERR_CUDA, "copy of xyz failed");
+  } else {
+    const QmdffNpt np{d_b, 1, d_w};
+    if ((rc = qmdff_launch(ff, d_q, nbeads, d_e, d_g, precision, nullptr, &np)) == CR_OK &&
+        (cudaMemcpy(e, d_e, nb * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+         cudaMemcpy(g, d_g, nq * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+         cudaMemcpy(vir, d_w, nb * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess))
+      rc = cr_set_error(CR_ERR_CUDA, "copy of results failed");
+  }
+  cudaFree(d_q);
+  cudaFree(d_e);
+  cudaFree(d_g);
+  cudaFree(d_b);
+  cudaFree(d_w);
   return rc;
 }
 

@@ -55,6 +55,24 @@ struct Schedule {
   const unsigned char* ncol;   // [batches]
 };
 
+// A periodic box (src/box_image.f90): edges and halves in bohr, and for the
+// mixed form the edges as (hi, lo) float pairs and the halves in FP32.
+struct PBox {
+  double len[3], half[3];
+  float flen[3], flen_lo[3], fhalf[3];
+};
+__host__ __device__ inline PBox make_box(const double* len) {
+  PBox b;
+  for (int k = 0; k < 3; ++k) {
+    b.len[k] = len[k];
+    b.half[k] = len[k] * 0.5;
+    b.flen[k] = (float)len[k];
+    b.flen_lo[k] = (float)(len[k] - (double)b.flen[k]);
+    b.fhalf[k] = (float)b.half[k];
+  }
+  return b;
+}
+
 struct Dev {
   int n;
   // [0] plain form: full 32-term batches, as many colours as needed (an FP64
@@ -73,11 +91,19 @@ struct Dev {
   double coul_cut, zahn_a, zahn_par, e_zero;
   float fcoul_cut, fzahn_a, fzahn_par;  // the same in FP32 (mixed form)
   int zahn;
-  // periodic box (src/set_periodic.f90, src/box_image.f90): edge lengths,
-  // halves and the dispersion/repulsion cutoff, bohr
+  // periodic box (src/set_periodic.f90, src/box_image.f90) and the
+  // dispersion/repulsion cutoff, bohr
   int periodic;
-  double len[3], half[3], vdw_cut;
-  float flen[3], flen_lo[3], fhalf[3], fvdw_cut;  // edges as (hi, lo) float pairs
+  PBox box;
+  double vdw_cut;
+  float fvdw_cut;
+  // NpT, set per launch: the box of each trajectory (3 edges, bohr) for
+  // beads [t tbox_beads, (t + 1) tbox_beads) in place of `box`, and the
+  // virial trace of each bead out (src/ff_eg.f90, ff_nonb.f90, eabhag.f90,
+  // eabxag.f90 `vir_ten`); NULL otherwise
+  const double* tbox;
+  int tbox_beads;
+  double* vir;
   int distinct;  // 1: every term's atoms are pairwise distinct
   int nterm[kKinds];  // terms per kind
   // mixed form, bond stretch gradient as a double-FP32 polynomial (see
@@ -287,7 +313,7 @@ struct BeadPos {
   const double* x;
   const float2* hl;  // (hi, lo) per coordinate (mixed form only)
   const double* w;   // tangent direction (dual coordinates only)
-  const Dev* pbc;    // the force field where the box is periodic, else NULL
+  const PBox* pbc;   // the bead's box where periodic, else NULL
 };
 
 // box_image (src/box_image.f90:36-63): subtract the edge while a component
@@ -832,7 +858,7 @@ __device__ inline F pair_term(const Dev& D, const Tables<typename ParamOf<F>::ty
   const F c6t6 = c6 * it6, c6t8 = c6 * it8;
   const F t27 = v[2] * c6t8;
   // periodic: dispersion and repulsion only within vdw_cut (src/ff_nonb.f90:107)
-  const bool vdw = !D.periodic || !(r > (std::is_same<F, float>::value ? F(D.fvdw_cut) : F(D.vdw_cut)));
+  const bool vdw = !x.pbc || !(r > (std::is_same<F, float>::value ? F(D.fvdw_cut) : F(D.vdw_cut)));
   F e = vdw ? -(c6t6 + t27) * eps2 : F(0);
   F drij = vdw ? eps2 * (c6t6 * F(6) * r4 * it6 + F(8) * t27 * r6 * it8) : F(0);
   if (vdw && r < F(25)) {
@@ -899,7 +925,7 @@ __device__ inline float pair_mixed_v(const Dev& D, const BeadPos& x, int i1, int
   const float r4 = r2 * r2, r6 = r4 * r2;
   const float it6 = rcp_approx(r6 + v[0]), it8 = rcp_approx(r6 * r2 + v[1]);
   const float d6 = v[2] * it6, d8 = v[3] * it8;
-  const bool vdw = !D.periodic || !(r > D.fvdw_cut);
+  const bool vdw = !x.pbc || !(r > D.fvdw_cut);
   float e = vdw ? -(d6 + d8) : 0.0f;
   float drij = vdw ? 6.0f * d6 * (r4 * it6) + 8.0f * d8 * (r6 * it8) : 0.0f;
   if (vdw && r < 25.0f) {
@@ -1121,11 +1147,68 @@ __device__ inline typename std::conditional<MIXED, float, double>::type term(
 
 // All batches of one term kind (NA atoms per term): each lane evaluates its
 // slot's term, then the warp scatters colour by colour.
-template <bool MIXED, int KIND, int NA>
+// The virial trace of one term as the reference accumulates `vir_ten` for
+// NpT: bonds (src/ff_eg.f90:133-150) rbond.g_i, rbond = r_i - r_j; angles
+// (:270-281) vab.g_i + vcb.g_k about the centre j; torsions (:317-320,
+// 420-440) vab.g_i + vcb.(g_k + g_l) + vdc.g_l with vab = r_i - r_j,
+// vcb = r_j - r_k, vdc = r_k - r_l, and inversions (:503-505, 583-603) the
+// same formula with vab = r_j - r_i, vcb = r_j - r_k, vdc = r_j - r_l (for
+// neither is it the sum of (r - r_j).g over the term's atoms); NCI pairs
+// (src/ff_nonb.f90:180-190, 318-328, 405-415, 495-505) vab.g_i1, vab = r_i1 - r_i2; hydrogen bonds
+// (src/eabhag.f90:54, 203-216) drah.g_A + drbh.g_B about H; halogen bonds
+// (src/eabxag.f90:86-87, 140-153) (r_A - r_X).g_A + (r_B - r_X).g_X, the
+// X atom's gradient with the B vector.  Vectors minimum-imaged as the
+// terms' own.  Mixed-form bonds carry g_i as (hi, lo) in g[0] and g[2].
+template <class F, int KIND>
+__device__ inline F term_virial(const Dev& D, const BeadPos& X, int m, const Contrib<F>& c) {
+  F u[3], v[3], w[3];
+  if constexpr (KIND == 0) {
+    disp<F>(X, c.a[0], c.a[1], u);
+    F g[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[d] = std::is_same<F, float>::value ? c.g[0][d] + c.g[2][d] : c.g[0][d];
+    return dot3(u, g);
+  } else if constexpr (KIND == 1) {
+    disp<F>(X, c.a[0], c.a[1], u);
+    disp<F>(X, c.a[2], c.a[1], v);
+    return dot3(u, c.g[0]) + dot3(v, c.g[2]);
+  } else if constexpr (KIND == 2) {
+    const int i = c.a[0], j = c.a[1], k = c.a[2], l = c.a[3];
+    if (D.tors[6 * m + 5] != 2) {
+      disp<F>(X, i, j, u);
+      disp<F>(X, j, k, v);
+      disp<F>(X, k, l, w);
+    } else {
+      disp<F>(X, j, i, u);
+      disp<F>(X, j, k, v);
+      disp<F>(X, j, l, w);
+    }
+    F gkl[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) gkl[d] = c.g[2][d] + c.g[3][d];
+    return dot3(u, c.g[0]) + dot3(v, gkl) + dot3(w, c.g[3]);
+  } else if constexpr (KIND == 3) {
+    disp<F>(X, c.a[0], c.a[1], u);
+    return dot3(u, c.g[0]);
+  } else {
+    disp<F>(X, c.a[0], c.a[2], u);
+    disp<F>(X, c.a[1], c.a[2], v);
+    const bool halogen = D.hb[4 * m + 3] != 1;
+    return dot3(u, c.g[0]) + dot3(v, halogen ? c.g[2] : c.g[1]);
+  }
+}
+
+// Box modes of the force kernel, compile-time so the free molecule's kernel
+// carries no imaging code: kFree (no box), kBox (the force field's periodic
+// box), kNpt (each trajectory's box from Dev::tbox, and the virial).
+constexpr int kFree = 0, kBox = 1, kNpt = 2;
+
+template <bool MIXED, int KIND, int NA, int MODE>
 __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
                                     Grad<typename std::conditional<MIXED, float, double>::type>& G,
                                     typename std::conditional<MIXED, float, double>::type& es,
-                                    typename std::conditional<MIXED, float, double>::type& ec, int lane) {
+                                    typename std::conditional<MIXED, float, double>::type& ec,
+                                    typename std::conditional<MIXED, float, double>::type& wv, int lane) {
   using F = typename std::conditional<MIXED, float, double>::type;
   const Schedule& S = D.sched[MIXED ? 1 : 0];
   const int b0 = S.boff[KIND], nb = S.nb[KIND];
@@ -1144,6 +1227,7 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
       } else {
         es += v;
       }
+      if constexpr (MODE == kNpt) wv += term_virial<F, KIND>(D, X, m, c);
     }
     for (int k = 0; k < ncol; ++k) {
       if (m >= 0 && col == k) {
@@ -1160,8 +1244,9 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
 // lane scatters right after its term; the next batch's slot, atom pair and
 // parameters are loaded before the current batch's arithmetic, so the L1
 // latency of the term tables overlaps the work.
+template <int MODE>
 __device__ inline void pair_batches_mixed(const Dev& D, const BeadPos& X, Grad<float>& G, float& es, float& ec,
-                                          int lane) {
+                                          float& wv, int lane) {
   const Schedule& S = D.sched[1];
   const int b0 = S.boff[3], nb = S.nb[3];
   if (nb <= 0) return;
@@ -1187,6 +1272,7 @@ __device__ inline void pair_batches_mixed(const Dev& D, const BeadPos& X, Grad<f
       const float t = es + e;
       ec += (fabsf(es) >= fabsf(e)) ? ((es - t) + e) : ((e - t) + es);
       es = t;
+      if constexpr (MODE == kNpt) wv += term_virial<float, 3>(D, X, mc, c);
       scatter_pair<2>(c, G);
     }
     __syncwarp();
@@ -1201,14 +1287,27 @@ __host__ __device__ inline size_t warp_smem_bytes(int n) { return (size_t)3 * n 
 // Energy (with E_zero) and gradient (times gscale) of one bead by one warp.
 // ws: the warp's shared memory with the bead's FP64 coordinates in its first
 // 3n doubles; gout: the gradient destination.  Returns the energy on every lane.
-template <bool MIXED>
-__device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, double gscale, int lane) {
+template <bool MIXED, int MODE = kFree>
+__device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, double gscale, int lane, int bead = 0) {
+  // MODE (kFree, kBox, kNpt): with kNpt the bead's trajectory box from D.tbox
+  // and the virial trace into D.vir
   using F = typename std::conditional<MIXED, float, double>::type;
   const int n3 = 3 * D.n;
   double* xs = ws;
   float2* hl = (float2*)(ws + n3);
   void* gs = hl + n3;
-  BeadPos X{xs, hl, nullptr, D.periodic ? &D : nullptr};
+  // the box as a local copy: taking the address of the kernel parameter D
+  // would move all of it from the constant bank to local memory
+  PBox tb;
+  const PBox* pb = nullptr;
+  if constexpr (MODE == kNpt) {  // this trajectory's box
+    tb = make_box(D.tbox + 3 * (size_t)(bead / D.tbox_beads));
+    pb = &tb;
+  } else if constexpr (MODE == kBox) {
+    tb = D.box;
+    pb = &tb;
+  }
+  BeadPos X{xs, hl, nullptr, pb};
   Grad<F> G;
   if constexpr (MIXED) {
     for (int a = lane; a < n3; a += 32) {
@@ -1228,16 +1327,23 @@ __device__ inline double warp_egrad(const Dev& D, double* ws, double* gout, doub
   }
   __syncwarp();
   F es = F(0), ec = F(0);  // compensated lane sum of term energies
-  kind_batches<MIXED, 0, 2>(D, X, G, es, ec, lane);
-  kind_batches<MIXED, 1, 3>(D, X, G, es, ec, lane);
-  kind_batches<MIXED, 2, 4>(D, X, G, es, ec, lane);
-  if constexpr (MIXED) pair_batches_mixed(D, X, G, es, ec, lane);
-  else kind_batches<MIXED, 3, 2>(D, X, G, es, ec, lane);
-  kind_batches<MIXED, 4, 3>(D, X, G, es, ec, lane);
+  F wv = F(0);             // lane sum of the terms' virial traces (NpT)
+  kind_batches<MIXED, 0, 2, MODE>(D, X, G, es, ec, wv, lane);
+  kind_batches<MIXED, 1, 3, MODE>(D, X, G, es, ec, wv, lane);
+  kind_batches<MIXED, 2, 4, MODE>(D, X, G, es, ec, wv, lane);
+  if constexpr (MIXED) pair_batches_mixed<MODE>(D, X, G, es, ec, wv, lane);
+  else kind_batches<MIXED, 3, 2, MODE>(D, X, G, es, ec, wv, lane);
+  kind_batches<MIXED, 4, 3, MODE>(D, X, G, es, ec, wv, lane);
   for (int a = lane; a < n3; a += 32) gout[a] = gscale * G.get(a);
   double e = (double)es + (double)ec;
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  if constexpr (MODE == kNpt) {
+    double w = (double)wv;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (lane == 0) D.vir[bead] = w;
+  }
   return e + D.e_zero;
 }
 
@@ -1304,7 +1410,9 @@ __device__ inline double warp_hvp(const Dev& D, double* ws, double* gout, double
     G.h[a] = 0.0;
   }
   __syncwarp();
-  BeadPos X{xs, nullptr, w, D.periodic ? &D : nullptr};
+  PBox tb;
+  if (D.periodic) tb = D.box;
+  BeadPos X{xs, nullptr, w, D.periodic ? &tb : nullptr};
   Dual es(0.0);
   kind_batches_dual<0, 2>(D, X, G, es, lane);
   kind_batches_dual<1, 3>(D, X, G, es, lane);
@@ -1334,7 +1442,9 @@ __device__ inline double warp_hvp(const Dev& D, double* ws, double* gout, double
 // Per term, out receives alpha * (v . grad E_t|unit) + beta * E_t|unit.
 __device__ inline void warp_param_vjp(const Dev& D, const Tables<double>& U, const double* xs, const double* vs,
                                       double alpha, double beta, double* out, int lane) {
-  const BeadPos X{xs, nullptr, nullptr, D.periodic ? &D : nullptr};
+  PBox tb;
+  if (D.periodic) tb = D.box;
+  const BeadPos X{xs, nullptr, nullptr, D.periodic ? &tb : nullptr};
   int off = 0;
 #pragma unroll 1
   for (int kind = 0; kind < 4; ++kind) {

@@ -22,9 +22,19 @@ struct cr_qmdff {
 // Warps per block of the QMDFF force kernel and its dynamic shared memory.
 constexpr int kQmdffWarps = 4;
 
-// e[b] (with E_zero) and g = dV/dq for nbeads beads of d_q(3, n, nbeads).
+// NpT arguments of one launch: each trajectory's box edges (tbox[3 t + k],
+// bohr) for beads [t beads_per_box, (t + 1) beads_per_box), and the virial
+// trace of each bead out (vir[b]).
+struct QmdffNpt {
+  const double* tbox;
+  int beads_per_box;
+  double* vir;
+};
+
+// e[b] (with E_zero) and g = dV/dq for nbeads beads of d_q(3, n, nbeads);
+// npt: per-trajectory boxes and the virial (NULL: the force field's box).
 int qmdff_launch(const cr_qmdff* ff, const double* d_q, int nbeads, double* d_e, double* d_g, int precision,
-                 cudaStream_t s);
+                 cudaStream_t s, const QmdffNpt* npt = nullptr);
 
 // Plain-form derivatives for the adjoint (bonds, angles, torsions, NCI pairs):
 // energy, gradient and H w per bead (d_e, d_g, d_dew may be NULL) ...

@@ -832,6 +832,40 @@ __global__ void __launch_bounds__(kFinishBlock) split_nhc_kernel(SplitParams s) 
   for (int x = threadIdx.x; x < P * NC; x += blockDim.x) s.p[tb + x] = sc * s.p[tb + x];
 }
 
+// NpT with the Berendsen barostat (src/verlet.f90:1111-1151), one block per
+// trajectory, after the second half kick: the pressure from the beads' virial
+// traces (the reference's kinetic stress tensor stays zero, so
+// p = (1/V)(0 - tr W)/3 with V the box at the start of the step), the scale
+// (1 + rate (p - p0))^(1/3) with rate = dt compress / taupres, then the box
+// and every bead's coordinates scaled.  A non-finite scale reaches the
+// coordinates and the step's NaN check.
+struct NptStep {
+  double* box;        // [T][3] edges, bohr
+  double* press;      // [T] the step's pressure, a.u.
+  const double* vir;  // [T][P] virial trace per bead
+  double pressure;    // target, a.u.
+  double rate;        // dt compress / taupres
+};
+__global__ void split_berendsen_kernel(SplitParams s, NptStep n) {
+  const int t = blockIdx.x;
+  const int P = s.P, nq = P * s.NC;
+  __shared__ double scale;
+  if (threadIdx.x == 0) {
+    double w = 0.0;
+    for (int b = 0; b < P; ++b) w += n.vir[(size_t)t * P + b];
+    double* L = n.box + 3 * (size_t)t;
+    const double factor = 1.0 / (L[0] * L[1] * L[2]);
+    const double pr = (factor * (0.0 - w)) / 3.0;
+    const double sc = pow(1.0 + n.rate * (pr - n.pressure), 1.0 / 3.0);
+    for (int k = 0; k < 3; ++k) L[k] = L[k] * sc;
+    n.press[t] = pr;
+    scale = sc;
+  }
+  __syncthreads();
+  double* q = s.q + (size_t)t * nq;
+  for (int i = threadIdx.x; i < nq; i += blockDim.x) q[i] = q[i] * scale;
+}
+
 __global__ void split_advance_kernel(int* istep) { *istep += 1; }
 __global__ void advance_by_kernel(int* istep, int n) { *istep += n; }
 

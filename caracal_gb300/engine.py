@@ -218,6 +218,24 @@ class QMDFFForceField:
                 "cr_qmdff_egrad")
         return e, g
 
+    def egrad_virial(self, xyz, box_bohr=None, precision="fp64"):
+        """Energies, gradients and each bead's virial trace (the reference's
+        vir_ten terms, NpT) of xyz (nbeads, n, 3) bohr; box_bohr (nbeads, 3)
+        or None for the force field's box (set_periodic first)."""
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        if x.ndim == 2:
+            x = x[None]
+        if x.shape[1:] != (self.n, 3):
+            raise ValueError(f"expected xyz of shape (nbeads, {self.n}, 3)")
+        nb = x.shape[0]
+        e, w = np.zeros(nb), np.zeros(nb)
+        g = np.zeros_like(x)
+        bx = None if box_bohr is None else np.ascontiguousarray(np.broadcast_to(box_bohr, (nb, 3)), dtype=np.float64)
+        prec = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        L.check(L.lib().cr_qmdff_egrad_virial(self._h, L.dptr(x), nb, None if bx is None else L.dptr(bx), L.dptr(e),
+                                              L.dptr(g), L.dptr(w), prec), "cr_qmdff_egrad_virial")
+        return e, g, w
+
     def _piece(self, fn, xyz, e, g, precision):
         x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, self.n, 3)
         prec = PRECISION[precision] if isinstance(precision, str) else int(precision)
@@ -526,6 +544,23 @@ class RPMDEngine:
 
     def set_andersen_step(self, n):
         L.check(L.lib().cr_engine_set_andersen_step(self._h, int(n)), "set_andersen_step")
+
+    def set_npt(self, pressure_atm, box_bohr=None):
+        """NpT with the Berendsen barostat (periodic QMDFF): target pressure
+        in atm, each trajectory's starting box (ntraj, 3) bohr or None for
+        the force field's."""
+        bx = None
+        if box_bohr is not None:
+            bx = np.ascontiguousarray(np.broadcast_to(box_bohr, (self.ntraj, 3)), dtype=np.float64)
+        L.check(L.lib().cr_engine_set_npt(self._h, float(pressure_atm), None if bx is None else L.dptr(bx)),
+                "set_npt")
+
+    def npt_state(self):
+        """(box (ntraj, 3) bohr, the last step's pressure (ntraj,) a.u.)."""
+        box = np.zeros((self.ntraj, 3))
+        pr = np.zeros(self.ntraj)
+        L.check(L.lib().cr_engine_get_npt(self._h, L.dptr(box), L.dptr(pr)), "get_npt")
+        return box, pr
 
     def set_launch(self, threads_per_block=0, threads_per_bead=1):
         """Threads per block and per bead of the persistent step kernel

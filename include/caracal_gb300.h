@@ -259,6 +259,17 @@ int cr_qmdff_file_counts(const char* path, int* natoms, int* counts);
 int cr_qmdff_destroy(cr_qmdff* ff);
 /* Host arrays xyz(3,natoms,nbeads) -> e(nbeads) (with E_zero), g(3,natoms,nbeads). */
 int cr_qmdff_egrad(cr_qmdff* ff, const double* xyz, int nbeads, double* e, double* g, int precision);
+/* cr_qmdff_egrad with each bead's virial trace vir[b] as the reference's
+ * ff_eg / ff_nonb / ff_hb accumulate vir_ten with calc_vir (NpT; the
+ * pressure takes its diagonal, src/verlet.f90:1123-1131): the terms'
+ * formulas of src/ff_eg.f90:138-150, 270-281, 420-440, 583-603,
+ * src/ff_nonb.f90:180-190, 318-328, 405-415, 495-505, src/eabhag.f90:203-216,
+ * src/eabxag.f90:140-153 (the torsion, inversion and halogen-bond forms are
+ * not the sum of (r - r_ref).g over the term's atoms; reproduced).  box: the
+ * edges of bead b at box[3 b .. 3 b + 2] (bohr), NULL for the force field's;
+ * the force field must be periodic (cr_qmdff_set_periodic). */
+int cr_qmdff_egrad_virial(cr_qmdff* ff, const double* xyz, int nbeads, const double* box, double* e, double* g,
+                          double* vir, int precision);
 /* The three pieces of Caracal's QMDFF call site (src/gradient.f90:341-358),
  * for a caller that redirects them one by one; same arrays as
  * cr_qmdff_egrad, E_zero in none of them.
@@ -525,6 +536,23 @@ int cr_engine_mdinit(cr_engine* e, unsigned draw);
  * equilibration, int(sqrt(child_interval)) between child batches
  * (src/recross.f90:239-242, 456-458). */
 int cr_engine_set_andersen_step(cr_engine* e, int andersen_step);
+
+/* NpT with the Berendsen barostat (ENSEMBLE NPT, BAROSTAT BERENDSEN,
+ * src/verlet.f90:1111-1151; constants of src/mdinit.f90:155-158) for an
+ * engine on one periodic QMDFF: every trajectory keeps its own box, starting
+ * from box_bohr[3 t .. 3 t + 2] (NULL: the force field's box).  Each step
+ * sums the beads' virial traces (the terms' vir_ten as the reference forms
+ * them), takes the pressure as -tr W / (3 V) (the reference's kinetic
+ * stress tensor stays zero) and after the second half kick scales the box
+ * and the coordinates by (1 + dt compress / taupres (p - p0))^(1/3),
+ * p0 = pressure_atm / prescon.  A Nose-Hoover chain thermostat is not
+ * applied under it (the reference calls neither nhc nor nhc_npt there).
+ * CR_ERR_UNSUPPORTED for other force fields, dE-EVB, constrained parents and
+ * umbrella windows. */
+int cr_engine_set_npt(cr_engine* e, double pressure_atm, const double* box_bohr);
+/* Each trajectory's box edges (bohr, T x 3) and its last step's pressure
+ * (a.u.; x prescon = 290371576.61 for atm); either pointer may be NULL. */
+int cr_engine_get_npt(cr_engine* e, double* box_bohr, double* pressure_au);
 
 /* Launch shape of the persistent step kernel (analytic surfaces; the graph
  * path of force fields has none and returns CR_ERR_UNSUPPORTED).  A

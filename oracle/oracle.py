@@ -127,6 +127,45 @@ def set_qmdff_periodic(box_ang, coul_cut_ang=50.0, vdw_cut_ang=10.0):
     return tuple(out)
 
 
+def qmdff_egrad_virial(q, box=None):
+    """The current QMDFF on q (nbeads, n, 3) bohr: V, dV/dq and each bead's
+    virial trace (the reference's vir_ten terms); box (nbeads, 3) bohr per
+    bead, or None for the force field's own."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    nb = q.shape[0]
+    V, g, w = np.zeros(nb), np.zeros_like(q), np.zeros(nb)
+    bx = None if box is None else np.ascontiguousarray(np.broadcast_to(box, (nb, 3)), dtype=np.float64)
+    rc = lib().orc_qmdff_egrad_virial(_dp(q), nb, None if bx is None else _dp(bx), _dp(V), _dp(g), _dp(w))
+    if rc:
+        raise ValueError("a box needs set_qmdff_periodic first")
+    return V, g, w
+
+
+# Berendsen barostat constants of mdinit (src/mdinit.f90:155-158) and the
+# pressure unit (src/general.f90:263: Hartree/bohr^3 -> atm)
+PRESCON = 290371576.61
+BERENDSEN_TAUPRES = 2.0
+BERENDSEN_COMPRESS = 0.000046 * PRESCON / 1000.0
+
+
+def run_npt(cfg, q, p, f, nsteps, box, pressure_atm, istep0=0, traj0=0, nthreads=0):
+    """run() under the Berendsen barostat (periodic QMDFF): box (ntraj, 3)
+    bohr; returns (q, p, f, epot, status, box, press) with press in a.u."""
+    q = np.array(q, dtype=np.float64)
+    p = np.array(p, dtype=np.float64)
+    f = np.array(f, dtype=np.float64)
+    T = q.shape[0]
+    bx = np.array(np.broadcast_to(box, (T, 3)), dtype=np.float64)
+    e, pr = np.zeros(T), np.zeros(T)
+    st = np.zeros(T, dtype=np.int32)
+    rc = lib().orc_run_npt(C.byref(cfg.c), T, traj0, istep0, nsteps, _dp(q), _dp(p), _dp(f), _dp(e),
+                           st.ctypes.data_as(C.POINTER(C.c_int)), _dp(bx), _dp(pr), pressure_atm / PRESCON,
+                           BERENDSEN_COMPRESS, BERENDSEN_TAUPRES, nthreads)
+    if rc:
+        raise ValueError("run_npt needs the periodic QMDFF (PES 4)")
+    return q, p, f, e, st, bx, pr
+
+
 class XiDef(C.Structure):
     _fields_ = [("nreac1", C.c_int), ("reac1", C.c_int * 8), ("nreac2", C.c_int),
                 ("reac2", C.c_int * 8), ("form", C.c_int * 2), ("brk", C.c_int * 2),
@@ -175,6 +214,9 @@ def lib():
         _lib.orc_qmdff_set.argtypes = [C.POINTER(QmdffDef)]
         _lib.orc_qmdff_set2.argtypes = [C.POINTER(QmdffDef)]
         _lib.orc_qmdff_set_periodic.argtypes = [d, C.c_double, C.c_double, d]
+        _lib.orc_qmdff_egrad_virial.argtypes = [d, C.c_int, d, d, d, d]
+        _lib.orc_run_npt.argtypes = [C.POINTER(Cfg), C.c_int, C.c_uint32, C.c_int, C.c_int, d, d, d, d,
+                                     C.POINTER(C.c_int), d, d, C.c_double, C.c_double, C.c_double, C.c_int]
         _lib.orc_evb_set.argtypes = [C.c_int, d]
         _lib.orc_nhc_half.argtypes = [C.POINTER(Cfg), d, d]
         _lib.orc_evb_fit.argtypes = [C.c_int, d, C.c_int, C.c_int, d, d, d, d, d]

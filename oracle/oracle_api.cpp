@@ -90,6 +90,61 @@ void orc_qmdff_set_periodic(const double* box_ang, double coul_cut_ang, double v
   }
 }
 
+int orc_qmdff_egrad_virial(const double* q, int nbeads, const double* box, double* V, double* g, double* vir) {
+  if (!g_qmdff.periodic && box) return -1;
+  orc::qmdff::FF ff = g_qmdff;
+  const size_t n3 = (size_t)3 * ff.n;
+  for (int b = 0; b < nbeads; ++b) {
+    if (box)
+      for (int k = 0; k < 3; ++k) {
+        ff.len[k] = box[3 * (size_t)b + k];
+        ff.half[k] = ff.len[k] * 0.5;
+      }
+    double w = 0.0;
+    ff.vir = &w;
+    orc::qmdff::egrad(ff, &q[b * n3], &V[b], &g[b * n3]);
+    vir[b] = w;
+  }
+  return 0;
+}
+
+int orc_run_npt(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q, double* p,
+                double* f, double* epot, int* status, double* box, double* press, double pressure, double compress,
+                double taupres, int nthreads) {
+  if (cf->pes != 4 || !g_qmdff.periodic || !box || !press) return -1;
+  orc::StepConfig s = to_step(cf);
+  orc::NptConfig np;
+  np.pressure = pressure;
+  np.compress = compress;
+  np.taupres = taupres;
+  const size_t per = (size_t)3 * cf->natoms * cf->nbeads;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int t = 0; t < ntraj; ++t) {
+    orc::qmdff::FF ff = g_qmdff;  // this trajectory's box
+    double w = 0.0;
+    ff.vir = &w;
+    double* L = &box[3 * (size_t)t];
+    auto pes = [&](const double* qb, double* V, double* g) {
+      for (int k = 0; k < 3; ++k) {
+        ff.len[k] = L[k];
+        ff.half[k] = L[k] * 0.5;
+      }
+      orc::qmdff::egrad(ff, qb, V, g);
+    };
+    int st = 0;
+    double e = 0.0;
+    for (int n = 1; n <= nsteps; ++n)
+      st |= orc::verlet_step_npt(s, np, traj0 + t, istep0 + n, &q[t * per], &p[t * per], &f[t * per], &e, pes, L,
+                                 &press[t], &w);
+    if (epot) epot[t] = e;
+    if (status) status[t] |= st;
+  }
+  return 0;
+}
+
 void orc_qmdff_set2(const orc_qmdff_def* d) {
   orc::qmdff::FF keep = g_qmdff;
   orc_qmdff_set(d);

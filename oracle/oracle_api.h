@@ -90,6 +90,17 @@ void orc_qmdff_set(const orc_qmdff_def* d);
  * Angstrom; cuts (may be NULL) receives coul_cut, vdw_cut, zahn_a, zahn_par
  * as set (bohr). */
 void orc_qmdff_set_periodic(const double* box_ang, double coul_cut_ang, double vdw_cut_ang, double* cuts);
+/* The current force field on nbeads beads q(3, n, nbeads): V, g and each
+ * bead's virial trace vir[b] (the reference's vir_ten terms), the box of
+ * bead b box[3 b .. 3 b + 2] (bohr) where box is not NULL (the force field
+ * must be periodic).  Returns 0, or -1 for a box without set_periodic. */
+int orc_qmdff_egrad_virial(const double* q, int nbeads, const double* box, double* V, double* g, double* vir);
+/* orc_run with the Berendsen barostat (PES 4, periodic): box[3 t ..] (bohr)
+ * per trajectory in and out, press[t] the pressure of the last step (a.u.);
+ * pressure (a.u.), compress and taupres as mdinit sets them. */
+int orc_run_npt(const orc_cfg* cf, int ntraj, uint32_t traj0, int istep0, int nsteps, double* q, double* p,
+                double* f, double* epot, int* status, double* box, double* press, double pressure, double compress,
+                double taupres, int nthreads);
 /* The second force field and the coupling of PES id 5 (dE-EVB of the two):
  * basis 0..7 = const, 1g, 2g, 3g, sp, sd, sd2, sp2d; par = offa..offh, offm, offn. */
 void orc_qmdff_set2(const orc_qmdff_def* d);

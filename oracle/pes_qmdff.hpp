@@ -26,6 +26,7 @@
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 namespace orc {
@@ -73,7 +74,29 @@ struct FF {
   bool periodic = false;
   double len[3] = {0, 0, 0}, half[3] = {0, 0, 0};
   double vdw_cut = 0.0;
+  // NpT: where set, the terms add their share of the virial trace here
+  // (vir_ten of src/ff_eg.f90, ff_nonb.f90, eabhag.f90, eabxag.f90; the
+  // pressure uses its diagonal only, src/verlet.f90:1123-1131)
+  double* vir = nullptr;
 };
+
+// vir += a . b (FP64 evaluations only)
+template <class T>
+inline void vir_add(const FF& ff, const T* a, const T* b) {
+  if constexpr (std::is_same<T, double>::value)
+    if (ff.vir) *ff.vir += a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+// a torsion's or inversion's vir_ten: vab.g_a + vcb.(g_c + g_d) + vdc.g_d
+template <class T>
+inline void vir_tors(const FF& ff, const T* vab, const T* vcb, const T* vdc, const T* ga, const T* gc, const T* gd) {
+  if constexpr (std::is_same<T, double>::value)
+    if (ff.vir) {
+      const T gcd[3] = {gc[0] + gd[0], gc[1] + gd[1], gc[2] + gd[2]};
+      vir_add(ff, vab, ga);
+      vir_add(ff, vcb, gcd);
+      vir_add(ff, vdc, gd);
+    }
+}
 
 // box_image (src/box_image.f90:36-63): subtract the edge while a component
 // exceeds half of it (bounded here at 64 subtractions).
@@ -278,10 +301,13 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
     T pa = pow(rij / r, aai), pa2 = pow(rij / r, aai2);
     e = e + kij * (1. + pa - 2. * pa2);
     T fac = aai * kij * (-pa + pa2) / r2;
+    T ga[3];
     for (int c = 0; c < 3; ++c) {
-      g[3 * i + c] += fac * rb[c];
-      g[3 * j + c] -= fac * rb[c];
+      ga[c] = fac * rb[c];
+      g[3 * i + c] += ga[c];
+      g[3 * j + c] -= ga[c];
     }
+    vir_add(ff, rb, ga);  // src/ff_eg.f90:138-150
   }
   for (int m = 0; m < ff.nangl; ++m) {
     int j = ff.angl[3 * m], i = ff.angl[3 * m + 1], k = ff.angl[3 * m + 2];
@@ -320,16 +346,21 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
     T rmul1 = -deddt / (rab2 * rp);
     crprod(vcb, vp, dedc);
     T rmul2 = deddt / (rcb2 * rp);
+    T gla[3], glc[3];
     for (int c = 0; c < 3; ++c) {
       deda[c] *= rmul1;
       dedc[c] *= rmul2;
       T dedb = deda[c] + dedc[c];
       T t1 = ea * damp2ij * dampjk * vab[c];
       T t2 = ea * damp2jk * dampij * vcb[c];
-      g[3 * i + c] += deda[c] * damp + t1;
+      gla[c] = deda[c] * damp + t1;
+      glc[c] = dedc[c] * damp + t2;
+      g[3 * i + c] += gla[c];
       g[3 * j + c] += -dedb * damp - t1 - t2;
-      g[3 * k + c] += dedc[c] * damp + t2;
+      g[3 * k + c] += glc[c];
     }
+    vir_add(ff, vab, gla);  // src/ff_eg.f90:270-281
+    vir_add(ff, vcb, glc);
   }
   for (int m = 0; m < ff.ntors; ++m) {
     int i = ff.tors[6 * m], j = ff.tors[6 * m + 1], k = ff.tors[6 * m + 2], l = ff.tors[6 * m + 3];
@@ -379,15 +410,20 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
       }
       et = et * vt[1];
       dij = dij * vt[1] * damp;
+      T gla[3], glc[3], gld[3];
       for (int c = 0; c < 3; ++c) {
         T t1 = et * d2a * dampjk * dampkl * vab[c];
         T t2 = et * d2b * dampij * dampkl * vcb[c];
         T t3 = et * d2c * dampij * dampjk * vdc[c];
-        g[3 * i + c] += dij * dda[c] + t1;
+        gla[c] = dij * dda[c] + t1;
+        glc[c] = dij * ddc[c] + t3 - t2;
+        gld[c] = dij * ddd[c] - t3;
+        g[3 * i + c] += gla[c];
         g[3 * j + c] += dij * ddb[c] - t1 + t2;
-        g[3 * k + c] += dij * ddc[c] + t3 - t2;
-        g[3 * l + c] += dij * ddd[c] - t3;
+        g[3 * k + c] += glc[c];
+        g[3 * l + c] += gld[c];
       }
+      vir_tors(ff, vab, vcb, vdc, gla, glc, gld);  // src/ff_eg.f90:420-440
       e = e + et * damp;
     } else {
       for (int c = 0; c < 3; ++c) {
@@ -418,15 +454,22 @@ inline void ff_eg(const FF& ff, const T* x, T* e_out, T* g) {
         et = vt[1] * (d * d);
         dij = 2. * vt[1] * sin(phi) * (cos(phi0) - cos(phi)) * damp;
       }
+      T gla[3], glc[3], gld[3];
       for (int c = 0; c < 3; ++c) {
         T t1 = et * d2a * dampjk * dampjl * vab[c];
         T t2 = et * d2b * dampij * dampjl * vcb[c];
         T t3 = et * d2c * dampij * dampjk * vdc[c];
-        g[3 * i + c] += dij * dda[c] - t1;
+        gla[c] = dij * dda[c] - t1;
+        glc[c] = dij * ddc[c] - t2;
+        gld[c] = dij * ddd[c] - t3;
+        g[3 * i + c] += gla[c];
         g[3 * j + c] += dij * ddb[c] + t1 + t2 + t3;
-        g[3 * k + c] += dij * ddc[c] - t2;
-        g[3 * l + c] += dij * ddd[c] - t3;
+        g[3 * k + c] += glc[c];
+        g[3 * l + c] += gld[c];
       }
+      // the torsions' formula with the inversion's vectors, which point at
+      // the centre j (src/ff_eg.f90:583-603)
+      vir_tors(ff, vab, vcb, vdc, gla, glc, gld);
       e = e + et * damp;
     }
   }
@@ -469,6 +512,7 @@ inline void ff_nonb(const FF& ff, const T* x, T* enb, T* g) {
       g[3 * i1 + c] += ga[c];
       g[3 * i2 + c] -= ga[c];
     }
+    vir_add(ff, vab, ga);  // src/ff_nonb.f90:180-190, 318-328
   }
   for (int kp = 0; kp < ff.nnci; ++kp) {
     int i1 = ff.nci[3 * kp], i2 = ff.nci[3 * kp + 1], nk = ff.nci[3 * kp + 2];
@@ -486,11 +530,13 @@ inline void ff_nonb(const FF& ff, const T* x, T* enb, T* g) {
       e0 = ff.q[i1] * ff.q[i2] * oner * ff.eps1[nk] * 1.0;
     e = e + e0;
     T drij = e0 / r2;
+    T ga[3];
     for (int c = 0; c < 3; ++c) {
-      T ga = -vab[c] * drij;
-      g[3 * i1 + c] += ga;
-      g[3 * i2 + c] -= ga;
+      ga[c] = -vab[c] * drij;
+      g[3 * i1 + c] += ga[c];
+      g[3 * i2 + c] -= ga[c];
     }
+    vir_add(ff, vab, ga);  // src/ff_nonb.f90:405-415, 495-505
   }
   *enb = *enb + e;
 }
@@ -579,6 +625,8 @@ inline void eabhag(const FF& ff, const T* x, int A, int B, int H, double ca, dou
     g[3 * B + c] += gb[c];
     g[3 * H + c] += gh[c];
   }
+  vir_add(ff, drah, ga);  // src/eabhag.f90:203-216
+  vir_add(ff, drbh, gb);
 }
 
 // eabx (src/eabx.f90:34-111): halogen-bond energy of A...X-B (X = H arg).
@@ -607,13 +655,16 @@ inline T eabx(const T* x, int A, int B, int H, double ca) {
 
 // eabxag (src/eabxag.f90:35-156): energy plus Caracal's difference quotients
 // (step 1e-6); each atom's three components all get the z-direction quotient.
+// The virial (src/eabxag.f90:86-87, 140-153) pairs (r_A - r_X) with A's
+// gradient and (r_B - r_X) with the X atom's, raw coordinates.
 template <class T>
-inline void eabxag(const T* x0, int n, int A, int B, int H, double ca, T* e, T* g) {
+inline void eabxag(const T* x0, int n, int A, int B, int H, double ca, T* e, T* g, const FF* ffv = nullptr) {
   std::vector<T> x(x0, x0 + 3 * n);
   *e = *e + eabx<T>(x.data(), A, B, H, ca);
   const double step = 1.0e-6;
   const double dum = 1.0 / (2.0 * step);
   const int atoms[3] = {A, B, H};
+  T lastq[3];
   for (int ia = 0; ia < 3; ++ia) {
     const int at = atoms[ia];
     T last = 0.0;
@@ -626,6 +677,18 @@ inline void eabxag(const T* x0, int n, int A, int B, int H, double ca, T* e, T* 
       last = (er - el) * dum;
     }
     for (int c = 0; c < 3; ++c) g[3 * at + c] += last;
+    lastq[ia] = last;
+  }
+  if (ffv) {
+    T vah[3], vbh[3], gA[3], gH[3];
+    for (int c = 0; c < 3; ++c) {
+      vah[c] = x0[3 * A + c] - x0[3 * H + c];
+      vbh[c] = x0[3 * B + c] - x0[3 * H + c];
+      gA[c] = lastq[0];
+      gH[c] = lastq[2];
+    }
+    vir_add(*ffv, vah, gA);
+    vir_add(*ffv, vbh, gH);
   }
 }
 
@@ -641,7 +704,7 @@ inline void ff_hb(const FF& ff, const T* x, T* eh, T* g) {
     T r = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
     if (r > 15.0) continue;
     if (ff.at[i] == 1) eabhag<T>(ff, x, i1, i2, i, ff.vhb[2 * k], ff.vhb[2 * k + 1], eh, g);
-    else eabxag<T>(x, ff.n, i1, i2, i, ff.vhb[2 * k], eh, g);
+    else eabxag<T>(x, ff.n, i1, i2, i, ff.vhb[2 * k], eh, g, &ff);
   }
 }
 

@@ -508,4 +508,54 @@ inline int verlet_step(const StepConfig& cf, uint32_t traj, int istep, double* q
   return status;
 }
 
+// NpT with the Berendsen barostat (src/verlet.f90, barostat 1): the box
+// (3 edges, bohr) scales with the coordinates after each step.
+struct NptConfig {
+  double pressure = 0.0;  // target, a.u. (PRES / prescon, src/dynamic.f90:1331-1335)
+  double compress = 0.0;  // mdinit: 0.000046 prescon / 1000 (src/mdinit.f90:155-158)
+  double taupres = 0.0;   // mdinit: 2.0
+};
+
+// One NpT step: verlet_step's order with the virial trace reset at the start
+// (src/verlet.f90:164-167) and accumulated by `egrad` into *vir over the
+// beads; NHC is not applied (under the Berendsen barostat the reference
+// calls neither nhc nor nhc_npt, src/verlet.f90:189-208, 1088-1106); after the
+// second half kick the pressure from the virial alone (the kinetic stress
+// tensor is accumulated by multiplication from zero and stays zero,
+// src/verlet.f90:1111-1132) and the Berendsen scaling of box and coordinates
+// (src/verlet.f90:1138-1151), then Andersen, the NaN check and transrot.
+template <class EGrad>
+inline int verlet_step_npt(const StepConfig& cf, const NptConfig& np, uint32_t traj, int istep, double* q,
+                           double* p, double* f, double* epot, EGrad egrad, double* box, double* press,
+                           double* vir) {
+  const int N = cf.natoms, P = cf.nbeads, n3 = 3 * N;
+  const size_t nall = (size_t)n3 * P;
+  const double volbox = box[0] * box[1] * box[2];
+  *vir = 0.0;
+  if (cf.thermostat == 3) pile_half(cf, traj, (uint32_t)istep, TAG_PILE_A, p);
+  for (size_t x = 0; x < nall; ++x) p[x] = p[x] - 0.5 * cf.dt * f[x];
+  free_rp_step(cf, q, p);
+  double e = 0.0;
+  for (int k = 0; k < P; ++k) {
+    double v;
+    egrad(&q[(size_t)k * n3], &v, &f[(size_t)k * n3]);
+    e = e + v;
+  }
+  *epot = e;
+  for (size_t x = 0; x < nall; ++x) p[x] = p[x] - 0.5 * cf.dt * f[x];
+  const double factor = 1.0 / volbox;
+  *press = (factor * (0.0 - *vir)) / 3.0;
+  const double scale = std::pow(1.0 + (cf.dt * np.compress / np.taupres) * (*press - np.pressure), 1.0 / 3.0);
+  for (int k = 0; k < 3; ++k) box[k] = box[k] * scale;
+  for (size_t x = 0; x < nall; ++x) q[x] = q[x] * scale;
+  if (cf.thermostat == 1 && istep % cf.andersen_step == 0)
+    andersen(cf, traj, (uint32_t)istep, TAG_ANDERSEN, p);
+  if (cf.thermostat == 3) pile_half(cf, traj, (uint32_t)istep, TAG_PILE_B, p);
+  int status = TRAJ_OK;
+  for (size_t x = 0; x < nall; ++x)
+    if (!std::isfinite(q[x])) status |= TRAJ_NONFINITE;
+  if (cf.transrot && transrot(cf, q, p)) status |= TRAJ_SINGULAR_INERTIA;
+  return status;
+}
+
 }  // namespace orc

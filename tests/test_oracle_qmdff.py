@@ -175,3 +175,82 @@ def test_periodic_rules_and_large_box_limit():
     assert c[0] == rc and c[2] == a
     assert abs(c[3] - (erfc(a * rc) / rc ** 2 + 2 * a / sqrt(pi) * exp(-(a * rc) ** 2) / rc)) < 1e-15
     orc.set_qmdff(ff, tab)
+
+
+def _no_torsions(ff):
+    from caracal_gb300 import qmdff as Q
+    return Q.QMDFF(**{**ff.__dict__, "tors": np.zeros((0, 6), int), "vtors": np.zeros((0, 14))})
+
+
+def test_virial_bonds_angles_pairs_is_the_scaling_derivative():
+    """The virial trace of the terms whose reference formula is the sum of
+    (r - r_ref).g over the term's atoms (bonds, angles, NCI pairs and
+    hydrogen bonds, src/ff_eg.f90:138-150, 270-281, src/ff_nonb.f90:180-190,
+    405-415): for a whole molecule in a box with cutoffs beyond every pair it
+    is dE/ds of the uniform scaling r -> s r at s = 1."""
+    from caracal_gb300 import qmdff as Q
+    ff = _no_torsions(Q.alkane())
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
+    orc.set_qmdff_periodic([400.0, 400.0, 400.0], 150.0, 150.0)
+    x = ff.xyz[None] + np.random.default_rng(7).normal(0, 0.05, (3,) + ff.xyz.shape)
+    _, g, w = orc.qmdff_egrad_virial(x)
+    assert np.allclose(w, np.einsum("bij,bij->b", x, g), rtol=1e-12, atol=1e-12)
+    h = 1e-6
+    ep, _ = orc.egrad("qmdff", x * (1 + h))
+    em, _ = orc.egrad("qmdff", x * (1 - h))
+    assert np.allclose(w, (ep - em) / (2 * h), rtol=1e-6, atol=1e-9)
+
+
+def test_virial_torsions_follow_the_reference_vectors():
+    """With torsions the reference's formula vab.g_i + vcb.(g_k + g_l) +
+    vdc.g_l (vcb = r_j - r_k, vdc = r_k - r_l, src/ff_eg.f90:317-320,
+    420-440) differs from sum (r - r_j).g; the difference is
+    -2 [(r_k - r_j).(g_k + g_l) + (r_l - r_k).g_l] per torsion, so the trace
+    is not the scaling derivative (and the force field's total is)."""
+    from caracal_gb300 import qmdff as Q
+    ff = Q.alkane()
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
+    orc.set_qmdff_periodic([400.0, 400.0, 400.0], 150.0, 150.0)
+    x = ff.xyz[None] + np.random.default_rng(8).normal(0, 0.05, (2,) + ff.xyz.shape)
+    _, g, w = orc.qmdff_egrad_virial(x)
+    orc.set_qmdff(_no_torsions(ff), Q.ElementTables.caracal())
+    orc.set_qmdff_periodic([400.0, 400.0, 400.0], 150.0, 150.0)
+    _, g0, w0 = orc.qmdff_egrad_virial(x)
+    gt = g - g0                                  # the torsions' gradient
+    consistent = np.einsum("bij,bij->b", x, gt)  # sum r.g of the torsion terms = dE_tors/ds
+    assert np.all(np.abs((w - w0) - consistent) > 1e-8 * np.abs(consistent).max())
+    # a rigid translation leaves it unchanged (each term's vectors are differences)
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
+    orc.set_qmdff_periodic([400.0, 400.0, 400.0], 150.0, 150.0)
+    _, _, wt = orc.qmdff_egrad_virial(x + np.array([0.3, -1.1, 2.0]))
+    assert np.allclose(wt, w, rtol=1e-10, atol=1e-12)
+
+
+def test_npt_berendsen_oracle_step():
+    """One Berendsen step (src/verlet.f90:1111-1151): the pressure is
+    -tr W / (3 V) from the step's virial, box and coordinates scale by
+    (1 + dt compress / taupres (p - p0))^(1/3)."""
+    from caracal_gb300 import qmdff as Q
+    from caracal_gb300.units import beta_from_kelvin, dt_fs_to_au, mass_au
+    ff = Q.alkane(nc=3)
+    orc.set_qmdff(ff, Q.ElementTables.caracal())
+    orc.set_qmdff_periodic([15.0, 15.0, 15.0], 50.0, 10.0)
+    mass = [mass_au("C" if z == 6 else "H") for z in ff.at]
+    dt = dt_fs_to_au(0.5)
+    cfg = orc.Config("qmdff", mass, 2, dt, beta_from_kelvin(300.0), thermostat="andersen", andersen_step=5,
+                     transrot=True, seed=3)
+    q = orc.init_positions(cfg, 2, ff.xyz, 0.02)
+    p = orc.init_momenta(cfg, 2)
+    f, _ = orc.init_forces(cfg, q)
+    box0 = np.full((2, 3), 15.0 / 0.52917721092)
+    q1, p1, f1, e1, st, box1, pr = orc.run_npt(cfg, q, p, f, 1, box0, 1.0)
+    # the pressure from the virial of the step's own forces: the pre-scaling
+    # positions are q1 / scale
+    scale = box1[:, 0] / box0[:, 0]
+    _, _, w = orc.qmdff_egrad_virial((q1 / scale[:, None, None, None]).reshape(-1, ff.n, 3),
+                                     np.repeat(box0, 2, axis=0))
+    V = np.prod(box0, axis=1)
+    assert np.allclose(pr, -w.reshape(2, 2).sum(axis=1) / (3 * V), rtol=1e-10)
+    rate = dt * orc.BERENDSEN_COMPRESS / orc.BERENDSEN_TAUPRES
+    assert np.allclose(scale, (1 + rate * (pr - 1.0 / orc.PRESCON)) ** (1 / 3), rtol=1e-14)
+    assert np.allclose(box1, box0 * scale[:, None], rtol=1e-15) and not st.any()
