@@ -186,7 +186,7 @@ def _sig(lib):
         "cr_engine_set_andersen_step": ([eng, C.c_int], C.c_int),
         "cr_engine_set_launch": ([eng, C.c_int, C.c_int], C.c_int),
         "cr_engine_set_npt": ([eng, C.c_double, d], C.c_int),
-        "cr_engine_get_npt": ([eng, d, d], C.c_int),
+        "cr_engine_get_npt": ([eng, d, d, d, C.c_int], C.c_int),
         "cr_engine_get_launch": ([eng, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
         "cr_engine_autotune": ([eng, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)],
                                C.c_int),

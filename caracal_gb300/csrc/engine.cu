@@ -584,8 +584,8 @@ int split_group_launches(cr_engine* e, const cr::SplitParams& s, int t0, int tn,
     }
   }
   if (e->npt) {  // pressure and Berendsen scaling (src/verlet.f90:1111-1151)
-    const cr::NptStep np{e->d_box + 3 * (size_t)t0, e->d_press + t0, e->d_vir + (size_t)t0 * e->P, e->npt_pressure,
-                         e->npt_rate};
+    const cr::NptStep np{e->d_box + 3 * (size_t)t0, e->d_press + 2 * (size_t)t0, e->d_vir + (size_t)t0 * e->P,
+                         e->npt_pressure, e->npt_rate};
     cr::split_berendsen_kernel<<<tn, 128, 0, st>>>(s, np);
     CR_CUDA(cudaGetLastError());
     ++n;
@@ -1779,11 +1779,11 @@ int cr_engine_set_npt(cr_engine* e, double pressure_atm, const double* box_bohr)
   CR_CUDA(cudaStreamSynchronize(e->stream));
   if (!e->d_box) {
     CR_CUDA(cudaMalloc(&e->d_box, 3 * T * sizeof(double)));
-    CR_CUDA(cudaMalloc(&e->d_press, T * sizeof(double)));
+    CR_CUDA(cudaMalloc(&e->d_press, 2 * T * sizeof(double)));
     CR_CUDA(cudaMalloc(&e->d_vir, T * (size_t)e->P * sizeof(double)));
   }
   CR_CUDA(cudaMemcpy(e->d_box, box.data(), 3 * T * sizeof(double), cudaMemcpyHostToDevice));
-  CR_CUDA(cudaMemset(e->d_press, 0, T * sizeof(double)));
+  CR_CUDA(cudaMemset(e->d_press, 0, 2 * T * sizeof(double)));
   CR_CUDA(cudaMemset(e->d_vir, 0, T * (size_t)e->P * sizeof(double)));
   // mdinit's Berendsen constants (src/mdinit.f90:155-158) and the pressure
   // unit (src/general.f90:263, src/dynamic.f90:1331-1335)
@@ -1795,12 +1795,22 @@ int cr_engine_set_npt(cr_engine* e, double pressure_atm, const double* box_bohr)
   return CR_OK;
 }
 
-int cr_engine_get_npt(cr_engine* e, double* box_bohr, double* pressure_au) {
+int cr_engine_get_npt(cr_engine* e, double* box_bohr, double* pressure_au, double* pressure_sum_au, int reset_sum) {
   if (!e) return fail(CR_ERR_ARG, "NULL engine");
   if (!e->npt) return fail(CR_ERR_ARG, "NpT is not set (cr_engine_set_npt)");
   CR_CUDA(cudaStreamSynchronize(e->stream));
-  if (box_bohr) CR_CUDA(cudaMemcpy(box_bohr, e->d_box, 3 * (size_t)e->T * sizeof(double), cudaMemcpyDeviceToHost));
-  if (pressure_au) CR_CUDA(cudaMemcpy(pressure_au, e->d_press, (size_t)e->T * sizeof(double), cudaMemcpyDeviceToHost));
+  const size_t T = (size_t)e->T;
+  if (box_bohr) CR_CUDA(cudaMemcpy(box_bohr, e->d_box, 3 * T * sizeof(double), cudaMemcpyDeviceToHost));
+  if (pressure_au || pressure_sum_au) {
+    std::vector<double> h(2 * T);
+    CR_CUDA(cudaMemcpy(h.data(), e->d_press, 2 * T * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t t = 0; t < T; ++t) {
+      if (pressure_au) pressure_au[t] = h[2 * t];
+      if (pressure_sum_au) pressure_sum_au[t] = h[2 * t + 1];
+    }
+  }
+  if (reset_sum)  // the running sums only: every other word
+    CR_CUDA(cudaMemset2D(e->d_press + 1, 2 * sizeof(double), 0, sizeof(double), T));
   return CR_OK;
 }
 

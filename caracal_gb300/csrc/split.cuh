@@ -841,7 +841,7 @@ __global__ void __launch_bounds__(kFinishBlock) split_nhc_kernel(SplitParams s) 
 // coordinates and the step's NaN check.
 struct NptStep {
   double* box;        // [T][3] edges, bohr
-  double* press;      // [T] the step's pressure, a.u.
+  double* press;      // [T][2] the step's pressure and the running sum, a.u.
   const double* vir;  // [T][P] virial trace per bead
   double pressure;    // target, a.u.
   double rate;        // dt compress / taupres
@@ -858,7 +858,8 @@ __global__ void split_berendsen_kernel(SplitParams s, NptStep n) {
     const double pr = (factor * (0.0 - w)) / 3.0;
     const double sc = pow(1.0 + n.rate * (pr - n.pressure), 1.0 / 3.0);
     for (int k = 0; k < 3; ++k) L[k] = L[k] * sc;
-    n.press[t] = pr;
+    n.press[2 * (size_t)t] = pr;
+    n.press[2 * (size_t)t + 1] += pr;  // press_avg (src/verlet.f90:1171-1173)
     scale = sc;
   }
   __syncthreads();

@@ -9,11 +9,17 @@ step (src/verlet.f90:780-800, 666-676, 1170-1205; src/dynamic.f90:1458-1486, 167
 each frame from a page-locked snapshot while the GPU runs the next steps
 (cr_engine_run_dump_async):
 
-  trajectory.xyz       natoms*nbeads, a blank line, `name x y z` (Angstrom) for
-                       every bead (not with OUTPUT_SPARSE and nbeads > 1)
+  trajectory.xyz       natoms*nbeads, a blank line (NpT: the box edges),
+                       `name x y z` (Angstrom) for every bead (not with
+                       OUTPUT_SPARSE and nbeads > 1)
   traj_centroid.xyz    the centroid frame (nbeads > 1)
   md_energies.dat      (E_CON) istep, Epot/P, Ekin/P, (Epot+Ekin)/P
-  stdout               " Step: ... -- pot. energy: ... Hartree -- temperature: ... K"
+  stdout               " Step: ... -- pot. energy: ... Hartree -- temperature: ... K";
+                       NpT: step, Epot/P, T, volume (A^3), the pressure averaged
+                       over the dump interval (atm), density (g/cm^3)
+
+ENSEMBLE NPT (Berendsen barostat, periodic QMDFF) dumps synchronously: the
+state, each trajectory's box and the pressure sum every TDUMP/DELTAT steps.
 
 Numbers are written as gfortran's list-directed output writes them (REAL(8):
 17 significant digits, G-style, 26 columns; INTEGER: 12 columns).  With
@@ -30,7 +36,9 @@ import numpy as np
 
 from . import keyfile as K
 from .units import BOHR_ANGSTROM, angstrom_to_bohr, beta_from_kelvin, dt_fs_to_au, mass_au, nose_q_to_au
-from .units import temperature_from_ekin
+from .units import EMASS_AMU, temperature_from_ekin
+
+PRESCON = 290371576.61  # Hartree/bohr^3 -> atm (src/general.f90:263)
 
 
 def fortran_real(x):
@@ -54,8 +62,11 @@ def fortran_int(n):
     return f"{int(n):>12}"
 
 
-def write_frame(f, names, xyz_ang):
-    f.write(fortran_int(len(names)) + "\n\n")
+def write_frame(f, names, xyz_ang, box_ang=None):
+    """One xyz frame; under NpT the comment line holds the box edges
+    (src/verlet.f90:669-673, 788-795)."""
+    comment = "" if box_ang is None else "".join(fortran_real(v) for v in box_ang)
+    f.write(fortran_int(len(names)) + "\n" + comment + "\n")
     for nm, r in zip(names, xyz_ang):
         f.write(" " + f"{nm:<3}" + "".join(fortran_real(v) for v in r) + "\n")
     f.flush()
@@ -107,6 +118,9 @@ def run(path, out_dir=None, quiet=False):
     eng = RPMDEngine(pes, mass, d.nbeads, d.ntraj, dt_fs_to_au(d.dt_fs), beta=beta, thermostat=thermo,
                      andersen_step=d.andersen_step, transrot=True, precision="fp64", seed=d.seed,
                      nose_q_au=nose_q_to_au(d.nose_damp, d.dt_fs))
+    npt = d.ensemble == "NPT"
+    if npt:  # Berendsen barostat on the periodic force field's box
+        eng.set_npt(d.pressure)
     eng.init_positions(q0, 0.0)
     eng.init_momenta(zero=nve)
     eng.compute_forces()
@@ -125,17 +139,26 @@ def run(path, out_dir=None, quiet=False):
         ener.write(" #   MD step   pot.energy    kin.energy   total energy \n")
     iw = max(d.iwrite, 1)
 
-    def dump(istep, q, p, epot):
+    def dump(istep, q, p, epot, box=None, press_avg=None):
         ekin = float(np.mean(np.sum(p * p / (2.0 * mass[None, None, :, None]), axis=(1, 2, 3))))
         ep = float(np.mean(epot))
+        b0 = None if box is None else box[0] * BOHR_ANGSTROM
         if traj:
-            write_frame(traj, names * P, q[0].reshape(-1, 3) * BOHR_ANGSTROM)
+            write_frame(traj, names * P, q[0].reshape(-1, 3) * BOHR_ANGSTROM, b0)
         if cen:
-            write_frame(cen, names, q[0].mean(axis=0) * BOHR_ANGSTROM)
+            write_frame(cen, names, q[0].mean(axis=0) * BOHR_ANGSTROM, b0)
         if ener:
             ener.write(fortran_int(istep) + fortran_real(ep / P) + fortran_real(ekin / P) +
                        fortran_real((ep + ekin) / P) + "\n")
-        if not quiet:
+        if not quiet and box is not None:
+            # src/verlet.f90:1190-1197: volume (A^3), press_avg (atm), density
+            # (g/cm^3; the REAL(4) literals 1.6605402E-24 and 1E-24 widened)
+            t = temperature_from_ekin(ekin, N, P)
+            vol = float(np.mean(np.prod(box, axis=1))) * BOHR_ANGSTROM ** 3
+            dens = (float(np.sum(mass)) * float(np.float32(1.6605402e-24)) * EMASS_AMU) / (vol * float(np.float32(1e-24)))
+            print(f"{istep:8d}{ep / P:12.5f}     {t:10.4f}  {vol:12.4f}{float(np.mean(press_avg)) * PRESCON:14.5f}"
+                  f"    {dens:12.6f}")
+        elif not quiet:
             if nve:
                 print(f" Step: {istep:8d}  --  pot. energy: {ep / P:12.5f} Hartree ")
             else:
@@ -145,8 +168,20 @@ def run(path, out_dir=None, quiet=False):
         return False
 
     try:
-        # frames are written from page-locked snapshots while the GPU steps on
-        eng.run_dump_async(d.nstep, iw, dump)
+        if npt:
+            # every iwrite steps: the state, the boxes and the pressure sum
+            done = 0
+            while done + iw <= d.nstep:
+                eng.run(iw)
+                done += iw
+                q, p, _, epot, _ = eng.get_state()
+                box, _, psum = eng.npt_state(reset_sum=True)
+                dump(done, q, p, epot, box, psum / iw)
+            if done < d.nstep:
+                eng.run(d.nstep - done)
+        else:
+            # frames are written from page-locked snapshots while the GPU steps on
+            eng.run_dump_async(d.nstep, iw, dump)
     finally:
         for fh in (traj, cen, ener):
             if fh:

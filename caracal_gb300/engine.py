@@ -555,12 +555,14 @@ class RPMDEngine:
         L.check(L.lib().cr_engine_set_npt(self._h, float(pressure_atm), None if bx is None else L.dptr(bx)),
                 "set_npt")
 
-    def npt_state(self):
-        """(box (ntraj, 3) bohr, the last step's pressure (ntraj,) a.u.)."""
+    def npt_state(self, reset_sum=False):
+        """(box (ntraj, 3) bohr, the last step's pressure (ntraj,) a.u., the
+        sum of the pressures since the last reset (ntraj,) a.u.)."""
         box = np.zeros((self.ntraj, 3))
-        pr = np.zeros(self.ntraj)
-        L.check(L.lib().cr_engine_get_npt(self._h, L.dptr(box), L.dptr(pr)), "get_npt")
-        return box, pr
+        pr, ps = np.zeros(self.ntraj), np.zeros(self.ntraj)
+        L.check(L.lib().cr_engine_get_npt(self._h, L.dptr(box), L.dptr(pr), L.dptr(ps), int(bool(reset_sum))),
+                "get_npt")
+        return box, pr, ps
 
     def set_launch(self, threads_per_block=0, threads_per_bead=1):
         """Threads per block and per bead of the persistent step kernel

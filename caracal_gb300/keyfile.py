@@ -4,9 +4,12 @@ A key file is a list of lines; the first word of a line is the keyword
 (case-insensitive), the rest its values, and a line `NAME {` opens a block
 closed by `}`.  Read here, with Caracal's defaults and checks:
 
-  general (src/dynamic.f90:243-320): XYZSTART file, RPMD_BEADS n, ENSEMBLE NVE|NVT,
+  general (src/dynamic.f90:243-320): XYZSTART file, RPMD_BEADS n, ENSEMBLE NVE|NVT|NPT,
     STEPS n, DELTAT dt_fs, TDUMP t_fs   (iwrite = nint(TDUMP / DELTAT))
   NVT { TEMP K, THERMOSTAT ANDERSEN|NOSE-HOOVER, ANDERSEN_STEP n, NOSE_DAMP n }
+  NPT { TEMP K, PRES atm, THERMOSTAT ..., BAROSTAT BERENDSEN, ANDERSEN_STEP n,
+    NOSE_DAMP n, BARO_DAMP n }  (src/dynamic.f90:478-580; periodic QMDFF only;
+    BAROSTAT NOSE-HOOVER stops: its chain is not built here)
     (src/dynamic.f90:382-473; defaults TEMP 0, ANDERSEN_STEP 70, NOSE_DAMP 100)
   PES ANA_H3 | ANA_CH4H | ANA_CH4OH | ANA_OH3 | ANA_GEH4OH | QMDFF | DE_EVB
     (src/read_pes.f90:203, 413-631)
@@ -31,7 +34,7 @@ import numpy as np
 
 ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh", "ANA_OH3": "oh3", "ANA_GEH4OH": "geh4oh"}
 EVB_BASES = ("1g", "2g", "3g", "sp", "sd", "sd2", "sp2d")
-KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE",
+KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE", "NPT",
          "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "READ_VEL", "PERIODIC", "}"}
 
 
@@ -64,6 +67,8 @@ class DynamicInput:
     zahn: bool = False           # QMDFF { COULOMB ZAHN }
     coul_cut: float = 50.0       # QMDFF { COUL_CUTOFF } (Angstrom where periodic)
     vdw_cut: float = 10.0        # QMDFF { VDW_CUTOFF } (Angstrom)
+    pressure: float = 0.0        # NPT { PRES } (atm)
+    barostat: str = ""           # NPT { BAROSTAT }: "berendsen"
     unsupported: list = field(default_factory=list)
     directory: str = "."
 
@@ -145,15 +150,14 @@ def parse(text, directory="."):
         raise KeyError_("The number of RPMD beads must be positive!")
     if d.ensemble not in ("NVE", "NVT", "NPT"):
         raise KeyError_("No valid thermodynamic ensemble given! Choose either NVE, NVT or NPT.")
-    if d.ensemble == "NPT":
-        raise KeyError_("NPT (barostat, periodic box) is not on this engine's path")
     if d.nstep < 1:
         raise KeyError_("The number of MD timesteps must be greater than zero!")
     if d.dt_fs < 1e-5:
         raise KeyError_("The MD timestep is too small to be useful!")
-    if d.ensemble == "NVT":
+    if d.ensemble in ("NVT", "NPT"):
         thermo = "none"
-        for ln in _blocks(lines, "NVT"):
+        baro = "BERENDSEN"  # src/dynamic.f90:485 (the default)
+        for ln in _blocks(lines, d.ensemble):
             w = _words(ln)
             k = w[0].upper()
             if k == "TEMP":
@@ -164,8 +168,20 @@ def parse(text, directory="."):
                 d.andersen_step = int(w[1])
             elif k == "NOSE_DAMP":
                 d.nose_damp = float(w[1])
+            elif k == "PRES" and d.ensemble == "NPT":
+                d.pressure = float(w[1].replace("d", "e").replace("D", "E"))
+            elif k == "BAROSTAT" and d.ensemble == "NPT":
+                baro = w[1].upper() if len(w) > 1 else ""
         if d.kelvin < 0.0:
             raise KeyError_("Give a positive temperature!")
+        if d.ensemble == "NPT":
+            if baro == "NOSE-HOOVER":
+                raise KeyError_("BAROSTAT NOSE-HOOVER (nhc_npt) is not on this engine's path; BERENDSEN is")
+            if baro != "BERENDSEN":
+                raise KeyError_("No valid barostat chosen! BERENDSEN and NOSE-HOOVER are available!")
+            if d.pressure < 0.0:
+                raise KeyError_("Give a positive pressure!")
+            d.barostat = "berendsen"
         if thermo == "ANDERSEN":
             d.thermostat = "andersen"
         elif thermo == "NOSE-HOOVER":
@@ -203,6 +219,10 @@ def parse(text, directory="."):
         raise KeyError_(f"PES {d.pes or '(none)'} is not on this engine's path")
     if d.box and d.pes in ANALYTIC:
         raise KeyError_("PERIODIC applies to QMDFF force fields on this engine")
+    if d.ensemble == "NPT" and not d.box:
+        raise KeyError_("The NPT ensemble can only be simulated in periodic systems!")
+    if d.ensemble == "NPT" and d.pes != "QMDFF":
+        raise KeyError_("NPT is built for one QMDFF force field on this engine")
     return d
 
 

@@ -550,9 +550,12 @@ int cr_engine_set_andersen_step(cr_engine* e, int andersen_step);
  * CR_ERR_UNSUPPORTED for other force fields, dE-EVB, constrained parents and
  * umbrella windows. */
 int cr_engine_set_npt(cr_engine* e, double pressure_atm, const double* box_bohr);
-/* Each trajectory's box edges (bohr, T x 3) and its last step's pressure
- * (a.u.; x prescon = 290371576.61 for atm); either pointer may be NULL. */
-int cr_engine_get_npt(cr_engine* e, double* box_bohr, double* pressure_au);
+/* Each trajectory's box edges (bohr, T x 3), its last step's pressure and
+ * the sum of its pressures since the last reset (a.u.; x prescon =
+ * 290371576.61 for atm; Caracal prints that sum / iwrite as press_avg,
+ * src/verlet.f90:1171-1210); any pointer may be NULL; reset_sum != 0 zeroes
+ * the sums after reading. */
+int cr_engine_get_npt(cr_engine* e, double* box_bohr, double* pressure_au, double* pressure_sum_au, int reset_sum);
 
 /* Launch shape of the persistent step kernel (analytic surfaces; the graph
  * path of force fields has none and returns CR_ERR_UNSUPPORTED).  A

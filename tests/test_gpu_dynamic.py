@@ -163,3 +163,46 @@ def test_dynamic_periodic_qmdff(require_gpu, tmp_path):
     # the frames are written with 17 digits: the energies agree to ~1e-12
     assert np.abs(e_dump - ep).max() < 1e-9 * max(1.0, np.abs(ep).max())
     assert np.abs(ep - ef).min() > 1e-6          # the cutoff acts on this chain
+
+
+def test_dynamic_npt_berendsen(require_gpu, tmp_path, capsys):
+    """ENSEMBLE NPT with the Berendsen barostat: the frames carry each dump's
+    box (Angstrom) on the comment line, equal to the engine's NpT state after
+    the same steps, and stdout has the NpT columns."""
+    from caracal_gb300.engine import QMDFFForceField
+    ff = Q.alkane(nc=4)
+    Q.write_qmdff(ff, tmp_path / "a.qmdff")
+    sym = ["C" if z == 6 else "H" for z in ff.at]
+    (tmp_path / "start.xyz").write_text(f"{ff.n}\n\n" + "".join(
+        f"{s} {a} {b} {c}\n" for s, (a, b, c) in zip(sym, ff.xyz * BOHR_ANGSTROM)))
+    key = ("XYZSTART start.xyz\nRPMD_BEADS 2\nENSEMBLE NPT\nSTEPS 20\nDELTAT 0.5\nTDUMP 2.5\nE_CON\nSEED 4\n"
+           "NPT {\n TEMP 300\n PRES 100.0\n THERMOSTAT ANDERSEN\n ANDERSEN_STEP 7\n}\nPES QMDFF\n"
+           "PERIODIC 16.0 16.0 16.0\nQMDFF {\n FFNAMES a.qmdff\n}\n")
+    (tmp_path / "p.key").write_text(key)
+    run(str(tmp_path / "p.key"), out_dir=str(tmp_path), quiet=False)
+    out = capsys.readouterr().out.splitlines()
+    assert len(out) == 4 and all(len(ln.split()) == 6 for ln in out)
+    lines = open(tmp_path / "trajectory.xyz").read().splitlines()
+    n = 2 * ff.n
+    boxes = [np.array([float(v) for v in lines[k * (n + 2) + 1].split()]) for k in range(4)]
+    assert all(b.shape == (3,) for b in boxes) and not np.allclose(boxes[0], boxes[-1])
+    # the same run through the engine
+    gff = QMDFFForceField(Q.read_qmdff(str(tmp_path / "a.qmdff")))
+    gff.set_periodic([16.0] * 3, 50.0, 10.0)
+    mass = [mass_au(s) for s in sym]
+    eng = RPMDEngine(gff, mass, 2, 1, dt_fs_to_au(0.5), beta=beta_from_kelvin(300.0), thermostat="andersen",
+                     andersen_step=7, transrot=True, seed=4)
+    eng.set_npt(100.0)
+    eng.init_positions(ff.xyz, 0.0)
+    eng.init_momenta()
+    eng.compute_forces()
+    eng.run(20)
+    box, _, _ = eng.npt_state()
+    q, _, _, _, _ = eng.get_state()
+    eng.close()
+    gff.close()
+    assert np.allclose(boxes[-1], box[0] * BOHR_ANGSTROM, rtol=1e-15, atol=0)
+    tr = frames(tmp_path / "trajectory.xyz")
+    assert np.allclose(tr[-1], q[0].reshape(-1, 3) * BOHR_ANGSTROM, rtol=1e-15, atol=1e-15)
+    vol = float(out[-1].split()[3])
+    assert abs(vol - np.prod(box[0]) * BOHR_ANGSTROM ** 3) < 1e-3

@@ -79,7 +79,7 @@ def test_npt_single_step(periodic_pair, chain, nbeads):
     eng, cfg, q, p, f = make_npt(periodic_pair, chain, nbeads, T, box=box0, pressure=500.0)
     eng.run(1)
     qg, pg, fg, eg, st = eng.get_state()
-    bg, pr = eng.npt_state()
+    bg, pr, _ = eng.npt_state()
     eng.close()
     qo, po, fo, eo, so, bo, pro = orc.run_npt(cfg, q, p, f, 1, box0, 500.0)
     assert not st.any() and not so.any()
@@ -98,7 +98,7 @@ def test_npt_100_steps(periodic_pair, chain, thermostat):
                                  oracle_thermostat="none" if thermostat == "nhc" else None)
     eng.run(100)
     qg, pg, fg, eg, st = eng.get_state()
-    bg, pr = eng.npt_state()
+    bg, pr, _ = eng.npt_state()
     eng.close()
     qo, po, fo, eo, so, bo, pro = orc.run_npt(cfg, q, p, f, 100, BOX_ANG / BOHR, 1.0)
     assert not st.any()
@@ -117,3 +117,17 @@ def test_npt_refused_without_periodic_qmdff(chain, require_gpu):
     with pytest.raises(Exception, match="periodic"):
         ff.egrad_virial(chain.xyz[None])
     ff.close()
+
+
+def test_npt_pressure_sum(periodic_pair, chain):
+    """The running sum Caracal prints as press_avg (src/verlet.f90:1171-1210):
+    the per-step pressures of 6 steps add up; a reset zeroes it."""
+    eng, cfg, q, p, f = make_npt(periodic_pair, chain, 2, 2)
+    steps = []
+    for _ in range(6):
+        eng.run(1)
+        steps.append(eng.npt_state()[1])
+    box, last, psum = eng.npt_state(reset_sum=True)
+    assert np.allclose(psum, np.sum(steps, axis=0), rtol=1e-14, atol=0) and np.array_equal(last, steps[-1])
+    assert not eng.npt_state()[2].any()
+    eng.close()

@@ -47,7 +47,11 @@ def test_fortran_nint_of_dump_interval():
     ("STEPS 1\nDELTAT 1e-7\nPES ANA_H3\n", "too small"),
     ("ENSEMBLE NVT\nSTEPS 1\nPES ANA_H3\nNVT {\n TEMP 300\n}\n", "THERMOSTAT"),
     ("ENSEMBLE NVT\nSTEPS 1\nPES ANA_H3\nNVT {\n TEMP 300\n THERMOSTAT ANDERSEN\n", "delimiter"),
-    ("ENSEMBLE NPT\nSTEPS 1\nPES ANA_H3\n", "NPT"),
+    ("ENSEMBLE NPT\nSTEPS 1\nPES ANA_H3\nNPT {\n TEMP 300\n THERMOSTAT ANDERSEN\n}\n", "periodic systems"),
+    ("ENSEMBLE NPT\nSTEPS 1\nPES QMDFF\nPERIODIC 20 20 20\nQMDFF {\n FFNAMES a.qmdff\n}\n"
+     "NPT {\n TEMP 300\n THERMOSTAT ANDERSEN\n BAROSTAT NOSE-HOOVER\n}\n", "BERENDSEN is"),
+    ("ENSEMBLE NPT\nSTEPS 1\nPES QMDFF\nPERIODIC 20 20 20\nQMDFF {\n FFNAMES a.qmdff\n}\n"
+     "NPT {\n TEMP 300\n PRES -1\n THERMOSTAT ANDERSEN\n}\n", "positive pressure"),
     ("STEPS 1\nPES ANA_O3\n", "not on this engine"),
     ("STEPS 1\nPES QMDFF\n", "QMDFFNAMES"),
 ])
@@ -121,3 +125,12 @@ def test_analytic_surfaces(name, pes):
     assert K.ANALYTIC[d.pes] == pes
     with pytest.raises(K.KeyError_, match="not on this engine's path"):
         K.parse("STEPS 5\nPES ANA_BRH2\n")
+
+
+def test_npt_block():
+    """ENSEMBLE NPT with its block (src/dynamic.f90:478-580): temperature,
+    pressure (atm), thermostat, Berendsen barostat (the default)."""
+    d = K.parse("ENSEMBLE NPT\nSTEPS 10\nPES QMDFF\nPERIODIC 20 20 20\nQMDFF {\n FFNAMES a.qmdff\n}\n"
+                "NPT {\n TEMP 300\n PRES 1.5\n THERMOSTAT ANDERSEN\n ANDERSEN_STEP 9\n}\n")
+    assert d.ensemble == "NPT" and d.kelvin == 300.0 and d.pressure == 1.5 and d.barostat == "berendsen"
+    assert d.thermostat == "andersen" and d.andersen_step == 9 and not d.unsupported
