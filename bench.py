@@ -236,6 +236,12 @@ def workload(name):
         return W.oh3_config(ntraj=4096, nbeads=32)
     if name == "geh4oh":
         return W.geh4oh_md_config(ntraj=2048, nbeads=32)
+    if name == "qmdff_npt":
+        # C20H42 in a periodic 40 A box under 1 atm, Berendsen barostat
+        wl = W.qmdff_config(ntraj=1024, nbeads=64)
+        wl.name = "qmdff_npt_c20h42_box40A_P64_T1024"
+        wl.extra.update(box_ang=[40.0] * 3, coul_cut_ang=50.0, vdw_cut_ang=10.0, npt_atm=1.0)
+        return wl
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -245,6 +251,8 @@ def make_pes(wl):
         from caracal_gb300.engine import QMDFFForceField
         if "gpu_ff" not in wl.extra:
             wl.extra["gpu_ff"] = QMDFFForceField(wl.extra["ff"])
+            if "box_ang" in wl.extra:
+                wl.extra["gpu_ff"].set_periodic(wl.extra["box_ang"], wl.extra["coul_cut_ang"], wl.extra["vdw_cut_ang"])
         return wl.extra["gpu_ff"]
     if wl.pes == "water":
         from caracal_gb300.engine import WaterBox
@@ -263,6 +271,8 @@ def make_engine(wl, precision, traj0=0, max_steps=0):
                      thermostat=wl.thermostat, andersen_step=wl.andersen_step,
                      pile_tau0_au=wl.pile_tau0_au, transrot=wl.transrot, precision=precision,
                      seed=wl.seed, traj0=traj0)
+    if "npt_atm" in wl.extra:
+        eng.set_npt(wl.extra["npt_atm"])
     rd = wl.extra.get("recross")
     if rd is not None:
         eng.set_recross(max_steps=max(1, max_steps), **rd)
@@ -285,6 +295,9 @@ class OracleRunner:
         if wl.pes == "qmdff":
             from caracal_gb300 import qmdff as Q
             orc.set_qmdff(wl.extra["ff"], Q.ElementTables.caracal())
+            if "box_ang" in wl.extra:
+                orc.set_qmdff_periodic(wl.extra["box_ang"], wl.extra["coul_cut_ang"], wl.extra["vdw_cut_ang"])
+        self.npt = wl.extra.get("npt_atm")
         if wl.pes == "water":
             from caracal_gb300 import water as Wt
             x = wl.extra
@@ -305,11 +318,16 @@ class OracleRunner:
             self.q = orc.init_positions(self.cfg, wl.ntraj, wl.q0, wl.sigma_bohr)
             self.p = orc.init_momenta(self.cfg, wl.ntraj)
             self.f, _ = orc.init_forces(self.cfg, self.q)
+            if self.npt is not None:
+                self.box = np.tile(np.asarray(wl.extra["box_ang"]) / 0.52917721092, (wl.ntraj, 1))
         self.istep = 0
 
     def advance(self, nsteps, cores):
         if self.xd is not None:
             self.orc.recross_children(self.cfg, self.xd, self.wl.ntraj, self.qpar, nsteps, nthreads=cores)
+        elif self.npt is not None:
+            self.q, self.p, self.f, _, _, self.box, _ = self.orc.run_npt(
+                self.cfg, self.q, self.p, self.f, nsteps, self.box, self.npt, istep0=self.istep, nthreads=cores)
         else:
             self.q, self.p, self.f, _, _ = self.orc.run(self.cfg, self.q, self.p, self.f, nsteps,
                                                          istep0=self.istep, nthreads=cores)
@@ -472,8 +490,15 @@ def run_ours(args):
     value = ws * bead_steps / (ms_mx * 1e-3)
     plain = ws * wl.ntraj * wl.nbeads * K64 / (ms_64 * 1e-3)
 
-    # force error of the mixed form against FP64 at the same positions
+    # force error of the mixed form against FP64 at the same positions (and,
+    # under NpT, in the same boxes)
     q, p, f, e, st = eng_64.get_state()
+    if "npt_atm" in wl.extra:
+        # after a Berendsen step the stored forces belong to the coordinates
+        # before the scaling (as Caracal's derivs do): recompute both forms
+        eng_64.set_state(q, p)
+        q, p, f, e, st = eng_64.get_state()
+        eng_mx.set_npt(wl.extra["npt_atm"], eng_64.npt_state()[0])
     eng_mx.set_state(q, p)          # recomputes forces in the mixed form
     _, _, f_mx, e_mx, _ = eng_mx.get_state()
     ferr = float(np.max(np.abs(f_mx - f)) / np.max(np.abs(f)))
@@ -926,6 +951,7 @@ def main():
                          "qmdff (C20H42 QMDFF, 1024 x 64, Andersen 300 K), qmdff_small (512 x 64), "
                          "water (flexible SPC, 64 molecules, periodic, 64 x 32), oh3 (OH + H2, 4096 x 32), "
                          "geh4oh (GeH4 + OH, 2048 x 32, Andersen 300 K), "
+                         "qmdff_npt (C20H42 in a 40 A box, 1 atm, Berendsen, 1024 x 64), "
                          "classes (H3 4096x8, CH4H 2048x32, CH4OH 512x64, QMDFF 128x128 in one batch), "
                          "classes_small (the same with 1/16 of the trajectories), "
                          "adjoint (force matching over 8192 C20H42 geometries and a 200-step trajectory adjoint)")
