@@ -35,6 +35,7 @@ CR_PES_EVB = 5
 CR_PES_WATER = 6
 CR_PES_OH3 = 7
 CR_PES_GEH4OH = 8
+CR_PES_BRH2 = 9
 
 CR_THERMO_NONE = 0
 CR_THERMO_ANDERSEN = 1
@@ -123,6 +124,8 @@ def _sig(lib):
         "cr_initialize_ch4oh": ([], C.c_int),
         "cr_egrad_geh4oh": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
         "cr_initialize_geh4oh": ([], C.c_int),
+        "cr_egrad_brh2": ([d, C.c_int, C.c_int, d, d, i], C.c_int),
+        "cr_initialize_brh2": ([], C.c_int),
         "cr_egrad_device": ([C.c_int, v, C.c_int, v, v, C.c_int, v], C.c_int),
         "cr_engine_create": ([C.POINTER(CrConfig), C.POINTER(C.c_void_p)], C.c_int),
         "cr_engine_destroy": ([eng], C.c_int),

@@ -43,7 +43,8 @@ int next_pow2(int x) {
 
 int pes_natoms(int pes) {
   switch (pes) {
-    case CR_PES_H3: return 3;
+    case CR_PES_H3:
+    case CR_PES_BRH2: return 3;
     case CR_PES_CH4H: return 6;
     case CR_PES_CH4OH:
     case CR_PES_GEH4OH: return 7;
@@ -838,6 +839,12 @@ int cr_egrad_geh4oh(const double* q, int natoms, int nbeads, double* V, double* 
 
 int cr_initialize_geh4oh(void) { return CR_OK; }
 
+int cr_egrad_brh2(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
+  return egrad_host(CR_PES_BRH2, 3, q, natoms, nbeads, V, dVdq, info);
+}
+
+int cr_initialize_brh2(void) { return CR_OK; }
+
 int cr_egrad_oh3(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info) {
   return egrad_host(CR_PES_OH3, 4, q, natoms, nbeads, V, dVdq, info);
 }
@@ -1240,6 +1247,7 @@ int cr_engine_init_positions(cr_engine* e, const double* q0, double sigma) {
   }
   switch (e->cfg.pes) {
     case CR_PES_H3:
+    case CR_PES_BRH2:
       cr::init_positions_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->d_q0, sigma, e->d_q);
       break;
@@ -1279,6 +1287,7 @@ static int init_momenta_draw(cr_engine* e, int zero, uint32_t draw) {
   }
   switch (e->cfg.pes) {
     case CR_PES_H3:
+    case CR_PES_BRH2:
       cr::init_momenta_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, zero, draw, e->d_p);
       break;
@@ -2009,6 +2018,7 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
   const int nb = e->T * e->P;
   switch (e->cfg.pes) {
     case CR_PES_H3:
+    case CR_PES_BRH2:
       cr::init_children_kernel<9><<<(nb + 127) / 128, 128, 0, e->stream>>>(
           e->T, e->P, e->cfg.seed, e->cfg.traj0, e->prm, e->d_qpar, e->d_q, e->d_p);
       break;
@@ -2033,6 +2043,7 @@ int cr_engine_init_children(cr_engine* e, const double* q_parent) {
   const int tb = 128, gb = (e->T + tb - 1) / tb;
   switch (e->cfg.pes) {
     case CR_PES_H3:
+    case CR_PES_BRH2:
       cr::child_flux_kernel<3><<<gb, tb, 0, e->stream>>>(e->T, e->P, e->prm, e->d_q, e->d_p, e->d_w, e->d_wpos);
       break;
     case CR_PES_CH4H:
@@ -2485,6 +2496,7 @@ const PesRuns* pes_runs(int pes) {
     case CR_PES_CH4OH: return &kRunsCH4OH;
     case CR_PES_OH3: return &kRunsOH3;
     case CR_PES_GEH4OH: return &kRunsGeH4OH;
+    case CR_PES_BRH2: return &kRunsBrH2;
     default: return nullptr;
   }
 }

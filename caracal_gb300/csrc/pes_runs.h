@@ -1,7 +1,7 @@
 // Launch entry points of the analytic surfaces' kernels.  Each surface's
 // persistent step kernel and one-thread-per-bead force kernel are compiled
 // in their own translation unit (rpmd_h3.cu, rpmd_ch4h.cu, rpmd_ch4oh.cu,
-// rpmd_oh3.cu, rpmd_geh4oh.cu), so the library builds them in parallel; the engine reaches
+// rpmd_oh3.cu, rpmd_geh4oh.cu, rpmd_brh2.cu), so the library builds them in parallel; the engine reaches
 // them through this table.
 #pragma once
 #include <cstddef>
@@ -23,9 +23,9 @@ struct PesRuns {
   cudaError_t (*egrad)(bool mixed, int nbeads, const double* q, double* V, double* g, cudaStream_t st);
 };
 
-// The table of CR_PES_H3 / CH4H / CH4OH / OH3 / GEH4OH; NULL for any other surface.
+// The table of CR_PES_H3 / CH4H / CH4OH / OH3 / GEH4OH / BRH2; NULL for any other surface.
 const PesRuns* pes_runs(int pes);
 
-extern const PesRuns kRunsH3, kRunsCH4H, kRunsCH4OH, kRunsOH3, kRunsGeH4OH;
+extern const PesRuns kRunsH3, kRunsCH4H, kRunsCH4OH, kRunsOH3, kRunsGeH4OH, kRunsBrH2;
 
 }  // namespace cr

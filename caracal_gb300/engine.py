@@ -19,8 +19,9 @@ from . import _lib as L
 from .units import beta_from_kelvin, dt_fs_to_au
 
 PES = {"h3": L.CR_PES_H3, "ana_h3": L.CR_PES_H3, "oh3": L.CR_PES_OH3, "ana_oh3": L.CR_PES_OH3, "ch4h": L.CR_PES_CH4H, "ana_ch4h": L.CR_PES_CH4H,
-       "ch4oh": L.CR_PES_CH4OH, "ana_ch4oh": L.CR_PES_CH4OH, "geh4oh": L.CR_PES_GEH4OH, "ana_geh4oh": L.CR_PES_GEH4OH}
-PES_NATOMS = {L.CR_PES_H3: 3, L.CR_PES_CH4H: 6, L.CR_PES_CH4OH: 7, L.CR_PES_OH3: 4, L.CR_PES_GEH4OH: 7}
+       "ch4oh": L.CR_PES_CH4OH, "ana_ch4oh": L.CR_PES_CH4OH, "geh4oh": L.CR_PES_GEH4OH, "ana_geh4oh": L.CR_PES_GEH4OH,
+       "brh2": L.CR_PES_BRH2, "ana_brh2": L.CR_PES_BRH2}
+PES_NATOMS = {L.CR_PES_H3: 3, L.CR_PES_CH4H: 6, L.CR_PES_CH4OH: 7, L.CR_PES_OH3: 4, L.CR_PES_GEH4OH: 7, L.CR_PES_BRH2: 3}
 THERMOSTAT = {"none": L.CR_THERMO_NONE, "nve": L.CR_THERMO_NONE, "andersen": L.CR_THERMO_ANDERSEN,
               "nose-hoover": L.CR_THERMO_NHC, "nhc": L.CR_THERMO_NHC, "pile": L.CR_THERMO_PILE}
 PRECISION = {"fp64": L.CR_PREC_FP64, "plain": L.CR_PREC_FP64, "mixed": L.CR_PREC_MIXED}
@@ -85,6 +86,22 @@ def egrad_geh4oh(q):
     g = np.zeros_like(q)
     info = C.c_int(0)
     L.check(L.lib().cr_egrad_geh4oh(L.dptr(q), 7, nb, L.dptr(V), L.dptr(g), C.byref(info)), "egrad_geh4oh")
+    return V, g
+
+
+def egrad_brh2(q):
+    """Br + H2 (DIM-3C, ANA_BRH2) energies and gradients of q (nbeads, 3, 3)
+    bohr, atoms H, Br, H."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    if q.ndim == 2:
+        q = q[None]
+    nb = q.shape[0]
+    if q.shape[1:] != (3, 3):
+        raise ValueError("egrad_brh2 expects q of shape (nbeads, 3, 3)")
+    V = np.zeros(nb)
+    g = np.zeros_like(q)
+    info = C.c_int(0)
+    L.check(L.lib().cr_egrad_brh2(L.dptr(q), 3, nb, L.dptr(V), L.dptr(g), C.byref(info)), "egrad_brh2")
     return V, g
 
 

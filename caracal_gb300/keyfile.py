@@ -11,7 +11,7 @@ closed by `}`.  Read here, with Caracal's defaults and checks:
     NOSE_DAMP n, BARO_DAMP n }  (src/dynamic.f90:478-580; periodic QMDFF only;
     BAROSTAT NOSE-HOOVER stops: its chain is not built here)
     (src/dynamic.f90:382-473; defaults TEMP 0, ANDERSEN_STEP 70, NOSE_DAMP 100)
-  PES ANA_H3 | ANA_CH4H | ANA_CH4OH | ANA_OH3 | ANA_GEH4OH | QMDFF | DE_EVB
+  PES ANA_H3 | ANA_BRH2 | ANA_CH4H | ANA_CH4OH | ANA_OH3 | ANA_GEH4OH | QMDFF | DE_EVB
     (src/read_pes.f90:203, 413-631)
   QMDFF { FFNAMES file [file2], ESHIFT e1 [e2], COULOMB ZAHN, COUL_CUTOFF A,
     VDW_CUTOFF A }  (src/read_pes.f90:1745-1863; defaults 50 and 10)
@@ -32,7 +32,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh", "ANA_OH3": "oh3", "ANA_GEH4OH": "geh4oh"}
+ANALYTIC = {"ANA_H3": "h3", "ANA_CH4H": "ch4h", "ANA_CH4OH": "ch4oh", "ANA_OH3": "oh3", "ANA_GEH4OH": "geh4oh", "ANA_BRH2": "brh2"}
 EVB_BASES = ("1g", "2g", "3g", "sp", "sd", "sd2", "sp2d")
 KNOWN = {"XYZSTART", "RPMD_BEADS", "ENSEMBLE", "STEPS", "DELTAT", "TDUMP", "TDUMP_CUT", "PES", "NVT", "NVE", "NPT",
          "QMDFF", "DE_EVB", "GPU_TRAJECTORIES", "SEED", "E_CON", "OUTPUT_SPARSE", "READ_VEL", "PERIODIC", "}"}

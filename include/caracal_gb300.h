@@ -44,6 +44,7 @@ extern "C" {
 #define CR_PES_WATER 6   /* flexible SPC water box: src/egrad_water.f90, src/water_init.f90 */
 #define CR_PES_OH3 7     /* ANA_OH3: OH + H2 (Schatz-Elgersma), src/egrad_oh3.f */
 #define CR_PES_GEH4OH 8  /* ANA_GEH4OH: GeH4 + OH, src/egrad_geh4oh.f + src/util_geh4oh.f */
+#define CR_PES_BRH2 9    /* ANA_BRH2: Br + H2 (DIM-3C), src/egrad_brh2.f */
 
 /* ---- thermostats (Caracal keyword THERMOSTAT) ---------------------------- */
 #define CR_THERMO_NONE 0      /* NVE */
@@ -57,7 +58,7 @@ extern "C" {
 
 typedef struct cr_config {
   int pes;            /* CR_PES_* */
-  int natoms;         /* must match the PES (H3: 3, CH4H: 6, CH4OH and GeH4OH: 7, OH3: 4, QMDFF: the force field's n) */
+  int natoms;         /* must match the PES (H3 and BrH2: 3, CH4H: 6, CH4OH and GeH4OH: 7, OH3: 4, QMDFF: the force field's n) */
   int nbeads;         /* 1..128 (RPMD_BEADS) */
   int ntraj;          /* independent trajectories in this engine */
   int thermostat;     /* CR_THERMO_* */
@@ -164,6 +165,13 @@ int cr_egrad_geh4oh(const double* q, int natoms, int nbeads, double* V, double* 
 /* Replaces `subroutine initialize_geh4oh()` (src/egrad_geh4oh.f:1823, called from
  * src/read_pes.f90:629); constants are compiled in, always CR_OK. */
 int cr_initialize_geh4oh(void);
+
+/* Replaces `subroutine egrad_brh2(q,Natoms,Nbeads,V,dVdq,info)` (src/egrad_brh2.f:33-78;
+ * called from src/gradient.f90:182-183): natoms = 3 in Caracal's order H, Br, H. */
+int cr_egrad_brh2(const double* q, int natoms, int nbeads, double* V, double* dVdq, int* info);
+/* Replaces `subroutine initialize_brh2()` (src/egrad_brh2.f:80-130, called from
+ * src/read_pes.f90:452); the set-up is compiled in, always CR_OK. */
+int cr_initialize_brh2(void);
 
 /* Any built PES (CR_PES_*) on device-resident arrays q(3,natoms,npts). */
 int cr_egrad_device(int pes, const double* d_q, int npts, double* d_V, double* d_dVdq, int precision,

@@ -19,7 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-PES_IDS = {"h3": 1, "ch4h": 2, "ch4oh": 3, "qmdff": 4, "evb": 5, "water": 6, "oh3": 7, "geh4oh": 8}
+PES_IDS = {"h3": 1, "ch4h": 2, "ch4oh": 3, "qmdff": 4, "evb": 5, "water": 6, "oh3": 7, "geh4oh": 8, "brh2": 9}
 EVB_BASES = {"const": 0, "1g": 1, "2g": 2, "3g": 3, "sp": 4, "sd": 5, "sd2": 6, "sp2d": 7}
 THERMOSTATS = {"none": 0, "andersen": 1, "nose-hoover": 2, "nhc": 2, "pile": 3}
 OPCOUNT_FIELDS = ("add", "mul", "div", "sqrt", "exp", "log", "pow", "sin", "cos",

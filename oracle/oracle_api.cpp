@@ -18,6 +18,7 @@
 #include "pes_qmdff.hpp"
 #include "pes_water.hpp"
 #include "pes_oh3.hpp"
+#include "pes_brh2.hpp"
 #include "philox.hpp"
 #include "recross.hpp"
 #include "rpmd.hpp"
@@ -59,6 +60,7 @@ struct BeadPES {
       case 6: *V = orc::water::egrad<double>(g_water, q, g); break;
       case 7: orc::oh3::egrad_bead<double>(q, V, g); break;
       case 8: orc::ch4oh::egrad_bead<double>(q, V, g, true); break;
+      case 9: orc::brh2::egrad_bead(q, V, g); break;
       default: *V = NAN; for (int x = 0; x < 3 * natoms; ++x) g[x] = NAN; break;
     }
   }

@@ -14,7 +14,7 @@ extern "C" {
 typedef struct orc_cfg {
   int pes;            /* 1 H3 (BKMP2), 2 CH4H, 3 CH4OH, 4 QMDFF (orc_qmdff_set), 5 dE-EVB of two QMDFFs,
                          6 flexible SPC water box (orc_water_set), 7 OH + H2 (ANA_OH3), 8 GeH4 + OH
-                         (ANA_GEH4OH) */
+                         (ANA_GEH4OH), 9 Br + H2 (ANA_BRH2) */
   int natoms;
   int nbeads;
   int thermostat;     /* 0 none, 1 Andersen, 2 Nose-Hoover chain, 3 PILE */

@@ -117,14 +117,14 @@ def test_periodic_and_coulomb_keywords():
 
 
 @pytest.mark.parametrize("name,pes", [("ANA_H3", "h3"), ("ANA_CH4H", "ch4h"), ("ANA_CH4OH", "ch4oh"),
-                                      ("ANA_OH3", "oh3"), ("ana_geh4oh", "geh4oh")])
+                                      ("ANA_OH3", "oh3"), ("ana_geh4oh", "geh4oh"), ("ANA_BRH2", "brh2")])
 def test_analytic_surfaces(name, pes):
     """The analytic PES keywords built on this engine (src/read_pes.f90:413-631);
     the others stop with an error."""
     d = K.parse(f"STEPS 5\nPES {name}\n")
     assert K.ANALYTIC[d.pes] == pes
     with pytest.raises(K.KeyError_, match="not on this engine's path"):
-        K.parse("STEPS 5\nPES ANA_BRH2\n")
+        K.parse("STEPS 5\nPES ANA_O3\n")
 
 
 def test_npt_block():
