@@ -59,7 +59,8 @@ struct Schedule {
 // mixed form the edges as (hi, lo) float pairs and the halves in FP32.
 struct PBox {
   double len[3], half[3];
-  float flen[3], flen_lo[3], fhalf[3];
+  float flen[3], flen_lo[3], fhalf[3], fhalf_lo[3];
+  float fhalf_dn[3], fhalf_up[3];  // half -+ 4 ulps: outside, the hi part decides the image
 };
 __host__ __device__ inline PBox make_box(const double* len) {
   PBox b;
@@ -69,6 +70,9 @@ __host__ __device__ inline PBox make_box(const double* len) {
     b.flen[k] = (float)len[k];
     b.flen_lo[k] = (float)(len[k] - (double)b.flen[k]);
     b.fhalf[k] = (float)b.half[k];
+    b.fhalf_lo[k] = (float)(b.half[k] - (double)b.fhalf[k]);
+    b.fhalf_dn[k] = (float)(b.half[k] * (1.0 - 4.8e-7));
+    b.fhalf_up[k] = (float)(b.half[k] * (1.0 + 4.8e-7));
   }
   return b;
 }
@@ -328,8 +332,23 @@ __device__ inline double image1(double v, double len, double half) {
 // FP32: the difference of two (hi, lo) coordinates as an exact float pair
 // first (atoms a box edge apart are not close enough for the hi parts to
 // subtract exactly), the edge subtracted as a pair, then rounded once.
-__device__ inline float image1(FF d, float len, float len_lo, float half) {
-  for (int it = 0; it < kImageIters && fabsf(d.hi) > half; ++it) {
+// |d| > half, so that the choice of image agrees with FP64's except within
+// ~1e-14 of half the edge: the hi part decides unless it lies within 4 ulps
+// of half, where |d| - half is formed as a float pair.
+static __device__ __noinline__ bool beyond_half_pair(FF d, float half, float half_lo) {
+  const FF a = d.hi < 0.0f ? FF{-d.hi, -d.lo} : d;
+  const FF t = ff_add(a, FF{-half, -half_lo});
+  return t.hi > 0.0f || (t.hi == 0.0f && t.lo > 0.0f);
+}
+__device__ inline bool beyond_half(FF d, const PBox& b, int k) {
+  const float ah = fabsf(d.hi);
+  if (ah > b.fhalf_up[k]) return true;
+  if (ah < b.fhalf_dn[k]) return false;
+  return beyond_half_pair(d, b.fhalf[k], b.fhalf_lo[k]);  // out of line: rarely taken
+}
+__device__ inline float image1(FF d, const PBox& b, int k) {
+  const float len = b.flen[k], len_lo = b.flen_lo[k];
+  for (int it = 0; it < kImageIters && beyond_half(d, b, k); ++it) {
     const float s = copysignf(1.0f, d.hi);
     d = ff_add(d, FF{-s * len, -s * len_lo});
   }
@@ -362,7 +381,8 @@ __device__ inline void disp<float>(const BeadPos& X, int a, int b, float* v) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float2 u = X.hl[3 * a + d], w = X.hl[3 * b + d];
-    if (X.pbc) v[d] = image1(ff_add(FF{u.x, u.y}, FF{-w.x, -w.y}), X.pbc->flen[d], X.pbc->flen_lo[d], X.pbc->fhalf[d]);
+    if (X.pbc)
+      v[d] = image1(ff_add(FF{u.x, u.y}, FF{-w.x, -w.y}), *X.pbc, d);
     else v[d] = (u.x - w.x) + (u.y - w.y);
   }
 }
@@ -418,7 +438,7 @@ __device__ inline float bond_mixed(const Dev& D, const BeadPos& x, int m, Contri
     const float2 a = x.hl[3 * i + d], b = x.hl[3 * j + d];
     dv[d] = ff_add(FF{a.x, a.y}, FF{-b.x, -b.y});
     if (x.pbc) {
-      for (int it = 0; it < kImageIters && fabsf(dv[d].hi) > x.pbc->fhalf[d]; ++it) {
+      for (int it = 0; it < kImageIters && beyond_half(dv[d], *x.pbc, d); ++it) {
         const float sg = copysignf(1.0f, dv[d].hi);
         dv[d] = ff_add(dv[d], FF{-sg * x.pbc->flen[d], -sg * x.pbc->flen_lo[d]});
       }
