@@ -538,8 +538,8 @@ def run_ours(args):
         L.lib().cr_host_free(ptr)
 
     # the same with the caller's own (pageable) numpy arrays, as Caracal's
-    # module arrays are: staged by the driver, then page-locked in place by
-    # cr_host_register (PinnedHost), which is how a Fortran caller would use it
+    # module arrays are: staged by the CUDA runtime, then page-locked in place
+    # by cr_host_register (PinnedHost), which is how a Fortran caller would use it
     from caracal_gb300.engine import PinnedHost
     aq, ap, af, ae = q.copy(), p.copy(), f.copy(), np.zeros(wl.ntraj)
 
@@ -970,7 +970,7 @@ def main():
         args.warmup = 3
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # N replicas need N ranks: start them with torch.distributed.run (one
-        # process per GPU, rendezvous on 127.0.0.1), as the driver would
+        # process per GPU, rendezvous on 127.0.0.1)
         cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
                "--master-addr", "127.0.0.1", "--master-port", os.environ.get("MASTER_PORT", "29531"),
                os.path.abspath(__file__)] + sys.argv[1:]
