@@ -206,3 +206,36 @@ def test_dynamic_npt_berendsen(require_gpu, tmp_path, capsys):
     assert np.allclose(tr[-1], q[0].reshape(-1, 3) * BOHR_ANGSTROM, rtol=1e-15, atol=1e-15)
     vol = float(out[-1].split()[3])
     assert abs(vol - np.prod(box[0]) * BOHR_ANGSTROM ** 3) < 1e-3
+
+
+@pytest.mark.parametrize("pes,sym,xyz_ang", [
+    ("ANA_BRH2", ["H", "Br", "H"], [[0.0, 0.0, -1.9], [0.0, 0.0, 1.4145], [0.0, 0.1, 0.0]]),
+    ("ANA_GEH4OH", None, None),
+])
+def test_dynamic_new_surfaces(require_gpu, tmp_path, pes, sym, xyz_ang):
+    """PES ANA_BRH2 / ANA_GEH4OH from a key file: the last frame equals the
+    engine's state after the same steps (element masses Br 78.918, Ge 72.61)."""
+    from caracal_gb300.keyfile import ANALYTIC
+    if sym is None:
+        from caracal_gb300.workloads import geh4oh_geometry
+        sym = ["H", "Ge", "H", "H", "H", "O", "H"]
+        xyz_ang = geh4oh_geometry() * BOHR_ANGSTROM
+    xyz_ang = np.asarray(xyz_ang, dtype=np.float64)
+    (tmp_path / "start.xyz").write_text(f"{len(sym)}\n\n" + "".join(
+        f"{s} {a} {b} {c}\n" for s, (a, b, c) in zip(sym, xyz_ang)))
+    (tmp_path / "d.key").write_text(
+        f"XYZSTART start.xyz\nRPMD_BEADS 4\nENSEMBLE NVT\nSTEPS 10\nDELTAT 0.1\nTDUMP 0.5\nPES {pes}\n"
+        "SEED 2\nNVT {\n TEMP 300\n THERMOSTAT ANDERSEN\n ANDERSEN_STEP 3\n}\n")
+    run(str(tmp_path / "d.key"), out_dir=str(tmp_path), quiet=True)
+    tr = frames(tmp_path / "trajectory.xyz")
+    mass = [mass_au(s) for s in sym]
+    eng = RPMDEngine(ANALYTIC[pes], mass, 4, 1, dt_fs_to_au(0.1), beta=beta_from_kelvin(300.0),
+                     thermostat="andersen", andersen_step=3, transrot=True, seed=2)
+    eng.init_positions(angstrom_to_bohr(xyz_ang), 0.0)
+    eng.init_momenta()
+    eng.compute_forces()
+    eng.run(10)
+    q, _, _, _, st = eng.get_state()
+    eng.close()
+    assert len(tr) == 2 and not st.any()
+    assert np.allclose(tr[-1], q[0].reshape(-1, 3) * BOHR_ANGSTROM, rtol=1e-15, atol=1e-15)
