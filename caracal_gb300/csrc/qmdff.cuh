@@ -937,7 +937,7 @@ __device__ inline float ex2_approx(float x) {
 // for a base-2 exponential).  The pair forces are ~1 % of the valence
 // forces, so hardware approximations stay far below the form's error budget.
 __device__ inline float pair_mixed_v(const Dev& D, const BeadPos& x, int i1, int i2, const float (&v)[kVPair],
-                                     Contrib<float>& c) {
+                                     Contrib<float>& c, float* vir = nullptr) {
   float vab[3];
   disp<float>(x, i1, i2, vab);
   const float r2 = dot3(vab, vab);
@@ -968,6 +968,7 @@ __device__ inline float pair_mixed_v(const Dev& D, const BeadPos& x, int i1, int
     c.g[0][d] = vab[d] * drij;
     c.g[1][d] = -vab[d] * drij;
   }
+  if (vir) *vir = r2 * drij;  // vab . g_i1 with g_i1 = vab drij (NpT)
   return e;
 }
 
@@ -1288,11 +1289,12 @@ __device__ inline void pair_batches_mixed(const Dev& D, const BeadPos& X, Grad<f
     }
     if (mc >= 0) {
       Contrib<float> c;
-      const float e = pair_mixed_v(D, X, ijc.x, ijc.y, v, c);
+      float w = 0.0f;
+      const float e = pair_mixed_v(D, X, ijc.x, ijc.y, v, c, MODE == kNpt ? &w : nullptr);
       const float t = es + e;
       ec += (fabsf(es) >= fabsf(e)) ? ((es - t) + e) : ((e - t) + es);
       es = t;
-      if constexpr (MODE == kNpt) wv += term_virial<float, 3>(D, X, mc, c);
+      if constexpr (MODE == kNpt) wv += w;
       scatter_pair<2>(c, G);
     }
     __syncwarp();
