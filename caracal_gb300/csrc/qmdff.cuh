@@ -591,11 +591,19 @@ __device__ inline F dihedral(const F* ra, const F* rb, const F* rc, F* na, F* nb
   return phi;
 }
 
+// vab.g_a + vcb.(g_c + g_d) + vdc.g_d with the term's own vectors: the
+// torsions' and inversions' vir_ten (src/ff_eg.f90:420-440, 583-603).
+template <class F>
+__device__ inline F tors_virial(const F* vab, const F* vcb, const F* vdc, const Contrib<F>& c) {
+  const F gcd[3] = {c.g[2][0] + c.g[3][0], c.g[2][1] + c.g[3][1], c.g[2][2] + c.g[3][2]};
+  return dot3(vab, c.g[0]) + dot3(vcb, gcd) + dot3(vdc, c.g[3]);
+}
+
 // Torsions (erf-blended cosine series, src/ff_eg.f90:303-440) and
 // inversions (tors type 2, src/ff_eg.f90:441-618).
 template <class F>
 __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>::type>& T, const BeadPos& x, int m,
-                                 Contrib<F>& c) {
+                                 Contrib<F>& c, F* vir = nullptr) {
   const F pi = (F)3.1415926535897932384626433832795029;
   const F pi2 = (F)6.28318530717958623199592693708837;
   const F spi = (F)1.77245385090551599275151910313925;
@@ -724,6 +732,7 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
       c.g[2][d] = dij * ddc[d] + t3 - t2;
       c.g[3][d] = dij * ddd[d] - t3;
     }
+    if (vir) *vir = tors_virial(vab, vcb, vdc, c);
     return et * damp;
   }
   // inversion: omega (src/omega.f90) and domegadr (src/domegadr.f90)
@@ -817,6 +826,7 @@ __device__ inline F torsion_term(const Dev& D, const Tables<typename ParamOf<F>:
     c.g[2][d] = dij * ddc[d] - t2;
     c.g[3][d] = dij * ddd[d] - t3;
   }
+  if (vir) *vir = tors_virial(vab, vcb, vdc, c);
   return et * damp;
 }
 
@@ -1240,7 +1250,16 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
     const int ncol = S.ncol[b];
     Contrib<F> c;
     if (m >= 0) {
-      const F v = term<MIXED>(D, KIND, X, m, c);
+      F v;
+      if constexpr (MODE == kNpt && KIND == 2) {  // the torsion's own vectors give its virial
+        F w;
+        if constexpr (MIXED) v = torsion_term<float>(D, D.f, X, m, c, &w);
+        else v = torsion_term<double>(D, D.d, X, m, c, &w);
+        wv += w;
+      } else {
+        v = term<MIXED>(D, KIND, X, m, c);
+        if constexpr (MODE == kNpt) wv += term_virial<F, KIND>(D, X, m, c);
+      }
       if constexpr (MIXED) {  // compensated FP32 lane sum
         const F t = es + v;
         ec += (fabs(es) >= fabs(v)) ? ((es - t) + v) : ((v - t) + es);
@@ -1248,7 +1267,6 @@ __device__ inline void kind_batches(const Dev& D, const BeadPos& X,
       } else {
         es += v;
       }
-      if constexpr (MODE == kNpt) wv += term_virial<F, KIND>(D, X, m, c);
     }
     for (int k = 0; k < ncol; ++k) {
       if (m >= 0 && col == k) {
